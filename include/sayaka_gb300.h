@@ -1,0 +1,197 @@
+/*
+ * sayaka_gb300 -- C ABI of the GB300 MAC pressure-Poisson solver.
+ *
+ * Drop-in boundary for the MAC solver path of the SayakaAmr library
+ * (haloless/SayakaAmr): the class sayaka::MacSolver (src/SayakaMacSolver.h)
+ * operating on an AmrTree (src/SayakaTree.h) and TreeData fields
+ * (src/SayakaTreeData.h).  Plain pointers and sizes only.
+ *
+ * Host field buffers use the reference's TreeData layout: block b, component
+ * c, cell (i,j,k) of the grown box at
+ *     b*cap*ncomp + c*cap + (i+g) + (j+g)*Gx + (k+g)*Gx*Gy
+ * with g = ngrow, Gx = nb+2g (+1 for x-face data), Gy likewise, cap = the
+ * grown box size (in 2D the third extent is 1 and carries no ghost layer).
+ * "compact" entry points take [block][k][j][i] valid cells (face data:
+ * [block][...][face index], the staggered valid box) for every tree block.
+ *
+ * Every entry point returns a sayaka_status; a non-OK status leaves a message
+ * for sayaka_mac_last_error().  Nothing here exits the process.
+ */
+#ifndef SAYAKA_GB300_H
+#define SAYAKA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sayaka_status {
+  SAYAKA_OK = 0,
+  SAYAKA_BREAKDOWN = 1,      /* BiCGSTAB breakdown: rho, r^.v or t.t == 0 (src/SayakaMacSolver.cpp:773-900) */
+  SAYAKA_NOT_CONVERGED = 2,  /* max_iter reached (the reference prints "failure", :915-917) */
+  SAYAKA_STALL_FALLBACK = 3, /* learned preconditioner stalled; finished with plain MG */
+  SAYAKA_BAD_INPUT = 4,
+  SAYAKA_CUDA_ERROR = 5
+} sayaka_status;
+
+/* ------------------------------------------------------------------------
+ * Tree tables: the AmrTree block arrays the solver reads
+ * (AmrTreeNode, src/SayakaTree.h:52-152).  Neighbour codes: >= 0 block id at
+ * the same level, -1 coarser neighbour, <= -20 physical boundary code.
+ * ---------------------------------------------------------------------- */
+typedef struct sayaka_tree_tables {
+  int32_t ndim;       /* 2 or 3 (SAYAKA_SPACEDIM, src/SayakaCommons.h:4-12) */
+  int32_t nb;         /* cells per block edge, even (blockValidIndex) */
+  int32_t num_blocks; /* AmrTree::numBlocks */
+  int32_t min_level;  /* AmrTree::minAmrLevel */
+  int32_t max_level;  /* AmrTree::maxAmrLevel */
+  const int32_t *level;       /* [num_blocks]   refineLevel */
+  const int32_t *neighbor;    /* [num_blocks*6] neighbor[MAX_FACE] */
+  const int32_t *child;       /* [num_blocks*8] child[MAX_CHILD] */
+  const int32_t *parent;      /* [num_blocks] */
+  const int32_t *which_child; /* [num_blocks] */
+  const int32_t *node_type;   /* [num_blocks]   TreeNodeType (src/SayakaTree.h:27-32) */
+  const double *block_len;    /* [num_blocks*3] blockLength */
+} sayaka_tree_tables;
+
+/* ------------------------------------------------------------------------
+ * Host tree mirror: AmrTree / regrid (src/SayakaTree.cpp, src/SayakaRegrid.cpp)
+ * ---------------------------------------------------------------------- */
+typedef struct sayaka_tree sayaka_tree;
+
+/* AmrTree::init with an explicit block capacity (src/SayakaTree.cpp:34-91) */
+int sayaka_tree_create(int32_t ndim, int32_t nb, int32_t min_level, int32_t max_level, int32_t capacity,
+                       sayaka_tree **out);
+void sayaka_tree_destroy(sayaka_tree *t);
+/* AmrTree::initUniformRootLevel (src/SayakaTree.cpp:93-201) */
+int sayaka_tree_init_uniform_root(sayaka_tree *t, const int32_t ndiv[3], const double lo[3], const double hi[3],
+                                  const int32_t bc_type[6], const int32_t periodic[6]);
+/* AmrTree::initRefineToMinLevel (src/SayakaTree.cpp:204-233) */
+int sayaka_tree_init_refine_to_min_level(sayaka_tree *t);
+/* AmrTree::refineFlag / coarsenFlag (src/SayakaTree.h:221-222), n <= capacity */
+int sayaka_tree_set_refine_flags(sayaka_tree *t, const int32_t *flags, int32_t n);
+int sayaka_tree_set_coarsen_flags(sayaka_tree *t, const int32_t *flags, int32_t n);
+/* AmrTree::regrid (src/SayakaRegrid.cpp:26-125) */
+int sayaka_tree_regrid(sayaka_tree *t);
+int32_t sayaka_tree_num_blocks(const sayaka_tree *t);
+/* tables of the current tree; pointers stay valid until the next regrid */
+int sayaka_tree_get_tables(sayaka_tree *t, sayaka_tree_tables *out);
+/* boundBox lo/hi, blockCenter [num_blocks*3] each; nodeType2 [num_blocks*6] */
+int sayaka_tree_get_geometry(const sayaka_tree *t, double *lo, double *hi, double *center);
+int sayaka_tree_get_node_type2(const sayaka_tree *t, int32_t *out);
+/* SurroundingBlocks blocks/types/bcrefs [num_blocks*27], position
+ * (ii,jj,kk) in {-1,0,1}^3 at (ii+1) + 3(jj+1) + 9(kk+1) (src/SayakaTree.h:336-526) */
+int sayaka_tree_get_surrounding(const sayaka_tree *t, int32_t *blocks, int32_t *types, int32_t *bcrefs);
+/* MGLevelTower block list and [begin,end) per sublevel 1..L
+ * (src/SayakaTower.cpp:28-187); sizes: blocks >= num_blocks, begin_end >= 2L */
+int sayaka_tree_get_tower(const sayaka_tree *t, int32_t L, int32_t *blocks, int32_t *n, int32_t *begin_end);
+/* BlockFaceRegister of every tower block, per face:
+ * type, neigh, fine_crse_offset[3], crse_fine_neigh[4]  (9 ints) */
+int sayaka_tree_get_face_regs(const sayaka_tree *t, int32_t L, int32_t *regs);
+
+/* ------------------------------------------------------------------------
+ * MAC solver (sayaka::MacSolver, src/SayakaMacSolver.h:25-425)
+ * ---------------------------------------------------------------------- */
+typedef struct sayaka_mac sayaka_mac;
+
+typedef struct sayaka_params {
+  int32_t max_iter;       /* setMaxIteration (src/SayakaMacSolver.h:349), default 2000 */
+  double tol_rel;         /* setTolerance (:350), default 1e-6 */
+  double tol_abs;         /* default 0 */
+  int32_t n_post_smooth;  /* setPostSmoothNum (:353), default 2 */
+  int32_t use_mg_precond; /* setCGUseMGPrecond (:358), default 0 */
+  double bot_tol_rel;     /* bottom BiCGSTAB, default 1e-6 (:78-80) */
+  double bot_tol_abs;     /* default 1e-6 */
+  int32_t bot_max_iter;   /* default 2000 */
+  int32_t precision;      /* 0: FP64 V-cycle; 1: FP32 V-cycle inside the FP64 outer solve */
+  int32_t bottom;         /* 0: BiCGSTAB bottom (reference); 1: dense direct bottom solve */
+  int32_t verbose;
+} sayaka_params;
+
+typedef struct sayaka_solve_info {
+  int32_t status;     /* sayaka_status of the solve */
+  int32_t iterations; /* outer BiCGSTAB iterations */
+  double rnorm0;      /* |r0|_inf */
+  double rnorm;       /* final |r|_inf (reference criterion, src/SayakaMacSolver.cpp:891) */
+  double seconds;     /* wall time of the solve */
+} sayaka_solve_info;
+
+void sayaka_params_default(sayaka_params *p);
+
+/* MacSolver(tree) + define + prepareSolver (src/SayakaMacSolver.h:56-87,
+ * src/SayakaMacOperator.cpp:13-60, src/SayakaMacSolver.cpp:12-26):
+ * alpha=0, beta=1, B=1, unit IB fractions */
+int sayaka_mac_create(const sayaka_tree_tables *tables, sayaka_mac **out);
+/* ~MacSolver (src/SayakaMacSolver.h:89-112) */
+void sayaka_mac_destroy(sayaka_mac *h);
+const char *sayaka_mac_last_error(const sayaka_mac *h);
+
+/* setScalars (src/SayakaMacSolver.h:346) */
+int sayaka_mac_set_scalars(sayaka_mac *h, double alpha, double beta);
+/* setCoefB(dir, TreeData, comp): leaf copy, c/f AVG sync, AVG restriction
+ * (src/SayakaMacCoef.cpp:36-76); face data of direction dir */
+int sayaka_mac_set_coef_b(sayaka_mac *h, int32_t dir, const double *face, int32_t ncomp, int32_t ngrow,
+                          int32_t comp);
+/* setIBFracByLS (src/SayakaMacIB.cpp:34-154): binary fractions, ls <= 0
+ * solid; ls cell data with ngrow >= 1 */
+int sayaka_mac_set_ib_frac_by_ls(sayaka_mac *h, const double *ls, int32_t ncomp, int32_t ngrow, int32_t comp);
+/* fractional IB fractions on leaf blocks (the protected m_ib_volfrac /
+ * m_ib_areafrac of src/SayakaMacSolver.h:383-384), then the same c/f AVG sync
+ * and AVG restriction; compact arrays, area[d] for d < ndim */
+int sayaka_mac_set_ib_frac_compact(sayaka_mac *h, const double *vol, const double *area0, const double *area1,
+                                   const double *area2);
+/* setBC(BCRegister) resolved to BlockBCRecord (src/SayakaMacOperator.cpp:1462-1469,
+ * src/SayakaBoundaryPatch.h:126-175): math BC per block face,
+ * [num_blocks*6], 0 Neumann, 1 Dirichlet, 2 SimpleFill (physical faces) */
+int sayaka_mac_set_bc(sayaka_mac *h, const int32_t *bc_type);
+/* fixBC (src/SayakaMacOperator.cpp:1470-1594): BC values in phi's ghost
+ * layer (ngrow >= 1) lifted into rhs on leaf blocks */
+int sayaka_mac_fix_bc(sayaka_mac *h, const double *phi, int32_t phi_ncomp, int32_t phi_ngrow, int32_t phi_comp,
+                      double *rhs, int32_t rhs_ncomp, int32_t rhs_ngrow, int32_t rhs_comp);
+
+/* setRhs / setInitSol / setZeroSol / getSol (src/SayakaMacSolver.h:117-132) */
+int sayaka_mac_set_rhs(sayaka_mac *h, const double *data, int32_t ncomp, int32_t ngrow, int32_t comp);
+int sayaka_mac_set_init_sol(sayaka_mac *h, const double *data, int32_t ncomp, int32_t ngrow, int32_t comp);
+int sayaka_mac_set_zero_sol(sayaka_mac *h);
+int sayaka_mac_get_sol(sayaka_mac *h, double *data, int32_t ncomp, int32_t ngrow, int32_t comp);
+/* compact variants; `on_device` != 0: the pointer is device memory */
+int sayaka_mac_set_rhs_compact(sayaka_mac *h, const double *cells, int32_t on_device);
+int sayaka_mac_get_sol_compact(sayaka_mac *h, double *cells, int32_t on_device);
+
+/* setTolerance / setMaxIteration / setPostSmoothNum / setCGUseMGPrecond */
+int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p);
+/* cg_solve (src/SayakaMacSolver.cpp:455-680): BiCGSTAB on the finest tower */
+int sayaka_mac_cg_solve(sayaka_mac *h, sayaka_solve_info *info);
+
+/* mg_flux_level (src/SayakaMacOperator.cpp:161-239): face flux -d(phi)/dh of
+ * direction dir on the leaf blocks; phi in TreeData layout (ngrow any) */
+int sayaka_mac_flux(sayaka_mac *h, int32_t dir, const double *phi, int32_t phi_ncomp, int32_t phi_ngrow,
+                    int32_t phi_comp, double *flux, int32_t flux_ncomp, int32_t flux_ngrow, int32_t flux_comp);
+
+/* ---- parity hooks on compact all-block arrays (tests and tools) ---- */
+/* mg_apply_level(L) (src/SayakaMacOperator.cpp:84-137) */
+int sayaka_mac_apply_compact(sayaka_mac *h, int32_t L, const double *x, double *y);
+/* mg_residual_level(L) (src/SayakaMacUtil.cpp:9-49) */
+int sayaka_mac_residual_compact(sayaka_mac *h, int32_t L, const double *x, const double *rhs, double *r);
+/* one mg_smooth_level(L) (src/SayakaMacOperator.cpp:140-159, 1028-1112) */
+int sayaka_mac_smooth_compact(sayaka_mac *h, int32_t L, const double *phi, const double *rhs, double *out);
+/* mg_restict_wgt for levels finest-1 .. 1 (src/SayakaMacIB.cpp:157-232) */
+int sayaka_mac_restrict_compact(sayaka_mac *h, const double *in, double *out);
+/* mg_prolong_wgt for levels 2 .. finest (src/SayakaMacIB.cpp:234-283) */
+int sayaka_mac_prolong_compact(sayaka_mac *h, const double *in, double *out);
+/* mg_precond_level(finest) (src/SayakaMacSolver.cpp:924-949) */
+int sayaka_mac_vcycle_compact(sayaka_mac *h, const double *p, double *phat);
+/* mg_flux_level on compact arrays; flux is compact face data of dir */
+int sayaka_mac_flux_compact(sayaka_mac *h, int32_t dir, const double *phi, double *flux);
+/* fixBC with phi as [block][grown box] (ngrow layers) and compact rhs */
+int sayaka_mac_fix_bc_compact(sayaka_mac *h, const double *phi_grown, int32_t ngrow, double *rhs);
+/* coefficient fields after sync/restriction: which 0 = B[dir], 1 = area
+ * fraction[dir], 2 = volume fraction */
+int sayaka_mac_get_coef_compact(sayaka_mac *h, int32_t which, int32_t dir, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SAYAKA_GB300_H */

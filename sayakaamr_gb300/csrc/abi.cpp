@@ -1,0 +1,608 @@
+// C ABI (include/sayaka_gb300.h) over the host tree mirror and the GPU MAC
+// solver.  Converts between the reference's TreeData buffer layout and the
+// compact device layout, validates inputs and turns failures into status codes.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/sayaka_gb300.h"
+#include "mac_solver.h"
+#include "tower.h"
+#include "tree.h"
+
+using namespace sayaka_gb300;
+
+struct sayaka_tree {
+  AmrTree t;
+  // SoA export of the current tree (refreshed on demand)
+  std::vector<int32_t> level, neighbor, child, parent, wc, nt;
+  std::vector<double> len;
+  std::vector<Tower> towers;
+  bool dirty = true;
+};
+
+struct sayaka_mac {
+  std::unique_ptr<MacGpu> gpu;
+  std::string err;
+  double *pinned = nullptr;  // staging for TreeData-layout transfers
+  size_t pinned_n = 0;
+  ~sayaka_mac() {
+    if (pinned) cudaFreeHost(pinned);
+  }
+};
+
+namespace {
+
+void refresh(sayaka_tree *h) {
+  if (!h->dirty) return;
+  const AmrTree &t = h->t;
+  const int n = t.num_blocks;
+  h->level.resize(n);
+  h->neighbor.resize((size_t)n * 6);
+  h->child.resize((size_t)n * 8);
+  h->parent.resize(n);
+  h->wc.resize(n);
+  h->nt.resize(n);
+  h->len.resize((size_t)n * 3);
+  for (int b = 0; b < n; b++) {
+    const TreeNode &x = t.nodes[b];
+    h->level[b] = x.level;
+    for (int f = 0; f < 6; f++) h->neighbor[b * 6 + f] = x.neighbor[f];
+    for (int c = 0; c < 8; c++) h->child[b * 8 + c] = x.child[c];
+    h->parent[b] = x.parent;
+    h->wc[b] = x.which_child;
+    h->nt[b] = x.node_type;
+    for (int d = 0; d < 3; d++) h->len[b * 3 + d] = x.length[d];
+  }
+  h->towers = build_towers(t);
+  h->dirty = false;
+}
+
+// TreeData layout of cell data (stag < 0) or face data of direction stag
+struct Layout {
+  int nd, nb, ncomp, g, comp, stag;
+  long G[3];
+  long cap;
+  Layout(int nd_, int nb_, int ncomp_, int g_, int comp_, int stag_)
+      : nd(nd_), nb(nb_), ncomp(ncomp_), g(g_), comp(comp_), stag(stag_) {
+    for (int d = 0; d < 3; d++) G[d] = d < nd ? nb + (d == stag) + 2 * g : 1;
+    cap = G[0] * G[1] * G[2];
+  }
+  long at(int b, int i, int j, int k) const {
+    const long gz = nd == 3 ? g : 0;
+    return (long)b * cap * ncomp + (long)comp * cap + (i + g) + G[0] * ((j + g) + G[1] * (k + gz));
+  }
+  bool ok() const { return ncomp >= 1 && comp >= 0 && comp < ncomp && g >= 0; }
+};
+
+// valid cells (or faces) of every block: TreeData layout <-> compact
+void pack(const Layout &L, int nblocks, const double *src, double *dst) {
+  const int e[3] = {L.nb + (L.stag == 0), L.nd >= 2 ? L.nb + (L.stag == 1) : 1, L.nd == 3 ? L.nb + (L.stag == 2) : 1};
+  size_t q = 0;
+  for (int b = 0; b < nblocks; b++)
+    for (int k = 0; k < e[2]; k++)
+      for (int j = 0; j < e[1]; j++) {
+        const double *row = src + L.at(b, 0, j, k);
+        std::memcpy(dst + q, row, e[0] * sizeof(double));
+        q += e[0];
+      }
+}
+void unpack(const Layout &L, int nblocks, const double *src, double *dst) {
+  const int e[3] = {L.nb + (L.stag == 0), L.nd >= 2 ? L.nb + (L.stag == 1) : 1, L.nd == 3 ? L.nb + (L.stag == 2) : 1};
+  size_t q = 0;
+  for (int b = 0; b < nblocks; b++)
+    for (int k = 0; k < e[2]; k++)
+      for (int j = 0; j < e[1]; j++) {
+        std::memcpy(dst + L.at(b, 0, j, k), src + q, e[0] * sizeof(double));
+        q += e[0];
+      }
+}
+
+int status_of(sayaka_mac *h) {
+  if (!h->gpu) return SAYAKA_BAD_INPUT;
+  if (!h->gpu->error().empty()) {
+    h->err = h->gpu->error();
+    return SAYAKA_CUDA_ERROR;
+  }
+  return SAYAKA_OK;
+}
+
+double *staging(sayaka_mac *h, size_t n) {
+  if (h->pinned_n < n) {
+    if (h->pinned) cudaFreeHost(h->pinned);
+    h->pinned = nullptr;
+    h->pinned_n = 0;
+    if (cudaMallocHost(&h->pinned, n * sizeof(double)) != cudaSuccess) return nullptr;
+    h->pinned_n = n;
+  }
+  return h->pinned;
+}
+
+template <typename F>
+int guarded(sayaka_mac *h, F &&f) {
+  if (!h) return SAYAKA_BAD_INPUT;
+  if (!h->gpu) {
+    h->err = "solver not created";
+    return SAYAKA_BAD_INPUT;
+  }
+  try {
+    const int r = f();
+    if (r != SAYAKA_OK) return r;
+  } catch (const std::exception &e) {
+    h->err = e.what();
+    return SAYAKA_BAD_INPUT;
+  }
+  return status_of(h);
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// tree mirror
+int sayaka_tree_create(int32_t ndim, int32_t nb, int32_t min_level, int32_t max_level, int32_t capacity,
+                       sayaka_tree **out) {
+  if (!out || ndim < 2 || ndim > 3 || nb < 2 || (nb & 1) || min_level < 1 || max_level < min_level ||
+      max_level > 16 || capacity < 1)
+    return SAYAKA_BAD_INPUT;
+  auto *h = new sayaka_tree;
+  h->t.init(ndim, nb, min_level, max_level, capacity);
+  *out = h;
+  return SAYAKA_OK;
+}
+void sayaka_tree_destroy(sayaka_tree *t) { delete t; }
+
+int sayaka_tree_init_uniform_root(sayaka_tree *t, const int32_t ndiv[3], const double lo[3], const double hi[3],
+                                  const int32_t bc_type[6], const int32_t periodic[6]) {
+  if (!t || !ndiv || !lo || !hi || !bc_type || !periodic) return SAYAKA_BAD_INPUT;
+  long n = 1;
+  for (int d = 0; d < 3; d++) {
+    if (ndiv[d] < 1 || (d >= t->t.ndim && ndiv[d] != 1)) return SAYAKA_BAD_INPUT;
+    n *= ndiv[d];
+  }
+  if (n > t->t.capacity) return SAYAKA_BAD_INPUT;
+  for (int f = 0; f < 2 * t->t.ndim; f++)
+    if (!periodic[f] && bc_type[f] > -20) return SAYAKA_BAD_INPUT;
+  bool per[6];
+  for (int f = 0; f < 6; f++) per[f] = periodic[f] != 0;
+  t->t.init_uniform_root(ndiv, lo, hi, bc_type, per);
+  t->dirty = true;
+  return SAYAKA_OK;
+}
+int sayaka_tree_init_refine_to_min_level(sayaka_tree *t) {
+  if (!t) return SAYAKA_BAD_INPUT;
+  const int rc = t->t.init_refine_to_min_level();
+  t->dirty = true;
+  return rc ? SAYAKA_BAD_INPUT : SAYAKA_OK;
+}
+int sayaka_tree_set_refine_flags(sayaka_tree *t, const int32_t *flags, int32_t n) {
+  if (!t || !flags || n < 0 || n > t->t.capacity) return SAYAKA_BAD_INPUT;
+  for (int i = 0; i < n; i++) t->t.refine_flag[i] = flags[i];
+  return SAYAKA_OK;
+}
+int sayaka_tree_set_coarsen_flags(sayaka_tree *t, const int32_t *flags, int32_t n) {
+  if (!t || !flags || n < 0 || n > t->t.capacity) return SAYAKA_BAD_INPUT;
+  for (int i = 0; i < n; i++) t->t.coarsen_flag[i] = flags[i];
+  return SAYAKA_OK;
+}
+int sayaka_tree_regrid(sayaka_tree *t) {
+  if (!t) return SAYAKA_BAD_INPUT;
+  const int rc = t->t.regrid();
+  t->dirty = true;
+  return rc ? SAYAKA_BAD_INPUT : SAYAKA_OK;
+}
+int32_t sayaka_tree_num_blocks(const sayaka_tree *t) { return t ? t->t.num_blocks : -1; }
+
+int sayaka_tree_get_tables(sayaka_tree *t, sayaka_tree_tables *o) {
+  if (!t || !o) return SAYAKA_BAD_INPUT;
+  refresh(t);
+  o->ndim = t->t.ndim;
+  o->nb = t->t.nb;
+  o->num_blocks = t->t.num_blocks;
+  o->min_level = t->t.min_level;
+  o->max_level = t->t.max_level;
+  o->level = t->level.data();
+  o->neighbor = t->neighbor.data();
+  o->child = t->child.data();
+  o->parent = t->parent.data();
+  o->which_child = t->wc.data();
+  o->node_type = t->nt.data();
+  o->block_len = t->len.data();
+  return SAYAKA_OK;
+}
+int sayaka_tree_get_geometry(const sayaka_tree *t, double *lo, double *hi, double *center) {
+  if (!t) return SAYAKA_BAD_INPUT;
+  for (int b = 0; b < t->t.num_blocks; b++)
+    for (int d = 0; d < 3; d++) {
+      if (lo) lo[b * 3 + d] = t->t.nodes[b].lo[d];
+      if (hi) hi[b * 3 + d] = t->t.nodes[b].hi[d];
+      if (center) center[b * 3 + d] = t->t.nodes[b].center[d];
+    }
+  return SAYAKA_OK;
+}
+int sayaka_tree_get_node_type2(const sayaka_tree *t, int32_t *out) {
+  if (!t || !out) return SAYAKA_BAD_INPUT;
+  for (int b = 0; b < t->t.num_blocks; b++)
+    for (int f = 0; f < 6; f++) out[b * 6 + f] = t->t.nodes[b].node_type2[f];
+  return SAYAKA_OK;
+}
+int sayaka_tree_get_surrounding(const sayaka_tree *t, int32_t *blocks, int32_t *types, int32_t *bcrefs) {
+  if (!t) return SAYAKA_BAD_INPUT;
+  for (int b = 0; b < t->t.num_blocks; b++)
+    for (int s = 0; s < 27; s++) {
+      if (blocks) blocks[b * 27 + s] = t->t.surr[b].blocks[s];
+      if (types) types[b * 27 + s] = t->t.surr[b].types[s];
+      if (bcrefs) bcrefs[b * 27 + s] = t->t.surr[b].bcrefs[s];
+    }
+  return SAYAKA_OK;
+}
+int sayaka_tree_get_tower(const sayaka_tree *tc, int32_t L, int32_t *blocks, int32_t *n, int32_t *begin_end) {
+  sayaka_tree *t = const_cast<sayaka_tree *>(tc);
+  if (!t || L < 1 || L > t->t.max_level || !n) return SAYAKA_BAD_INPUT;
+  refresh(t);
+  const Tower &tw = t->towers[L];
+  *n = (int)tw.blocks.size();
+  if (blocks) std::memcpy(blocks, tw.blocks.data(), tw.blocks.size() * sizeof(int32_t));
+  if (begin_end)
+    for (int l = 1; l <= L; l++) {
+      begin_end[2 * (l - 1)] = tw.empty() ? 0 : tw.begin[l];
+      begin_end[2 * (l - 1) + 1] = tw.empty() ? 0 : tw.end[l];
+    }
+  return SAYAKA_OK;
+}
+int sayaka_tree_get_face_regs(const sayaka_tree *tc, int32_t L, int32_t *regs) {
+  sayaka_tree *t = const_cast<sayaka_tree *>(tc);
+  if (!t || L < 1 || L > t->t.max_level || !regs) return SAYAKA_BAD_INPUT;
+  refresh(t);
+  const Tower &tw = t->towers[L];
+  const int nf = t->t.num_face();
+  size_t q = 0;
+  for (size_t p = 0; p < tw.blocks.size(); p++)
+    for (int f = 0; f < nf; f++) {
+      const FaceReg &r = tw.regs[p * 6 + f];
+      regs[q++] = r.type;
+      regs[q++] = r.neigh;
+      for (int d = 0; d < 3; d++) regs[q++] = r.type == kFaceFineCrse ? r.fc_off[d] : 0;
+      for (int c = 0; c < 4; c++) regs[q++] = r.type == kFaceCrseFine ? r.cf_neigh[c] : -1;
+    }
+  return SAYAKA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// solver
+void sayaka_params_default(sayaka_params *p) {
+  if (!p) return;
+  SolverParams d;
+  p->max_iter = d.max_iter;
+  p->tol_rel = d.tol_rel;
+  p->tol_abs = d.tol_abs;
+  p->n_post_smooth = d.n_post;
+  p->use_mg_precond = d.use_mg_precond;
+  p->bot_tol_rel = d.bot_tol_rel;
+  p->bot_tol_abs = d.bot_tol_abs;
+  p->bot_max_iter = d.bot_max_iter;
+  p->precision = d.precision;
+  p->bottom = d.bottom;
+  p->verbose = d.verbose;
+}
+
+int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
+  if (!tb || !out) return SAYAKA_BAD_INPUT;
+  *out = nullptr;
+  const int n = tb->num_blocks;
+  if (n <= 0 || tb->ndim < 2 || tb->ndim > 3 || tb->nb < 2 || (tb->nb & 1) || tb->min_level < 1 ||
+      tb->max_level < tb->min_level || !tb->level || !tb->neighbor || !tb->child || !tb->parent ||
+      !tb->which_child || !tb->node_type || !tb->block_len)
+    return SAYAKA_BAD_INPUT;
+  TreeTables tt;
+  tt.ndim = tb->ndim;
+  tt.nb = tb->nb;
+  tt.num_blocks = n;
+  tt.min_level = tb->min_level;
+  tt.max_level = tb->max_level;
+  tt.level.assign(tb->level, tb->level + n);
+  tt.neighbor.assign(tb->neighbor, tb->neighbor + (size_t)n * 6);
+  tt.child.assign(tb->child, tb->child + (size_t)n * 8);
+  tt.parent.assign(tb->parent, tb->parent + n);
+  tt.which_child.assign(tb->which_child, tb->which_child + n);
+  tt.node_type.assign(tb->node_type, tb->node_type + n);
+  tt.block_len.assign(tb->block_len, tb->block_len + (size_t)n * 3);
+  // table sanity: ids in range, levels in range
+  for (int b = 0; b < n; b++) {
+    if (tt.level[b] < 1 || tt.level[b] > tt.max_level) return SAYAKA_BAD_INPUT;
+    for (int f = 0; f < 6; f++)
+      if (tt.neighbor[b * 6 + f] >= n) return SAYAKA_BAD_INPUT;
+    for (int c = 0; c < 8; c++)
+      if (tt.child[b * 8 + c] >= n) return SAYAKA_BAD_INPUT;
+    if (tt.parent[b] >= n) return SAYAKA_BAD_INPUT;
+  }
+  auto *h = new sayaka_mac;
+  try {
+    h->gpu.reset(new MacGpu(tt));
+  } catch (const std::exception &e) {
+    h->err = e.what();
+  }
+  if (!h->gpu || !h->gpu->error().empty()) {
+    const int st = SAYAKA_CUDA_ERROR;
+    delete h;
+    return st;
+  }
+  *out = h;
+  return SAYAKA_OK;
+}
+
+void sayaka_mac_destroy(sayaka_mac *h) { delete h; }
+
+const char *sayaka_mac_last_error(const sayaka_mac *h) {
+  if (!h) return "null handle";
+  if (!h->err.empty()) return h->err.c_str();
+  if (h->gpu && !h->gpu->error().empty()) return h->gpu->error().c_str();
+  return "";
+}
+
+int sayaka_mac_set_scalars(sayaka_mac *h, double alpha, double beta) {
+  return guarded(h, [&] {
+    h->gpu->set_scalars(alpha, beta);
+    return SAYAKA_OK;
+  });
+}
+
+int sayaka_mac_set_coef_b(sayaka_mac *h, int32_t dir, const double *face, int32_t ncomp, int32_t ngrow,
+                          int32_t comp) {
+  return guarded(h, [&] {
+    MacGpu &g = *h->gpu;
+    if (dir < 0 || dir >= g.ndim() || !face) return (int)SAYAKA_BAD_INPUT;
+    Layout L(g.ndim(), g.nb(), ncomp, ngrow, comp, dir);
+    if (!L.ok()) return (int)SAYAKA_BAD_INPUT;
+    std::vector<double> c((size_t)g.num_blocks() * g.nfb());
+    pack(L, g.num_blocks(), face, c.data());
+    g.set_coef_b_leaf(dir, c.data());
+    return (int)SAYAKA_OK;
+  });
+}
+
+int sayaka_mac_set_ib_frac_by_ls(sayaka_mac *h, const double *ls, int32_t ncomp, int32_t ngrow, int32_t comp) {
+  return guarded(h, [&] {
+    MacGpu &g = *h->gpu;
+    if (!ls || ngrow < 1) return (int)SAYAKA_BAD_INPUT;
+    Layout L(g.ndim(), g.nb(), ncomp, ngrow, comp, -1);
+    if (!L.ok()) return (int)SAYAKA_BAD_INPUT;
+    // extract the grown box of component `comp` for every block
+    std::vector<double> grown((size_t)g.num_blocks() * L.cap);
+    for (int b = 0; b < g.num_blocks(); b++)
+      std::memcpy(&grown[(size_t)b * L.cap], ls + (size_t)b * L.cap * ncomp + (size_t)comp * L.cap,
+                  L.cap * sizeof(double));
+    g.set_ib_frac_by_ls(grown.data(), ngrow);
+    return (int)SAYAKA_OK;
+  });
+}
+
+int sayaka_mac_set_ib_frac_compact(sayaka_mac *h, const double *vol, const double *a0, const double *a1,
+                                   const double *a2) {
+  return guarded(h, [&] {
+    MacGpu &g = *h->gpu;
+    if (!vol || !a0 || (g.ndim() >= 2 && !a1) || (g.ndim() == 3 && !a2)) return (int)SAYAKA_BAD_INPUT;
+    const double *a[3] = {a0, a1, a2};
+    g.set_ib_frac_leaf(vol, a);
+    return (int)SAYAKA_OK;
+  });
+}
+
+int sayaka_mac_set_bc(sayaka_mac *h, const int32_t *bc) {
+  return guarded(h, [&] {
+    if (!bc) return (int)SAYAKA_BAD_INPUT;
+    for (int i = 0; i < h->gpu->num_blocks() * 6; i++)
+      if (bc[i] < -1 || bc[i] > 2) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->set_bc_types(bc);
+    return (int)SAYAKA_OK;
+  });
+}
+
+int sayaka_mac_fix_bc(sayaka_mac *h, const double *phi, int32_t pn, int32_t pg, int32_t pc, double *rhs, int32_t rn,
+                      int32_t rg, int32_t rc) {
+  return guarded(h, [&] {
+    MacGpu &g = *h->gpu;
+    if (!phi || !rhs || pg < 1) return (int)SAYAKA_BAD_INPUT;
+    Layout P(g.ndim(), g.nb(), pn, pg, pc, -1), R(g.ndim(), g.nb(), rn, rg, rc, -1);
+    if (!P.ok() || !R.ok()) return (int)SAYAKA_BAD_INPUT;
+    std::vector<double> grown((size_t)g.num_blocks() * P.cap);
+    for (int b = 0; b < g.num_blocks(); b++)
+      std::memcpy(&grown[(size_t)b * P.cap], phi + (size_t)b * P.cap * pn + (size_t)pc * P.cap,
+                  P.cap * sizeof(double));
+    std::vector<double> r((size_t)g.num_blocks() * g.ncell());
+    pack(R, g.num_blocks(), rhs, r.data());
+    g.fix_bc(grown.data(), pg, r.data());
+    unpack(R, g.num_blocks(), r.data(), rhs);
+    return (int)SAYAKA_OK;
+  });
+}
+
+static int set_field(sayaka_mac *h, const double *data, int32_t ncomp, int32_t ngrow, int32_t comp, bool rhs) {
+  return guarded(h, [&] {
+    MacGpu &g = *h->gpu;
+    if (!data) return (int)SAYAKA_BAD_INPUT;
+    Layout L(g.ndim(), g.nb(), ncomp, ngrow, comp, -1);
+    if (!L.ok()) return (int)SAYAKA_BAD_INPUT;
+    double *st = staging(h, (size_t)g.num_blocks() * g.ncell());
+    if (!st) return (int)SAYAKA_CUDA_ERROR;
+    pack(L, g.num_blocks(), data, st);
+    if (rhs)
+      g.set_rhs(st);
+    else
+      g.set_sol(st);
+    cudaStreamSynchronize(g.stream());
+    return (int)SAYAKA_OK;
+  });
+}
+
+int sayaka_mac_set_rhs(sayaka_mac *h, const double *d, int32_t nc, int32_t ng, int32_t c) {
+  return set_field(h, d, nc, ng, c, true);
+}
+int sayaka_mac_set_init_sol(sayaka_mac *h, const double *d, int32_t nc, int32_t ng, int32_t c) {
+  return set_field(h, d, nc, ng, c, false);
+}
+int sayaka_mac_set_zero_sol(sayaka_mac *h) {
+  return guarded(h, [&] {
+    h->gpu->zero_sol();
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_get_sol(sayaka_mac *h, double *data, int32_t ncomp, int32_t ngrow, int32_t comp) {
+  return guarded(h, [&] {
+    MacGpu &g = *h->gpu;
+    if (!data) return (int)SAYAKA_BAD_INPUT;
+    Layout L(g.ndim(), g.nb(), ncomp, ngrow, comp, -1);
+    if (!L.ok()) return (int)SAYAKA_BAD_INPUT;
+    double *st = staging(h, (size_t)g.num_blocks() * g.ncell());
+    if (!st) return (int)SAYAKA_CUDA_ERROR;
+    g.get_sol(st);
+    unpack(L, g.num_blocks(), st, data);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_set_rhs_compact(sayaka_mac *h, const double *cells, int32_t on_device) {
+  return guarded(h, [&] {
+    if (!cells) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->set_rhs(cells, on_device != 0);
+    cudaStreamSynchronize(h->gpu->stream());
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_get_sol_compact(sayaka_mac *h, double *cells, int32_t on_device) {
+  return guarded(h, [&] {
+    if (!cells) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->get_sol(cells, on_device != 0);
+    return (int)SAYAKA_OK;
+  });
+}
+
+int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
+  return guarded(h, [&] {
+    if (!p || p->max_iter < 0 || p->n_post_smooth < 0 || p->bot_max_iter < 0 || p->precision < 0 ||
+        p->precision > 1 || p->bottom < 0 || p->bottom > 1)
+      return (int)SAYAKA_BAD_INPUT;
+    SolverParams s;
+    s.max_iter = p->max_iter;
+    s.tol_rel = p->tol_rel;
+    s.tol_abs = p->tol_abs;
+    s.n_post = p->n_post_smooth;
+    s.use_mg_precond = p->use_mg_precond;
+    s.bot_tol_rel = p->bot_tol_rel;
+    s.bot_tol_abs = p->bot_tol_abs;
+    s.bot_max_iter = p->bot_max_iter;
+    s.precision = p->precision;
+    s.bottom = p->bottom;
+    s.verbose = p->verbose;
+    h->gpu->set_params(s);
+    return (int)SAYAKA_OK;
+  });
+}
+
+int sayaka_mac_cg_solve(sayaka_mac *h, sayaka_solve_info *info) {
+  return guarded(h, [&] {
+    SolveInfo si;
+    const int st = h->gpu->cg_solve(&si);
+    if (info) {
+      info->status = si.status;
+      info->iterations = si.iterations;
+      info->rnorm0 = si.rnorm0;
+      info->rnorm = si.rnorm;
+      info->seconds = si.seconds;
+    }
+    if (st < 0) return (int)SAYAKA_CUDA_ERROR;
+    return si.status == 0 ? (int)SAYAKA_OK : (si.status == 1 ? (int)SAYAKA_BREAKDOWN : (int)SAYAKA_NOT_CONVERGED);
+  });
+}
+
+int sayaka_mac_flux(sayaka_mac *h, int32_t dir, const double *phi, int32_t pn, int32_t pg, int32_t pc, double *flux,
+                    int32_t fn, int32_t fg, int32_t fc) {
+  return guarded(h, [&] {
+    MacGpu &g = *h->gpu;
+    if (dir < 0 || dir >= g.ndim() || !phi || !flux) return (int)SAYAKA_BAD_INPUT;
+    Layout P(g.ndim(), g.nb(), pn, pg, pc, -1), F(g.ndim(), g.nb(), fn, fg, fc, dir);
+    if (!P.ok() || !F.ok()) return (int)SAYAKA_BAD_INPUT;
+    std::vector<double> p((size_t)g.num_blocks() * g.ncell()), f((size_t)g.num_blocks() * g.nfb());
+    pack(P, g.num_blocks(), phi, p.data());
+    g.flux(dir, p.data(), f.data());
+    // leaf blocks only (the tower the flux is defined on)
+    std::vector<double> full((size_t)g.num_blocks() * g.nfb());
+    pack(F, g.num_blocks(), flux, full.data());
+    for (int b : g.tower_blocks(g.finest()))
+      std::memcpy(&full[(size_t)b * g.nfb()], &f[(size_t)b * g.nfb()], g.nfb() * sizeof(double));
+    unpack(F, g.num_blocks(), full.data(), flux);
+    return (int)SAYAKA_OK;
+  });
+}
+
+// ---- parity hooks ----
+int sayaka_mac_apply_compact(sayaka_mac *h, int32_t L, const double *x, double *y) {
+  return guarded(h, [&] {
+    if (L < 1 || !x || !y) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->apply(L, x, y);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_residual_compact(sayaka_mac *h, int32_t L, const double *x, const double *rhs, double *r) {
+  return guarded(h, [&] {
+    if (L < 1 || !x || !rhs || !r) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->residual(L, x, rhs, r);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_smooth_compact(sayaka_mac *h, int32_t L, const double *phi, const double *rhs, double *out) {
+  return guarded(h, [&] {
+    if (L < 1 || !phi || !rhs || !out) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->smooth(L, phi, rhs, out);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_restrict_compact(sayaka_mac *h, const double *in, double *out) {
+  return guarded(h, [&] {
+    if (!in || !out) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->restrict_sweep(in, out);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_prolong_compact(sayaka_mac *h, const double *in, double *out) {
+  return guarded(h, [&] {
+    if (!in || !out) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->prolong_sweep(in, out);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_vcycle_compact(sayaka_mac *h, const double *p, double *phat) {
+  return guarded(h, [&] {
+    if (!p || !phat) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->vcycle(p, phat);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_flux_compact(sayaka_mac *h, int32_t dir, const double *phi, double *flux) {
+  return guarded(h, [&] {
+    if (dir < 0 || dir >= h->gpu->ndim() || !phi || !flux) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->flux(dir, phi, flux);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_fix_bc_compact(sayaka_mac *h, const double *phi_grown, int32_t ngrow, double *rhs) {
+  return guarded(h, [&] {
+    if (!phi_grown || !rhs || ngrow < 1) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->fix_bc(phi_grown, ngrow, rhs);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_get_coef_compact(sayaka_mac *h, int32_t which, int32_t dir, double *out) {
+  return guarded(h, [&] {
+    if (!out || which < 0 || which > 2 || (which < 2 && (dir < 0 || dir >= h->gpu->ndim())))
+      return (int)SAYAKA_BAD_INPUT;
+    h->gpu->get_coef(which, dir, out);
+    return (int)SAYAKA_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,85 @@
+// Device-side data of the MAC solver and the kernel launch interface.
+//
+// HBM layout (one pool per field, all blocks of all levels, indexed by the
+// tree's block id):
+//   cell field   : [block][k][j][i]              nb^ndim values per block
+//   face field d : [block][..][face index in d]  (nb+1)*nb^(ndim-1) per block,
+//                  the reference's face-centred valid-box order
+// No ghost cells are stored: every kernel gathers the values a ghost cell
+// would hold straight from the owning block (see mac_kernels.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sayaka_gb300 {
+
+enum BCMath { kBCNeumann = 0, kBCDirichlet = 1, kBCSimpleFill = 2 };
+
+// tables shared by every kernel (device pointers)
+struct Topo {
+  int ndim, nb, ncell;  // ncell = nb^ndim
+  int nfb;              // faces per block per direction
+  int nblocks;
+  const int *neighbor;   // [nblocks*6]
+  const int *child;      // [nblocks*8]
+  const int *parent;     // [nblocks]
+  const int *which_child;// [nblocks]
+  const int *fc_neigh;   // [nblocks*6] coarse leaf behind a -1 neighbour
+  const int *bc_type;    // [nblocks*6] BCMath of physical faces, -1 otherwise
+};
+
+template <typename T>
+struct Coef {
+  const T *geom;      // [nblocks*8]: dx[3], ds[3], dv, unused
+  const T *tff[3];    // same-level face coefficient ((beta*ds)/dx)*B*a
+  const T *bcoef[3];  // face B
+  const T *afrac[3];  // IB area fraction
+  const T *vf;        // IB volume fraction
+  T alpha, beta;
+};
+
+// a block list with per-block packed face types (2 bits per face)
+struct BlockList {
+  const int *blocks;
+  const uint16_t *ftypes;  // may be null for lists that need no face types
+  int n;
+};
+
+// solver scalars kept on the device (FP64)
+struct Scalars {
+  double rho, rho1, alpha, omega, beta;
+  double rnorm0, rnorm;
+  double dots[4];
+  int iter, stat, done, conv;
+};
+
+// ---- launchers (mac_kernels.cu) ----
+template <typename T>
+void launch_face_coef(const Topo &t, const double *geom64, const T *bcoef[3], const T *afrac[3],
+                      double beta, T *tff[3], cudaStream_t s);
+
+template <typename T>
+void launch_apply(const Topo &t, const Coef<T> &c, const BlockList &L, const T *x, T *y,
+                  const T *rhs /*null: y = Ax; else y = rhs - Ax (masked)*/, const int *guard,
+                  cudaStream_t s);
+
+template <typename T>
+void launch_smooth(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi,
+                   const T *rhs, const int *guard, cudaStream_t s);
+
+template <typename T>
+void launch_restrict(const Topo &t, const Coef<T> &c, const BlockList &crse, T *phi,
+                     const int *guard, cudaStream_t s);
+
+template <typename T>
+void launch_prolong(const Topo &t, const Coef<T> &c, const BlockList &fine, T *phi,
+                    const int *guard, cudaStream_t s);
+
+void launch_flux(const Topo &t, const Coef<double> &c, const BlockList &L, int dir,
+                 const double *phi, double *flux, cudaStream_t s);
+
+void launch_fix_bc(const Topo &t, const Coef<double> &c, const BlockList &L,
+                   const double *phi_grown, int ngrow, double *rhs, cudaStream_t s);
+
+}  // namespace sayaka_gb300

@@ -1,0 +1,568 @@
+// Stencil, smoother and inter-level transfer kernels of the MAC solver.
+//
+// Every kernel works on one block list (a tower, one level of a tower, or a
+// tree level) in a single launch, one thread per (block, cell).  Values that
+// the reference obtains through ghost-cell fills and coarse/fine flux
+// registers are gathered directly:
+//   FINE_FINE face : the neighbour block's boundary cell
+//                    (src/SayakaFillPatch.cpp:92-190)
+//   FINE_CRSE face : the coarse leaf behind the parent's face, injected
+//                    (src/SayakaFillPatch.cpp:192-299, src/SayakaInterpPatch.cpp:157-189)
+//   CRSE_FINE face : sum over the fine faces of T_fine * phi_fine, i.e. the
+//                    fine-side save + RESTRICT_SUM + copy of
+//                    src/SayakaTower.cpp:298-415, src/SayakaInterpPatch.cpp:627-691
+// The arithmetic is written operation by operation in the reference's order
+// (src/SayakaMacOperator.cpp:1115-1459) and this file is compiled without
+// FMA contraction, so FP64 results are bit-identical to the reference's.
+#include <cstdint>
+
+#include "mac_device.h"
+
+namespace sayaka_gb300 {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int face_type_of(uint16_t ft, int f) { return (ft >> (2 * f)) & 3; }
+
+template <int ND>
+__device__ __forceinline__ void decode(int c, int nb, int ijk[3]) {
+  ijk[0] = c % nb;
+  ijk[1] = ND >= 2 ? (c / nb) % nb : 0;
+  ijk[2] = ND == 3 ? c / (nb * nb) : 0;
+}
+
+__device__ __forceinline__ int encode(const int ijk[3], int nb) { return ijk[0] + nb * (ijk[1] + nb * ijk[2]); }
+
+// face index of the face on side s of cell ijk in direction d (face-centred
+// valid box of the reference, first dimension fastest)
+__device__ __forceinline__ int face_index(int d, const int ijk[3], int s, int nb) {
+  int f[3] = {ijk[0], ijk[1], ijk[2]};
+  f[d] += s;
+  const int e0 = nb + (d == 0), e1 = nb + (d == 1);
+  return f[0] + e0 * (f[1] + e1 * f[2]);
+}
+
+template <typename T>
+__device__ __forceinline__ T geom(const Coef<T> &c, int b, int q) { return c.geom[b * 8 + q]; }
+
+// coefficient of a coarse/fine face: ((beta*ds)/(dx*h))*B*a
+// (src/SayakaMacOperator.cpp:1155-1161 and :1258-1266)
+template <typename T>
+__device__ __forceinline__ T cf_coef(const Coef<T> &c, const Topo &t, int b, int d, int fidx, T h) {
+  T v = c.beta * geom(c, b, 3 + d) / (geom(c, b, d) * h);
+  v = v * c.bcoef[d][(long)b * t.nfb + fidx];
+  v = v * c.afrac[d][(long)b * t.nfb + fidx];
+  return v;
+}
+
+// CRSE_FINE face: sum of the fine-side contributions T_f * phi_f over the
+// fine faces covering coarse face (d, s) of cell ijk of block b, in the
+// reference's RESTRICT_SUM order (lower transverse dimension fastest)
+template <typename T, int ND>
+__device__ __forceinline__ T crse_fine_sum(const Topo &t, const Coef<T> &c, int b, int f, const int ijk[3],
+                                           const T *__restrict__ x) {
+  const int nb = t.nb, half = nb >> 1;
+  const int d = f >> 1, s = f & 1;
+  const int N = t.neighbor[b * 6 + f];
+  int cidx = (1 - s) << d;
+  int base[3] = {0, 0, 0};
+  int tq[2] = {0, 0}, nt = 0;
+  for (int q = 0; q < ND; q++) {
+    if (q == d) continue;
+    const int sq = ijk[q] >= half ? 1 : 0;
+    cidx |= sq << q;
+    base[q] = 2 * (ijk[q] - sq * half);
+    tq[nt++] = q;
+  }
+  const int F = t.child[N * 8 + cidx];
+  int fi[3];
+  fi[d] = s == 1 ? 0 : nb - 1;
+  const int fside = s == 1 ? 0 : 1;  // the fine block's face toward b
+  const T h15 = (T)1.5;
+  T val = 0;
+  const int n1 = ND == 3 ? 2 : 1;
+  for (int a1 = 0; a1 < n1; a1++) {
+    for (int a0 = 0; a0 < 2; a0++) {
+      fi[tq[0]] = base[tq[0]] + a0;
+      if (ND == 3) fi[tq[1]] = base[tq[1]] + a1;
+      if (ND == 2) fi[2] = 0;
+      const int fx = face_index(d, fi, fside, nb);
+      const T tf = cf_coef(c, t, F, d, fx, h15);
+      val += tf * x[(long)F * t.ncell + encode(fi, nb)];
+    }
+  }
+  return val;
+}
+
+// value a FINE_CRSE ghost cell holds: the coarse leaf's boundary cell
+// (injection through the parent's ghost layer)
+template <typename T, int ND>
+__device__ __forceinline__ T fine_crse_ghost(const Topo &t, int b, int f, const int ijk[3], const T *__restrict__ x) {
+  const int nb = t.nb, half = nb >> 1;
+  const int d = f >> 1, s = f & 1;
+  const int C = t.fc_neigh[b * 6 + f];
+  const int wc = t.which_child[b];
+  int ci[3] = {0, 0, 0};
+  for (int q = 0; q < ND; q++) {
+    if (q == d)
+      ci[q] = s == 1 ? 0 : nb - 1;
+    else
+      ci[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
+  }
+  return x[(long)C * t.ncell + encode(ci, nb)];
+}
+
+// mirrored boundary cell of the same-level neighbour
+template <typename T>
+__device__ __forceinline__ T same_level_ghost(const Topo &t, int b, int f, const int ijk[3], const T *__restrict__ x) {
+  const int d = f >> 1, s = f & 1;
+  const int n = t.neighbor[b * 6 + f];
+  int ni[3] = {ijk[0], ijk[1], ijk[2]};
+  ni[d] = s == 1 ? 0 : t.nb - 1;
+  return x[(long)n * t.ncell + encode(ni, t.nb)];
+}
+
+// ---------------------------------------------------------------------------
+// MAC operator L(phi) = (phi_c*sum T - sum T*phi_nb) / (dv*vf)
+// (src/SayakaMacOperator.cpp:1325-1459); residual variant
+// r = rhs - L(phi) (src/SayakaMacUtil.cpp:9-49)
+template <typename T, int ND>
+__global__ void __launch_bounds__(kThreads) k_apply(Topo t, Coef<T> c, BlockList L, const T *__restrict__ x,
+                                                    T *__restrict__ y, const T *__restrict__ rhs, const int *guard) {
+  if (guard && *guard) return;
+  const int nb = t.nb, ncell = t.ncell;
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    const int ci = (int)(it - (long)p * ncell);
+    const int b = L.blocks[p];
+    const uint16_t ft = L.ftypes[p];
+    int ijk[3];
+    decode<ND>(ci, nb, ijk);
+    const long cb = (long)b * ncell;
+    const T dv = geom(c, b, 6);
+    const T phic = x[cb + ci];
+    T diag = c.alpha * dv;
+    T off = 0;
+#pragma unroll
+    for (int f = 0; f < 2 * ND; f++) {
+      const int d = f >> 1, s = f & 1;
+      const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+      const int fx = face_index(d, ijk, s, nb);
+      T coef, val;
+      if (!bnd) {
+        coef = c.tff[d][(long)b * t.nfb + fx];
+        const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+        val = coef * x[cb + ci + (s ? stride : -stride)];
+      } else {
+        const int ty = face_type_of(ft, f);
+        if (ty == 0) {  // FINE_FINE
+          coef = c.tff[d][(long)b * t.nfb + fx];
+          val = coef * same_level_ghost(t, b, f, ijk, x);
+        } else if (ty == 1) {  // FINE_BC
+          if (t.bc_type[b * 6 + f] == kBCNeumann) {
+            coef = 0;
+            val = 0;
+          } else {
+            coef = c.tff[d][(long)b * t.nfb + fx];
+            val = -coef * phic;
+          }
+        } else if (ty == 2) {  // FINE_CRSE
+          coef = cf_coef(c, t, b, d, fx, (T)1.5);
+          val = coef * fine_crse_ghost<T, ND>(t, b, f, ijk, x);
+        } else {  // CRSE_FINE
+          coef = cf_coef(c, t, b, d, fx, (T)0.75);
+          val = crse_fine_sum<T, ND>(t, c, b, f, ijk, x);
+        }
+      }
+      diag += coef;
+      off += val;
+    }
+    const T lphi = (phic * diag - off) / dv;
+    const T vfv = c.vf[cb + ci];
+    T out = vfv > 0 ? lphi / vfv : (T)0;
+    if (rhs) out = vfv > 0 ? rhs[cb + ci] - out : (T)0;
+    y[cb + ci] = out;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// red-black Gauss-Seidel, one colour over one level of a tower
+// (src/SayakaMacOperator.cpp:1191-1323).  Colour = (i+j+k)%2 in block-local
+// indices; nb is even so colours match across same-level block faces.
+template <typename T, int ND>
+__global__ void __launch_bounds__(kThreads) k_smooth(Topo t, Coef<T> c, BlockList L, int color, T *__restrict__ phi,
+                                                     const T *__restrict__ rhs, const int *guard) {
+  if (guard && *guard) return;
+  const int nb = t.nb, ncell = t.ncell, hrow = nb >> 1;
+  const int nhalf = ncell >> 1;
+  const long total = (long)L.n * nhalf;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / nhalf);
+    const int h = (int)(it - (long)p * nhalf);
+    const int row = h / hrow;
+    int ijk[3];
+    ijk[1] = ND >= 2 ? row % nb : 0;
+    ijk[2] = ND == 3 ? row / nb : 0;
+    ijk[0] = 2 * (h - row * hrow) + ((color + ijk[1] + ijk[2]) & 1);
+    const int ci = encode(ijk, nb);
+    const int b = L.blocks[p];
+    const uint16_t ft = L.ftypes[p];
+    const long cb = (long)b * ncell;
+    const T dv = geom(c, b, 6);
+    T diag = c.alpha * dv;
+    T off = 0;
+#pragma unroll
+    for (int f = 0; f < 2 * ND; f++) {
+      const int d = f >> 1, s = f & 1;
+      const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+      const int fx = face_index(d, ijk, s, nb);
+      T coef, val;
+      if (!bnd) {
+        coef = c.tff[d][(long)b * t.nfb + fx];
+        const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+        val = coef * phi[cb + ci + (s ? stride : -stride)];
+      } else {
+        const int ty = face_type_of(ft, f);
+        if (ty == 0) {
+          coef = c.tff[d][(long)b * t.nfb + fx];
+          val = coef * same_level_ghost(t, b, f, ijk, phi);
+        } else if (ty == 1) {
+          if (t.bc_type[b * 6 + f] == kBCNeumann) {
+            coef = 0;
+          } else {
+            coef = c.tff[d][(long)b * t.nfb + fx] * (T)2.0;
+          }
+          val = 0;
+        } else if (ty == 2) {
+          coef = cf_coef(c, t, b, d, fx, (T)1.5);
+          val = coef * fine_crse_ghost<T, ND>(t, b, f, ijk, phi);
+        } else {
+          coef = cf_coef(c, t, b, d, fx, (T)0.75);
+          val = crse_fine_sum<T, ND>(t, c, b, f, ijk, phi);
+        }
+      }
+      diag += coef;
+      off += val;
+    }
+    const T vfv = c.vf[cb + ci];
+    T unew = 0;
+    if (vfv > 0) unew = (rhs[cb + ci] * dv * vfv + off) / diag;
+    phi[cb + ci] = unew;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// volume-weighted restriction onto the non-leaf blocks of a level:
+// coarse = avg(fine*vf_fine)/vf_coarse (src/SayakaMacIB.cpp:157-232 with
+// src/SayakaInterpPatch.cpp:398-444)
+template <typename T, int ND>
+__global__ void __launch_bounds__(kThreads) k_restrict(Topo t, Coef<T> c, BlockList L, T *__restrict__ phi,
+                                                       const int *guard) {
+  if (guard && *guard) return;
+  const int nb = t.nb, ncell = t.ncell, half = nb >> 1;
+  const long total = (long)L.n * ncell;
+  const T wgt = (T)1.0 / (T)(1 << ND);
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    const int ci = (int)(it - (long)p * ncell);
+    const int b = L.blocks[p];
+    int ijk[3];
+    decode<ND>(ci, nb, ijk);
+    int cidx = 0, fb[3] = {0, 0, 0};
+    for (int q = 0; q < ND; q++) {
+      const int sq = ijk[q] >= half ? 1 : 0;
+      cidx |= sq << q;
+      fb[q] = 2 * (ijk[q] - sq * half);
+    }
+    const int F = t.child[b * 8 + cidx];
+    const long fbase = (long)F * ncell;
+    T sum = 0;
+    for (int kk = 0; kk < (ND == 3 ? 2 : 1); kk++)
+      for (int jj = 0; jj < 2; jj++)
+        for (int ii = 0; ii < 2; ii++) {
+          const int fi[3] = {fb[0] + ii, fb[1] + jj, ND == 3 ? fb[2] + kk : 0};
+          const long q = fbase + encode(fi, nb);
+          const T wv = phi[q] * c.vf[q];
+          sum += wv;
+        }
+    const T vfc = c.vf[(long)b * ncell + ci];
+    const T avg = sum * wgt;
+    phi[(long)b * ncell + ci] = vfc > 0 ? avg / vfc : (T)0;
+  }
+}
+
+// masked injection onto every block of a level (src/SayakaMacIB.cpp:234-283)
+template <typename T, int ND>
+__global__ void __launch_bounds__(kThreads) k_prolong(Topo t, Coef<T> c, BlockList L, T *__restrict__ phi,
+                                                      const int *guard) {
+  if (guard && *guard) return;
+  const int nb = t.nb, ncell = t.ncell, half = nb >> 1;
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    const int ci = (int)(it - (long)p * ncell);
+    const int b = L.blocks[p];
+    int ijk[3];
+    decode<ND>(ci, nb, ijk);
+    const int P = t.parent[b], wc = t.which_child[b];
+    int pc[3] = {0, 0, 0};
+    for (int q = 0; q < ND; q++) pc[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
+    const T v = phi[(long)P * ncell + encode(pc, nb)];
+    const long q = (long)b * ncell + ci;
+    phi[q] = c.vf[q] > 0 ? v : (T)0;
+  }
+}
+
+// same-level face coefficient ((beta*ds)/dx)*B*a for every face of every block
+template <typename T>
+__global__ void k_face_coef(Topo t, const double *geom64, const T *b0, const T *b1, const T *b2, const T *a0,
+                            const T *a1, const T *a2, double beta, T *t0, T *t1, T *t2) {
+  const long per = (long)t.nfb;
+  const long total = (long)t.nblocks * per * t.ndim;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int d = (int)(it / ((long)t.nblocks * per));
+    const long r = it - (long)d * t.nblocks * per;
+    const int b = (int)(r / per);
+    const T *B = d == 0 ? b0 : (d == 1 ? b1 : b2);
+    const T *A = d == 0 ? a0 : (d == 1 ? a1 : a2);
+    T *O = d == 0 ? t0 : (d == 1 ? t1 : t2);
+    const T ds = (T)geom64[b * 8 + 3 + d], dx = (T)geom64[b * 8 + d];
+    T v = (T)beta * ds / dx;
+    v = v * B[r];
+    v = v * A[r];
+    O[r] = v;
+  }
+}
+
+// face flux -(phi_hi - phi_lo)/h on every face of direction `dir` of a tower
+// (src/SayakaMacOperator.cpp:161-239 and :929-1025): FINE_BC faces get 0,
+// FINE_CRSE faces use h = 1.5 dx with the injected coarse ghost, CRSE_FINE
+// faces the average of the fine FINE_CRSE fluxes behind them (FLUX_SYNC_AVG).
+template <int ND>
+__global__ void k_flux(Topo t, Coef<double> c, BlockList L, int dir, const double *__restrict__ phi,
+                       double *__restrict__ flux) {
+  const int nb = t.nb, ncell = t.ncell, nfb = t.nfb;
+  const long total = (long)L.n * nfb;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / nfb);
+    const int fxi = (int)(it - (long)p * nfb);
+    const int b = L.blocks[p];
+    const uint16_t ft = L.ftypes[p];
+    // decode the face-centred index: dimension dir has nb+1 entries
+    const int e0 = nb + (dir == 0), e1 = nb + (dir == 1);
+    int fi[3];
+    fi[0] = fxi % e0;
+    fi[1] = ND >= 2 ? (fxi / e0) % e1 : 0;
+    fi[2] = ND == 3 ? fxi / (e0 * e1) : 0;
+    const int m = fi[dir];
+    const double dh = c.geom[b * 8 + dir];
+    const long cb = (long)b * ncell;
+    double out;
+    if (m > 0 && m < nb) {
+      int hi[3] = {fi[0], fi[1], fi[2]}, lo[3] = {fi[0], fi[1], fi[2]};
+      lo[dir] = m - 1;
+      out = -(phi[cb + encode(hi, nb)] - phi[cb + encode(lo, nb)]) / dh;
+    } else {
+      const int s = m == 0 ? 0 : 1;
+      const int f = 2 * dir + s;
+      const int ty = face_type_of(ft, f);
+      int own[3] = {fi[0], fi[1], fi[2]};
+      own[dir] = s == 0 ? 0 : nb - 1;
+      const double po = phi[cb + encode(own, nb)];
+      if (ty == 1) {
+        out = 0;
+      } else if (ty == 0) {
+        const double g = same_level_ghost(t, b, f, own, phi);
+        out = s == 0 ? -(po - g) / dh : -(g - po) / dh;
+      } else if (ty == 2) {
+        const double g = fine_crse_ghost<double, ND>(t, b, f, own, phi);
+        const double h = dh * 1.5;
+        out = s == 0 ? -(po - g) / h : -(g - po) / h;
+      } else {
+        // average of the fine FINE_CRSE fluxes on this face
+        const int N = t.neighbor[b * 6 + f];
+        const int half = nb >> 1;
+        int cidx = (1 - s) << dir, base[3] = {0, 0, 0}, tq[2] = {0, 0}, nt = 0;
+        for (int q = 0; q < ND; q++) {
+          if (q == dir) continue;
+          const int sq = own[q] >= half ? 1 : 0;
+          cidx |= sq << q;
+          base[q] = 2 * (own[q] - sq * half);
+          tq[nt++] = q;
+        }
+        const int F = t.child[N * 8 + cidx];
+        const double dhf = c.geom[F * 8 + dir] * 1.5;
+        int fc[3];
+        fc[dir] = s == 1 ? 0 : nb - 1;
+        double sum = 0;
+        for (int a1 = 0; a1 < (ND == 3 ? 2 : 1); a1++)
+          for (int a0 = 0; a0 < 2; a0++) {
+            fc[tq[0]] = base[tq[0]] + a0;
+            if (ND == 3) fc[tq[1]] = base[tq[1]] + a1;
+            if (ND == 2) fc[2] = 0;
+            const double pf = phi[(long)F * ncell + encode(fc, nb)];
+            // the fine block's ghost toward b is b's boundary cell `own`
+            const double fl = s == 1 ? -(pf - po) / dhf : -(po - pf) / dhf;
+            sum += fl;
+          }
+        out = sum * (ND == 3 ? 0.25 : 0.5);
+      }
+    }
+    flux[(long)b * nfb + fxi] = out;
+  }
+}
+
+// Dirichlet / SimpleFill lift of the right-hand side from BC values held in
+// the ghost layer of phi (src/SayakaMacOperator.cpp:1470-1594)
+template <int ND>
+__global__ void k_fix_bc(Topo t, Coef<double> c, BlockList L, const double *__restrict__ phig, int ng,
+                         double *__restrict__ rhs) {
+  const int nb = t.nb, ncell = t.ncell;
+  const int G = nb + 2 * ng;
+  const long gstride = ND == 3 ? (long)G * G * G : (long)G * G;
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    const int ci = (int)(it - (long)p * ncell);
+    const int b = L.blocks[p];
+    const uint16_t ft = L.ftypes[p];
+    int ijk[3];
+    decode<ND>(ci, nb, ijk);
+    const double dv = c.geom[b * 8 + 6];
+    const long q = (long)b * ncell + ci;
+    double r = rhs[q];
+    for (int f = 0; f < 2 * ND; f++) {
+      if (face_type_of(ft, f) != 1) continue;
+      const int d = f >> 1, s = f & 1;
+      if (ijk[d] != (s ? nb - 1 : 0)) continue;
+      const int bct = t.bc_type[b * 6 + f];
+      auto gidx = [&](int i, int j, int k) {
+        return (long)b * gstride + (i + ng) + (long)G * ((j + ng) + (long)G * (ND == 3 ? k + ng : 0));
+      };
+      const double p0 = phig[gidx(ijk[0], ijk[1], ijk[2])];
+      int gi[3] = {ijk[0], ijk[1], ijk[2]};
+      gi[d] += s ? 1 : -1;
+      const double p1 = phig[gidx(gi[0], gi[1], gi[2])];
+      const int fx = face_index(d, ijk, s, nb);
+      double coef = c.beta * c.geom[b * 8 + 3 + d] / c.geom[b * 8 + d];
+      coef *= c.bcoef[d][(long)b * t.nfb + fx];
+      coef *= c.afrac[d][(long)b * t.nfb + fx];
+      double corr = 0;
+      if (bct == kBCDirichlet) {
+        const double pbc = 0.5 * (p0 + p1);
+        corr = pbc * 2.0 * coef;
+      } else if (bct == kBCSimpleFill) {
+        const double pbc = p1;
+        corr = pbc * 2.0 * coef;
+      }
+      const double vfv = c.vf[q];
+      if (vfv > 0) {
+        corr /= (dv * vfv);
+        r += corr;
+      }
+    }
+    rhs[q] = r;
+  }
+}
+
+inline int grid_for(long work) {
+  long g = (work + kThreads - 1) / kThreads;
+  if (g < 1) g = 1;
+  if (g > 152 * 32) g = 152 * 32;
+  return (int)g;
+}
+
+}  // namespace
+
+template <typename T>
+void launch_face_coef(const Topo &t, const double *geom64, const T *bcoef[3], const T *afrac[3], double beta,
+                      T *tff[3], cudaStream_t s) {
+  const long work = (long)t.nblocks * t.nfb * t.ndim;
+  if (work == 0) return;
+  k_face_coef<T><<<grid_for(work), kThreads, 0, s>>>(t, geom64, bcoef[0], bcoef[1], bcoef[2], afrac[0], afrac[1],
+                                                     afrac[2], beta, tff[0], tff[1], tff[2]);
+}
+
+template <typename T>
+void launch_apply(const Topo &t, const Coef<T> &c, const BlockList &L, const T *x, T *y, const T *rhs,
+                  const int *guard, cudaStream_t s) {
+  const long work = (long)L.n * t.ncell;
+  if (work == 0) return;
+  if (t.ndim == 2)
+    k_apply<T, 2><<<grid_for(work), kThreads, 0, s>>>(t, c, L, x, y, rhs, guard);
+  else
+    k_apply<T, 3><<<grid_for(work), kThreads, 0, s>>>(t, c, L, x, y, rhs, guard);
+}
+
+template <typename T>
+void launch_smooth(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
+                   const int *guard, cudaStream_t s) {
+  const long work = (long)L.n * (t.ncell / 2);
+  if (work == 0) return;
+  if (t.ndim == 2)
+    k_smooth<T, 2><<<grid_for(work), kThreads, 0, s>>>(t, c, L, color, phi, rhs, guard);
+  else
+    k_smooth<T, 3><<<grid_for(work), kThreads, 0, s>>>(t, c, L, color, phi, rhs, guard);
+}
+
+template <typename T>
+void launch_restrict(const Topo &t, const Coef<T> &c, const BlockList &L, T *phi, const int *guard,
+                     cudaStream_t s) {
+  const long work = (long)L.n * t.ncell;
+  if (work == 0) return;
+  if (t.ndim == 2)
+    k_restrict<T, 2><<<grid_for(work), kThreads, 0, s>>>(t, c, L, phi, guard);
+  else
+    k_restrict<T, 3><<<grid_for(work), kThreads, 0, s>>>(t, c, L, phi, guard);
+}
+
+template <typename T>
+void launch_prolong(const Topo &t, const Coef<T> &c, const BlockList &L, T *phi, const int *guard,
+                    cudaStream_t s) {
+  const long work = (long)L.n * t.ncell;
+  if (work == 0) return;
+  if (t.ndim == 2)
+    k_prolong<T, 2><<<grid_for(work), kThreads, 0, s>>>(t, c, L, phi, guard);
+  else
+    k_prolong<T, 3><<<grid_for(work), kThreads, 0, s>>>(t, c, L, phi, guard);
+}
+
+void launch_flux(const Topo &t, const Coef<double> &c, const BlockList &L, int dir, const double *phi, double *flux,
+                 cudaStream_t s) {
+  const long work = (long)L.n * t.nfb;
+  if (work == 0) return;
+  if (t.ndim == 2)
+    k_flux<2><<<grid_for(work), kThreads, 0, s>>>(t, c, L, dir, phi, flux);
+  else
+    k_flux<3><<<grid_for(work), kThreads, 0, s>>>(t, c, L, dir, phi, flux);
+}
+
+void launch_fix_bc(const Topo &t, const Coef<double> &c, const BlockList &L, const double *phig, int ng, double *rhs,
+                   cudaStream_t s) {
+  const long work = (long)L.n * t.ncell;
+  if (work == 0) return;
+  if (t.ndim == 2)
+    k_fix_bc<2><<<grid_for(work), kThreads, 0, s>>>(t, c, L, phig, ng, rhs);
+  else
+    k_fix_bc<3><<<grid_for(work), kThreads, 0, s>>>(t, c, L, phig, ng, rhs);
+}
+
+#define SAYAKA_INST(T)                                                                                          \
+  template void launch_face_coef<T>(const Topo &, const double *, const T *[3], const T *[3], double, T *[3],  \
+                                    cudaStream_t);                                                              \
+  template void launch_apply<T>(const Topo &, const Coef<T> &, const BlockList &, const T *, T *, const T *,   \
+                                const int *, cudaStream_t);                                                     \
+  template void launch_smooth<T>(const Topo &, const Coef<T> &, const BlockList &, int, T *, const T *,        \
+                                 const int *, cudaStream_t);                                                    \
+  template void launch_restrict<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,         \
+                                   cudaStream_t);                                                               \
+  template void launch_prolong<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,          \
+                                  cudaStream_t);
+SAYAKA_INST(double)
+SAYAKA_INST(float)
+#undef SAYAKA_INST
+
+}  // namespace sayaka_gb300

@@ -1,0 +1,894 @@
+// Host orchestration of the GPU MAC solver: device pools, block lists,
+// coefficient setup, vector kernels / reductions, the V-cycle preconditioner
+// and the BiCGSTAB driver.
+#include "mac_solver.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "tower.h"
+#include "tree.h"
+
+namespace sayaka_gb300 {
+
+#define CK(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess) {                                                                    \
+      fail(std::string(#x) + ": " + cudaGetErrorString(e_));                                   \
+      return;                                                                                   \
+    }                                                                                           \
+  } while (0)
+#define CKR(x, r)                                                                               \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess) {                                                                    \
+      fail(std::string(#x) + ": " + cudaGetErrorString(e_));                                   \
+      return r;                                                                                 \
+    }                                                                                           \
+  } while (0)
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kRedBlocks = 2 * 152;
+
+inline int grid_for(long work) {
+  long g = (work + kThreads - 1) / kThreads;
+  if (g < 1) g = 1;
+  if (g > 152 * 32) g = 152 * 32;
+  return (int)g;
+}
+
+__global__ void k_copy(BlockList L, int ncell, double *dst, const double *src) {
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    const long q = (long)L.blocks[p] * ncell + (it - (long)p * ncell);
+    dst[q] = src[q];
+  }
+}
+__global__ void k_zero(BlockList L, int ncell, double *dst) {
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    dst[(long)L.blocks[p] * ncell + (it - (long)p * ncell)] = 0.0;
+  }
+}
+// out = a*x + b*y (src/SayakaBlockData.cpp:213-261)
+__global__ void k_axpby(BlockList L, int ncell, double *out, double a, const double *x, double b, const double *y) {
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    const long q = (long)L.blocks[p] * ncell + (it - (long)p * ncell);
+    out[q] = a * x[q] + b * y[q];
+  }
+}
+// masked copy r = (vf > 0) ? src : 0
+__global__ void k_masked_copy(BlockList L, int ncell, const double *vf, double *dst, const double *src) {
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    const long q = (long)L.blocks[p] * ncell + (it - (long)p * ncell);
+    dst[q] = vf[q] > 0 ? src[q] - 0.0 : 0.0;
+  }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// MODE 0: sum a*b ; MODE 1: max |a|.  Two-level reduction, the last block
+// to finish combines the per-block partials in a fixed order.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_reduce(BlockList L, int ncell, const double *a, const double *b,
+                                                     double *partials, unsigned *counter, double *out) {
+  __shared__ double sh[kThreads / 32];
+  __shared__ bool last;
+  double acc = 0.0;
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    const long q = (long)L.blocks[p] * ncell + (it - (long)p * ncell);
+    if (MODE == 0)
+      acc += a[q] * b[q];
+    else
+      acc = fmax(acc, fabs(a[q]));
+  }
+  acc = MODE == 0 ? warp_sum(acc) : warp_max(acc);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < kThreads / 32 ? sh[threadIdx.x] : 0.0;
+    v = MODE == 0 ? warp_sum(v) : warp_max(v);
+    if (threadIdx.x == 0) {
+      partials[blockIdx.x] = v;
+      __threadfence();
+      const unsigned t = atomicAdd(counter, 1u);
+      last = (t == gridDim.x - 1);
+    }
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double v = 0.0;
+  for (int i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+    const double pv = ((volatile double *)partials)[i];
+    v = MODE == 0 ? v + pv : fmax(v, pv);
+  }
+  v = MODE == 0 ? warp_sum(v) : warp_max(v);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < kThreads / 32; w++) r = MODE == 0 ? r + sh[w] : fmax(r, sh[w]);
+    *out = r;
+    *counter = 0;
+  }
+}
+
+template <typename T>
+T *dalloc(size_t n) {
+  T *p = nullptr;
+  if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
+  cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T));
+  return p;
+}
+
+void tree_from_tables(const TreeTables &tt, AmrTree &t) {
+  t.init(tt.ndim, tt.nb, tt.min_level, tt.max_level, std::max(tt.num_blocks, 1));
+  t.num_blocks = tt.num_blocks;
+  for (int b = 0; b < tt.num_blocks; b++) {
+    TreeNode &n = t.nodes[b];
+    n.level = tt.level[b];
+    for (int f = 0; f < 6; f++) n.neighbor[f] = tt.neighbor[b * 6 + f];
+    for (int c = 0; c < 8; c++) n.child[c] = tt.child[b * 8 + c];
+    n.parent = tt.parent[b];
+    n.which_child = tt.which_child[b];
+    n.node_type = tt.node_type[b];
+  }
+  for (int l = 1; l <= tt.max_level; l++) t.levels[l].clear();
+  for (int b = 0; b < tt.num_blocks; b++)
+    if (tt.level[b] >= 1 && tt.level[b] <= tt.max_level) t.levels[tt.level[b]].push_back(b);
+}
+
+}  // namespace
+
+void MacGpu::fail(const std::string &m) {
+  if (err_.empty()) err_ = m;
+}
+
+MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
+  const int nd = tt.ndim, nb = tt.nb, nbk = tt.num_blocks;
+  if (nd < 2 || nd > 3 || nb < 2 || (nb & 1) || nbk <= 0) {
+    fail("bad tree tables (ndim 2|3, even nb, blocks > 0)");
+    return;
+  }
+  ncell_ = nd == 2 ? nb * nb : nb * nb * nb;
+  nfb_ = nd == 2 ? (nb + 1) * nb : (nb + 1) * nb * nb;
+  finest_ = 0;
+  for (int b = 0; b < nbk; b++) finest_ = std::max(finest_, tt.level[b]);
+  if (finest_ < 1 || finest_ > tt.max_level) {
+    fail("bad block levels");
+    return;
+  }
+  CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+
+  // geometry exactly as the reference computes it (src/SayakaTree.h:277-301)
+  geom_.assign((size_t)nbk * 8, 0.0);
+  for (int b = 0; b < nbk; b++) {
+    double dx[3], ds[3] = {1, 1, 1}, v = 1.0;
+    for (int d = 0; d < 3; d++) dx[d] = tt.block_len[b * 3 + d];
+    for (int d = 0; d < nd; d++) dx[d] /= nb;
+    for (int d = 0; d < nd; d++) v *= dx[d];
+    for (int d = 0; d < nd; d++) ds[d] = v / dx[d];
+    for (int d = 0; d < 3; d++) {
+      geom_[b * 8 + d] = dx[d];
+      geom_[b * 8 + 3 + d] = ds[d];
+    }
+    geom_[b * 8 + 6] = v;
+  }
+  // coarse leaf behind a coarse/fine face: the parent's neighbour
+  fc_neigh_.assign((size_t)nbk * 6, -1);
+  for (int b = 0; b < nbk; b++)
+    for (int f = 0; f < 2 * nd; f++) {
+      const int nbr = tt.neighbor[b * 6 + f];
+      if (nbr < 0 && nbr > kPhysBndry && tt.parent[b] >= 0) fc_neigh_[b * 6 + f] = tt.neighbor[tt.parent[b] * 6 + f];
+    }
+  bc_type_.assign((size_t)nbk * 6, -1);
+  for (int d = 0; d < 3; d++) {
+    bcoef_[d].assign(d < nd ? (size_t)nbk * nfb_ : 1, 1.0);
+    afrac_[d].assign(d < nd ? (size_t)nbk * nfb_ : 1, 1.0);
+  }
+  vf_.assign((size_t)nbk * ncell_, 1.0);
+
+  // towers and level lists
+  AmrTree t;
+  tree_from_tables(tt, t);
+  std::vector<Tower> tw = build_towers(t);
+  towers_.resize(tt.max_level + 1);
+  for (int L = 1; L <= tt.max_level; L++) {
+    const Tower &src = tw[L];
+    DevTower &dt = towers_[L];
+    dt.begin = src.begin;
+    dt.end = src.end;
+    dt.blocks = src.blocks;
+    const int n = (int)src.blocks.size();
+    std::vector<uint16_t> ft(n, 0);
+    for (int p = 0; p < n; p++) {
+      uint16_t v = 0;
+      for (int f = 0; f < 2 * nd; f++) v |= (uint16_t)(src.regs[p * 6 + f].type & 3) << (2 * f);
+      ft[p] = v;
+    }
+    dt.all.n = n;
+    dt.all.blocks = dalloc<int>(n);
+    dt.all.ftypes = dalloc<uint16_t>(n);
+    if (n) {
+      CK(cudaMemcpy(dt.all.blocks, src.blocks.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(dt.all.ftypes, ft.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    }
+  }
+  levels_.resize(tt.max_level + 1);
+  nonleaf_.resize(tt.max_level + 1);
+  level_blocks_.resize(tt.max_level + 1);
+  nonleaf_blocks_.resize(tt.max_level + 1);
+  for (int l = 1; l <= tt.max_level; l++) {
+    level_blocks_[l] = t.levels[l];
+    for (int b : t.levels[l])
+      if (tt.node_type[b] != kNodeLeaf) nonleaf_blocks_[l].push_back(b);
+    for (int k = 0; k < 2; k++) {
+      const std::vector<int> &v = k == 0 ? level_blocks_[l] : nonleaf_blocks_[l];
+      DevList &dl = k == 0 ? levels_[l] : nonleaf_[l];
+      dl.n = (int)v.size();
+      dl.blocks = dalloc<int>(v.size());
+      if (!v.empty()) CK(cudaMemcpy(dl.blocks, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+  }
+
+  // device tables
+  d_neighbor_ = dalloc<int>((size_t)nbk * 6);
+  d_child_ = dalloc<int>((size_t)nbk * 8);
+  d_parent_ = dalloc<int>(nbk);
+  d_wc_ = dalloc<int>(nbk);
+  d_fc_neigh_ = dalloc<int>((size_t)nbk * 6);
+  d_bc_type_ = dalloc<int>((size_t)nbk * 6);
+  d_geom_ = dalloc<double>((size_t)nbk * 8);
+  CK(cudaMemcpy(d_neighbor_, tt.neighbor.data(), (size_t)nbk * 6 * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_child_, tt.child.data(), (size_t)nbk * 8 * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_parent_, tt.parent.data(), (size_t)nbk * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_wc_, tt.which_child.data(), (size_t)nbk * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_fc_neigh_, fc_neigh_.data(), (size_t)nbk * 6 * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_geom_, geom_.data(), (size_t)nbk * 8 * sizeof(double), cudaMemcpyHostToDevice));
+  for (int d = 0; d < nd; d++) {
+    d_bcoef_[d] = dalloc<double>((size_t)nbk * nfb_);
+    d_afrac_[d] = dalloc<double>((size_t)nbk * nfb_);
+    d_tff_[d] = dalloc<double>((size_t)nbk * nfb_);
+  }
+  d_vf_ = dalloc<double>((size_t)nbk * ncell_);
+  for (int v = 0; v < kNumVec; v++) {
+    vec_[v] = dalloc<double>((size_t)nbk * ncell_);
+    if (!vec_[v]) {
+      fail("out of device memory");
+      return;
+    }
+  }
+  d_red_ = dalloc<double>(kRedBlocks + 8);
+  d_counter_ = dalloc<unsigned>(4);
+  CK(cudaMallocHost(&h_red_, 8 * sizeof(double)));
+
+  topo_.ndim = nd;
+  topo_.nb = nb;
+  topo_.ncell = ncell_;
+  topo_.nfb = nfb_;
+  topo_.nblocks = nbk;
+  topo_.neighbor = d_neighbor_;
+  topo_.child = d_child_;
+  topo_.parent = d_parent_;
+  topo_.which_child = d_wc_;
+  topo_.fc_neigh = d_fc_neigh_;
+  topo_.bc_type = d_bc_type_;
+
+  c64_.geom = d_geom_;
+  for (int d = 0; d < 3; d++) {
+    c64_.tff[d] = d_tff_[d];
+    c64_.bcoef[d] = d_bcoef_[d];
+    c64_.afrac[d] = d_afrac_[d];
+  }
+  c64_.vf = d_vf_;
+  // physical faces without setBC behave as Dirichlet-0 in the reference's
+  // release build (src/SayakaMacOperator.cpp:1142-1151); start from that
+  for (int b = 0; b < nbk; b++)
+    for (int f = 0; f < 2 * nd; f++)
+      if (tt.neighbor[b * 6 + f] <= kPhysBndry) bc_type_[b * 6 + f] = kBCDirichlet;
+  CK(cudaMemcpy(d_bc_type_, bc_type_.data(), (size_t)nbk * 6 * sizeof(int), cudaMemcpyHostToDevice));
+  set_scalars(0.0, 1.0);
+}
+
+MacGpu::~MacGpu() {
+  auto fr = [](void *p) {
+    if (p) cudaFree(p);
+  };
+  for (auto &t : towers_) {
+    fr(t.all.blocks);
+    fr(t.all.ftypes);
+  }
+  for (auto &l : levels_) fr(l.blocks);
+  for (auto &l : nonleaf_) fr(l.blocks);
+  fr(d_neighbor_);
+  fr(d_child_);
+  fr(d_parent_);
+  fr(d_wc_);
+  fr(d_fc_neigh_);
+  fr(d_bc_type_);
+  fr(d_geom_);
+  for (int d = 0; d < 3; d++) {
+    fr(d_bcoef_[d]);
+    fr(d_afrac_[d]);
+    fr(d_tff_[d]);
+  }
+  fr(d_vf_);
+  for (auto *v : vec_) fr(v);
+  fr(d_red_);
+  fr(d_counter_);
+  if (h_red_) cudaFreeHost(h_red_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+// ---------------------------------------------------------------------------
+// block lists
+BlockList MacGpu::tower_list(int L) const {
+  const DevTower &t = towers_[L];
+  return BlockList{t.all.blocks, t.all.ftypes, t.all.n};
+}
+BlockList MacGpu::sublevel_list(int L, int l) const {
+  const DevTower &t = towers_[L];
+  const int b = t.begin[l], e = t.end[l];
+  return BlockList{t.all.blocks + b, t.all.ftypes + b, e - b};
+}
+BlockList MacGpu::level_list(int l) const { return BlockList{levels_[l].blocks, nullptr, levels_[l].n}; }
+BlockList MacGpu::nonleaf_list(int l) const { return BlockList{nonleaf_[l].blocks, nullptr, nonleaf_[l].n}; }
+
+// ---------------------------------------------------------------------------
+// coefficients
+void MacGpu::set_scalars(double alpha, double beta) {
+  alpha_ = alpha;
+  beta_ = beta;
+  c64_.alpha = alpha;
+  c64_.beta = beta;
+  upload_coefs();
+}
+
+void MacGpu::upload_coefs() {
+  const int nd = tt_.ndim, nbk = tt_.num_blocks;
+  for (int d = 0; d < nd; d++) {
+    CK(cudaMemcpyAsync(d_bcoef_[d], bcoef_[d].data(), (size_t)nbk * nfb_ * sizeof(double), cudaMemcpyHostToDevice,
+                       stream_));
+    CK(cudaMemcpyAsync(d_afrac_[d], afrac_[d].data(), (size_t)nbk * nfb_ * sizeof(double), cudaMemcpyHostToDevice,
+                       stream_));
+  }
+  CK(cudaMemcpyAsync(d_vf_, vf_.data(), (size_t)nbk * ncell_ * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  recompute_face_coef();
+  CK(cudaStreamSynchronize(stream_));
+}
+
+void MacGpu::recompute_face_coef() {
+  const double *b[3] = {d_bcoef_[0], d_bcoef_[1], d_bcoef_[2]};
+  const double *a[3] = {d_afrac_[0], d_afrac_[1], d_afrac_[2]};
+  double *o[3] = {d_tff_[0], d_tff_[1], d_tff_[2]};
+  for (int d = tt_.ndim; d < 3; d++) {
+    b[d] = b[0];
+    a[d] = a[0];
+    o[d] = o[0];
+  }
+  launch_face_coef<double>(topo_, d_geom_, b, a, beta_, o, stream_);
+}
+
+// index helpers for host-side face/cell restriction
+static inline int cell_index(int i, int j, int k, int nb) { return i + nb * (j + nb * k); }
+static inline int face_idx(int d, int i, int j, int k, int nb) {
+  const int e0 = nb + (d == 0), e1 = nb + (d == 1);
+  return i + e0 * (j + e1 * k);
+}
+
+// FLUX_SYNC_AVG of face data at coarse/fine faces of the finest tower
+// (src/SayakaTower.cpp:298-415): fine face values are averaged into the
+// parent's face, then copied to the coarse neighbour's matching face.
+void MacGpu::sync_face_avg_host(int dir, std::vector<double> &F) const {
+  const int nd = tt_.ndim, nb = tt_.nb, half = nb / 2;
+  const DevTower &tw = towers_[finest_];
+  const double scale = nd == 3 ? 0.25 : 0.5;
+  const int kz = nd == 3 ? 1 : 0;
+  for (int l = finest_; l >= 2; l--) {
+    // fine level: restrict FINE_CRSE faces into the parent
+    for (int p = tw.begin[l]; p < tw.end[l]; p++) {
+      const int b = tw.blocks[p];
+      for (int side = 0; side <= 1; side++) {
+        const int f = 2 * dir + side;
+        const int nbr = tt_.neighbor[b * 6 + f];
+        if (!(nbr < 0 && nbr > kPhysBndry)) continue;  // not FINE_CRSE
+        const int P = tt_.parent[b], wc = tt_.which_child[b];
+        int off[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+        for (int q = 0; q < nd; q++) {
+          off[q] = ((wc >> q) & 1) * half;
+          lo[q] = off[q];
+          hi[q] = off[q] + half - 1;
+        }
+        // boundary face of the child's sub-box on `side`
+        lo[dir] = hi[dir] = side == 0 ? off[dir] : off[dir] + half;
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            for (int i = lo[0]; i <= hi[0]; i++) {
+              const int cc[3] = {i, j, k};
+              double val = 0;
+              const int t0 = dir == 0 ? 1 : 0;
+              const int t1 = dir == 2 ? 1 : 2;
+              for (int a1 = 0; a1 <= (nd == 3 ? 1 : 0); a1++)
+                for (int a0 = 0; a0 <= 1; a0++) {
+                  int fi[3];
+                  fi[dir] = 2 * (cc[dir] - off[dir]);
+                  fi[t0] = 2 * (cc[t0] - off[t0]) + a0;
+                  if (nd == 3) fi[t1] = 2 * (cc[t1] - off[t1]) + a1;
+                  else fi[2] = 0;
+                  if (nd == 2 && t0 == 2) continue;
+                  val += F[(size_t)b * nfb_ + face_idx(dir, fi[0], fi[1], fi[2], nb)];
+                }
+              F[(size_t)P * nfb_ + face_idx(dir, i, j, k, nb)] = val * scale;
+            }
+        (void)kz;
+      }
+    }
+    // coarse level: copy into CRSE_FINE faces
+    for (int p = tw.begin[l - 1]; p < tw.end[l - 1]; p++) {
+      const int b = tw.blocks[p];
+      for (int side = 0; side <= 1; side++) {
+        const int f = 2 * dir + side;
+        const int nbr = tt_.neighbor[b * 6 + f];
+        if (!(nbr >= 0 && tt_.node_type[nbr] != kNodeLeaf)) continue;
+        // CRSE_FINE only when the coarse block sits below the tower level
+        if (l - 1 >= finest_) continue;
+        int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+        for (int q = 0; q < nd; q++) hi[q] = nb - 1;
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            for (int i = lo[0]; i <= hi[0]; i++) {
+              int di[3] = {i, j, k}, si[3] = {i, j, k};
+              if (((dir == 0) && i != 0) || ((dir == 1) && j != 0) || ((dir == 2) && k != 0)) continue;
+              di[dir] = side == 0 ? 0 : nb;
+              si[dir] = side == 0 ? nb : 0;
+              F[(size_t)b * nfb_ + face_idx(dir, di[0], di[1], di[2], nb)] =
+                  F[(size_t)nbr * nfb_ + face_idx(dir, si[0], si[1], si[2], nb)];
+            }
+      }
+    }
+  }
+}
+
+// AVG restriction of face data onto non-leaf blocks, finest-1 .. 1
+// (src/SayakaFillPatch.cpp:401-447 with src/SayakaInterpPatch.cpp:627-691)
+void MacGpu::restrict_face_avg_host(int dir, std::vector<double> &F) const {
+  const int nd = tt_.ndim, nb = tt_.nb, half = nb / 2;
+  const double scale = nd == 3 ? 0.25 : 0.5;
+  for (int l = finest_ - 1; l >= 1; l--) {
+    for (int b : nonleaf_blocks_[l]) {
+      for (int c = 0; c < (1 << nd); c++) {
+        const int C = tt_.child[b * 8 + c];
+        int off[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+        for (int q = 0; q < nd; q++) {
+          off[q] = ((c >> q) & 1) * half;
+          lo[q] = off[q];
+          hi[q] = off[q] + half - 1;
+        }
+        hi[dir] += 1;  // staggered in dir
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            for (int i = lo[0]; i <= hi[0]; i++) {
+              const int cc[3] = {i, j, k};
+              double val = 0;
+              const int t0 = dir == 0 ? 1 : 0;
+              const int t1 = dir == 2 ? 1 : 2;
+              for (int a1 = 0; a1 <= (nd == 3 ? 1 : 0); a1++)
+                for (int a0 = 0; a0 <= 1; a0++) {
+                  int fi[3];
+                  fi[dir] = 2 * (cc[dir] - off[dir]);
+                  fi[t0] = 2 * (cc[t0] - off[t0]) + a0;
+                  if (nd == 3) fi[t1] = 2 * (cc[t1] - off[t1]) + a1;
+                  else fi[2] = 0;
+                  val += F[(size_t)C * nfb_ + face_idx(dir, fi[0], fi[1], fi[2], nb)];
+                }
+              F[(size_t)b * nfb_ + face_idx(dir, i, j, k, nb)] = val * scale;
+            }
+      }
+    }
+  }
+}
+
+// AVG restriction of cell data onto non-leaf blocks, finest-1 .. 1
+void MacGpu::restrict_cell_avg_host(std::vector<double> &V) const {
+  const int nd = tt_.ndim, nb = tt_.nb, half = nb / 2;
+  const double wgt = 1.0 / (1 << nd);
+  for (int l = finest_ - 1; l >= 1; l--) {
+    for (int b : nonleaf_blocks_[l]) {
+      for (int k = 0; k < (nd == 3 ? nb : 1); k++)
+        for (int j = 0; j < nb; j++)
+          for (int i = 0; i < nb; i++) {
+            const int ijk[3] = {i, j, k};
+            int c = 0, fb[3] = {0, 0, 0};
+            for (int q = 0; q < nd; q++) {
+              const int s = ijk[q] >= half;
+              c |= s << q;
+              fb[q] = 2 * (ijk[q] - s * half);
+            }
+            const int C = tt_.child[b * 8 + c];
+            double sum = 0;
+            for (int kk = 0; kk < (nd == 3 ? 2 : 1); kk++)
+              for (int jj = 0; jj < 2; jj++)
+                for (int ii = 0; ii < 2; ii++)
+                  sum += V[(size_t)C * ncell_ + cell_index(fb[0] + ii, fb[1] + jj, fb[2] + kk, nb)];
+            V[(size_t)b * ncell_ + cell_index(i, j, k, nb)] = sum * wgt;
+          }
+    }
+  }
+}
+
+void MacGpu::set_coef_b_leaf(int dir, const double *face_all) {
+  std::vector<double> &B = bcoef_[dir];
+  const DevTower &tw = towers_[finest_];
+  for (int b : tw.blocks) std::memcpy(&B[(size_t)b * nfb_], &face_all[(size_t)b * nfb_], nfb_ * sizeof(double));
+  sync_face_avg_host(dir, B);
+  restrict_face_avg_host(dir, B);
+  upload_coefs();
+}
+
+void MacGpu::set_ib_frac_leaf(const double *vol_all, const double *const area_all[3]) {
+  const DevTower &tw = towers_[finest_];
+  for (int b : tw.blocks) {
+    std::memcpy(&vf_[(size_t)b * ncell_], &vol_all[(size_t)b * ncell_], ncell_ * sizeof(double));
+    for (int d = 0; d < tt_.ndim; d++)
+      std::memcpy(&afrac_[d][(size_t)b * nfb_], &area_all[d][(size_t)b * nfb_], nfb_ * sizeof(double));
+  }
+  for (int d = 0; d < tt_.ndim; d++) sync_face_avg_host(d, afrac_[d]);
+  restrict_cell_avg_host(vf_);
+  for (int d = 0; d < tt_.ndim; d++) restrict_face_avg_host(d, afrac_[d]);
+  upload_coefs();
+}
+
+// binary fractions from a level set with >= 1 ghost layer, ls <= 0 solid
+// (src/SayakaMacIB.cpp:99-154)
+void MacGpu::set_ib_frac_by_ls(const double *ls, int ng) {
+  const int nd = tt_.ndim, nb = tt_.nb;
+  const int G = nb + 2 * ng;
+  const size_t gsz = nd == 3 ? (size_t)G * G * G : (size_t)G * G;
+  auto L = [&](int b, int i, int j, int k) {
+    return ls[(size_t)b * gsz + (i + ng) + (size_t)G * ((j + ng) + (size_t)G * (nd == 3 ? k + ng : 0))];
+  };
+  std::vector<double> vol(vf_);
+  std::vector<double> area[3];
+  for (int d = 0; d < nd; d++) area[d] = afrac_[d];
+  const DevTower &tw = towers_[finest_];
+  for (int b : tw.blocks) {
+    for (int k = 0; k < (nd == 3 ? nb : 1); k++)
+      for (int j = 0; j < nb; j++)
+        for (int i = 0; i < nb; i++) vol[(size_t)b * ncell_ + cell_index(i, j, k, nb)] = L(b, i, j, k) <= 0 ? 0.0 : 1.0;
+    for (int d = 0; d < nd; d++) {
+      const int ii = d == 0, jj = d == 1, kk = d == 2;
+      for (int k = 0; k < (nd == 3 ? nb + kk : 1); k++)
+        for (int j = 0; j < nb + jj; j++)
+          for (int i = 0; i < nb + ii; i++) {
+            const bool solid = L(b, i - ii, j - jj, k - kk) <= 0 || L(b, i, j, k) <= 0;
+            area[d][(size_t)b * nfb_ + face_idx(d, i, j, k, nb)] = solid ? 0.0 : 1.0;
+          }
+    }
+  }
+  const double *ap[3] = {area[0].data(), nd >= 2 ? area[1].data() : nullptr, nd == 3 ? area[2].data() : nullptr};
+  set_ib_frac_leaf(vol.data(), ap);
+}
+
+void MacGpu::set_bc_types(const int *bc6) {
+  for (int b = 0; b < tt_.num_blocks; b++)
+    for (int f = 0; f < 6; f++) {
+      const bool phys = f < 2 * tt_.ndim && tt_.neighbor[b * 6 + f] <= kPhysBndry;
+      bc_type_[b * 6 + f] = phys ? bc6[b * 6 + f] : -1;
+    }
+  CK(cudaMemcpy(d_bc_type_, bc_type_.data(), bc_type_.size() * sizeof(int), cudaMemcpyHostToDevice));
+}
+
+void MacGpu::get_coef(int which, int dir, double *out) const {
+  if (which == 0)
+    std::memcpy(out, bcoef_[dir].data(), bcoef_[dir].size() * sizeof(double));
+  else if (which == 1)
+    std::memcpy(out, afrac_[dir].data(), afrac_[dir].size() * sizeof(double));
+  else
+    std::memcpy(out, vf_.data(), vf_.size() * sizeof(double));
+}
+
+// ---------------------------------------------------------------------------
+// user vectors
+void MacGpu::set_rhs(const double *all, bool dev) {
+  CK(cudaMemcpyAsync(vec_[kRHS], all, (size_t)tt_.num_blocks * ncell_ * sizeof(double),
+                     dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream_));
+}
+void MacGpu::set_sol(const double *all, bool dev) {
+  CK(cudaMemcpyAsync(vec_[kSOL], all, (size_t)tt_.num_blocks * ncell_ * sizeof(double),
+                     dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream_));
+}
+void MacGpu::zero_sol() { CK(cudaMemsetAsync(vec_[kSOL], 0, (size_t)tt_.num_blocks * ncell_ * sizeof(double), stream_)); }
+void MacGpu::get_sol(double *all, bool dev) const {
+  cudaMemcpyAsync(all, vec_[kSOL], (size_t)tt_.num_blocks * ncell_ * sizeof(double),
+                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+}
+
+// ---------------------------------------------------------------------------
+// vector ops over block lists
+void MacGpu::vcopy(const BlockList &L, double *dst, const double *src) {
+  const long w = (long)L.n * ncell_;
+  if (w) k_copy<<<grid_for(w), kThreads, 0, stream_>>>(L, ncell_, dst, src);
+}
+void MacGpu::vzero(const BlockList &L, double *dst) {
+  const long w = (long)L.n * ncell_;
+  if (w) k_zero<<<grid_for(w), kThreads, 0, stream_>>>(L, ncell_, dst);
+}
+void MacGpu::vaxpby(const BlockList &L, double *out, double a, const double *x, double b, const double *y) {
+  const long w = (long)L.n * ncell_;
+  if (w) k_axpby<<<grid_for(w), kThreads, 0, stream_>>>(L, ncell_, out, a, x, b, y);
+}
+double MacGpu::vdot(const BlockList &L, const double *a, const double *b) {
+  const long w = (long)L.n * ncell_;
+  const int g = std::min<long>(kRedBlocks, std::max<long>(1, (w + kThreads - 1) / kThreads));
+  k_reduce<0><<<g, kThreads, 0, stream_>>>(L, ncell_, a, b, d_red_, d_counter_, d_red_ + kRedBlocks);
+  CKR(cudaMemcpyAsync(h_red_, d_red_ + kRedBlocks, sizeof(double), cudaMemcpyDeviceToHost, stream_), 0.0);
+  CKR(cudaStreamSynchronize(stream_), 0.0);
+  return h_red_[0];
+}
+double MacGpu::vnorm(const BlockList &L, const double *a) {
+  const long w = (long)L.n * ncell_;
+  const int g = std::min<long>(kRedBlocks, std::max<long>(1, (w + kThreads - 1) / kThreads));
+  k_reduce<1><<<g, kThreads, 0, stream_>>>(L, ncell_, a, a, d_red_, d_counter_, d_red_ + kRedBlocks);
+  CKR(cudaMemcpyAsync(h_red_, d_red_ + kRedBlocks, sizeof(double), cudaMemcpyDeviceToHost, stream_), 0.0);
+  CKR(cudaStreamSynchronize(stream_), 0.0);
+  return h_red_[0];
+}
+
+// ---------------------------------------------------------------------------
+// MG building blocks (FP64)
+void MacGpu::mg_apply(int L, double *out, const double *in, const double *rhs) {
+  if (towers_[L].all.n == 0) return;
+  launch_apply<double>(topo_, c64_, tower_list(L), in, out, rhs, nullptr, stream_);
+}
+
+// mg_smooth_level_usefill: fine -> coarse over the tower's levels, two
+// colours each (src/SayakaMacOperator.cpp:1028-1112)
+void MacGpu::mg_smooth(int L, double *phi, const double *rhs) {
+  if (towers_[L].all.n == 0) return;
+  for (int l = L; l >= 1; l--) {
+    BlockList sl = sublevel_list(L, l);
+    if (sl.n == 0) break;
+    for (int rb = 0; rb < 2; rb++) launch_smooth<double>(topo_, c64_, sl, rb, phi, rhs, nullptr, stream_);
+  }
+}
+
+void MacGpu::mg_restrict(int lc, double *phi) {
+  if (lc >= tt_.max_level) return;
+  if (levels_[lc].n == 0 || levels_[lc + 1].n == 0) return;
+  launch_restrict<double>(topo_, c64_, nonleaf_list(lc), phi, nullptr, stream_);
+}
+
+void MacGpu::mg_prolong(int lf, double *phi) {
+  if (lf <= 1 || levels_[lf].n == 0) return;
+  launch_prolong<double>(topo_, c64_, level_list(lf), phi, nullptr, stream_);
+}
+
+// one V-cycle with zero initial guess: sol = M^-1 rhs on tower L
+// (src/SayakaMacSolver.cpp:924-949 -> :245-374 with fixed_iter = 1)
+void MacGpu::precond(int L, double *sol, const double *rhs) {
+  BlockList TL = tower_list(L);
+  // SOL = 0; RESID = rhs - L(0) = rhs on fluid cells
+  k_masked_copy<<<grid_for((long)TL.n * ncell_), kThreads, 0, stream_>>>(TL, ncell_, d_vf_, vec_[kRESID], rhs);
+  vzero(TL, vec_[kCORR]);
+  for (int l = L; l >= 2; l--) mg_restrict(l - 1, vec_[kRESID]);
+  const int rb = bottom_solve();
+  if (rb != 0) {
+    // bottom breakdown: the reference skips the up-sweep and returns SOL = 0
+    vzero(TL, sol);
+    return;
+  }
+  for (int l = 2; l <= L; l++) {
+    mg_prolong(l, vec_[kCORR]);
+    for (int s = 0; s < prm_.n_post; s++) mg_smooth(l, vec_[kCORR], vec_[kRESID]);
+  }
+  // SOL(=0) += CORR ; sol = SOL
+  vaxpby(TL, sol, 1.0, vec_[kCORR], 0.0, vec_[kCORR]);
+}
+
+// mg_solve_bottom (src/SayakaMacSolver.cpp:164-242): CORR on tower(1) from
+// RESID, unpreconditioned BiCGSTAB in its own buffers
+int MacGpu::bottom_solve() {
+  BlockList T1 = tower_list(1);
+  vzero(T1, vec_[kCORR]);
+  SolveInfo info;
+  const int stat = bicgstab(1, vec_[kCORR], vec_[kRESID], prm_.bot_tol_rel, prm_.bot_tol_abs, prm_.bot_max_iter,
+                            false, true, &info);
+  return stat;
+}
+
+// BiCGSTAB of cg_solve_level (src/SayakaMacSolver.cpp:683-920)
+int MacGpu::bicgstab(int L, double *sol, const double *rhs, double tol_rel, double tol_abs, int max_iter,
+                     bool use_precond, bool bottom, SolveInfo *info) {
+  BlockList TL = tower_list(L);
+  double *X0 = vec_[bottom ? kBX0 : kX0], *X = vec_[bottom ? kBX : kX], *R = vec_[bottom ? kBR : kR];
+  double *RHAT = vec_[bottom ? kBRHAT : kRHAT], *P = vec_[bottom ? kBP : kP];
+  double *S = vec_[bottom ? kBS : kS], *V = vec_[bottom ? kBV : kV], *Tt = vec_[bottom ? kBT : kT];
+  double *PHAT = bottom ? P : vec_[kPHAT], *SHAT = bottom ? S : vec_[kSHAT];
+  if (L == 1) use_precond = false;
+
+  vcopy(TL, X0, sol);
+  mg_apply(L, R, X0, rhs);  // R = rhs - A x0 (masked)
+  vcopy(TL, RHAT, R);
+  vzero(TL, X);
+  const double rnorm0 = vnorm(TL, R);
+  info->rnorm0 = rnorm0;
+  info->rnorm = rnorm0;
+  info->iterations = 0;
+  if (!err_.empty()) return -1;
+  if (rnorm0 == 0) return 0;
+
+  double rho1 = 0, alpha = 0, omega = 0;
+  bool conv = false;
+  int stat = 0, iter;
+  for (iter = 1; iter <= max_iter; iter++) {
+    const double rho = vdot(TL, RHAT, R);
+    if (rho == 0) {
+      stat = 1;
+      break;
+    }
+    if (iter == 1) {
+      vcopy(TL, P, R);
+    } else {
+      const double beta = (rho / rho1) * (alpha / omega);
+      vaxpby(TL, P, 1.0, P, -omega, V);
+      vaxpby(TL, P, 1.0, R, beta, P);
+    }
+    if (use_precond) precond(L, PHAT, P);
+    mg_apply(L, V, use_precond ? PHAT : P, nullptr);
+    alpha = vdot(TL, RHAT, V);
+    if (alpha == 0) {
+      stat = 1;
+      break;
+    }
+    alpha = rho / alpha;
+    vaxpby(TL, S, 1.0, R, -alpha, V);
+    vaxpby(TL, X, 1.0, X, alpha, use_precond ? PHAT : P);
+    double rnorm = vnorm(TL, S);
+    info->rnorm = rnorm;
+    if (rnorm < rnorm0 * tol_rel || rnorm < tol_abs) {
+      conv = true;
+      break;
+    }
+    if (use_precond) precond(L, SHAT, S);
+    mg_apply(L, Tt, use_precond ? SHAT : S, nullptr);
+    const double tds = vdot(TL, Tt, S);
+    const double tdt = vdot(TL, Tt, Tt);
+    if (tdt == 0) {
+      stat = 1;
+      break;
+    }
+    omega = tds / tdt;
+    vaxpby(TL, X, 1.0, X, omega, use_precond ? SHAT : S);
+    vaxpby(TL, R, 1.0, S, -omega, Tt);
+    rnorm = vnorm(TL, R);
+    info->rnorm = rnorm;
+    if (prm_.verbose && !bottom) fprintf(stderr, "bicgstab iter=%d |r|=%.6e\n", iter, rnorm);
+    if (rnorm < rnorm0 * tol_rel + tol_abs) {
+      conv = true;
+      break;
+    }
+    if (omega == 0) {
+      stat = 1;
+      break;
+    }
+    rho1 = rho;
+    if (!err_.empty()) return -1;
+  }
+  info->iterations = std::min(iter, max_iter);
+  if (conv) {
+    vaxpby(TL, X0, 1.0, X0, 1.0, X);
+    vcopy(TL, sol, X0);
+  }
+  info->status = stat ? 1 : (conv ? 0 : 2);
+  return stat;
+}
+
+int MacGpu::cg_solve(SolveInfo *info) {
+  auto t0 = std::chrono::steady_clock::now();
+  const int stat = bicgstab(finest_, vec_[kSOL], vec_[kRHS], prm_.tol_rel, prm_.tol_abs, prm_.max_iter,
+                            prm_.use_mg_precond != 0, false, info);
+  cudaStreamSynchronize(stream_);
+  info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (!err_.empty()) return -1;
+  return stat;
+}
+
+// ---------------------------------------------------------------------------
+// parity hooks (compact all-block arrays on the host)
+void MacGpu::apply(int L, const double *x, double *y) {
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  CK(cudaMemcpyAsync(vec_[kP], x, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemsetAsync(vec_[kV], 0, n * sizeof(double), stream_));
+  mg_apply(L, vec_[kV], vec_[kP], nullptr);
+  CK(cudaMemcpyAsync(y, vec_[kV], n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+}
+void MacGpu::residual(int L, const double *x, const double *rhs, double *r) {
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  CK(cudaMemcpyAsync(vec_[kP], x, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemcpyAsync(vec_[kS], rhs, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemsetAsync(vec_[kT], 0, n * sizeof(double), stream_));
+  mg_apply(L, vec_[kT], vec_[kP], vec_[kS]);
+  CK(cudaMemcpyAsync(r, vec_[kT], n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+}
+void MacGpu::smooth(int L, const double *phi, const double *rhs, double *out) {
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  CK(cudaMemcpyAsync(vec_[kCORR], phi, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemcpyAsync(vec_[kRESID], rhs, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  mg_smooth(L, vec_[kCORR], vec_[kRESID]);
+  CK(cudaMemcpyAsync(out, vec_[kCORR], n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+}
+void MacGpu::restrict_sweep(const double *in, double *out) {
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  CK(cudaMemcpyAsync(vec_[kRESID], in, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  for (int l = finest_; l >= 2; l--) mg_restrict(l - 1, vec_[kRESID]);
+  CK(cudaMemcpyAsync(out, vec_[kRESID], n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+}
+void MacGpu::prolong_sweep(const double *in, double *out) {
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  CK(cudaMemcpyAsync(vec_[kCORR], in, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  for (int l = 2; l <= finest_; l++) mg_prolong(l, vec_[kCORR]);
+  CK(cudaMemcpyAsync(out, vec_[kCORR], n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+}
+void MacGpu::vcycle(const double *p, double *phat) {
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  for (int v = 0; v < kNumVec; v++) CK(cudaMemsetAsync(vec_[v], 0, n * sizeof(double), stream_));
+  CK(cudaMemcpyAsync(vec_[kP], p, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  precond(finest_, vec_[kPHAT], vec_[kP]);
+  CK(cudaMemcpyAsync(phat, vec_[kPHAT], n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+}
+void MacGpu::flux(int dir, const double *phi, double *out) {
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  const size_t nf = (size_t)tt_.num_blocks * nfb_;
+  CK(cudaMemcpyAsync(vec_[kP], phi, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  double *fl = nullptr;
+  CK(cudaMalloc(&fl, nf * sizeof(double)));
+  CK(cudaMemsetAsync(fl, 0, nf * sizeof(double), stream_));
+  launch_flux(topo_, c64_, tower_list(finest_), dir, vec_[kP], fl, stream_);
+  CK(cudaMemcpyAsync(out, fl, nf * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  cudaFree(fl);
+}
+void MacGpu::fix_bc(const double *phig, int ng, double *rhs) {
+  const int nd = tt_.ndim, G = tt_.nb + 2 * ng;
+  const size_t gsz = (size_t)tt_.num_blocks * (nd == 3 ? (size_t)G * G * G : (size_t)G * G);
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  double *dg = nullptr;
+  CK(cudaMalloc(&dg, gsz * sizeof(double)));
+  CK(cudaMemcpyAsync(dg, phig, gsz * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemcpyAsync(vec_[kTMP], rhs, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  launch_fix_bc(topo_, c64_, tower_list(finest_), dg, ng, vec_[kTMP], stream_);
+  CK(cudaMemcpyAsync(rhs, vec_[kTMP], n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  cudaFree(dg);
+}
+
+}  // namespace sayaka_gb300

@@ -1,0 +1,170 @@
+// GPU MAC solver: owns the device block pools and runs the reference's
+// MG-preconditioned BiCGSTAB (src/SayakaMacSolver.cpp:683-949) with the
+// kernels of mac_kernels.cu.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "mac_device.h"
+
+namespace sayaka_gb300 {
+
+// the tree as plain tables (what the C ABI receives)
+struct TreeTables {
+  int ndim = 2, nb = 8, num_blocks = 0, min_level = 1, max_level = 1;
+  std::vector<int> level, neighbor, child, parent, which_child, node_type;  // 1, 6, 8, 1, 1, 1 per block
+  std::vector<double> block_len;                                            // 3 per block
+};
+
+struct SolverParams {
+  int max_iter = 2000;      // outer BiCGSTAB (src/SayakaMacSolver.h:72)
+  double tol_rel = 1e-6;    // (src/SayakaMacSolver.h:73)
+  double tol_abs = 0.0;     // (src/SayakaMacSolver.h:74)
+  int n_post = 2;           // post-smoothing sweeps (src/SayakaMacSolver.h:77)
+  double bot_tol_rel = 1e-6, bot_tol_abs = 1e-6;  // (src/SayakaMacSolver.h:78-79)
+  int bot_max_iter = 2000;                        // (src/SayakaMacSolver.h:80)
+  int use_mg_precond = 0;   // setCGUseMGPrecond (src/SayakaMacSolver.h:358)
+  int precision = 0;        // 0: FP64 V-cycle, 1: FP32 V-cycle (FP64 outer + bottom)
+  int bottom = 0;           // 0: BiCGSTAB (reference), 1: dense direct solve
+  int verbose = 0;
+};
+
+struct SolveInfo {
+  int status = 0;        // 0 ok, 1 breakdown, 2 not converged
+  int iterations = 0;
+  double rnorm0 = 0, rnorm = 0;
+  double seconds = 0;
+};
+
+class MacGpu {
+ public:
+  explicit MacGpu(const TreeTables &tt);
+  ~MacGpu();
+  MacGpu(const MacGpu &) = delete;
+  MacGpu &operator=(const MacGpu &) = delete;
+
+  const std::string &error() const { return err_; }
+  int ndim() const { return tt_.ndim; }
+  int nb() const { return tt_.nb; }
+  int ncell() const { return ncell_; }
+  int nfb() const { return nfb_; }
+  int num_blocks() const { return tt_.num_blocks; }
+  int finest() const { return finest_; }
+  const std::vector<int> &tower_blocks(int L) const { return towers_[L].blocks; }
+
+  // coefficients and fractions (all blocks, compact layouts).  Setters taking
+  // leaf values perform the reference's c/f AVG sync and AVG restriction.
+  void set_scalars(double alpha, double beta);
+  void set_coef_b_leaf(int dir, const double *face_all);       // src/SayakaMacCoef.cpp:36-76
+  void set_ib_frac_leaf(const double *vol_all, const double *const area_all[3]);  // src/SayakaMacIB.cpp:34-97
+  void set_ib_frac_by_ls(const double *ls_grown, int ngrow);   // binary fractions from a level set
+  void set_bc_types(const int *bc6);                            // math BC per block face (-1 interior)
+  void get_coef(int which, int dir, double *out_all) const;     // 0 B, 1 area frac, 2 vol frac
+
+  // user vectors (compact, all blocks)
+  void set_rhs(const double *all, bool on_device = false);
+  void set_sol(const double *all, bool on_device = false);
+  void zero_sol();
+  void get_sol(double *all, bool on_device = false) const;
+  double *rhs_dev() { return vec_[kRHS]; }
+  double *sol_dev() { return vec_[kSOL]; }
+
+  void set_params(const SolverParams &p) { prm_ = p; }
+  const SolverParams &params() const { return prm_; }
+
+  int cg_solve(SolveInfo *info);
+
+  // building blocks, exposed for parity tests (compact arrays, all blocks)
+  void apply(int L, const double *x_all, double *y_all);
+  void residual(int L, const double *x_all, const double *rhs_all, double *r_all);
+  void smooth(int L, const double *phi_all, const double *rhs_all, double *out_all);
+  void restrict_sweep(const double *in_all, double *out_all);
+  void prolong_sweep(const double *in_all, double *out_all);
+  void vcycle(const double *p_all, double *phat_all);
+  void flux(int dir, const double *phi_all, double *flux_all);
+  void fix_bc(const double *phi_grown, int ngrow, double *rhs_all);
+
+  cudaStream_t stream() const { return stream_; }
+
+ private:
+  enum Vec {
+    kRHS, kSOL, kRESID, kCORR, kTMP,
+    kX0, kX, kR, kRHAT, kP, kPHAT, kS, kSHAT, kV, kT,
+    kBX0, kBX, kBR, kBRHAT, kBP, kBS, kBV, kBT,
+    kNumVec
+  };
+  struct DevList {
+    int *blocks = nullptr;
+    uint16_t *ftypes = nullptr;
+    int n = 0;
+  };
+  struct DevTower {
+    DevList all;
+    std::vector<int> begin, end;
+    std::vector<int> blocks;
+  };
+
+  BlockList tower_list(int L) const;
+  BlockList sublevel_list(int L, int l) const;
+  BlockList level_list(int l) const;
+  BlockList nonleaf_list(int l) const;
+
+  void upload_coefs();
+  void recompute_face_coef();
+  void sync_face_avg_host(int dir, std::vector<double> &face) const;
+  void restrict_face_avg_host(int dir, std::vector<double> &face) const;
+  void restrict_cell_avg_host(std::vector<double> &cell) const;
+
+  // vector ops over a block list (FP64)
+  void vcopy(const BlockList &L, double *dst, const double *src);
+  void vzero(const BlockList &L, double *dst);
+  void vaxpby(const BlockList &L, double *out, double a, const double *x, double b, const double *y);
+  double vdot(const BlockList &L, const double *a, const double *b);
+  double vnorm(const BlockList &L, const double *a);
+
+  void mg_apply(int L, double *out, const double *in, const double *rhs_for_residual);
+  void mg_smooth(int L, double *phi, const double *rhs);
+  void mg_restrict(int lc, double *phi);
+  void mg_prolong(int lf, double *phi);
+  void precond(int L, double *sol, const double *rhs);
+  int bottom_solve();
+  int bicgstab(int L, double *sol, const double *rhs, double tol_rel, double tol_abs, int max_iter, bool use_precond,
+               bool bottom, SolveInfo *info);
+
+  void fail(const std::string &m);
+
+  TreeTables tt_;
+  SolverParams prm_;
+  std::string err_;
+  int ncell_ = 0, nfb_ = 0, finest_ = 0;
+  cudaStream_t stream_ = nullptr;
+
+  // host mirrors
+  std::vector<double> geom_;           // [nblocks*8]
+  std::vector<double> bcoef_[3], afrac_[3], vf_;
+  std::vector<int> bc_type_;           // [nblocks*6]
+  std::vector<int> fc_neigh_;          // [nblocks*6]
+  double alpha_ = 0.0, beta_ = 1.0;
+
+  // device tables
+  int *d_neighbor_ = nullptr, *d_child_ = nullptr, *d_parent_ = nullptr, *d_wc_ = nullptr;
+  int *d_fc_neigh_ = nullptr, *d_bc_type_ = nullptr;
+  double *d_geom_ = nullptr;
+  double *d_bcoef_[3] = {nullptr, nullptr, nullptr}, *d_afrac_[3] = {nullptr, nullptr, nullptr};
+  double *d_tff_[3] = {nullptr, nullptr, nullptr}, *d_vf_ = nullptr;
+  double *vec_[kNumVec] = {};
+  double *d_red_ = nullptr;        // reduction partials
+  unsigned *d_counter_ = nullptr;  // last-block counter
+  double *h_red_ = nullptr;        // pinned scalar readback
+
+  std::vector<DevTower> towers_;
+  std::vector<DevList> levels_, nonleaf_;
+  std::vector<std::vector<int>> level_blocks_, nonleaf_blocks_;
+
+  Topo topo_{};
+  Coef<double> c64_{};
+};
+
+}  // namespace sayaka_gb300
