@@ -348,7 +348,7 @@ class MacSolver:
     def apply(self, L, x):
         y = self._cells()
         a, p = _f64(x)
-        _check(self.lib.sayaka_mac_apply_compact(self.h, L, p, y.ctypes.data_as(_f64p)), "apply", self.h)
+        _check(self.lib.sayaka_mac_apply_compact(self.h, int(L), p, y.ctypes.data_as(_f64p)), "apply", self.h)
         return y
 
     def residual(self, L, x, rhs):

@@ -1,0 +1,257 @@
+"""Seeded synthetic MAC-Poisson problems with the shapes of the benchmark
+configurations (there is no public data set; the reference's own drivers use
+analytic geometry the same way, src/Test6.h:1045-1101).
+
+Every problem is built through this package's tree mirror and returned as
+compact all-block arrays:
+    tables (dict)      tree tables (AmrTree.tables())
+    bc     [n*6]       math BC per block face
+    vol    [n*ncell]   IB volume fraction (leaf values)
+    area   [ndim][n*nfb] IB area fractions (leaf values)
+    bface  [ndim][n*nfb] face coefficient B = 1/rho (leaf values)
+    rhs    [n*ncell]   right-hand side (leaf cells; the reference solves
+                       -div(B grad p) = rhs, so rhs = -f)
+"""
+import math
+
+import numpy as np
+
+from . import AmrTree, NEUMANN
+
+
+class Problem:
+    def __init__(self, name, tree, tables, bc, vol, area, bface, rhs, params):
+        self.name, self.tree, self.tables = name, tree, tables
+        self.bc, self.vol, self.area, self.bface, self.rhs = bc, vol, area, bface, rhs
+        self.params = params
+        nd, nb = tables["ndim"], tables["nb"]
+        self.ndim, self.nb, self.num_blocks = nd, nb, tables["num_blocks"]
+        self.ncell = nb ** nd
+        self.nfb = (nb + 1) * nb ** (nd - 1)
+        self.leaf = np.nonzero(tables["node_type"] == 1)[0]
+        self.leaf_cells = len(self.leaf) * self.ncell
+
+    def describe(self):
+        lv = self.tables["level"]
+        return dict(blocks=int(self.num_blocks), leaf_blocks=int(len(self.leaf)), leaf_cells=int(self.leaf_cells),
+                    levels=int(lv.max()), nb=int(self.nb), ndim=int(self.ndim))
+
+
+def _block_geom(tb):
+    n, nd, nb = tb["num_blocks"], tb["ndim"], tb["nb"]
+    lo = tb["block_lo"].reshape(n, 3)[:, :nd]
+    dx = tb["block_len"].reshape(n, 3)[:, :nd] / nb
+    return lo, dx
+
+
+def cell_centres(tb):
+    """[n, nb^nd, nd] cell-centre coordinates ([k][j][i] cell order)."""
+    n, nd, nb = tb["num_blocks"], tb["ndim"], tb["nb"]
+    lo, dx = _block_geom(tb)
+    g = np.meshgrid(*[np.arange(nb)] * nd, indexing="ij")[::-1]  # i, j, (k)
+    idx = np.stack([a.reshape(-1) for a in g], axis=1)  # [ncell, nd]
+    return lo[:, None, :] + (idx[None, :, :] + 0.5) * dx[:, None, :]
+
+
+def face_centres(tb, fd):
+    n, nd, nb = tb["num_blocks"], tb["ndim"], tb["nb"]
+    lo, dx = _block_geom(tb)
+    ext = [nb + (d == fd) for d in range(nd)]
+    g = np.meshgrid(*[np.arange(e) for e in ext[::-1]], indexing="ij")[::-1]
+    idx = np.stack([a.reshape(-1) for a in g], axis=1).astype(np.float64) + 0.5
+    idx[:, fd] -= 0.5
+    return lo[:, None, :] + idx[None, :, :] * dx[:, None, :]
+
+
+def refine_tree(ndim, nb, nroot, lo, hi, min_level, max_level, need_refine, bc_code=(-20,) * 6, capacity=200000):
+    """Root grid + static refinement to min_level + level-by-level refinement
+    of the leaf blocks for which need_refine(block_lo, block_hi, level) is true."""
+    t = AmrTree(ndim, nb, min_level, max_level, capacity)
+    t.init_uniform_root(nroot, lo, hi, bc_code, (0,) * 6)
+    t.init_refine_to_min_level()
+    for level in range(1, max_level):
+        tb = t.tables()
+        n = tb["num_blocks"]
+        blo = tb["block_lo"].reshape(n, 3)[:, :ndim]
+        bhi = tb["block_hi"].reshape(n, 3)[:, :ndim]
+        sel = (tb["level"] == level) & (tb["node_type"] == 1)
+        flags = np.zeros(n, dtype=np.int32)
+        idx = np.nonzero(sel)[0]
+        if len(idx):
+            flags[idx] = need_refine(blo[idx], bhi[idx], level).astype(np.int32)
+        if not flags.any():
+            continue
+        t.set_refine_flags(flags)
+        t.regrid()
+    return t
+
+
+def _straddle(sdf, blo, bhi, pad):
+    """sdf changes sign (with a margin of `pad` block widths) over the block"""
+    nd = blo.shape[1]
+    corners = []
+    for c in range(1 << nd):
+        pts = np.where([(c >> d) & 1 for d in range(nd)], bhi, blo)
+        corners.append(sdf(pts))
+    corners = np.stack(corners, axis=1)
+    h = np.max(bhi - blo, axis=1) * pad
+    centre = sdf(0.5 * (blo + bhi))
+    return (corners.min(axis=1) < h) & (corners.max(axis=1) > -h) | (np.abs(centre) < h)
+
+
+def _smooth_heaviside(phi, w):
+    return np.clip(0.5 - phi / w, 0.0, 1.0)
+
+
+def gaussian_rhs(rng, pts, ndim, n_g=8, sigma=0.05):
+    amp = rng.standard_normal(n_g)
+    cen = rng.uniform(0.1, 0.9, size=(n_g, ndim))
+    f = np.zeros(pts.shape[:-1])
+    for g in range(n_g):
+        r2 = np.sum((pts - cen[g]) ** 2, axis=-1)
+        f += amp[g] * np.exp(-r2 / (2 * sigma * sigma))
+    return f
+
+
+def _finish(name, t, tb, vol, area, bface, f, neumann, params):
+    n, nd = tb["num_blocks"], tb["ndim"]
+    ncell = tb["nb"] ** nd
+    leaf = tb["node_type"] == 1
+    lens = tb["block_len"].reshape(n, 3)[:, :nd] / tb["nb"]
+    dv = np.prod(lens, axis=1)
+    vol2 = vol.reshape(n, ncell)
+    f = f.reshape(n, ncell) * leaf[:, None]
+    if neumann:
+        w = (dv[:, None] * vol2) * leaf[:, None]
+        m = np.sum(f * w) / np.sum(w)
+        f = np.where(leaf[:, None], f - m, 0.0)
+    bc = np.full((n, 6), -1, dtype=np.int32)
+    nbr = tb["neighbor"].reshape(n, 6)
+    for fc in range(2 * nd):
+        bc[nbr[:, fc] <= -20, fc] = NEUMANN
+    return Problem(name, t, tb, bc.reshape(-1), vol.reshape(-1), [a.reshape(-1) for a in area],
+                   [b.reshape(-1) for b in bface], (-f).reshape(-1), params)
+
+
+def config1(seed=20251):
+    """2D unit square, 4x4 roots of 8x8, levels 1..4 refined around the circle
+    r=0.25 at the centre; beta=1, Neumann walls, 8 Gaussians, tol 1e-10."""
+    def sdf(p):
+        return np.sqrt(np.sum((p - 0.5) ** 2, axis=-1)) - 0.25
+
+    t = refine_tree(2, 8, (4, 4, 1), (0, 0, 0), (1, 1, 0), 1, 4,
+                    lambda lo, hi, l: _corner_straddle(sdf, lo, hi))
+    tb = t.tables()
+    n, ncell, nfb = tb["num_blocks"], 64, 72
+    rng = np.random.default_rng(seed)
+    f = gaussian_rhs(rng, cell_centres(tb), 2)
+    ones_c = np.ones(n * ncell)
+    ones_f = [np.ones(n * nfb) for _ in range(2)]
+    return _finish("config1", t, tb, ones_c, ones_f, [np.ones(n * nfb) for _ in range(2)], f, True,
+                   dict(tol_rel=1e-10))
+
+
+def _corner_straddle(sdf, blo, bhi):
+    nd = blo.shape[1]
+    nin = np.zeros(len(blo), dtype=int)
+    for c in range(1 << nd):
+        pts = np.where([(c >> d) & 1 for d in range(nd)], bhi, blo)
+        nin += sdf(pts) < 0
+    return (nin > 0) & (nin < (1 << nd))
+
+
+def config2(seed=2, nb=16, max_level=6, roots=2):
+    """2D, 16x16 blocks, 6 levels (~1.5k leaf blocks); two-phase B = 1/rho with
+    rho 1 | 1000 across a seeded ellipse smoothed over 2 cells; solid disk IB
+    with fractional volume/area fractions from its signed distance; Neumann
+    walls; seeded zero-mean 8-Gaussian right-hand side."""
+    rng = np.random.default_rng(seed)
+    ec = rng.uniform(0.35, 0.65, 2)
+    ea, eb = rng.uniform(0.24, 0.30), rng.uniform(0.14, 0.18)
+    th = rng.uniform(0, math.pi)
+    dc = rng.uniform(0.25, 0.75, 2)
+    dr = rng.uniform(0.06, 0.09)
+    ct, st = math.cos(th), math.sin(th)
+
+    def ellipse(p):
+        x = p[..., 0] - ec[0]
+        y = p[..., 1] - ec[1]
+        u = (x * ct + y * st) / ea
+        v = (-x * st + y * ct) / eb
+        # approximate signed distance (scaled by the minor axis)
+        return (np.sqrt(u * u + v * v) - 1.0) * min(ea, eb)
+
+    def disk(p):
+        return np.sqrt(np.sum((p - dc) ** 2, axis=-1)) - dr
+
+    def need(lo, hi, level):
+        return _straddle(ellipse, lo, hi, 1.5) | _straddle(disk, lo, hi, 1.5)
+
+    t = refine_tree(2, nb, (roots, roots, 1), (0, 0, 0), (1, 1, 0), 2, max_level, need)
+    tb = t.tables()
+    n = tb["num_blocks"]
+    lo, dx = _block_geom(tb)
+    pc = cell_centres(tb)
+    h = dx[:, 0][:, None]
+    vol = np.clip(disk(pc) / h + 0.5, 0.0, 1.0)
+    area, bface = [], []
+    for fd in range(2):
+        pf = face_centres(tb, fd)
+        area.append(np.clip(disk(pf) / h + 0.5, 0.0, 1.0))
+        rho = 1.0 + 999.0 * _smooth_heaviside(ellipse(pf), 2.0 * h)
+        bface.append(1.0 / rho)
+    f = gaussian_rhs(rng, pc, 2)
+    return _finish("config2", t, tb, vol, area, bface, f, True, dict(tol_rel=1e-8))
+
+
+def config3(seed=3, nb=16, max_level=5):
+    """3D, 16^3 blocks, 5 levels refined on the sphere r=0.2 (IB solid inside
+    a smaller seeded sphere, binary mask), B ratio 100 across a seeded blob."""
+    rng = np.random.default_rng(seed)
+    bc_ = rng.uniform(0.35, 0.65, 3)
+    br = rng.uniform(0.12, 0.18)
+    sc = np.array([0.5, 0.5, 0.5])
+
+    def sphere(p):
+        return np.sqrt(np.sum((p - sc) ** 2, axis=-1)) - 0.2
+
+    def blob(p):
+        r = np.sqrt(np.sum((p - bc_) ** 2, axis=-1))
+        return r - br
+
+    def need(lo, hi, level):
+        return _straddle(sphere, lo, hi, 0.2)
+
+    t = refine_tree(3, nb, (1, 1, 1), (0, 0, 0), (1, 1, 1), 2, max_level, need)
+    tb = t.tables()
+    lo, dx = _block_geom(tb)
+    pc = cell_centres(tb)
+    h = dx[:, 0][:, None]
+    solid = lambda p: np.sqrt(np.sum((p - sc) ** 2, axis=-1)) - 0.08  # noqa: E731
+    vol = (solid(pc) > 0).astype(np.float64)
+    area, bface = [], []
+    for fd in range(3):
+        pf = face_centres(tb, fd)
+        area.append((solid(pf) > 0).astype(np.float64))
+        rho = 1.0 + 99.0 * _smooth_heaviside(blob(pf), 2.0 * h)
+        bface.append(1.0 / rho)
+    f = gaussian_rhs(rng, pc, 3, sigma=0.08)
+    return _finish("config3", t, tb, vol, area, bface, f, True, dict(tol_rel=1e-8))
+
+
+CONFIGS = {"config1": config1, "config2": config2, "config3": config3}
+
+
+def make_solver(prob, **params):
+    """A MacSolver set up with the problem's BCs, fractions, B and RHS."""
+    from . import MacSolver
+    S = MacSolver(prob.tables)
+    S.set_bc(prob.bc)
+    S.set_ib_frac_compact(prob.vol, prob.area)
+    for d in range(prob.ndim):
+        S.set_coef_b(d, prob.bface[d])
+    S.set_rhs_compact(prob.rhs)
+    S.set_zero_sol()
+    if params:
+        S.set_params(**params)
+    return S

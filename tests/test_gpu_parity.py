@@ -1,0 +1,272 @@
+"""GPU kernels and solver against the reference library's own results
+(golden fixtures from oracle/ref_dump.cpp).
+
+FP64 stencil, smoother, transfer, flux and BC kernels must be bit-identical to
+the reference (same operation order, no FMA contraction).  The V-cycle holds
+BiCGSTAB whose 1e-6 stopping test makes it agree with the reference to that
+level (and with the bit-pinned C oracle to 1e-10 once the bottom converges);
+the full solve is compared to 1e-8 relative L2 over fluid leaf cells, after removing the
+volume-weighted mean when the problem is all-Neumann."""
+import numpy as np
+import pytest
+
+import golden_io
+import sayakaamr_gb300 as sg
+from cases import CASES, all_neumann, bc_table, build_tree
+
+pytestmark = pytest.mark.gpu
+
+OPS = [n for n in sorted(CASES) if CASES[n]["do_ops"]]
+
+
+def _frac(c, pts, h):
+    nd = len(pts)
+    d2 = np.zeros_like(pts[0])
+    for d in range(nd):
+        d2 = d2 + (pts[d] - c["ibc"][d]) * (pts[d] - c["ibc"][d])
+    s = (np.sqrt(d2) - c["ibr"]) / h + 0.5
+    s = np.clip(s, 0.0, 1.0)
+    return np.floor(s * 64.0) / 64.0
+
+
+def fractional_ib(name, tb):
+    """leaf IB fractions exactly as ProbeSolver::injectIBFrac computes them"""
+    c = CASES[name]
+    nd, nb, n = tb["ndim"], tb["nb"], tb["num_blocks"]
+    lo = tb["block_lo"].reshape(n, 3)
+    dx = tb["block_len"].reshape(n, 3).copy()
+    dx[:, :nd] = dx[:, :nd] / nb
+    vol = np.zeros((n,) + (nb,) * nd)
+    areas = []
+    # cell centres, [k][j][i] order
+    grids = np.meshgrid(*[np.arange(nb)] * nd, indexing="ij")[::-1]  # i, j, (k)
+    for b in range(n):
+        pts = [lo[b, d] + (grids[d] + 0.5) * dx[b, d] for d in range(nd)]
+        vol[b] = _frac(c, pts, dx[b, 0])
+    for fd in range(nd):
+        ext = [nb + (d == fd) for d in range(nd)]
+        g = np.meshgrid(*[np.arange(e) for e in ext[::-1]], indexing="ij")[::-1]
+        a = np.zeros((n,) + tuple(ext[::-1]))
+        for b in range(n):
+            pts = []
+            for d in range(nd):
+                x = lo[b, d] + (g[d] + 0.5) * dx[b, d]
+                if d == fd:
+                    x = x - 0.5 * dx[b, d]
+                pts.append(x)
+            a[b] = _frac(c, pts, dx[b, 0])
+        areas.append(a.reshape(-1))
+    return vol.reshape(-1), areas
+
+
+def setup_solver(name):
+    g = golden_io.load(name)
+    t = build_tree(name)
+    tb = t.tables()
+    S = sg.MacSolver(tb)
+    S.set_bc(bc_table(name, tb))
+    c = CASES[name]
+    if c["ibr"] > 0:
+        if c["ib_binary"]:
+            S.set_ib_frac_by_ls(g["in_ls_grown"], ncomp=1, ngrow=1, comp=0)
+        else:
+            vol, areas = fractional_ib(name, tb)
+            S.set_ib_frac_compact(vol, areas)
+    if c["bamp"] != 0:
+        for d in range(tb["ndim"]):
+            S.set_coef_b(d, g["in_b%d" % d], ncomp=1, ngrow=0, comp=0)
+    return g, t, tb, S
+
+
+@pytest.fixture(scope="module", params=OPS)
+def prob(request):
+    return (request.param,) + setup_solver(request.param)
+
+
+def block_slice(arr, blocks, per):
+    a = arr.reshape(-1, per)
+    return a[np.asarray(blocks)].reshape(-1)
+
+
+def same_bits(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    # -0.0 == +0.0 is accepted; everything else must match exactly
+    return a.shape == b.shape and bool(np.all((a == b) | (np.isnan(a) & np.isnan(b))))
+
+
+def test_coefficients(prob):
+    name, g, t, tb, S = prob
+    c = CASES[name]
+    if c["ibr"] > 0:
+        assert same_bits(S.get_coef(2), g["vf"]), name
+        for d in range(tb["ndim"]):
+            assert same_bits(S.get_coef(1, d), g["af%d" % d]), (name, d)
+    if c["bamp"] != 0:
+        for d in range(tb["ndim"]):
+            assert same_bits(S.get_coef(0, d), g["bcoef%d" % d]), (name, d)
+
+
+def test_apply_every_tower(prob):
+    name, g, t, tb, S = prob
+    n, nc = tb["num_blocks"], S.ncell
+    x = golden_io.seeded_input(name, "op_x", n * nc)
+    for L in range(1, tb["level"].max() + 1):
+        key = "op_apply_%d" % L
+        if key not in g:
+            continue
+        y = S.apply(L, x)
+        blocks, _ = t.tower(L)
+        assert same_bits(block_slice(y, blocks, nc), g[key]), (name, L)
+
+
+def test_residual(prob):
+    name, g, t, tb, S = prob
+    n, nc = tb["num_blocks"], S.ncell
+    x = golden_io.seeded_input(name, "op_x", n * nc)
+    rhs = golden_io.seeded_input(name, "op_rhs", n * nc)
+    finest = tb["level"].max()
+    r = S.residual(finest, x, rhs)
+    blocks, _ = t.tower(finest)
+    assert same_bits(block_slice(r, blocks, nc), g["op_resid"]), name
+
+
+def test_smoother_every_tower(prob):
+    name, g, t, tb, S = prob
+    n, nc = tb["num_blocks"], S.ncell
+    corr = golden_io.seeded_input(name, "sm_corr0", n * nc)
+    res = golden_io.seeded_input(name, "sm_resid", n * nc)
+    for L in range(1, tb["level"].max() + 1):
+        key = "sm_out_%d" % L
+        if key not in g:
+            continue
+        out = S.smooth(L, corr, res)
+        blocks, _ = t.tower(L)
+        assert same_bits(block_slice(out, blocks, nc), g[key]), (name, L)
+
+
+def test_restrict_and_prolong_sweeps(prob):
+    name, g, t, tb, S = prob
+    n, nc = tb["num_blocks"], S.ncell
+    rs = S.restrict_sweep(golden_io.seeded_input(name, "rs_in", n * nc))
+    assert same_bits(rs, g["rs_out"]), name
+    pr = S.prolong_sweep(golden_io.seeded_input(name, "pr_in", n * nc))
+    assert same_bits(pr, g["pr_out"]), name
+
+
+def test_flux(prob):
+    name, g, t, tb, S = prob
+    n, nc = tb["num_blocks"], S.ncell
+    phi = golden_io.seeded_input(name, "fx_phi", n * nc)
+    blocks, _ = t.tower(tb["level"].max())
+    for d in range(tb["ndim"]):
+        f = S.flux_compact(d, phi)
+        assert same_bits(block_slice(f, blocks, S.nfb), g["fx_out%d" % d]), (name, d)
+
+
+def test_fix_bc(prob):
+    name, g, t, tb, S = prob
+    n, nc, nd, nb = tb["num_blocks"], S.ncell, tb["ndim"], tb["nb"]
+    gs = (nb + 2) ** nd
+    phig = golden_io.seeded_input(name, "bc_phi", n * gs)
+    r0 = golden_io.seeded_input(name, "bc_rhs0", n * nc)
+    r = S.fix_bc_compact(phig, 1, r0)
+    assert same_bits(r, g["bc_rhs"]), name
+
+
+def mean_removed_vc_p(name, g, t, tb, S):
+    n, nc = tb["num_blocks"], S.ncell
+    p = golden_io.seeded_input(name, "vc_p", n * nc)
+    if not all_neumann(name):
+        return p
+    vf = S.get_coef(2)
+    blocks, _ = t.tower(tb["level"].max())
+    dvs = tb["block_len"].reshape(n, 3)
+    s = 0.0
+    v = 0.0
+    nd, nb = tb["ndim"], tb["nb"]
+    for b in blocks:
+        dv = 1.0
+        for d in range(nd):
+            dv *= dvs[b, d] / nb
+        for q in range(nc):
+            w = vf[b * nc + q]
+            if w > 0:
+                s += p[b * nc + q] * dv * w
+                v += dv * w
+    m = s / v
+    for b in blocks:
+        p[b * nc:(b + 1) * nc] -= m
+    return p
+
+
+def test_vcycle(prob):
+    """The V-cycle's bottom BiCGSTAB stops at a 1e-6 residual, so against the
+    reference it agrees to that tolerance only; against the bit-pinned oracle
+    with a converged bottom solve (1e-13) it agrees to 1e-10."""
+    from oracle import pyoracle
+    name, g, t, tb, S = prob
+    p = mean_removed_vc_p(name, g, t, tb, S)
+    blocks, _ = t.tower(tb["level"].max())
+    S.set_params(n_post_smooth=2, bot_tol_rel=1e-6, bot_tol_abs=1e-6, bot_max_iter=2000, precision=0, bottom=0)
+    mine = block_slice(S.vcycle(p), blocks, S.ncell)
+    ref = g["vc_phat"]
+    err = np.linalg.norm(mine - ref) / np.linalg.norm(ref)
+    assert err < 1e-4, (name, err)
+    nd = tb["ndim"]
+    O = pyoracle.Oracle(tb, bc_table(name, tb), S.get_coef(2), [S.get_coef(1, d) for d in range(nd)],
+                        [S.get_coef(0, d) for d in range(nd)])
+    S.set_params(bot_tol_rel=1e-13, bot_tol_abs=0.0)
+    mine = block_slice(S.vcycle(p), blocks, S.ncell)
+    orc = block_slice(O.vcycle(p, pyoracle.params(bot_tol_rel=1e-13, bot_tol_abs=0.0)), blocks, S.ncell)
+    err = np.linalg.norm(mine - orc) / np.linalg.norm(orc)
+    assert err < 1e-10, (name, err)
+
+
+def solution_error(name, tb, S, blocks, sol, ref):
+    n, nc, nd, nb = tb["num_blocks"], S.ncell, tb["ndim"], tb["nb"]
+    vf = block_slice(S.get_coef(2), blocks, nc)
+    lens = tb["block_len"].reshape(n, 3)
+    dv = np.repeat([np.prod(lens[b, :nd] / nb) for b in blocks], nc)
+    m = vf > 0
+    a = sol.copy()
+    r = ref.copy()
+    if all_neumann(name):
+        w = dv[m] * vf[m]
+        a[m] -= np.sum(a[m] * w) / np.sum(w)
+        r[m] -= np.sum(r[m] * w) / np.sum(w)
+    return np.linalg.norm(a[m] - r[m]) / np.linalg.norm(r[m])
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_solve_matches_reference(name):
+    """The converged solution is the same whatever the preconditioner, so the
+    V-cycle's bottom solve runs to a relative 1e-8 here: with the reference's
+    default absolute 1e-6 bottom tolerance the preconditioner degrades as the
+    outer residual falls and the outer iteration count becomes erratic (the
+    reference needs 290 iterations on c1 with its own rounding)."""
+    g, t, tb, S = setup_solver(name)
+    c = CASES[name]
+    S.set_rhs_compact(g["sv_rhs"])
+    S.set_zero_sol()
+    S.set_params(tol_rel=min(c["tol_rel"], 1e-11), tol_abs=0.0, use_mg_precond=1, max_iter=2000, precision=0,
+                 bottom=0, bot_tol_rel=1e-8, bot_tol_abs=0.0)
+    info = S.cg_solve()
+    assert info["status"] == 0, info
+    blocks, _ = t.tower(tb["level"].max())
+    sol = block_slice(S.get_sol_compact(), blocks, S.ncell)
+    err = solution_error(name, tb, S, blocks, sol, g["sv_sol"])
+    assert err < 1e-8, (name, err, info)
+
+
+def test_reference_parameters_converge_t2b():
+    """the reference's own default bottom tolerances (1e-6 rel and abs)"""
+    g, t, tb, S = setup_solver("t2b")
+    S.set_rhs_compact(g["sv_rhs"])
+    S.set_zero_sol()
+    S.set_params(tol_rel=1e-11, tol_abs=0.0, use_mg_precond=1, max_iter=2000)
+    info = S.cg_solve()
+    assert info["status"] == 0, info
+    blocks, _ = t.tower(tb["level"].max())
+    sol = block_slice(S.get_sol_compact(), blocks, S.ncell)
+    assert solution_error("t2b", tb, S, blocks, sol, g["sv_sol"]) < 1e-8

@@ -1,0 +1,122 @@
+"""Pins the C oracle (oracle/mac_oracle.c) against the reference library's own
+outputs (golden fixtures from oracle/ref_dump.cpp).  The oracle keeps the
+reference's serial operation order, so every comparison here is bit-exact,
+including the V-cycle (bottom BiCGSTAB) and whole solves."""
+import numpy as np
+import pytest
+
+import golden_io
+from cases import CASES, all_neumann, bc_table, build_tree
+from oracle import pyoracle
+
+OPS = [n for n in sorted(CASES) if CASES[n]["do_ops"]]
+
+
+def oracle_for(name):
+    g = golden_io.load(name)
+    t = build_tree(name)
+    tb = t.tables()
+    nd, nb, n = tb["ndim"], tb["nb"], tb["num_blocks"]
+    nc, nfb = nb ** nd, (nb + 1) * nb ** (nd - 1)
+    vf = g["vf"] if "vf" in g else np.ones(n * nc)
+    af = [g["af%d" % d] if "af%d" % d in g else np.ones(n * nfb) for d in range(nd)]
+    bc = [g["bcoef%d" % d] if "bcoef%d" % d in g else np.ones(n * nfb) for d in range(nd)]
+    return g, t, tb, pyoracle.Oracle(tb, bc_table(name, tb), vf, af, bc)
+
+
+@pytest.fixture(scope="module", params=OPS)
+def prob(request):
+    return (request.param,) + oracle_for(request.param)
+
+
+def rows(a, blocks, per):
+    return a.reshape(-1, per)[np.asarray(blocks)].reshape(-1)
+
+
+def exact(a, b):
+    return a.shape == b.shape and bool(np.all(a == b))
+
+
+def test_towers(prob):
+    name, g, t, tb, O = prob
+    for L in range(1, tb["max_level"] + 1):
+        blocks, be, ft = O.tower(L)
+        np.testing.assert_array_equal(blocks, g["tower_%d_blocks" % L])
+        regs = g["tower_%d_face_regs" % L].reshape(-1, 2 * tb["ndim"], 9)
+        np.testing.assert_array_equal(ft.reshape(-1, 6)[:, :2 * tb["ndim"]], regs[:, :, 0])
+
+
+def test_apply_residual(prob):
+    name, g, t, tb, O = prob
+    n, nc = tb["num_blocks"], O.ncell
+    x = golden_io.seeded_input(name, "op_x", n * nc)
+    for L in range(1, tb["level"].max() + 1):
+        if "op_apply_%d" % L in g:
+            assert exact(rows(O.apply(L, x), t.tower(L)[0], nc), g["op_apply_%d" % L]), (name, L)
+    finest = tb["level"].max()
+    r = O.residual(finest, x, golden_io.seeded_input(name, "op_rhs", n * nc))
+    assert exact(rows(r, t.tower(finest)[0], nc), g["op_resid"])
+
+
+def test_smooth(prob):
+    name, g, t, tb, O = prob
+    n, nc = tb["num_blocks"], O.ncell
+    corr = golden_io.seeded_input(name, "sm_corr0", n * nc)
+    res = golden_io.seeded_input(name, "sm_resid", n * nc)
+    for L in range(1, tb["level"].max() + 1):
+        if "sm_out_%d" % L in g:
+            assert exact(rows(O.smooth(L, corr, res), t.tower(L)[0], nc), g["sm_out_%d" % L]), (name, L)
+
+
+def test_transfers_flux_bc(prob):
+    name, g, t, tb, O = prob
+    n, nc, nd, nb = tb["num_blocks"], O.ncell, tb["ndim"], tb["nb"]
+    assert exact(O.restrict_sweep(golden_io.seeded_input(name, "rs_in", n * nc)), g["rs_out"])
+    assert exact(O.prolong_sweep(golden_io.seeded_input(name, "pr_in", n * nc)), g["pr_out"])
+    phi = golden_io.seeded_input(name, "fx_phi", n * nc)
+    leaf = t.tower(tb["level"].max())[0]
+    for d in range(nd):
+        assert exact(rows(O.flux(d, phi), leaf, O.nfb), g["fx_out%d" % d]), (name, d)
+    phig = golden_io.seeded_input(name, "bc_phi", n * (nb + 2) ** nd)
+    r0 = golden_io.seeded_input(name, "bc_rhs0", n * nc)
+    assert exact(O.fix_bc(phig, r0), g["bc_rhs"])
+
+
+def vc_input(name, g, t, tb, vf):
+    n, nc, nd, nb = tb["num_blocks"], tb["nb"] ** tb["ndim"], tb["ndim"], tb["nb"]
+    p = golden_io.seeded_input(name, "vc_p", n * nc)
+    if all_neumann(name):
+        lens = tb["block_len"].reshape(n, 3)
+        s = v = 0.0
+        leaf = t.tower(tb["level"].max())[0]
+        for b in leaf:
+            dv = 1.0
+            for d in range(nd):
+                dv *= lens[b, d] / nb
+            for q in range(nc):
+                w = vf[b * nc + q]
+                if w > 0:
+                    s += p[b * nc + q] * dv * w
+                    v += dv * w
+        for b in leaf:
+            p[b * nc:(b + 1) * nc] -= s / v
+    return p
+
+
+def test_vcycle_bit_exact(prob):
+    name, g, t, tb, O = prob
+    n, nc = tb["num_blocks"], O.ncell
+    vf = g["vf"] if "vf" in g else np.ones(n * nc)
+    p = vc_input(name, g, t, tb, vf)
+    phat = O.vcycle(p, pyoracle.params())
+    assert exact(rows(phat, t.tower(tb["level"].max())[0], nc), g["vc_phat"]), name
+
+
+@pytest.mark.parametrize("name", ["t2b", "t3n", "t3s"])
+def test_solve_bit_exact(name):
+    g, t, tb, O = oracle_for(name)
+    c = CASES[name]
+    sol, info = O.cg_solve(g["sv_rhs"], pyoracle.params(tol_rel=c["tol_rel"], tol_abs=0.0))
+    assert info["status"] == 0
+    leaf = t.tower(tb["level"].max())[0]
+    assert exact(rows(sol, leaf, O.ncell), g["sv_sol"]), name
