@@ -1,0 +1,361 @@
+#!/usr/bin/env python3
+"""Benchmark: MAC-Poisson time to a 1e-8 relative residual and leaf cells/s on
+one GB300, for the config-2 workload (2D, 16x16 blocks, 6 levels, two-phase
+B = 1/rho with rho 1:1000, fractional IB disk, seeded Gaussian RHS).
+
+A step is one complete MG-preconditioned BiCGSTAB solve from a zero initial
+guess to |r|_inf < 1e-8 |r0|_inf (the reference's criterion,
+src/SayakaMacSolver.cpp:891).
+
+  value : leaf cells / device time of a solve, inputs resident in HBM,
+          L2 flushed (256 MiB write) before every timed solve; N replicas
+          under torchrun add up (replicas only: one tree per GPU)
+  e2e   : the same through the C ABI with host buffers in the reference's
+          TreeData layout (setRhs -> cg_solve -> getSol per step)
+  cpu_baseline / --impl reference : the C oracle (bit-exact restatement of
+          the reference solver) on the host cores, bounded sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MAC Poisson time to 1e-8 rel residual & cells/s: learned+FP32 vs plain MG, GB300"
+TOL = 1e-8
+# outer BiCGSTAB iterations the reference algorithm (default bottom
+# tolerances, FP64) takes on the config-2 workload to 1e-8, measured with the
+# C oracle (a full CPU solve is too long for the bench's CPU sample)
+REF_ITERS_CONFIG2 = None
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="config2")
+    ap.add_argument("--precision", type=int, default=1, help="1: FP32 V-cycle (default), 0: FP64 V-cycle")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region"""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def treedata_cell_buffer(prob, cells, ngrow=1):
+    """compact cells -> the reference's TreeData layout (1 component, ngrow ghosts)"""
+    nd, nb, n = prob.ndim, prob.nb, prob.num_blocks
+    G = nb + 2 * ngrow
+    shape = (n,) + (G,) * nd
+    buf = np.zeros(shape)
+    inner = (slice(None),) + (slice(ngrow, ngrow + nb),) * nd
+    buf[inner] = cells.reshape((n,) + (nb,) * nd)
+    return buf.reshape(-1)
+
+
+def cpu_sample(prob, seconds, ref_iters):
+    """time outer iterations of the oracle's reference solver (1 thread)"""
+    from oracle import pyoracle
+    vf, af, bc = pyoracle.setup_coefficients(prob.tables, prob.bc, prob.vol, prob.area, prob.bface)
+    O = pyoracle.Oracle(prob.tables, prob.bc, vf, af, bc)
+    it = 1
+    t0 = time.perf_counter()
+    O.cg_solve(prob.rhs, pyoracle.params(max_iter=it, tol_rel=TOL, tol_abs=0.0))
+    t1 = time.perf_counter() - t0
+    per = t1
+    more = int(max(0, min(50, seconds / max(per, 1e-3) - 1)))
+    if more > 0:
+        t0 = time.perf_counter()
+        _, info = O.cg_solve(prob.rhs, pyoracle.params(max_iter=1 + more, tol_rel=TOL, tol_abs=0.0))
+        done = max(1, info["iterations"])
+        per = (time.perf_counter() - t0) / done
+        it = done
+    tts = per * ref_iters
+    return dict(value=prob.leaf_cells / tts, seconds_per_iteration=per, iterations_timed=it,
+                time_to_tol_s=tts)
+
+
+def _cpu_worker(args):
+    name, seconds, ref_iters = args
+    from sayakaamr_gb300 import workloads
+    prob = workloads.CONFIGS[name]()
+    return cpu_sample(prob, seconds, ref_iters)
+
+
+def reference_iterations(name):
+    """outer iterations of the reference algorithm to 1e-8 on the workload"""
+    return {"config2": REF_ITERS_CONFIG2}.get(name)
+
+
+def run_reference(args):
+    """--impl reference: the reference solver (C oracle port, the reference
+    library itself does not travel to the GPU host) on every host core, each
+    core solving its own copy; one step = one bounded sample per core."""
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from sayakaamr_gb300 import workloads
+    prob = workloads.CONFIGS[args.config]()
+    ref_iters = reference_iterations(args.config)
+    if ref_iters is None:
+        print(json.dumps({"impl": "reference", "unavailable": "no measured reference iteration count for %s"
+                          % args.config}))
+        return
+    cores = os.cpu_count() or 1
+    per_core_s = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    ctx = mp.get_context("spawn")
+    vals = []
+    t_all = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        for s in range(args.warmup + args.steps):
+            res = pool.map(_cpu_worker, [(args.config, per_core_s, ref_iters)] * cores)
+            if s >= args.warmup:
+                vals.append(sum(r["value"] for r in res))
+    wall = time.perf_counter() - t_all
+    v = statistics.mean(vals)
+    ms = prob.leaf_cells / v * 1e3 * cores
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.config, "leaf_cells": prob.leaf_cells, **prob.describe()},
+        "cpu_baseline": {"value": v, "unit": "cells/s", "cores": cores, "kind": "port",
+                         "sample": "C oracle (bit-exact restatement of the reference solver), one copy per core, "
+                                   "%.1f s of outer BiCGSTAB iterations each, time to 1e-8 = s/iteration x %d "
+                                   "reference iterations" % (per_core_s, ref_iters)},
+        "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    ws, rank, local = dist_info()
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import sayakaamr_gb300 as sg
+    from sayakaamr_gb300 import workloads
+
+    prob = workloads.CONFIGS[args.config]()
+    S = workloads.make_solver(prob)
+    S.set_params(tol_rel=TOL, tol_abs=0.0, use_mg_precond=1, max_iter=2000, precision=args.precision, bottom=1)
+    S.prepare()
+    ext = torch.cuda.ExternalStream(S.stream())
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    finest = int(prob.tables["level"].max())
+
+    def one(timed_events=None):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        if timed_events:
+            timed_events[0].record(ext)
+        S.set_zero_sol()
+        S.cg_solve_async()
+        if timed_events:
+            timed_events[1].record(ext)
+        return S.solve_info()
+
+    for _ in range(args.warmup):
+        info = one()
+        if info["status"] != 0:
+            raise SystemExit("warm-up solve failed: %s" % info)
+    pro, per_it, epi = S.launch_counts()
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    infos = []
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            infos.append(one(events[k]))
+        torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = [a.elapsed_time(b) for a, b in events]
+    ms_step = statistics.mean(ms)
+    if ws > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    bad = [i for i in infos if i["status"] != 0 or not (i["rnorm"] < TOL * i["rnorm0"])]
+    if bad:
+        raise SystemExit("timed solve did not converge: %s" % bad[0])
+    iters = [i["iterations"] for i in infos]
+    value = ws * prob.leaf_cells / (ms_step / 1e3)
+    launches = int(round(statistics.mean(pro + it * per_it + epi for it in iters)))
+
+    # ---- end to end through the C ABI with host TreeData buffers ----
+    rhs_td = treedata_cell_buffer(prob, prob.rhs, ngrow=1)
+    sol_td = np.zeros_like(rhs_td)
+    import ctypes
+    pin_rhs = torch.from_numpy(rhs_td).pin_memory()
+    pin_sol = torch.from_numpy(sol_td).pin_memory()
+    rhs_np = pin_rhs.numpy()
+    sol_np = pin_sol.numpy()
+    e2e_t = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        S.set_rhs(rhs_np, ncomp=1, ngrow=1, comp=0)
+        S.set_zero_sol()
+        info = S.cg_solve()
+        S.get_sol(sol_np, ncomp=1, ngrow=1, comp=0)
+        t1 = time.perf_counter()
+        if info["status"] != 0:
+            raise SystemExit("e2e solve failed: %s" % info)
+        if k >= args.warmup:
+            e2e_t.append(t1 - t0)
+    e2e_s = statistics.mean(e2e_t)
+    h2d = prob.num_blocks * prob.ncell * 8
+    d2h = prob.num_blocks * prob.ncell * 8
+
+    # ---- roofline of the dominant kernel, timed live on the solver stream ----
+    roof = roofline(S, prob, ext, torch, finest)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 outer BiCGSTAB + %s V-cycle, f64 bottom" % ("f32" if args.precision == 1 else "f64"),
+        "data": "synthetic",
+        "config": {"workload": "%s: 2D 16x16 blocks, %d levels, %d leaf blocks, rho 1:1000 ellipse, fractional IB "
+                               "disk, p=0 top wall" % (args.config, finest, len(prob.leaf)),
+                   "leaf_cells": prob.leaf_cells, "blocks": prob.num_blocks, "tol_rel": TOL,
+                   "l2": "flushed (256 MiB write) before every timed solve", "precision": args.precision,
+                   "iterations_per_solve": statistics.mean(iters), "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "e2e": {"value": ws * prob.leaf_cells / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": launches,
+        "roofline": roof,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu:
+        ref_iters = reference_iterations(args.config)
+        if ref_iters:
+            cs = cpu_sample(prob, args.cpu_seconds, ref_iters)
+            out["cpu_baseline"] = {"value": cs["value"], "unit": "cells/s", "cores": 1, "kind": "port",
+                                   "sample": "C oracle (bit-exact restatement of the reference solver), 1 thread: "
+                                             "%d outer BiCGSTAB iterations at %.3f s each; time to 1e-8 = that x %d "
+                                             "reference iterations" % (cs["iterations_timed"],
+                                                                       cs["seconds_per_iteration"], ref_iters)}
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def roofline(S, prob, ext, torch, finest):
+    """dominant kernel: the FP32 red-black sweep over the finest level of the
+    finest tower.  Algorithmic bytes per launch = cells of that level x
+    4 B x (2 + ndim): one colour reads/writes every phi once (half read, half
+    written), rhs and vf of the updated half, and every face coefficient."""
+    import json as _json
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak = float(_json.load(f)["hbm_gbs"])
+            src = "measured"
+    nblk = S.tower_size(finest, finest)
+    cells = nblk * prob.ncell
+    bytes_per_launch = cells * 4 * (2 + prob.ndim)
+    reps = 200
+    for _ in range(10):
+        S.enqueue_kernel(1, finest)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(ext)
+    for _ in range(reps):
+        S.enqueue_kernel(1, finest)
+    b.record(ext)
+    torch.cuda.synchronize()
+    us = a.elapsed_time(b) * 1e3 / reps
+    achieved = bytes_per_launch / (us * 1e-6) / 1e9
+    return {"kernel": "k_smooth<float,2> (finest level, one colour)", "bound": "hbm", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "bytes_per_launch": bytes_per_launch, "us_per_launch": us, "peak_source": src + " (burst copy)",
+            "note": "working set is L2-resident at this size; traffic from profiles/"}
+
+
+if __name__ == "__main__":
+    main()

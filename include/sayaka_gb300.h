@@ -164,6 +164,27 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p);
 /* cg_solve (src/SayakaMacSolver.cpp:455-680): BiCGSTAB on the finest tower */
 int sayaka_mac_cg_solve(sayaka_mac *h, sayaka_solve_info *info);
 
+/* Device-resident solve path (params.bottom = 1, use_mg_precond = 1):
+ * build the FP32 coefficient copies, the dense level-1 inverse and the CUDA
+ * graph of one BiCGSTAB iteration ahead of time ... */
+int sayaka_mac_prepare(sayaka_mac *h);
+/* ... enqueue a whole cg_solve on the solver's stream without waiting ... */
+int sayaka_mac_cg_solve_async(sayaka_mac *h);
+/* ... and read its outcome (waits for the stream) */
+int sayaka_mac_solve_info(sayaka_mac *h, sayaka_solve_info *info);
+/* the CUDA stream (cudaStream_t) every launch of this handle goes to */
+void *sayaka_mac_stream(sayaka_mac *h);
+/* enqueue one launch of a hot kernel on the solver's current data, for
+ * per-kernel timing: which = 0 FP64 operator on tower L (x = solution),
+ * 1 FP32 red-black sweep (colour 0) of the finest level of tower L,
+ * 2 FP64 red-black sweep (colour 0) of the finest level of tower L */
+int sayaka_mac_enqueue_kernel(sayaka_mac *h, int32_t which, int32_t L);
+/* kernel launches of a device-resident solve: prologue + per iteration +
+ * epilogue (out pointers may be NULL) */
+int sayaka_mac_launch_counts(sayaka_mac *h, int32_t *prologue, int32_t *per_iteration, int32_t *epilogue);
+/* number of blocks in tower L, or at one level of it (sublevel >= 1) */
+int32_t sayaka_mac_tower_size(sayaka_mac *h, int32_t L, int32_t sublevel);
+
 /* mg_flux_level (src/SayakaMacOperator.cpp:161-239): face flux -d(phi)/dh of
  * direction dir on the leaf blocks; phi in TreeData layout (ngrow any) */
 int sayaka_mac_flux(sayaka_mac *h, int32_t dir, const double *phi, int32_t phi_ncomp, int32_t phi_ngrow,

@@ -24,6 +24,7 @@
  *   src/SayakaMacOperator.cpp:1470-1594  BC lift                 orc_fix_bc
  *   src/SayakaMacUtil.cpp:9-207     residual, norms, dots, axpby
  *   src/SayakaMacSolver.cpp:164-374, 683-949  bottom, V-cycle, BiCGSTAB
+ *   src/SayakaMacCoef.cpp:36-76, src/SayakaMacIB.cpp:34-154  coefficient setup
  */
 #include <math.h>
 #include <stdint.h>
@@ -950,6 +951,98 @@ int orc_tower(const orc_problem *P, int L, int32_t *blocks, int32_t *n, int32_t 
     begin_end[2 * (l - 1)] = t->n ? t->begin[l] : 0;
     begin_end[2 * (l - 1) + 1] = t->n ? t->end[l] : 0;
   }
+  ctx_free(&c);
+  return 0;
+}
+
+/* AVG restriction of face data of direction dir onto the non-leaf blocks of
+ * levels finest-1 .. 1 (src/SayakaFillPatch.cpp:401-447 with
+ * src/SayakaInterpPatch.cpp:627-691) */
+static void restrict_face_levels(const ctx_t *c, int dir, double *F) {
+  const orc_problem *P = c->P;
+  const int nb = c->nb, nd = c->nd, half = nb / 2;
+  const double scale = nd == 3 ? 0.25 : 0.5;
+  for (int l = c->finest - 1; l >= 1; l--)
+    for (int q = 0; q < c->nlev[l]; q++) {
+      const int b = c->lev[l][q];
+      if (P->node_type[b] == 1) continue;
+      for (int ch = 0; ch < (1 << nd); ch++) {
+        const int cb = P->child[b * 8 + ch];
+        int off[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+        for (int d = 0; d < nd; d++) {
+          off[d] = ((ch >> d) & 1) * half;
+          lo[d] = off[d];
+          hi[d] = off[d] + half - 1;
+        }
+        hi[dir] += 1;
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            for (int i = lo[0]; i <= hi[0]; i++) {
+              const int ii1 = dir == 0 ? 0 : 1, jj1 = (dir == 1 || nd < 2) ? 0 : 1, kk1 = (dir == 2 || nd < 3) ? 0 : 1;
+              double val = 0;
+              for (int kind = -kk1; kind <= kk1; kind += 2)
+                for (int jind = -jj1; jind <= jj1; jind += 2)
+                  for (int iind = -ii1; iind <= ii1; iind += 2) {
+                    const int fi = (i - off[0]) * 2 + (dir == 0 ? 0 : (iind + 1) / 2);
+                    const int fj = nd >= 2 ? (j - off[1]) * 2 + (dir == 1 ? 0 : (jind + 1) / 2) : j;
+                    const int fk = nd == 3 ? (k - off[2]) * 2 + (dir == 2 ? 0 : (kind + 1) / 2) : k;
+                    val += F_(c, F, cb, dir, fi, fj, fk);
+                  }
+              F_(c, F, b, dir, i, j, k) = val * scale;
+            }
+      }
+    }
+}
+
+/* AVG restriction of cell data onto non-leaf blocks, finest-1 .. 1 */
+static void restrict_cell_levels(const ctx_t *c, double *V) {
+  const orc_problem *P = c->P;
+  const int nb = c->nb, nd = c->nd, half = nb / 2;
+  const double wgt = 1.0 / (1 << nd);
+  for (int l = c->finest - 1; l >= 1; l--)
+    for (int q = 0; q < c->nlev[l]; q++) {
+      const int b = c->lev[l][q];
+      if (P->node_type[b] == 1) continue;
+      for (int ch = 0; ch < (1 << nd); ch++) {
+        const int cb = P->child[b * 8 + ch];
+        int off[3] = {0, 0, 0};
+        for (int d = 0; d < nd; d++) off[d] = ((ch >> d) & 1) * half;
+        for (int kc = off[2]; kc < off[2] + (nd == 3 ? half : 1); kc++)
+          for (int jc = off[1]; jc < off[1] + half; jc++)
+            for (int ic = off[0]; ic < off[0] + half; ic++) {
+              double sum = 0;
+              for (int kk = 0; kk <= (nd == 3 ? 1 : 0); kk++)
+                for (int jj = 0; jj <= 1; jj++)
+                  for (int ii = 0; ii <= 1; ii++)
+                    sum += V_(c, V, cb, (ic - off[0]) * 2 + ii, (jc - off[1]) * 2 + jj,
+                              nd == 3 ? (kc - off[2]) * 2 + kk : 0);
+              V_(c, V, b, ic, jc, kc) = sum * wgt;
+            }
+      }
+    }
+}
+
+/* setCoefB (src/SayakaMacCoef.cpp:36-76) and the fraction part of
+ * calcIBFracByLS (src/SayakaMacIB.cpp:69-96): the arrays hold leaf values
+ * on entry (other blocks are overwritten); c/f AVG sync on the finest tower,
+ * then AVG restriction to the parents.  Any pointer may be NULL. */
+int orc_setup_coefficients(const orc_problem *P, double *vf, double *af0, double *af1, double *af2, double *b0,
+                           double *b1, double *b2) {
+  ctx_t c;
+  ctx_init(&c, P);
+  double *af[3] = {af0, af1, af2}, *bc[3] = {b0, b1, b2};
+  for (int d = 0; d < c.nd; d++) {
+    if (bc[d]) {
+      for (int l = c.finest; l >= 2; l--) sync_cf(&c, c.finest, l, d, bc[d], 1);
+      restrict_face_levels(&c, d, bc[d]);
+    }
+  }
+  for (int d = 0; d < c.nd; d++)
+    if (af[d])
+      for (int l = c.finest; l >= 2; l--) sync_cf(&c, c.finest, l, d, af[d], 1);
+  if (vf) restrict_cell_levels(&c, vf);
+  for (int d = 0; d < c.nd; d++)
+    if (af[d]) restrict_face_levels(&c, d, af[d]);
   ctx_free(&c);
   return 0;
 }

@@ -51,6 +51,31 @@ def params(max_iter=2000, tol_rel=1e-6, tol_abs=0.0, n_post=2, use_precond=1, bo
     return _Params(max_iter, tol_rel, tol_abs, n_post, use_precond, bot_tol_rel, bot_tol_abs, bot_max_iter)
 
 
+def setup_coefficients(tables, bc, vf=None, af=None, bcoef=None):
+    """Coefficient sync + restriction of the reference on leaf-valued arrays
+    (returns new arrays; None entries are skipped)."""
+    lib = load()
+    nd = int(tables["ndim"])
+    keep = []
+    vf2 = None if vf is None else np.array(vf, dtype=np.float64)
+    af2 = [None] * 3 if af is None else [np.array(a, dtype=np.float64) for a in af] + [None] * (3 - len(af))
+    b2 = [None] * 3 if bcoef is None else [np.array(a, dtype=np.float64) for a in bcoef] + [None] * (3 - len(bcoef))
+    n = int(tables["num_blocks"])
+    nb = int(tables["nb"])
+    ones_c = np.ones(n * nb ** nd)
+    ones_f = [np.ones(n * (nb + 1) * nb ** (nd - 1)) for _ in range(nd)]
+    O = Oracle(tables, bc, vf2 if vf2 is not None else ones_c, [a if a is not None else ones_f[d] for d, a in
+                                                                 enumerate(af2[:nd])],
+               [a if a is not None else ones_f[d] for d, a in enumerate(b2[:nd])])
+
+    def ptr(a):
+        return C.cast(0, _f64p) if a is None else a.ctypes.data_as(_f64p)
+
+    lib.orc_setup_coefficients(C.byref(O.P), ptr(vf2), ptr(af2[0]), ptr(af2[1]), ptr(af2[2]), ptr(b2[0]), ptr(b2[1]),
+                               ptr(b2[2]))
+    return vf2, af2[:nd], b2[:nd]
+
+
 class Oracle:
     """CPU restatement of the reference MAC solver over one tree.
 

@@ -81,6 +81,13 @@ SIGNATURES = {
     "sayaka_mac_get_sol_compact": (C.c_int, [_V, _V, C.c_int32]),
     "sayaka_mac_set_params": (C.c_int, [_V, C.POINTER(Params)]),
     "sayaka_mac_cg_solve": (C.c_int, [_V, C.POINTER(SolveInfo)]),
+    "sayaka_mac_prepare": (C.c_int, [_V]),
+    "sayaka_mac_cg_solve_async": (C.c_int, [_V]),
+    "sayaka_mac_solve_info": (C.c_int, [_V, C.POINTER(SolveInfo)]),
+    "sayaka_mac_stream": (C.c_void_p, [_V]),
+    "sayaka_mac_enqueue_kernel": (C.c_int, [_V, C.c_int32, C.c_int32]),
+    "sayaka_mac_tower_size": (C.c_int32, [_V, C.c_int32, C.c_int32]),
+    "sayaka_mac_launch_counts": (C.c_int, [_V, _i32p, _i32p, _i32p]),
     "sayaka_mac_flux": (C.c_int, [_V, C.c_int32, _f64p, C.c_int32, C.c_int32, C.c_int32, _f64p, C.c_int32,
                                   C.c_int32, C.c_int32]),
     "sayaka_mac_apply_compact": (C.c_int, [_V, C.c_int32, _f64p, _f64p]),
@@ -340,6 +347,33 @@ class MacSolver:
             _check(rc, "cg_solve", self.h)
         return dict(status=info.status, iterations=info.iterations, rnorm0=info.rnorm0, rnorm=info.rnorm,
                     seconds=info.seconds, rc=rc)
+
+    # --- device-resident path ---
+    def prepare(self):
+        _check(self.lib.sayaka_mac_prepare(self.h), "prepare", self.h)
+
+    def cg_solve_async(self):
+        _check(self.lib.sayaka_mac_cg_solve_async(self.h), "cg_solve_async", self.h)
+
+    def solve_info(self):
+        info = SolveInfo()
+        _check(self.lib.sayaka_mac_solve_info(self.h, C.byref(info)), "solve_info", self.h)
+        return dict(status=info.status, iterations=info.iterations, rnorm0=info.rnorm0, rnorm=info.rnorm)
+
+    def stream(self):
+        return self.lib.sayaka_mac_stream(self.h)
+
+    def enqueue_kernel(self, which, L):
+        _check(self.lib.sayaka_mac_enqueue_kernel(self.h, int(which), int(L)), "enqueue_kernel", self.h)
+
+    def launch_counts(self):
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(self.lib.sayaka_mac_launch_counts(self.h, C.byref(a), C.byref(b), C.byref(c)), "launch_counts",
+               self.h)
+        return a.value, b.value, c.value
+
+    def tower_size(self, L, sublevel=0):
+        return self.lib.sayaka_mac_tower_size(self.h, int(L), int(sublevel))
 
     # --- parity hooks (compact arrays over all blocks) ---
     def _cells(self):

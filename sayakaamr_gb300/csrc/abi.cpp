@@ -519,6 +519,48 @@ int sayaka_mac_cg_solve(sayaka_mac *h, sayaka_solve_info *info) {
   });
 }
 
+int sayaka_mac_prepare(sayaka_mac *h) {
+  return guarded(h, [&] {
+    if (h->gpu->params().bottom != 1 || !h->gpu->params().use_mg_precond) {
+      h->err = "prepare needs params.bottom = 1 and use_mg_precond = 1";
+      return (int)SAYAKA_BAD_INPUT;
+    }
+    return h->gpu->prepare_device() == 0 ? (int)SAYAKA_OK : (int)SAYAKA_CUDA_ERROR;
+  });
+}
+int sayaka_mac_cg_solve_async(sayaka_mac *h) {
+  return guarded(h, [&] { return h->gpu->cg_solve_enqueue() == 0 ? (int)SAYAKA_OK : (int)SAYAKA_BAD_INPUT; });
+}
+int sayaka_mac_solve_info(sayaka_mac *h, sayaka_solve_info *info) {
+  return guarded(h, [&] {
+    SolveInfo si;
+    if (h->gpu->solve_state(&si) != 0) return (int)SAYAKA_CUDA_ERROR;
+    if (info) {
+      info->status = si.status;
+      info->iterations = si.iterations;
+      info->rnorm0 = si.rnorm0;
+      info->rnorm = si.rnorm;
+      info->seconds = 0;
+    }
+    return (int)SAYAKA_OK;
+  });
+}
+void *sayaka_mac_stream(sayaka_mac *h) { return (h && h->gpu) ? (void *)h->gpu->stream() : nullptr; }
+int sayaka_mac_enqueue_kernel(sayaka_mac *h, int32_t which, int32_t L) {
+  return guarded(h, [&] { return h->gpu->enqueue_kernel(which, L) == 0 ? (int)SAYAKA_OK : (int)SAYAKA_BAD_INPUT; });
+}
+int sayaka_mac_launch_counts(sayaka_mac *h, int32_t *pro, int32_t *per, int32_t *epi) {
+  return guarded(h, [&] {
+    if (pro) *pro = MacGpu::kPrologueKernels;
+    if (per) *per = h->gpu->kernels_per_iteration();
+    if (epi) *epi = MacGpu::kEpilogueKernels;
+    return (int)SAYAKA_OK;
+  });
+}
+int32_t sayaka_mac_tower_size(sayaka_mac *h, int32_t L, int32_t sublevel) {
+  return (h && h->gpu) ? h->gpu->tower_size(L, sublevel) : -1;
+}
+
 int sayaka_mac_flux(sayaka_mac *h, int32_t dir, const double *phi, int32_t pn, int32_t pg, int32_t pc, double *flux,
                     int32_t fn, int32_t fg, int32_t fc) {
   return guarded(h, [&] {

@@ -46,12 +46,17 @@ struct BlockList {
   int n;
 };
 
-// solver scalars kept on the device (FP64)
-struct Scalars {
+// BiCGSTAB state kept on the device (FP64 scalars and control flags) by the
+// graph-captured solve of mac_fast.cu
+struct FState {
   double rho, rho1, alpha, omega, beta;
   double rnorm0, rnorm;
-  double dots[4];
-  int iter, stat, done, conv;
+  double tol_rel, tol_abs;
+  int iter, max_iter;
+  int done;     // loop ends (converged, breakdown or max_iter)
+  int stat;     // 1 = breakdown
+  int conv;     // converged
+  int trivial;  // zero initial residual
 };
 
 // ---- launchers (mac_kernels.cu) ----

@@ -1,0 +1,791 @@
+// Device-resident MG-preconditioned BiCGSTAB (the iteration of
+// src/SayakaMacSolver.cpp:683-920) for production solves:
+//  * scalars (rho, alpha, omega, norms, flags) stay in device memory; the last
+//    CTA of every reduction runs the reference's scalar logic (breakdown and
+//    convergence tests) in its epilogue, so a solve needs no host round trip;
+//  * vector updates are fused with the reductions that follow them;
+//  * one iteration is captured in a CUDA graph under a conditional WHILE node
+//    that a kernel re-arms until the convergence flag is set;
+//  * the V-cycle runs in FP64 or FP32 (residual, transfers, smoother), the
+//    bottom level is solved directly with a dense FP64 inverse of the
+//    level-1 operator built on the GPU at setup (singular Neumann components
+//    are pinned at one cell).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mac_solver.h"
+#include "cuda_check.h"
+#include "mac_stencil.cuh"
+
+namespace sayaka_gb300 {
+
+namespace {
+
+constexpr int kTPB = 256;
+constexpr int kMaxRedBlocks = 152 * 4;
+
+inline int red_grid(long work) {
+  long g = (work + kTPB - 1) / kTPB;
+  return (int)std::max<long>(1, std::min<long>(g, kMaxRedBlocks));
+}
+inline int ew_grid(long work) {
+  long g = (work + kTPB - 1) / kTPB;
+  return (int)std::max<long>(1, std::min<long>(g, 152 * 32));
+}
+
+__device__ __forceinline__ double wsum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double wmax(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Grid-wide reduction of NV values (bit i of maxmask: max, else sum).  Each
+// CTA writes its partials; the last CTA to arrive combines them in CTA order
+// (deterministic for a fixed grid) and runs `epi` on thread 0.
+template <int NV, class Epi>
+__device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, double *partials, unsigned *counter,
+                                            Epi epi) {
+  __shared__ double sh[NV][kTPB / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    const double r = ((maxmask >> i) & 1) ? wmax(v[i]) : wsum(v[i]);
+    if (lane == 0) sh[i][w] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+      double r = 0.0;
+      for (int q = 0; q < kTPB / 32; q++) r = ((maxmask >> i) & 1) ? fmax(r, sh[i][q]) : r + sh[i][q];
+      partials[blockIdx.x * NV + i] = r;
+    }
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double acc[NV];
+#pragma unroll
+  for (int i = 0; i < NV; i++) acc[i] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+      const double pv = ((volatile double *)partials)[b * NV + i];
+      acc[i] = ((maxmask >> i) & 1) ? fmax(acc[i], pv) : acc[i] + pv;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    const double r = ((maxmask >> i) & 1) ? wmax(acc[i]) : wsum(acc[i]);
+    if (lane == 0) sh[i][w] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double fin[NV];
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+      double r = 0.0;
+      for (int q = 0; q < kTPB / 32; q++) r = ((maxmask >> i) & 1) ? fmax(r, sh[i][q]) : r + sh[i][q];
+      fin[i] = r;
+    }
+    epi(fin);
+    *counter = 0;
+  }
+}
+
+__device__ __forceinline__ long cell_of(const BlockList &L, int ncell, long it) {
+  const int p = (int)(it / ncell);
+  return (long)L.blocks[p] * ncell + (it - (long)p * ncell);
+}
+
+// ---- epilogues: the reference's scalar logic (src/SayakaMacSolver.cpp:766-904)
+struct EpiInit {  // after r0 = b - A x0: |r0|, rho = r0.r0
+  FState *st;
+  __device__ void operator()(const double *v) const {
+    st->rnorm0 = v[0];
+    st->rnorm = v[0];
+    st->iter = 1;
+    if (v[0] == 0) {  // initial convergence: solution untouched
+      st->done = 1;
+      st->conv = 0;
+      st->stat = 0;
+      st->trivial = 1;
+      return;
+    }
+    st->rho = v[1];
+    if (v[1] == 0) {
+      st->stat = 1;
+      st->done = 1;
+    }
+  }
+};
+struct EpiAlpha {  // rhat.v
+  FState *st;
+  __device__ void operator()(const double *v) const {
+    if (v[0] == 0) {
+      st->stat = 1;
+      st->done = 1;
+      return;
+    }
+    st->alpha = st->rho / v[0];
+  }
+};
+struct EpiHalf {  // |s|
+  FState *st;
+  __device__ void operator()(const double *v) const {
+    st->rnorm = v[0];
+    if (v[0] < st->rnorm0 * st->tol_rel || v[0] < st->tol_abs) {
+      st->conv = 1;
+      st->done = 1;
+    }
+  }
+};
+struct EpiOmega {  // t.s, t.t
+  FState *st;
+  __device__ void operator()(const double *v) const {
+    if (v[1] == 0) {
+      st->stat = 1;
+      st->done = 1;
+      return;
+    }
+    st->omega = v[0] / v[1];
+  }
+};
+struct EpiEnd {  // |r|, rhat.r of the next iteration
+  FState *st;
+  __device__ void operator()(const double *v) const {
+    st->rnorm = v[0];
+    if (v[0] < st->rnorm0 * st->tol_rel + st->tol_abs) {
+      st->conv = 1;
+      st->done = 1;
+      return;
+    }
+    if (st->omega == 0) {
+      st->stat = 1;
+      st->done = 1;
+      return;
+    }
+    st->rho1 = st->rho;
+    st->iter += 1;
+    if (st->iter > st->max_iter) {
+      st->iter = st->max_iter;
+      st->done = 1;
+      return;
+    }
+    st->rho = v[1];
+    if (v[1] == 0) {
+      st->stat = 1;
+      st->done = 1;
+      return;
+    }
+    st->beta = (st->rho / st->rho1) * (st->alpha / st->omega);
+  }
+};
+
+// ---- kernels -------------------------------------------------------------
+__global__ void k_set_cond(cudaGraphConditionalHandle h, const FState *st) {
+  cudaGraphSetConditional(h, st->done ? 0u : 1u);
+}
+
+// x0 = sol, x = 0 on the tower
+__global__ void k_pro_copy(BlockList L, int ncell, const double *sol, double *x0, double *x) {
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const long q = cell_of(L, ncell, it);
+    x0[q] = sol[q];
+    x[q] = 0.0;
+  }
+}
+
+// p = r (first iteration) or p = r + beta*(p - omega*v) in the reference's two
+// saxby steps; the V-cycle's residual (rhs - A*0) = masked p in precision T
+template <typename T>
+__global__ void k_pupdate(BlockList L, int ncell, const FState *st, const double *r, double *p, const double *v,
+                          const double *vf, T *resid) {
+  if (st->done) return;
+  const bool first = st->iter == 1;
+  const double beta = st->beta, om = st->omega;
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const long q = cell_of(L, ncell, it);
+    double pv;
+    if (first) {
+      pv = r[q];
+    } else {
+      const double p1 = 1.0 * p[q] + (-om) * v[q];
+      pv = 1.0 * r[q] + beta * p1;
+    }
+    p[q] = pv;
+    resid[q] = vf[q] > 0 ? (T)pv : (T)0;
+  }
+}
+
+// s = r - alpha v ; x = x + alpha phat ; V-cycle residual = masked s ; |s|
+template <typename T>
+__global__ void __launch_bounds__(kTPB) k_supdate(BlockList L, int ncell, FState *st, const double *r, const double *v,
+                                                double *s, double *x, const double *phat, const double *vf, T *resid,
+                                                double *partials, unsigned *counter) {
+  if (st->done) return;
+  const double a = st->alpha;
+  double m[1] = {0.0};
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const long q = cell_of(L, ncell, it);
+    const double sv = 1.0 * r[q] + (-a) * v[q];
+    s[q] = sv;
+    x[q] = 1.0 * x[q] + a * phat[q];
+    resid[q] = vf[q] > 0 ? (T)sv : (T)0;
+    m[0] = fmax(m[0], fabs(sv));
+  }
+  grid_reduce<1>(m, 1u, partials, counter, EpiHalf{st});
+}
+
+// x = x + omega shat ; r = s - omega t ; |r| ; rhat.r
+__global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, FState *st, double *x, const double *shat,
+                                                double *r, const double *s, const double *t, const double *rhat,
+                                                double *partials, unsigned *counter) {
+  if (st->done) return;
+  const double om = st->omega;
+  double m[2] = {0.0, 0.0};
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const long q = cell_of(L, ncell, it);
+    x[q] = 1.0 * x[q] + om * shat[q];
+    const double rv = 1.0 * s[q] + (-om) * t[q];
+    r[q] = rv;
+    m[0] = fmax(m[0], fabs(rv));
+    m[1] += rhat[q] * rv;
+  }
+  grid_reduce<2>(m, 1u, partials, counter, EpiEnd{st});
+}
+
+// after the loop: x0 += x ; sol = x0 when converged
+__global__ void k_finish(BlockList L, int ncell, const FState *st, double *x0, const double *x, double *sol) {
+  if (!st->conv) return;
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const long q = cell_of(L, ncell, it);
+    const double v = x0[q] + x[q];
+    x0[q] = v;
+    sol[q] = v;
+  }
+}
+
+// phat (FP64) = SOL(=0) + CORR over the tower, from precision T
+template <typename T>
+__global__ void k_vc_out(BlockList L, int ncell, const FState *st, const T *corr, double *out) {
+  if (st->done) return;
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const long q = cell_of(L, ncell, it);
+    out[q] = 0.0 + (double)corr[q];
+  }
+}
+
+// Operator fused with its dot products: y = A x (FP64, the reference's exact
+// arithmetic via the shared device functions of mac_kernels.cu) and
+// MODE 0: rhat.y (EpiAlpha) ; MODE 1: y.w, y.y (EpiOmega) ; MODE 2: residual
+// y = rhs - A x with |y|, y.y (EpiInit)
+template <int ND, int MODE>
+__global__ void __launch_bounds__(kTPB) k_apply_red(Topo t, Coef<double> c, BlockList L, const double *x, double *y,
+                                                  const double *w, FState *st, double *partials, unsigned *counter) {
+  if (MODE != 2 && st->done) return;
+  double acc[2] = {0.0, 0.0};
+  const int ncell = t.ncell;
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    const int ci = (int)(it - (long)p * ncell);
+    const double out = stencil::apply_cell<double, ND>(t, c, L.blocks[p], L.ftypes[p], ci, x);
+    const long q = (long)L.blocks[p] * ncell + ci;
+    const double vfv = c.vf[q];
+    double yv = vfv > 0 ? out : 0.0;
+    if (MODE == 2) yv = vfv > 0 ? w[q] - yv : 0.0;
+    y[q] = yv;
+    if (MODE == 0) acc[0] += w[q] * yv;
+    if (MODE == 1) {
+      acc[0] += yv * w[q];
+      acc[1] += yv * yv;
+    }
+    if (MODE == 2) {
+      acc[0] = fmax(acc[0], fabs(yv));
+      acc[1] += yv * yv;
+    }
+  }
+  if (MODE == 0) grid_reduce<2>(acc, 0u, partials, counter, EpiAlpha{st});
+  if (MODE == 1) grid_reduce<2>(acc, 0u, partials, counter, EpiOmega{st});
+  if (MODE == 2) grid_reduce<2>(acc, 1u, partials, counter, EpiInit{st});
+}
+
+// dense bottom solve: corr(level 1) = Binv * resid(level 1), one warp per row
+template <typename T>
+__global__ void __launch_bounds__(kTPB) k_bottom_gemv(int n, const double *__restrict__ binv, const int *blocks,
+                                                    int ncell, const T *__restrict__ resid, T *__restrict__ corr,
+                                                    const FState *st) {
+  if (st && st->done) return;
+  extern __shared__ double rv[];
+  for (int j = threadIdx.x; j < n; j += blockDim.x) rv[j] = (double)resid[(long)blocks[j / ncell] * ncell + j % ncell];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= n) return;
+  const double *a = binv + (long)row * n;
+  double s = 0.0;
+  for (int j = lane; j < n; j += 32) s += a[j] * rv[j];
+  s = wsum(s);
+  if (lane == 0) corr[(long)blocks[row / ncell] * ncell + row % ncell] = (T)s;
+}
+
+// in-place Gauss-Jordan inversion step k (no pivoting: the pinned, row-scaled
+// level-1 operator has positive pivots)
+__global__ void k_gj_save(int n, int k, const double *a, double *row, double *col) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    row[i] = a[(long)k * n + i];
+    col[i] = a[(long)i * n + k];
+  }
+}
+__global__ void k_gj_step(int n, int k, double *a, const double *row, const double *col) {
+  const double piv = row[k];
+  const long total = (long)n * n;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(it / n), j = (int)(it - (long)i * n);
+    double v;
+    if (i == k)
+      v = j == k ? 1.0 / piv : row[j] / piv;
+    else
+      v = j == k ? -col[i] / piv : a[it] - col[i] * (row[j] / piv);
+    a[it] = v;
+  }
+}
+__global__ void k_zero_cols(int n, double *a, const int *cols, int ncols) {
+  const long total = (long)n * ncols;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int r = (int)(it / ncols), q = (int)(it - (long)r * ncols);
+    a[(long)r * n + cols[q]] = 0.0;
+  }
+}
+
+__global__ void k_to_f32(long n, const double *src, float *dst) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+void MacGpu::ensure_fast_buffers() {
+  if (fast_ready_) return;
+  const int nd = tt_.ndim, nbk = tt_.num_blocks;
+  const size_t nc = (size_t)nbk * ncell_, nf = (size_t)nbk * nfb_;
+  auto fa = [&](size_t n) {
+    float *p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(float)) != cudaSuccess) fail("out of device memory (fp32)");
+    else cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(float));
+    return p;
+  };
+  for (int d = 0; d < nd; d++) {
+    d_tff32_[d] = fa(nf);
+    d_bcoef32_[d] = fa(nf);
+    d_afrac32_[d] = fa(nf);
+  }
+  d_vf32_ = fa(nc);
+  d_geom32_ = fa((size_t)nbk * 8);
+  d_resid32_ = fa(nc);
+  d_corr32_ = fa(nc);
+  if (cudaMalloc(&d_st_, sizeof(FState)) != cudaSuccess) fail("alloc state");
+  if (cudaMallocHost(&h_st_, sizeof(FState)) != cudaSuccess) fail("alloc pinned state");
+  if (cudaMalloc(&d_part_, sizeof(double) * kMaxRedBlocks * 4) != cudaSuccess) fail("alloc partials");
+  if (cudaMalloc(&d_cnt_, sizeof(unsigned) * 4) != cudaSuccess) fail("alloc counter");
+  cudaMemset(d_cnt_, 0, sizeof(unsigned) * 4);
+  c32_.geom = d_geom32_;
+  for (int d = 0; d < 3; d++) {
+    const int dd = d < nd ? d : 0;
+    c32_.tff[d] = d_tff32_[dd];
+    c32_.bcoef[d] = d_bcoef32_[dd];
+    c32_.afrac[d] = d_afrac32_[dd];
+  }
+  c32_.vf = d_vf32_;
+  fast_ready_ = true;
+}
+
+// FP32 copies of the coefficients for the FP32 V-cycle
+void MacGpu::refresh_fp32() {
+  const int nd = tt_.ndim, nbk = tt_.num_blocks;
+  const long nc = (long)nbk * ncell_, nf = (long)nbk * nfb_;
+  for (int d = 0; d < nd; d++) {
+    k_to_f32<<<ew_grid(nf), kTPB, 0, stream_>>>(nf, d_tff_[d], d_tff32_[d]);
+    k_to_f32<<<ew_grid(nf), kTPB, 0, stream_>>>(nf, d_bcoef_[d], d_bcoef32_[d]);
+    k_to_f32<<<ew_grid(nf), kTPB, 0, stream_>>>(nf, d_afrac_[d], d_afrac32_[d]);
+  }
+  k_to_f32<<<ew_grid(nc), kTPB, 0, stream_>>>(nc, d_vf_, d_vf32_);
+  k_to_f32<<<ew_grid((long)nbk * 8), kTPB, 0, stream_>>>((long)nbk * 8, d_geom_, d_geom32_);
+  c32_.alpha = (float)alpha_;
+  c32_.beta = (float)beta_;
+}
+
+// Dense FP64 inverse of the level-1 operator (tower 1 = every level-1 block,
+// faces FINE_FINE or FINE_BC only), rows in tower order, cells in block order.
+void MacGpu::build_bottom() {
+  const int nd = tt_.ndim, nb = tt_.nb;
+  const std::vector<int> &B1 = towers_[1].blocks;
+  const int nblk1 = (int)B1.size();
+  const int n = nblk1 * ncell_;
+  n_bot_ = n;
+  if (n == 0) return;
+  if ((double)n * n * 8 > 4.0e9) {
+    fail("level-1 problem too large for the dense bottom solve");
+    return;
+  }
+  std::vector<int> pos(tt_.num_blocks, -1);
+  for (int p = 0; p < nblk1; p++) pos[B1[p]] = p;
+  std::vector<double> A((size_t)n * n, 0.0);
+  std::vector<int> dir_touch(n, 0);
+  // adjacency for the connected components (face coefficient > 0)
+  std::vector<std::vector<int>> adj(n);
+  auto fidx = [&](int d, const int ijk[3], int s) {
+    int f[3] = {ijk[0], ijk[1], ijk[2]};
+    f[d] += s;
+    const int e0 = nb + (d == 0), e1 = nb + (d == 1);
+    return f[0] + e0 * (f[1] + e1 * f[2]);
+  };
+  for (int p = 0; p < nblk1; p++) {
+    const int b = B1[p];
+    const double dv = geom_[b * 8 + 6];
+    for (int c = 0; c < ncell_; c++) {
+      const int row = p * ncell_ + c;
+      int ijk[3] = {c % nb, nd >= 2 ? (c / nb) % nb : 0, nd == 3 ? c / (nb * nb) : 0};
+      const double vf = vf_[(size_t)b * ncell_ + c];
+      if (!(vf > 0)) {
+        A[(size_t)row * n + row] = 1.0;
+        continue;
+      }
+      double diag = 0.0;
+      for (int f = 0; f < 2 * nd; f++) {
+        const int d = f >> 1, s = f & 1;
+        const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+        const int fx = fidx(d, ijk, s);
+        double T = beta_ * geom_[b * 8 + 3 + d] / geom_[b * 8 + d];
+        T = T * bcoef_[d][(size_t)b * nfb_ + fx];
+        T = T * afrac_[d][(size_t)b * nfb_ + fx];
+        int ncol = -1;
+        if (!bnd) {
+          int q[3] = {ijk[0], ijk[1], ijk[2]};
+          q[d] += s ? 1 : -1;
+          ncol = p * ncell_ + (q[0] + nb * (q[1] + nb * q[2]));
+        } else {
+          const int nbr = tt_.neighbor[b * 6 + f];
+          if (nbr >= 0) {
+            if (pos[nbr] < 0) {
+              fail("level-1 neighbour outside tower 1");
+              return;
+            }
+            int q[3] = {ijk[0], ijk[1], ijk[2]};
+            q[d] = s ? 0 : nb - 1;
+            ncol = pos[nbr] * ncell_ + (q[0] + nb * (q[1] + nb * q[2]));
+          } else {
+            const int bct = bc_type_[b * 6 + f];
+            if (bct == kBCNeumann) T = 0.0;
+            else {
+              T = 2.0 * T;
+              if (T > 0) dir_touch[row] = 1;
+            }
+          }
+        }
+        diag += T;
+        if (ncol >= 0) {
+          A[(size_t)row * n + ncol] -= T / dv / vf;
+          if (T > 0) adj[row].push_back(ncol);
+        }
+      }
+      A[(size_t)row * n + row] += diag / dv / vf;
+    }
+  }
+  // pin one cell of every fluid component that has no Dirichlet face
+  std::vector<int> comp(n, -1), pins;
+  for (int r0 = 0; r0 < n; r0++) {
+    const int b = B1[r0 / ncell_];
+    if (comp[r0] >= 0 || !(vf_[(size_t)b * ncell_ + r0 % ncell_] > 0)) continue;
+    std::vector<int> stack{r0};
+    comp[r0] = r0;
+    bool dirichlet = false;
+    while (!stack.empty()) {
+      const int r = stack.back();
+      stack.pop_back();
+      dirichlet |= dir_touch[r] != 0;
+      for (int q : adj[r])
+        if (comp[q] < 0) {
+          comp[q] = r0;
+          stack.push_back(q);
+        }
+    }
+    if (!dirichlet) {
+      for (int j = 0; j < n; j++) A[(size_t)r0 * n + j] = 0.0;
+      A[(size_t)r0 * n + r0] = 1.0;
+      pins.push_back(r0);
+    }
+  }
+  if (d_binv_) cudaFree(d_binv_);
+  d_binv_ = nullptr;
+  if (cudaMalloc(&d_binv_, (size_t)n * n * sizeof(double)) != cudaSuccess) {
+    fail("out of device memory (bottom inverse)");
+    return;
+  }
+  double *row = nullptr, *col = nullptr;
+  int *dpins = nullptr;
+  CK_(cudaMalloc(&row, n * sizeof(double)));
+  CK_(cudaMalloc(&col, n * sizeof(double)));
+  CK_(cudaMemcpyAsync(d_binv_, A.data(), (size_t)n * n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  const long nn = (long)n * n;
+  for (int k = 0; k < n; k++) {
+    k_gj_save<<<(n + kTPB - 1) / kTPB, kTPB, 0, stream_>>>(n, k, d_binv_, row, col);
+    k_gj_step<<<ew_grid(nn), kTPB, 0, stream_>>>(n, k, d_binv_, row, col);
+  }
+  if (!pins.empty()) {
+    CK_(cudaMalloc(&dpins, pins.size() * sizeof(int)));
+    CK_(cudaMemcpyAsync(dpins, pins.data(), pins.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    k_zero_cols<<<ew_grid((long)n * pins.size()), kTPB, 0, stream_>>>(n, d_binv_, dpins, (int)pins.size());
+  }
+  CK_(cudaStreamSynchronize(stream_));
+  cudaFree(row);
+  cudaFree(col);
+  if (dpins) cudaFree(dpins);
+  n_pins_ = (int)pins.size();
+  bottom_ready_ = true;
+}
+
+// one V-cycle with zero initial guess in precision T; the input residual
+// (masked rhs) is already in `resid`, the result goes to `out` (FP64)
+template <typename T>
+void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *out) {
+  const int *guard = &d_st_->done;
+  for (int l = L; l >= 2; l--) {
+    if (l - 1 >= tt_.max_level || levels_[l - 1].n == 0 || levels_[l].n == 0) continue;
+    launch_restrict<T>(topo_, c, nonleaf_list(l - 1), resid, guard, stream_);
+  }
+  // dense bottom solve on level 1
+  const int rows_per_cta = kTPB / 32;
+  const size_t smem = (size_t)n_bot_ * sizeof(double);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_bottom_gemv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_bottom_gemv<T><<<(n_bot_ + rows_per_cta - 1) / rows_per_cta, kTPB, smem, stream_>>>(
+      n_bot_, d_binv_, towers_[1].all.blocks, ncell_, resid, corr, d_st_);
+  for (int l = 2; l <= L; l++) {
+    if (levels_[l].n == 0) continue;
+    launch_prolong<T>(topo_, c, level_list(l), corr, guard, stream_);
+    for (int s = 0; s < prm_.n_post; s++) {
+      for (int ll = l; ll >= 1; ll--) {
+        BlockList sl = sublevel_list(l, ll);
+        if (sl.n == 0) break;
+        for (int rb = 0; rb < 2; rb++) launch_smooth<T>(topo_, c, sl, rb, corr, resid, guard, stream_);
+      }
+    }
+  }
+  BlockList TL = tower_list(L);
+  k_vc_out<T><<<ew_grid((long)TL.n * ncell_), kTPB, 0, stream_>>>(TL, ncell_, d_st_, corr, out);
+}
+
+template <typename T>
+void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
+  const int L = finest_;
+  BlockList TL = tower_list(L);
+  const long w = (long)TL.n * ncell_;
+  double *R = vec_[kR], *RHAT = vec_[kRHAT], *P = vec_[kP], *PH = vec_[kPHAT], *S = vec_[kS], *SH = vec_[kSHAT];
+  double *V = vec_[kV], *Tt = vec_[kT], *X = vec_[kX];
+  k_pupdate<T><<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, R, P, V, d_vf_, resid);
+  vcycle_device<T>(L, resid, corr, c, PH);
+  if (tt_.ndim == 2)
+    k_apply_red<2, 0><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, PH, V, RHAT, d_st_, d_part_, d_cnt_);
+  else
+    k_apply_red<3, 0><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, PH, V, RHAT, d_st_, d_part_, d_cnt_);
+  k_supdate<T><<<red_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, R, V, S, X, PH, d_vf_, resid, d_part_, d_cnt_);
+  vcycle_device<T>(L, resid, corr, c, SH);
+  if (tt_.ndim == 2)
+    k_apply_red<2, 1><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, SH, Tt, S, d_st_, d_part_, d_cnt_);
+  else
+    k_apply_red<3, 1><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, SH, Tt, S, d_st_, d_part_, d_cnt_);
+  k_rupdate<<<red_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, X, SH, R, S, Tt, RHAT, d_part_, d_cnt_);
+}
+
+void MacGpu::capture_loop(int precision) {
+  if (graph_exec_) {
+    cudaGraphExecDestroy(graph_exec_);
+    graph_exec_ = nullptr;
+  }
+  if (graph_) {
+    cudaGraphDestroy(graph_);
+    graph_ = nullptr;
+  }
+  CK_(cudaGraphCreate(&graph_, 0));
+  cudaGraphConditionalHandle h;
+  CK_(cudaGraphConditionalHandleCreate(&h, graph_, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK_(cudaGraphAddNode(&node, graph_, nullptr, nullptr, 0, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  CK_(cudaStreamBeginCaptureToGraph(stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  if (precision == 1)
+    iteration_device<float>(d_resid32_, d_corr32_, c32_);
+  else
+    iteration_device<double>(vec_[kRESID], vec_[kCORR], c64_);
+  k_set_cond<<<1, 1, 0, stream_>>>(h, d_st_);
+  cudaGraph_t out = nullptr;
+  CK_(cudaStreamEndCapture(stream_, &out));
+  // count the kernel nodes of one iteration (reported as launches per step)
+  size_t nn = 0;
+  CK_(cudaGraphGetNodes(body, nullptr, &nn));
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn) CK_(cudaGraphGetNodes(body, nodes.data(), &nn));
+  kernels_per_iter_ = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType ty;
+    if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) kernels_per_iter_++;
+  }
+  CK_(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+  graph_prec_ = precision;
+  graph_npost_ = prm_.n_post;
+}
+
+int MacGpu::cg_solve_device(SolveInfo *info) {
+  ensure_fast_buffers();
+  if (!err_.empty()) return -1;
+  if (coef_version_ != fast_coef_version_) {
+    refresh_fp32();
+    build_bottom();
+    fast_coef_version_ = coef_version_;
+    if (!err_.empty()) return -1;
+  }
+  if (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post) {
+    capture_loop(prm_.precision);
+    if (!err_.empty()) return -1;
+  }
+  const int L = finest_;
+  BlockList TL = tower_list(L);
+  const long w = (long)TL.n * ncell_;
+  auto t0 = std::chrono::steady_clock::now();
+  FState init{};
+  init.tol_rel = prm_.tol_rel;
+  init.tol_abs = prm_.tol_abs;
+  init.max_iter = prm_.max_iter;
+  *h_st_ = init;
+  CKR_(cudaMemcpyAsync(d_st_, h_st_, sizeof(FState), cudaMemcpyHostToDevice, stream_), -1);
+  // prologue: x0 = sol, x = 0, r = rhs - A x0, rhat = r, |r0|, rho
+  k_pro_copy<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, vec_[kSOL], vec_[kX0], vec_[kX]);
+  if (tt_.ndim == 2)
+    k_apply_red<2, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_st_,
+                                                       d_part_, d_cnt_);
+  else
+    k_apply_red<3, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_st_,
+                                                       d_part_, d_cnt_);
+  vcopy(TL, vec_[kRHAT], vec_[kR]);
+  if (prm_.max_iter > 0) CKR_(cudaGraphLaunch(graph_exec_, stream_), -1);
+  k_finish<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, vec_[kX0], vec_[kX], vec_[kSOL]);
+  CKR_(cudaMemcpyAsync(h_st_, d_st_, sizeof(FState), cudaMemcpyDeviceToHost, stream_), -1);
+  CKR_(cudaStreamSynchronize(stream_), -1);
+  info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  const FState &st = *h_st_;
+  info->iterations = st.trivial ? 0 : st.iter;
+  info->rnorm0 = st.rnorm0;
+  info->rnorm = st.rnorm;
+  info->status = st.stat ? 1 : ((st.conv || st.trivial) ? 0 : 2);
+  return st.stat;
+}
+
+// asynchronous solve for benchmarking: everything enqueued on `stream_`,
+// no host synchronisation (the caller times it with events)
+int MacGpu::cg_solve_enqueue() {
+  ensure_fast_buffers();
+  if (!err_.empty() || !graph_exec_ || !bottom_ready_) return -1;
+  const int L = finest_;
+  BlockList TL = tower_list(L);
+  const long w = (long)TL.n * ncell_;
+  FState init{};
+  init.tol_rel = prm_.tol_rel;
+  init.tol_abs = prm_.tol_abs;
+  init.max_iter = prm_.max_iter;
+  *h_st_ = init;
+  CKR_(cudaMemcpyAsync(d_st_, h_st_, sizeof(FState), cudaMemcpyHostToDevice, stream_), -1);
+  k_pro_copy<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, vec_[kSOL], vec_[kX0], vec_[kX]);
+  if (tt_.ndim == 2)
+    k_apply_red<2, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_st_,
+                                                       d_part_, d_cnt_);
+  else
+    k_apply_red<3, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_st_,
+                                                       d_part_, d_cnt_);
+  vcopy(TL, vec_[kRHAT], vec_[kR]);
+  CKR_(cudaGraphLaunch(graph_exec_, stream_), -1);
+  k_finish<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, vec_[kX0], vec_[kX], vec_[kSOL]);
+  return 0;
+}
+
+}  // namespace sayaka_gb300
+
+namespace sayaka_gb300 {
+
+// everything a device-resident solve needs, built ahead of the timed region
+int MacGpu::prepare_device() {
+  ensure_fast_buffers();
+  if (!err_.empty()) return -1;
+  if (coef_version_ != fast_coef_version_) {
+    refresh_fp32();
+    build_bottom();
+    fast_coef_version_ = coef_version_;
+    if (!err_.empty()) return -1;
+  }
+  if (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post) capture_loop(prm_.precision);
+  return err_.empty() ? 0 : -1;
+}
+
+}  // namespace sayaka_gb300
+
+namespace sayaka_gb300 {
+
+int MacGpu::solve_state(SolveInfo *info) {
+  CKR_(cudaMemcpyAsync(h_st_, d_st_, sizeof(FState), cudaMemcpyDeviceToHost, stream_), -1);
+  CKR_(cudaStreamSynchronize(stream_), -1);
+  const FState &st = *h_st_;
+  info->iterations = st.trivial ? 0 : st.iter;
+  info->rnorm0 = st.rnorm0;
+  info->rnorm = st.rnorm;
+  info->status = st.stat ? 1 : ((st.conv || st.trivial) ? 0 : 2);
+  info->seconds = 0;
+  return 0;
+}
+
+int MacGpu::tower_size(int L, int sublevel) const {
+  if (L < 1 || L > tt_.max_level) return -1;
+  const DevTower &t = towers_[L];
+  if (sublevel <= 0) return t.all.n;
+  if (sublevel > L || t.all.n == 0) return 0;
+  return t.end[sublevel] - t.begin[sublevel];
+}
+
+int MacGpu::enqueue_kernel(int which, int L) {
+  if (L < 1 || L > tt_.max_level || towers_[L].all.n == 0) return -1;
+  ensure_fast_buffers();
+  if (which == 0) {
+    launch_apply<double>(topo_, c64_, tower_list(L), vec_[kSOL], vec_[kV], nullptr, nullptr, stream_);
+  } else if (which == 1) {
+    launch_smooth<float>(topo_, c32_, sublevel_list(L, L), 0, d_corr32_, d_resid32_, nullptr, stream_);
+  } else if (which == 2) {
+    launch_smooth<double>(topo_, c64_, sublevel_list(L, L), 0, vec_[kCORR], vec_[kRESID], nullptr, stream_);
+  } else {
+    return -1;
+  }
+  return err_.empty() ? 0 : -1;
+}
+
+}  // namespace sayaka_gb300

@@ -14,22 +14,7 @@
 
 namespace sayaka_gb300 {
 
-#define CK(x)                                                                                   \
-  do {                                                                                          \
-    cudaError_t e_ = (x);                                                                       \
-    if (e_ != cudaSuccess) {                                                                    \
-      fail(std::string(#x) + ": " + cudaGetErrorString(e_));                                   \
-      return;                                                                                   \
-    }                                                                                           \
-  } while (0)
-#define CKR(x, r)                                                                               \
-  do {                                                                                          \
-    cudaError_t e_ = (x);                                                                       \
-    if (e_ != cudaSuccess) {                                                                    \
-      fail(std::string(#x) + ": " + cudaGetErrorString(e_));                                   \
-      return r;                                                                                 \
-    }                                                                                           \
-  } while (0)
+#include "cuda_check.h"
 
 namespace {
 
@@ -338,6 +323,22 @@ MacGpu::~MacGpu() {
   for (auto *v : vec_) fr(v);
   fr(d_red_);
   fr(d_counter_);
+  for (int d = 0; d < 3; d++) {
+    fr(d_tff32_[d]);
+    fr(d_bcoef32_[d]);
+    fr(d_afrac32_[d]);
+  }
+  fr(d_vf32_);
+  fr(d_geom32_);
+  fr(d_resid32_);
+  fr(d_corr32_);
+  fr(d_st_);
+  fr(d_part_);
+  fr(d_cnt_);
+  fr(d_binv_);
+  if (h_st_) cudaFreeHost(h_st_);
+  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  if (graph_) cudaGraphDestroy(graph_);
   if (h_red_) cudaFreeHost(h_red_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -376,6 +377,7 @@ void MacGpu::upload_coefs() {
   }
   CK(cudaMemcpyAsync(d_vf_, vf_.data(), (size_t)nbk * ncell_ * sizeof(double), cudaMemcpyHostToDevice, stream_));
   recompute_face_coef();
+  coef_version_++;
   CK(cudaStreamSynchronize(stream_));
 }
 
@@ -598,6 +600,7 @@ void MacGpu::set_bc_types(const int *bc6) {
       bc_type_[b * 6 + f] = phys ? bc6[b * 6 + f] : -1;
     }
   CK(cudaMemcpy(d_bc_type_, bc_type_.data(), bc_type_.size() * sizeof(int), cudaMemcpyHostToDevice));
+  coef_version_++;
 }
 
 void MacGpu::get_coef(int which, int dir, double *out) const {
@@ -807,6 +810,7 @@ int MacGpu::bicgstab(int L, double *sol, const double *rhs, double tol_rel, doub
 }
 
 int MacGpu::cg_solve(SolveInfo *info) {
+  if (prm_.bottom == 1 && prm_.use_mg_precond) return cg_solve_device(info);
   auto t0 = std::chrono::steady_clock::now();
   const int stat = bicgstab(finest_, vec_[kSOL], vec_[kRHS], prm_.tol_rel, prm_.tol_abs, prm_.max_iter,
                             prm_.use_mg_precond != 0, false, info);

@@ -75,6 +75,14 @@ class MacGpu {
   const SolverParams &params() const { return prm_; }
 
   int cg_solve(SolveInfo *info);
+  // graph-captured device-resident solve (dense bottom); enqueue variant for
+  // timing: no host synchronisation, the result stays on the device
+  int cg_solve_device(SolveInfo *info);
+  int cg_solve_enqueue();
+  int prepare_device();
+  int solve_state(SolveInfo *info);
+  int enqueue_kernel(int which, int L);
+  int tower_size(int L, int sublevel) const;
 
   // building blocks, exposed for parity tests (compact arrays, all blocks)
   void apply(int L, const double *x_all, double *y_all);
@@ -135,6 +143,16 @@ class MacGpu {
 
   void fail(const std::string &m);
 
+  // device-resident path (mac_fast.cu)
+  void ensure_fast_buffers();
+  void refresh_fp32();
+  void build_bottom();
+  template <typename T>
+  void vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *out);
+  template <typename T>
+  void iteration_device(T *resid, T *corr, const Coef<T> &c);
+  void capture_loop(int precision);
+
   TreeTables tt_;
   SolverParams prm_;
   std::string err_;
@@ -165,6 +183,28 @@ class MacGpu {
 
   Topo topo_{};
   Coef<double> c64_{};
+
+  // device-resident path
+  bool fast_ready_ = false, bottom_ready_ = false;
+  long coef_version_ = 1, fast_coef_version_ = 0;
+  float *d_tff32_[3] = {}, *d_bcoef32_[3] = {}, *d_afrac32_[3] = {}, *d_vf32_ = nullptr, *d_geom32_ = nullptr;
+  float *d_resid32_ = nullptr, *d_corr32_ = nullptr;
+  Coef<float> c32_{};
+  FState *d_st_ = nullptr, *h_st_ = nullptr;
+  double *d_part_ = nullptr;
+  unsigned *d_cnt_ = nullptr;
+  double *d_binv_ = nullptr;
+  int n_bot_ = 0, n_pins_ = 0;
+  cudaGraph_t graph_ = nullptr;
+  cudaGraphExec_t graph_exec_ = nullptr;
+  int graph_prec_ = -1, graph_npost_ = -1;
+  int kernels_per_iter_ = 0;
+
+ public:
+  // kernel launches of one captured BiCGSTAB iteration; a device solve
+  // launches kPrologueKernels + iterations * this + kEpilogueKernels
+  int kernels_per_iteration() const { return kernels_per_iter_; }
+  static constexpr int kPrologueKernels = 3, kEpilogueKernels = 1;
 };
 
 }  // namespace sayaka_gb300

@@ -1,0 +1,167 @@
+// Device-side stencil helpers shared by every kernel that evaluates the MAC
+// operator: index arithmetic of the compact block layout and the gathers
+// that replace the reference's ghost-cell fills and coarse/fine flux
+// registers (see mac_kernels.cu for the mapping to the reference).
+#pragma once
+
+#include <cstdint>
+
+#include "mac_device.h"
+
+namespace sayaka_gb300 {
+namespace stencil {
+__device__ __forceinline__ int face_type_of(uint16_t ft, int f) { return (ft >> (2 * f)) & 3; }
+
+template <int ND>
+__device__ __forceinline__ void decode(int c, int nb, int ijk[3]) {
+  ijk[0] = c % nb;
+  ijk[1] = ND >= 2 ? (c / nb) % nb : 0;
+  ijk[2] = ND == 3 ? c / (nb * nb) : 0;
+}
+
+__device__ __forceinline__ int encode(const int ijk[3], int nb) { return ijk[0] + nb * (ijk[1] + nb * ijk[2]); }
+
+// face index of the face on side s of cell ijk in direction d (face-centred
+// valid box of the reference, first dimension fastest)
+__device__ __forceinline__ int face_index(int d, const int ijk[3], int s, int nb) {
+  int f[3] = {ijk[0], ijk[1], ijk[2]};
+  f[d] += s;
+  const int e0 = nb + (d == 0), e1 = nb + (d == 1);
+  return f[0] + e0 * (f[1] + e1 * f[2]);
+}
+
+template <typename T>
+__device__ __forceinline__ T geom(const Coef<T> &c, int b, int q) { return c.geom[b * 8 + q]; }
+
+// coefficient of a coarse/fine face: ((beta*ds)/(dx*h))*B*a
+// (src/SayakaMacOperator.cpp:1155-1161 and :1258-1266)
+template <typename T>
+__device__ __forceinline__ T cf_coef(const Coef<T> &c, const Topo &t, int b, int d, int fidx, T h) {
+  T v = c.beta * geom(c, b, 3 + d) / (geom(c, b, d) * h);
+  v = v * c.bcoef[d][(long)b * t.nfb + fidx];
+  v = v * c.afrac[d][(long)b * t.nfb + fidx];
+  return v;
+}
+
+// CRSE_FINE face: sum of the fine-side contributions T_f * phi_f over the
+// fine faces covering coarse face (d, s) of cell ijk of block b, in the
+// reference's RESTRICT_SUM order (lower transverse dimension fastest)
+template <typename T, int ND>
+__device__ __forceinline__ T crse_fine_sum(const Topo &t, const Coef<T> &c, int b, int f, const int ijk[3],
+                                           const T *__restrict__ x) {
+  const int nb = t.nb, half = nb >> 1;
+  const int d = f >> 1, s = f & 1;
+  const int N = t.neighbor[b * 6 + f];
+  int cidx = (1 - s) << d;
+  int base[3] = {0, 0, 0};
+  int tq[2] = {0, 0}, nt = 0;
+  for (int q = 0; q < ND; q++) {
+    if (q == d) continue;
+    const int sq = ijk[q] >= half ? 1 : 0;
+    cidx |= sq << q;
+    base[q] = 2 * (ijk[q] - sq * half);
+    tq[nt++] = q;
+  }
+  const int F = t.child[N * 8 + cidx];
+  int fi[3];
+  fi[d] = s == 1 ? 0 : nb - 1;
+  const int fside = s == 1 ? 0 : 1;  // the fine block's face toward b
+  const T h15 = (T)1.5;
+  T val = 0;
+  const int n1 = ND == 3 ? 2 : 1;
+  for (int a1 = 0; a1 < n1; a1++) {
+    for (int a0 = 0; a0 < 2; a0++) {
+      fi[tq[0]] = base[tq[0]] + a0;
+      if (ND == 3) fi[tq[1]] = base[tq[1]] + a1;
+      if (ND == 2) fi[2] = 0;
+      const int fx = face_index(d, fi, fside, nb);
+      const T tf = cf_coef(c, t, F, d, fx, h15);
+      val += tf * x[(long)F * t.ncell + encode(fi, nb)];
+    }
+  }
+  return val;
+}
+
+// value a FINE_CRSE ghost cell holds: the coarse leaf's boundary cell
+// (injection through the parent's ghost layer)
+template <typename T, int ND>
+__device__ __forceinline__ T fine_crse_ghost(const Topo &t, int b, int f, const int ijk[3], const T *__restrict__ x) {
+  const int nb = t.nb, half = nb >> 1;
+  const int d = f >> 1, s = f & 1;
+  const int C = t.fc_neigh[b * 6 + f];
+  const int wc = t.which_child[b];
+  int ci[3] = {0, 0, 0};
+  for (int q = 0; q < ND; q++) {
+    if (q == d)
+      ci[q] = s == 1 ? 0 : nb - 1;
+    else
+      ci[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
+  }
+  return x[(long)C * t.ncell + encode(ci, nb)];
+}
+
+// mirrored boundary cell of the same-level neighbour
+template <typename T>
+__device__ __forceinline__ T same_level_ghost(const Topo &t, int b, int f, const int ijk[3], const T *__restrict__ x) {
+  const int d = f >> 1, s = f & 1;
+  const int n = t.neighbor[b * 6 + f];
+  int ni[3] = {ijk[0], ijk[1], ijk[2]};
+  ni[d] = s == 1 ? 0 : t.nb - 1;
+  return x[(long)n * t.ncell + encode(ni, t.nb)];
+}
+
+
+// operator value of cell ci of block b: (phi_c*sum T - sum T*phi_nb)/dv/vf,
+// 0 on cells with vf = 0 (src/SayakaMacOperator.cpp:1325-1459)
+template <typename T, int ND>
+__device__ __forceinline__ T apply_cell(const Topo &t, const Coef<T> &c, int b, uint16_t ft, int ci,
+                                        const T *__restrict__ x) {
+  const int nb = t.nb;
+  int ijk[3];
+  decode<ND>(ci, nb, ijk);
+  const long cb = (long)b * t.ncell;
+  const T dv = geom(c, b, 6);
+  const T phic = x[cb + ci];
+  T diag = c.alpha * dv;
+  T off = 0;
+#pragma unroll
+  for (int f = 0; f < 2 * ND; f++) {
+    const int d = f >> 1, s = f & 1;
+    const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+    const int fx = face_index(d, ijk, s, nb);
+    T coef, val;
+    if (!bnd) {
+      coef = c.tff[d][(long)b * t.nfb + fx];
+      const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+      val = coef * x[cb + ci + (s ? stride : -stride)];
+    } else {
+      const int ty = face_type_of(ft, f);
+      if (ty == 0) {  // FINE_FINE
+        coef = c.tff[d][(long)b * t.nfb + fx];
+        val = coef * same_level_ghost(t, b, f, ijk, x);
+      } else if (ty == 1) {  // FINE_BC
+        if (t.bc_type[b * 6 + f] == kBCNeumann) {
+          coef = 0;
+          val = 0;
+        } else {
+          coef = c.tff[d][(long)b * t.nfb + fx];
+          val = -coef * phic;
+        }
+      } else if (ty == 2) {  // FINE_CRSE
+        coef = cf_coef(c, t, b, d, fx, (T)1.5);
+        val = coef * fine_crse_ghost<T, ND>(t, b, f, ijk, x);
+      } else {  // CRSE_FINE
+        coef = cf_coef(c, t, b, d, fx, (T)0.75);
+        val = crse_fine_sum<T, ND>(t, c, b, f, ijk, x);
+      }
+    }
+    diag += coef;
+    off += val;
+  }
+  const T lphi = (phic * diag - off) / dv;
+  const T vfv = c.vf[cb + ci];
+  return vfv > 0 ? lphi / vfv : (T)0;
+}
+
+}  // namespace stencil
+}  // namespace sayaka_gb300

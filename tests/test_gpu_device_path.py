@@ -1,0 +1,65 @@
+"""Device-resident solve path (device scalars, CUDA-graph WHILE loop, dense
+FP64 bottom solve, FP64 or FP32 V-cycle) against the reference solutions and
+the C oracle."""
+import numpy as np
+import pytest
+
+import golden_io
+from cases import CASES, build_tree
+from test_gpu_parity import block_slice, setup_solver, solution_error
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_device_solve_matches_reference(name, precision):
+    g, t, tb, S = setup_solver(name)
+    S.set_rhs_compact(g["sv_rhs"])
+    S.set_zero_sol()
+    S.set_params(tol_rel=1e-11, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=precision, bottom=1)
+    info = S.cg_solve()
+    assert info["status"] == 0, info
+    blocks, _ = t.tower(tb["level"].max())
+    sol = block_slice(S.get_sol_compact(), blocks, S.ncell)
+    err = solution_error(name, tb, S, blocks, sol, g["sv_sol"])
+    assert err < 1e-8, (name, precision, err, info)
+
+
+def test_async_solve_and_info():
+    g, t, tb, S = setup_solver("t2s")
+    S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=1, bottom=1)
+    S.prepare()
+    S.set_rhs_compact(g["sv_rhs"])
+    for _ in range(2):
+        S.set_zero_sol()
+        S.cg_solve_async()
+        info = S.solve_info()
+        assert info["status"] == 0 and info["iterations"] > 0, info
+        assert info["rnorm"] < 1e-10 * info["rnorm0"]
+
+
+def test_device_path_matches_oracle_on_workload():
+    """config-1 workload: device-resident FP32/FP64 solves against the C
+    oracle's converged solve of the same problem"""
+    from oracle import pyoracle
+    from sayakaamr_gb300 import workloads
+    p = workloads.config1()
+    S = workloads.make_solver(p)
+    vf, af, bc = pyoracle.setup_coefficients(p.tables, p.bc, p.vol, p.area, p.bface)
+    O = pyoracle.Oracle(p.tables, p.bc, vf, af, bc)
+    ref, oinfo = O.cg_solve(p.rhs, pyoracle.params(tol_rel=1e-11, tol_abs=0.0, bot_tol_rel=1e-10, bot_tol_abs=0.0))
+    assert oinfo["status"] == 0, oinfo
+    leaf = p.leaf
+    nc = p.ncell
+    w = np.repeat(np.prod(p.tables["block_len"].reshape(-1, 3)[leaf, :2] / p.nb, axis=1), nc)
+    for precision in (0, 1):
+        S.set_zero_sol()
+        S.set_params(tol_rel=1e-11, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=precision, bottom=1)
+        info = S.cg_solve()
+        assert info["status"] == 0, info
+        a = S.get_sol_compact().reshape(-1, nc)[leaf].reshape(-1)
+        r = ref.reshape(-1, nc)[leaf].reshape(-1)
+        a = a - np.sum(a * w) / np.sum(w)
+        r = r - np.sum(r * w) / np.sum(w)
+        assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-8, (precision, info)

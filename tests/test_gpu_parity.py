@@ -19,44 +19,7 @@ pytestmark = pytest.mark.gpu
 OPS = [n for n in sorted(CASES) if CASES[n]["do_ops"]]
 
 
-def _frac(c, pts, h):
-    nd = len(pts)
-    d2 = np.zeros_like(pts[0])
-    for d in range(nd):
-        d2 = d2 + (pts[d] - c["ibc"][d]) * (pts[d] - c["ibc"][d])
-    s = (np.sqrt(d2) - c["ibr"]) / h + 0.5
-    s = np.clip(s, 0.0, 1.0)
-    return np.floor(s * 64.0) / 64.0
-
-
-def fractional_ib(name, tb):
-    """leaf IB fractions exactly as ProbeSolver::injectIBFrac computes them"""
-    c = CASES[name]
-    nd, nb, n = tb["ndim"], tb["nb"], tb["num_blocks"]
-    lo = tb["block_lo"].reshape(n, 3)
-    dx = tb["block_len"].reshape(n, 3).copy()
-    dx[:, :nd] = dx[:, :nd] / nb
-    vol = np.zeros((n,) + (nb,) * nd)
-    areas = []
-    # cell centres, [k][j][i] order
-    grids = np.meshgrid(*[np.arange(nb)] * nd, indexing="ij")[::-1]  # i, j, (k)
-    for b in range(n):
-        pts = [lo[b, d] + (grids[d] + 0.5) * dx[b, d] for d in range(nd)]
-        vol[b] = _frac(c, pts, dx[b, 0])
-    for fd in range(nd):
-        ext = [nb + (d == fd) for d in range(nd)]
-        g = np.meshgrid(*[np.arange(e) for e in ext[::-1]], indexing="ij")[::-1]
-        a = np.zeros((n,) + tuple(ext[::-1]))
-        for b in range(n):
-            pts = []
-            for d in range(nd):
-                x = lo[b, d] + (g[d] + 0.5) * dx[b, d]
-                if d == fd:
-                    x = x - 0.5 * dx[b, d]
-                pts.append(x)
-            a[b] = _frac(c, pts, dx[b, 0])
-        areas.append(a.reshape(-1))
-    return vol.reshape(-1), areas
+from test_gpu_parity_helpers import fractional_ib  # noqa: E402
 
 
 def setup_solver(name):
@@ -244,13 +207,16 @@ def test_solve_matches_reference(name):
     V-cycle's bottom solve runs to a relative 1e-8 here: with the reference's
     default absolute 1e-6 bottom tolerance the preconditioner degrades as the
     outer residual falls and the outer iteration count becomes erratic (the
-    reference needs 290 iterations on c1 with its own rounding)."""
+    reference needs 290 iterations on c1 with its own rounding).  A small
+    absolute floor stays: on singular (all-Neumann) problems the restricted
+    residual is compatible only to rounding, which a purely relative bottom
+    tolerance eventually cannot meet."""
     g, t, tb, S = setup_solver(name)
     c = CASES[name]
     S.set_rhs_compact(g["sv_rhs"])
     S.set_zero_sol()
     S.set_params(tol_rel=min(c["tol_rel"], 1e-11), tol_abs=0.0, use_mg_precond=1, max_iter=2000, precision=0,
-                 bottom=0, bot_tol_rel=1e-8, bot_tol_abs=0.0)
+                 bottom=0, bot_tol_rel=1e-8, bot_tol_abs=1e-13)
     info = S.cg_solve()
     assert info["status"] == 0, info
     blocks, _ = t.tower(tb["level"].max())

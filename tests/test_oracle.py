@@ -120,3 +120,19 @@ def test_solve_bit_exact(name):
     assert info["status"] == 0
     leaf = t.tower(tb["level"].max())[0]
     assert exact(rows(sol, leaf, O.ncell), g["sv_sol"]), name
+
+
+@pytest.mark.parametrize("name", ["t2s", "t3s"])
+def test_coefficient_setup(name):
+    """setCoefB / IB-fraction sync + restriction against the reference"""
+    from test_gpu_parity_helpers import fractional_ib
+    g = golden_io.load(name)
+    t = build_tree(name)
+    tb = t.tables()
+    vol, areas = fractional_ib(name, tb)
+    nd = tb["ndim"]
+    vf, af, bc = pyoracle.setup_coefficients(tb, bc_table(name, tb), vol, areas, [g["in_b%d" % d] for d in range(nd)])
+    assert exact(vf, g["vf"])
+    for d in range(nd):
+        assert exact(af[d], g["af%d" % d]), d
+        assert exact(bc[d], g["bcoef%d" % d]), d
