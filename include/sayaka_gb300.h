@@ -107,6 +107,14 @@ typedef struct sayaka_params {
   int32_t precision;      /* 0: FP64 V-cycle; 1: FP32 V-cycle inside the FP64 outer solve */
   int32_t bottom;         /* 0: BiCGSTAB bottom (reference); 1: dense direct bottom solve */
   int32_t verbose;
+  int32_t graph;          /* device path: 1 = CUDA graph with a WHILE node (default), 0 = the same
+                             kernels launched from a host loop (for per-kernel profilers) */
+  int32_t vcycle_kernel;  /* device path: 0 = one launch per restriction / smoother / prolongation phase,
+                             1 = the whole V-cycle as one cooperative launch,
+                             2 = restriction and smoothing phases inside one thread-block cluster */
+  int32_t pdl;            /* device path: 1 = programmatic dependent launch between kernels (default 0) */
+  int32_t cluster_cells;  /* vcycle_kernel 2: runs of consecutive phases that each touch at most this many
+                             cells share one cluster launch; larger phases get their own launch (16384) */
 } sayaka_params;
 
 typedef struct sayaka_solve_info {

@@ -677,6 +677,63 @@ static void run_case(const Case &c, const char *outdir, int cap) {
 	}
 }
 
+// moving-circle regrid sequence (refine near the interface, coarsen away from
+// it), tables dumped after every regrid -- exercises coarsenBlocks' packing
+static void run_regrid_case(const char *outdir, const std::string &name) {
+  std::string path = std::string(outdir) + "/" + name + ".bin";
+  Dump D(path.c_str());
+  Case c;
+  c.name = name;
+  c.nroot[0] = 3;
+  c.nroot[1] = 2;
+  c.hi[0] = 1.5;
+  c.hi[1] = 1.0;
+  if (NDIM == 3) c.hi[2] = 1.0;
+  c.nb = 4;
+  c.minlevel = 2;
+  c.maxlevel = NDIM == 3 ? 4 : 6;
+  c.rr = 0.22;
+  AmrTree tree;
+  c.rc[0] = 0.35;
+  c.rc[1] = 0.45;
+  c.rc[2] = 0.5;
+  build_tree(c, tree, 20000);
+  D.scalar_i("steps", 6);
+  for (int step = 0; step < 6; step++) {
+    c.rc[0] += 0.11;
+    c.rc[1] += 0.03 * (step % 2 ? -1 : 1);
+    for (int pass = 0; pass < c.maxlevel; pass++) {
+      for (int i = 0; i < tree.numBlocks; i++) {
+        tree.refineFlag[i] = 0;
+        tree.coarsenFlag[i] = 0;
+        if (!tree[i].isLeaf()) continue;
+        const bool near = block_straddles(c, tree[i]);
+        if (near && tree[i].getLevel() < c.maxlevel) tree.refineFlag[i] = 1;
+        if (!near && tree[i].getLevel() > c.minlevel) tree.coarsenFlag[i] = 1;
+      }
+      tree.regrid();
+    }
+    std::vector<int> level(tree.numBlocks), nbr(tree.numBlocks * 6), ch(tree.numBlocks * 8), par(tree.numBlocks);
+    std::vector<int> sb(tree.numBlocks * 27);
+    for (int i = 0; i < tree.numBlocks; i++) {
+      level[i] = tree[i].refineLevel;
+      par[i] = tree[i].parent;
+      for (int f = 0; f < 6; f++) nbr[i * 6 + f] = tree[i].neighbor[f];
+      for (int q = 0; q < 8; q++) ch[i * 8 + q] = tree[i].child[q];
+      for (int kk = 0; kk < 3; kk++)
+        for (int jj = 0; jj < 3; jj++)
+          for (int ii = 0; ii < 3; ii++) sb[i * 27 + ii + 3 * jj + 9 * kk] = tree.surrBlocks[i].blocks[ii][jj][kk];
+    }
+    const std::string p = "step_" + std::to_string(step) + "_";
+    D.i32(p + "level", level);
+    D.i32(p + "neighbor", nbr);
+    D.i32(p + "child", ch);
+    D.i32(p + "parent", par);
+    D.i32(p + "surr_blocks", sb);
+  }
+  fprintf(stderr, "[%s] blocks=%d\n", name.c_str(), tree.numBlocks);
+}
+
 // ---------------------------------------------------------------------------
 static Case make_case(const std::string &name) {
 	Case c;
@@ -746,6 +803,10 @@ int main(int argc, char **argv) {
 		return 2;
 	}
 	for (int a = 2; a < argc; a++) {
+		if (std::string(argv[a]).rfind("rg", 0) == 0) {
+			run_regrid_case(argv[1], argv[a]);
+			continue;
+		}
 		Case c = make_case(argv[a]);
 		run_case(c, argv[1], 20000);
 	}

@@ -36,7 +36,9 @@ class Params(C.Structure):
     _fields_ = [("max_iter", C.c_int32), ("tol_rel", C.c_double), ("tol_abs", C.c_double),
                 ("n_post_smooth", C.c_int32), ("use_mg_precond", C.c_int32), ("bot_tol_rel", C.c_double),
                 ("bot_tol_abs", C.c_double), ("bot_max_iter", C.c_int32), ("precision", C.c_int32),
-                ("bottom", C.c_int32), ("verbose", C.c_int32)]
+                ("bottom", C.c_int32), ("verbose", C.c_int32), ("graph", C.c_int32),
+                ("vcycle_kernel", C.c_int32), ("pdl", C.c_int32),
+                ("cluster_cells", C.c_int32)]
 
 
 class SolveInfo(C.Structure):

@@ -289,6 +289,10 @@ void sayaka_params_default(sayaka_params *p) {
   p->precision = d.precision;
   p->bottom = d.bottom;
   p->verbose = d.verbose;
+  p->graph = d.graph;
+  p->vcycle_kernel = d.vcycle_kernel;
+  p->pdl = d.pdl;
+  p->cluster_cells = d.cluster_cells;
 }
 
 int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
@@ -498,6 +502,10 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.precision = p->precision;
     s.bottom = p->bottom;
     s.verbose = p->verbose;
+    s.graph = p->graph;
+    s.vcycle_kernel = p->vcycle_kernel;
+    s.pdl = p->pdl;
+    s.cluster_cells = p->cluster_cells;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
   });

@@ -59,27 +59,39 @@ struct FState {
   int trivial;  // zero initial residual
 };
 
+// one phase of the cooperative V-cycle program (mac_vcycle.cu)
+enum PhaseOp { kPhaseRestrict = 0, kPhaseBottom = 1, kPhaseProlong = 2, kPhaseSmooth = 3, kPhaseOut = 4 };
+struct VPhase {
+  int op;
+  int color;
+  int n;
+  int pad;
+  const int *blocks;
+  const uint16_t *ftypes;
+};
+
 // ---- launchers (mac_kernels.cu) ----
 template <typename T>
 void launch_face_coef(const Topo &t, const double *geom64, const T *bcoef[3], const T *afrac[3],
                       double beta, T *tff[3], cudaStream_t s);
 
+// pdl: launch with Programmatic Dependent Launch (see launch.cuh)
 template <typename T>
 void launch_apply(const Topo &t, const Coef<T> &c, const BlockList &L, const T *x, T *y,
                   const T *rhs /*null: y = Ax; else y = rhs - Ax (masked)*/, const int *guard,
-                  cudaStream_t s);
+                  cudaStream_t s, bool pdl = false);
 
 template <typename T>
 void launch_smooth(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi,
-                   const T *rhs, const int *guard, cudaStream_t s);
+                   const T *rhs, const int *guard, cudaStream_t s, bool pdl = false);
 
 template <typename T>
 void launch_restrict(const Topo &t, const Coef<T> &c, const BlockList &crse, T *phi,
-                     const int *guard, cudaStream_t s);
+                     const int *guard, cudaStream_t s, bool pdl = false);
 
 template <typename T>
 void launch_prolong(const Topo &t, const Coef<T> &c, const BlockList &fine, T *phi,
-                    const int *guard, cudaStream_t s);
+                    const int *guard, cudaStream_t s, bool pdl = false);
 
 void launch_flux(const Topo &t, const Coef<double> &c, const BlockList &L, int dir,
                  const double *phi, double *flux, cudaStream_t s);

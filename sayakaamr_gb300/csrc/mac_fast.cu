@@ -19,6 +19,7 @@
 #include "mac_solver.h"
 #include "cuda_check.h"
 #include "mac_stencil.cuh"
+#include "launch.cuh"
 
 namespace sayaka_gb300 {
 
@@ -194,11 +195,13 @@ struct EpiEnd {  // |r|, rhat.r of the next iteration
 
 // ---- kernels -------------------------------------------------------------
 __global__ void k_set_cond(cudaGraphConditionalHandle h, const FState *st) {
+  pdl_enter();
   cudaGraphSetConditional(h, st->done ? 0u : 1u);
 }
 
 // x0 = sol, x = 0 on the tower
 __global__ void k_pro_copy(BlockList L, int ncell, const double *sol, double *x0, double *x) {
+  pdl_enter();
   const long total = (long)L.n * ncell;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const long q = cell_of(L, ncell, it);
@@ -212,6 +215,7 @@ __global__ void k_pro_copy(BlockList L, int ncell, const double *sol, double *x0
 template <typename T>
 __global__ void k_pupdate(BlockList L, int ncell, const FState *st, const double *r, double *p, const double *v,
                           const double *vf, T *resid) {
+  pdl_enter();
   if (st->done) return;
   const bool first = st->iter == 1;
   const double beta = st->beta, om = st->omega;
@@ -235,6 +239,7 @@ template <typename T>
 __global__ void __launch_bounds__(kTPB) k_supdate(BlockList L, int ncell, FState *st, const double *r, const double *v,
                                                 double *s, double *x, const double *phat, const double *vf, T *resid,
                                                 double *partials, unsigned *counter) {
+  pdl_enter();
   if (st->done) return;
   const double a = st->alpha;
   double m[1] = {0.0};
@@ -254,6 +259,7 @@ __global__ void __launch_bounds__(kTPB) k_supdate(BlockList L, int ncell, FState
 __global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, FState *st, double *x, const double *shat,
                                                 double *r, const double *s, const double *t, const double *rhat,
                                                 double *partials, unsigned *counter) {
+  pdl_enter();
   if (st->done) return;
   const double om = st->omega;
   double m[2] = {0.0, 0.0};
@@ -271,6 +277,7 @@ __global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, FState
 
 // after the loop: x0 += x ; sol = x0 when converged
 __global__ void k_finish(BlockList L, int ncell, const FState *st, double *x0, const double *x, double *sol) {
+  pdl_enter();
   if (!st->conv) return;
   const long total = (long)L.n * ncell;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
@@ -284,6 +291,7 @@ __global__ void k_finish(BlockList L, int ncell, const FState *st, double *x0, c
 // phat (FP64) = SOL(=0) + CORR over the tower, from precision T
 template <typename T>
 __global__ void k_vc_out(BlockList L, int ncell, const FState *st, const T *corr, double *out) {
+  pdl_enter();
   if (st->done) return;
   const long total = (long)L.n * ncell;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
@@ -299,6 +307,7 @@ __global__ void k_vc_out(BlockList L, int ncell, const FState *st, const T *corr
 template <int ND, int MODE>
 __global__ void __launch_bounds__(kTPB) k_apply_red(Topo t, Coef<double> c, BlockList L, const double *x, double *y,
                                                   const double *w, FState *st, double *partials, unsigned *counter) {
+  pdl_enter();
   if (MODE != 2 && st->done) return;
   double acc[2] = {0.0, 0.0};
   const int ncell = t.ncell;
@@ -332,6 +341,7 @@ template <typename T>
 __global__ void __launch_bounds__(kTPB) k_bottom_gemv(int n, const double *__restrict__ binv, const int *blocks,
                                                     int ncell, const T *__restrict__ resid, T *__restrict__ corr,
                                                     const FState *st) {
+  pdl_enter();
   if (st && st->done) return;
   extern __shared__ double rv[];
   for (int j = threadIdx.x; j < n; j += blockDim.x) rv[j] = (double)resid[(long)blocks[j / ncell] * ncell + j % ncell];
@@ -570,29 +580,46 @@ void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *o
   const int *guard = &d_st_->done;
   for (int l = L; l >= 2; l--) {
     if (l - 1 >= tt_.max_level || levels_[l - 1].n == 0 || levels_[l].n == 0) continue;
-    launch_restrict<T>(topo_, c, nonleaf_list(l - 1), resid, guard, stream_);
+    launch_restrict<T>(topo_, c, nonleaf_list(l - 1), resid, guard, stream_, prm_.pdl != 0);
   }
-  // dense bottom solve on level 1
-  const int rows_per_cta = kTPB / 32;
-  const size_t smem = (size_t)n_bot_ * sizeof(double);
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_bottom_gemv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_bottom_gemv<T><<<(n_bot_ + rows_per_cta - 1) / rows_per_cta, kTPB, smem, stream_>>>(
-      n_bot_, d_binv_, towers_[1].all.blocks, ncell_, resid, corr, d_st_);
+  bottom_launch<T>(resid, corr);
   for (int l = 2; l <= L; l++) {
     if (levels_[l].n == 0) continue;
-    launch_prolong<T>(topo_, c, level_list(l), corr, guard, stream_);
+    launch_prolong<T>(topo_, c, level_list(l), corr, guard, stream_, prm_.pdl != 0);
     for (int s = 0; s < prm_.n_post; s++) {
       for (int ll = l; ll >= 1; ll--) {
         BlockList sl = sublevel_list(l, ll);
         if (sl.n == 0) break;
-        for (int rb = 0; rb < 2; rb++) launch_smooth<T>(topo_, c, sl, rb, corr, resid, guard, stream_);
+        for (int rb = 0; rb < 2; rb++)
+          launch_smooth<T>(topo_, c, sl, rb, corr, resid, guard, stream_, prm_.pdl != 0);
       }
     }
   }
-  BlockList TL = tower_list(L);
-  k_vc_out<T><<<ew_grid((long)TL.n * ncell_), kTPB, 0, stream_>>>(TL, ncell_, d_st_, corr, out);
+  vc_out_launch<T>(tower_list(L), corr, out);
 }
+
+// V-cycle result on the tower, widened to FP64: out = 0 + corr
+template <typename T>
+void MacGpu::vc_out_launch(const BlockList &TL, T *corr, double *out) {
+  launch_k(prm_.pdl != 0, k_vc_out<T>, ew_grid((long)TL.n * ncell_), kTPB, 0, stream_, TL, ncell_,
+           (const FState *)d_st_, (const T *)corr, out);
+}
+template void MacGpu::vc_out_launch<float>(const BlockList &, float *, double *);
+template void MacGpu::vc_out_launch<double>(const BlockList &, double *, double *);
+
+// dense bottom solve of the level-1 problem: corr = Binv * resid
+template <typename T>
+void MacGpu::bottom_launch(T *resid, T *corr) {
+  const int rows_per_cta = kTPB / 32;
+  const size_t smem = (size_t)n_bot_ * sizeof(double);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_bottom_gemv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  launch_k(prm_.pdl != 0, k_bottom_gemv<T>, (n_bot_ + rows_per_cta - 1) / rows_per_cta, kTPB, smem, stream_, n_bot_,
+           (const double *)d_binv_, (const int *)towers_[1].all.blocks, ncell_, (const T *)resid, corr,
+           (const FState *)d_st_);
+}
+template void MacGpu::bottom_launch<float>(float *, float *);
+template void MacGpu::bottom_launch<double>(double *, double *);
 
 template <typename T>
 void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
@@ -601,19 +628,37 @@ void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
   const long w = (long)TL.n * ncell_;
   double *R = vec_[kR], *RHAT = vec_[kRHAT], *P = vec_[kP], *PH = vec_[kPHAT], *S = vec_[kS], *SH = vec_[kSHAT];
   double *V = vec_[kV], *Tt = vec_[kT], *X = vec_[kX];
-  k_pupdate<T><<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, R, P, V, d_vf_, resid);
-  vcycle_device<T>(L, resid, corr, c, PH);
-  if (tt_.ndim == 2)
-    k_apply_red<2, 0><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, PH, V, RHAT, d_st_, d_part_, d_cnt_);
+  const bool pdl = prm_.pdl != 0;
+  launch_k(pdl, k_pupdate<T>, ew_grid(w), kTPB, 0, stream_, TL, ncell_, (const FState *)d_st_, (const double *)R, P,
+           (const double *)V, (const double *)d_vf_, resid);
+  if (prm_.vcycle_kernel == 2)
+    vcycle_cluster<T>(resid, corr, c, PH);
+  else if (prm_.vcycle_kernel == 1)
+    vcycle_coop<T>(resid, corr, c, PH);
   else
-    k_apply_red<3, 0><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, PH, V, RHAT, d_st_, d_part_, d_cnt_);
-  k_supdate<T><<<red_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, R, V, S, X, PH, d_vf_, resid, d_part_, d_cnt_);
-  vcycle_device<T>(L, resid, corr, c, SH);
+    vcycle_device<T>(L, resid, corr, c, PH);
   if (tt_.ndim == 2)
-    k_apply_red<2, 1><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, SH, Tt, S, d_st_, d_part_, d_cnt_);
+    launch_k(pdl, k_apply_red<2, 0>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)PH, V,
+             (const double *)RHAT, d_st_, d_part_, d_cnt_);
   else
-    k_apply_red<3, 1><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, SH, Tt, S, d_st_, d_part_, d_cnt_);
-  k_rupdate<<<red_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, X, SH, R, S, Tt, RHAT, d_part_, d_cnt_);
+    launch_k(pdl, k_apply_red<3, 0>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)PH, V,
+             (const double *)RHAT, d_st_, d_part_, d_cnt_);
+  launch_k(pdl, k_supdate<T>, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, (const double *)R, (const double *)V,
+           S, X, (const double *)PH, (const double *)d_vf_, resid, d_part_, d_cnt_);
+  if (prm_.vcycle_kernel == 2)
+    vcycle_cluster<T>(resid, corr, c, SH);
+  else if (prm_.vcycle_kernel == 1)
+    vcycle_coop<T>(resid, corr, c, SH);
+  else
+    vcycle_device<T>(L, resid, corr, c, SH);
+  if (tt_.ndim == 2)
+    launch_k(pdl, k_apply_red<2, 1>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)SH, Tt,
+             (const double *)S, d_st_, d_part_, d_cnt_);
+  else
+    launch_k(pdl, k_apply_red<3, 1>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)SH, Tt,
+             (const double *)S, d_st_, d_part_, d_cnt_);
+  launch_k(pdl, k_rupdate, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, X, (const double *)SH, R,
+           (const double *)S, (const double *)Tt, (const double *)RHAT, d_part_, d_cnt_);
 }
 
 void MacGpu::capture_loop(int precision) {
@@ -641,7 +686,7 @@ void MacGpu::capture_loop(int precision) {
     iteration_device<float>(d_resid32_, d_corr32_, c32_);
   else
     iteration_device<double>(vec_[kRESID], vec_[kCORR], c64_);
-  k_set_cond<<<1, 1, 0, stream_>>>(h, d_st_);
+  launch_k(prm_.pdl != 0, k_set_cond, 1, 1, 0, stream_, h, (const FState *)d_st_);
   cudaGraph_t out = nullptr;
   CK_(cudaStreamEndCapture(stream_, &out));
   // count the kernel nodes of one iteration (reported as launches per step)
@@ -657,25 +702,37 @@ void MacGpu::capture_loop(int precision) {
   CK_(cudaGraphInstantiate(&graph_exec_, graph_, 0));
   graph_prec_ = precision;
   graph_npost_ = prm_.n_post;
+  graph_coop_ = prm_.vcycle_kernel;
+  graph_pdl_ = prm_.pdl;
+  graph_cc_ = prm_.cluster_cells;
 }
 
 int MacGpu::cg_solve_device(SolveInfo *info) {
+  if (prepare_device() != 0) return -1;
+  auto t0 = std::chrono::steady_clock::now();
+  if (enqueue_solve() != 0) return -1;
+  if (solve_state(info) != 0) return -1;
+  info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return info->status == 1 ? 1 : 0;
+}
+
+// asynchronous solve for benchmarking: everything enqueued on `stream_`,
+// no host synchronisation in graph mode (the caller times it with events)
+int MacGpu::cg_solve_enqueue() {
   ensure_fast_buffers();
-  if (!err_.empty()) return -1;
-  if (coef_version_ != fast_coef_version_) {
-    refresh_fp32();
-    build_bottom();
-    fast_coef_version_ = coef_version_;
-    if (!err_.empty()) return -1;
-  }
-  if (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post) {
-    capture_loop(prm_.precision);
-    if (!err_.empty()) return -1;
-  }
+  if (!err_.empty() || !bottom_ready_) return -1;
+  if (prm_.graph && (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
+                     graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl ||
+                     graph_cc_ != prm_.cluster_cells))
+    return -1;
+  if (prm_.vcycle_kernel && program_npost_ != prm_.n_post) return -1;
+  return enqueue_solve();
+}
+
+int MacGpu::enqueue_solve() {
   const int L = finest_;
   BlockList TL = tower_list(L);
   const long w = (long)TL.n * ncell_;
-  auto t0 = std::chrono::steady_clock::now();
   FState init{};
   init.tol_rel = prm_.tol_rel;
   init.tol_abs = prm_.tol_abs;
@@ -686,49 +743,30 @@ int MacGpu::cg_solve_device(SolveInfo *info) {
   k_pro_copy<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, vec_[kSOL], vec_[kX0], vec_[kX]);
   if (tt_.ndim == 2)
     k_apply_red<2, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_st_,
-                                                       d_part_, d_cnt_);
+                                                         d_part_, d_cnt_);
   else
     k_apply_red<3, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_st_,
-                                                       d_part_, d_cnt_);
+                                                         d_part_, d_cnt_);
   vcopy(TL, vec_[kRHAT], vec_[kR]);
-  if (prm_.max_iter > 0) CKR_(cudaGraphLaunch(graph_exec_, stream_), -1);
+  if (prm_.max_iter > 0) {
+    if (prm_.graph) {
+      CKR_(cudaGraphLaunch(graph_exec_, stream_), -1);
+    } else {
+      // the captured iteration's kernels, launched directly; the host reads
+      // the convergence flag after every iteration
+      for (int it = 0; it < prm_.max_iter; it++) {
+        if (prm_.precision == 1)
+          iteration_device<float>(d_resid32_, d_corr32_, c32_);
+        else
+          iteration_device<double>(vec_[kRESID], vec_[kCORR], c64_);
+        CKR_(cudaMemcpyAsync(h_st_, d_st_, sizeof(FState), cudaMemcpyDeviceToHost, stream_), -1);
+        CKR_(cudaStreamSynchronize(stream_), -1);
+        if (h_st_->done) break;
+      }
+    }
+  }
   k_finish<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, vec_[kX0], vec_[kX], vec_[kSOL]);
-  CKR_(cudaMemcpyAsync(h_st_, d_st_, sizeof(FState), cudaMemcpyDeviceToHost, stream_), -1);
-  CKR_(cudaStreamSynchronize(stream_), -1);
-  info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  const FState &st = *h_st_;
-  info->iterations = st.trivial ? 0 : st.iter;
-  info->rnorm0 = st.rnorm0;
-  info->rnorm = st.rnorm;
-  info->status = st.stat ? 1 : ((st.conv || st.trivial) ? 0 : 2);
-  return st.stat;
-}
-
-// asynchronous solve for benchmarking: everything enqueued on `stream_`,
-// no host synchronisation (the caller times it with events)
-int MacGpu::cg_solve_enqueue() {
-  ensure_fast_buffers();
-  if (!err_.empty() || !graph_exec_ || !bottom_ready_) return -1;
-  const int L = finest_;
-  BlockList TL = tower_list(L);
-  const long w = (long)TL.n * ncell_;
-  FState init{};
-  init.tol_rel = prm_.tol_rel;
-  init.tol_abs = prm_.tol_abs;
-  init.max_iter = prm_.max_iter;
-  *h_st_ = init;
-  CKR_(cudaMemcpyAsync(d_st_, h_st_, sizeof(FState), cudaMemcpyHostToDevice, stream_), -1);
-  k_pro_copy<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, vec_[kSOL], vec_[kX0], vec_[kX]);
-  if (tt_.ndim == 2)
-    k_apply_red<2, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_st_,
-                                                       d_part_, d_cnt_);
-  else
-    k_apply_red<3, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_st_,
-                                                       d_part_, d_cnt_);
-  vcopy(TL, vec_[kRHAT], vec_[kR]);
-  CKR_(cudaGraphLaunch(graph_exec_, stream_), -1);
-  k_finish<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, vec_[kX0], vec_[kX], vec_[kSOL]);
-  return 0;
+  return err_.empty() ? 0 : -1;
 }
 
 }  // namespace sayaka_gb300
@@ -745,7 +783,11 @@ int MacGpu::prepare_device() {
     fast_coef_version_ = coef_version_;
     if (!err_.empty()) return -1;
   }
-  if (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post) capture_loop(prm_.precision);
+  if (prm_.vcycle_kernel && program_npost_ != prm_.n_post) build_vcycle_program();
+  if (prm_.graph && (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
+                     graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl ||
+                     graph_cc_ != prm_.cluster_cells))
+    capture_loop(prm_.precision);
   return err_.empty() ? 0 : -1;
 }
 
@@ -756,6 +798,15 @@ namespace sayaka_gb300 {
 int MacGpu::solve_state(SolveInfo *info) {
   CKR_(cudaMemcpyAsync(h_st_, d_st_, sizeof(FState), cudaMemcpyDeviceToHost, stream_), -1);
   CKR_(cudaStreamSynchronize(stream_), -1);
+  if (d_bar_) {
+    unsigned w[4];
+    CKR_(cudaMemcpy(w, d_bar_, sizeof(w), cudaMemcpyDeviceToHost), -1);
+    if (w[2] != 0) {
+      cudaMemset(d_bar_, 0, 4 * sizeof(unsigned));
+      fail("cooperative V-cycle: grid barrier timed out");
+      return -1;
+    }
+  }
   const FState &st = *h_st_;
   info->iterations = st.trivial ? 0 : st.iter;
   info->rnorm0 = st.rnorm0;

@@ -18,6 +18,7 @@
 
 #include "mac_device.h"
 #include "mac_stencil.cuh"
+#include "launch.cuh"
 
 namespace sayaka_gb300 {
 
@@ -33,6 +34,7 @@ using namespace stencil;
 template <typename T, int ND>
 __global__ void __launch_bounds__(kThreads) k_apply(Topo t, Coef<T> c, BlockList L, const T *__restrict__ x,
                                                     T *__restrict__ y, const T *__restrict__ rhs, const int *guard) {
+  pdl_enter();
   if (guard && *guard) return;
   const int ncell = t.ncell;
   const long total = (long)L.n * ncell;
@@ -54,62 +56,15 @@ __global__ void __launch_bounds__(kThreads) k_apply(Topo t, Coef<T> c, BlockList
 template <typename T, int ND>
 __global__ void __launch_bounds__(kThreads) k_smooth(Topo t, Coef<T> c, BlockList L, int color, T *__restrict__ phi,
                                                      const T *__restrict__ rhs, const int *guard) {
+  pdl_enter();
   if (guard && *guard) return;
-  const int nb = t.nb, ncell = t.ncell, hrow = nb >> 1;
-  const int nhalf = ncell >> 1;
+  const int nhalf = t.ncell >> 1;
   const long total = (long)L.n * nhalf;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int p = (int)(it / nhalf);
-    const int h = (int)(it - (long)p * nhalf);
-    const int row = h / hrow;
     int ijk[3];
-    ijk[1] = ND >= 2 ? row % nb : 0;
-    ijk[2] = ND == 3 ? row / nb : 0;
-    ijk[0] = 2 * (h - row * hrow) + ((color + ijk[1] + ijk[2]) & 1);
-    const int ci = encode(ijk, nb);
-    const int b = L.blocks[p];
-    const uint16_t ft = L.ftypes[p];
-    const long cb = (long)b * ncell;
-    const T dv = geom(c, b, 6);
-    T diag = c.alpha * dv;
-    T off = 0;
-#pragma unroll
-    for (int f = 0; f < 2 * ND; f++) {
-      const int d = f >> 1, s = f & 1;
-      const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
-      const int fx = face_index(d, ijk, s, nb);
-      T coef, val;
-      if (!bnd) {
-        coef = c.tff[d][(long)b * t.nfb + fx];
-        const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
-        val = coef * phi[cb + ci + (s ? stride : -stride)];
-      } else {
-        const int ty = face_type_of(ft, f);
-        if (ty == 0) {
-          coef = c.tff[d][(long)b * t.nfb + fx];
-          val = coef * same_level_ghost(t, b, f, ijk, phi);
-        } else if (ty == 1) {
-          if (t.bc_type[b * 6 + f] == kBCNeumann) {
-            coef = 0;
-          } else {
-            coef = c.tff[d][(long)b * t.nfb + fx] * (T)2.0;
-          }
-          val = 0;
-        } else if (ty == 2) {
-          coef = cf_coef(c, t, b, d, fx, (T)1.5);
-          val = coef * fine_crse_ghost<T, ND>(t, b, f, ijk, phi);
-        } else {
-          coef = cf_coef(c, t, b, d, fx, (T)0.75);
-          val = crse_fine_sum<T, ND>(t, c, b, f, ijk, phi);
-        }
-      }
-      diag += coef;
-      off += val;
-    }
-    const T vfv = c.vf[cb + ci];
-    T unew = 0;
-    if (vfv > 0) unew = (rhs[cb + ci] * dv * vfv + off) / diag;
-    phi[cb + ci] = unew;
+    color_cell<ND>((int)(it - (long)p * nhalf), t.nb, color, ijk);
+    smooth_cell<T, ND>(t, c, L.blocks[p], L.ftypes[p], ijk, phi, rhs);
   }
 }
 
@@ -120,36 +75,13 @@ __global__ void __launch_bounds__(kThreads) k_smooth(Topo t, Coef<T> c, BlockLis
 template <typename T, int ND>
 __global__ void __launch_bounds__(kThreads) k_restrict(Topo t, Coef<T> c, BlockList L, T *__restrict__ phi,
                                                        const int *guard) {
+  pdl_enter();
   if (guard && *guard) return;
-  const int nb = t.nb, ncell = t.ncell, half = nb >> 1;
+  const int ncell = t.ncell;
   const long total = (long)L.n * ncell;
-  const T wgt = (T)1.0 / (T)(1 << ND);
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int p = (int)(it / ncell);
-    const int ci = (int)(it - (long)p * ncell);
-    const int b = L.blocks[p];
-    int ijk[3];
-    decode<ND>(ci, nb, ijk);
-    int cidx = 0, fb[3] = {0, 0, 0};
-    for (int q = 0; q < ND; q++) {
-      const int sq = ijk[q] >= half ? 1 : 0;
-      cidx |= sq << q;
-      fb[q] = 2 * (ijk[q] - sq * half);
-    }
-    const int F = t.child[b * 8 + cidx];
-    const long fbase = (long)F * ncell;
-    T sum = 0;
-    for (int kk = 0; kk < (ND == 3 ? 2 : 1); kk++)
-      for (int jj = 0; jj < 2; jj++)
-        for (int ii = 0; ii < 2; ii++) {
-          const int fi[3] = {fb[0] + ii, fb[1] + jj, ND == 3 ? fb[2] + kk : 0};
-          const long q = fbase + encode(fi, nb);
-          const T wv = phi[q] * c.vf[q];
-          sum += wv;
-        }
-    const T vfc = c.vf[(long)b * ncell + ci];
-    const T avg = sum * wgt;
-    phi[(long)b * ncell + ci] = vfc > 0 ? avg / vfc : (T)0;
+    restrict_cell<T, ND>(t, c, L.blocks[p], (int)(it - (long)p * ncell), phi);
   }
 }
 
@@ -157,21 +89,13 @@ __global__ void __launch_bounds__(kThreads) k_restrict(Topo t, Coef<T> c, BlockL
 template <typename T, int ND>
 __global__ void __launch_bounds__(kThreads) k_prolong(Topo t, Coef<T> c, BlockList L, T *__restrict__ phi,
                                                       const int *guard) {
+  pdl_enter();
   if (guard && *guard) return;
-  const int nb = t.nb, ncell = t.ncell, half = nb >> 1;
+  const int ncell = t.ncell;
   const long total = (long)L.n * ncell;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int p = (int)(it / ncell);
-    const int ci = (int)(it - (long)p * ncell);
-    const int b = L.blocks[p];
-    int ijk[3];
-    decode<ND>(ci, nb, ijk);
-    const int P = t.parent[b], wc = t.which_child[b];
-    int pc[3] = {0, 0, 0};
-    for (int q = 0; q < ND; q++) pc[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
-    const T v = phi[(long)P * ncell + encode(pc, nb)];
-    const long q = (long)b * ncell + ci;
-    phi[q] = c.vf[q] > 0 ? v : (T)0;
+    prolong_cell<T, ND>(t, c, L.blocks[p], (int)(it - (long)p * ncell), phi);
   }
 }
 
@@ -347,46 +271,46 @@ void launch_face_coef(const Topo &t, const double *geom64, const T *bcoef[3], co
 
 template <typename T>
 void launch_apply(const Topo &t, const Coef<T> &c, const BlockList &L, const T *x, T *y, const T *rhs,
-                  const int *guard, cudaStream_t s) {
+                  const int *guard, cudaStream_t s, bool pdl) {
   const long work = (long)L.n * t.ncell;
   if (work == 0) return;
   if (t.ndim == 2)
-    k_apply<T, 2><<<grid_for(work), kThreads, 0, s>>>(t, c, L, x, y, rhs, guard);
+    launch_k(pdl, k_apply<T, 2>, grid_for(work), kThreads, 0, s, t, c, L, x, y, rhs, guard);
   else
-    k_apply<T, 3><<<grid_for(work), kThreads, 0, s>>>(t, c, L, x, y, rhs, guard);
+    launch_k(pdl, k_apply<T, 3>, grid_for(work), kThreads, 0, s, t, c, L, x, y, rhs, guard);
 }
 
 template <typename T>
 void launch_smooth(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
-                   const int *guard, cudaStream_t s) {
+                   const int *guard, cudaStream_t s, bool pdl) {
   const long work = (long)L.n * (t.ncell / 2);
   if (work == 0) return;
   if (t.ndim == 2)
-    k_smooth<T, 2><<<grid_for(work), kThreads, 0, s>>>(t, c, L, color, phi, rhs, guard);
+    launch_k(pdl, k_smooth<T, 2>, grid_for(work), kThreads, 0, s, t, c, L, color, phi, rhs, guard);
   else
-    k_smooth<T, 3><<<grid_for(work), kThreads, 0, s>>>(t, c, L, color, phi, rhs, guard);
+    launch_k(pdl, k_smooth<T, 3>, grid_for(work), kThreads, 0, s, t, c, L, color, phi, rhs, guard);
 }
 
 template <typename T>
 void launch_restrict(const Topo &t, const Coef<T> &c, const BlockList &L, T *phi, const int *guard,
-                     cudaStream_t s) {
+                     cudaStream_t s, bool pdl) {
   const long work = (long)L.n * t.ncell;
   if (work == 0) return;
   if (t.ndim == 2)
-    k_restrict<T, 2><<<grid_for(work), kThreads, 0, s>>>(t, c, L, phi, guard);
+    launch_k(pdl, k_restrict<T, 2>, grid_for(work), kThreads, 0, s, t, c, L, phi, guard);
   else
-    k_restrict<T, 3><<<grid_for(work), kThreads, 0, s>>>(t, c, L, phi, guard);
+    launch_k(pdl, k_restrict<T, 3>, grid_for(work), kThreads, 0, s, t, c, L, phi, guard);
 }
 
 template <typename T>
 void launch_prolong(const Topo &t, const Coef<T> &c, const BlockList &L, T *phi, const int *guard,
-                    cudaStream_t s) {
+                    cudaStream_t s, bool pdl) {
   const long work = (long)L.n * t.ncell;
   if (work == 0) return;
   if (t.ndim == 2)
-    k_prolong<T, 2><<<grid_for(work), kThreads, 0, s>>>(t, c, L, phi, guard);
+    launch_k(pdl, k_prolong<T, 2>, grid_for(work), kThreads, 0, s, t, c, L, phi, guard);
   else
-    k_prolong<T, 3><<<grid_for(work), kThreads, 0, s>>>(t, c, L, phi, guard);
+    launch_k(pdl, k_prolong<T, 3>, grid_for(work), kThreads, 0, s, t, c, L, phi, guard);
 }
 
 void launch_flux(const Topo &t, const Coef<double> &c, const BlockList &L, int dir, const double *phi, double *flux,
@@ -413,13 +337,13 @@ void launch_fix_bc(const Topo &t, const Coef<double> &c, const BlockList &L, con
   template void launch_face_coef<T>(const Topo &, const double *, const T *[3], const T *[3], double, T *[3],  \
                                     cudaStream_t);                                                              \
   template void launch_apply<T>(const Topo &, const Coef<T> &, const BlockList &, const T *, T *, const T *,   \
-                                const int *, cudaStream_t);                                                     \
+                                const int *, cudaStream_t, bool);                                               \
   template void launch_smooth<T>(const Topo &, const Coef<T> &, const BlockList &, int, T *, const T *,        \
-                                 const int *, cudaStream_t);                                                    \
+                                 const int *, cudaStream_t, bool);                                              \
   template void launch_restrict<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,         \
-                                   cudaStream_t);                                                               \
+                                   cudaStream_t, bool);                                                         \
   template void launch_prolong<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,          \
-                                  cudaStream_t);
+                                  cudaStream_t, bool);
 SAYAKA_INST(double)
 SAYAKA_INST(float)
 #undef SAYAKA_INST

@@ -336,6 +336,8 @@ MacGpu::~MacGpu() {
   fr(d_part_);
   fr(d_cnt_);
   fr(d_binv_);
+  fr(d_phases_);
+  fr(d_bar_);
   if (h_st_) cudaFreeHost(h_st_);
   if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
   if (graph_) cudaGraphDestroy(graph_);

@@ -29,6 +29,10 @@ struct SolverParams {
   int precision = 0;        // 0: FP64 V-cycle, 1: FP32 V-cycle (FP64 outer + bottom)
   int bottom = 0;           // 0: BiCGSTAB (reference), 1: dense direct solve
   int verbose = 0;
+  int graph = 1;            // device path: 1 graph + WHILE node, 0 host loop of direct launches
+  int vcycle_kernel = 0;    // device path: 0 one launch per phase, 1 one cooperative launch, 2 cluster phases
+  int pdl = 0;              // device path: programmatic dependent launch between the iteration's kernels
+  int cluster_cells = 16384;  // vcycle_kernel 2: phases touching at most this many cells run in the cluster
 };
 
 struct SolveInfo {
@@ -152,6 +156,16 @@ class MacGpu {
   template <typename T>
   void iteration_device(T *resid, T *corr, const Coef<T> &c);
   void capture_loop(int precision);
+  int enqueue_solve();
+  void build_vcycle_program();
+  template <typename T>
+  void vcycle_coop(T *resid, T *corr, const Coef<T> &c, double *out);
+  template <typename T>
+  void vcycle_cluster(T *resid, T *corr, const Coef<T> &c, double *out);
+  template <typename T>
+  void bottom_launch(T *resid, T *corr);
+  template <typename T>
+  void vc_out_launch(const BlockList &TL, T *corr, double *out);
 
   TreeTables tt_;
   SolverParams prm_;
@@ -199,6 +213,14 @@ class MacGpu {
   cudaGraphExec_t graph_exec_ = nullptr;
   int graph_prec_ = -1, graph_npost_ = -1;
   int kernels_per_iter_ = 0;
+  int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1;
+  // cooperative V-cycle
+  VPhase *d_phases_ = nullptr;
+  std::vector<VPhase> h_phases_;
+  int n_phases_ = 0, program_npost_ = -1, coop_grid_ = 0;
+  unsigned *d_bar_ = nullptr;  // [0] count, [1] generation, [2] error word
+  // cluster V-cycle: restriction program, bottom, prolongation/smoothing program
+  int n_down_ = 0, cluster_size_ = 0;
 
  public:
   // kernel launches of one captured BiCGSTAB iteration; a device solve

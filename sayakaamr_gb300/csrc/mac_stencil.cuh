@@ -1,7 +1,11 @@
 // Device-side stencil helpers shared by every kernel that evaluates the MAC
-// operator: index arithmetic of the compact block layout and the gathers
-// that replace the reference's ghost-cell fills and coarse/fine flux
-// registers (see mac_kernels.cu for the mapping to the reference).
+// operator, the red-black smoother or the inter-level transfers: index
+// arithmetic of the compact block layout and the gathers that replace the
+// reference's ghost-cell fills and coarse/fine flux registers (the mapping to
+// the reference is described in mac_kernels.cu).
+//
+// Template flag CG: loads of fields that other CTAs write inside the same
+// cooperative kernel go through L2 (ld.global.cg) instead of L1.
 #pragma once
 
 #include <cstdint>
@@ -10,6 +14,13 @@
 
 namespace sayaka_gb300 {
 namespace stencil {
+
+template <bool CG, typename T>
+__device__ __forceinline__ T ld(const T *p) {
+  if (CG) return __ldcg(p);
+  return *p;
+}
+
 __device__ __forceinline__ int face_type_of(uint16_t ft, int f) { return (ft >> (2 * f)) & 3; }
 
 template <int ND>
@@ -46,7 +57,7 @@ __device__ __forceinline__ T cf_coef(const Coef<T> &c, const Topo &t, int b, int
 // CRSE_FINE face: sum of the fine-side contributions T_f * phi_f over the
 // fine faces covering coarse face (d, s) of cell ijk of block b, in the
 // reference's RESTRICT_SUM order (lower transverse dimension fastest)
-template <typename T, int ND>
+template <typename T, int ND, bool CG = false>
 __device__ __forceinline__ T crse_fine_sum(const Topo &t, const Coef<T> &c, int b, int f, const int ijk[3],
                                            const T *__restrict__ x) {
   const int nb = t.nb, half = nb >> 1;
@@ -76,7 +87,7 @@ __device__ __forceinline__ T crse_fine_sum(const Topo &t, const Coef<T> &c, int 
       if (ND == 2) fi[2] = 0;
       const int fx = face_index(d, fi, fside, nb);
       const T tf = cf_coef(c, t, F, d, fx, h15);
-      val += tf * x[(long)F * t.ncell + encode(fi, nb)];
+      val += tf * ld<CG>(&x[(long)F * t.ncell + encode(fi, nb)]);
     }
   }
   return val;
@@ -84,7 +95,7 @@ __device__ __forceinline__ T crse_fine_sum(const Topo &t, const Coef<T> &c, int 
 
 // value a FINE_CRSE ghost cell holds: the coarse leaf's boundary cell
 // (injection through the parent's ghost layer)
-template <typename T, int ND>
+template <typename T, int ND, bool CG = false>
 __device__ __forceinline__ T fine_crse_ghost(const Topo &t, int b, int f, const int ijk[3], const T *__restrict__ x) {
   const int nb = t.nb, half = nb >> 1;
   const int d = f >> 1, s = f & 1;
@@ -97,23 +108,22 @@ __device__ __forceinline__ T fine_crse_ghost(const Topo &t, int b, int f, const 
     else
       ci[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
   }
-  return x[(long)C * t.ncell + encode(ci, nb)];
+  return ld<CG>(&x[(long)C * t.ncell + encode(ci, nb)]);
 }
 
 // mirrored boundary cell of the same-level neighbour
-template <typename T>
+template <typename T, bool CG = false>
 __device__ __forceinline__ T same_level_ghost(const Topo &t, int b, int f, const int ijk[3], const T *__restrict__ x) {
   const int d = f >> 1, s = f & 1;
   const int n = t.neighbor[b * 6 + f];
   int ni[3] = {ijk[0], ijk[1], ijk[2]};
   ni[d] = s == 1 ? 0 : t.nb - 1;
-  return x[(long)n * t.ncell + encode(ni, t.nb)];
+  return ld<CG>(&x[(long)n * t.ncell + encode(ni, t.nb)]);
 }
-
 
 // operator value of cell ci of block b: (phi_c*sum T - sum T*phi_nb)/dv/vf,
 // 0 on cells with vf = 0 (src/SayakaMacOperator.cpp:1325-1459)
-template <typename T, int ND>
+template <typename T, int ND, bool CG = false>
 __device__ __forceinline__ T apply_cell(const Topo &t, const Coef<T> &c, int b, uint16_t ft, int ci,
                                         const T *__restrict__ x) {
   const int nb = t.nb;
@@ -121,7 +131,7 @@ __device__ __forceinline__ T apply_cell(const Topo &t, const Coef<T> &c, int b, 
   decode<ND>(ci, nb, ijk);
   const long cb = (long)b * t.ncell;
   const T dv = geom(c, b, 6);
-  const T phic = x[cb + ci];
+  const T phic = ld<CG>(&x[cb + ci]);
   T diag = c.alpha * dv;
   T off = 0;
 #pragma unroll
@@ -133,12 +143,12 @@ __device__ __forceinline__ T apply_cell(const Topo &t, const Coef<T> &c, int b, 
     if (!bnd) {
       coef = c.tff[d][(long)b * t.nfb + fx];
       const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
-      val = coef * x[cb + ci + (s ? stride : -stride)];
+      val = coef * ld<CG>(&x[cb + ci + (s ? stride : -stride)]);
     } else {
       const int ty = face_type_of(ft, f);
       if (ty == 0) {  // FINE_FINE
         coef = c.tff[d][(long)b * t.nfb + fx];
-        val = coef * same_level_ghost(t, b, f, ijk, x);
+        val = coef * same_level_ghost<T, CG>(t, b, f, ijk, x);
       } else if (ty == 1) {  // FINE_BC
         if (t.bc_type[b * 6 + f] == kBCNeumann) {
           coef = 0;
@@ -149,10 +159,10 @@ __device__ __forceinline__ T apply_cell(const Topo &t, const Coef<T> &c, int b, 
         }
       } else if (ty == 2) {  // FINE_CRSE
         coef = cf_coef(c, t, b, d, fx, (T)1.5);
-        val = coef * fine_crse_ghost<T, ND>(t, b, f, ijk, x);
+        val = coef * fine_crse_ghost<T, ND, CG>(t, b, f, ijk, x);
       } else {  // CRSE_FINE
         coef = cf_coef(c, t, b, d, fx, (T)0.75);
-        val = crse_fine_sum<T, ND>(t, c, b, f, ijk, x);
+        val = crse_fine_sum<T, ND, CG>(t, c, b, f, ijk, x);
       }
     }
     diag += coef;
@@ -161,6 +171,112 @@ __device__ __forceinline__ T apply_cell(const Topo &t, const Coef<T> &c, int b, 
   const T lphi = (phic * diag - off) / dv;
   const T vfv = c.vf[cb + ci];
   return vfv > 0 ? lphi / vfv : (T)0;
+}
+
+// one red-black Gauss-Seidel update of cell ijk of block b (tower face types
+// ft): unew = (rhs*dv*vf + sum T*phi_nb) / sum T, 0 where vf = 0
+// (src/SayakaMacOperator.cpp:1191-1323)
+template <typename T, int ND, bool CG = false>
+__device__ __forceinline__ void smooth_cell(const Topo &t, const Coef<T> &c, int b, uint16_t ft, const int ijk[3],
+                                            T *__restrict__ phi, const T *__restrict__ rhs) {
+  const int nb = t.nb;
+  const int ci = encode(ijk, nb);
+  const long cb = (long)b * t.ncell;
+  const T dv = geom(c, b, 6);
+  T diag = c.alpha * dv;
+  T off = 0;
+#pragma unroll
+  for (int f = 0; f < 2 * ND; f++) {
+    const int d = f >> 1, s = f & 1;
+    const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+    const int fx = face_index(d, ijk, s, nb);
+    T coef, val;
+    if (!bnd) {
+      coef = c.tff[d][(long)b * t.nfb + fx];
+      const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+      val = coef * ld<CG>(&phi[cb + ci + (s ? stride : -stride)]);
+    } else {
+      const int ty = face_type_of(ft, f);
+      if (ty == 0) {
+        coef = c.tff[d][(long)b * t.nfb + fx];
+        val = coef * same_level_ghost<T, CG>(t, b, f, ijk, phi);
+      } else if (ty == 1) {
+        if (t.bc_type[b * 6 + f] == kBCNeumann)
+          coef = 0;
+        else
+          coef = c.tff[d][(long)b * t.nfb + fx] * (T)2.0;
+        val = 0;
+      } else if (ty == 2) {
+        coef = cf_coef(c, t, b, d, fx, (T)1.5);
+        val = coef * fine_crse_ghost<T, ND, CG>(t, b, f, ijk, phi);
+      } else {
+        coef = cf_coef(c, t, b, d, fx, (T)0.75);
+        val = crse_fine_sum<T, ND, CG>(t, c, b, f, ijk, phi);
+      }
+    }
+    diag += coef;
+    off += val;
+  }
+  const T vfv = c.vf[cb + ci];
+  T unew = 0;
+  if (vfv > 0) unew = (ld<CG>(&rhs[cb + ci]) * dv * vfv + off) / diag;
+  phi[cb + ci] = unew;
+}
+
+// cell (block-local index ijk) of colour `color` for the h-th half-cell of a block
+template <int ND>
+__device__ __forceinline__ void color_cell(int h, int nb, int color, int ijk[3]) {
+  const int hrow = nb >> 1;
+  const int row = h / hrow;
+  ijk[1] = ND >= 2 ? row % nb : 0;
+  ijk[2] = ND == 3 ? row / nb : 0;
+  ijk[0] = 2 * (h - row * hrow) + ((color + ijk[1] + ijk[2]) & 1);
+}
+
+// volume-weighted restriction of one coarse cell of non-leaf block b:
+// avg(fine*vf_fine)/vf_coarse (src/SayakaMacIB.cpp:157-232,
+// src/SayakaInterpPatch.cpp:398-444)
+template <typename T, int ND, bool CG = false>
+__device__ __forceinline__ void restrict_cell(const Topo &t, const Coef<T> &c, int b, int ci, T *__restrict__ phi) {
+  const int nb = t.nb, ncell = t.ncell, half = nb >> 1;
+  const T wgt = (T)1.0 / (T)(1 << ND);
+  int ijk[3];
+  decode<ND>(ci, nb, ijk);
+  int cidx = 0, fb[3] = {0, 0, 0};
+  for (int q = 0; q < ND; q++) {
+    const int sq = ijk[q] >= half ? 1 : 0;
+    cidx |= sq << q;
+    fb[q] = 2 * (ijk[q] - sq * half);
+  }
+  const int F = t.child[b * 8 + cidx];
+  const long fbase = (long)F * ncell;
+  T sum = 0;
+  for (int kk = 0; kk < (ND == 3 ? 2 : 1); kk++)
+    for (int jj = 0; jj < 2; jj++)
+      for (int ii = 0; ii < 2; ii++) {
+        const int fi[3] = {fb[0] + ii, fb[1] + jj, ND == 3 ? fb[2] + kk : 0};
+        const long q = fbase + encode(fi, nb);
+        const T wv = ld<CG>(&phi[q]) * c.vf[q];
+        sum += wv;
+      }
+  const T vfc = c.vf[(long)b * ncell + ci];
+  const T avg = sum * wgt;
+  phi[(long)b * ncell + ci] = vfc > 0 ? avg / vfc : (T)0;
+}
+
+// masked injection of one fine cell of block b from its parent
+// (src/SayakaMacIB.cpp:234-283)
+template <typename T, int ND, bool CG = false>
+__device__ __forceinline__ void prolong_cell(const Topo &t, const Coef<T> &c, int b, int ci, T *__restrict__ phi) {
+  const int nb = t.nb, ncell = t.ncell, half = nb >> 1;
+  int ijk[3];
+  decode<ND>(ci, nb, ijk);
+  const int P = t.parent[b], wc = t.which_child[b];
+  int pc[3] = {0, 0, 0};
+  for (int q = 0; q < ND; q++) pc[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
+  const T v = ld<CG>(&phi[(long)P * ncell + encode(pc, nb)]);
+  const long q = (long)b * ncell + ci;
+  phi[q] = c.vf[q] > 0 ? v : (T)0;
 }
 
 }  // namespace stencil

@@ -8,8 +8,8 @@ HERE="$(cd "$(dirname "$0")" && pwd)"
 ROOT="$(cd "$HERE/../.." && pwd)"
 make -C "$ROOT/oracle" -j8 ${REF:+REF=$REF} >/dev/null
 TMP="$(mktemp -d)"
-"$ROOT/oracle/_ref/ref_dump2" "$TMP" t2s t2b c1 > "$TMP/log2.txt" 2>&1
-"$ROOT/oracle/_ref/ref_dump3" "$TMP" t3s t3n > "$TMP/log3.txt" 2>&1
+"$ROOT/oracle/_ref/ref_dump2" "$TMP" t2s t2b c1 rg2 > "$TMP/log2.txt" 2>&1
+"$ROOT/oracle/_ref/ref_dump3" "$TMP" t3s t3n rg3 > "$TMP/log3.txt" 2>&1
 for f in "$TMP"/*.bin; do
   gzip -9 -n -c "$f" > "$HERE/$(basename "$f").gz"
 done

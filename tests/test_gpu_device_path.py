@@ -63,3 +63,42 @@ def test_device_path_matches_oracle_on_workload():
         a = a - np.sum(a * w) / np.sum(w)
         r = r - np.sum(r * w) / np.sum(w)
         assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-8, (precision, info)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", ["t2s", "t3s", "c1"])
+def test_fused_vcycles_match_per_phase_launches(name, precision):
+    """the one-launch cooperative V-cycle and the thread-block-cluster V-cycle
+    run the same cell functions in the same phase order: identical iterations
+    and bit-identical solutions"""
+    g, t, tb, S = setup_solver(name)
+    S.set_rhs_compact(g["sv_rhs"])
+    out = []
+    # (vcycle_kernel, cluster_cells): per-phase, cooperative, cluster with a
+    # mix of cluster runs and full launches, whole V-cycle in the cluster
+    for vk, cc in ((0, 16384), (1, 16384), (2, 600), (2, 1 << 30)):
+        S.set_zero_sol()
+        S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=precision, bottom=1,
+                     vcycle_kernel=vk, cluster_cells=cc)
+        info = S.cg_solve()
+        assert info["status"] == 0, info
+        out.append((info["iterations"], S.get_sol_compact()))
+    for k in (1, 2, 3):
+        assert out[0][0] == out[k][0], k
+        assert np.array_equal(out[0][1], out[k][1]), k
+
+
+@pytest.mark.parametrize("name", ["t2s", "t3n", "c1"])
+def test_programmatic_dependent_launch_is_transparent(name):
+    """PDL changes launch timing only: identical iterations and solution"""
+    g, t, tb, S = setup_solver(name)
+    S.set_rhs_compact(g["sv_rhs"])
+    out = []
+    for pdl in (0, 1):
+        S.set_zero_sol()
+        S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=1, bottom=1, pdl=pdl)
+        info = S.cg_solve()
+        assert info["status"] == 0, info
+        out.append((info["iterations"], S.get_sol_compact()))
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
