@@ -203,6 +203,20 @@ int sayaka_mac_flux(sayaka_mac *h, int32_t dir, const double *phi, int32_t phi_n
 int sayaka_mac_apply_compact(sayaka_mac *h, int32_t L, const double *x, double *y);
 /* mg_residual_level(L) (src/SayakaMacUtil.cpp:9-49) */
 int sayaka_mac_residual_compact(sayaka_mac *h, int32_t L, const double *x, const double *rhs, double *r);
+/* The residual of mg_residual_level(L) (src/SayakaMacUtil.cpp:9-49) with its
+ * norms, allocating no device memory: for callers that cannot call cudaMalloc
+ * where they need the norm (a fixed memory pool, a host callback).  No
+ * counterpart in the reference.  x, rhs, r: DEVICE pointers to compact
+ * all-block arrays; norms: DEVICE pointer to 2 doubles, set to {|r|_inf, r.r}
+ * over tower L; r is written on the tower's cells only.  Enqueued on stream
+ * (a cudaStream_t; NULL = the solver's stream) without host synchronisation.
+ * Scratch is a static 128 KiB device array: towers of more than 2,097,152
+ * cells are rejected (SAYAKA_BAD_INPUT, see sayaka_mac_last_error).  All calls
+ * on a device share that scratch, so calls must not overlap (one stream, or
+ * a synchronisation between them).  The first call on a device looks up the
+ * scratch address and should come before any stream capture. */
+int sayaka_mac_residual_norm_noalloc(sayaka_mac *h, int32_t L, const double *x, const double *rhs, double *r,
+                                     double *norms, void *stream);
 /* one mg_smooth_level(L) (src/SayakaMacOperator.cpp:140-159, 1028-1112) */
 int sayaka_mac_smooth_compact(sayaka_mac *h, int32_t L, const double *phi, const double *rhs, double *out);
 /* mg_restict_wgt for levels finest-1 .. 1 (src/SayakaMacIB.cpp:157-232) */

@@ -94,6 +94,7 @@ SIGNATURES = {
                                   C.c_int32, C.c_int32]),
     "sayaka_mac_apply_compact": (C.c_int, [_V, C.c_int32, _f64p, _f64p]),
     "sayaka_mac_residual_compact": (C.c_int, [_V, C.c_int32, _f64p, _f64p, _f64p]),
+    "sayaka_mac_residual_norm_noalloc": (C.c_int, [_V, C.c_int32, _V, _V, _V, _V, _V]),
     "sayaka_mac_smooth_compact": (C.c_int, [_V, C.c_int32, _f64p, _f64p, _f64p]),
     "sayaka_mac_restrict_compact": (C.c_int, [_V, _f64p, _f64p]),
     "sayaka_mac_prolong_compact": (C.c_int, [_V, _f64p, _f64p]),

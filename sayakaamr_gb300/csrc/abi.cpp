@@ -604,6 +604,20 @@ int sayaka_mac_residual_compact(sayaka_mac *h, int32_t L, const double *x, const
     return (int)SAYAKA_OK;
   });
 }
+int sayaka_mac_residual_norm_noalloc(sayaka_mac *h, int32_t L, const double *x, const double *rhs, double *r,
+                                     double *norms, void *stream) {
+  if (!h) return SAYAKA_BAD_INPUT;
+  if (!h->gpu) {
+    h->err = "solver not created";
+    return SAYAKA_BAD_INPUT;
+  }
+  std::string why;
+  const cudaStream_t s = stream ? (cudaStream_t)stream : h->gpu->stream();
+  const int st = h->gpu->residual_norm_noalloc(L, x, rhs, r, norms, s, &why);
+  if (st == 0) return SAYAKA_OK;
+  h->err = why;
+  return st == 1 ? SAYAKA_BAD_INPUT : SAYAKA_CUDA_ERROR;
+}
 int sayaka_mac_smooth_compact(sayaka_mac *h, int32_t L, const double *phi, const double *rhs, double *out) {
   return guarded(h, [&] {
     if (L < 1 || !phi || !rhs || !out) return (int)SAYAKA_BAD_INPUT;

@@ -98,6 +98,13 @@ class MacGpu {
   void flux(int dir, const double *phi_all, double *flux_all);
   void fix_bc(const double *phi_grown, int ngrow, double *rhs_all);
 
+  // r = rhs - A x on tower L and out = {|r|_inf, r.r}; device pointers to
+  // compact all-block arrays, enqueued on s, no device allocation (scratch in
+  // a static device array).  0 ok, 1 bad input or size (why says which),
+  // 2 CUDA error
+  int residual_norm_noalloc(int L, const double *x, const double *rhs, double *r, double *out, cudaStream_t s,
+                            std::string *why);
+
   cudaStream_t stream() const { return stream_; }
 
  private:
