@@ -38,6 +38,11 @@ TOL = 1e-8
 # 2000 iterations (the bottom tolerance becomes absolute as the residual
 # falls; see the design notes).
 CPU_BOTTOM_TOL = 1e-10
+WORKLOADS = {
+    "config1": "unit square, 4x4 roots, circle r=0.25 refinement, B=1, Neumann walls",
+    "config2": "rho 1:1000 across a smoothed ellipse, fractional IB disk, p=0 top wall",
+    "config3": "sphere r=0.2 refinement band, IB sphere mask, B ratio 100 across a blob, p=0 top wall",
+}
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -58,6 +63,10 @@ def parse():
                     help="vcycle-kernel 2: largest phase (cells) that runs inside the cluster")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--kernel", type=int, default=-1,
+                    help="time one kernel alone and exit (for ncu): 0 FP64 operator on the finest tower, "
+                         "1 FP32 / 2 FP64 red-black sweep (one colour) of the finest level, "
+                         "3 the device solve's FP64 operator + dot product")
     ap.add_argument("--profile", action="store_true",
                     help="run one solve between cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     return ap.parse_args()
@@ -232,6 +241,9 @@ def main():
                  pdl=args.pdl)
     S.prepare()
     ext = torch.cuda.ExternalStream(S.stream())
+    if args.kernel >= 0:
+        kernel_only(S, prob, ext, torch, args)
+        return
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     finest = int(prob.tables["level"].max())
 
@@ -317,14 +329,16 @@ def main():
         "vs_baseline": None,
         "dtype": "f64 outer BiCGSTAB + %s V-cycle, f64 bottom" % ("f32" if args.precision == 1 else "f64"),
         "data": "synthetic",
-        "config": {"workload": "%s: 2D 16x16 blocks, %d levels, %d leaf blocks, rho 1:1000 ellipse, fractional IB "
-                               "disk, p=0 top wall" % (args.config, finest, len(prob.leaf)),
+        "config": {"workload": "%s: %s" % (args.config, WORKLOADS.get(args.config, "")) +
+                               " (%dD, %d^%d-cell blocks, %d levels, %d leaf blocks)"
+                               % (prob.ndim, prob.nb, prob.ndim, finest, len(prob.leaf)),
                    "leaf_cells": prob.leaf_cells, "blocks": prob.num_blocks, "tol_rel": TOL,
                    "l2": "flushed (256 MiB write) before every timed solve", "precision": args.precision,
                    "iterations_per_solve": statistics.mean(iters), "n_post_smooth": args.n_post,
                    "vcycle_kernel": ("per-phase launches", "cooperative", "cluster")[args.vcycle_kernel],
                    "cluster_cells": args.cluster_cells if args.vcycle_kernel == 2 else None,
                    "pdl": bool(args.pdl),
+                   "smoother_autotune": dict(zip(("variant", "us_per_variant"), S.tuned_smoother(args.precision))),
                    "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "e2e": {"value": ws * prob.leaf_cells / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
@@ -343,6 +357,22 @@ def main():
         print(json.dumps(out))
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def kernel_only(S, prob, ext, torch, args):
+    """args.warmup + args.steps launches of one kernel on the solver stream"""
+    finest = int(prob.tables["level"].max())
+    for _ in range(args.warmup):
+        S.enqueue_kernel(args.kernel, finest)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(ext)
+    for _ in range(args.steps):
+        S.enqueue_kernel(args.kernel, finest)
+    b.record(ext)
+    torch.cuda.synchronize()
+    print(json.dumps({"kernel": args.kernel, "config": args.config, "launches": args.steps,
+                      "us_per_launch": a.elapsed_time(b) * 1e3 / args.steps}))
 
 
 def roofline(S, prob, ext, torch, finest):

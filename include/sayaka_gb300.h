@@ -115,6 +115,8 @@ typedef struct sayaka_params {
   int32_t pdl;            /* device path: 1 = programmatic dependent launch between kernels (default 0) */
   int32_t cluster_cells;  /* vcycle_kernel 2: runs of consecutive phases that each touch at most this many
                              cells share one cluster launch; larger phases get their own launch (16384) */
+  int32_t smooth_variant; /* device smoother launch bounds (register cap): -1 = autotuned at prepare by
+                             timing every variant on the finest level (default), 0..4 = fixed */
 } sayaka_params;
 
 typedef struct sayaka_solve_info {
@@ -185,11 +187,17 @@ void *sayaka_mac_stream(sayaka_mac *h);
 /* enqueue one launch of a hot kernel on the solver's current data, for
  * per-kernel timing: which = 0 FP64 operator on tower L (x = solution),
  * 1 FP32 red-black sweep (colour 0) of the finest level of tower L,
- * 2 FP64 red-black sweep (colour 0) of the finest level of tower L */
+ * 2 FP64 red-black sweep (colour 0) of the finest level of tower L,
+ * 3 the device solve's FP64 operator with its dot product (L = finest) */
 int sayaka_mac_enqueue_kernel(sayaka_mac *h, int32_t which, int32_t L);
 /* kernel launches of a device-resident solve: prologue + per iteration +
  * epilogue (out pointers may be NULL) */
 int sayaka_mac_launch_counts(sayaka_mac *h, int32_t *prologue, int32_t *per_iteration, int32_t *epilogue);
+/* the launch-bounds variant of the device smoother that the autotuner chose
+ * for precision (0 FP64, 1 FP32 V-cycle) at sayaka_mac_prepare, -1 if not
+ * tuned yet; us (may be NULL) receives the measured microseconds per variant
+ * (n entries, 5 variants) */
+int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n);
 /* number of blocks in tower L, or at one level of it (sublevel >= 1) */
 int32_t sayaka_mac_tower_size(sayaka_mac *h, int32_t L, int32_t sublevel);
 

@@ -38,7 +38,7 @@ class Params(C.Structure):
                 ("bot_tol_abs", C.c_double), ("bot_max_iter", C.c_int32), ("precision", C.c_int32),
                 ("bottom", C.c_int32), ("verbose", C.c_int32), ("graph", C.c_int32),
                 ("vcycle_kernel", C.c_int32), ("pdl", C.c_int32),
-                ("cluster_cells", C.c_int32)]
+                ("cluster_cells", C.c_int32), ("smooth_variant", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -89,6 +89,7 @@ SIGNATURES = {
     "sayaka_mac_stream": (C.c_void_p, [_V]),
     "sayaka_mac_enqueue_kernel": (C.c_int, [_V, C.c_int32, C.c_int32]),
     "sayaka_mac_tower_size": (C.c_int32, [_V, C.c_int32, C.c_int32]),
+    "sayaka_mac_tuned_smoother": (C.c_int32, [_V, C.c_int32, C.POINTER(C.c_float), C.c_int32]),
     "sayaka_mac_launch_counts": (C.c_int, [_V, _i32p, _i32p, _i32p]),
     "sayaka_mac_flux": (C.c_int, [_V, C.c_int32, _f64p, C.c_int32, C.c_int32, C.c_int32, _f64p, C.c_int32,
                                   C.c_int32, C.c_int32]),
@@ -374,6 +375,12 @@ class MacSolver:
         _check(self.lib.sayaka_mac_launch_counts(self.h, C.byref(a), C.byref(b), C.byref(c)), "launch_counts",
                self.h)
         return a.value, b.value, c.value
+
+    def tuned_smoother(self, precision):
+        """(chosen variant, microseconds per variant) of the smoother autotuner"""
+        us = (C.c_float * 5)()
+        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 5)
+        return int(v), [float(x) for x in us]
 
     def tower_size(self, L, sublevel=0):
         return self.lib.sayaka_mac_tower_size(self.h, int(L), int(sublevel))

@@ -293,6 +293,7 @@ void sayaka_params_default(sayaka_params *p) {
   p->vcycle_kernel = d.vcycle_kernel;
   p->pdl = d.pdl;
   p->cluster_cells = d.cluster_cells;
+  p->smooth_variant = d.smooth_variant;
 }
 
 int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
@@ -506,6 +507,7 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.vcycle_kernel = p->vcycle_kernel;
     s.pdl = p->pdl;
     s.cluster_cells = p->cluster_cells;
+    s.smooth_variant = p->smooth_variant;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
   });
@@ -603,6 +605,14 @@ int sayaka_mac_residual_compact(sayaka_mac *h, int32_t L, const double *x, const
     h->gpu->residual(L, x, rhs, r);
     return (int)SAYAKA_OK;
   });
+}
+int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n) {
+  if (!h || !h->gpu) return -1;
+  float tmp[8] = {};
+  const int v = h->gpu->tuned_smoother(precision, tmp, 8);
+  if (us)
+    for (int i = 0; i < n && i < 8; i++) us[i] = tmp[i];
+  return v;
 }
 int sayaka_mac_residual_norm_noalloc(sayaka_mac *h, int32_t L, const double *x, const double *rhs, double *r,
                                      double *norms, void *stream) {

@@ -19,6 +19,7 @@ enum BCMath { kBCNeumann = 0, kBCDirichlet = 1, kBCSimpleFill = 2 };
 // tables shared by every kernel (device pointers)
 struct Topo {
   int ndim, nb, ncell;  // ncell = nb^ndim
+  int lnb;              // log2(nb) when nb is a power of two, else -1
   int nfb;              // faces per block per direction
   int nblocks;
   const int *neighbor;   // [nblocks*6]
@@ -84,6 +85,13 @@ void launch_apply(const Topo &t, const Coef<T> &c, const BlockList &L, const T *
 template <typename T>
 void launch_smooth(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi,
                    const T *rhs, const int *guard, cudaStream_t s, bool pdl = false);
+// the device solve's smoother (smooth_cell_fast); `variant` picks the
+// launch bounds (0..kRbgsVariants-1), chosen per workload by the autotuner
+constexpr int kRbgsVariants = 5;
+template <typename T>
+void launch_rbgs(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi,
+                   const T *rhs, const int *guard, cudaStream_t s, bool pdl = false,
+                 int variant = 0);
 
 template <typename T>
 void launch_restrict(const Topo &t, const Coef<T> &c, const BlockList &crse, T *phi,

@@ -300,35 +300,115 @@ __global__ void k_vc_out(BlockList L, int ncell, const FState *st, const T *corr
   }
 }
 
-// Operator fused with its dot products: y = A x (FP64, the reference's exact
-// arithmetic via the shared device functions of mac_kernels.cu) and
-// MODE 0: rhat.y (EpiAlpha) ; MODE 1: y.w, y.y (EpiOmega) ; MODE 2: residual
-// y = rhs - A x with |y|, y.y (EpiInit)
+// The outer BiCGSTAB's operator on the finest tower.  The reference evaluates
+// y = (phi_c * sum T - sum T phi_nb) / dv / vf with two FP64 divisions per
+// cell; GB300's FP64 rate is low, so the device solve folds everything that
+// depends on the coefficients alone into two per-cell factors built once per
+// coefficient set:
+//   S = 1/(dv*vf) (0 where vf = 0),  P = D*S,
+// D being the diagonal sum T with physical Dirichlet faces counted twice
+// (their ghost value is -phi_c).  Then y = phi_c*P - S*sum' T phi_nb over the
+// faces that are not physical boundaries, with FMA: 7 FMA + 1 multiply per
+// cell instead of about 40 FP64 operations.  The result differs from the
+// reference's operator by rounding only (about 1e-16 relative).
+template <int ND>
+__global__ void __launch_bounds__(kTPB) k_op_prep(Topo t, Coef<double> c, BlockList L, double *P, double *S) {
+  using namespace stencil;
+  const int nb = t.nb, total = L.n * t.ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+    int p, ci, ijk[3];
+    split_cell<ND>(it, t, p, ci);
+    decode_fast<ND>(ci, t, ijk);
+    const int b = L.blocks[p];
+    const uint16_t ft = L.ftypes[p];
+    const double dv = geom(c, b, 6);
+    double diag = c.alpha * dv;
+    for (int f = 0; f < 2 * ND; f++) {
+      const int d = f >> 1, s = f & 1;
+      const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+      const int fx = face_index(d, ijk, s, nb);
+      const double tf = c.tff[d][(long)b * t.nfb + fx];
+      if (!bnd) {
+        diag += tf;
+        continue;
+      }
+      const int ty = face_type_of(ft, f);
+      if (ty == 0)
+        diag += tf;
+      else if (ty == 1)
+        diag += t.bc_type[b * 6 + f] == kBCNeumann ? 0.0 : 2.0 * tf;
+      else
+        diag += cf_coef(c, t, b, d, fx, ty == 2 ? 1.5 : 0.75);
+    }
+    const long q = (long)b * t.ncell + ci;
+    const double vfv = c.vf[q];
+    const double sc = vfv > 0 ? 1.0 / (dv * vfv) : 0.0;
+    S[q] = sc;
+    P[q] = diag * sc;
+  }
+}
+
+// sum T * phi_nb over the faces of cell ijk that are not physical boundaries
+template <int ND>
+__device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &c, int b, uint16_t ft,
+                                             const int ijk[3], int ci, const double *__restrict__ x) {
+  using namespace stencil;
+  const int nb = t.nb;
+  const long cb = (long)b * t.ncell;
+  double off = 0.0;
+#pragma unroll
+  for (int f = 0; f < 2 * ND; f++) {
+    const int d = f >> 1, s = f & 1;
+    const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+    const int fx = face_index(d, ijk, s, nb);
+    if (!bnd) {
+      const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+      off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], x[cb + ci + (s ? stride : -stride)], off);
+    } else {
+      const int ty = face_type_of(ft, f);
+      if (ty == 0)
+        off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], same_level_ghost<double, false>(t, b, f, ijk, x), off);
+      else if (ty == 2)
+        off = __fma_rn(cf_coef(c, t, b, d, fx, 1.5), fine_crse_ghost<double, ND, false>(t, b, f, ijk, x), off);
+      else if (ty == 3)
+        off += crse_fine_sum<double, ND, false>(t, c, b, f, ijk, x);
+    }
+  }
+  return off;
+}
+
+// operator fused with its dot products:
+// MODE 0: y = A x, rhat.y (EpiAlpha) ; MODE 1: y = A x, y.w, y.y (EpiOmega) ;
+// MODE 2: y = w - A x (0 where vf = 0), |y|, y.y (EpiInit)
 template <int ND, int MODE>
-__global__ void __launch_bounds__(kTPB) k_apply_red(Topo t, Coef<double> c, BlockList L, const double *x, double *y,
-                                                  const double *w, FState *st, double *partials, unsigned *counter) {
+__global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockList L, const double *__restrict__ x,
+                                               double *__restrict__ y, const double *__restrict__ w,
+                                               const double *__restrict__ P, const double *__restrict__ S,
+                                               FState *st, double *partials, unsigned *counter) {
+  using namespace stencil;
   pdl_enter();
   if (MODE != 2 && st->done) return;
   double acc[2] = {0.0, 0.0};
-  const int ncell = t.ncell;
-  const long total = (long)L.n * ncell;
-  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
-    const int p = (int)(it / ncell);
-    const int ci = (int)(it - (long)p * ncell);
-    const double out = stencil::apply_cell<double, ND>(t, c, L.blocks[p], L.ftypes[p], ci, x);
-    const long q = (long)L.blocks[p] * ncell + ci;
-    const double vfv = c.vf[q];
-    double yv = vfv > 0 ? out : 0.0;
-    if (MODE == 2) yv = vfv > 0 ? w[q] - yv : 0.0;
+  const int total = L.n * t.ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+    int p, ci, ijk[3];
+    split_cell<ND>(it, t, p, ci);
+    decode_fast<ND>(ci, t, ijk);
+    const int b = L.blocks[p];
+    const long q = (long)b * t.ncell + ci;
+    const double off = op_offdiag<ND>(t, c, b, L.ftypes[p], ijk, ci, x);
+    const double sc = S[q];
+    double yv = __fma_rn(x[q], P[q], -off * sc);
+    if (MODE == 2) yv = sc != 0.0 ? w[q] - yv : 0.0;
     y[q] = yv;
-    if (MODE == 0) acc[0] += w[q] * yv;
+    if (MODE == 0) acc[0] = __fma_rn(w[q], yv, acc[0]);
     if (MODE == 1) {
-      acc[0] += yv * w[q];
-      acc[1] += yv * yv;
+      acc[0] = __fma_rn(yv, w[q], acc[0]);
+      acc[1] = __fma_rn(yv, yv, acc[1]);
     }
     if (MODE == 2) {
       acc[0] = fmax(acc[0], fabs(yv));
-      acc[1] += yv * yv;
+      acc[1] = __fma_rn(yv, yv, acc[1]);
     }
   }
   if (MODE == 0) grid_reduce<2>(acc, 0u, partials, counter, EpiAlpha{st});
@@ -412,6 +492,8 @@ void MacGpu::ensure_fast_buffers() {
   d_geom32_ = fa((size_t)nbk * 8);
   d_resid32_ = fa(nc);
   d_corr32_ = fa(nc);
+  if (cudaMalloc(&d_opP_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
+  if (cudaMalloc(&d_opS_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
   if (cudaMalloc(&d_st_, sizeof(FState)) != cudaSuccess) fail("alloc state");
   if (cudaMallocHost(&h_st_, sizeof(FState)) != cudaSuccess) fail("alloc pinned state");
   if (cudaMalloc(&d_part_, sizeof(double) * kMaxRedBlocks * 4) != cudaSuccess) fail("alloc partials");
@@ -426,6 +508,83 @@ void MacGpu::ensure_fast_buffers() {
   }
   c32_.vf = d_vf32_;
   fast_ready_ = true;
+}
+
+// Autotuner of the device smoother: every launch-bounds variant (register
+// cap) of k_rbgs is timed on the finest level of the finest tower -- the
+// largest smoother launch of a V-cycle -- and the fastest is used by the
+// V-cycle from then on.  The variants compute identical values, so the
+// choice changes timing only.  Runs once per solver and precision (again
+// after a forced variant is released), before the graph is captured.
+void MacGpu::tune_smoother(int precision) {
+  const int pi = precision == 1 ? 1 : 0;
+  if (prm_.smooth_variant >= 0) {
+    rbgs_variant_[pi] = std::min(prm_.smooth_variant, kRbgsVariants - 1);
+    return;
+  }
+  if (rbgs_variant_[pi] >= 0 && rbgs_us_[pi][0] > 0) return;
+  const BlockList sl = sublevel_list(finest_, finest_);
+  if (sl.n == 0) {
+    rbgs_variant_[pi] = 2;
+    return;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int reps = 6;
+  float best = 1e30f;
+  int bi = 2;
+  for (int v = 0; v < kRbgsVariants; v++) {
+    auto go = [&](int color) {
+      if (pi)
+        launch_rbgs<float>(topo_, c32_, sl, color, d_corr32_, d_resid32_, nullptr, stream_, false, v);
+      else
+        launch_rbgs<double>(topo_, c64_, sl, color, vec_[kCORR], vec_[kRESID], nullptr, stream_, false, v);
+    };
+    go(0);
+    go(1);
+    CK(cudaEventRecord(e0, stream_));
+    for (int r = 0; r < reps; r++) go(r & 1);
+    CK(cudaEventRecord(e1, stream_));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    rbgs_us_[pi][v] = ms * 1e3f / reps;
+    if (rbgs_us_[pi][v] < best) {
+      best = rbgs_us_[pi][v];
+      bi = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  rbgs_variant_[pi] = bi;
+  // the sweeps above scribbled on the V-cycle work vectors
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  if (pi) {
+    CK(cudaMemsetAsync(d_corr32_, 0, n * sizeof(float), stream_));
+    CK(cudaMemsetAsync(d_resid32_, 0, n * sizeof(float), stream_));
+  } else {
+    CK(cudaMemsetAsync(vec_[kCORR], 0, n * sizeof(double), stream_));
+    CK(cudaMemsetAsync(vec_[kRESID], 0, n * sizeof(double), stream_));
+  }
+}
+
+int MacGpu::tuned_smoother(int precision, float *us, int n) const {
+  const int pi = precision == 1 ? 1 : 0;
+  for (int v = 0; v < n && v < kRbgsVariants; v++) us[v] = rbgs_us_[pi][v];
+  return rbgs_variant_[pi];
+}
+
+// per-cell factors of the device solve's FP64 operator on the finest tower
+void MacGpu::build_op_factors() {
+  const BlockList TL = tower_list(finest_);
+  const long w = (long)TL.n * ncell_;
+  if (w == 0) return;
+  if (tt_.ndim == 2)
+    k_op_prep<2><<<ew_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, d_opP_, d_opS_);
+  else
+    k_op_prep<3><<<ew_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, d_opP_, d_opS_);
+  CK(cudaGetLastError());
 }
 
 // FP32 copies of the coefficients for the FP32 V-cycle
@@ -591,7 +750,7 @@ void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *o
         BlockList sl = sublevel_list(l, ll);
         if (sl.n == 0) break;
         for (int rb = 0; rb < 2; rb++)
-          launch_smooth<T>(topo_, c, sl, rb, corr, resid, guard, stream_, prm_.pdl != 0);
+          launch_rbgs<T>(topo_, c, sl, rb, corr, resid, guard, stream_, prm_.pdl != 0, rbgs_var<T>());
       }
     }
   }
@@ -638,11 +797,11 @@ void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
   else
     vcycle_device<T>(L, resid, corr, c, PH);
   if (tt_.ndim == 2)
-    launch_k(pdl, k_apply_red<2, 0>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)PH, V,
-             (const double *)RHAT, d_st_, d_part_, d_cnt_);
+    launch_k(pdl, k_op_red<2, 0>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)PH, V,
+             (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
   else
-    launch_k(pdl, k_apply_red<3, 0>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)PH, V,
-             (const double *)RHAT, d_st_, d_part_, d_cnt_);
+    launch_k(pdl, k_op_red<3, 0>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)PH, V,
+             (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
   launch_k(pdl, k_supdate<T>, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, (const double *)R, (const double *)V,
            S, X, (const double *)PH, (const double *)d_vf_, resid, d_part_, d_cnt_);
   if (prm_.vcycle_kernel == 2)
@@ -652,11 +811,11 @@ void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
   else
     vcycle_device<T>(L, resid, corr, c, SH);
   if (tt_.ndim == 2)
-    launch_k(pdl, k_apply_red<2, 1>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)SH, Tt,
-             (const double *)S, d_st_, d_part_, d_cnt_);
+    launch_k(pdl, k_op_red<2, 1>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)SH, Tt,
+             (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
   else
-    launch_k(pdl, k_apply_red<3, 1>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)SH, Tt,
-             (const double *)S, d_st_, d_part_, d_cnt_);
+    launch_k(pdl, k_op_red<3, 1>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)SH, Tt,
+             (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
   launch_k(pdl, k_rupdate, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, X, (const double *)SH, R,
            (const double *)S, (const double *)Tt, (const double *)RHAT, d_part_, d_cnt_);
 }
@@ -705,6 +864,7 @@ void MacGpu::capture_loop(int precision) {
   graph_coop_ = prm_.vcycle_kernel;
   graph_pdl_ = prm_.pdl;
   graph_cc_ = prm_.cluster_cells;
+  graph_var_ = rbgs_variant_[precision == 1];
 }
 
 int MacGpu::cg_solve_device(SolveInfo *info) {
@@ -723,7 +883,8 @@ int MacGpu::cg_solve_enqueue() {
   if (!err_.empty() || !bottom_ready_) return -1;
   if (prm_.graph && (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
                      graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl ||
-                     graph_cc_ != prm_.cluster_cells))
+                     graph_cc_ != prm_.cluster_cells ||
+                     graph_var_ != rbgs_variant_[prm_.precision == 1]))
     return -1;
   if (prm_.vcycle_kernel && program_npost_ != prm_.n_post) return -1;
   return enqueue_solve();
@@ -742,11 +903,11 @@ int MacGpu::enqueue_solve() {
   // prologue: x0 = sol, x = 0, r = rhs - A x0, rhat = r, |r0|, rho
   k_pro_copy<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, vec_[kSOL], vec_[kX0], vec_[kX]);
   if (tt_.ndim == 2)
-    k_apply_red<2, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_st_,
-                                                         d_part_, d_cnt_);
+    k_op_red<2, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_opP_,
+                                                      d_opS_, d_st_, d_part_, d_cnt_);
   else
-    k_apply_red<3, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_st_,
-                                                         d_part_, d_cnt_);
+    k_op_red<3, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_opP_,
+                                                      d_opS_, d_st_, d_part_, d_cnt_);
   vcopy(TL, vec_[kRHAT], vec_[kR]);
   if (prm_.max_iter > 0) {
     if (prm_.graph) {
@@ -779,14 +940,18 @@ int MacGpu::prepare_device() {
   if (!err_.empty()) return -1;
   if (coef_version_ != fast_coef_version_) {
     refresh_fp32();
+    build_op_factors();
     build_bottom();
     fast_coef_version_ = coef_version_;
     if (!err_.empty()) return -1;
   }
+  tune_smoother(prm_.precision);
+  if (!err_.empty()) return -1;
   if (prm_.vcycle_kernel && program_npost_ != prm_.n_post) build_vcycle_program();
   if (prm_.graph && (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
                      graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl ||
-                     graph_cc_ != prm_.cluster_cells))
+                     graph_cc_ != prm_.cluster_cells ||
+                     graph_var_ != rbgs_variant_[prm_.precision == 1]))
     capture_loop(prm_.precision);
   return err_.empty() ? 0 : -1;
 }
@@ -830,9 +995,22 @@ int MacGpu::enqueue_kernel(int which, int L) {
   if (which == 0) {
     launch_apply<double>(topo_, c64_, tower_list(L), vec_[kSOL], vec_[kV], nullptr, nullptr, stream_);
   } else if (which == 1) {
-    launch_smooth<float>(topo_, c32_, sublevel_list(L, L), 0, d_corr32_, d_resid32_, nullptr, stream_);
+    launch_rbgs<float>(topo_, c32_, sublevel_list(L, L), 0, d_corr32_, d_resid32_, nullptr, stream_, false,
+                       rbgs_var<float>());
   } else if (which == 2) {
-    launch_smooth<double>(topo_, c64_, sublevel_list(L, L), 0, vec_[kCORR], vec_[kRESID], nullptr, stream_);
+    launch_rbgs<double>(topo_, c64_, sublevel_list(L, L), 0, vec_[kCORR], vec_[kRESID], nullptr, stream_, false,
+                        rbgs_var<double>());
+  } else if (which == 3) {
+    if (L != finest_) return -1;
+    const BlockList TL = tower_list(L);
+    const long w = (long)TL.n * ncell_;
+    CKR_(cudaMemsetAsync(d_st_, 0, sizeof(FState), stream_), -1);
+    if (tt_.ndim == 2)
+      k_op_red<2, 0><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kSOL], vec_[kV], vec_[kRHAT], d_opP_,
+                                                        d_opS_, d_st_, d_part_, d_cnt_);
+    else
+      k_op_red<3, 0><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kSOL], vec_[kV], vec_[kRHAT], d_opP_,
+                                                        d_opS_, d_st_, d_part_, d_cnt_);
   } else {
     return -1;
   }

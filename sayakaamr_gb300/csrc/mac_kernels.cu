@@ -14,6 +14,7 @@
 // The arithmetic is written operation by operation in the reference's order
 // (src/SayakaMacOperator.cpp:1115-1459) and this file is compiled without
 // FMA contraction, so FP64 results are bit-identical to the reference's.
+#include <algorithm>
 #include <cstdint>
 
 #include "mac_device.h"
@@ -66,6 +67,22 @@ __global__ void __launch_bounds__(kThreads) k_smooth(Topo t, Coef<T> c, BlockLis
     color_cell<ND>((int)(it - (long)p * nhalf), t.nb, color, ijk);
     smooth_cell<T, ND>(t, c, L.blocks[p], L.ftypes[p], ijk, phi, rhs);
   }
+}
+
+// the device solve's smoother (smooth_cell_fast): blockIdx.y walks the
+// blocks of the list, blockIdx.x the chunks of a block's half cells, so the
+// block id and face types are uniform across a CTA and no thread divides
+template <typename T, int ND, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_rbgs(Topo t, Coef<T> c, BlockList L, int color,
+                                                         T *__restrict__ phi, const T *__restrict__ rhs,
+                                                         const int *guard) {
+  pdl_enter();
+  if (guard && *guard) return;
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= (t.ncell >> 1)) return;
+  int ijk[3];
+  color_cell_fast<ND>(h, t, color, ijk);
+  for (int p = blockIdx.y; p < L.n; p += gridDim.y) smooth_cell_fast<T, ND>(t, c, L.blocks[p], L.ftypes[p], ijk, phi, rhs);
 }
 
 // ---------------------------------------------------------------------------
@@ -280,6 +297,39 @@ void launch_apply(const Topo &t, const Coef<T> &c, const BlockList &L, const T *
     launch_k(pdl, k_apply<T, 3>, grid_for(work), kThreads, 0, s, t, c, L, x, y, rhs, guard);
 }
 
+// variant v: launch bounds (256 threads, kRbgsMinBlocks[v] CTAs per SM), i.e.
+// a register cap of 65536 / (256 * min CTAs); same arithmetic in every variant
+template <typename T, int ND, int MINB>
+static void rbgs_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
+                    const int *guard, cudaStream_t s, bool pdl, dim3 grid, int threads) {
+  launch_k(pdl, k_rbgs<T, ND, MINB>, grid, threads, 0, s, t, c, L, color, phi, rhs, guard);
+}
+
+template <typename T, int ND>
+static void rbgs_nd(int variant, const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi,
+                    const T *rhs, const int *guard, cudaStream_t s, bool pdl, dim3 grid, int threads) {
+  switch (variant) {
+    case 0: rbgs_go<T, ND, 2>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
+    case 1: rbgs_go<T, ND, 3>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
+    case 2: rbgs_go<T, ND, 4>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
+    case 3: rbgs_go<T, ND, 6>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
+    default: rbgs_go<T, ND, 8>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
+  }
+}
+
+template <typename T>
+void launch_rbgs(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
+                 const int *guard, cudaStream_t s, bool pdl, int variant) {
+  const int nhalf = t.ncell / 2;
+  if (L.n == 0 || nhalf == 0) return;
+  const int threads = std::min(kThreads, (nhalf + 31) / 32 * 32);
+  const dim3 grid((nhalf + threads - 1) / threads, std::min(L.n, 65535));
+  if (t.ndim == 2)
+    rbgs_nd<T, 2>(variant, t, c, L, color, phi, rhs, guard, s, pdl, grid, threads);
+  else
+    rbgs_nd<T, 3>(variant, t, c, L, color, phi, rhs, guard, s, pdl, grid, threads);
+}
+
 template <typename T>
 void launch_smooth(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
                    const int *guard, cudaStream_t s, bool pdl) {
@@ -340,6 +390,8 @@ void launch_fix_bc(const Topo &t, const Coef<double> &c, const BlockList &L, con
                                 const int *, cudaStream_t, bool);                                               \
   template void launch_smooth<T>(const Topo &, const Coef<T> &, const BlockList &, int, T *, const T *,        \
                                  const int *, cudaStream_t, bool);                                              \
+  template void launch_rbgs<T>(const Topo &, const Coef<T> &, const BlockList &, int, T *, const T *,          \
+                               const int *, cudaStream_t, bool, int);                                           \
   template void launch_restrict<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,         \
                                    cudaStream_t, bool);                                                         \
   template void launch_prolong<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,          \

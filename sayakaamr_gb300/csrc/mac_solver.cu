@@ -271,6 +271,7 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
 
   topo_.ndim = nd;
   topo_.nb = nb;
+  topo_.lnb = (nb & (nb - 1)) == 0 ? __builtin_ctz((unsigned)nb) : -1;
   topo_.ncell = ncell_;
   topo_.nfb = nfb_;
   topo_.nblocks = nbk;
@@ -334,6 +335,8 @@ MacGpu::~MacGpu() {
   fr(d_corr32_);
   fr(d_st_);
   fr(d_part_);
+  fr(d_opP_);
+  fr(d_opS_);
   fr(d_cnt_);
   fr(d_binv_);
   fr(d_phases_);

@@ -33,6 +33,7 @@ struct SolverParams {
   int vcycle_kernel = 0;    // device path: 0 one launch per phase, 1 one cooperative launch, 2 cluster phases
   int pdl = 0;              // device path: programmatic dependent launch between the iteration's kernels
   int cluster_cells = 16384;  // vcycle_kernel 2: phases touching at most this many cells run in the cluster
+  int smooth_variant = -1;    // device smoother launch bounds: -1 autotune at prepare, else variant index
 };
 
 struct SolveInfo {
@@ -87,6 +88,7 @@ class MacGpu {
   int solve_state(SolveInfo *info);
   int enqueue_kernel(int which, int L);
   int tower_size(int L, int sublevel) const;
+  int tuned_smoother(int precision, float *us, int n) const;
 
   // building blocks, exposed for parity tests (compact arrays, all blocks)
   void apply(int L, const double *x_all, double *y_all);
@@ -157,6 +159,13 @@ class MacGpu {
   // device-resident path (mac_fast.cu)
   void ensure_fast_buffers();
   void refresh_fp32();
+  void build_op_factors();
+  void tune_smoother(int precision);
+  template <typename T>
+  int rbgs_var() const {
+    const int v = rbgs_variant_[sizeof(T) == 4 ? 1 : 0];
+    return v < 0 ? 2 : v;
+  }
   void build_bottom();
   template <typename T>
   void vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *out);
@@ -213,6 +222,7 @@ class MacGpu {
   Coef<float> c32_{};
   FState *d_st_ = nullptr, *h_st_ = nullptr;
   double *d_part_ = nullptr;
+  double *d_opP_ = nullptr, *d_opS_ = nullptr;  // factors of the device solve's operator
   unsigned *d_cnt_ = nullptr;
   double *d_binv_ = nullptr;
   int n_bot_ = 0, n_pins_ = 0;
@@ -220,7 +230,9 @@ class MacGpu {
   cudaGraphExec_t graph_exec_ = nullptr;
   int graph_prec_ = -1, graph_npost_ = -1;
   int kernels_per_iter_ = 0;
-  int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1;
+  int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1;
+  int rbgs_variant_[2] = {-1, -1};  // tuned smoother variant per precision (0 FP64, 1 FP32)
+  float rbgs_us_[2][8] = {};        // measured microseconds per variant
   // cooperative V-cycle
   VPhase *d_phases_ = nullptr;
   std::vector<VPhase> h_phases_;

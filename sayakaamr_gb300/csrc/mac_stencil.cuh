@@ -32,6 +32,31 @@ __device__ __forceinline__ void decode(int c, int nb, int ijk[3]) {
 
 __device__ __forceinline__ int encode(const int ijk[3], int nb) { return ijk[0] + nb * (ijk[1] + nb * ijk[2]); }
 
+// decode with shifts when nb is a power of two
+template <int ND>
+__device__ __forceinline__ void decode_fast(int c, const Topo &t, int ijk[3]) {
+  if (t.lnb >= 0) {
+    const int m = t.nb - 1;
+    ijk[0] = c & m;
+    ijk[1] = ND >= 2 ? (c >> t.lnb) & m : 0;
+    ijk[2] = ND == 3 ? c >> (2 * t.lnb) : 0;
+  } else {
+    decode<ND>(c, t.nb, ijk);
+  }
+}
+
+// flat (list entry, cell) index -> list entry p and cell ci (32-bit)
+template <int ND>
+__device__ __forceinline__ void split_cell(int it, const Topo &t, int &p, int &ci) {
+  if (t.lnb >= 0) {
+    p = it >> (ND * t.lnb);
+    ci = it & (t.ncell - 1);
+  } else {
+    p = it / t.ncell;
+    ci = it - p * t.ncell;
+  }
+}
+
 // face index of the face on side s of cell ijk in direction d (face-centred
 // valid box of the reference, first dimension fastest)
 __device__ __forceinline__ int face_index(int d, const int ijk[3], int s, int nb) {
@@ -221,6 +246,83 @@ __device__ __forceinline__ void smooth_cell(const Topo &t, const Coef<T> &c, int
   T unew = 0;
   if (vfv > 0) unew = (ld<CG>(&rhs[cb + ci]) * dv * vfv + off) / diag;
   phi[cb + ci] = unew;
+}
+
+__device__ __forceinline__ float fast_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double fast_div(double a, double b) { return a / b; }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// red-black update of the device solve's V-cycle: the smoother of
+// smooth_cell with 32-bit shift indexing, FMA accumulation and a fast
+// division.  Same face coefficients and gathers, different rounding; every
+// V-cycle variant of the device solve uses it, so they agree bit for bit.
+template <typename T, int ND, bool CG = false>
+__device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c, int b, uint16_t ft,
+                                                 const int ijk[3], T *__restrict__ phi, const T *__restrict__ rhs) {
+  const int nb = t.nb;
+  const int ci = t.lnb >= 0 ? ijk[0] + ((ijk[1] + (ijk[2] << t.lnb)) << t.lnb) : encode(ijk, nb);
+  const long cb = (long)b * t.ncell;
+  const long fb = (long)b * t.nfb;
+  const T dv = geom(c, b, 6);
+  T diag = c.alpha * dv;
+  T off = 0;
+#pragma unroll
+  for (int f = 0; f < 2 * ND; f++) {
+    const int d = f >> 1, s = f & 1;
+    const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+    // face index (first dimension fastest, nb+1 faces along d)
+    int fx;
+    if (d == 0)
+      fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+    else if (d == 1)
+      fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+    else
+      fx = ci + s * nb * nb;
+    if (!bnd) {
+      const T coef = c.tff[d][fb + fx];
+      const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+      diag += coef;
+      off = fma_t(coef, ld<CG>(&phi[cb + ci + (s ? stride : -stride)]), off);
+    } else {
+      const int ty = face_type_of(ft, f);
+      if (ty == 0) {
+        const T coef = c.tff[d][fb + fx];
+        diag += coef;
+        off = fma_t(coef, same_level_ghost<T, CG>(t, b, f, ijk, phi), off);
+      } else if (ty == 1) {
+        if (t.bc_type[b * 6 + f] != kBCNeumann) diag += c.tff[d][fb + fx] * (T)2.0;
+      } else if (ty == 2) {
+        const T coef = cf_coef(c, t, b, d, fx, (T)1.5);
+        diag += coef;
+        off = fma_t(coef, fine_crse_ghost<T, ND, CG>(t, b, f, ijk, phi), off);
+      } else {
+        diag += cf_coef(c, t, b, d, fx, (T)0.75);
+        off += crse_fine_sum<T, ND, CG>(t, c, b, f, ijk, phi);
+      }
+    }
+  }
+  const T vfv = c.vf[cb + ci];
+  T unew = 0;
+  if (vfv > 0) unew = fast_div(fma_t(ld<CG>(&rhs[cb + ci]) * dv, vfv, off), diag);
+  phi[cb + ci] = unew;
+}
+
+// colour cell with shifts when nb is a power of two
+template <int ND>
+__device__ __forceinline__ void color_cell_fast(int h, const Topo &t, int color, int ijk[3]) {
+  if (t.lnb < 1) {
+    const int hrow = t.nb >> 1;
+    const int row = h / hrow;
+    ijk[1] = ND >= 2 ? row % t.nb : 0;
+    ijk[2] = ND == 3 ? row / t.nb : 0;
+    ijk[0] = 2 * (h - row * hrow) + ((color + ijk[1] + ijk[2]) & 1);
+    return;
+  }
+  const int row = h >> (t.lnb - 1);
+  ijk[1] = ND >= 2 ? row & (t.nb - 1) : 0;
+  ijk[2] = ND == 3 ? row >> t.lnb : 0;
+  ijk[0] = 2 * (h & ((t.nb >> 1) - 1)) + ((color + ijk[1] + ijk[2]) & 1);
 }
 
 // cell (block-local index ijk) of colour `color` for the h-th half-cell of a block

@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kVT) k_vcycle_coop(Topo t, Coef<T> c, const VP
         const int p = (int)(it / nhalf);
         int ijk[3];
         color_cell<ND>((int)(it - (long)p * nhalf), t.nb, P.color, ijk);
-        smooth_cell<T, ND, true>(t, c, P.blocks[p], P.ftypes[p], ijk, corr, resid);
+        smooth_cell_fast<T, ND, true>(t, c, P.blocks[p], P.ftypes[p], ijk, corr, resid);
       }
     } else if (P.op == kPhaseProlong) {
       const long total = (long)P.n * ncell;
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kCT, 1) k_vcycle_cluster(Topo t, Coef<T> c, co
         const int p = (int)(it / nhalf);
         int ijk[3];
         color_cell<ND>((int)(it - (long)p * nhalf), t.nb, P.color, ijk);
-        smooth_cell<T, ND, true>(t, c, P.blocks[p], P.ftypes[p], ijk, corr, resid);
+        smooth_cell_fast<T, ND, true>(t, c, P.blocks[p], P.ftypes[p], ijk, corr, resid);
       }
     } else if (P.op == kPhaseProlong) {
       const long total = (long)P.n * ncell;
@@ -352,7 +352,7 @@ void MacGpu::vcycle_cluster(T *resid, T *corr, const Coef<T> &c, double *out) {
       case kPhaseRestrict: launch_restrict<T>(topo_, c, bl, resid, guard, stream_, pdl); break;
       case kPhaseBottom: bottom_launch<T>(resid, corr); break;
       case kPhaseProlong: launch_prolong<T>(topo_, c, bl, corr, guard, stream_, pdl); break;
-      case kPhaseSmooth: launch_smooth<T>(topo_, c, bl, P.color, corr, resid, guard, stream_, pdl); break;
+      case kPhaseSmooth: launch_rbgs<T>(topo_, c, bl, P.color, corr, resid, guard, stream_, pdl, rbgs_var<T>()); break;
       default: vc_out_launch<T>(bl, corr, out); break;
     }
     i++;

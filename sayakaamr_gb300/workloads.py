@@ -207,8 +207,9 @@ def config2(seed=2, nb=16, max_level=6, roots=2):
 
 
 def config3(seed=3, nb=16, max_level=5):
-    """3D, 16^3 blocks, 5 levels refined on the sphere r=0.2 (IB solid inside
-    a smaller seeded sphere, binary mask), B ratio 100 across a seeded blob."""
+    """3D, 16^3 blocks, 5 levels refined on the sphere r=0.2 (a band of 3
+    block widths: 3872 leaf blocks, 15.9M cells), IB solid sphere r=0.08
+    (binary mask), B ratio 100 across a seeded blob, p=0 on the top wall."""
     rng = np.random.default_rng(seed)
     bc_ = rng.uniform(0.35, 0.65, 3)
     br = rng.uniform(0.12, 0.18)
@@ -222,7 +223,7 @@ def config3(seed=3, nb=16, max_level=5):
         return r - br
 
     def need(lo, hi, level):
-        return _straddle(sphere, lo, hi, 0.2)
+        return _straddle(sphere, lo, hi, 3.0)
 
     t = refine_tree(3, nb, (1, 1, 1), (0, 0, 0), (1, 1, 1), 2, max_level, need)
     tb = t.tables()
@@ -238,7 +239,7 @@ def config3(seed=3, nb=16, max_level=5):
         rho = 1.0 + 99.0 * _smooth_heaviside(blob(pf), 2.0 * h)
         bface.append(1.0 / rho)
     f = gaussian_rhs(rng, pc, 3, sigma=0.08)
-    return _finish("config3", t, tb, vol, area, bface, f, True, dict(tol_rel=1e-8))
+    return _finish("config3", t, tb, vol, area, bface, f, True, dict(tol_rel=1e-8), dirichlet_faces=(5,))
 
 
 CONFIGS = {"config1": config1, "config2": config2, "config3": config3}

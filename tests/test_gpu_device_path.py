@@ -102,3 +102,25 @@ def test_programmatic_dependent_launch_is_transparent(name):
         out.append((info["iterations"], S.get_sol_compact()))
     assert out[0][0] == out[1][0]
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("name", ["t2s", "t3s"])
+def test_smoother_variants_are_bit_identical(name):
+    """the autotuner's launch-bounds variants differ in register caps only:
+    identical iterations and solutions, and the tuner reports its timings"""
+    g, t, tb, S = setup_solver(name)
+    S.set_rhs_compact(g["sv_rhs"])
+    out = []
+    for var in (-1, 0, 4):
+        S.set_zero_sol()
+        S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=1, bottom=1,
+                     smooth_variant=var)
+        info = S.cg_solve()
+        assert info["status"] == 0, info
+        out.append((info["iterations"], S.get_sol_compact()))
+        if var == -1:
+            v, us = S.tuned_smoother(1)
+            assert 0 <= v < 5 and all(u > 0 for u in us), (v, us)
+    for k in (1, 2):
+        assert out[0][0] == out[k][0], k
+        assert np.array_equal(out[0][1], out[k][1]), k
