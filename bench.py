@@ -53,7 +53,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="config2")
-    ap.add_argument("--precision", type=int, default=1, help="1: FP32 V-cycle (default), 0: FP64 V-cycle")
+    ap.add_argument("--precision", type=int, default=-1,
+                    help="V-cycle precision: 1 FP32, 0 FP64, -1 (default) the faster of the two, timed during "
+                         "warm-up (the outer BiCGSTAB and its 1e-8 test are FP64 either way)")
     ap.add_argument("--n-post", type=int, default=2, help="post-smoothing sweeps per level (setPostSmoothNum)")
     ap.add_argument("--pdl", type=int, default=0, help="programmatic dependent launch between kernels")
     ap.add_argument("--vcycle-kernel", type=int, default=0,
@@ -235,7 +237,8 @@ def main():
 
     prob = workloads.CONFIGS[args.config]()
     S = workloads.make_solver(prob)
-    S.set_params(tol_rel=TOL, tol_abs=0.0, use_mg_precond=1, max_iter=2000, precision=args.precision, bottom=1,
+    S.set_params(tol_rel=TOL, tol_abs=0.0, use_mg_precond=1, max_iter=2000, precision=max(args.precision, 0),
+                 bottom=1,
                  graph=0 if args.profile else 1, n_post_smooth=args.n_post, vcycle_kernel=args.vcycle_kernel,
                  cluster_cells=args.cluster_cells,
                  pdl=args.pdl)
@@ -258,10 +261,29 @@ def main():
             timed_events[1].record(ext)
         return S.solve_info()
 
-    for _ in range(args.warmup):
-        info = one()
-        if info["status"] != 0:
-            raise SystemExit("warm-up solve failed: %s" % info)
+    def warm():
+        for _ in range(args.warmup):
+            info = one()
+            if info["status"] != 0:
+                raise SystemExit("warm-up solve failed: %s" % info)
+
+    tuning = None
+    if args.precision < 0:
+        # the faster V-cycle precision on this workload, from timed warm-up solves
+        tuning = {}
+        for prec in (1, 0):
+            S.set_params(precision=prec)
+            S.prepare()
+            warm()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+            for e in ev:
+                one(e)
+            torch.cuda.synchronize()
+            tuning[prec] = statistics.mean(a.elapsed_time(b) for a, b in ev)
+        args.precision = min(tuning, key=tuning.get)
+        S.set_params(precision=args.precision)
+        S.prepare()
+    warm()
     if args.profile:
         torch.cuda.synchronize()
         torch.cuda.profiler.start()
@@ -321,7 +343,7 @@ def main():
     d2h = prob.num_blocks * prob.ncell * 8
 
     # ---- roofline of the dominant kernel, timed live on the solver stream ----
-    roof = roofline(S, prob, ext, torch, finest)
+    roof = roofline(S, prob, ext, torch, finest, args.precision)
 
     out = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
@@ -334,6 +356,7 @@ def main():
                                % (prob.ndim, prob.nb, prob.ndim, finest, len(prob.leaf)),
                    "leaf_cells": prob.leaf_cells, "blocks": prob.num_blocks, "tol_rel": TOL,
                    "l2": "flushed (256 MiB write) before every timed solve", "precision": args.precision,
+                   "precision_tuning_ms": tuning,
                    "iterations_per_solve": statistics.mean(iters), "n_post_smooth": args.n_post,
                    "vcycle_kernel": ("per-phase launches", "cooperative", "cluster")[args.vcycle_kernel],
                    "cluster_cells": args.cluster_cells if args.vcycle_kernel == 2 else None,
@@ -375,11 +398,13 @@ def kernel_only(S, prob, ext, torch, args):
                       "us_per_launch": a.elapsed_time(b) * 1e3 / args.steps}))
 
 
-def roofline(S, prob, ext, torch, finest):
-    """dominant kernel: the FP32 red-black sweep over the finest level of the
-    finest tower.  Algorithmic bytes per launch = cells of that level x
-    4 B x (2 + ndim): one colour reads/writes every phi once (half read, half
-    written), rhs and vf of the updated half, and every face coefficient."""
+def roofline(S, prob, ext, torch, finest, precision):
+    """dominant kernel: the red-black sweep (one colour) over the finest level
+    of the finest tower, in the V-cycle's precision, with the variant the
+    autotuner chose.  Algorithmic bytes per launch = cells of that level x
+    p x (2 + ndim) (p = 4 or 8 bytes): phi of the other colour read and the
+    updated colour written (p/2 + p/2), rhs and vf of the updated colour
+    (p/2 + p/2) and every face coefficient of the level (ndim x p)."""
     import json as _json
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, src = 6800.0, "fallback"
@@ -387,24 +412,32 @@ def roofline(S, prob, ext, torch, finest):
         with open(peaks_path) as f:
             peak = float(_json.load(f)["hbm_gbs"])
             src = "measured"
+    which = 1 if precision == 1 else 2
+    p = 4 if precision == 1 else 8
     nblk = S.tower_size(finest, finest)
     cells = nblk * prob.ncell
-    bytes_per_launch = cells * 4 * (2 + prob.ndim)
+    bytes_per_launch = cells * p * (2 + prob.ndim)
     reps = 200
     for _ in range(10):
-        S.enqueue_kernel(1, finest)
+        S.enqueue_kernel(which, finest)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(ext)
     for _ in range(reps):
-        S.enqueue_kernel(1, finest)
+        S.enqueue_kernel(which, finest)
     b.record(ext)
     torch.cuda.synchronize()
     us = a.elapsed_time(b) * 1e3 / reps
     achieved = bytes_per_launch / (us * 1e-6) / 1e9
-    return {"kernel": "k_smooth<float,2> (finest level, one colour)", "bound": "hbm", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-            "bytes_per_launch": bytes_per_launch, "us_per_launch": us, "peak_source": src + " (burst copy)",
-            "note": "working set is L2-resident at this size; traffic from profiles/"}
+    variant, _ = S.tuned_smoother(precision)
+    kind = "k_rbgs_tile (block staged in shared memory)" if variant >= 5 else "k_rbgs (one thread per cell)"
+    l2 = bytes_per_launch < 100e6
+    return {"kernel": "%s<%s,%dD>, autotuned variant %d, finest level, one colour"
+                      % (kind, "float" if p == 4 else "double", prob.ndim, variant),
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "bytes_per_launch": bytes_per_launch, "us_per_launch": us,
+            "peak_source": src + " (burst copy)",
+            "note": ("working set fits in L2 at this size: latency-bound; " if l2 else "") +
+                    "DRAM traffic per launch from the ncu summaries"}
 
 
 if __name__ == "__main__":

@@ -378,8 +378,8 @@ class MacSolver:
 
     def tuned_smoother(self, precision):
         """(chosen variant, microseconds per variant) of the smoother autotuner"""
-        us = (C.c_float * 5)()
-        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 5)
+        us = (C.c_float * 8)()
+        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 8)
         return int(v), [float(x) for x in us]
 
     def tower_size(self, L, sublevel=0):

@@ -87,7 +87,7 @@ void launch_smooth(const Topo &t, const Coef<T> &c, const BlockList &L, int colo
                    const T *rhs, const int *guard, cudaStream_t s, bool pdl = false);
 // the device solve's smoother (smooth_cell_fast); `variant` picks the
 // launch bounds (0..kRbgsVariants-1), chosen per workload by the autotuner
-constexpr int kRbgsVariants = 5;
+constexpr int kRbgsVariants = 8;
 template <typename T>
 void launch_rbgs(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi,
                    const T *rhs, const int *guard, cudaStream_t s, bool pdl = false,

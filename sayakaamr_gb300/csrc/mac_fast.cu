@@ -14,6 +14,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "mac_solver.h"
@@ -104,9 +105,9 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, d
   }
 }
 
-__device__ __forceinline__ long cell_of(const BlockList &L, int ncell, long it) {
-  const int p = (int)(it / ncell);
-  return (long)L.blocks[p] * ncell + (it - (long)p * ncell);
+__device__ __forceinline__ long cell_of(const BlockList &L, int ncell, int it) {
+  const int p = it / ncell;
+  return (long)L.blocks[p] * ncell + (it - p * ncell);
 }
 
 // ---- epilogues: the reference's scalar logic (src/SayakaMacSolver.cpp:766-904)
@@ -202,8 +203,8 @@ __global__ void k_set_cond(cudaGraphConditionalHandle h, const FState *st) {
 // x0 = sol, x = 0 on the tower
 __global__ void k_pro_copy(BlockList L, int ncell, const double *sol, double *x0, double *x) {
   pdl_enter();
-  const long total = (long)L.n * ncell;
-  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+  const int total = L.n * ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     const long q = cell_of(L, ncell, it);
     x0[q] = sol[q];
     x[q] = 0.0;
@@ -219,15 +220,14 @@ __global__ void k_pupdate(BlockList L, int ncell, const FState *st, const double
   if (st->done) return;
   const bool first = st->iter == 1;
   const double beta = st->beta, om = st->omega;
-  const long total = (long)L.n * ncell;
-  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+  const int total = L.n * ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     const long q = cell_of(L, ncell, it);
     double pv;
     if (first) {
       pv = r[q];
     } else {
-      const double p1 = 1.0 * p[q] + (-om) * v[q];
-      pv = 1.0 * r[q] + beta * p1;
+      pv = __fma_rn(beta, __fma_rn(-om, v[q], p[q]), r[q]);
     }
     p[q] = pv;
     resid[q] = vf[q] > 0 ? (T)pv : (T)0;
@@ -235,20 +235,21 @@ __global__ void k_pupdate(BlockList L, int ncell, const FState *st, const double
 }
 
 // s = r - alpha v ; x = x + alpha phat ; V-cycle residual = masked s ; |s|
-template <typename T>
+// (phat: the FP64 V-cycle's output itself, or the FP32 one widened to FP64)
+template <typename T, typename TP>
 __global__ void __launch_bounds__(kTPB) k_supdate(BlockList L, int ncell, FState *st, const double *r, const double *v,
-                                                double *s, double *x, const double *phat, const double *vf, T *resid,
+                                                double *s, double *x, const TP *phat, const double *vf, T *resid,
                                                 double *partials, unsigned *counter) {
   pdl_enter();
   if (st->done) return;
   const double a = st->alpha;
   double m[1] = {0.0};
-  const long total = (long)L.n * ncell;
-  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+  const int total = L.n * ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     const long q = cell_of(L, ncell, it);
-    const double sv = 1.0 * r[q] + (-a) * v[q];
+    const double sv = __fma_rn(-a, v[q], r[q]);
     s[q] = sv;
-    x[q] = 1.0 * x[q] + a * phat[q];
+    x[q] = __fma_rn(a, (double)phat[q], x[q]);
     resid[q] = vf[q] > 0 ? (T)sv : (T)0;
     m[0] = fmax(m[0], fabs(sv));
   }
@@ -256,21 +257,22 @@ __global__ void __launch_bounds__(kTPB) k_supdate(BlockList L, int ncell, FState
 }
 
 // x = x + omega shat ; r = s - omega t ; |r| ; rhat.r
-__global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, FState *st, double *x, const double *shat,
+template <typename T>
+__global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, FState *st, double *x, const T *shat,
                                                 double *r, const double *s, const double *t, const double *rhat,
                                                 double *partials, unsigned *counter) {
   pdl_enter();
   if (st->done) return;
   const double om = st->omega;
   double m[2] = {0.0, 0.0};
-  const long total = (long)L.n * ncell;
-  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+  const int total = L.n * ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     const long q = cell_of(L, ncell, it);
-    x[q] = 1.0 * x[q] + om * shat[q];
-    const double rv = 1.0 * s[q] + (-om) * t[q];
+    x[q] = __fma_rn(om, (double)shat[q], x[q]);
+    const double rv = __fma_rn(-om, t[q], s[q]);
     r[q] = rv;
     m[0] = fmax(m[0], fabs(rv));
-    m[1] += rhat[q] * rv;
+    m[1] = __fma_rn(rhat[q], rv, m[1]);
   }
   grid_reduce<2>(m, 1u, partials, counter, EpiEnd{st});
 }
@@ -279,8 +281,8 @@ __global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, FState
 __global__ void k_finish(BlockList L, int ncell, const FState *st, double *x0, const double *x, double *sol) {
   pdl_enter();
   if (!st->conv) return;
-  const long total = (long)L.n * ncell;
-  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+  const int total = L.n * ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     const long q = cell_of(L, ncell, it);
     const double v = x0[q] + x[q];
     x0[q] = v;
@@ -293,8 +295,8 @@ template <typename T>
 __global__ void k_vc_out(BlockList L, int ncell, const FState *st, const T *corr, double *out) {
   pdl_enter();
   if (st->done) return;
-  const long total = (long)L.n * ncell;
-  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+  const int total = L.n * ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     const long q = cell_of(L, ncell, it);
     out[q] = 0.0 + (double)corr[q];
   }
@@ -349,9 +351,9 @@ __global__ void __launch_bounds__(kTPB) k_op_prep(Topo t, Coef<double> c, BlockL
 }
 
 // sum T * phi_nb over the faces of cell ijk that are not physical boundaries
-template <int ND>
+template <int ND, typename TX>
 __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &c, int b, uint16_t ft,
-                                             const int ijk[3], int ci, const double *__restrict__ x) {
+                                             const int ijk[3], int ci, const TX *__restrict__ x) {
   using namespace stencil;
   const int nb = t.nb;
   const long cb = (long)b * t.ncell;
@@ -363,13 +365,13 @@ __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &
     const int fx = face_index(d, ijk, s, nb);
     if (!bnd) {
       const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
-      off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], x[cb + ci + (s ? stride : -stride)], off);
+      off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], (double)x[cb + ci + (s ? stride : -stride)], off);
     } else {
       const int ty = face_type_of(ft, f);
       if (ty == 0)
-        off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], same_level_ghost<double, false>(t, b, f, ijk, x), off);
+        off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], (double)same_level_ghost<TX, false>(t, b, f, ijk, x), off);
       else if (ty == 2)
-        off = __fma_rn(cf_coef(c, t, b, d, fx, 1.5), fine_crse_ghost<double, ND, false>(t, b, f, ijk, x), off);
+        off = __fma_rn(cf_coef(c, t, b, d, fx, 1.5), (double)fine_crse_ghost<TX, ND, false>(t, b, f, ijk, x), off);
       else if (ty == 3)
         off += crse_fine_sum<double, ND, false>(t, c, b, f, ijk, x);
     }
@@ -380,8 +382,8 @@ __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &
 // operator fused with its dot products:
 // MODE 0: y = A x, rhat.y (EpiAlpha) ; MODE 1: y = A x, y.w, y.y (EpiOmega) ;
 // MODE 2: y = w - A x (0 where vf = 0), |y|, y.y (EpiInit)
-template <int ND, int MODE>
-__global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockList L, const double *__restrict__ x,
+template <int ND, int MODE, typename TX>
+__global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockList L, const TX *__restrict__ x,
                                                double *__restrict__ y, const double *__restrict__ w,
                                                const double *__restrict__ P, const double *__restrict__ S,
                                                FState *st, double *partials, unsigned *counter) {
@@ -396,9 +398,9 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
     decode_fast<ND>(ci, t, ijk);
     const int b = L.blocks[p];
     const long q = (long)b * t.ncell + ci;
-    const double off = op_offdiag<ND>(t, c, b, L.ftypes[p], ijk, ci, x);
+    const double off = op_offdiag<ND, TX>(t, c, b, L.ftypes[p], ijk, ci, x);
     const double sc = S[q];
-    double yv = __fma_rn(x[q], P[q], -off * sc);
+    double yv = __fma_rn((double)x[q], P[q], -off * sc);
     if (MODE == 2) yv = sc != 0.0 ? w[q] - yv : 0.0;
     y[q] = yv;
     if (MODE == 0) acc[0] = __fma_rn(w[q], yv, acc[0]);
@@ -754,7 +756,7 @@ void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *o
       }
     }
   }
-  vc_out_launch<T>(tower_list(L), corr, out);
+  if (out) vc_out_launch<T>(tower_list(L), corr, out);
 }
 
 // V-cycle result on the tower, widened to FP64: out = 0 + corr
@@ -785,38 +787,47 @@ void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
   const int L = finest_;
   BlockList TL = tower_list(L);
   const long w = (long)TL.n * ncell_;
-  double *R = vec_[kR], *RHAT = vec_[kRHAT], *P = vec_[kP], *PH = vec_[kPHAT], *S = vec_[kS], *SH = vec_[kSHAT];
+  // An FP64 V-cycle's output (corr) serves as phat and later as shat: phat
+  // is consumed before the second V-cycle overwrites corr.  An FP32 V-cycle's
+  // output is widened once into FP64 phat / shat (widening inside the FP64
+  // kernels would cost one FP64-pipe conversion per neighbour read).
+  double *R = vec_[kR], *RHAT = vec_[kRHAT], *P = vec_[kP], *S = vec_[kS];
+  constexpr bool widen = sizeof(T) == 4;
+  using TO = typename std::conditional<widen, double, T>::type;
+  double *out_p = widen ? vec_[kPHAT] : nullptr, *out_s = widen ? vec_[kSHAT] : nullptr;
+  const TO *PH = widen ? reinterpret_cast<const TO *>(vec_[kPHAT]) : reinterpret_cast<const TO *>(corr);
+  const TO *SH = widen ? reinterpret_cast<const TO *>(vec_[kSHAT]) : reinterpret_cast<const TO *>(corr);
   double *V = vec_[kV], *Tt = vec_[kT], *X = vec_[kX];
   const bool pdl = prm_.pdl != 0;
   launch_k(pdl, k_pupdate<T>, ew_grid(w), kTPB, 0, stream_, TL, ncell_, (const FState *)d_st_, (const double *)R, P,
            (const double *)V, (const double *)d_vf_, resid);
   if (prm_.vcycle_kernel == 2)
-    vcycle_cluster<T>(resid, corr, c, PH);
+    vcycle_cluster<T>(resid, corr, c, out_p);
   else if (prm_.vcycle_kernel == 1)
-    vcycle_coop<T>(resid, corr, c, PH);
+    vcycle_coop<T>(resid, corr, c, out_p);
   else
-    vcycle_device<T>(L, resid, corr, c, PH);
+    vcycle_device<T>(L, resid, corr, c, out_p);
   if (tt_.ndim == 2)
-    launch_k(pdl, k_op_red<2, 0>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)PH, V,
+    launch_k(pdl, k_op_red<2, 0, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, PH, V,
              (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
   else
-    launch_k(pdl, k_op_red<3, 0>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)PH, V,
+    launch_k(pdl, k_op_red<3, 0, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, PH, V,
              (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
-  launch_k(pdl, k_supdate<T>, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, (const double *)R, (const double *)V,
-           S, X, (const double *)PH, (const double *)d_vf_, resid, d_part_, d_cnt_);
+  launch_k(pdl, k_supdate<T, TO>, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, (const double *)R, (const double *)V,
+           S, X, PH, (const double *)d_vf_, resid, d_part_, d_cnt_);
   if (prm_.vcycle_kernel == 2)
-    vcycle_cluster<T>(resid, corr, c, SH);
+    vcycle_cluster<T>(resid, corr, c, out_s);
   else if (prm_.vcycle_kernel == 1)
-    vcycle_coop<T>(resid, corr, c, SH);
+    vcycle_coop<T>(resid, corr, c, out_s);
   else
-    vcycle_device<T>(L, resid, corr, c, SH);
+    vcycle_device<T>(L, resid, corr, c, out_s);
   if (tt_.ndim == 2)
-    launch_k(pdl, k_op_red<2, 1>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)SH, Tt,
+    launch_k(pdl, k_op_red<2, 1, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, SH, Tt,
              (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
   else
-    launch_k(pdl, k_op_red<3, 1>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)SH, Tt,
+    launch_k(pdl, k_op_red<3, 1, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, SH, Tt,
              (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
-  launch_k(pdl, k_rupdate, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, X, (const double *)SH, R,
+  launch_k(pdl, k_rupdate<TO>, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, X, SH, R,
            (const double *)S, (const double *)Tt, (const double *)RHAT, d_part_, d_cnt_);
 }
 
@@ -903,10 +914,10 @@ int MacGpu::enqueue_solve() {
   // prologue: x0 = sol, x = 0, r = rhs - A x0, rhat = r, |r0|, rho
   k_pro_copy<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, vec_[kSOL], vec_[kX0], vec_[kX]);
   if (tt_.ndim == 2)
-    k_op_red<2, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_opP_,
+    k_op_red<2, 2, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_opP_,
                                                       d_opS_, d_st_, d_part_, d_cnt_);
   else
-    k_op_red<3, 2><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_opP_,
+    k_op_red<3, 2, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_opP_,
                                                       d_opS_, d_st_, d_part_, d_cnt_);
   vcopy(TL, vec_[kRHAT], vec_[kR]);
   if (prm_.max_iter > 0) {
@@ -1006,10 +1017,10 @@ int MacGpu::enqueue_kernel(int which, int L) {
     const long w = (long)TL.n * ncell_;
     CKR_(cudaMemsetAsync(d_st_, 0, sizeof(FState), stream_), -1);
     if (tt_.ndim == 2)
-      k_op_red<2, 0><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kSOL], vec_[kV], vec_[kRHAT], d_opP_,
+      k_op_red<2, 0, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kSOL], vec_[kV], vec_[kRHAT], d_opP_,
                                                         d_opS_, d_st_, d_part_, d_cnt_);
     else
-      k_op_red<3, 0><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kSOL], vec_[kV], vec_[kRHAT], d_opP_,
+      k_op_red<3, 0, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kSOL], vec_[kV], vec_[kRHAT], d_opP_,
                                                         d_opS_, d_st_, d_part_, d_cnt_);
   } else {
     return -1;

@@ -297,6 +297,147 @@ void launch_apply(const Topo &t, const Coef<T> &c, const BlockList &L, const T *
     launch_k(pdl, k_apply<T, 3>, grid_for(work), kThreads, 0, s, t, c, L, x, y, rhs, guard);
 }
 
+// The same sweep with the block staged in shared memory: one CTA per block
+// of the list loads the block's phi tile (full sectors) and, once per
+// boundary face cell of the sweep's colour, the face's contribution
+// (diagonal part hc, off-diagonal factor hk and value hv: FINE_FINE and
+// FINE_CRSE give T and the gathered ghost, CRSE_FINE the coarse-side T, 1 and
+// the fine-side sum, physical faces 0 or 2T and 0); cells then read their
+// neighbours from the tile.  Every value is combined in smooth_cell_fast's
+// order with the same operations, so the result is bit-identical.  The tile
+// (both colours, black cells unchanged) is written back whole.
+template <typename T, int ND, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c, BlockList L, int color,
+                                                              T *__restrict__ phi, const T *__restrict__ rhs,
+                                                              const int *guard) {
+  extern __shared__ __align__(16) unsigned char rbgs_smem[];
+  pdl_enter();
+  if (guard && *guard) return;
+  const int nb = t.nb, ncell = t.ncell, nhalf = ncell >> 1;
+  const int nface = ND == 3 ? nb * nb : nb;  // cells on one block face
+  T *tile = reinterpret_cast<T *>(rbgs_smem);
+  T *hc = tile + ncell;
+  T *hk = hc + 2 * ND * nface;
+  T *hv = hk + 2 * ND * nface;
+  for (int p = blockIdx.x; p < L.n; p += gridDim.x) {
+    const int b = L.blocks[p];
+    const uint16_t ft = L.ftypes[p];
+    const long cb = (long)b * ncell;
+    const long fb = (long)b * t.nfb;
+    if ((ncell & 3) == 0 && sizeof(T) == 4) {
+      const float4 *src = reinterpret_cast<const float4 *>(phi + cb);
+      float4 *dst = reinterpret_cast<float4 *>(tile);
+      for (int i = threadIdx.x; i < (ncell >> 2); i += blockDim.x) dst[i] = src[i];
+    } else {
+      for (int i = threadIdx.x; i < ncell; i += blockDim.x) tile[i] = phi[cb + i];
+    }
+    // boundary contributions of the cells of this colour
+    for (int e = threadIdx.x; e < 2 * ND * nface; e += blockDim.x) {
+      const int f = e / nface, m = e - f * nface;
+      const int d = f >> 1, s = f & 1;
+      int ijk[3];
+      ijk[d] = s ? nb - 1 : 0;
+      const int q0 = d == 0 ? 1 : 0, q1 = d == 2 ? 1 : 2;
+      ijk[q0] = m % nb;
+      if (ND == 3) ijk[q1] = m / nb;
+      else if (d != 2) ijk[2] = 0;
+      if (ND == 2) ijk[2] = 0;
+      if (((ijk[0] + ijk[1] + ijk[2]) & 1) != color) continue;
+      int fx;
+      if (d == 0)
+        fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+      else if (d == 1)
+        fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+      else
+        fx = encode(ijk, nb) + s * nb * nb;
+      const int ty = face_type_of(ft, f);
+      T vc = 0, vk = 0, vv = 0;
+      if (ty == 0) {
+        vc = vk = c.tff[d][fb + fx];
+        vv = same_level_ghost<T, false>(t, b, f, ijk, phi);
+      } else if (ty == 1) {
+        if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
+      } else if (ty == 2) {
+        vc = vk = cf_coef(c, t, b, d, fx, (T)1.5);
+        vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi);
+      } else {
+        vc = cf_coef(c, t, b, d, fx, (T)0.75);
+        vk = (T)1;
+        vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi);
+      }
+      hc[e] = vc;
+      hk[e] = vk;
+      hv[e] = vv;
+    }
+    __syncthreads();
+    const T dv = geom(c, b, 6);
+    for (int h = threadIdx.x; h < nhalf; h += blockDim.x) {
+      int ijk[3];
+      color_cell_fast<ND>(h, t, color, ijk);
+      const int ci = t.lnb >= 0 ? ijk[0] + ((ijk[1] + (ijk[2] << t.lnb)) << t.lnb) : encode(ijk, nb);
+      T diag = c.alpha * dv;
+      T off = 0;
+#pragma unroll
+      for (int f = 0; f < 2 * ND; f++) {
+        const int d = f >> 1, s = f & 1;
+        const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+        if (!bnd) {
+          int fx;
+          if (d == 0)
+            fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+          else if (d == 1)
+            fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+          else
+            fx = ci + s * nb * nb;
+          const T coef = c.tff[d][fb + fx];
+          const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+          diag += coef;
+          off = fma_t(coef, tile[ci + (s ? stride : -stride)], off);
+        } else {
+          const int q0 = d == 0 ? 1 : 0, q1 = d == 2 ? 1 : 2;
+          const int m = ijk[q0] + (ND == 3 ? nb * ijk[q1] : 0);
+          const int e = f * nface + m;
+          diag += hc[e];
+          off = fma_t(hk[e], hv[e], off);
+        }
+      }
+      const T vfv = c.vf[cb + ci];
+      T unew = 0;
+      if (vfv > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+      tile[ci] = unew;
+    }
+    __syncthreads();
+    if ((ncell & 3) == 0 && sizeof(T) == 4) {
+      const float4 *src = reinterpret_cast<const float4 *>(tile);
+      float4 *dst = reinterpret_cast<float4 *>(phi + cb);
+      for (int i = threadIdx.x; i < (ncell >> 2); i += blockDim.x) dst[i] = src[i];
+    } else {
+      for (int i = threadIdx.x; i < ncell; i += blockDim.x) phi[cb + i] = tile[i];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int ND>
+static size_t rbgs_tile_smem(const Topo &t) {
+  const int nface = ND == 3 ? t.nb * t.nb : t.nb;
+  return sizeof(T) * ((size_t)t.ncell + 3 * 2 * ND * (size_t)nface);
+}
+
+template <typename T, int ND, int MINB>
+static void rbgs_tile_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
+                         const int *guard, cudaStream_t s, bool pdl) {
+  const size_t smem = rbgs_tile_smem<T, ND>(t);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_rbgs_tile<T, ND, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  const int threads = std::min(kThreads, ((t.ncell >> 1) + 31) / 32 * 32);
+  const int grid = std::min(L.n, 152 * 64);
+  launch_k(pdl, k_rbgs_tile<T, ND, MINB>, grid, threads, smem, s, t, c, L, color, phi, rhs, guard);
+}
+
 // variant v: launch bounds (256 threads, kRbgsMinBlocks[v] CTAs per SM), i.e.
 // a register cap of 65536 / (256 * min CTAs); same arithmetic in every variant
 template <typename T, int ND, int MINB>
@@ -313,7 +454,10 @@ static void rbgs_nd(int variant, const Topo &t, const Coef<T> &c, const BlockLis
     case 1: rbgs_go<T, ND, 3>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
     case 2: rbgs_go<T, ND, 4>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
     case 3: rbgs_go<T, ND, 6>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
-    default: rbgs_go<T, ND, 8>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
+    case 4: rbgs_go<T, ND, 8>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
+    case 5: rbgs_tile_go<T, ND, 2>(t, c, L, color, phi, rhs, guard, s, pdl); break;
+    case 6: rbgs_tile_go<T, ND, 4>(t, c, L, color, phi, rhs, guard, s, pdl); break;
+    default: rbgs_tile_go<T, ND, 6>(t, c, L, color, phi, rhs, guard, s, pdl); break;
   }
 }
 
@@ -322,6 +466,9 @@ void launch_rbgs(const Topo &t, const Coef<T> &c, const BlockList &L, int color,
                  const int *guard, cudaStream_t s, bool pdl, int variant) {
   const int nhalf = t.ncell / 2;
   if (L.n == 0 || nhalf == 0) return;
+  // the tiled variants need the tile and halo in shared memory (<= 200 KiB)
+  const size_t tile = t.ndim == 2 ? rbgs_tile_smem<T, 2>(t) : rbgs_tile_smem<T, 3>(t);
+  if (variant >= 5 && tile > 200 * 1024) variant = 3;
   const int threads = std::min(kThreads, (nhalf + 31) / 32 * 32);
   const dim3 grid((nhalf + threads - 1) / threads, std::min(L.n, 65535));
   if (t.ndim == 2)

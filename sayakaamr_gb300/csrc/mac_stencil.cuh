@@ -82,9 +82,9 @@ __device__ __forceinline__ T cf_coef(const Coef<T> &c, const Topo &t, int b, int
 // CRSE_FINE face: sum of the fine-side contributions T_f * phi_f over the
 // fine faces covering coarse face (d, s) of cell ijk of block b, in the
 // reference's RESTRICT_SUM order (lower transverse dimension fastest)
-template <typename T, int ND, bool CG = false>
+template <typename T, int ND, bool CG = false, typename TX = T>
 __device__ __forceinline__ T crse_fine_sum(const Topo &t, const Coef<T> &c, int b, int f, const int ijk[3],
-                                           const T *__restrict__ x) {
+                                           const TX *__restrict__ x) {
   const int nb = t.nb, half = nb >> 1;
   const int d = f >> 1, s = f & 1;
   const int N = t.neighbor[b * 6 + f];
@@ -112,7 +112,7 @@ __device__ __forceinline__ T crse_fine_sum(const Topo &t, const Coef<T> &c, int 
       if (ND == 2) fi[2] = 0;
       const int fx = face_index(d, fi, fside, nb);
       const T tf = cf_coef(c, t, F, d, fx, h15);
-      val += tf * ld<CG>(&x[(long)F * t.ncell + encode(fi, nb)]);
+      val += tf * (T)ld<CG>(&x[(long)F * t.ncell + encode(fi, nb)]);
     }
   }
   return val;

@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kVT) k_vcycle_coop(Topo t, Coef<T> c, const VP
           if (lane == 0) corr[(long)bblocks[row / ncell] * ncell + row % ncell] = (T)s;
         }
       }
-    } else {  // kPhaseOut: phat (FP64) = 0 + corr over the tower
+    } else if (out) {  // kPhaseOut: phat (FP64) = 0 + corr over the tower
       const long total = (long)P.n * ncell;
       for (long it = tid; it < total; it += nthr) {
         const int p = (int)(it / ncell);
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(kCT, 1) k_vcycle_cluster(Topo t, Coef<T> c, co
         const int p = (int)(it / ncell);
         prolong_cell<T, ND, true>(t, c, P.blocks[p], (int)(it - (long)p * ncell), corr);
       }
-    } else if (P.op == kPhaseOut) {
+    } else if (P.op == kPhaseOut && out) {
       const long total = (long)P.n * ncell;
       for (long it = tid; it < total; it += nthr) {
         const int p = (int)(it / ncell);
@@ -353,7 +353,9 @@ void MacGpu::vcycle_cluster(T *resid, T *corr, const Coef<T> &c, double *out) {
       case kPhaseBottom: bottom_launch<T>(resid, corr); break;
       case kPhaseProlong: launch_prolong<T>(topo_, c, bl, corr, guard, stream_, pdl); break;
       case kPhaseSmooth: launch_rbgs<T>(topo_, c, bl, P.color, corr, resid, guard, stream_, pdl, rbgs_var<T>()); break;
-      default: vc_out_launch<T>(bl, corr, out); break;
+      default:
+        if (out) vc_out_launch<T>(bl, corr, out);
+        break;
     }
     i++;
   }
