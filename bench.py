@@ -65,6 +65,8 @@ def parse():
                     help="vcycle-kernel 2: largest phase (cells) that runs inside the cluster")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--smooth-variant", type=int, default=-1,
+                    help="device smoother launch-bounds variant (-1: autotuned at prepare)")
     ap.add_argument("--kernel", type=int, default=-1,
                     help="time one kernel alone and exit (for ncu): 0 FP64 operator on the finest tower, "
                          "1 FP32 / 2 FP64 red-black sweep (one colour) of the finest level, "
@@ -240,7 +242,7 @@ def main():
     S.set_params(tol_rel=TOL, tol_abs=0.0, use_mg_precond=1, max_iter=2000, precision=max(args.precision, 0),
                  bottom=1,
                  graph=0 if args.profile else 1, n_post_smooth=args.n_post, vcycle_kernel=args.vcycle_kernel,
-                 cluster_cells=args.cluster_cells,
+                 cluster_cells=args.cluster_cells, smooth_variant=args.smooth_variant,
                  pdl=args.pdl)
     S.prepare()
     ext = torch.cuda.ExternalStream(S.stream())

@@ -45,6 +45,9 @@ struct BlockList {
   const int *blocks;
   const uint16_t *ftypes;  // may be null for lists that need no face types
   int n;
+  // FP64 smoother factors of a tower sublevel list, [entry][cell]:
+  // sa = dv*vf/diag, ia = 1/diag (0 where vf = 0); null when not built
+  const double *sa = nullptr, *ia = nullptr;
 };
 
 // BiCGSTAB state kept on the device (FP64 scalars and control flags) by the
@@ -69,6 +72,7 @@ struct VPhase {
   int pad;
   const int *blocks;
   const uint16_t *ftypes;
+  const double *sa, *ia;  // FP64 smoother factors (see BlockList)
 };
 
 // ---- launchers (mac_kernels.cu) ----

@@ -350,6 +350,48 @@ __global__ void __launch_bounds__(kTPB) k_op_prep(Topo t, Coef<double> c, BlockL
   }
 }
 
+// Factors of the FP64 smoother for every cell of a tower's block list:
+// sa = dv*vf/diag, ia = 1/diag (0 where vf = 0), diag = alpha*dv + sum of
+// the face coefficients with this tower's face types (physical Dirichlet
+// faces twice, Neumann faces not at all), so the sweep needs no FP64 division
+// and no diagonal sum.
+template <int ND>
+__global__ void __launch_bounds__(kTPB) k_smooth_factors(Topo t, Coef<double> c, BlockList L, double *sa,
+                                                        double *ia) {
+  using namespace stencil;
+  const int nb = t.nb, total = L.n * t.ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+    int p, ci, ijk[3];
+    split_cell<ND>(it, t, p, ci);
+    decode_fast<ND>(ci, t, ijk);
+    const int b = L.blocks[p];
+    const uint16_t ft = L.ftypes[p];
+    const double dv = geom(c, b, 6);
+    double diag = c.alpha * dv;
+    for (int f = 0; f < 2 * ND; f++) {
+      const int d = f >> 1, s = f & 1;
+      const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+      const int fx = face_index(d, ijk, s, nb);
+      const double tf = c.tff[d][(long)b * t.nfb + fx];
+      if (!bnd) {
+        diag += tf;
+        continue;
+      }
+      const int ty = face_type_of(ft, f);
+      if (ty == 0)
+        diag += tf;
+      else if (ty == 1)
+        diag += t.bc_type[b * 6 + f] == kBCNeumann ? 0.0 : 2.0 * tf;
+      else
+        diag += cf_coef(c, t, b, d, fx, ty == 2 ? 1.5 : 0.75);
+    }
+    const double vfv = c.vf[(long)b * t.ncell + ci];
+    const long o = (long)p * t.ncell + ci;
+    sa[o] = vfv > 0 ? dv * vfv / diag : 0.0;
+    ia[o] = vfv > 0 ? 1.0 / diag : 0.0;
+  }
+}
+
 // sum T * phi_nb over the faces of cell ijk that are not physical boundaries
 template <int ND, typename TX>
 __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &c, int b, uint16_t ft,
@@ -510,6 +552,26 @@ void MacGpu::ensure_fast_buffers() {
   }
   c32_.vf = d_vf32_;
   fast_ready_ = true;
+}
+
+// FP64 smoother factors for the towers the V-cycle smooths (2 .. finest)
+void MacGpu::build_smooth_factors() {
+  if ((int)d_sfac_.size() < finest_ + 1) d_sfac_.resize(finest_ + 1, nullptr);
+  for (int l = 2; l <= finest_; l++) {
+    const BlockList TL = tower_list(l);
+    const long w = (long)TL.n * ncell_;
+    if (w == 0) continue;
+    if (!d_sfac_[l] && cudaMalloc(&d_sfac_[l], 2 * w * sizeof(double)) != cudaSuccess) {
+      d_sfac_[l] = nullptr;
+      fail("out of device memory (smoother factors)");
+      return;
+    }
+    if (tt_.ndim == 2)
+      k_smooth_factors<2><<<ew_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, d_sfac_[l], d_sfac_[l] + w);
+    else
+      k_smooth_factors<3><<<ew_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, d_sfac_[l], d_sfac_[l] + w);
+    CK(cudaGetLastError());
+  }
 }
 
 // Autotuner of the device smoother: every launch-bounds variant (register
@@ -952,6 +1014,7 @@ int MacGpu::prepare_device() {
   if (coef_version_ != fast_coef_version_) {
     refresh_fp32();
     build_op_factors();
+    build_smooth_factors();
     build_bottom();
     fast_coef_version_ = coef_version_;
     if (!err_.empty()) return -1;

@@ -82,7 +82,11 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs(Topo t, Coef<T> c, Bloc
   if (h >= (t.ncell >> 1)) return;
   int ijk[3];
   color_cell_fast<ND>(h, t, color, ijk);
-  for (int p = blockIdx.y; p < L.n; p += gridDim.y) smooth_cell_fast<T, ND>(t, c, L.blocks[p], L.ftypes[p], ijk, phi, rhs);
+  for (int p = blockIdx.y; p < L.n; p += gridDim.y) {
+    const long fo = (long)p * t.ncell;
+    smooth_cell_fast<T, ND>(t, c, L.blocks[p], L.ftypes[p], ijk, phi, rhs, L.sa ? L.sa + fo : nullptr,
+                            L.ia ? L.ia + fo : nullptr);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -401,9 +405,14 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
           off = fma_t(hk[e], hv[e], off);
         }
       }
-      const T vfv = c.vf[cb + ci];
       T unew = 0;
-      if (vfv > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+      if (sizeof(T) == 8 && L.sa) {
+        const long fo = (long)p * ncell + ci;
+        unew = fma_t(rhs[cb + ci], (T)L.sa[fo], off * (T)L.ia[fo]);
+      } else {
+        const T vfv = c.vf[cb + ci];
+        if (vfv > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+      }
       tile[ci] = unew;
     }
     __syncthreads();

@@ -336,6 +336,7 @@ MacGpu::~MacGpu() {
   fr(d_st_);
   fr(d_part_);
   fr(d_opP_);
+  for (auto &q : d_sfac_) fr(q);
   fr(d_opS_);
   fr(d_cnt_);
   fr(d_binv_);
@@ -357,7 +358,13 @@ BlockList MacGpu::tower_list(int L) const {
 BlockList MacGpu::sublevel_list(int L, int l) const {
   const DevTower &t = towers_[L];
   const int b = t.begin[l], e = t.end[l];
-  return BlockList{t.all.blocks + b, t.all.ftypes + b, e - b};
+  BlockList r{t.all.blocks + b, t.all.ftypes + b, e - b};
+  if (L < (int)d_sfac_.size() && d_sfac_[L]) {
+    const long w = (long)t.all.n * ncell_;
+    r.sa = d_sfac_[L] + (long)b * ncell_;
+    r.ia = d_sfac_[L] + w + (long)b * ncell_;
+  }
+  return r;
 }
 BlockList MacGpu::level_list(int l) const { return BlockList{levels_[l].blocks, nullptr, levels_[l].n}; }
 BlockList MacGpu::nonleaf_list(int l) const { return BlockList{nonleaf_[l].blocks, nullptr, nonleaf_[l].n}; }

@@ -160,6 +160,7 @@ class MacGpu {
   void ensure_fast_buffers();
   void refresh_fp32();
   void build_op_factors();
+  void build_smooth_factors();
   void tune_smoother(int precision);
   template <typename T>
   int rbgs_var() const {
@@ -223,6 +224,7 @@ class MacGpu {
   FState *d_st_ = nullptr, *h_st_ = nullptr;
   double *d_part_ = nullptr;
   double *d_opP_ = nullptr, *d_opS_ = nullptr;  // factors of the device solve's operator
+  std::vector<double *> d_sfac_;                // FP64 smoother factors per tower: sa then ia
   unsigned *d_cnt_ = nullptr;
   double *d_binv_ = nullptr;
   int n_bot_ = 0, n_pins_ = 0;

@@ -257,9 +257,12 @@ __device__ __forceinline__ double fma_t(double a, double b, double c) { return _
 // smooth_cell with 32-bit shift indexing, FMA accumulation and a fast
 // division.  Same face coefficients and gathers, different rounding; every
 // V-cycle variant of the device solve uses it, so they agree bit for bit.
+// With FP64 factors (sa, ia of the block's list entry, see BlockList) the
+// diagonal is not summed and unew = rhs*sa + off*ia: no FP64 division.
 template <typename T, int ND, bool CG = false>
 __device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c, int b, uint16_t ft,
-                                                 const int ijk[3], T *__restrict__ phi, const T *__restrict__ rhs) {
+                                                 const int ijk[3], T *__restrict__ phi, const T *__restrict__ rhs,
+                                                 const double *sa = nullptr, const double *ia = nullptr) {
   const int nb = t.nb;
   const int ci = t.lnb >= 0 ? ijk[0] + ((ijk[1] + (ijk[2] << t.lnb)) << t.lnb) : encode(ijk, nb);
   const long cb = (long)b * t.ncell;
@@ -301,6 +304,10 @@ __device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c
         off += crse_fine_sum<T, ND, CG>(t, c, b, f, ijk, phi);
       }
     }
+  }
+  if (sizeof(T) == 8 && sa) {
+    phi[cb + ci] = fma_t(ld<CG>(&rhs[cb + ci]), (T)sa[ci], off * (T)ia[ci]);
+    return;
   }
   const T vfv = c.vf[cb + ci];
   T unew = 0;

@@ -93,7 +93,9 @@ __global__ void __launch_bounds__(kVT) k_vcycle_coop(Topo t, Coef<T> c, const VP
         const int p = (int)(it / nhalf);
         int ijk[3];
         color_cell<ND>((int)(it - (long)p * nhalf), t.nb, P.color, ijk);
-        smooth_cell_fast<T, ND, true>(t, c, P.blocks[p], P.ftypes[p], ijk, corr, resid);
+        smooth_cell_fast<T, ND, true>(t, c, P.blocks[p], P.ftypes[p], ijk, corr, resid,
+                                      P.sa ? P.sa + (long)p * ncell : nullptr,
+                                      P.ia ? P.ia + (long)p * ncell : nullptr);
       }
     } else if (P.op == kPhaseProlong) {
       const long total = (long)P.n * ncell;
@@ -143,6 +145,8 @@ void MacGpu::build_vcycle_program() {
     p.n = bl.n;
     p.blocks = bl.blocks;
     p.ftypes = bl.ftypes;
+    p.sa = bl.sa;
+    p.ia = bl.ia;
     v.push_back(p);
   };
   for (int l = L; l >= 2; l--) {
@@ -263,7 +267,9 @@ __global__ void __launch_bounds__(kCT, 1) k_vcycle_cluster(Topo t, Coef<T> c, co
         const int p = (int)(it / nhalf);
         int ijk[3];
         color_cell<ND>((int)(it - (long)p * nhalf), t.nb, P.color, ijk);
-        smooth_cell_fast<T, ND, true>(t, c, P.blocks[p], P.ftypes[p], ijk, corr, resid);
+        smooth_cell_fast<T, ND, true>(t, c, P.blocks[p], P.ftypes[p], ijk, corr, resid,
+                                      P.sa ? P.sa + (long)p * ncell : nullptr,
+                                      P.ia ? P.ia + (long)p * ncell : nullptr);
       }
     } else if (P.op == kPhaseProlong) {
       const long total = (long)P.n * ncell;
@@ -347,7 +353,7 @@ void MacGpu::vcycle_cluster(T *resid, T *corr, const Coef<T> &c, double *out) {
       continue;
     }
     const VPhase &P = h_phases_[i];
-    const BlockList bl{P.blocks, P.ftypes, P.n};
+    const BlockList bl{P.blocks, P.ftypes, P.n, P.sa, P.ia};
     switch (P.op) {
       case kPhaseRestrict: launch_restrict<T>(topo_, c, bl, resid, guard, stream_, pdl); break;
       case kPhaseBottom: bottom_launch<T>(resid, corr); break;

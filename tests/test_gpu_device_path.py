@@ -104,8 +104,9 @@ def test_programmatic_dependent_launch_is_transparent(name):
     assert np.array_equal(out[0][1], out[1][1])
 
 
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name", ["t2s", "t3s", "c1"])
-def test_smoother_variants_are_bit_identical(name):
+def test_smoother_variants_are_bit_identical(name, precision):
     """the autotuner's launch-bounds variants differ in register caps only:
     identical iterations and solutions, and the tuner reports its timings"""
     g, t, tb, S = setup_solver(name)
@@ -113,13 +114,13 @@ def test_smoother_variants_are_bit_identical(name):
     out = []
     for var in (-1, 0, 4, 5, 7):
         S.set_zero_sol()
-        S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=1, bottom=1,
+        S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=precision, bottom=1,
                      smooth_variant=var)
         info = S.cg_solve()
         assert info["status"] == 0, info
         out.append((info["iterations"], S.get_sol_compact()))
         if var == -1:
-            v, us = S.tuned_smoother(1)
+            v, us = S.tuned_smoother(precision)
             assert 0 <= v < 8 and all(u > 0 for u in us), (v, us)
     for k in range(1, len(out)):
         assert out[0][0] == out[k][0], k
