@@ -400,6 +400,26 @@ def kernel_only(S, prob, ext, torch, args):
                       "us_per_launch": a.elapsed_time(b) * 1e3 / args.steps}))
 
 
+# ncu summaries of the dominant sweep per (workload, V-cycle precision)
+PROFILES = {("config2", 0): "k_rbgs_config2.md", ("config3", 1): "k_rbgs_tile_config3.md"}
+
+
+def profiled_traffic(workload, precision):
+    """DRAM bytes per launch (read + write) from the committed ncu summary of
+    this workload's smoother sweep, or None"""
+    import re
+    name = PROFILES.get((workload, precision))
+    if not name:
+        return None, None
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None, None
+    m = re.search(r"dram__bytes_read\.sum \+ dram__bytes_write\.sum \| .*= ([0-9.]+) MB", open(path).read())
+    if not m:
+        return None, None
+    return float(m.group(1)) * 1e6, "profiles/" + name
+
+
 def roofline(S, prob, ext, torch, finest, precision):
     """dominant kernel: the red-black sweep (one colour) over the finest level
     of the finest tower, in the V-cycle's precision, with the variant the
@@ -431,12 +451,14 @@ def roofline(S, prob, ext, torch, finest, precision):
     us = a.elapsed_time(b) * 1e3 / reps
     achieved = bytes_per_launch / (us * 1e-6) / 1e9
     variant, _ = S.tuned_smoother(precision)
+    traffic, traffic_src = profiled_traffic(prob.name, precision)
     kind = "k_rbgs_tile (block staged in shared memory)" if variant >= 5 else "k_rbgs (one thread per cell)"
     l2 = bytes_per_launch < 100e6
     return {"kernel": "%s<%s,%dD>, autotuned variant %d, finest level, one colour"
                       % (kind, "float" if p == 4 else "double", prob.ndim, variant),
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "bytes_per_launch": bytes_per_launch, "us_per_launch": us,
+            "traffic": traffic, "traffic_source": traffic_src,
+            "bytes_per_launch": bytes_per_launch, "us_per_launch": us,
             "peak_source": src + " (burst copy)",
             "note": ("working set fits in L2 at this size: latency-bound; " if l2 else "") +
                     "DRAM traffic per launch from the ncu summaries"}
