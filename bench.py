@@ -76,6 +76,21 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(x, ws, device):
+    """the slowest rank's time: every replica's solve must be done"""
+    if ws <= 1:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(cells_per_rank, ws, ms_step):
+    """whole-job cells/s: ws replicas of the workload in the slowest rank's time"""
+    return ws * cells_per_rank / (ms_step / 1e3)
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -308,15 +323,12 @@ def main():
         torch.distributed.barrier()
     ms = [a.elapsed_time(b) for a, b in events]
     ms_step = statistics.mean(ms)
-    if ws > 1:
-        t = torch.tensor([ms_step], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(ms_step, ws, "cuda")
     bad = [i for i in infos if i["status"] != 0 or not (i["rnorm"] < TOL * i["rnorm0"])]
     if bad:
         raise SystemExit("timed solve did not converge: %s" % bad[0])
     iters = [i["iterations"] for i in infos]
-    value = ws * prob.leaf_cells / (ms_step / 1e3)
+    value = job_value(prob.leaf_cells, ws, ms_step)
     launches = int(round(statistics.mean(pro + it * per_it + epi for it in iters)))
 
     # ---- end to end through the C ABI with host TreeData buffers ----
