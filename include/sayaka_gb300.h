@@ -207,7 +207,25 @@ int32_t sayaka_mac_tower_size(sayaka_mac *h, int32_t L, int32_t sublevel);
 int sayaka_mac_flux(sayaka_mac *h, int32_t dir, const double *phi, int32_t phi_ncomp, int32_t phi_ngrow,
                     int32_t phi_comp, double *flux, int32_t flux_ncomp, int32_t flux_ngrow, int32_t flux_comp);
 
+/* ---- projection step around the solve ---- */
+/* The solve's right-hand side from a face velocity, on the device, then
+ * setRhs: rhs = sum_d (scale/dh_d) * (u_d(i+1) - u_d(i)) on every block,
+ * accumulated from d = 0 (calc_pres_rhs_block, src/Test7.h:587-609, with
+ * scale = -1/dt; calc_block_rhs_value, src/Test6.h:798-830, with scale = 1
+ * and, when wcomp >= 0, both face values weighted by component wcomp of the
+ * same buffer).  u[d] (d < ndim): face TreeData of direction d. */
+int sayaka_mac_set_rhs_div(sayaka_mac *h, const double *const *u, int32_t ncomp, int32_t ngrow, int32_t ucomp,
+                           int32_t wcomp, double scale);
+/* corr_vel (src/Test7.h:634-645): u_dir += dt * mg_flux_level(finest, dir,
+ * solution) on the finest tower's blocks (TreeData::AddEqual,
+ * src/SayakaTreeData.cpp:311-334); the solution never leaves the device.
+ * u: face TreeData of direction dir, updated in place. */
+int sayaka_mac_correct_vel(sayaka_mac *h, int32_t dir, double dt, double *u, int32_t ncomp, int32_t ngrow,
+                           int32_t comp);
+
 /* ---- parity hooks on compact all-block arrays (tests and tools) ---- */
+/* the solve's right-hand side (all blocks) */
+int sayaka_mac_get_rhs_compact(sayaka_mac *h, double *out);
 /* mg_apply_level(L) (src/SayakaMacOperator.cpp:84-137) */
 int sayaka_mac_apply_compact(sayaka_mac *h, int32_t L, const double *x, double *y);
 /* mg_residual_level(L) (src/SayakaMacUtil.cpp:9-49) */

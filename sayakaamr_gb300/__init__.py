@@ -96,6 +96,10 @@ SIGNATURES = {
     "sayaka_mac_apply_compact": (C.c_int, [_V, C.c_int32, _f64p, _f64p]),
     "sayaka_mac_residual_compact": (C.c_int, [_V, C.c_int32, _f64p, _f64p, _f64p]),
     "sayaka_mac_residual_norm_noalloc": (C.c_int, [_V, C.c_int32, _V, _V, _V, _V, _V]),
+    "sayaka_mac_set_rhs_div": (C.c_int, [_V, C.POINTER(_f64p), C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                         C.c_double]),
+    "sayaka_mac_correct_vel": (C.c_int, [_V, C.c_int32, C.c_double, _f64p, C.c_int32, C.c_int32, C.c_int32]),
+    "sayaka_mac_get_rhs_compact": (C.c_int, [_V, _f64p]),
     "sayaka_mac_smooth_compact": (C.c_int, [_V, C.c_int32, _f64p, _f64p, _f64p]),
     "sayaka_mac_restrict_compact": (C.c_int, [_V, _f64p, _f64p]),
     "sayaka_mac_prolong_compact": (C.c_int, [_V, _f64p, _f64p]),
@@ -375,6 +379,26 @@ class MacSolver:
         _check(self.lib.sayaka_mac_launch_counts(self.h, C.byref(a), C.byref(b), C.byref(c)), "launch_counts",
                self.h)
         return a.value, b.value, c.value
+
+    # --- projection step around the solve ---
+    def set_rhs_div(self, u, scale, ncomp=1, ngrow=0, ucomp=0, wcomp=-1):
+        """rhs = sum_d (scale/dh_d) (u_d(i+1) - u_d(i)) from face TreeData
+        buffers u[d] (optionally weighted by component wcomp)"""
+        keep = [np.ascontiguousarray(a, dtype=np.float64) for a in u]
+        arr = (_f64p * 3)(*[k.ctypes.data_as(_f64p) for k in keep] + [None] * (3 - len(keep)))
+        _check(self.lib.sayaka_mac_set_rhs_div(self.h, arr, ncomp, ngrow, ucomp, wcomp, float(scale)),
+               "set_rhs_div", self.h)
+
+    def correct_vel(self, d, dt, u, ncomp=1, ngrow=0, comp=0):
+        """u_d += dt * flux of the solution on the finest tower, in place"""
+        assert u.dtype == np.float64 and u.flags.c_contiguous
+        _check(self.lib.sayaka_mac_correct_vel(self.h, int(d), float(dt), u.ctypes.data_as(_f64p), ncomp, ngrow,
+                                               comp), "correct_vel", self.h)
+
+    def get_rhs_compact(self):
+        r = self._cells()
+        _check(self.lib.sayaka_mac_get_rhs_compact(self.h, r.ctypes.data_as(_f64p)), "get_rhs", self.h)
+        return r
 
     def tuned_smoother(self, precision):
         """(chosen variant, microseconds per variant) of the smoother autotuner"""

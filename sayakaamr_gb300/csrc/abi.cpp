@@ -591,6 +591,56 @@ int sayaka_mac_flux(sayaka_mac *h, int32_t dir, const double *phi, int32_t pn, i
   });
 }
 
+// ---- projection step around the solve ----
+int sayaka_mac_set_rhs_div(sayaka_mac *h, const double *const *u, int32_t ncomp, int32_t ngrow, int32_t ucomp,
+                           int32_t wcomp, double scale) {
+  return guarded(h, [&] {
+    MacGpu &g = *h->gpu;
+    if (!u) return (int)SAYAKA_BAD_INPUT;
+    const size_t nf = (size_t)g.num_blocks() * g.nfb();
+    std::vector<std::vector<double>> uc(g.ndim()), wc(g.ndim());
+    const double *up[3] = {}, *wp[3] = {};
+    for (int d = 0; d < g.ndim(); d++) {
+      if (!u[d]) return (int)SAYAKA_BAD_INPUT;
+      Layout Lu(g.ndim(), g.nb(), ncomp, ngrow, ucomp, d);
+      if (!Lu.ok()) return (int)SAYAKA_BAD_INPUT;
+      uc[d].resize(nf);
+      pack(Lu, g.num_blocks(), u[d], uc[d].data());
+      up[d] = uc[d].data();
+      if (wcomp >= 0) {
+        Layout Lw(g.ndim(), g.nb(), ncomp, ngrow, wcomp, d);
+        if (!Lw.ok()) return (int)SAYAKA_BAD_INPUT;
+        wc[d].resize(nf);
+        pack(Lw, g.num_blocks(), u[d], wc[d].data());
+        wp[d] = wc[d].data();
+      }
+    }
+    g.rhs_from_div(up, wcomp >= 0 ? wp : nullptr, scale);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_correct_vel(sayaka_mac *h, int32_t dir, double dt, double *u, int32_t ncomp, int32_t ngrow,
+                           int32_t comp) {
+  return guarded(h, [&] {
+    MacGpu &g = *h->gpu;
+    if (dir < 0 || dir >= g.ndim() || !u) return (int)SAYAKA_BAD_INPUT;
+    Layout L(g.ndim(), g.nb(), ncomp, ngrow, comp, dir);
+    if (!L.ok()) return (int)SAYAKA_BAD_INPUT;
+    std::vector<double> c((size_t)g.num_blocks() * g.nfb());
+    pack(L, g.num_blocks(), u, c.data());
+    g.correct_vel(dir, dt, c.data());
+    unpack(L, g.num_blocks(), c.data(), u);
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_get_rhs_compact(sayaka_mac *h, double *out) {
+  return guarded(h, [&] {
+    if (!out) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->get_rhs(out);
+    return (int)SAYAKA_OK;
+  });
+}
+
 // ---- parity hooks ----
 int sayaka_mac_apply_compact(sayaka_mac *h, int32_t L, const double *x, double *y) {
   return guarded(h, [&] {

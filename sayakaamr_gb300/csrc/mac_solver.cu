@@ -337,6 +337,7 @@ MacGpu::~MacGpu() {
   fr(d_part_);
   fr(d_opP_);
   for (auto &q : d_sfac_) fr(q);
+  for (auto &q : d_face_) fr(q);
   fr(d_opS_);
   fr(d_cnt_);
   fr(d_binv_);

@@ -100,6 +100,11 @@ class MacGpu {
   void flux(int dir, const double *phi_all, double *flux_all);
   void fix_bc(const double *phi_grown, int ngrow, double *rhs_all);
 
+  // projection step around the solve (compact all-block face arrays, host)
+  void rhs_from_div(const double *const *u_all, const double *const *w_all, double scale);
+  void correct_vel(int dir, double dt, double *u_all);
+  void get_rhs(double *all);
+
   // r = rhs - A x on tower L and out = {|r|_inf, r.r}; device pointers to
   // compact all-block arrays, enqueued on s, no device allocation (scratch in
   // a static device array).  0 ok, 1 bad input or size (why says which),
@@ -225,6 +230,8 @@ class MacGpu {
   double *d_part_ = nullptr;
   double *d_opP_ = nullptr, *d_opS_ = nullptr;  // factors of the device solve's operator
   std::vector<double *> d_sfac_;                // FP64 smoother factors per tower: sa then ia
+  std::vector<double *> d_face_;                // face fields of the projection step (u, w, flux)
+  double *face_scratch(int k);
   unsigned *d_cnt_ = nullptr;
   double *d_binv_ = nullptr;
   int n_bot_ = 0, n_pins_ = 0;
