@@ -117,6 +117,8 @@ typedef struct sayaka_params {
                              cells share one cluster launch; larger phases get their own launch (16384) */
   int32_t smooth_variant; /* device smoother launch bounds (register cap): -1 = autotuned at prepare by
                              timing every variant on the finest level (default), 0..7 = fixed */
+  int32_t learned;        /* device path with the FP32 V-cycle: 1 = add the trained learned block
+                             correction after every V-cycle (default 0); see sayaka_mac_learned_* */
 } sayaka_params;
 
 typedef struct sayaka_solve_info {
@@ -206,6 +208,33 @@ int32_t sayaka_mac_tower_size(sayaka_mac *h, int32_t L, int32_t sublevel);
  * direction dir on the leaf blocks; phi in TreeData layout (ngrow any) */
 int sayaka_mac_flux(sayaka_mac *h, int32_t dir, const double *phi, int32_t phi_ncomp, int32_t phi_ngrow,
                     int32_t phi_comp, double *flux, int32_t flux_ncomp, int32_t flux_ngrow, int32_t flux_comp);
+
+/* ---- learned block correction (no counterpart in the reference) ----
+ * A per-block convolutional network (3x3 convolutions 3 -> 32 -> 32 -> 1,
+ * ReLU; inputs: the block's residual after the V-cycle scaled by its max,
+ * log10 of the face-averaged B, the volume fraction) predicts the V-cycle's
+ * remaining error as a multiple of the Jacobi correction; the device solve
+ * with the FP32 V-cycle adds it after every V-cycle when params.learned = 1,
+ * and switches it off (status SAYAKA_STALL_FALLBACK on convergence) when the
+ * residual stops improving.  Training minimises the residual the correction
+ * leaves under the block's own operator.  2D trees with 8x8 or 16x16 blocks. */
+int32_t sayaka_mac_learned_nparam(void);
+/* training pairs from one plain device solve of the current right-hand side
+ * (zero initial guess, tolerance 1e-12, at most max_iter iterations): one
+ * pair per iterate and finest-tower block; the solution is reset to zero */
+int sayaka_mac_learned_collect(sayaka_mac *h, int32_t max_iter, int32_t *iterates);
+/* Adam on the collected pairs, FP32 forward/backward kernels on the GPU;
+ * loss = mean over blocks of the weighted squared error (last epoch) */
+int sayaka_mac_learned_train(sayaka_mac *h, int32_t epochs, float lr, int32_t batch, uint32_t seed, float *loss);
+int sayaka_mac_learned_get_weights(sayaka_mac *h, float *w, int32_t n);
+int sayaka_mac_learned_set_weights(sayaka_mac *h, const float *w, int32_t n);
+/* test hooks: loss and weight gradient of explicit blocks (feat [n][3][nb*nb];
+ * aux [n][2*nb*nb + 2*(nb+1)*nb] = Jacobi factor, dv*vf, x-face and y-face
+ * coefficients of the block-local operator), and the tensor-core (BF16)
+ * forward of explicit feature blocks (y [n][nb*nb]) */
+int sayaka_mac_learned_loss_grad(sayaka_mac *h, const float *feat, const float *aux, int32_t n, float *grad,
+                                 float *loss);
+int sayaka_mac_learned_forward(sayaka_mac *h, const float *feat, int32_t n, float *y);
 
 /* ---- projection step around the solve ---- */
 /* The solve's right-hand side from a face velocity, on the device, then

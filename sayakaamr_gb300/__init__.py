@@ -24,6 +24,7 @@ PHYS_BNDRY = -20
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
+_f32p = C.POINTER(C.c_float)
 
 
 class TreeTables(C.Structure):
@@ -38,7 +39,7 @@ class Params(C.Structure):
                 ("bot_tol_abs", C.c_double), ("bot_max_iter", C.c_int32), ("precision", C.c_int32),
                 ("bottom", C.c_int32), ("verbose", C.c_int32), ("graph", C.c_int32),
                 ("vcycle_kernel", C.c_int32), ("pdl", C.c_int32),
-                ("cluster_cells", C.c_int32), ("smooth_variant", C.c_int32)]
+                ("cluster_cells", C.c_int32), ("smooth_variant", C.c_int32), ("learned", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -100,6 +101,13 @@ SIGNATURES = {
                                          C.c_double]),
     "sayaka_mac_correct_vel": (C.c_int, [_V, C.c_int32, C.c_double, _f64p, C.c_int32, C.c_int32, C.c_int32]),
     "sayaka_mac_get_rhs_compact": (C.c_int, [_V, _f64p]),
+    "sayaka_mac_learned_nparam": (C.c_int32, []),
+    "sayaka_mac_learned_collect": (C.c_int, [_V, C.c_int32, _i32p]),
+    "sayaka_mac_learned_train": (C.c_int, [_V, C.c_int32, C.c_float, C.c_int32, C.c_uint32, _f32p]),
+    "sayaka_mac_learned_get_weights": (C.c_int, [_V, _f32p, C.c_int32]),
+    "sayaka_mac_learned_set_weights": (C.c_int, [_V, _f32p, C.c_int32]),
+    "sayaka_mac_learned_loss_grad": (C.c_int, [_V, _f32p, _f32p, C.c_int32, _f32p, _f32p]),
+    "sayaka_mac_learned_forward": (C.c_int, [_V, _f32p, C.c_int32, _f32p]),
     "sayaka_mac_smooth_compact": (C.c_int, [_V, C.c_int32, _f64p, _f64p, _f64p]),
     "sayaka_mac_restrict_compact": (C.c_int, [_V, _f64p, _f64p]),
     "sayaka_mac_prolong_compact": (C.c_int, [_V, _f64p, _f64p]),
@@ -379,6 +387,48 @@ class MacSolver:
         _check(self.lib.sayaka_mac_launch_counts(self.h, C.byref(a), C.byref(b), C.byref(c)), "launch_counts",
                self.h)
         return a.value, b.value, c.value
+
+    # --- learned block correction ---
+    def learned_collect(self, max_iter=200):
+        n = C.c_int32()
+        _check(self.lib.sayaka_mac_learned_collect(self.h, int(max_iter), C.byref(n)), "learned_collect", self.h)
+        return n.value
+
+    def learned_train(self, epochs=20, lr=1e-3, batch=256, seed=1):
+        loss = C.c_float()
+        _check(self.lib.sayaka_mac_learned_train(self.h, int(epochs), float(lr), int(batch), int(seed),
+                                                 C.byref(loss)), "learned_train", self.h)
+        return loss.value
+
+    def learned_weights(self):
+        n = self.lib.sayaka_mac_learned_nparam()
+        w = np.zeros(n, dtype=np.float32)
+        _check(self.lib.sayaka_mac_learned_get_weights(self.h, w.ctypes.data_as(_f32p), n), "learned_weights",
+               self.h)
+        return w
+
+    def set_learned_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        _check(self.lib.sayaka_mac_learned_set_weights(self.h, w.ctypes.data_as(_f32p), w.size),
+               "set_learned_weights", self.h)
+
+    def learned_loss_grad(self, feat, aux):
+        feat, aux = (np.ascontiguousarray(a, dtype=np.float32) for a in (feat, aux))
+        n = feat.shape[0]
+        g = np.zeros(self.lib.sayaka_mac_learned_nparam(), dtype=np.float32)
+        loss = C.c_float()
+        _check(self.lib.sayaka_mac_learned_loss_grad(self.h, feat.ctypes.data_as(_f32p), aux.ctypes.data_as(_f32p),
+                                                     n, g.ctypes.data_as(_f32p), C.byref(loss)),
+               "learned_loss_grad", self.h)
+        return loss.value, g
+
+    def learned_forward(self, feat):
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        n = feat.shape[0]
+        y = np.zeros((n, feat.shape[-1]), dtype=np.float32)
+        _check(self.lib.sayaka_mac_learned_forward(self.h, feat.ctypes.data_as(_f32p), n, y.ctypes.data_as(_f32p)),
+               "learned_forward", self.h)
+        return y
 
     # --- projection step around the solve ---
     def set_rhs_div(self, u, scale, ncomp=1, ngrow=0, ucomp=0, wcomp=-1):

@@ -294,6 +294,7 @@ void sayaka_params_default(sayaka_params *p) {
   p->pdl = d.pdl;
   p->cluster_cells = d.cluster_cells;
   p->smooth_variant = d.smooth_variant;
+  p->learned = d.learned;
 }
 
 int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
@@ -508,6 +509,7 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.pdl = p->pdl;
     s.cluster_cells = p->cluster_cells;
     s.smooth_variant = p->smooth_variant;
+    s.learned = p->learned;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
   });
@@ -588,6 +590,56 @@ int sayaka_mac_flux(sayaka_mac *h, int32_t dir, const double *phi, int32_t pn, i
       std::memcpy(&full[(size_t)b * g.nfb()], &f[(size_t)b * g.nfb()], g.nfb() * sizeof(double));
     unpack(F, g.num_blocks(), full.data(), flux);
     return (int)SAYAKA_OK;
+  });
+}
+
+// ---- learned block correction ----
+int32_t sayaka_mac_learned_nparam(void) { return learned::kNParam; }
+int sayaka_mac_learned_collect(sayaka_mac *h, int32_t max_iter, int32_t *iterates) {
+  return guarded(h, [&] {
+    if (!h->gpu->learned_supported()) {
+      h->err = "learned correction: 2D trees with 8x8 or 16x16 blocks only";
+      return (int)SAYAKA_BAD_INPUT;
+    }
+    const int n = h->gpu->learned_collect(max_iter > 0 ? max_iter : 200);
+    if (iterates) *iterates = n < 0 ? 0 : n;
+    return n < 0 ? (int)SAYAKA_CUDA_ERROR : (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_learned_train(sayaka_mac *h, int32_t epochs, float lr, int32_t batch, uint32_t seed, float *loss) {
+  return guarded(h, [&] {
+    if (epochs < 0 || batch < 1 || !(lr > 0)) return (int)SAYAKA_BAD_INPUT;
+    if (h->gpu->learned_samples() == 0) {
+      h->err = "learned correction: no training pairs (call sayaka_mac_learned_collect first)";
+      return (int)SAYAKA_BAD_INPUT;
+    }
+    const float l = h->gpu->learned_train(epochs, lr, batch, seed);
+    if (loss) *loss = l;
+    return l < 0 ? (int)SAYAKA_CUDA_ERROR : (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_learned_get_weights(sayaka_mac *h, float *w, int32_t n) {
+  return guarded(h, [&] { return h->gpu->learned_get_weights(w, n) == 0 ? (int)SAYAKA_OK : (int)SAYAKA_BAD_INPUT; });
+}
+int sayaka_mac_learned_set_weights(sayaka_mac *h, const float *w, int32_t n) {
+  return guarded(h, [&] {
+    if (!w || n != learned::kNParam || !h->gpu->learned_supported()) return (int)SAYAKA_BAD_INPUT;
+    return h->gpu->learned_set_weights(w, n) == 0 ? (int)SAYAKA_OK : (int)SAYAKA_CUDA_ERROR;
+  });
+}
+int sayaka_mac_learned_loss_grad(sayaka_mac *h, const float *feat, const float *aux, int32_t n, float *grad,
+                                 float *loss) {
+  return guarded(h, [&] {
+    if (!feat || !aux || !grad || n < 1 || !h->gpu->learned_supported()) return (int)SAYAKA_BAD_INPUT;
+    const float l = h->gpu->learned_loss_grad(feat, aux, n, grad);
+    if (loss) *loss = l;
+    return (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_learned_forward(sayaka_mac *h, const float *feat, int32_t n, float *y) {
+  return guarded(h, [&] {
+    if (!feat || !y || n < 1 || !h->gpu->learned_supported()) return (int)SAYAKA_BAD_INPUT;
+    return h->gpu->learned_forward(feat, n, y) == 0 ? (int)SAYAKA_OK : (int)SAYAKA_CUDA_ERROR;
   });
 }
 

@@ -61,6 +61,10 @@ struct FState {
   int stat;     // 1 = breakdown
   int conv;     // converged
   int trivial;  // zero initial residual
+  // learned correction: on, switched off after a stall, iterations since the
+  // best residual, best residual
+  int nn_on, nn_off, nn_since, pad_;
+  double nn_best;
 };
 
 // one phase of the cooperative V-cycle program (mac_vcycle.cu)

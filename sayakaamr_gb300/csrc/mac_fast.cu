@@ -172,6 +172,16 @@ struct EpiEnd {  // |r|, rhat.r of the next iteration
       st->done = 1;
       return;
     }
+    // learned correction: without a 10% gain on the best residual within 4
+    // iterations it is switched off and the solve goes on with the plain MG
+    if (st->nn_on && !st->nn_off) {
+      if (v[0] < 0.9 * st->nn_best) {
+        st->nn_best = v[0];
+        st->nn_since = 0;
+      } else if (++st->nn_since >= 4) {
+        st->nn_off = 1;
+      }
+    }
     if (st->omega == 0) {
       st->stat = 1;
       st->done = 1;
@@ -844,6 +854,24 @@ void MacGpu::bottom_launch(T *resid, T *corr) {
 template void MacGpu::bottom_launch<float>(float *, float *);
 template void MacGpu::bottom_launch<double>(double *, double *);
 
+// one preconditioner application: the V-cycle, then (FP32, when enabled and
+// trained) the learned block correction, then the widening into out
+template <typename T>
+void MacGpu::precondition(int L, T *resid, T *corr, const Coef<T> &c, double *out) {
+  const bool nn = sizeof(T) == 4 && learned_active();
+  double *o = nn ? nullptr : out;
+  if (prm_.vcycle_kernel == 2)
+    vcycle_cluster<T>(resid, corr, c, o);
+  else if (prm_.vcycle_kernel == 1)
+    vcycle_coop<T>(resid, corr, c, o);
+  else
+    vcycle_device<T>(L, resid, corr, c, o);
+  if (nn) {
+    learned_apply(reinterpret_cast<float *>(resid), reinterpret_cast<float *>(corr));
+    if (out) vc_out_launch<T>(tower_list(L), corr, out);
+  }
+}
+
 template <typename T>
 void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
   const int L = finest_;
@@ -863,12 +891,7 @@ void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
   const bool pdl = prm_.pdl != 0;
   launch_k(pdl, k_pupdate<T>, ew_grid(w), kTPB, 0, stream_, TL, ncell_, (const FState *)d_st_, (const double *)R, P,
            (const double *)V, (const double *)d_vf_, resid);
-  if (prm_.vcycle_kernel == 2)
-    vcycle_cluster<T>(resid, corr, c, out_p);
-  else if (prm_.vcycle_kernel == 1)
-    vcycle_coop<T>(resid, corr, c, out_p);
-  else
-    vcycle_device<T>(L, resid, corr, c, out_p);
+  precondition<T>(L, resid, corr, c, out_p);
   if (tt_.ndim == 2)
     launch_k(pdl, k_op_red<2, 0, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, PH, V,
              (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
@@ -877,12 +900,7 @@ void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
              (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
   launch_k(pdl, k_supdate<T, TO>, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, (const double *)R, (const double *)V,
            S, X, PH, (const double *)d_vf_, resid, d_part_, d_cnt_);
-  if (prm_.vcycle_kernel == 2)
-    vcycle_cluster<T>(resid, corr, c, out_s);
-  else if (prm_.vcycle_kernel == 1)
-    vcycle_coop<T>(resid, corr, c, out_s);
-  else
-    vcycle_device<T>(L, resid, corr, c, out_s);
+  precondition<T>(L, resid, corr, c, out_s);
   if (tt_.ndim == 2)
     launch_k(pdl, k_op_red<2, 1, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, SH, Tt,
              (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
@@ -938,6 +956,7 @@ void MacGpu::capture_loop(int precision) {
   graph_pdl_ = prm_.pdl;
   graph_cc_ = prm_.cluster_cells;
   graph_var_ = rbgs_variant_[precision == 1];
+  graph_nn_ = (int)learned_active();
 }
 
 int MacGpu::cg_solve_device(SolveInfo *info) {
@@ -957,7 +976,8 @@ int MacGpu::cg_solve_enqueue() {
   if (prm_.graph && (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
                      graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl ||
                      graph_cc_ != prm_.cluster_cells ||
-                     graph_var_ != rbgs_variant_[prm_.precision == 1]))
+                     graph_var_ != rbgs_variant_[prm_.precision == 1] ||
+                     graph_nn_ != (int)learned_active()))
     return -1;
   if (prm_.vcycle_kernel && program_npost_ != prm_.n_post) return -1;
   return enqueue_solve();
@@ -971,6 +991,8 @@ int MacGpu::enqueue_solve() {
   init.tol_rel = prm_.tol_rel;
   init.tol_abs = prm_.tol_abs;
   init.max_iter = prm_.max_iter;
+  init.nn_on = learned_active() ? 1 : 0;
+  init.nn_best = 1e300;
   *h_st_ = init;
   CKR_(cudaMemcpyAsync(d_st_, h_st_, sizeof(FState), cudaMemcpyHostToDevice, stream_), -1);
   // prologue: x0 = sol, x = 0, r = rhs - A x0, rhat = r, |r0|, rho
@@ -993,6 +1015,16 @@ int MacGpu::enqueue_solve() {
           iteration_device<float>(d_resid32_, d_corr32_, c32_);
         else
           iteration_device<double>(vec_[kRESID], vec_[kCORR], c64_);
+        if (record_) {  // a collection solve keeps every iterate
+          double *cp = nullptr;
+          const size_t n = (size_t)tt_.num_blocks * ncell_;
+          if (cudaMalloc(&cp, n * sizeof(double)) != cudaSuccess) {
+            fail("out of device memory (recorded iterates)");
+            return -1;
+          }
+          CKR_(cudaMemcpyAsync(cp, vec_[kX], n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), -1);
+          record_->push_back(cp);
+        }
         CKR_(cudaMemcpyAsync(h_st_, d_st_, sizeof(FState), cudaMemcpyDeviceToHost, stream_), -1);
         CKR_(cudaStreamSynchronize(stream_), -1);
         if (h_st_->done) break;
@@ -1020,12 +1052,14 @@ int MacGpu::prepare_device() {
     if (!err_.empty()) return -1;
   }
   tune_smoother(prm_.precision);
+  if (learned_active()) learned_prepare();
   if (!err_.empty()) return -1;
   if (prm_.vcycle_kernel && program_npost_ != prm_.n_post) build_vcycle_program();
   if (prm_.graph && (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
                      graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl ||
                      graph_cc_ != prm_.cluster_cells ||
-                     graph_var_ != rbgs_variant_[prm_.precision == 1]))
+                     graph_var_ != rbgs_variant_[prm_.precision == 1] ||
+                     graph_nn_ != (int)learned_active()))
     capture_loop(prm_.precision);
   return err_.empty() ? 0 : -1;
 }
@@ -1050,7 +1084,7 @@ int MacGpu::solve_state(SolveInfo *info) {
   info->iterations = st.trivial ? 0 : st.iter;
   info->rnorm0 = st.rnorm0;
   info->rnorm = st.rnorm;
-  info->status = st.stat ? 1 : ((st.conv || st.trivial) ? 0 : 2);
+  info->status = st.stat ? 1 : ((st.conv || st.trivial) ? (st.nn_off ? 3 : 0) : 2);
   info->seconds = 0;
   return 0;
 }

@@ -1,0 +1,845 @@
+// Learned block correction of the device solve's FP32 V-cycle (2D blocks of
+// 8x8 or 16x16 cells): feature assembly, FP32 training forward/backward,
+// Adam, BF16 tensor-core inference, and the collection of training pairs from
+// the plain solver's own iterates.  The network and its inputs are described
+// in mac_learned.h.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <random>
+#include <vector>
+
+#include "cuda_check.h"
+#include "mac_learned.h"
+#include "mac_solver.h"
+#include "mac_stencil.cuh"
+#include "launch.cuh"
+
+namespace sayaka_gb300 {
+
+using namespace learned;
+
+namespace {
+
+__device__ __forceinline__ float wmaxf(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float wsumf(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block-wide max over NC threads (NC a multiple of 32)
+template <int NC>
+__device__ __forceinline__ float block_max(float v, float *red) {
+  v = wmaxf(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float m = 0.f;
+  for (int i = 0; i < NC / 32; i++) m = fmaxf(m, red[i]);
+  __syncthreads();
+  return m;
+}
+
+// block-wide sum (fixed order over warps)
+template <int NC>
+__device__ __forceinline__ float block_sum(float v, float *red) {
+  v = wsumf(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float m = 0.f;
+  for (int i = 0; i < NC / 32; i++) m += red[i];
+  __syncthreads();
+  return m;
+}
+
+// v minus its least-squares fit by {1, x, y} over the block (the basis is
+// orthogonal on the full nb x nb grid): the block-local part of a field,
+// with the block's constant and linear trend left to the V-cycle
+template <int NB>
+__device__ __forceinline__ float local_part(float v, float *red) {
+  constexpr int NC = NB * NB;
+  const float xi = (float)(threadIdx.x % NB) - 0.5f * (NB - 1), yj = (float)(threadIdx.x / NB) - 0.5f * (NB - 1);
+  const float sxx = (float)NB * (float)(NB * (NB * NB - 1)) / 12.f;  // sum of xi^2 over the block
+  const float a0 = block_sum<NC>(v, red) / (float)NC;
+  const float a1 = block_sum<NC>(v * xi, red) / sxx;
+  const float a2 = block_sum<NC>(v * yj, red) / sxx;
+  return v - a0 - a1 * xi - a2 * yj;
+}
+
+// input features of one cell: r1/s, log10(B averaged over the cell's faces)/3, vf
+template <int NB>
+__device__ __forceinline__ void cell_features(const Topo &t, const Coef<float> &c, int b, int ci, float r1, float s,
+                                              float *f) {
+  const int i = ci % NB, j = ci / NB;
+  const long fb = (long)b * t.nfb;
+  const float bx = c.bcoef[0][fb + i + (NB + 1) * j] + c.bcoef[0][fb + i + 1 + (NB + 1) * j];
+  const float by = c.bcoef[1][fb + i + NB * j] + c.bcoef[1][fb + i + NB * (j + 1)];
+  const float bavg = 0.25f * (bx + by);
+  f[0] = r1 / s;
+  f[1] = log10f(fmaxf(bavg, 1e-12f)) * (1.0f / 3.0f);
+  f[2] = c.vf[(long)b * NB * NB + ci];
+}
+
+// ---- training pairs: the features of r1 and, per block, the data of the
+// block-local operator the loss uses: aux = [sa][dv*vf][x-face T][y-face T]
+template <int NB>
+__global__ void k_nn_pairs(Topo t, Coef<float> c, BlockList L, const float *__restrict__ r1,
+                           const double *__restrict__ sa, float *feat, float *aux) {
+  constexpr int NC = NB * NB, NF = (NB + 1) * NB, AUXN = 2 * NC + 2 * NF;
+  __shared__ float red[NC / 32];
+  const int p = blockIdx.x, ci = threadIdx.x;
+  const int b = L.blocks[p];
+  const long q = (long)b * NC + ci;
+  const float rv = r1[q];
+  const float m = block_max<NC>(fabsf(rv), red);
+  const float s = m > 0.f ? m : 1.f;
+  float f[3];
+  cell_features<NB>(t, c, b, ci, rv, s, f);
+  for (int k = 0; k < 3; k++) feat[((long)p * 3 + k) * NC + ci] = f[k];
+  float *ax = aux + (long)p * AUXN;
+  ax[ci] = (float)sa[(long)p * NC + ci];
+  ax[NC + ci] = c.geom[b * 8 + 6] * c.vf[q];
+  for (int k = threadIdx.x; k < NF; k += blockDim.x) {
+    ax[2 * NC + k] = c.tff[0][(long)b * t.nfb + k];
+    ax[2 * NC + NF + k] = c.tff[1][(long)b * t.nfb + k];
+  }
+}
+
+// (K u)_c = sum over the cell's faces of T_f (u_c - u_nb), u = 0 outside the
+// block (u in a padded tile with a zero halo); tx [j][i+s], ty [j+s][i]
+template <int NB>
+__device__ __forceinline__ float local_K(const float *u, const float *tx, const float *ty, int i, int j) {
+  constexpr int P = NB + 2;
+  const int pc = (j + 1) * P + (i + 1);
+  const float uc = u[pc];
+  return tx[i + (NB + 1) * j] * (uc - u[pc - 1]) + tx[i + 1 + (NB + 1) * j] * (uc - u[pc + 1]) +
+         ty[i + NB * j] * (uc - u[pc - P]) + ty[i + NB * (j + 1)] * (uc - u[pc + P]);
+}
+
+// ---- FP32 forward for training: activations and the loss gradient
+// The loss of one block is the residual the correction leaves behind under
+// the block-local operator A = D^-1 K (K symmetric: face coefficients T,
+// zero outside the block; D = dv*vf):
+//   L = inv_norm * sum (r1/s - A u)^2,  u = sa * P(y)
+// dL/du = K (D^-1 g) with g = -2 inv_norm (r1/s - A u), dL/dy = P(sa dL/du).
+template <int NB>
+__global__ void __launch_bounds__(NB *NB) k_nn_fwd(const float *__restrict__ W, const float *__restrict__ feat,
+                                                   const float *__restrict__ aux, const int *__restrict__ idx,
+                                                   float *h1g, float *h2g, float *dyg, float *loss, float inv_norm) {
+  constexpr int NC = NB * NB, P = NB + 2, PP = P * P, NF = (NB + 1) * NB, AUXN = 2 * NC + 2 * NF;
+  extern __shared__ float sm[];
+  float *x0 = sm;             // [3][P][P]
+  float *h1 = x0 + 3 * PP;    // [32][P][P]
+  float *h2 = h1 + kC * PP;   // [32][P][P]
+  float *w = h2 + kC * PP;    // [kNParam]
+  float *ax = w + kNParam;    // [AUXN]
+  float *ut = ax + AUXN;      // [P][P] u, then D^-1 g
+  __shared__ float red[NC / 32];
+  const int s = idx[blockIdx.x];
+  const int ci = threadIdx.x, i = ci % NB, j = ci / NB, pc = (j + 1) * P + (i + 1);
+  for (int k = threadIdx.x; k < kNParam; k += blockDim.x) w[k] = W[k];
+  for (int k = threadIdx.x; k < AUXN; k += blockDim.x) ax[k] = aux[(long)s * AUXN + k];
+  for (int k = threadIdx.x; k < (3 + 2 * kC) * PP; k += blockDim.x) sm[k] = 0.f;
+  for (int k = threadIdx.x; k < PP; k += blockDim.x) ut[k] = 0.f;
+  __syncthreads();
+  for (int c = 0; c < 3; c++) x0[c * PP + pc] = feat[((long)s * 3 + c) * NC + ci];
+  __syncthreads();
+  for (int co = 0; co < kC; co++) {
+    float a = w[kOB1 + co];
+    for (int cin = 0; cin < kCin; cin++)
+      for (int tp = 0; tp < 9; tp++) a += w[kOW1 + (co * kCin + cin) * 9 + tp] * x0[cin * PP + pc + (tp / 3 - 1) * P + (tp % 3 - 1)];
+    h1[co * PP + pc] = fmaxf(a, 0.f);
+  }
+  __syncthreads();
+  for (int co = 0; co < kC; co++) {
+    float a = w[kOB2 + co];
+    for (int cin = 0; cin < kC; cin++)
+      for (int tp = 0; tp < 9; tp++) a += w[kOW2 + (co * kC + cin) * 9 + tp] * h1[cin * PP + pc + (tp / 3 - 1) * P + (tp % 3 - 1)];
+    h2[co * PP + pc] = fmaxf(a, 0.f);
+  }
+  __syncthreads();
+  float y = w[kOB3];
+  for (int cin = 0; cin < kC; cin++)
+    for (int tp = 0; tp < 9; tp++) y += w[kOW3 + cin * 9 + tp] * h2[cin * PP + pc + (tp / 3 - 1) * P + (tp % 3 - 1)];
+  for (int co = 0; co < kC; co++) {
+    h1g[((long)blockIdx.x * kC + co) * NC + ci] = h1[co * PP + pc];
+    h2g[((long)blockIdx.x * kC + co) * NC + ci] = h2[co * PP + pc];
+  }
+  const float *sav = ax, *dvvf = ax + NC, *tx = ax + 2 * NC, *ty = ax + 2 * NC + NF;
+  y = local_part<NB>(y, red);
+  ut[pc] = sav[ci] * y;
+  __syncthreads();
+  const float au = dvvf[ci] > 0.f ? local_K<NB>(ut, tx, ty, i, j) / dvvf[ci] : 0.f;
+  const float res = x0[pc] - au;
+  const float gv = -2.f * inv_norm * res;
+  __syncthreads();
+  ut[pc] = dvvf[ci] > 0.f ? gv / dvvf[ci] : 0.f;
+  __syncthreads();
+  const float dldu = local_K<NB>(ut, tx, ty, i, j);
+  // the projection is symmetric: the gradient goes back through it unchanged
+  dyg[(long)blockIdx.x * NC + ci] = local_part<NB>(sav[ci] * dldu, red);
+  float l = wsumf(res * res * inv_norm);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float tot = 0.f;
+    for (int k = 0; k < NC / 32; k++) tot += red[k];
+    atomicAdd(loss, tot);
+  }
+}
+
+// ---- FP32 backward: weight gradients accumulated into G
+template <int NB>
+__global__ void __launch_bounds__(NB *NB) k_nn_bwd(const float *__restrict__ W, const float *__restrict__ feat,
+                                                   const int *__restrict__ idx, const float *__restrict__ h1g,
+                                                   const float *__restrict__ h2g, const float *__restrict__ dyg,
+                                                   float *G) {
+  constexpr int NC = NB * NB, P = NB + 2, PP = P * P;
+  extern __shared__ float sm[];
+  float *x0 = sm;             // [3][P][P]
+  float *h1 = x0 + 3 * PP;    // [32][P][P]
+  float *h2 = h1 + kC * PP;   // [32][P][P], later dh1
+  float *dh2 = h2 + kC * PP;  // [32][P][P]
+  float *dy = dh2 + kC * PP;  // [P][P]
+  float *w = dy + PP;         // [kNParam]
+  const int s = idx[blockIdx.x];
+  const int ci = threadIdx.x, i = ci % NB, j = ci / NB, pc = (j + 1) * P + (i + 1);
+  for (int k = threadIdx.x; k < kNParam; k += blockDim.x) w[k] = W[k];
+  for (int k = threadIdx.x; k < (3 + 3 * kC + 1) * PP; k += blockDim.x) sm[k] = 0.f;
+  __syncthreads();
+  for (int c = 0; c < 3; c++) x0[c * PP + pc] = feat[((long)s * 3 + c) * NC + ci];
+  for (int c = 0; c < kC; c++) {
+    h1[c * PP + pc] = h1g[((long)blockIdx.x * kC + c) * NC + ci];
+    h2[c * PP + pc] = h2g[((long)blockIdx.x * kC + c) * NC + ci];
+  }
+  dy[pc] = dyg[(long)blockIdx.x * NC + ci];
+  __syncthreads();
+  // output layer: dW3, db3
+  for (int e = threadIdx.x; e < kC * 9; e += blockDim.x) {
+    const int cin = e / 9, tp = e % 9, off = (tp / 3 - 1) * P + (tp % 3 - 1);
+    float a = 0.f;
+    for (int q = 0; q < NC; q++) {
+      const int pq = (q / NB + 1) * P + (q % NB + 1);
+      a += dy[pq] * h2[cin * PP + pq + off];
+    }
+    atomicAdd(&G[kOW3 + e], a);
+  }
+  if (threadIdx.x == 0) {
+    float a = 0.f;
+    for (int q = 0; q < NC; q++) a += dy[(q / NB + 1) * P + (q % NB + 1)];
+    atomicAdd(&G[kOB3], a);
+  }
+  // dh2 = (W3^T * dy) masked by ReLU
+  for (int c = 0; c < kC; c++) {
+    float a = 0.f;
+    for (int tp = 0; tp < 9; tp++) a += w[kOW3 + c * 9 + tp] * dy[pc - (tp / 3 - 1) * P - (tp % 3 - 1)];
+    dh2[c * PP + pc] = h2[c * PP + pc] > 0.f ? a : 0.f;
+  }
+  __syncthreads();
+  // hidden layer: dW2, db2
+  for (int e = threadIdx.x; e < kC * kC * 9; e += blockDim.x) {
+    const int co = e / (kC * 9), cin = (e / 9) % kC, tp = e % 9, off = (tp / 3 - 1) * P + (tp % 3 - 1);
+    float a = 0.f;
+    for (int q = 0; q < NC; q++) {
+      const int pq = (q / NB + 1) * P + (q % NB + 1);
+      a += dh2[co * PP + pq] * h1[cin * PP + pq + off];
+    }
+    atomicAdd(&G[kOW2 + e], a);
+  }
+  for (int co = threadIdx.x; co < kC; co += blockDim.x) {
+    float a = 0.f;
+    for (int q = 0; q < NC; q++) a += dh2[co * PP + (q / NB + 1) * P + (q % NB + 1)];
+    atomicAdd(&G[kOB2 + co], a);
+  }
+  // dh1 = (W2^T * dh2) masked by ReLU, into h2's space
+  float *dh1 = h2;
+  __syncthreads();
+  for (int cin = 0; cin < kC; cin++) {
+    float a = 0.f;
+    for (int co = 0; co < kC; co++)
+      for (int tp = 0; tp < 9; tp++)
+        a += w[kOW2 + (co * kC + cin) * 9 + tp] * dh2[co * PP + pc - (tp / 3 - 1) * P - (tp % 3 - 1)];
+    dh1[cin * PP + pc] = h1[cin * PP + pc] > 0.f ? a : 0.f;
+  }
+  __syncthreads();
+  // input layer: dW1, db1
+  for (int e = threadIdx.x; e < kC * kCin * 9; e += blockDim.x) {
+    const int co = e / (kCin * 9), cin = (e / 9) % kCin, tp = e % 9, off = (tp / 3 - 1) * P + (tp % 3 - 1);
+    float a = 0.f;
+    for (int q = 0; q < NC; q++) {
+      const int pq = (q / NB + 1) * P + (q % NB + 1);
+      a += dh1[co * PP + pq] * x0[cin * PP + pq + off];
+    }
+    atomicAdd(&G[kOW1 + e], a);
+  }
+  for (int co = threadIdx.x; co < kC; co += blockDim.x) {
+    float a = 0.f;
+    for (int q = 0; q < NC; q++) a += dh1[co * PP + (q / NB + 1) * P + (q % NB + 1)];
+    atomicAdd(&G[kOB1 + co], a);
+  }
+}
+
+__global__ void k_adam(float *w, float *g, float *m, float *v, int n, float lr, float b1, float b2, float c1,
+                       float c2) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const float gk = g[k];
+    const float mk = b1 * m[k] + (1.f - b1) * gk;
+    const float vk = b2 * v[k] + (1.f - b2) * gk * gk;
+    m[k] = mk;
+    v[k] = vk;
+    w[k] -= lr * (mk / c1) / (sqrtf(vk / c2) + 1e-8f);
+    g[k] = 0.f;
+  }
+}
+
+// w2 FP32 [out][in][tap] -> BF16 [tap][out][in] (the B operand layout)
+__global__ void k_w2_bf16(const float *W, __nv_bfloat16 *o) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < kC * kC * 9; k += gridDim.x * blockDim.x) {
+    const int tp = k / (kC * kC), co = (k / kC) % kC, cin = k % kC;
+    o[k] = __float2bfloat16_rn(W[kOW2 + (co * kC + cin) * 9 + tp]);
+  }
+}
+
+// ---- inference: r1 = resid - A corr on the tower (skipped once stalled)
+template <int ND>
+__global__ void __launch_bounds__(256) k_nn_resid(Topo t, Coef<float> c, BlockList L, const float *__restrict__ corr,
+                                                  const float *__restrict__ resid, float *__restrict__ r1,
+                                                  const FState *st) {
+  if (st->done || st->nn_off) return;
+  const int total = L.n * t.ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+    const int p = it / t.ncell, ci = it - p * t.ncell;
+    const int b = L.blocks[p];
+    const long q = (long)b * t.ncell + ci;
+    const float a = stencil::apply_cell<float, ND>(t, c, b, L.ftypes[p], ci, corr);
+    r1[q] = c.vf[q] > 0 ? resid[q] - a : 0.f;
+  }
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// The network on one block staged in shared memory (x0 [3][P][P] holds the
+// features with a zero halo); returns y of the calling thread's cell.  The
+// 32 -> 32 layer runs as an implicit GEMM on tensor cores (M = cells, N = 32,
+// K = 9 taps x 32 channels, BF16 operands, FP32 accumulation), the small
+// layers on the FP32 pipes.
+template <int NB>
+__device__ __forceinline__ float nn_tail_bf16(const float *__restrict__ W, const __nv_bfloat16 *__restrict__ w2bf,
+                                              float *x0, unsigned char *rest) {
+  constexpr int P = NB + 2, PP = P * P, CS = 40;  // channel stride of the BF16 tile (padded)
+  float *h2 = reinterpret_cast<float *>(rest);   // [32][P][P] FP32
+  float *ws = h2 + kC * PP;                        // w1, b1 | b2 | w3, b3
+  float *w1 = ws, *b1 = ws + kC * kCin * 9, *b2 = b1 + kC, *w3 = b2 + kC, *b3 = w3 + kC * 9;
+  __nv_bfloat16 *h1 = reinterpret_cast<__nv_bfloat16 *>(b3 + 1);  // [P*P][CS]
+  __nv_bfloat16 *wb = h1 + PP * CS;                                // [9][32][32]
+  const int ci = threadIdx.x, pc = (ci / NB + 1) * P + (ci % NB + 1);
+  for (int k = threadIdx.x; k < kC * kCin * 9 + kC; k += blockDim.x) ws[k] = W[kOW1 + k];
+  for (int k = threadIdx.x; k < kC; k += blockDim.x) b2[k] = W[kOB2 + k];
+  for (int k = threadIdx.x; k < kC * 9 + 1; k += blockDim.x) w3[k] = W[kOW3 + k];
+  for (int k = threadIdx.x; k < 9 * kC * kC / 2; k += blockDim.x)
+    reinterpret_cast<uint32_t *>(wb)[k] = reinterpret_cast<const uint32_t *>(w2bf)[k];
+  for (int k = threadIdx.x; k < PP * CS / 2; k += blockDim.x) reinterpret_cast<uint32_t *>(h1)[k] = 0u;
+  for (int k = threadIdx.x; k < kC * PP; k += blockDim.x) h2[k] = 0.f;
+  __syncthreads();
+  // input layer (FP32) -> BF16 tile [pixel][channel]
+  for (int co = 0; co < kC; co++) {
+    float a = b1[co];
+    for (int cin = 0; cin < kCin; cin++)
+      for (int tp = 0; tp < 9; tp++) a += w1[(co * kCin + cin) * 9 + tp] * x0[cin * PP + pc + (tp / 3 - 1) * P + (tp % 3 - 1)];
+    h1[pc * CS + co] = __float2bfloat16_rn(fmaxf(a, 0.f));
+  }
+  __syncthreads();
+  // hidden layer: warp w owns cells [32w, 32w+32) = two m16 tiles, all four
+  // n8 tiles of the 32 output channels
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+  float acc[2][4][4];
+  for (int mt = 0; mt < 2; mt++)
+    for (int nt = 0; nt < 4; nt++)
+      for (int r = 0; r < 4; r++) acc[mt][nt][r] = 0.f;
+  int prow[2][2];  // padded pixel of fragment rows g and g+8 of each m tile
+  for (int mt = 0; mt < 2; mt++)
+    for (int hh = 0; hh < 2; hh++) {
+      const int cell = warp * 32 + mt * 16 + g + 8 * hh;
+      prow[mt][hh] = (cell / NB + 1) * P + (cell % NB + 1);
+    }
+  const uint32_t *h1w = reinterpret_cast<const uint32_t *>(h1);
+  const uint32_t *wbw = reinterpret_cast<const uint32_t *>(wb);
+  for (int tp = 0; tp < 9; tp++) {
+    const int off = (tp / 3 - 1) * P + (tp % 3 - 1);
+    for (int kh = 0; kh < 2; kh++) {
+      const int k0 = kh * 16 + 2 * tq;  // channel of the fragment's first column pair
+      uint32_t bfr[4][2];
+      for (int nt = 0; nt < 4; nt++) {
+        const int n = nt * 8 + g;
+        bfr[nt][0] = wbw[((tp * kC + n) * kC + k0) >> 1];
+        bfr[nt][1] = wbw[((tp * kC + n) * kC + k0 + 8) >> 1];
+      }
+      for (int mt = 0; mt < 2; mt++) {
+        const int r0 = (prow[mt][0] + off) * CS + k0, r1i = (prow[mt][1] + off) * CS + k0;
+        const uint32_t a0 = h1w[r0 >> 1], a1 = h1w[r1i >> 1], a2 = h1w[(r0 + 8) >> 1], a3 = h1w[(r1i + 8) >> 1];
+        for (int nt = 0; nt < 4; nt++) mma_bf16(acc[mt][nt], a0, a1, a2, a3, bfr[nt][0], bfr[nt][1]);
+      }
+    }
+  }
+  for (int mt = 0; mt < 2; mt++)
+    for (int nt = 0; nt < 4; nt++)
+      for (int r = 0; r < 4; r++) {
+        const int pix = prow[mt][r >> 1];
+        const int n = nt * 8 + 2 * tq + (r & 1);
+        h2[n * PP + pix] = fmaxf(acc[mt][nt][r] + b2[n], 0.f);
+      }
+  __syncthreads();
+  float y = b3[0];
+  for (int cin = 0; cin < kC; cin++)
+    for (int tp = 0; tp < 9; tp++) y += w3[cin * 9 + tp] * h2[cin * PP + pc + (tp / 3 - 1) * P + (tp % 3 - 1)];
+  return y;
+}
+
+// inference inside the solve: corr += s * sa * net(features of r1), one CTA
+// per block of the finest tower, one thread per cell
+template <int NB>
+__global__ void __launch_bounds__(NB *NB) k_nn_infer(Topo t, Coef<float> c, BlockList L, const float *__restrict__ W,
+                                                     const __nv_bfloat16 *__restrict__ w2bf,
+                                                     const float *__restrict__ r1, const double *__restrict__ sa,
+                                                     float *__restrict__ corr, const FState *st) {
+  constexpr int NC = NB * NB, P = NB + 2, PP = P * P;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float *x0 = reinterpret_cast<float *>(smraw);  // [3][P][P]
+  __shared__ float red[NC / 32];
+  if (st->done || st->nn_off) return;
+  const int p = blockIdx.x, ci = threadIdx.x, pc = (ci / NB + 1) * P + (ci % NB + 1);
+  const int b = L.blocks[p];
+  const long q = (long)b * NC + ci;
+  for (int k = threadIdx.x; k < 3 * PP; k += blockDim.x) x0[k] = 0.f;
+  const float rv = r1[q];
+  const float m = block_max<NC>(fabsf(rv), red);
+  const float s = m > 0.f ? m : 1.f;
+  float f[3];
+  cell_features<NB>(t, c, b, ci, rv, s, f);
+  for (int k = 0; k < 3; k++) x0[k * PP + pc] = f[k];
+  const float y = local_part<NB>(nn_tail_bf16<NB>(W, w2bf, x0, smraw + 3 * PP * sizeof(float)), red);
+  corr[q] += s * (float)sa[(long)p * NC + ci] * y;
+}
+
+// the tensor-core forward on explicit feature blocks (test hook)
+template <int NB>
+__global__ void __launch_bounds__(NB *NB) k_nn_forward(const float *__restrict__ W,
+                                                       const __nv_bfloat16 *__restrict__ w2bf,
+                                                       const float *__restrict__ feat, float *__restrict__ y) {
+  constexpr int NC = NB * NB, P = NB + 2, PP = P * P;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float *x0 = reinterpret_cast<float *>(smraw);
+  const int ci = threadIdx.x, pc = (ci / NB + 1) * P + (ci % NB + 1);
+  for (int k = threadIdx.x; k < 3 * PP; k += blockDim.x) x0[k] = 0.f;
+  __syncthreads();
+  for (int k = 0; k < 3; k++) x0[k * PP + pc] = feat[((long)blockIdx.x * 3 + k) * NC + ci];
+  y[(long)blockIdx.x * NC + ci] = nn_tail_bf16<NB>(W, w2bf, x0, smraw + 3 * PP * sizeof(float));
+}
+
+template <int NB>
+constexpr size_t fwd_smem() {
+  return sizeof(float) * ((3 + 2 * kC) * (NB + 2) * (NB + 2) + kNParam + 2 * NB * NB + 2 * (NB + 1) * NB +
+                          (NB + 2) * (NB + 2));
+}
+template <int NB>
+constexpr size_t bwd_smem() {
+  return sizeof(float) * ((3 + 3 * kC + 1) * (NB + 2) * (NB + 2) + kNParam);
+}
+template <int NB>
+constexpr size_t infer_smem() {
+  return sizeof(float) * ((3 + kC) * (NB + 2) * (NB + 2) + kC * kCin * 9 + kC + kC + kC * 9 + 1) +
+         sizeof(__nv_bfloat16) * ((size_t)(NB + 2) * (NB + 2) * 40 + 9 * kC * kC) + 16;
+}
+
+}  // namespace
+
+static void set_smem_attrs() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(k_nn_fwd<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem<16>());
+  cudaFuncSetAttribute(k_nn_bwd<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem<16>());
+  cudaFuncSetAttribute(k_nn_fwd<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem<8>());
+  cudaFuncSetAttribute(k_nn_bwd<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem<8>());
+  cudaFuncSetAttribute(k_nn_infer<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem<16>());
+  cudaFuncSetAttribute(k_nn_infer<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem<8>());
+  cudaFuncSetAttribute(k_nn_forward<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem<16>());
+  cudaFuncSetAttribute(k_nn_forward<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem<8>());
+  done = true;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+bool MacGpu::learned_supported() const { return tt_.ndim == 2 && (tt_.nb == 8 || tt_.nb == 16); }
+
+void MacGpu::learned_init(unsigned seed) {
+  LearnedState &L = ls_;
+  L.nb = tt_.nb;
+  auto fa = [&](float *&p, size_t n) {
+    if (!p && cudaMalloc(&p, n * sizeof(float)) != cudaSuccess) {
+      p = nullptr;
+      fail("out of device memory (learned)");
+    }
+  };
+  fa(L.w, kNParam);
+  fa(L.g, kNParam);
+  fa(L.m, kNParam);
+  fa(L.v, kNParam);
+  fa(L.loss, 1);
+  if (!L.w2bf && cudaMalloc(&L.w2bf, 9 * kC * kC * sizeof(uint16_t)) != cudaSuccess) fail("out of device memory");
+  if (!err_.empty()) return;
+  // He initialisation; the output layer starts at zero, so the untrained
+  // correction is zero and the preconditioner is the plain V-cycle
+  std::mt19937 rng(seed);
+  std::vector<float> w(kNParam, 0.f);
+  std::normal_distribution<float> n1(0.f, std::sqrt(2.f / (kCin * 9))), n2(0.f, std::sqrt(2.f / (kC * 9)));
+  for (int k = kOW1; k < kOB1; k++) w[k] = n1(rng);
+  for (int k = kOW2; k < kOB2; k++) w[k] = n2(rng);
+  CK(cudaMemcpyAsync(L.w, w.data(), kNParam * sizeof(float), cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemsetAsync(L.g, 0, kNParam * sizeof(float), stream_));
+  CK(cudaMemsetAsync(L.m, 0, kNParam * sizeof(float), stream_));
+  CK(cudaMemsetAsync(L.v, 0, kNParam * sizeof(float), stream_));
+  L.step = 0;
+  L.trained = false;
+  learned_sync_bf16();
+}
+
+void MacGpu::learned_sync_bf16() {
+  k_w2_bf16<<<36, 256, 0, stream_>>>(ls_.w, reinterpret_cast<__nv_bfloat16 *>(ls_.w2bf));
+  CK(cudaGetLastError());
+}
+
+int MacGpu::learned_set_weights(const float *w, int n) {
+  if (n != kNParam) return -1;
+  if (!ls_.w) learned_init(1);
+  CKR_(cudaMemcpyAsync(ls_.w, w, kNParam * sizeof(float), cudaMemcpyHostToDevice, stream_), -1);
+  learned_sync_bf16();
+  ls_.trained = true;
+  return err_.empty() ? 0 : -1;
+}
+
+int MacGpu::learned_get_weights(float *w, int n) {
+  if (n != kNParam || !ls_.w) return -1;
+  CKR_(cudaMemcpyAsync(w, ls_.w, kNParam * sizeof(float), cudaMemcpyDeviceToHost, stream_), -1);
+  CKR_(cudaStreamSynchronize(stream_), -1);
+  return 0;
+}
+
+// reserve room for `more` training blocks
+void MacGpu::learned_reserve(int more) {
+  LearnedState &L = ls_;
+  const int need = L.nsamp + more;
+  if (need <= L.cap) return;
+  const int cap = std::max(need, 2 * L.cap);
+  const size_t nc = (size_t)ncell_;
+  const size_t na = aux_len();
+  float *f = nullptr, *a = nullptr;
+  if (cudaMalloc(&f, (size_t)cap * 3 * nc * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&a, (size_t)cap * na * sizeof(float)) != cudaSuccess) {
+    if (f) cudaFree(f);
+    fail("out of device memory (training set)");
+    return;
+  }
+  if (L.nsamp) {
+    CK(cudaMemcpyAsync(f, L.feat, (size_t)L.nsamp * 3 * nc * sizeof(float), cudaMemcpyDeviceToDevice, stream_));
+    CK(cudaMemcpyAsync(a, L.aux, (size_t)L.nsamp * na * sizeof(float), cudaMemcpyDeviceToDevice, stream_));
+  }
+  if (L.feat) cudaFree(L.feat);
+  if (L.aux) cudaFree(L.aux);
+  L.feat = f;
+  L.aux = a;
+  L.cap = cap;
+}
+
+void MacGpu::learned_free() {
+  LearnedState &L = ls_;
+  for (float *p : {L.w, L.g, L.m, L.v, L.loss, L.feat, L.aux, L.r1, L.scale})
+    if (p) cudaFree(p);
+  if (L.w2bf) cudaFree(L.w2bf);
+  L = LearnedState{};
+}
+
+// the FP32 V-cycle's output on the finest tower for residual r (tower cells)
+void MacGpu::learned_vcycle(float *r, float *z) {
+  const int L = finest_;
+  CK(cudaMemsetAsync(d_st_, 0, sizeof(FState), stream_));
+  // the V-cycle reads its residual from d_resid32_ and writes d_corr32_
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  CK(cudaMemcpyAsync(d_resid32_, r, n * sizeof(float), cudaMemcpyDeviceToDevice, stream_));
+  vcycle_device<float>(L, d_resid32_, d_corr32_, c32_, nullptr);
+  CK(cudaMemcpyAsync(z, d_corr32_, n * sizeof(float), cudaMemcpyDeviceToDevice, stream_));
+}
+
+namespace {
+// e = x* - x_k (FP64 -> FP32) on the tower cells; everything else 0
+__global__ void k_err32(BlockList L, int ncell, const double *xs, const double *xk, float *e) {
+  const int total = L.n * ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+    const int p = it / ncell;
+    const long q = (long)L.blocks[p] * ncell + (it - p * ncell);
+    e[q] = (float)(xs[q] - xk[q]);
+  }
+}
+__global__ void k_sub32(BlockList L, int ncell, const float *a, const float *b, float *o) {
+  const int total = L.n * ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+    const int p = it / ncell;
+    const long q = (long)L.blocks[p] * ncell + (it - p * ncell);
+    o[q] = a[q] - b[q];
+  }
+}
+inline int lgrid(long w) { return (int)std::max<long>(1, std::min<long>((w + 255) / 256, 152 * 16)); }
+}  // namespace
+
+// Training pairs from the plain solver: one device solve of the current
+// right-hand side from x0 = 0 with the plain FP32 V-cycle, tightened to
+// tol_rel 1e-12, records every iterate x_k; then, with x* the converged
+// solution, e = x* - x_k, r = A e (FP32), z = V(r), r1 = r - A z, e1 = e - z
+// become one training block per tower block.
+int MacGpu::learned_collect(int max_iters) {
+  if (!learned_supported()) {
+    fail("learned correction: 2D blocks of 8 or 16 cells only");
+    return -1;
+  }
+  if (!ls_.w) learned_init(1);
+  SolverParams save = prm_;
+  prm_.precision = 1;
+  prm_.use_mg_precond = 1;
+  prm_.bottom = 1;
+  prm_.graph = 0;
+  prm_.learned = 0;
+  prm_.tol_rel = 1e-12;
+  prm_.tol_abs = 0.0;
+  prm_.max_iter = std::max(1, max_iters);
+  if (prepare_device() != 0) {
+    prm_ = save;
+    return -1;
+  }
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  std::vector<double *> rec;
+  record_ = &rec;
+  zero_sol();
+  const int rc = enqueue_solve();
+  record_ = nullptr;
+  prm_ = save;
+  if (rc != 0) {
+    for (double *p : rec) cudaFree(p);
+    return -1;
+  }
+  CKR_(cudaStreamSynchronize(stream_), -1);
+  const int L = finest_;
+  const BlockList TL = tower_list(L);
+  const long w = (long)TL.n * ncell_;
+  float *e = nullptr, *r = nullptr, *z = nullptr, *r1 = nullptr;
+  cudaMalloc(&e, n * sizeof(float));
+  cudaMalloc(&r, n * sizeof(float));
+  cudaMalloc(&z, n * sizeof(float));
+  cudaMalloc(&r1, n * sizeof(float));
+  if (!e || !r || !z || !r1) {
+    fail("out of device memory (collection)");
+    return -1;
+  }
+  cudaMemsetAsync(e, 0, n * sizeof(float), stream_);
+  cudaMemsetAsync(r, 0, n * sizeof(float), stream_);
+  learned_reserve((int)rec.size() * TL.n);
+  const double *sa = d_sfac_.size() > (size_t)L ? d_sfac_[L] : nullptr;
+  for (double *xk : rec) {
+    if (!err_.empty() || !sa) break;
+    k_err32<<<lgrid(w), 256, 0, stream_>>>(TL, ncell_, vec_[kSOL], xk, e);
+    launch_apply<float>(topo_, c32_, TL, e, r, nullptr, nullptr, stream_);
+    learned_vcycle(r, z);
+    launch_apply<float>(topo_, c32_, TL, z, r1, r, nullptr, stream_);
+    k_sub32<<<lgrid(w), 256, 0, stream_>>>(TL, ncell_, e, z, e);
+    const long o = (long)ls_.nsamp * ncell_, oa = (long)ls_.nsamp * aux_len();
+    if (tt_.nb == 16)
+      k_nn_pairs<16><<<TL.n, 256, 0, stream_>>>(topo_, c32_, TL, r1, sa, ls_.feat + 3 * o, ls_.aux + oa);
+    else
+      k_nn_pairs<8><<<TL.n, 64, 0, stream_>>>(topo_, c32_, TL, r1, sa, ls_.feat + 3 * o, ls_.aux + oa);
+    CKR_(cudaGetLastError(), -1);
+    ls_.nsamp += TL.n;
+  }
+  CKR_(cudaStreamSynchronize(stream_), -1);
+  for (double *p : rec) cudaFree(p);
+  cudaFree(e);
+  cudaFree(r);
+  cudaFree(z);
+  cudaFree(r1);
+  // the collection solve overwrote the solution: leave a zero guess
+  zero_sol();
+  return err_.empty() ? (int)rec.size() : -1;
+}
+
+// one gradient of the loss over the blocks idx[0..nblk) (accumulated into g),
+// returns the loss; the activations go to the scratch vectors
+float MacGpu::learned_grad(const int *d_idx, int nblk, float inv_norm, float *h1, float *h2, float *dy) {
+  CKR_(cudaMemsetAsync(ls_.loss, 0, sizeof(float), stream_), 0.f);
+  if (ls_.nb == 16) {
+    k_nn_fwd<16><<<nblk, 256, fwd_smem<16>(), stream_>>>(ls_.w, ls_.feat, ls_.aux, d_idx, h1, h2, dy,
+                                                         ls_.loss, inv_norm);
+    k_nn_bwd<16><<<nblk, 256, bwd_smem<16>(), stream_>>>(ls_.w, ls_.feat, d_idx, h1, h2, dy, ls_.g);
+  } else {
+    k_nn_fwd<8><<<nblk, 64, fwd_smem<8>(), stream_>>>(ls_.w, ls_.feat, ls_.aux, d_idx, h1, h2, dy,
+                                                      ls_.loss, inv_norm);
+    k_nn_bwd<8><<<nblk, 64, bwd_smem<8>(), stream_>>>(ls_.w, ls_.feat, d_idx, h1, h2, dy, ls_.g);
+  }
+  CKR_(cudaGetLastError(), 0.f);
+  float l = 0.f;
+  CKR_(cudaMemcpyAsync(&l, ls_.loss, sizeof(float), cudaMemcpyDeviceToHost, stream_), 0.f);
+  CKR_(cudaStreamSynchronize(stream_), 0.f);
+  return l;
+}
+
+// Adam over the training set in shuffled minibatches; returns the mean loss
+// of the last epoch (per block), or -1
+float MacGpu::learned_train(int epochs, float lr, int batch, unsigned seed) {
+  if (!ls_.w || ls_.nsamp == 0) return -1.f;
+  set_smem_attrs();
+  batch = std::max(1, std::min(batch, ls_.nsamp));
+  const size_t nc = (size_t)ncell_;
+  float *h1 = nullptr, *h2 = nullptr, *dy = nullptr;
+  int *d_idx = nullptr;
+  cudaMalloc(&h1, (size_t)batch * kC * nc * sizeof(float));
+  cudaMalloc(&h2, (size_t)batch * kC * nc * sizeof(float));
+  cudaMalloc(&dy, (size_t)batch * nc * sizeof(float));
+  cudaMalloc(&d_idx, (size_t)ls_.nsamp * sizeof(int));
+  if (!h1 || !h2 || !dy || !d_idx) {
+    fail("out of device memory (training)");
+    return -1.f;
+  }
+  std::mt19937 rng(seed);
+  std::vector<int> idx(ls_.nsamp);
+  float last = 0.f;
+  for (int ep = 0; ep < epochs && err_.empty(); ep++) {
+    for (int k = 0; k < ls_.nsamp; k++) idx[k] = k;
+    std::shuffle(idx.begin(), idx.end(), rng);
+    CKR_(cudaMemcpyAsync(d_idx, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), -1.f);
+    double tot = 0.0;
+    for (int s0 = 0; s0 < ls_.nsamp; s0 += batch) {
+      const int nblk = std::min(batch, ls_.nsamp - s0);
+      const float inv = 1.f / (float)nblk;
+      tot += learned_grad(d_idx + s0, nblk, inv, h1, h2, dy) * nblk;
+      ls_.step++;
+      const float b1 = 0.9f, b2 = 0.999f;
+      k_adam<<<41, 256, 0, stream_>>>(ls_.w, ls_.g, ls_.m, ls_.v, kNParam, lr, b1, b2,
+                                      1.f - std::pow(b1, (float)ls_.step), 1.f - std::pow(b2, (float)ls_.step));
+    }
+    last = (float)(tot / ls_.nsamp);
+  }
+  CKR_(cudaStreamSynchronize(stream_), -1.f);
+  cudaFree(h1);
+  cudaFree(h2);
+  cudaFree(dy);
+  cudaFree(d_idx);
+  learned_sync_bf16();
+  ls_.trained = true;
+  return err_.empty() ? last : -1.f;
+}
+
+// loss and gradient of explicit training blocks (a test hook): feat
+// [n][3][ncell] and aux [n][aux_len()] on the host; grad [kNParam]
+float MacGpu::learned_loss_grad(const float *feat, const float *aux, int n, float *grad) {
+  if (!ls_.w) learned_init(1);
+  set_smem_attrs();
+  const int keep = ls_.nsamp;
+  ls_.nsamp = 0;
+  learned_reserve(n);
+  const size_t nc = (size_t)ncell_;
+  CKR_(cudaMemcpyAsync(ls_.feat, feat, (size_t)n * 3 * nc * sizeof(float), cudaMemcpyHostToDevice, stream_), -1.f);
+  CKR_(cudaMemcpyAsync(ls_.aux, aux, (size_t)n * aux_len() * sizeof(float), cudaMemcpyHostToDevice, stream_),
+       -1.f);
+  ls_.nsamp = n;
+  float *h1 = nullptr, *h2 = nullptr, *dy = nullptr;
+  int *d_idx = nullptr;
+  cudaMalloc(&h1, (size_t)n * kC * nc * sizeof(float));
+  cudaMalloc(&h2, (size_t)n * kC * nc * sizeof(float));
+  cudaMalloc(&dy, (size_t)n * nc * sizeof(float));
+  cudaMalloc(&d_idx, (size_t)n * sizeof(int));
+  std::vector<int> idx(n);
+  for (int k = 0; k < n; k++) idx[k] = k;
+  cudaMemcpyAsync(d_idx, idx.data(), n * sizeof(int), cudaMemcpyHostToDevice, stream_);
+  CKR_(cudaMemsetAsync(ls_.g, 0, kNParam * sizeof(float), stream_), -1.f);
+  const float l = learned_grad(d_idx, n, 1.f / (float)n, h1, h2, dy);
+  CKR_(cudaMemcpyAsync(grad, ls_.g, kNParam * sizeof(float), cudaMemcpyDeviceToHost, stream_), -1.f);
+  CKR_(cudaStreamSynchronize(stream_), -1.f);
+  CKR_(cudaMemsetAsync(ls_.g, 0, kNParam * sizeof(float), stream_), -1.f);
+  cudaFree(h1);
+  cudaFree(h2);
+  cudaFree(dy);
+  cudaFree(d_idx);
+  // the explicit blocks replaced the training set
+  (void)keep;
+  ls_.nsamp = 0;
+  return l;
+}
+
+// the tensor-core forward of explicit feature blocks (test hook)
+int MacGpu::learned_forward(const float *feat, int n, float *y) {
+  if (!ls_.w) learned_init(1);
+  set_smem_attrs();
+  const size_t nc = (size_t)ncell_;
+  float *df = nullptr, *dy = nullptr;
+  if (cudaMalloc(&df, (size_t)n * 3 * nc * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&dy, (size_t)n * nc * sizeof(float)) != cudaSuccess) {
+    if (df) cudaFree(df);
+    fail("out of device memory");
+    return -1;
+  }
+  CKR_(cudaMemcpyAsync(df, feat, (size_t)n * 3 * nc * sizeof(float), cudaMemcpyHostToDevice, stream_), -1);
+  if (ls_.nb == 16)
+    k_nn_forward<16><<<n, 256, infer_smem<16>(), stream_>>>(ls_.w, (const __nv_bfloat16 *)ls_.w2bf, df, dy);
+  else
+    k_nn_forward<8><<<n, 64, infer_smem<8>(), stream_>>>(ls_.w, (const __nv_bfloat16 *)ls_.w2bf, df, dy);
+  CKR_(cudaGetLastError(), -1);
+  CKR_(cudaMemcpyAsync(y, dy, (size_t)n * nc * sizeof(float), cudaMemcpyDeviceToHost, stream_), -1);
+  CKR_(cudaStreamSynchronize(stream_), -1);
+  cudaFree(df);
+  cudaFree(dy);
+  return 0;
+}
+
+// buffers and kernel attributes of the correction, set up before a graph
+// capture (no allocation happens inside the captured iteration)
+void MacGpu::learned_prepare() {
+  set_smem_attrs();
+  if (ls_.r1) return;
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  if (cudaMalloc(&ls_.r1, n * sizeof(float)) != cudaSuccess) {
+    ls_.r1 = nullptr;
+    fail("out of device memory (learned)");
+    return;
+  }
+  CK(cudaMemsetAsync(ls_.r1, 0, n * sizeof(float), stream_));
+}
+
+// the correction inside the device iteration: r1 = resid - A corr, then
+// corr += s * sa * net(...) on every block of the finest tower
+void MacGpu::learned_apply(float *resid, float *corr) {
+  const int L = finest_;
+  const BlockList TL = tower_list(L);
+  const long w = (long)TL.n * ncell_;
+  if (!ls_.r1) {
+    fail("learned correction used before its buffers were prepared");
+    return;
+  }
+  const double *sa = d_sfac_[L];
+  launch_k(false, k_nn_resid<2>, lgrid(w), 256, 0, stream_, topo_, c32_, TL, (const float *)corr,
+           (const float *)resid, ls_.r1, (const FState *)d_st_);
+  if (ls_.nb == 16)
+    launch_k(false, k_nn_infer<16>, TL.n, 256, infer_smem<16>(), stream_, topo_, c32_, TL, (const float *)ls_.w,
+             (const __nv_bfloat16 *)ls_.w2bf, (const float *)ls_.r1, sa, corr, (const FState *)d_st_);
+  else
+    launch_k(false, k_nn_infer<8>, TL.n, 64, infer_smem<8>(), stream_, topo_, c32_, TL, (const float *)ls_.w,
+             (const __nv_bfloat16 *)ls_.w2bf, (const float *)ls_.r1, sa, corr, (const FState *)d_st_);
+}
+
+}  // namespace sayaka_gb300

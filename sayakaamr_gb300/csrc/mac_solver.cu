@@ -338,6 +338,7 @@ MacGpu::~MacGpu() {
   fr(d_opP_);
   for (auto &q : d_sfac_) fr(q);
   for (auto &q : d_face_) fr(q);
+  learned_free();
   fr(d_opS_);
   fr(d_cnt_);
   fr(d_binv_);

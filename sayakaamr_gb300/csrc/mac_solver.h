@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "mac_device.h"
+#include "mac_learned.h"
 
 namespace sayaka_gb300 {
 
@@ -34,6 +35,7 @@ struct SolverParams {
   int pdl = 0;              // device path: programmatic dependent launch between the iteration's kernels
   int cluster_cells = 16384;  // vcycle_kernel 2: phases touching at most this many cells run in the cluster
   int smooth_variant = -1;    // device smoother launch bounds: -1 autotune at prepare, else variant index
+  int learned = 0;            // device path, FP32 V-cycle: apply the trained block correction
 };
 
 struct SolveInfo {
@@ -99,6 +101,18 @@ class MacGpu {
   void vcycle(const double *p_all, double *phat_all);
   void flux(int dir, const double *phi_all, double *flux_all);
   void fix_bc(const double *phi_grown, int ngrow, double *rhs_all);
+
+  // learned block correction (mac_learned.cu)
+  bool learned_supported() const;
+  int learned_collect(int max_iters);
+  float learned_train(int epochs, float lr, int batch, unsigned seed);
+  float learned_loss_grad(const float *feat, const float *aux, int n, float *grad);
+  int aux_len() const { return 2 * tt_.nb * tt_.nb + 2 * (tt_.nb + 1) * tt_.nb; }
+  int learned_forward(const float *feat, int n, float *y);
+  int learned_set_weights(const float *w, int n);
+  int learned_get_weights(float *w, int n);
+  int learned_samples() const { return ls_.nsamp; }
+  bool learned_ready() const { return ls_.trained; }
 
   // projection step around the solve (compact all-block face arrays, host)
   void rhs_from_div(const double *const *u_all, const double *const *w_all, double scale);
@@ -187,6 +201,9 @@ class MacGpu {
   template <typename T>
   void bottom_launch(T *resid, T *corr);
   template <typename T>
+  void precondition(int L, T *resid, T *corr, const Coef<T> &c, double *out);
+  bool learned_active() const { return prm_.learned && prm_.precision == 1 && ls_.trained && learned_supported(); }
+  template <typename T>
   void vc_out_launch(const BlockList &TL, T *corr, double *out);
 
   TreeTables tt_;
@@ -231,6 +248,16 @@ class MacGpu {
   double *d_opP_ = nullptr, *d_opS_ = nullptr;  // factors of the device solve's operator
   std::vector<double *> d_sfac_;                // FP64 smoother factors per tower: sa then ia
   std::vector<double *> d_face_;                // face fields of the projection step (u, w, flux)
+  LearnedState ls_;
+  std::vector<double *> *record_ = nullptr;     // iterates recorded by a collection solve
+  void learned_init(unsigned seed);
+  void learned_sync_bf16();
+  void learned_reserve(int more);
+  void learned_free();
+  void learned_vcycle(float *r, float *z);
+  void learned_apply(float *resid, float *corr);
+  void learned_prepare();
+  float learned_grad(const int *d_idx, int nblk, float inv_norm, float *h1, float *h2, float *dy);
   double *face_scratch(int k);
   unsigned *d_cnt_ = nullptr;
   double *d_binv_ = nullptr;
@@ -239,7 +266,7 @@ class MacGpu {
   cudaGraphExec_t graph_exec_ = nullptr;
   int graph_prec_ = -1, graph_npost_ = -1;
   int kernels_per_iter_ = 0;
-  int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1;
+  int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1, graph_nn_ = -1;
   int rbgs_variant_[2] = {-1, -1};  // tuned smoother variant per precision (0 FP64, 1 FP32)
   float rbgs_us_[2][8] = {};        // measured microseconds per variant (kRbgsVariants <= 8)
   // cooperative V-cycle

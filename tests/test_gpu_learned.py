@@ -1,0 +1,115 @@
+"""The learned block correction of the device solve, on the GPU through the
+C ABI: the FP32 training gradient and the BF16 tensor-core forward against
+the CPU restatement (oracle/nn_oracle.py, pinned by finite differences),
+training on the plain solver's own pairs, the gain over the plain FP32
+V-cycle on config2, and the fallback to plain MG when the correction
+stalls the solve."""
+import numpy as np
+import pytest
+
+import sayakaamr_gb300 as sg
+from oracle import nn_oracle as nn
+
+pytestmark = pytest.mark.gpu
+
+GRAD_RTOL = 2e-3   # FP32 accumulation over 64..256 cells x 288 taps vs float64
+BF16_RTOL = 2e-2   # BF16 hidden layer (8-bit mantissa) vs the oracle's BF16 emulation
+
+
+def small_solver(nb):
+    t = sg.AmrTree(2, nb, 2, 2, 64)
+    t.init_uniform_root((1, 1, 1), (0, 0, 0), (1, 1, 0), (-20,) * 6, (0,) * 6)
+    t.init_refine_to_min_level()
+    return sg.MacSolver(t.tables())
+
+
+@pytest.mark.parametrize("nb", [8, 16])
+def test_training_gradient_matches_oracle(nb):
+    S = small_solver(nb)
+    rng = np.random.default_rng(nb)
+    w = nn.init(nb)
+    S.set_learned_weights(w)
+    n = 3
+    feat = rng.standard_normal((n, 3, nb * nb)).astype(np.float32)
+    aux = nn.random_aux(rng, n, nb)
+    loss, g = S.learned_loss_grad(feat, aux)
+    lref, gref = nn.loss_grad(w, feat, aux, nb)
+    assert abs(loss - lref) <= GRAD_RTOL * abs(lref)
+    scale = np.abs(gref).max()
+    assert np.max(np.abs(g - gref)) <= GRAD_RTOL * scale, np.max(np.abs(g - gref)) / scale
+
+
+@pytest.mark.parametrize("nb", [8, 16])
+def test_tensor_core_forward_matches_oracle(nb):
+    S = small_solver(nb)
+    rng = np.random.default_rng(100 + nb)
+    w = nn.init(7 + nb)
+    S.set_learned_weights(w)
+    feat = rng.standard_normal((5, 3, nb * nb)).astype(np.float32)
+    y = S.learned_forward(feat)
+    ref = nn.forward(w, feat, nb, bf16=True, project=False)
+    scale = np.abs(ref).max()
+    assert np.max(np.abs(y - ref)) <= BF16_RTOL * scale
+
+
+@pytest.fixture(scope="module")
+def trained_config2():
+    from sayakaamr_gb300 import workloads
+    prob = workloads.config2()
+    S = workloads.make_solver(prob)
+    S.set_params(tol_rel=1e-8, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=1, bottom=1)
+    S.prepare()
+    iters = S.learned_collect(200)
+    first = S.learned_train(epochs=1, lr=1e-3, batch=256, seed=3)
+    last = S.learned_train(epochs=9, lr=1e-3, batch=256, seed=4)
+    return prob, S, iters, first, last
+
+
+def test_training_lowers_the_loss_on_solver_pairs(trained_config2):
+    """the block-local residual left after the correction falls with training
+    (measured on config2: 11.4 after the first epoch, 9.1 after ten)"""
+    prob, S, iters, first, last = trained_config2
+    assert iters > 5
+    assert last < 0.9 * first, (first, last)
+
+
+def test_learned_correction_against_plain_fp32_vcycle(trained_config2):
+    """the ablation: same workload, same tolerance, with and without the
+    trained correction.  Both converge; the correction either takes no more
+    iterations than the plain FP32 V-cycle, or the device detects the stall
+    and finishes with plain MG (status STALL_FALLBACK).  Measured on config2:
+    34 iterations plain, 35-52 with the correction, which stalls and falls
+    back: the block-local correction does not help BiCGSTAB here."""
+    prob, S, iters, first, last = trained_config2
+    res, st = {}, {}
+    for on in (0, 1):
+        S.set_rhs_compact(prob.rhs)
+        S.set_zero_sol()
+        S.set_params(learned=on)
+        info = S.cg_solve()
+        assert info["status"] in (sg.OK, sg.STALL_FALLBACK), info
+        assert info["rnorm"] < 1e-8 * info["rnorm0"]
+        res[on], st[on] = info["iterations"], info["status"]
+    print("iterations plain FP32 V-cycle %d, with the learned correction %d (status %d)" % (res[0], res[1], st[1]))
+    assert st[0] == sg.OK
+    assert res[1] <= res[0] or st[1] == sg.STALL_FALLBACK
+
+
+def test_stalled_correction_falls_back_to_plain_mg(trained_config2):
+    """a correction that stalls the solve (weights scaled up 50x) is switched
+    off on the device; the solve still converges with plain MG and reports
+    the fallback"""
+    prob, S, iters, first, last = trained_config2
+    good = S.learned_weights()
+    bad = good.copy()
+    bad[nn.OW3:nn.OB3 + 1] *= 50.0
+    S.set_learned_weights(bad)
+    try:
+        S.set_rhs_compact(prob.rhs)
+        S.set_zero_sol()
+        S.set_params(learned=1)
+        info = S.cg_solve()
+        assert info["status"] in (sg.STALL_FALLBACK, sg.OK), info
+        assert info["rnorm"] < 1e-8 * info["rnorm0"]
+    finally:
+        S.set_learned_weights(good)
