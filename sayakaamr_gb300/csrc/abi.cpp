@@ -6,7 +6,9 @@
 #include <cstring>
 #include <exception>
 #include <memory>
+#include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/sayaka_gb300.h"
@@ -80,26 +82,50 @@ struct Layout {
 };
 
 // valid cells (or faces) of every block: TreeData layout <-> compact
+// fn(b0, b1) over block ranges, on up to 16 host threads for large fields
+// (the row copies of a 16M-cell field take tens of milliseconds on one core)
+template <class F>
+void for_blocks(int nblocks, size_t bytes, F &&fn) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = bytes < (4u << 20) ? 1 : (int)std::min<unsigned>(16u, hw);
+  if (nt <= 1 || nblocks < 2 * nt) {
+    fn(0, nblocks);
+    return;
+  }
+  std::vector<std::thread> th;
+  const int per = (nblocks + nt - 1) / nt;
+  for (int t = 0; t < nt; t++) {
+    const int b0 = t * per, b1 = std::min(nblocks, b0 + per);
+    if (b0 < b1) th.emplace_back([&fn, b0, b1] { fn(b0, b1); });
+  }
+  for (auto &x : th) x.join();
+}
+
 void pack(const Layout &L, int nblocks, const double *src, double *dst) {
   const int e[3] = {L.nb + (L.stag == 0), L.nd >= 2 ? L.nb + (L.stag == 1) : 1, L.nd == 3 ? L.nb + (L.stag == 2) : 1};
-  size_t q = 0;
-  for (int b = 0; b < nblocks; b++)
-    for (int k = 0; k < e[2]; k++)
-      for (int j = 0; j < e[1]; j++) {
-        const double *row = src + L.at(b, 0, j, k);
-        std::memcpy(dst + q, row, e[0] * sizeof(double));
-        q += e[0];
-      }
+  const size_t per = (size_t)e[0] * e[1] * e[2];
+  for_blocks(nblocks, nblocks * per * sizeof(double), [&](int b0, int b1) {
+    size_t q = (size_t)b0 * per;
+    for (int b = b0; b < b1; b++)
+      for (int k = 0; k < e[2]; k++)
+        for (int j = 0; j < e[1]; j++) {
+          std::memcpy(dst + q, src + L.at(b, 0, j, k), e[0] * sizeof(double));
+          q += e[0];
+        }
+  });
 }
 void unpack(const Layout &L, int nblocks, const double *src, double *dst) {
   const int e[3] = {L.nb + (L.stag == 0), L.nd >= 2 ? L.nb + (L.stag == 1) : 1, L.nd == 3 ? L.nb + (L.stag == 2) : 1};
-  size_t q = 0;
-  for (int b = 0; b < nblocks; b++)
-    for (int k = 0; k < e[2]; k++)
-      for (int j = 0; j < e[1]; j++) {
-        std::memcpy(dst + L.at(b, 0, j, k), src + q, e[0] * sizeof(double));
-        q += e[0];
-      }
+  const size_t per = (size_t)e[0] * e[1] * e[2];
+  for_blocks(nblocks, nblocks * per * sizeof(double), [&](int b0, int b1) {
+    size_t q = (size_t)b0 * per;
+    for (int b = b0; b < b1; b++)
+      for (int k = 0; k < e[2]; k++)
+        for (int j = 0; j < e[1]; j++) {
+          std::memcpy(dst + L.at(b, 0, j, k), src + q, e[0] * sizeof(double));
+          q += e[0];
+        }
+  });
 }
 
 int status_of(sayaka_mac *h) {
