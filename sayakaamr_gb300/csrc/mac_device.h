@@ -67,6 +67,19 @@ struct FState {
   double nn_best;
 };
 
+// The dense FP64 bottom solve: one inverse per connected component of the
+// level-1 blocks (a forest of independent problems has one per problem),
+// rows grouped by component, one CTA tile per 8 rows.
+struct BottomDev {
+  const double *binv;          // the components' row-major inverses, back to back
+  const int *blocks;           // level-1 block of every ncell rows, in row order
+  const int *comp_row0, *comp_n;
+  const long long *comp_off;   // start of each component's inverse in binv
+  const int *tile_comp, *tile_row0;
+  int ntiles, ncell, max_n;
+};
+constexpr int kBottomTileRows = 8;
+
 // one phase of the cooperative V-cycle program (mac_vcycle.cu)
 enum PhaseOp { kPhaseRestrict = 0, kPhaseBottom = 1, kPhaseProlong = 2, kPhaseSmooth = 3, kPhaseOut = 4 };
 struct VPhase {

@@ -42,8 +42,12 @@ __device__ __forceinline__ double wsum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// max that keeps NaN (fmax drops it): a NaN anywhere in a vector must reach
+// the convergence test and end the solve as a breakdown, not as convergence
+__device__ __forceinline__ double nmax(double a, double b) { return (a != a || b != b) ? a + b : fmax(a, b); }
+
 __device__ __forceinline__ double wmax(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) v = nmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 
@@ -66,7 +70,7 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, d
 #pragma unroll
     for (int i = 0; i < NV; i++) {
       double r = 0.0;
-      for (int q = 0; q < kTPB / 32; q++) r = ((maxmask >> i) & 1) ? fmax(r, sh[i][q]) : r + sh[i][q];
+      for (int q = 0; q < kTPB / 32; q++) r = ((maxmask >> i) & 1) ? nmax(r, sh[i][q]) : r + sh[i][q];
       partials[blockIdx.x * NV + i] = r;
     }
     __threadfence();
@@ -82,7 +86,7 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, d
 #pragma unroll
     for (int i = 0; i < NV; i++) {
       const double pv = ((volatile double *)partials)[b * NV + i];
-      acc[i] = ((maxmask >> i) & 1) ? fmax(acc[i], pv) : acc[i] + pv;
+      acc[i] = ((maxmask >> i) & 1) ? nmax(acc[i], pv) : acc[i] + pv;
     }
   }
   __syncthreads();
@@ -97,7 +101,7 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, d
 #pragma unroll
     for (int i = 0; i < NV; i++) {
       double r = 0.0;
-      for (int q = 0; q < kTPB / 32; q++) r = ((maxmask >> i) & 1) ? fmax(r, sh[i][q]) : r + sh[i][q];
+      for (int q = 0; q < kTPB / 32; q++) r = ((maxmask >> i) & 1) ? nmax(r, sh[i][q]) : r + sh[i][q];
       fin[i] = r;
     }
     epi(fin);
@@ -146,6 +150,11 @@ struct EpiHalf {  // |s|
   FState *st;
   __device__ void operator()(const double *v) const {
     st->rnorm = v[0];
+    if (v[0] != v[0]) {  // NaN: breakdown
+      st->stat = 1;
+      st->done = 1;
+      return;
+    }
     if (v[0] < st->rnorm0 * st->tol_rel || v[0] < st->tol_abs) {
       st->conv = 1;
       st->done = 1;
@@ -167,6 +176,11 @@ struct EpiEnd {  // |r|, rhat.r of the next iteration
   FState *st;
   __device__ void operator()(const double *v) const {
     st->rnorm = v[0];
+    if (v[0] != v[0]) {  // NaN: breakdown
+      st->stat = 1;
+      st->done = 1;
+      return;
+    }
     if (v[0] < st->rnorm0 * st->tol_rel + st->tol_abs) {
       st->conv = 1;
       st->done = 1;
@@ -261,7 +275,7 @@ __global__ void __launch_bounds__(kTPB) k_supdate(BlockList L, int ncell, FState
     s[q] = sv;
     x[q] = __fma_rn(a, (double)phat[q], x[q]);
     resid[q] = vf[q] > 0 ? (T)sv : (T)0;
-    m[0] = fmax(m[0], fabs(sv));
+    m[0] = nmax(m[0], fabs(sv));
   }
   grid_reduce<1>(m, 1u, partials, counter, EpiHalf{st});
 }
@@ -281,7 +295,7 @@ __global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, FState
     x[q] = __fma_rn(om, (double)shat[q], x[q]);
     const double rv = __fma_rn(-om, t[q], s[q]);
     r[q] = rv;
-    m[0] = fmax(m[0], fabs(rv));
+    m[0] = nmax(m[0], fabs(rv));
     m[1] = __fma_rn(rhat[q], rv, m[1]);
   }
   grid_reduce<2>(m, 1u, partials, counter, EpiEnd{st});
@@ -397,8 +411,10 @@ __global__ void __launch_bounds__(kTPB) k_smooth_factors(Topo t, Coef<double> c,
     }
     const double vfv = c.vf[(long)b * t.ncell + ci];
     const long o = (long)p * t.ncell + ci;
-    sa[o] = vfv > 0 ? dv * vfv / diag : 0.0;
-    ia[o] = vfv > 0 ? 1.0 / diag : 0.0;
+    // a fluid cell whose faces are all closed has no equation (diag 0): it
+    // is left at zero instead of dividing by zero
+    sa[o] = vfv > 0 && diag > 0 ? dv * vfv / diag : 0.0;
+    ia[o] = vfv > 0 && diag > 0 ? 1.0 / diag : 0.0;
   }
 }
 
@@ -461,7 +477,7 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
       acc[1] = __fma_rn(yv, yv, acc[1]);
     }
     if (MODE == 2) {
-      acc[0] = fmax(acc[0], fabs(yv));
+      acc[0] = nmax(acc[0], fabs(yv));
       acc[1] = __fma_rn(yv, yv, acc[1]);
     }
   }
@@ -470,53 +486,50 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
   if (MODE == 2) grid_reduce<2>(acc, 1u, partials, counter, EpiInit{st});
 }
 
-// dense bottom solve: corr(level 1) = Binv * resid(level 1), one warp per row
+// dense bottom solve: corr(level 1) = Binv * resid(level 1), one CTA per
+// tile of 8 rows of one component
 template <typename T>
-__global__ void __launch_bounds__(kTPB) k_bottom_gemv(int n, const double *__restrict__ binv, const int *blocks,
-                                                    int ncell, const T *__restrict__ resid, T *__restrict__ corr,
-                                                    const FState *st) {
+__global__ void __launch_bounds__(kTPB) k_bottom_gemv(BottomDev bd, const T *__restrict__ resid,
+                                                    T *__restrict__ corr, const FState *st) {
   pdl_enter();
   if (st && st->done) return;
   extern __shared__ double rv[];
-  for (int j = threadIdx.x; j < n; j += blockDim.x) rv[j] = (double)resid[(long)blocks[j / ncell] * ncell + j % ncell];
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (row >= n) return;
-  const double *a = binv + (long)row * n;
-  double s = 0.0;
-  for (int j = lane; j < n; j += 32) s += a[j] * rv[j];
-  s = wsum(s);
-  if (lane == 0) corr[(long)blocks[row / ncell] * ncell + row % ncell] = (T)s;
+  stencil::bottom_tile<T>(bd, blockIdx.x, resid, corr, rv);
 }
 
-// in-place Gauss-Jordan inversion step k (no pivoting: the pinned, row-scaled
-// level-1 operator has positive pivots)
-__global__ void k_gj_save(int n, int k, const double *a, double *row, double *col) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    row[i] = a[(long)k * n + i];
-    col[i] = a[(long)i * n + k];
+// in-place Gauss-Jordan inversion step k of nmat matrices of order m at
+// offsets offs (no pivoting: the pinned, row-scaled level-1 operator has
+// positive pivots)
+__global__ void k_gj_save(int m, int k, int nmat, const long long *offs, const double *a, double *row, double *col) {
+  const long total = (long)nmat * m;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int mat = (int)(it / m), i = (int)(it - (long)mat * m);
+    const double *am = a + offs[mat];
+    row[it] = am[(long)k * m + i];
+    col[it] = am[(long)i * m + k];
   }
 }
-__global__ void k_gj_step(int n, int k, double *a, const double *row, const double *col) {
-  const double piv = row[k];
-  const long total = (long)n * n;
+__global__ void k_gj_step(int m, int k, int nmat, const long long *offs, double *a, const double *row,
+                          const double *col) {
+  const long mm = (long)m * m, total = (long)nmat * mm;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(it / n), j = (int)(it - (long)i * n);
+    const int mat = (int)(it / mm);
+    const long e = it - (long)mat * mm;
+    const int i = (int)(e / m), j = (int)(e - (long)i * m);
+    const double *rw = row + (long)mat * m, *cl = col + (long)mat * m;
+    const double piv = rw[k];
+    double *am = a + offs[mat];
     double v;
     if (i == k)
-      v = j == k ? 1.0 / piv : row[j] / piv;
+      v = j == k ? 1.0 / piv : rw[j] / piv;
     else
-      v = j == k ? -col[i] / piv : a[it] - col[i] * (row[j] / piv);
-    a[it] = v;
+      v = j == k ? -cl[i] / piv : am[e] - cl[i] * (rw[j] / piv);
+    am[e] = v;
   }
 }
-__global__ void k_zero_cols(int n, double *a, const int *cols, int ncols) {
-  const long total = (long)n * ncols;
-  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
-    const int r = (int)(it / ncols), q = (int)(it - (long)r * ncols);
-    a[(long)r * n + cols[q]] = 0.0;
-  }
+// zero column col of the order-m matrix at off (a pinned Neumann cell)
+__global__ void k_zero_col(long long off, int m, int col, double *a) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) a[off + (long)r * m + col] = 0.0;
 }
 
 __global__ void k_to_f32(long n, const double *src, float *dst) {
@@ -682,128 +695,215 @@ void MacGpu::build_bottom() {
   const int nd = tt_.ndim, nb = tt_.nb;
   const std::vector<int> &B1 = towers_[1].blocks;
   const int nblk1 = (int)B1.size();
-  const int n = nblk1 * ncell_;
-  n_bot_ = n;
-  if (n == 0) return;
-  if ((double)n * n * 8 > 4.0e9) {
+  n_bot_ = nblk1 * ncell_;
+  if (n_bot_ == 0) return;
+  std::vector<int> pos1(tt_.num_blocks, -1);
+  for (int p = 0; p < nblk1; p++) pos1[B1[p]] = p;
+  // connected components of the level-1 blocks; within a component the
+  // blocks keep their tower order
+  std::vector<int> bcomp(nblk1, -1);
+  std::vector<std::vector<int>> comps;
+  for (int p0 = 0; p0 < nblk1; p0++) {
+    if (bcomp[p0] >= 0) continue;
+    const int c = (int)comps.size();
+    comps.emplace_back();
+    std::vector<int> stack{p0};
+    bcomp[p0] = c;
+    while (!stack.empty()) {
+      const int p = stack.back();
+      stack.pop_back();
+      comps[c].push_back(p);
+      for (int f = 0; f < 2 * nd; f++) {
+        const int nbr = tt_.neighbor[B1[p] * 6 + f];
+        if (nbr < 0) continue;
+        if (pos1[nbr] < 0) {
+          fail("level-1 neighbour outside tower 1");
+          return;
+        }
+        if (bcomp[pos1[nbr]] < 0) {
+          bcomp[pos1[nbr]] = c;
+          stack.push_back(pos1[nbr]);
+        }
+      }
+    }
+    std::sort(comps[c].begin(), comps[c].end());
+  }
+  const int nc = (int)comps.size();
+  std::vector<int> order, comp_row0(nc), comp_n(nc), rowpos(tt_.num_blocks, -1);
+  std::vector<long long> comp_off(nc);
+  long long tot = 0;
+  int max_n = 0;
+  for (int c = 0; c < nc; c++) {
+    comp_row0[c] = (int)order.size() * ncell_;
+    comp_n[c] = (int)comps[c].size() * ncell_;
+    comp_off[c] = tot;
+    tot += (long long)comp_n[c] * comp_n[c];
+    max_n = std::max(max_n, comp_n[c]);
+    for (int p : comps[c]) {
+      rowpos[B1[p]] = (int)order.size();
+      order.push_back(B1[p]);
+    }
+  }
+  if ((double)tot * 8 > 4.0e9 || (double)max_n * 8 > 200.0 * 1024) {
     fail("level-1 problem too large for the dense bottom solve");
     return;
   }
-  std::vector<int> pos(tt_.num_blocks, -1);
-  for (int p = 0; p < nblk1; p++) pos[B1[p]] = p;
-  std::vector<double> A((size_t)n * n, 0.0);
-  std::vector<int> dir_touch(n, 0);
-  // adjacency for the connected components (face coefficient > 0)
-  std::vector<std::vector<int>> adj(n);
+  std::vector<double> A((size_t)tot, 0.0);
+  std::vector<int> dir_touch(n_bot_, 0), rcomp(n_bot_);
+  std::vector<std::vector<int>> adj(n_bot_);  // global rows, face coefficient > 0
   auto fidx = [&](int d, const int ijk[3], int s) {
     int f[3] = {ijk[0], ijk[1], ijk[2]};
     f[d] += s;
     const int e0 = nb + (d == 0), e1 = nb + (d == 1);
     return f[0] + e0 * (f[1] + e1 * f[2]);
   };
-  for (int p = 0; p < nblk1; p++) {
-    const int b = B1[p];
-    const double dv = geom_[b * 8 + 6];
-    for (int c = 0; c < ncell_; c++) {
-      const int row = p * ncell_ + c;
-      int ijk[3] = {c % nb, nd >= 2 ? (c / nb) % nb : 0, nd == 3 ? c / (nb * nb) : 0};
-      const double vf = vf_[(size_t)b * ncell_ + c];
-      if (!(vf > 0)) {
-        A[(size_t)row * n + row] = 1.0;
-        continue;
-      }
-      double diag = 0.0;
-      for (int f = 0; f < 2 * nd; f++) {
-        const int d = f >> 1, s = f & 1;
-        const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
-        const int fx = fidx(d, ijk, s);
-        double T = beta_ * geom_[b * 8 + 3 + d] / geom_[b * 8 + d];
-        T = T * bcoef_[d][(size_t)b * nfb_ + fx];
-        T = T * afrac_[d][(size_t)b * nfb_ + fx];
-        int ncol = -1;
-        if (!bnd) {
-          int q[3] = {ijk[0], ijk[1], ijk[2]};
-          q[d] += s ? 1 : -1;
-          ncol = p * ncell_ + (q[0] + nb * (q[1] + nb * q[2]));
-        } else {
-          const int nbr = tt_.neighbor[b * 6 + f];
-          if (nbr >= 0) {
-            if (pos[nbr] < 0) {
-              fail("level-1 neighbour outside tower 1");
-              return;
-            }
+  for (int c = 0; c < nc; c++) {
+    const int m = comp_n[c], r0 = comp_row0[c];
+    double *Ac = A.data() + comp_off[c];
+    for (int p : comps[c]) {
+      const int b = B1[p];
+      const double dv = geom_[b * 8 + 6];
+      for (int cc = 0; cc < ncell_; cc++) {
+        const int g = rowpos[b] * ncell_ + cc, row = g - r0;
+        rcomp[g] = c;
+        int ijk[3] = {cc % nb, nd >= 2 ? (cc / nb) % nb : 0, nd == 3 ? cc / (nb * nb) : 0};
+        const double vf = vf_[(size_t)b * ncell_ + cc];
+        if (!(vf > 0)) {
+          Ac[(size_t)row * m + row] = 1.0;
+          continue;
+        }
+        double diag = 0.0;
+        for (int f = 0; f < 2 * nd; f++) {
+          const int d = f >> 1, s = f & 1;
+          const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+          const int fx = fidx(d, ijk, s);
+          double T = beta_ * geom_[b * 8 + 3 + d] / geom_[b * 8 + d];
+          T = T * bcoef_[d][(size_t)b * nfb_ + fx];
+          T = T * afrac_[d][(size_t)b * nfb_ + fx];
+          int ncol = -1;
+          if (!bnd) {
             int q[3] = {ijk[0], ijk[1], ijk[2]};
-            q[d] = s ? 0 : nb - 1;
-            ncol = pos[nbr] * ncell_ + (q[0] + nb * (q[1] + nb * q[2]));
+            q[d] += s ? 1 : -1;
+            ncol = rowpos[b] * ncell_ + (q[0] + nb * (q[1] + nb * q[2]));
           } else {
-            const int bct = bc_type_[b * 6 + f];
-            if (bct == kBCNeumann) T = 0.0;
-            else {
-              T = 2.0 * T;
-              if (T > 0) dir_touch[row] = 1;
+            const int nbr = tt_.neighbor[b * 6 + f];
+            if (nbr >= 0) {
+              int q[3] = {ijk[0], ijk[1], ijk[2]};
+              q[d] = s ? 0 : nb - 1;
+              ncol = rowpos[nbr] * ncell_ + (q[0] + nb * (q[1] + nb * q[2]));
+            } else {
+              const int bct = bc_type_[b * 6 + f];
+              if (bct == kBCNeumann) T = 0.0;
+              else {
+                T = 2.0 * T;
+                if (T > 0) dir_touch[g] = 1;
+              }
             }
           }
+          diag += T;
+          if (ncol >= 0) {
+            Ac[(size_t)row * m + (ncol - r0)] -= T / dv / vf;
+            if (T > 0) adj[g].push_back(ncol);
+          }
         }
-        diag += T;
-        if (ncol >= 0) {
-          A[(size_t)row * n + ncol] -= T / dv / vf;
-          if (T > 0) adj[row].push_back(ncol);
-        }
+        Ac[(size_t)row * m + row] += diag / dv / vf;
       }
-      A[(size_t)row * n + row] += diag / dv / vf;
     }
   }
   // pin one cell of every fluid component that has no Dirichlet face
-  std::vector<int> comp(n, -1), pins;
-  for (int r0 = 0; r0 < n; r0++) {
-    const int b = B1[r0 / ncell_];
-    if (comp[r0] >= 0 || !(vf_[(size_t)b * ncell_ + r0 % ncell_] > 0)) continue;
+  std::vector<int> seen(n_bot_, -1), pins;
+  for (int r0 = 0; r0 < n_bot_; r0++) {
+    const int b = order[r0 / ncell_];
+    if (seen[r0] >= 0 || !(vf_[(size_t)b * ncell_ + r0 % ncell_] > 0)) continue;
     std::vector<int> stack{r0};
-    comp[r0] = r0;
+    seen[r0] = r0;
     bool dirichlet = false;
     while (!stack.empty()) {
       const int r = stack.back();
       stack.pop_back();
       dirichlet |= dir_touch[r] != 0;
       for (int q : adj[r])
-        if (comp[q] < 0) {
-          comp[q] = r0;
+        if (seen[q] < 0) {
+          seen[q] = r0;
           stack.push_back(q);
         }
     }
     if (!dirichlet) {
-      for (int j = 0; j < n; j++) A[(size_t)r0 * n + j] = 0.0;
-      A[(size_t)r0 * n + r0] = 1.0;
+      const int c = rcomp[r0], m = comp_n[c], lr = r0 - comp_row0[c];
+      double *Ac = A.data() + comp_off[c];
+      for (int j = 0; j < m; j++) Ac[(size_t)lr * m + j] = 0.0;
+      Ac[(size_t)lr * m + lr] = 1.0;
       pins.push_back(r0);
     }
   }
-  if (d_binv_) cudaFree(d_binv_);
-  d_binv_ = nullptr;
-  if (cudaMalloc(&d_binv_, (size_t)n * n * sizeof(double)) != cudaSuccess) {
-    fail("out of device memory (bottom inverse)");
-    return;
+  bottom_free();
+  std::vector<int> tile_comp, tile_row0;
+  for (int c = 0; c < nc; c++)
+    for (int r = 0; r < comp_n[c]; r += kBottomTileRows) {
+      tile_comp.push_back(c);
+      tile_row0.push_back(r);
+    }
+  auto up = [&](auto *&dptr, const auto &v) {
+    using E = typename std::remove_reference<decltype(v[0])>::type;
+    if (cudaMalloc(&dptr, std::max<size_t>(v.size(), 1) * sizeof(E)) != cudaSuccess) {
+      fail("out of device memory (bottom solve)");
+      return;
+    }
+    if (!v.empty()) CK_(cudaMemcpyAsync(dptr, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, stream_));
+  };
+  up(d_binv_, A);
+  up(d_bot_blocks_, order);
+  up(d_comp_row0_, comp_row0);
+  up(d_comp_n_, comp_n);
+  up(d_comp_off_, comp_off);
+  up(d_tile_comp_, tile_comp);
+  up(d_tile_row0_, tile_row0);
+  if (!err_.empty()) return;
+  // Gauss-Jordan, batched over the components of equal order
+  std::vector<int> sizes(comp_n);
+  std::sort(sizes.begin(), sizes.end());
+  sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+  for (int m : sizes) {
+    std::vector<long long> offs;
+    for (int c = 0; c < nc; c++)
+      if (comp_n[c] == m) offs.push_back(comp_off[c]);
+    const int nmat = (int)offs.size();
+    long long *d_offs = nullptr;
+    double *row = nullptr, *col = nullptr;
+    CK_(cudaMalloc(&d_offs, nmat * sizeof(long long)));
+    CK_(cudaMalloc(&row, (size_t)nmat * m * sizeof(double)));
+    CK_(cudaMalloc(&col, (size_t)nmat * m * sizeof(double)));
+    CK_(cudaMemcpyAsync(d_offs, offs.data(), nmat * sizeof(long long), cudaMemcpyHostToDevice, stream_));
+    const long work = (long)nmat * m * m;
+    for (int k = 0; k < m; k++) {
+      k_gj_save<<<ew_grid((long)nmat * m), kTPB, 0, stream_>>>(m, k, nmat, d_offs, d_binv_, row, col);
+      k_gj_step<<<ew_grid(work), kTPB, 0, stream_>>>(m, k, nmat, d_offs, d_binv_, row, col);
+    }
+    CK_(cudaStreamSynchronize(stream_));
+    cudaFree(d_offs);
+    cudaFree(row);
+    cudaFree(col);
   }
-  double *row = nullptr, *col = nullptr;
-  int *dpins = nullptr;
-  CK_(cudaMalloc(&row, n * sizeof(double)));
-  CK_(cudaMalloc(&col, n * sizeof(double)));
-  CK_(cudaMemcpyAsync(d_binv_, A.data(), (size_t)n * n * sizeof(double), cudaMemcpyHostToDevice, stream_));
-  const long nn = (long)n * n;
-  for (int k = 0; k < n; k++) {
-    k_gj_save<<<(n + kTPB - 1) / kTPB, kTPB, 0, stream_>>>(n, k, d_binv_, row, col);
-    k_gj_step<<<ew_grid(nn), kTPB, 0, stream_>>>(n, k, d_binv_, row, col);
-  }
-  if (!pins.empty()) {
-    CK_(cudaMalloc(&dpins, pins.size() * sizeof(int)));
-    CK_(cudaMemcpyAsync(dpins, pins.data(), pins.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
-    k_zero_cols<<<ew_grid((long)n * pins.size()), kTPB, 0, stream_>>>(n, d_binv_, dpins, (int)pins.size());
+  for (int r0 : pins) {
+    const int c = rcomp[r0];
+    k_zero_col<<<(comp_n[c] + kTPB - 1) / kTPB, kTPB, 0, stream_>>>(comp_off[c], comp_n[c], r0 - comp_row0[c], d_binv_);
   }
   CK_(cudaStreamSynchronize(stream_));
-  cudaFree(row);
-  cudaFree(col);
-  if (dpins) cudaFree(dpins);
+  bot_ = BottomDev{d_binv_, d_bot_blocks_, d_comp_row0_, d_comp_n_, d_comp_off_, d_tile_comp_, d_tile_row0_,
+                   (int)tile_comp.size(), ncell_, max_n};
   n_pins_ = (int)pins.size();
+  n_bot_comp_ = nc;
   bottom_ready_ = true;
+}
+
+void MacGpu::bottom_free() {
+  for (void *p : {(void *)d_binv_, (void *)d_bot_blocks_, (void *)d_comp_row0_, (void *)d_comp_n_,
+                  (void *)d_comp_off_, (void *)d_tile_comp_, (void *)d_tile_row0_})
+    if (p) cudaFree(p);
+  d_binv_ = nullptr;
+  d_bot_blocks_ = d_comp_row0_ = d_comp_n_ = d_tile_comp_ = d_tile_row0_ = nullptr;
+  d_comp_off_ = nullptr;
+  bot_ = BottomDev{};
 }
 
 // one V-cycle with zero initial guess in precision T; the input residual
@@ -843,12 +943,11 @@ template void MacGpu::vc_out_launch<double>(const BlockList &, double *, double 
 // dense bottom solve of the level-1 problem: corr = Binv * resid
 template <typename T>
 void MacGpu::bottom_launch(T *resid, T *corr) {
-  const int rows_per_cta = kTPB / 32;
-  const size_t smem = (size_t)n_bot_ * sizeof(double);
+  if (bot_.ntiles == 0) return;
+  const size_t smem = (size_t)bot_.max_n * sizeof(double);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k_bottom_gemv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  launch_k(prm_.pdl != 0, k_bottom_gemv<T>, (n_bot_ + rows_per_cta - 1) / rows_per_cta, kTPB, smem, stream_, n_bot_,
-           (const double *)d_binv_, (const int *)towers_[1].all.blocks, ncell_, (const T *)resid, corr,
+  launch_k(prm_.pdl != 0, k_bottom_gemv<T>, bot_.ntiles, kTPB, smem, stream_, bot_, (const T *)resid, corr,
            (const FState *)d_st_);
 }
 template void MacGpu::bottom_launch<float>(float *, float *);

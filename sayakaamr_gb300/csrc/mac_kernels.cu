@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
         unew = fma_t(rhs[cb + ci], (T)L.sa[fo], off * (T)L.ia[fo]);
       } else {
         const T vfv = c.vf[cb + ci];
-        if (vfv > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+        if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
       }
       tile[ci] = unew;
     }

@@ -341,7 +341,7 @@ MacGpu::~MacGpu() {
   learned_free();
   fr(d_opS_);
   fr(d_cnt_);
-  fr(d_binv_);
+  bottom_free();
   fr(d_phases_);
   fr(d_bar_);
   if (h_st_) cudaFreeHost(h_st_);

@@ -261,7 +261,12 @@ class MacGpu {
   double *face_scratch(int k);
   unsigned *d_cnt_ = nullptr;
   double *d_binv_ = nullptr;
-  int n_bot_ = 0, n_pins_ = 0;
+  int *d_bot_blocks_ = nullptr, *d_comp_row0_ = nullptr, *d_comp_n_ = nullptr, *d_tile_comp_ = nullptr,
+      *d_tile_row0_ = nullptr;
+  long long *d_comp_off_ = nullptr;
+  BottomDev bot_{};
+  int n_bot_ = 0, n_pins_ = 0, n_bot_comp_ = 0;
+  void bottom_free();
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graph_exec_ = nullptr;
   int graph_prec_ = -1, graph_npost_ = -1;

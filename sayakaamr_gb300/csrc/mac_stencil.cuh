@@ -311,7 +311,7 @@ __device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c
   }
   const T vfv = c.vf[cb + ci];
   T unew = 0;
-  if (vfv > 0) unew = fast_div(fma_t(ld<CG>(&rhs[cb + ci]) * dv, vfv, off), diag);
+  if (vfv > 0 && diag > 0) unew = fast_div(fma_t(ld<CG>(&rhs[cb + ci]) * dv, vfv, off), diag);
   phi[cb + ci] = unew;
 }
 
@@ -386,6 +386,29 @@ __device__ __forceinline__ void prolong_cell(const Topo &t, const Coef<T> &c, in
   const T v = ld<CG>(&phi[(long)P * ncell + encode(pc, nb)]);
   const long q = (long)b * ncell + ci;
   phi[q] = c.vf[q] > 0 ? v : (T)0;
+}
+
+// rows [row0, row0 + 8) of one component of the bottom solve:
+// corr = Binv_c * resid_c, one warp per row; rv: shared memory for the
+// component's residual (max_n doubles); every thread of the CTA calls it
+template <typename T, bool CG = false>
+__device__ __forceinline__ void bottom_tile(const BottomDev &bd, int tile, const T *resid, T *corr, double *rv) {
+  const int c = bd.tile_comp[tile], r0 = bd.comp_row0[c], m = bd.comp_n[c], nc = bd.ncell;
+  for (int j = threadIdx.x; j < m; j += blockDim.x) {
+    const int g = r0 + j;
+    rv[j] = (double)ld<CG>(&resid[(long)bd.blocks[g / nc] * nc + g % nc]);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, row = bd.tile_row0[tile] + (threadIdx.x >> 5);
+  if ((threadIdx.x >> 5) < kBottomTileRows && row < m) {
+    const double *a = bd.binv + bd.comp_off[c] + (long long)row * m;
+    double s = 0.0;
+    for (int j = lane; j < m; j += 32) s += a[j] * rv[j];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const int g = r0 + row;
+    if (lane == 0) corr[(long)bd.blocks[g / nc] * nc + g % nc] = (T)s;
+  }
+  __syncthreads();
 }
 
 }  // namespace stencil

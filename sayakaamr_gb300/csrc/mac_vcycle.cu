@@ -27,11 +27,6 @@ namespace {
 
 constexpr int kVT = 256;
 
-__device__ __forceinline__ double wsum_v(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
 // sense-by-generation grid barrier (bounded spin); returns false when the
 // kernel must stop (timeout here or in another CTA)
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
@@ -70,8 +65,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
 
 template <typename T, int ND>
 __global__ void __launch_bounds__(kVT) k_vcycle_coop(Topo t, Coef<T> c, const VPhase *__restrict__ phases,
-                                                     int nphases, T *resid, T *corr, double *out, int n_bot,
-                                                     const double *__restrict__ binv, const int *__restrict__ bblocks,
+                                                     int nphases, T *resid, T *corr, double *out, BottomDev bd,
                                                      const FState *st, unsigned *bar, int *err) {
   using namespace stencil;
   if (st->done) return;
@@ -104,21 +98,8 @@ __global__ void __launch_bounds__(kVT) k_vcycle_coop(Topo t, Coef<T> c, const VP
         prolong_cell<T, ND, true>(t, c, P.blocks[p], (int)(it - (long)p * ncell), corr);
       }
     } else if (P.op == kPhaseBottom) {
-      // dense FP64 solve of the level-1 problem, one warp per row
-      const int wpb = blockDim.x >> 5;
-      if ((long)blockIdx.x * wpb < n_bot) {
-        for (int j = threadIdx.x; j < n_bot; j += blockDim.x)
-          rv[j] = (double)__ldcg(&resid[(long)bblocks[j / ncell] * ncell + j % ncell]);
-        __syncthreads();
-        const int lane = threadIdx.x & 31;
-        for (int row = blockIdx.x * wpb + (threadIdx.x >> 5); row < n_bot; row += gridDim.x * wpb) {
-          const double *a = binv + (long)row * n_bot;
-          double s = 0.0;
-          for (int j = lane; j < n_bot; j += 32) s += a[j] * rv[j];
-          s = wsum_v(s);
-          if (lane == 0) corr[(long)bblocks[row / ncell] * ncell + row % ncell] = (T)s;
-        }
-      }
+      // dense FP64 solve of the level-1 components, tile by tile
+      for (int tile = blockIdx.x; tile < bd.ntiles; tile += gridDim.x) bottom_tile<T, true>(bd, tile, resid, corr, rv);
     } else if (out) {  // kPhaseOut: phat (FP64) = 0 + corr over the tower
       const long total = (long)P.n * ncell;
       for (long it = tid; it < total; it += nthr) {
@@ -181,7 +162,7 @@ void MacGpu::build_vcycle_program() {
 
 template <typename T>
 void MacGpu::vcycle_coop(T *resid, T *corr, const Coef<T> &c, double *out) {
-  const size_t smem = (size_t)n_bot_ * sizeof(double);
+  const size_t smem = (size_t)std::max(bot_.max_n, 1) * sizeof(double);
   const void *fn = tt_.ndim == 2 ? (const void *)k_vcycle_coop<T, 2> : (const void *)k_vcycle_coop<T, 3>;
   if (coop_grid_ <= 0) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -206,19 +187,16 @@ void MacGpu::vcycle_coop(T *resid, T *corr, const Coef<T> &c, double *out) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const double *binv = d_binv_;
-  const int *bb = towers_[1].all.blocks;
+  const BottomDev bd = bot_;
   const VPhase *ph = d_phases_;
-  const int np = n_phases_, nbot = n_bot_;
+  const int np = n_phases_;
   const FState *st = d_st_;
   unsigned *bar = d_bar_;
   cudaError_t e;
   if (tt_.ndim == 2)
-    e = cudaLaunchKernelEx(&cfg, k_vcycle_coop<T, 2>, topo_, c, ph, np, resid, corr, out, nbot, binv, bb, st, bar,
-                           err);
+    e = cudaLaunchKernelEx(&cfg, k_vcycle_coop<T, 2>, topo_, c, ph, np, resid, corr, out, bd, st, bar, err);
   else
-    e = cudaLaunchKernelEx(&cfg, k_vcycle_coop<T, 3>, topo_, c, ph, np, resid, corr, out, nbot, binv, bb, st, bar,
-                           err);
+    e = cudaLaunchKernelEx(&cfg, k_vcycle_coop<T, 3>, topo_, c, ph, np, resid, corr, out, bd, st, bar, err);
   if (e != cudaSuccess) fail(std::string("cooperative V-cycle launch: ") + cudaGetErrorString(e));
 }
 

@@ -113,9 +113,29 @@ def gaussian_rhs(rng, pts, ndim, n_g=8, sigma=0.05):
     return f
 
 
+def _close_isolated(vol, area, n, nb, nd):
+    """a cell with fluid volume but every face closed has no equation (zero
+    operator row, a zero divisor in the smoother): make it solid"""
+    shp = (n,) + (nb,) * nd
+    v = vol.reshape(shp).copy()
+    closed = np.ones(shp, dtype=bool)
+    for d in range(nd):
+        fs = [nb] * nd
+        fs[nd - 1 - d] += 1  # face arrays are [block][k][j][i], dimension d has nb+1 entries
+        a = area[d].reshape((n,) + tuple(fs))
+        lo = [slice(None)] * (nd + 1)
+        hi = [slice(None)] * (nd + 1)
+        lo[nd - d] = slice(0, nb)
+        hi[nd - d] = slice(1, nb + 1)
+        closed &= (a[tuple(lo)] == 0) & (a[tuple(hi)] == 0)
+    v[closed] = 0.0
+    return v.reshape(-1)
+
+
 def _finish(name, t, tb, vol, area, bface, f, neumann, params, dirichlet_faces=()):
     n, nd = tb["num_blocks"], tb["ndim"]
     ncell = tb["nb"] ** nd
+    vol = _close_isolated(np.asarray(vol).reshape(-1), [np.asarray(a).reshape(-1) for a in area], n, tb["nb"], nd)
     leaf = tb["node_type"] == 1
     lens = tb["block_len"].reshape(n, 3)[:, :nd] / tb["nb"]
     dv = np.prod(lens, axis=1)
@@ -242,7 +262,107 @@ def config3(seed=3, nb=16, max_level=5):
     return _finish("config3", t, tb, vol, area, bface, f, True, dict(tol_rel=1e-8), dirichlet_faces=(5,))
 
 
-CONFIGS = {"config1": config1, "config2": config2, "config3": config3}
+def _ellipse_sdf(c, a, b, th):
+    ct, st = math.cos(th), math.sin(th)
+
+    def sdf(p):
+        x = p[..., 0] - c[0]
+        y = p[..., 1] - c[1]
+        u = (x * ct + y * st) / a
+        v = (-x * st + y * ct) / b
+        return (np.sqrt(u * u + v * v) - 1.0) * min(a, b)
+    return sdf
+
+
+def batch_problem(rng, name, nb=16, max_leaves=1024):
+    """One problem of the batch workload: unit square, 8x8 blocks at level 4,
+    refined (up to 7 levels) around 1-4 seeded ellipse IB solids (fractional
+    fractions) and a seeded density ellipse (rho ratio 10-1000, smoothed over
+    2 cells); Neumann walls with p = 0 on the top wall; 8-Gaussian zero-mean
+    right-hand side scaled to |rhs|_inf = 1 over the fluid cells."""
+    solids = []
+    for _ in range(int(rng.integers(1, 5))):
+        a = rng.uniform(0.04, 0.10)
+        solids.append(_ellipse_sdf(rng.uniform(0.2, 0.8, 2), a, a * rng.uniform(0.4, 1.0), rng.uniform(0, math.pi)))
+    da = rng.uniform(0.12, 0.22)
+    dens = _ellipse_sdf(rng.uniform(0.3, 0.7, 2), da, da * rng.uniform(0.5, 1.0), rng.uniform(0, math.pi))
+    ratio = 10.0 ** rng.uniform(1.0, 3.0)
+    max_level = int(rng.integers(5, 8))
+
+    def need(lo, hi, level):
+        m = _straddle(dens, lo, hi, 1.0)
+        for sd in solids:
+            m = m | _straddle(sd, lo, hi, 1.0)
+        return m
+
+    while True:
+        t = refine_tree(2, nb, (1, 1, 1), (0, 0, 0), (1, 1, 0), 4, max_level, need, capacity=8000)
+        tb = t.tables()
+        if (tb["node_type"] == 1).sum() <= max_leaves or max_level <= 5:
+            break
+        max_level -= 1
+    lo, dx = _block_geom(tb)
+    pc = cell_centres(tb)
+    h = dx[:, 0][:, None]
+
+    def frac(p):
+        v = np.ones(p.shape[:-1])
+        for sd in solids:
+            v = np.minimum(v, np.clip(sd(p) / h + 0.5, 0.0, 1.0))
+        return v
+    vol = frac(pc)
+    area, bface = [], []
+    for fd in range(2):
+        pf = face_centres(tb, fd)
+        area.append(frac(pf))
+        bface.append(1.0 / (1.0 + (ratio - 1.0) * _smooth_heaviside(dens(pf), 2.0 * h)))
+    f = gaussian_rhs(rng, pc, 2)
+    prob = _finish(name, t, tb, vol, area, bface, f, True, dict(tol_rel=1e-8), dirichlet_faces=(3,))
+    fluid = prob.vol > 0
+    m = np.abs(prob.rhs[fluid]).max()
+    prob.rhs = prob.rhs / (m if m > 0 else 1.0)
+    return prob
+
+
+def forest(problems, name):
+    """Independent problems as one forest: their block tables concatenated
+    with block-id offsets (neighbour, child and parent links stay inside each
+    problem; physical-boundary codes are kept), fields concatenated.  One
+    solve of the forest is one block-diagonal system: with every right-hand
+    side scaled to |r0|_inf = 1, the joint criterion |r|_inf < 1e-8 holds for
+    every problem."""
+    tbs = [p.tables for p in problems]
+    off = np.cumsum([0] + [t["num_blocks"] for t in tbs[:-1]])
+    cat = {}
+    for key in ("level", "which_child", "node_type", "block_len", "block_lo", "block_hi", "block_center"):
+        cat[key] = np.concatenate([t[key] for t in tbs])
+    for key in ("neighbor", "child", "parent"):
+        cat[key] = np.concatenate([np.where(t[key] >= 0, t[key] + o, t[key]) for t, o in zip(tbs, off)]).astype(
+            np.int32)
+    cat["node_type2"] = np.concatenate([t["node_type2"] for t in tbs])
+    t0 = tbs[0]
+    cat.update(ndim=t0["ndim"], nb=t0["nb"], num_blocks=int(sum(t["num_blocks"] for t in tbs)),
+               min_level=int(min(t["min_level"] for t in tbs)), max_level=int(max(t["max_level"] for t in tbs)))
+    nd = t0["ndim"]
+    prob = Problem(name, None, cat, np.concatenate([p.bc for p in problems]),
+                   np.concatenate([p.vol for p in problems]),
+                   [np.concatenate([p.area[d] for p in problems]) for d in range(nd)],
+                   [np.concatenate([p.bface[d] for p in problems]) for d in range(nd)],
+                   np.concatenate([p.rhs for p in problems]), dict(tol_rel=1e-8))
+    prob.block_offsets = off
+    prob.parts = problems
+    return prob
+
+
+def config4(seed=4, n_problems=256, nb=16):
+    """Batch of independent 2D problems of uneven size (64-1024 leaf blocks
+    of 16x16 cells), each with 1-4 seeded ellipse IB solids and rho ratio
+    10-1000, solved together as one forest."""
+    rng = np.random.default_rng(seed)
+    return forest([batch_problem(rng, "config4_%d" % k, nb) for k in range(n_problems)], "config4")
+
+
+CONFIGS = {"config1": config1, "config2": config2, "config3": config3, "config4": config4}
 
 
 def make_solver(prob, **params):

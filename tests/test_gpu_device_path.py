@@ -125,3 +125,17 @@ def test_smoother_variants_are_bit_identical(name, precision):
     for k in range(1, len(out)):
         assert out[0][0] == out[k][0], k
         assert np.array_equal(out[0][1], out[k][1]), k
+
+
+def test_nan_in_the_rhs_ends_as_breakdown_not_convergence():
+    """a NaN anywhere (here planted in the right-hand side) reaches the max
+    norms of the device solve and ends it as a breakdown"""
+    g, t, tb, S = setup_solver("t2s")
+    rhs = np.array(g["sv_rhs"], dtype=np.float64)
+    leaf = np.nonzero(tb["node_type"] == 1)[0]
+    rhs.reshape(tb["num_blocks"], -1)[leaf[0], 3] = np.nan
+    S.set_rhs_compact(rhs)
+    S.set_zero_sol()
+    S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=50, precision=1, bottom=1)
+    info = S.cg_solve()
+    assert info["status"] == 1, info
