@@ -44,6 +44,8 @@ WORKLOADS = {
     "config3": "sphere r=0.2 refinement band, IB sphere mask, B ratio 100 across a blob, p=0 top wall",
     "config4": "256 independent problems (64-1024 leaf blocks, 1-4 ellipse IB solids, rho ratio 10-1000) "
                "solved as one forest",
+    "config5": "90-degree elbow pipe (tube 0.1, bend 0.3) with a sphere inside as IB, p=0 outlet, first solve "
+               "of the regrid sequence",
 }
 L2_FLUSH_BYTES = 256 << 20
 

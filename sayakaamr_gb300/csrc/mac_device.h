@@ -65,6 +65,10 @@ struct FState {
   // best residual, best residual
   int nn_on, nn_off, nn_since, pad_;
   double nn_best;
+  // verified convergence: the recursive residual passed and the true
+  // residual is being checked; the next iteration restarts from p = r;
+  // restarts so far
+  int verify, restart, restarts, pad2_;
 };
 
 // The dense FP64 bottom solve: one inverse per connected component of the

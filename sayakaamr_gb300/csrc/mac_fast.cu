@@ -138,6 +138,7 @@ struct EpiInit {  // after r0 = b - A x0: |r0|, rho = r0.r0
 struct EpiAlpha {  // rhat.v
   FState *st;
   __device__ void operator()(const double *v) const {
+    st->restart = 0;  // the p-update of this iteration has read it
     if (v[0] == 0) {
       st->stat = 1;
       st->done = 1;
@@ -156,7 +157,7 @@ struct EpiHalf {  // |s|
       return;
     }
     if (v[0] < st->rnorm0 * st->tol_rel || v[0] < st->tol_abs) {
-      st->conv = 1;
+      st->verify = 1;  // x is final for this pass: check its true residual
       st->done = 1;
     }
   }
@@ -172,6 +173,38 @@ struct EpiOmega {  // t.s, t.t
     st->omega = v[0] / v[1];
   }
 };
+// The recursively updated residual of BiCGSTAB drifts from b - A x by about
+// eps |A| |x| per iteration; with small volume fractions (large 1/(dv vf))
+// the gap reaches the tolerance.  A converged pass is therefore verified with
+// the true residual r = b - A x0 (x folded into x0); if that misses the
+// tolerance the solve restarts from x0 with r^ = p = r (at most kMaxRestarts
+// times, then it ends as not converged).
+constexpr int kMaxRestarts = 5;
+struct EpiVerify {  // |b - A x0|, r.r
+  FState *st;
+  __device__ void operator()(const double *v) const {
+    st->verify = 0;
+    st->rnorm = v[0];
+    if (v[0] != v[0]) {
+      st->stat = 1;
+      return;
+    }
+    if (v[0] < st->rnorm0 * st->tol_rel + st->tol_abs) {
+      st->conv = 1;
+      return;
+    }
+    if (st->restarts >= kMaxRestarts) return;  // done, not converged
+    st->restarts += 1;
+    st->rho = v[1];
+    if (v[1] == 0) {
+      st->stat = 1;
+      return;
+    }
+    st->restart = 1;
+    st->done = 0;
+  }
+};
+
 struct EpiEnd {  // |r|, rhat.r of the next iteration
   FState *st;
   __device__ void operator()(const double *v) const {
@@ -182,7 +215,7 @@ struct EpiEnd {  // |r|, rhat.r of the next iteration
       return;
     }
     if (v[0] < st->rnorm0 * st->tol_rel + st->tol_abs) {
-      st->conv = 1;
+      st->verify = 1;  // check the true residual before accepting
       st->done = 1;
       return;
     }
@@ -242,7 +275,7 @@ __global__ void k_pupdate(BlockList L, int ncell, const FState *st, const double
                           const double *vf, T *resid) {
   pdl_enter();
   if (st->done) return;
-  const bool first = st->iter == 1;
+  const bool first = st->iter == 1 || st->restart;
   const double beta = st->beta, om = st->omega;
   const int total = L.n * ncell;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
@@ -449,15 +482,18 @@ __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &
 
 // operator fused with its dot products:
 // MODE 0: y = A x, rhat.y (EpiAlpha) ; MODE 1: y = A x, y.w, y.y (EpiOmega) ;
-// MODE 2: y = w - A x (0 where vf = 0), |y|, y.y (EpiInit)
+// MODE 2: y = w - A x (0 where vf = 0), |y|, y.y (EpiInit) ;
+// MODE 3: only while verifying: y = y2 = w - A x, |y|, y.y (EpiVerify)
 template <int ND, int MODE, typename TX>
 __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockList L, const TX *__restrict__ x,
                                                double *__restrict__ y, const double *__restrict__ w,
                                                const double *__restrict__ P, const double *__restrict__ S,
-                                               FState *st, double *partials, unsigned *counter) {
+                                               FState *st, double *partials, unsigned *counter,
+                                               double *__restrict__ y2 = nullptr) {
   using namespace stencil;
   pdl_enter();
-  if (MODE != 2 && st->done) return;
+  if (MODE == 3 && !st->verify) return;
+  if (MODE < 2 && st->done) return;
   double acc[2] = {0.0, 0.0};
   const int total = L.n * t.ncell;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
@@ -469,14 +505,15 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
     const double off = op_offdiag<ND, TX>(t, c, b, L.ftypes[p], ijk, ci, x);
     const double sc = S[q];
     double yv = __fma_rn((double)x[q], P[q], -off * sc);
-    if (MODE == 2) yv = sc != 0.0 ? w[q] - yv : 0.0;
+    if (MODE >= 2) yv = sc != 0.0 ? w[q] - yv : 0.0;
     y[q] = yv;
+    if (MODE == 3) y2[q] = yv;
     if (MODE == 0) acc[0] = __fma_rn(w[q], yv, acc[0]);
     if (MODE == 1) {
       acc[0] = __fma_rn(yv, w[q], acc[0]);
       acc[1] = __fma_rn(yv, yv, acc[1]);
     }
-    if (MODE == 2) {
+    if (MODE >= 2) {
       acc[0] = nmax(acc[0], fabs(yv));
       acc[1] = __fma_rn(yv, yv, acc[1]);
     }
@@ -484,6 +521,20 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
   if (MODE == 0) grid_reduce<2>(acc, 0u, partials, counter, EpiAlpha{st});
   if (MODE == 1) grid_reduce<2>(acc, 0u, partials, counter, EpiOmega{st});
   if (MODE == 2) grid_reduce<2>(acc, 1u, partials, counter, EpiInit{st});
+  if (MODE == 3) grid_reduce<2>(acc, 1u, partials, counter, EpiVerify{st});
+}
+
+// while verifying: x0 += x, x = 0 (the pass's solution folded into x0)
+__global__ void __launch_bounds__(kTPB) k_verify_fold(BlockList L, int ncell, const FState *st, double *x0,
+                                                    double *x) {
+  pdl_enter();
+  if (!st->verify) return;
+  const int total = L.n * ncell;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+    const long q = cell_of(L, ncell, it);
+    x0[q] = x0[q] + x[q];
+    x[q] = 0.0;
+  }
 }
 
 // dense bottom solve: corr(level 1) = Binv * resid(level 1), one CTA per
@@ -993,24 +1044,35 @@ void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
   precondition<T>(L, resid, corr, c, out_p);
   if (tt_.ndim == 2)
     launch_k(pdl, k_op_red<2, 0, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, PH, V,
-             (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
+             (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_, (double *)nullptr);
   else
     launch_k(pdl, k_op_red<3, 0, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, PH, V,
-             (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
+             (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_, (double *)nullptr);
   launch_k(pdl, k_supdate<T, TO>, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, (const double *)R, (const double *)V,
            S, X, PH, (const double *)d_vf_, resid, d_part_, d_cnt_);
   precondition<T>(L, resid, corr, c, out_s);
   if (tt_.ndim == 2)
     launch_k(pdl, k_op_red<2, 1, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, SH, Tt,
-             (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
+             (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_, (double *)nullptr);
   else
     launch_k(pdl, k_op_red<3, 1, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, SH, Tt,
-             (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_);
+             (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_, (double *)nullptr);
   launch_k(pdl, k_rupdate<TO>, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, X, SH, R,
            (const double *)S, (const double *)Tt, (const double *)RHAT, d_part_, d_cnt_);
+  // verified convergence (both kernels return at once unless a pass converged)
+  double *X0 = vec_[kX0];
+  launch_k(pdl, k_verify_fold, ew_grid(w), kTPB, 0, stream_, TL, ncell_, (const FState *)d_st_, X0, X);
+  if (tt_.ndim == 2)
+    launch_k(pdl, k_op_red<2, 3, double>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)X0, R,
+             (const double *)vec_[kRHS], (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_,
+             RHAT);
+  else
+    launch_k(pdl, k_op_red<3, 3, double>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)X0, R,
+             (const double *)vec_[kRHS], (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_,
+             RHAT);
 }
 
-void MacGpu::capture_loop(int precision) {
+void MacGpu::drop_graph() {
   if (graph_exec_) {
     cudaGraphExecDestroy(graph_exec_);
     graph_exec_ = nullptr;
@@ -1019,6 +1081,10 @@ void MacGpu::capture_loop(int precision) {
     cudaGraphDestroy(graph_);
     graph_ = nullptr;
   }
+}
+
+void MacGpu::capture_loop(int precision) {
+  drop_graph();
   CK_(cudaGraphCreate(&graph_, 0));
   cudaGraphConditionalHandle h;
   CK_(cudaGraphConditionalHandleCreate(&h, graph_, 1, cudaGraphCondAssignDefault));
@@ -1071,7 +1137,9 @@ int MacGpu::cg_solve_device(SolveInfo *info) {
 // no host synchronisation in graph mode (the caller times it with events)
 int MacGpu::cg_solve_enqueue() {
   ensure_fast_buffers();
-  if (!err_.empty() || !bottom_ready_) return -1;
+  // coefficients changed since sayaka_mac_prepare: the fast-path data and the
+  // graph must be rebuilt first
+  if (!err_.empty() || !bottom_ready_ || coef_version_ != fast_coef_version_) return -1;
   if (prm_.graph && (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
                      graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl ||
                      graph_cc_ != prm_.cluster_cells ||
@@ -1143,6 +1211,12 @@ int MacGpu::prepare_device() {
   ensure_fast_buffers();
   if (!err_.empty()) return -1;
   if (coef_version_ != fast_coef_version_) {
+    // The captured graph holds kernel arguments by value, among them the
+    // bottom solve's device arrays, which build_bottom frees and allocates
+    // again: drop the graph (after the stream's work is done) so that the
+    // next solve captures it afresh with the new arguments.
+    CKR_(cudaStreamSynchronize(stream_), -1);
+    drop_graph();
     refresh_fp32();
     build_op_factors();
     build_smooth_factors();

@@ -267,6 +267,7 @@ class MacGpu {
   BottomDev bot_{};
   int n_bot_ = 0, n_pins_ = 0, n_bot_comp_ = 0;
   void bottom_free();
+  void drop_graph();
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graph_exec_ = nullptr;
   int graph_prec_ = -1, graph_npost_ = -1;

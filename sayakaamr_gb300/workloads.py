@@ -132,10 +132,19 @@ def _close_isolated(vol, area, n, nb, nd):
     return v.reshape(-1)
 
 
+# cut cells and faces below this fraction are solid: a sliver with volume
+# fraction 1e-5 scales its operator row by 1e5 and makes the residual there
+# ill-conditioned (rounding differences amplified by 1/(dv vf))
+MIN_FRACTION = 1e-3
+
+
 def _finish(name, t, tb, vol, area, bface, f, neumann, params, dirichlet_faces=()):
     n, nd = tb["num_blocks"], tb["ndim"]
     ncell = tb["nb"] ** nd
-    vol = _close_isolated(np.asarray(vol).reshape(-1), [np.asarray(a).reshape(-1) for a in area], n, tb["nb"], nd)
+    vol = np.asarray(vol, dtype=np.float64).reshape(-1)
+    vol = np.where(vol < MIN_FRACTION, 0.0, vol)
+    area = [np.where(np.asarray(a) < MIN_FRACTION, 0.0, np.asarray(a, dtype=np.float64)) for a in area]
+    vol = _close_isolated(vol, [a.reshape(-1) for a in area], n, tb["nb"], nd)
     leaf = tb["node_type"] == 1
     lens = tb["block_len"].reshape(n, 3)[:, :nd] / tb["nb"]
     dv = np.prod(lens, axis=1)
@@ -362,7 +371,122 @@ def config4(seed=4, n_problems=256, nb=16):
     return forest([batch_problem(rng, "config4_%d" % k, nb) for k in range(n_problems)], "config4")
 
 
-CONFIGS = {"config1": config1, "config2": config2, "config3": config3, "config4": config4}
+# ---- elbow pipe with a moving sphere (3D, 8^3 blocks, regrid every few solves)
+ELBOW_C = np.array([0.15, 0.15, 0.5])
+ELBOW_R, ELBOW_TUBE, SPHERE_R = 0.3, 0.1, 0.04
+
+
+def _seg_dist(p, a, b):
+    ab = b - a
+    t = np.clip(np.sum((p - a) * ab, axis=-1) / np.dot(ab, ab), 0.0, 1.0)
+    return np.linalg.norm(p - (a + t[..., None] * ab), axis=-1)
+
+
+def elbow_dist(p):
+    """distance to the centreline of a 90-degree elbow in the plane z = 0.5:
+    inlet leg along y from y = 0, quarter arc of radius 0.3 about (0.15,
+    0.15), outlet leg along x to x = 0"""
+    c, R = ELBOW_C, ELBOW_R
+    x, y, z = p[..., 0] - c[0], p[..., 1] - c[1], p[..., 2] - c[2]
+    ang = np.arctan2(y, x)
+    d = np.where((ang >= 0) & (ang <= 0.5 * math.pi), np.sqrt((np.hypot(x, y) - R) ** 2 + z * z), np.inf)
+    d = np.minimum(d, _seg_dist(p, np.array([c[0] + R, 0.0, c[2]]), np.array([c[0] + R, c[1], c[2]])))
+    return np.minimum(d, _seg_dist(p, np.array([c[0], c[1] + R, c[2]]), np.array([0.0, c[1] + R, c[2]])))
+
+
+def elbow_point(s):
+    """centreline point at arc length fraction s in [0, 1] from the inlet"""
+    c, R = ELBOW_C, ELBOW_R
+    l1, la, l2 = c[1], 0.5 * math.pi * R, c[0]
+    t = s * (l1 + la + l2)
+    if t <= l1:
+        return np.array([c[0] + R, t, c[2]])
+    if t <= l1 + la:
+        a = (t - l1) / R
+        return np.array([c[0] + R * math.cos(a), c[1] + R * math.sin(a), c[2]])
+    return np.array([c[0] - (t - l1 - la), c[1] + R, c[2]])
+
+
+def elbow_target_level(blo, bhi, sc, max_level=7):
+    """refinement target per block: max_level within 0.04 of the tube wall's
+    outside (the tube and a band around it) and around the moving sphere,
+    one level less up to 0.2 outside the tube, the far solid at level 2
+    (about 30k blocks of 8^3 cells at 7 levels)"""
+    centre = 0.5 * (blo + bhi)
+    half = 0.5 * np.max(bhi - blo, axis=1) * math.sqrt(3.0)
+    d = elbow_dist(centre) - half  # lower bound of the centreline distance over the block
+    tgt = np.full(blo.shape[0], 2)
+    tgt = np.where(d < ELBOW_TUBE + 0.2, max_level - 1, tgt)
+    tgt = np.where(d < ELBOW_TUBE + 0.04, max_level, tgt)
+    sph = lambda p: np.linalg.norm(p - sc, axis=-1) - SPHERE_R  # noqa: E731
+    return np.where(_straddle(sph, blo, bhi, 1.0), max_level, tgt)
+
+
+def elbow_tree(sc, nb=8, max_level=7):
+    def need(lo, hi, level):
+        return elbow_target_level(lo, hi, sc, max_level) > level
+    return refine_tree(3, nb, (1, 1, 1), (0, 0, 0), (1, 1, 1), 2, max_level, need, capacity=400000)
+
+
+def elbow_regrid(t, sc, max_level=7):
+    """refine / coarsen the leaves toward the new targets (max_level passes,
+    as the reference's regrid driver does)"""
+    for _ in range(max_level):
+        tb = t.tables()
+        n = tb["num_blocks"]
+        blo = tb["block_lo"].reshape(n, 3)
+        bhi = tb["block_hi"].reshape(n, 3)
+        leaf = tb["node_type"] == 1
+        tgt = elbow_target_level(blo, bhi, sc, max_level)
+        ref = (leaf & (tb["level"] < tgt)).astype(np.int32)
+        crs = (leaf & (tb["level"] > tgt)).astype(np.int32)
+        if not ref.any() and not crs.any():
+            break
+        t.set_refine_flags(ref)
+        t.set_coarsen_flags(crs)
+        t.regrid()
+    return t
+
+
+def elbow_problem(t, sc, seed, name="config5"):
+    """fractions, B and right-hand side of the elbow on tree t with the sphere
+    at sc: fluid inside the tube and outside the sphere (fractional
+    fractions), B = 1, p = 0 on the outlet face x = 0, Neumann elsewhere"""
+    tb = t.tables()
+    rng = np.random.default_rng(seed)
+    lo, dx = _block_geom(tb)
+    h = dx[:, 0][:, None]
+    phi = lambda p: np.minimum(ELBOW_TUBE - elbow_dist(p), np.linalg.norm(p - sc, axis=-1) - SPHERE_R)  # noqa
+    vol = np.clip(phi(cell_centres(tb)) / h + 0.5, 0.0, 1.0)
+    area, bface = [], []
+    for fd in range(3):
+        pf = face_centres(tb, fd)
+        area.append(np.clip(phi(pf) / h + 0.5, 0.0, 1.0))
+        bface.append(np.ones(pf.shape[:2]))
+    f = gaussian_rhs(rng, cell_centres(tb), 3, sigma=0.08)
+    return _finish(name, t, tb, vol, area, bface, f, False, dict(tol_rel=1e-8), dirichlet_faces=(0,))
+
+
+def config5_sequence(steps=100, regrid_every=5, max_level=7, seed=5):
+    """the elbow sequence: the sphere moves along the centreline over `steps`
+    pressure solves; the tree is regridded every `regrid_every` steps.
+    Yields (step, regridded, problem)."""
+    sc = elbow_point(0.1)
+    t = elbow_tree(sc, max_level=max_level)
+    for k in range(steps):
+        sc = elbow_point(0.1 + 0.8 * k / max(1, steps - 1))
+        regridded = k > 0 and k % regrid_every == 0
+        if regridded:
+            elbow_regrid(t, sc, max_level)
+        yield k, regridded or k == 0, elbow_problem(t, sc, seed * 1000 + k)
+
+
+def config5(max_level=7):
+    """one pressure solve of the elbow sequence (the first step)"""
+    return next(config5_sequence(steps=1, max_level=max_level))[2]
+
+
+CONFIGS = {"config1": config1, "config2": config2, "config3": config3, "config4": config4, "config5": config5}
 
 
 def make_solver(prob, **params):
