@@ -736,10 +736,10 @@ int sayaka_mac_residual_compact(sayaka_mac *h, int32_t L, const double *x, const
 }
 int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n) {
   if (!h || !h->gpu) return -1;
-  float tmp[8] = {};
-  const int v = h->gpu->tuned_smoother(precision, tmp, 8);
+  float tmp[16] = {};
+  const int v = h->gpu->tuned_smoother(precision, tmp, 16);
   if (us)
-    for (int i = 0; i < n && i < 8; i++) us[i] = tmp[i];
+    for (int i = 0; i < n && i < 16; i++) us[i] = tmp[i];
   return v;
 }
 int sayaka_mac_residual_norm_noalloc(sayaka_mac *h, int32_t L, const double *x, const double *rhs, double *r,

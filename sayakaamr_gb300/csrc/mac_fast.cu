@@ -1253,6 +1253,10 @@ int MacGpu::solve_state(SolveInfo *info) {
       return -1;
     }
   }
+  if (rbgs_bulk_error(true) > 0) {
+    fail("bulk-copy smoother: an mbarrier wait timed out");
+    return -1;
+  }
   const FState &st = *h_st_;
   info->iterations = st.trivial ? 0 : st.iter;
   info->rnorm0 = st.rnorm0;

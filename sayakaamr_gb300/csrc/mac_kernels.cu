@@ -427,6 +427,201 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
   }
 }
 
+// ---- the same sweep with the block's phi tile and face coefficients staged
+// by TMA bulk copies (cp.async.bulk, completion on an mbarrier): in the
+// compact layout both are contiguous per block.  The boundary contributions
+// are gathered while the copies are in flight; the update then reads tile
+// and coefficients from shared memory.  The wait is bounded: a CTA that
+// times out raises g_rbgs_err, waits (bounded) for its own copies and leaves
+// the block unchanged.
+__device__ int g_rbgs_err;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *mbar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(mbar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *mbar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(mbar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, unsigned long long *mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(mbar))
+      : "memory");
+}
+// bounded wait for phase `parity` of the mbarrier; true when it completed
+__device__ __forceinline__ bool mbar_wait(unsigned long long *mbar, unsigned parity, long limit) {
+  for (long i = 0; i < limit; i++) {
+    unsigned done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(mbar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (i > 64) __nanosleep(64);
+  }
+  return false;
+}
+
+template <typename T, int ND>
+__global__ void __launch_bounds__(kThreads, 2) k_rbgs_bulk(Topo t, Coef<T> c, BlockList L, int color,
+                                                          T *__restrict__ phi, const T *__restrict__ rhs,
+                                                          const int *guard) {
+  extern __shared__ __align__(128) unsigned char rbgs_bulk_smem[];
+  pdl_enter();
+  if (guard && *guard) return;
+  const int nb = t.nb, ncell = t.ncell, nhalf = ncell >> 1, nfb = t.nfb;
+  const int nface = ND == 3 ? nb * nb : nb;
+  unsigned long long *mbar = reinterpret_cast<unsigned long long *>(rbgs_bulk_smem);
+  T *tile = reinterpret_cast<T *>(rbgs_bulk_smem + 16);
+  T *tf[3];
+  for (int d = 0; d < 3; d++) tf[d] = tile + ncell + d * nfb;
+  T *hc = tile + ncell + ND * nfb;
+  T *hk = hc + 2 * ND * nface;
+  T *hv = hk + 2 * ND * nface;
+  const int p = blockIdx.x;
+  const int b = L.blocks[p];
+  const uint16_t ft = L.ftypes[p];
+  const long cb = (long)b * ncell, fb = (long)b * nfb;
+  const unsigned tile_bytes = (unsigned)(ncell * sizeof(T)), face_bytes = (unsigned)(nfb * sizeof(T));
+  if (threadIdx.x == 0) mbar_init(mbar, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(mbar, tile_bytes + ND * face_bytes);
+    bulk_copy(tile, phi + cb, tile_bytes, mbar);
+    for (int d = 0; d < ND; d++) bulk_copy(tf[d], c.tff[d] + fb, face_bytes, mbar);
+  }
+  // boundary contributions of the cells of this colour, from global memory
+  for (int e = threadIdx.x; e < 2 * ND * nface; e += blockDim.x) {
+    const int f = e / nface, m = e - f * nface;
+    const int d = f >> 1, s = f & 1;
+    int ijk[3] = {0, 0, 0};
+    ijk[d] = s ? nb - 1 : 0;
+    const int q0 = d == 0 ? 1 : 0, q1 = d == 2 ? 1 : 2;
+    ijk[q0] = m % nb;
+    if (ND == 3) ijk[q1] = m / nb;
+    if (((ijk[0] + ijk[1] + ijk[2]) & 1) != color) continue;
+    int fx;
+    if (d == 0)
+      fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+    else if (d == 1)
+      fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+    else
+      fx = encode(ijk, nb) + s * nb * nb;
+    const int ty = face_type_of(ft, f);
+    T vc = 0, vk = 0, vv = 0;
+    if (ty == 0) {
+      vc = vk = c.tff[d][fb + fx];
+      vv = same_level_ghost<T, false>(t, b, f, ijk, phi);
+    } else if (ty == 1) {
+      if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
+    } else if (ty == 2) {
+      vc = vk = cf_coef(c, t, b, d, fx, (T)1.5);
+      vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi);
+    } else {
+      vc = cf_coef(c, t, b, d, fx, (T)0.75);
+      vk = (T)1;
+      vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi);
+    }
+    hc[e] = vc;
+    hk[e] = vk;
+    hv[e] = vv;
+  }
+  const long kWait = 1l << 22;  // about 0.3 s with the back-off: never reached unless the copy engine failed
+  const bool ok = mbar_wait(mbar, 0, kWait);
+  if (__syncthreads_or(!ok)) {
+    if (threadIdx.x == 0) {
+      atomicExch(&g_rbgs_err, 1);
+      mbar_wait(mbar, 0, kWait);  // let the copies into this CTA's shared memory land before it exits
+    }
+    return;
+  }
+  const T dv = geom(c, b, 6);
+  for (int h = threadIdx.x; h < nhalf; h += blockDim.x) {
+    int ijk[3];
+    color_cell_fast<ND>(h, t, color, ijk);
+    const int ci = t.lnb >= 0 ? ijk[0] + ((ijk[1] + (ijk[2] << t.lnb)) << t.lnb) : encode(ijk, nb);
+    T diag = c.alpha * dv;
+    T off = 0;
+#pragma unroll
+    for (int f = 0; f < 2 * ND; f++) {
+      const int d = f >> 1, s = f & 1;
+      const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+      if (!bnd) {
+        int fx;
+        if (d == 0)
+          fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+        else if (d == 1)
+          fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+        else
+          fx = ci + s * nb * nb;
+        const T coef = tf[d][fx];
+        const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+        diag += coef;
+        off = fma_t(coef, tile[ci + (s ? stride : -stride)], off);
+      } else {
+        const int q0 = d == 0 ? 1 : 0, q1 = d == 2 ? 1 : 2;
+        const int m = ijk[q0] + (ND == 3 ? nb * ijk[q1] : 0);
+        const int e = f * nface + m;
+        diag += hc[e];
+        off = fma_t(hk[e], hv[e], off);
+      }
+    }
+    T unew = 0;
+    if (sizeof(T) == 8 && L.sa) {
+      const long fo = (long)p * ncell + ci;
+      unew = fma_t(rhs[cb + ci], (T)L.sa[fo], off * (T)L.ia[fo]);
+    } else {
+      const T vfv = c.vf[cb + ci];
+      if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+    }
+    tile[ci] = unew;
+  }
+  __syncthreads();
+  if ((ncell & 3) == 0 && sizeof(T) == 4) {
+    const float4 *src = reinterpret_cast<const float4 *>(tile);
+    float4 *dst = reinterpret_cast<float4 *>(phi + cb);
+    for (int i = threadIdx.x; i < (ncell >> 2); i += blockDim.x) dst[i] = src[i];
+  } else {
+    for (int i = threadIdx.x; i < ncell; i += blockDim.x) phi[cb + i] = tile[i];
+  }
+}
+
+template <typename T, int ND>
+static size_t rbgs_bulk_smem(const Topo &t) {
+  const int nface = ND == 3 ? t.nb * t.nb : t.nb;
+  return 16 + sizeof(T) * ((size_t)t.ncell + (size_t)ND * t.nfb + 3 * 2 * ND * (size_t)nface);
+}
+
+template <typename T, int ND>
+static void rbgs_bulk_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
+                         const int *guard, cudaStream_t s, bool pdl) {
+  const size_t smem = rbgs_bulk_smem<T, ND>(t);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_rbgs_bulk<T, ND>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  const int threads = std::min(kThreads, ((t.ncell >> 1) + 31) / 32 * 32);
+  launch_k(pdl, k_rbgs_bulk<T, ND>, L.n, threads, smem, s, t, c, L, color, phi, rhs, guard);
+}
+
+int rbgs_bulk_error(bool clear) {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_rbgs_err, sizeof(int)) != cudaSuccess) return -1;
+  if (clear && v) {
+    const int z = 0;
+    cudaMemcpyToSymbol(g_rbgs_err, &z, sizeof(int));
+  }
+  return v;
+}
+
 template <typename T, int ND>
 static size_t rbgs_tile_smem(const Topo &t) {
   const int nface = ND == 3 ? t.nb * t.nb : t.nb;
@@ -466,7 +661,8 @@ static void rbgs_nd(int variant, const Topo &t, const Coef<T> &c, const BlockLis
     case 4: rbgs_go<T, ND, 8>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
     case 5: rbgs_tile_go<T, ND, 2>(t, c, L, color, phi, rhs, guard, s, pdl); break;
     case 6: rbgs_tile_go<T, ND, 4>(t, c, L, color, phi, rhs, guard, s, pdl); break;
-    default: rbgs_tile_go<T, ND, 6>(t, c, L, color, phi, rhs, guard, s, pdl); break;
+    case 7: rbgs_tile_go<T, ND, 6>(t, c, L, color, phi, rhs, guard, s, pdl); break;
+    default: rbgs_bulk_go<T, ND>(t, c, L, color, phi, rhs, guard, s, pdl); break;
   }
 }
 
@@ -475,9 +671,15 @@ void launch_rbgs(const Topo &t, const Coef<T> &c, const BlockList &L, int color,
                  const int *guard, cudaStream_t s, bool pdl, int variant) {
   const int nhalf = t.ncell / 2;
   if (L.n == 0 || nhalf == 0) return;
-  // the tiled variants need the tile and halo in shared memory (<= 200 KiB)
+  // the tiled variants need the tile and halo in shared memory (<= 200 KiB);
+  // the bulk-copy variant also needs 16-byte multiples for the tile and the
+  // face rows of a block (and L.n CTAs in one grid dimension)
   const size_t tile = t.ndim == 2 ? rbgs_tile_smem<T, 2>(t) : rbgs_tile_smem<T, 3>(t);
   if (variant >= 5 && tile > 200 * 1024) variant = 3;
+  if (variant == 8) {
+    const size_t bulk = t.ndim == 2 ? rbgs_bulk_smem<T, 2>(t) : rbgs_bulk_smem<T, 3>(t);
+    if (bulk > 200 * 1024 || (t.ncell * sizeof(T)) % 16 != 0 || (t.nfb * sizeof(T)) % 16 != 0) variant = 7;
+  }
   const int threads = std::min(kThreads, (nhalf + 31) / 32 * 32);
   const dim3 grid((nhalf + threads - 1) / threads, std::min(L.n, 65535));
   if (t.ndim == 2)

@@ -274,7 +274,7 @@ class MacGpu {
   int kernels_per_iter_ = 0;
   int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1, graph_nn_ = -1;
   int rbgs_variant_[2] = {-1, -1};  // tuned smoother variant per precision (0 FP64, 1 FP32)
-  float rbgs_us_[2][8] = {};        // measured microseconds per variant (kRbgsVariants <= 8)
+  float rbgs_us_[2][16] = {};       // measured microseconds per variant (kRbgsVariants <= 16)
   // cooperative V-cycle
   VPhase *d_phases_ = nullptr;
   std::vector<VPhase> h_phases_;
