@@ -116,7 +116,7 @@ typedef struct sayaka_params {
   int32_t cluster_cells;  /* vcycle_kernel 2: runs of consecutive phases that each touch at most this many
                              cells share one cluster launch; larger phases get their own launch (16384) */
   int32_t smooth_variant; /* device smoother launch bounds (register cap): -1 = autotuned at prepare by
-                             timing every variant on the finest level (default), 0..8 = fixed */
+                             timing every variant on the finest level (default), 0..9 = fixed */
   int32_t learned;        /* device path with the FP32 V-cycle: 1 = add the trained learned block
                              correction after every V-cycle (default 0); see sayaka_mac_learned_* */
 } sayaka_params;
@@ -198,9 +198,10 @@ int sayaka_mac_launch_counts(sayaka_mac *h, int32_t *prologue, int32_t *per_iter
 /* the launch-bounds variant of the device smoother that the autotuner chose
  * for precision (0 FP64, 1 FP32 V-cycle) at sayaka_mac_prepare, -1 if not
  * tuned yet; us (may be NULL) receives the measured microseconds per variant
- * (n entries, 9 variants: 0-4 one thread per cell with register caps
+ * (n entries, 10 variants: 0-4 one thread per cell with register caps
  * 128/80/64/40/32, 5-7 the block staged in shared memory, caps 128/64/40,
- * 8 the block's tile and face coefficients staged by TMA bulk copies) */
+ * 8 the block's tile and face coefficients staged by TMA bulk copies,
+ * 9 persistent CTAs streaming blocks through double-buffered bulk copies) */
 int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n);
 /* number of blocks in tower L, or at one level of it (sublevel >= 1) */
 int32_t sayaka_mac_tower_size(sayaka_mac *h, int32_t L, int32_t sublevel);

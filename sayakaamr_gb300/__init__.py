@@ -452,8 +452,8 @@ class MacSolver:
 
     def tuned_smoother(self, precision):
         """(chosen variant, microseconds per variant) of the smoother autotuner"""
-        us = (C.c_float * 9)()
-        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 9)
+        us = (C.c_float * 10)()
+        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 10)
         return int(v), [float(x) for x in us]
 
     def tower_size(self, L, sublevel=0):

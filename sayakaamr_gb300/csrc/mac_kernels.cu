@@ -593,6 +593,176 @@ __global__ void __launch_bounds__(kThreads, 2) k_rbgs_bulk(Topo t, Coef<T> c, Bl
   }
 }
 
+// ---- persistent, double-buffered: one CTA per SM walks blocks p = blockIdx.x,
+// blockIdx.x + gridDim.x, ...; while it gathers the boundary contributions of
+// block i and updates it from shared memory, the copy engine streams block
+// i+1's tile, face coefficients, rhs and vf into the other buffer.
+constexpr int kStreamThreads = 512;
+
+template <typename T, int ND>
+__global__ void __launch_bounds__(kStreamThreads, 1) k_rbgs_stream(Topo t, Coef<T> c, BlockList L, int color,
+                                                                   T *__restrict__ phi, const T *__restrict__ rhs,
+                                                                   const int *guard) {
+  extern __shared__ __align__(128) unsigned char rbgs_stream_smem[];
+  pdl_enter();
+  if (guard && *guard) return;
+  const int nb = t.nb, ncell = t.ncell, nhalf = ncell >> 1, nfb = t.nfb;
+  const int nface = ND == 3 ? nb * nb : nb;
+  const size_t buf_elems = (size_t)3 * ncell + (size_t)ND * nfb;  // tile, rhs, vf, faces
+  unsigned long long *mbar = reinterpret_cast<unsigned long long *>(rbgs_stream_smem);  // [2]
+  T *buf0 = reinterpret_cast<T *>(rbgs_stream_smem + 16);
+  T *hc = buf0 + 2 * buf_elems;
+  T *hk = hc + 2 * ND * nface;
+  T *hv = hk + 2 * ND * nface;
+  const unsigned tile_bytes = (unsigned)(ncell * sizeof(T)), face_bytes = (unsigned)(nfb * sizeof(T));
+  const unsigned tx = 3 * tile_bytes + ND * face_bytes;
+  auto issue = [&](int pp, int j) {  // thread 0: copies of list entry pp into buffer j
+    const int bb = L.blocks[pp];
+    T *bt = buf0 + j * buf_elems;
+    mbar_expect_tx(&mbar[j], tx);
+    bulk_copy(bt, phi + (long)bb * ncell, tile_bytes, &mbar[j]);
+    bulk_copy(bt + ncell, rhs + (long)bb * ncell, tile_bytes, &mbar[j]);
+    bulk_copy(bt + 2 * ncell, c.vf + (long)bb * ncell, tile_bytes, &mbar[j]);
+    for (int d = 0; d < ND; d++) bulk_copy(bt + 3 * ncell + d * nfb, c.tff[d] + (long)bb * nfb, face_bytes, &mbar[j]);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+  }
+  __syncthreads();
+  if (blockIdx.x >= L.n) return;
+  if (threadIdx.x == 0) issue(blockIdx.x, 0);
+  const long kWait = 1l << 22;
+  unsigned phase[2] = {0u, 0u};
+  int k = 0;
+  for (int p = blockIdx.x; p < L.n; p += gridDim.x, k++) {
+    const int j = k & 1;
+    if (threadIdx.x == 0 && p + (int)gridDim.x < L.n) issue(p + gridDim.x, j ^ 1);
+    const int b = L.blocks[p];
+    const uint16_t ft = L.ftypes[p];
+    const long cb = (long)b * ncell, fb = (long)b * nfb;
+    for (int e = threadIdx.x; e < 2 * ND * nface; e += blockDim.x) {
+      const int f = e / nface, m = e - f * nface;
+      const int d = f >> 1, s = f & 1;
+      int ijk[3] = {0, 0, 0};
+      ijk[d] = s ? nb - 1 : 0;
+      const int q0 = d == 0 ? 1 : 0, q1 = d == 2 ? 1 : 2;
+      ijk[q0] = m % nb;
+      if (ND == 3) ijk[q1] = m / nb;
+      if (((ijk[0] + ijk[1] + ijk[2]) & 1) != color) continue;
+      int fx;
+      if (d == 0)
+        fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+      else if (d == 1)
+        fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+      else
+        fx = encode(ijk, nb) + s * nb * nb;
+      const int ty = face_type_of(ft, f);
+      T vc = 0, vk = 0, vv = 0;
+      if (ty == 0) {
+        vc = vk = c.tff[d][fb + fx];
+        vv = same_level_ghost<T, false>(t, b, f, ijk, phi);
+      } else if (ty == 1) {
+        if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
+      } else if (ty == 2) {
+        vc = vk = cf_coef(c, t, b, d, fx, (T)1.5);
+        vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi);
+      } else {
+        vc = cf_coef(c, t, b, d, fx, (T)0.75);
+        vk = (T)1;
+        vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi);
+      }
+      hc[e] = vc;
+      hk[e] = vk;
+      hv[e] = vv;
+    }
+    const bool ok = mbar_wait(&mbar[j], phase[j], kWait);
+    phase[j] ^= 1u;
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(&g_rbgs_err, 1);
+        // let this CTA's copies land before it exits
+        mbar_wait(&mbar[j], phase[j] ^ 1u, kWait);
+        if (p + (int)gridDim.x < L.n) mbar_wait(&mbar[j ^ 1], phase[j ^ 1], kWait);
+      }
+      return;
+    }
+    T *tile = buf0 + j * buf_elems;
+    const T *rh = tile + ncell, *vfs = tile + 2 * ncell, *tf0 = tile + 3 * ncell;
+    const T dv = geom(c, b, 6);
+    for (int h = threadIdx.x; h < nhalf; h += blockDim.x) {
+      int ijk[3];
+      color_cell_fast<ND>(h, t, color, ijk);
+      const int ci = t.lnb >= 0 ? ijk[0] + ((ijk[1] + (ijk[2] << t.lnb)) << t.lnb) : encode(ijk, nb);
+      T diag = c.alpha * dv;
+      T off = 0;
+#pragma unroll
+      for (int f = 0; f < 2 * ND; f++) {
+        const int d = f >> 1, s = f & 1;
+        const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+        if (!bnd) {
+          int fx;
+          if (d == 0)
+            fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+          else if (d == 1)
+            fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+          else
+            fx = ci + s * nb * nb;
+          const T coef = tf0[d * nfb + fx];
+          const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+          diag += coef;
+          off = fma_t(coef, tile[ci + (s ? stride : -stride)], off);
+        } else {
+          const int q0 = d == 0 ? 1 : 0, q1 = d == 2 ? 1 : 2;
+          const int m = ijk[q0] + (ND == 3 ? nb * ijk[q1] : 0);
+          const int e = f * nface + m;
+          diag += hc[e];
+          off = fma_t(hk[e], hv[e], off);
+        }
+      }
+      T unew = 0;
+      if (sizeof(T) == 8 && L.sa) {
+        const long fo = (long)p * ncell + ci;
+        unew = fma_t(rh[ci], (T)L.sa[fo], off * (T)L.ia[fo]);
+      } else {
+        const T vfv = vfs[ci];
+        if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rh[ci] * dv, vfv, off), diag);
+      }
+      tile[ci] = unew;
+    }
+    __syncthreads();
+    if ((ncell & 3) == 0 && sizeof(T) == 4) {
+      const float4 *src = reinterpret_cast<const float4 *>(tile);
+      float4 *dst = reinterpret_cast<float4 *>(phi + cb);
+      for (int i = threadIdx.x; i < (ncell >> 2); i += blockDim.x) dst[i] = src[i];
+    } else {
+      for (int i = threadIdx.x; i < ncell; i += blockDim.x) phi[cb + i] = tile[i];
+    }
+    __syncthreads();  // buffer j and the boundary arrays are free again
+  }
+}
+
+template <typename T, int ND>
+static size_t rbgs_stream_smem(const Topo &t) {
+  const int nface = ND == 3 ? t.nb * t.nb : t.nb;
+  return 16 + sizeof(T) * (2 * ((size_t)3 * t.ncell + (size_t)ND * t.nfb) + 3 * 2 * ND * (size_t)nface);
+}
+
+template <typename T, int ND>
+static void rbgs_stream_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
+                           const int *guard, cudaStream_t s, bool pdl) {
+  const size_t smem = rbgs_stream_smem<T, ND>(t);
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncSetAttribute(k_rbgs_stream<T, ND>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  }
+  launch_k(pdl, k_rbgs_stream<T, ND>, std::min(L.n, nsm), kStreamThreads, smem, s, t, c, L, color, phi, rhs,
+           guard);
+}
+
 template <typename T, int ND>
 static size_t rbgs_bulk_smem(const Topo &t) {
   const int nface = ND == 3 ? t.nb * t.nb : t.nb;
@@ -662,7 +832,8 @@ static void rbgs_nd(int variant, const Topo &t, const Coef<T> &c, const BlockLis
     case 5: rbgs_tile_go<T, ND, 2>(t, c, L, color, phi, rhs, guard, s, pdl); break;
     case 6: rbgs_tile_go<T, ND, 4>(t, c, L, color, phi, rhs, guard, s, pdl); break;
     case 7: rbgs_tile_go<T, ND, 6>(t, c, L, color, phi, rhs, guard, s, pdl); break;
-    default: rbgs_bulk_go<T, ND>(t, c, L, color, phi, rhs, guard, s, pdl); break;
+    case 8: rbgs_bulk_go<T, ND>(t, c, L, color, phi, rhs, guard, s, pdl); break;
+    default: rbgs_stream_go<T, ND>(t, c, L, color, phi, rhs, guard, s, pdl); break;
   }
 }
 
@@ -676,9 +847,14 @@ void launch_rbgs(const Topo &t, const Coef<T> &c, const BlockList &L, int color,
   // face rows of a block (and L.n CTAs in one grid dimension)
   const size_t tile = t.ndim == 2 ? rbgs_tile_smem<T, 2>(t) : rbgs_tile_smem<T, 3>(t);
   if (variant >= 5 && tile > 200 * 1024) variant = 3;
+  const bool aligned = (t.ncell * sizeof(T)) % 16 == 0 && (t.nfb * sizeof(T)) % 16 == 0;
   if (variant == 8) {
     const size_t bulk = t.ndim == 2 ? rbgs_bulk_smem<T, 2>(t) : rbgs_bulk_smem<T, 3>(t);
-    if (bulk > 200 * 1024 || (t.ncell * sizeof(T)) % 16 != 0 || (t.nfb * sizeof(T)) % 16 != 0) variant = 7;
+    if (bulk > 200 * 1024 || !aligned) variant = 7;
+  }
+  if (variant == 9) {
+    const size_t st = t.ndim == 2 ? rbgs_stream_smem<T, 2>(t) : rbgs_stream_smem<T, 3>(t);
+    if (st > 227 * 1024 || !aligned) variant = 7;
   }
   const int threads = std::min(kThreads, (nhalf + 31) / 32 * 32);
   const dim3 grid((nhalf + threads - 1) / threads, std::min(L.n, 65535));
