@@ -128,6 +128,12 @@ void launch_restrict(const Topo &t, const Coef<T> &c, const BlockList &crse, T *
 template <typename T>
 void launch_prolong(const Topo &t, const Coef<T> &c, const BlockList &fine, T *phi,
                     const int *guard, cudaStream_t s, bool pdl = false);
+// prolongation of a level fused with the first red sweep of its sublevel
+// (the level's blocks with the tower's face types); same values as
+// launch_prolong + launch_rbgs(color 0)
+template <typename T>
+void launch_prolong_red(const Topo &t, const Coef<T> &c, const BlockList &L, T *phi, const T *rhs,
+                        const int *guard, cudaStream_t s, bool pdl = false);
 
 void launch_flux(const Topo &t, const Coef<double> &c, const BlockList &L, int dir,
                  const double *phi, double *flux, cudaStream_t s);

@@ -969,13 +969,22 @@ void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *o
   bottom_launch<T>(resid, corr);
   for (int l = 2; l <= L; l++) {
     if (levels_[l].n == 0) continue;
-    launch_prolong<T>(topo_, c, level_list(l), corr, guard, stream_, prm_.pdl != 0);
+    // the level's own sublevel of tower l holds every block of the level, so
+    // the prolongation and the red sweep that follows it can be one launch
+    const BlockList top = sublevel_list(l, l);
+    const bool fused = prm_.fuse_prolong && prm_.n_post > 0 && top.n == levels_[l].n;
+    if (fused)
+      launch_prolong_red<T>(topo_, c, top, corr, resid, guard, stream_, prm_.pdl != 0);
+    else
+      launch_prolong<T>(topo_, c, level_list(l), corr, guard, stream_, prm_.pdl != 0);
     for (int s = 0; s < prm_.n_post; s++) {
       for (int ll = l; ll >= 1; ll--) {
         BlockList sl = sublevel_list(l, ll);
         if (sl.n == 0) break;
-        for (int rb = 0; rb < 2; rb++)
+        for (int rb = 0; rb < 2; rb++) {
+          if (fused && s == 0 && ll == l && rb == 0) continue;
           launch_rbgs<T>(topo_, c, sl, rb, corr, resid, guard, stream_, prm_.pdl != 0, rbgs_var<T>());
+        }
       }
     }
   }

@@ -792,6 +792,154 @@ int rbgs_bulk_error(bool clear) {
   return v;
 }
 
+// ---- prolongation of a level fused with the first (red) sweep that follows
+// it: one CTA per block of the level; the block's tile is filled with its
+// prolonged values (masked injection from the parent, as k_prolong), the
+// red cells' same-level neighbours outside the block are prolonged on the
+// fly from their own parents, coarse neighbours (FINE_CRSE) are read as they
+// are; the red cells are then updated with the tiled sweep's arithmetic and
+// the whole tile is written.  Same values as k_prolong + k_rbgs_tile.
+template <typename T, int ND>
+__device__ __forceinline__ T prolonged_value(const Topo &t, const Coef<T> &c, int b, const int ijk[3],
+                                             const T *__restrict__ phi) {
+  const int nb = t.nb, half = nb >> 1;
+  const int P = t.parent[b], wc = t.which_child[b];
+  int pc[3] = {0, 0, 0};
+  for (int q = 0; q < ND; q++) pc[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
+  const long q = (long)b * t.ncell + encode(ijk, nb);
+  return c.vf[q] > 0 ? phi[(long)P * t.ncell + encode(pc, nb)] : (T)0;
+}
+
+template <typename T, int ND>
+__global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, BlockList L, T *__restrict__ phi,
+                                                            const T *__restrict__ rhs, const int *guard) {
+  extern __shared__ __align__(16) unsigned char pr_smem[];
+  pdl_enter();
+  if (guard && *guard) return;
+  const int nb = t.nb, ncell = t.ncell, nhalf = ncell >> 1;
+  const int nface = ND == 3 ? nb * nb : nb;
+  T *tile = reinterpret_cast<T *>(pr_smem);
+  T *hc = tile + ncell;
+  T *hk = hc + 2 * ND * nface;
+  T *hv = hk + 2 * ND * nface;
+  for (int p = blockIdx.x; p < L.n; p += gridDim.x) {
+    const int b = L.blocks[p];
+    const uint16_t ft = L.ftypes[p];
+    const long cb = (long)b * ncell;
+    const long fb = (long)b * t.nfb;
+    for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+      int ijk[3];
+      decode<ND>(i, nb, ijk);
+      tile[i] = prolonged_value<T, ND>(t, c, b, ijk, phi);
+    }
+    for (int e = threadIdx.x; e < 2 * ND * nface; e += blockDim.x) {
+      const int f = e / nface, m = e - f * nface;
+      const int d = f >> 1, s = f & 1;
+      int ijk[3] = {0, 0, 0};
+      ijk[d] = s ? nb - 1 : 0;
+      const int q0 = d == 0 ? 1 : 0, q1 = d == 2 ? 1 : 2;
+      ijk[q0] = m % nb;
+      if (ND == 3) ijk[q1] = m / nb;
+      if ((ijk[0] + ijk[1] + ijk[2]) & 1) continue;  // red cells only
+      int fx;
+      if (d == 0)
+        fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+      else if (d == 1)
+        fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+      else
+        fx = encode(ijk, nb) + s * nb * nb;
+      const int ty = face_type_of(ft, f);
+      T vc = 0, vk = 0, vv = 0;
+      if (ty == 0) {
+        const int n = t.neighbor[b * 6 + f];
+        int ni[3] = {ijk[0], ijk[1], ijk[2]};
+        ni[d] = s ? 0 : nb - 1;
+        vc = vk = c.tff[d][fb + fx];
+        vv = prolonged_value<T, ND>(t, c, n, ni, phi);
+      } else if (ty == 1) {
+        if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
+      } else if (ty == 2) {
+        vc = vk = cf_coef(c, t, b, d, fx, (T)1.5);
+        vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi);
+      } else {  // not at the finest level of a tower
+        vc = cf_coef(c, t, b, d, fx, (T)0.75);
+        vk = (T)1;
+        vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi);
+      }
+      hc[e] = vc;
+      hk[e] = vk;
+      hv[e] = vv;
+    }
+    __syncthreads();
+    const T dv = geom(c, b, 6);
+    for (int h = threadIdx.x; h < nhalf; h += blockDim.x) {
+      int ijk[3];
+      color_cell_fast<ND>(h, t, 0, ijk);
+      const int ci = t.lnb >= 0 ? ijk[0] + ((ijk[1] + (ijk[2] << t.lnb)) << t.lnb) : encode(ijk, nb);
+      T diag = c.alpha * dv;
+      T off = 0;
+#pragma unroll
+      for (int f = 0; f < 2 * ND; f++) {
+        const int d = f >> 1, s = f & 1;
+        const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+        if (!bnd) {
+          int fx;
+          if (d == 0)
+            fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+          else if (d == 1)
+            fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+          else
+            fx = ci + s * nb * nb;
+          const T coef = c.tff[d][fb + fx];
+          const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+          diag += coef;
+          off = fma_t(coef, tile[ci + (s ? stride : -stride)], off);
+        } else {
+          const int q0 = d == 0 ? 1 : 0, q1 = d == 2 ? 1 : 2;
+          const int m = ijk[q0] + (ND == 3 ? nb * ijk[q1] : 0);
+          const int e = f * nface + m;
+          diag += hc[e];
+          off = fma_t(hk[e], hv[e], off);
+        }
+      }
+      T unew = 0;
+      if (sizeof(T) == 8 && L.sa) {
+        const long fo = (long)p * ncell + ci;
+        unew = fma_t(rhs[cb + ci], (T)L.sa[fo], off * (T)L.ia[fo]);
+      } else {
+        const T vfv = c.vf[cb + ci];
+        if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+      }
+      tile[ci] = unew;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < ncell; i += blockDim.x) phi[cb + i] = tile[i];
+    __syncthreads();
+  }
+}
+
+template <typename T>
+void launch_prolong_red(const Topo &t, const Coef<T> &c, const BlockList &L, T *phi, const T *rhs,
+                        const int *guard, cudaStream_t s, bool pdl) {
+  if (L.n == 0) return;
+  const int nface = t.ndim == 3 ? t.nb * t.nb : t.nb;
+  const size_t smem = sizeof(T) * ((size_t)t.ncell + 3 * 2 * t.ndim * (size_t)nface);
+  static bool attr[2] = {false, false};
+  if (!attr[t.ndim - 2]) {
+    if (t.ndim == 2)
+      cudaFuncSetAttribute(k_prolong_red<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    else
+      cudaFuncSetAttribute(k_prolong_red<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr[t.ndim - 2] = true;
+  }
+  const int threads = std::min(kThreads, ((t.ncell >> 1) + 31) / 32 * 32);
+  const int grid = std::min(L.n, 152 * 64);
+  if (t.ndim == 2)
+    launch_k(pdl, k_prolong_red<T, 2>, grid, threads, smem, s, t, c, L, phi, rhs, guard);
+  else
+    launch_k(pdl, k_prolong_red<T, 3>, grid, threads, smem, s, t, c, L, phi, rhs, guard);
+}
+
 template <typename T, int ND>
 static size_t rbgs_tile_smem(const Topo &t) {
   const int nface = ND == 3 ? t.nb * t.nb : t.nb;
@@ -929,7 +1077,9 @@ void launch_fix_bc(const Topo &t, const Coef<double> &c, const BlockList &L, con
   template void launch_restrict<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,         \
                                    cudaStream_t, bool);                                                         \
   template void launch_prolong<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,          \
-                                  cudaStream_t, bool);
+                                  cudaStream_t, bool);                                                          \
+  template void launch_prolong_red<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const T *,        \
+                                      const int *, cudaStream_t, bool);
 SAYAKA_INST(double)
 SAYAKA_INST(float)
 #undef SAYAKA_INST

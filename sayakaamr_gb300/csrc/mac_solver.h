@@ -36,6 +36,7 @@ struct SolverParams {
   int cluster_cells = 16384;  // vcycle_kernel 2: phases touching at most this many cells run in the cluster
   int smooth_variant = -1;    // device smoother launch bounds: -1 autotune at prepare, else variant index
   int learned = 0;            // device path, FP32 V-cycle: apply the trained block correction
+  int fuse_prolong = 1;       // device path: prolongation fused with the first red sweep of its level
 };
 
 struct SolveInfo {
