@@ -60,7 +60,9 @@ def parse():
     ap.add_argument("--precision", type=int, default=-1,
                     help="V-cycle precision: 1 FP32, 0 FP64, -1 (default) the faster of the two, timed during "
                          "warm-up (the outer BiCGSTAB and its 1e-8 test are FP64 either way)")
-    ap.add_argument("--n-post", type=int, default=2, help="post-smoothing sweeps per level (setPostSmoothNum)")
+    ap.add_argument("--n-post", type=int, default=-1,
+                    help="post-smoothing sweeps per level (the reference's setPostSmoothNum, its default 2); "
+                         "-1 (default): 1 or 2, whichever solves faster in the warm-up timing")
     ap.add_argument("--pdl", type=int, default=0, help="programmatic dependent launch between kernels")
     ap.add_argument("--vcycle-kernel", type=int, default=0,
                     help="0: one launch per phase, 1: whole V-cycle as one cooperative launch, "
@@ -260,7 +262,8 @@ def main():
     S = workloads.make_solver(prob)
     S.set_params(tol_rel=TOL, tol_abs=0.0, use_mg_precond=1, max_iter=2000, precision=max(args.precision, 0),
                  bottom=1,
-                 graph=0 if args.profile else 1, n_post_smooth=args.n_post, vcycle_kernel=args.vcycle_kernel,
+                 graph=0 if args.profile else 1, n_post_smooth=max(args.n_post, 1) if args.n_post >= 0 else 2,
+                 vcycle_kernel=args.vcycle_kernel,
                  cluster_cells=args.cluster_cells, smooth_variant=args.smooth_variant,
                  pdl=args.pdl)
     S.prepare()
@@ -289,20 +292,27 @@ def main():
                 raise SystemExit("warm-up solve failed: %s" % info)
 
     tuning = None
-    if args.precision < 0:
-        # the faster V-cycle precision on this workload, from timed warm-up solves
+    if args.precision < 0 or args.n_post < 0:
+        # the faster solver setting on this workload, from timed warm-up
+        # solves: V-cycle precision (FP32 / FP64) and post-smoothing sweeps
         tuning = {}
-        for prec in (1, 0):
-            S.set_params(precision=prec)
-            S.prepare()
-            warm()
-            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
-            for e in ev:
-                one(e)
-            torch.cuda.synchronize()
-            tuning[prec] = statistics.mean(a.elapsed_time(b) for a, b in ev)
-        args.precision = min(tuning, key=tuning.get)
-        S.set_params(precision=args.precision)
+        precs = (1, 0) if args.precision < 0 else (args.precision,)
+        posts = (1, 2) if args.n_post < 0 else (args.n_post,)
+        for prec in precs:
+            for npost in posts:
+                S.set_params(precision=prec, n_post_smooth=npost)
+                S.prepare()
+                warm()
+                ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+                for e in ev:
+                    one(e)
+                torch.cuda.synchronize()
+                tuning["precision %d, n_post %d" % (prec, npost)] = (
+                    statistics.mean(a.elapsed_time(b) for a, b in ev), prec, npost)
+        best = min(tuning.values())
+        args.precision, args.n_post = best[1], best[2]
+        tuning = {k: v[0] for k, v in tuning.items()}
+        S.set_params(precision=args.precision, n_post_smooth=args.n_post)
         S.prepare()
     warm()
     if args.profile:
@@ -374,7 +384,7 @@ def main():
                                % (prob.ndim, prob.nb, prob.ndim, finest, len(prob.leaf)),
                    "leaf_cells": prob.leaf_cells, "blocks": prob.num_blocks, "tol_rel": TOL,
                    "l2": "flushed (256 MiB write) before every timed solve", "precision": args.precision,
-                   "precision_tuning_ms": tuning,
+                   "setting_tuning_ms": tuning,
                    "iterations_per_solve": statistics.mean(iters), "n_post_smooth": args.n_post,
                    "vcycle_kernel": ("per-phase launches", "cooperative", "cluster")[args.vcycle_kernel],
                    "cluster_cells": args.cluster_cells if args.vcycle_kernel == 2 else None,
