@@ -254,6 +254,15 @@ int sayaka_mac_set_rhs_div(sayaka_mac *h, const double *const *u, int32_t ncomp,
 int sayaka_mac_correct_vel(sayaka_mac *h, int32_t dir, double dt, double *u, int32_t ncomp, int32_t ngrow,
                            int32_t comp);
 
+/* After AmrTree::regrid: the solution of the solver `old` (on the tree
+ * before the regrid, same device) becomes the initial solution of `h` (on the
+ * new tree), as the cell data part of initNewBlockDataAfterRegrid
+ * (src/SayakaRegrid.cpp:987-1105): blocks matched by root and child path are
+ * copied, refined blocks injected from their old leaf ancestor (prolongBlock),
+ * blocks that became leaves by coarsening get the average of their old
+ * children; a block with a deeper old subtree starts from zero. */
+int sayaka_mac_init_from(sayaka_mac *h, const sayaka_mac *old);
+
 /* ---- parity hooks on compact all-block arrays (tests and tools) ---- */
 /* the solve's right-hand side (all blocks) */
 int sayaka_mac_get_rhs_compact(sayaka_mac *h, double *out);

@@ -101,6 +101,7 @@ SIGNATURES = {
                                          C.c_double]),
     "sayaka_mac_correct_vel": (C.c_int, [_V, C.c_int32, C.c_double, _f64p, C.c_int32, C.c_int32, C.c_int32]),
     "sayaka_mac_get_rhs_compact": (C.c_int, [_V, _f64p]),
+    "sayaka_mac_init_from": (C.c_int, [_V, _V]),
     "sayaka_mac_learned_nparam": (C.c_int32, []),
     "sayaka_mac_learned_collect": (C.c_int, [_V, C.c_int32, _i32p]),
     "sayaka_mac_learned_train": (C.c_int, [_V, C.c_int32, C.c_float, C.c_int32, C.c_uint32, _f32p]),
@@ -444,6 +445,11 @@ class MacSolver:
         assert u.dtype == np.float64 and u.flags.c_contiguous
         _check(self.lib.sayaka_mac_correct_vel(self.h, int(d), float(dt), u.ctypes.data_as(_f64p), ncomp, ngrow,
                                                comp), "correct_vel", self.h)
+
+    def init_from(self, old):
+        """the solution of `old` (the solver of the tree before a regrid) as
+        this solver's initial solution"""
+        _check(self.lib.sayaka_mac_init_from(self.h, old.h), "init_from", self.h)
 
     def get_rhs_compact(self):
         r = self._cells()

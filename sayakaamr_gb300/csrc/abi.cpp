@@ -711,6 +711,18 @@ int sayaka_mac_correct_vel(sayaka_mac *h, int32_t dir, double dt, double *u, int
     return (int)SAYAKA_OK;
   });
 }
+int sayaka_mac_init_from(sayaka_mac *h, const sayaka_mac *old) {
+  return guarded(h, [&] {
+    if (!old || !old->gpu) return (int)SAYAKA_BAD_INPUT;
+    std::string why;
+    const int st = h->gpu->init_solution_from(*old->gpu, &why);
+    if (st == 1) {
+      h->err = why;
+      return (int)SAYAKA_BAD_INPUT;
+    }
+    return st == 0 ? (int)SAYAKA_OK : (int)SAYAKA_CUDA_ERROR;
+  });
+}
 int sayaka_mac_get_rhs_compact(sayaka_mac *h, double *out) {
   return guarded(h, [&] {
     if (!out) return (int)SAYAKA_BAD_INPUT;

@@ -119,6 +119,9 @@ class MacGpu {
   void rhs_from_div(const double *const *u_all, const double *const *w_all, double scale);
   void correct_vel(int dir, double dt, double *u_all);
   void get_rhs(double *all);
+  // the solution of a solver on the tree before a regrid, carried onto this
+  // tree (0 ok, 1 bad input: why says which, 2 CUDA error)
+  int init_solution_from(const MacGpu &old, std::string *why);
 
   // r = rhs - A x on tower L and out = {|r|_inf, r.r}; device pointers to
   // compact all-block arrays, enqueued on s, no device allocation (scratch in
