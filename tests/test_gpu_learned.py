@@ -66,8 +66,7 @@ def trained_config2():
 
 
 def test_training_lowers_the_loss_on_solver_pairs(trained_config2):
-    """the block-local residual left after the correction falls with training
-    (measured on config2: 11.4 after the first epoch, 9.1 after ten)"""
+    """the block-local residual left after the correction falls with training"""
     prob, S, iters, first, last = trained_config2
     assert iters > 5
     assert last < 0.9 * first, (first, last)
@@ -78,7 +77,7 @@ def test_learned_correction_against_plain_fp32_vcycle(trained_config2):
     trained correction.  Both converge; the correction either takes no more
     iterations than the plain FP32 V-cycle, or the device detects the stall
     and finishes with plain MG (status STALL_FALLBACK).  Measured on config2:
-    34 iterations plain, 35-52 with the correction, which stalls and falls
+    10 iterations plain, 21 with the correction, which stalls and falls
     back: the block-local correction does not help BiCGSTAB here."""
     prob, S, iters, first, last = trained_config2
     res, st = {}, {}
