@@ -119,6 +119,9 @@ typedef struct sayaka_params {
                              timing every variant on the finest level (default), 0..9 = fixed */
   int32_t learned;        /* device path with the FP32 V-cycle: 1 = add the trained learned block
                              correction after every V-cycle (default 0); see sayaka_mac_learned_* */
+  int32_t sublevel_order; /* device V-cycle smoothing over a tower's sublevels: 0 = finest to coarsest,
+                             red then black per sublevel (the reference's order, mg_smooth_level);
+                             1 = one launch per colour and level parity (default) */
 } sayaka_params;
 
 typedef struct sayaka_solve_info {

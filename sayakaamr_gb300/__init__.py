@@ -39,7 +39,8 @@ class Params(C.Structure):
                 ("bot_tol_abs", C.c_double), ("bot_max_iter", C.c_int32), ("precision", C.c_int32),
                 ("bottom", C.c_int32), ("verbose", C.c_int32), ("graph", C.c_int32),
                 ("vcycle_kernel", C.c_int32), ("pdl", C.c_int32),
-                ("cluster_cells", C.c_int32), ("smooth_variant", C.c_int32), ("learned", C.c_int32)]
+                ("cluster_cells", C.c_int32), ("smooth_variant", C.c_int32), ("learned", C.c_int32),
+                ("sublevel_order", C.c_int32)]
 
 
 class SolveInfo(C.Structure):

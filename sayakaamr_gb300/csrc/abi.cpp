@@ -321,6 +321,7 @@ void sayaka_params_default(sayaka_params *p) {
   p->cluster_cells = d.cluster_cells;
   p->smooth_variant = d.smooth_variant;
   p->learned = d.learned;
+  p->sublevel_order = d.sublevel_order;
 }
 
 int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
@@ -536,6 +537,7 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.cluster_cells = p->cluster_cells;
     s.smooth_variant = p->smooth_variant;
     s.learned = p->learned;
+    s.sublevel_order = p->sublevel_order;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
   });

@@ -646,6 +646,24 @@ void MacGpu::build_smooth_factors() {
       k_smooth_factors<3><<<ew_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, d_sfac_[l], d_sfac_[l] + w);
     CK(cudaGetLastError());
   }
+  // the same factors for the parity-grouped lists (same cells, regrouped)
+  if ((int)d_pfac_.size() < finest_ + 1) d_pfac_.resize(finest_ + 1, nullptr);
+  for (int l = 2; l <= finest_; l++) {
+    const DevTower &tw = towers_[l];
+    const BlockList PL{tw.par.blocks, tw.par.ftypes, tw.par.n};
+    const long w = (long)PL.n * ncell_;
+    if (w == 0) continue;
+    if (!d_pfac_[l] && cudaMalloc(&d_pfac_[l], 2 * w * sizeof(double)) != cudaSuccess) {
+      d_pfac_[l] = nullptr;
+      fail("out of device memory (smoother factors)");
+      return;
+    }
+    if (tt_.ndim == 2)
+      k_smooth_factors<2><<<ew_grid(w), kTPB, 0, stream_>>>(topo_, c64_, PL, d_pfac_[l], d_pfac_[l] + w);
+    else
+      k_smooth_factors<3><<<ew_grid(w), kTPB, 0, stream_>>>(topo_, c64_, PL, d_pfac_[l], d_pfac_[l] + w);
+    CK(cudaGetLastError());
+  }
 }
 
 // Autotuner of the device smoother: every launch-bounds variant (register
@@ -978,6 +996,17 @@ void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *o
     else
       launch_prolong<T>(topo_, c, level_list(l), corr, guard, stream_, prm_.pdl != 0);
     for (int s = 0; s < prm_.n_post; s++) {
+      if (prm_.sublevel_order == 1) {
+        // one launch per colour and level parity: within a launch no cell
+        // reads another that the launch writes (same-level neighbours have
+        // the other colour, coarse/fine neighbours the other parity)
+        for (int rb = 0; rb < 2; rb++)
+          for (int g = 0; g < 2; g++) {
+            const BlockList gl = parity_list(l, g, fused && s == 0 && rb == 0 && g == 0);
+            if (gl.n > 0) launch_rbgs<T>(topo_, c, gl, rb, corr, resid, guard, stream_, prm_.pdl != 0, rbgs_var<T>());
+          }
+        continue;
+      }
       for (int ll = l; ll >= 1; ll--) {
         BlockList sl = sublevel_list(l, ll);
         if (sl.n == 0) break;
@@ -1131,6 +1160,15 @@ void MacGpu::capture_loop(int precision) {
   graph_cc_ = prm_.cluster_cells;
   graph_var_ = rbgs_variant_[precision == 1];
   graph_nn_ = (int)learned_active();
+  graph_order_ = prm_.sublevel_order;
+}
+
+// the captured graph was recorded with other parameters than the current ones
+bool MacGpu::graph_stale() const {
+  return !graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
+         graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl || graph_cc_ != prm_.cluster_cells ||
+         graph_var_ != rbgs_variant_[prm_.precision == 1] || graph_nn_ != (int)learned_active() ||
+         graph_order_ != prm_.sublevel_order;
 }
 
 int MacGpu::cg_solve_device(SolveInfo *info) {
@@ -1149,13 +1187,9 @@ int MacGpu::cg_solve_enqueue() {
   // coefficients changed since sayaka_mac_prepare: the fast-path data and the
   // graph must be rebuilt first
   if (!err_.empty() || !bottom_ready_ || coef_version_ != fast_coef_version_) return -1;
-  if (prm_.graph && (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
-                     graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl ||
-                     graph_cc_ != prm_.cluster_cells ||
-                     graph_var_ != rbgs_variant_[prm_.precision == 1] ||
-                     graph_nn_ != (int)learned_active()))
+  if (prm_.graph && graph_stale())
     return -1;
-  if (prm_.vcycle_kernel && program_npost_ != prm_.n_post) return -1;
+  if (prm_.vcycle_kernel && (program_npost_ != prm_.n_post || program_order_ != prm_.sublevel_order)) return -1;
   return enqueue_solve();
 }
 
@@ -1236,12 +1270,9 @@ int MacGpu::prepare_device() {
   tune_smoother(prm_.precision);
   if (learned_active()) learned_prepare();
   if (!err_.empty()) return -1;
-  if (prm_.vcycle_kernel && program_npost_ != prm_.n_post) build_vcycle_program();
-  if (prm_.graph && (!graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
-                     graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl ||
-                     graph_cc_ != prm_.cluster_cells ||
-                     graph_var_ != rbgs_variant_[prm_.precision == 1] ||
-                     graph_nn_ != (int)learned_active()))
+  if (prm_.vcycle_kernel && (program_npost_ != prm_.n_post || program_order_ != prm_.sublevel_order))
+    build_vcycle_program();
+  if (prm_.graph && graph_stale())
     capture_loop(prm_.precision);
   return err_.empty() ? 0 : -1;
 }

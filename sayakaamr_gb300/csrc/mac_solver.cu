@@ -220,6 +220,28 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
       CK(cudaMemcpy(dt.all.blocks, src.blocks.data(), n * sizeof(int), cudaMemcpyHostToDevice));
       CK(cudaMemcpy(dt.all.ftypes, ft.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice));
     }
+    // parity-grouped copy of the sublevels the V-cycle smooths (L down to
+    // the first empty sublevel, as the per-sublevel loop does)
+    int low = L;
+    while (low - 1 >= 1 && src.end[low - 1] > src.begin[low - 1]) low--;
+    std::vector<int> pb;
+    std::vector<uint16_t> pf;
+    for (int g = 0; g < 2; g++) {
+      if (g == 1) dt.par_split = (int)pb.size();
+      for (int l = L - g; l >= low; l -= 2)
+        for (int p = src.begin[l]; p < src.end[l]; p++) {
+          pb.push_back(src.blocks[p]);
+          pf.push_back(ft[p]);
+        }
+      if (g == 0) dt.par_top = src.end[L] - src.begin[L];
+    }
+    dt.par.n = (int)pb.size();
+    dt.par.blocks = dalloc<int>(pb.size());
+    dt.par.ftypes = dalloc<uint16_t>(pb.size());
+    if (!pb.empty()) {
+      CK(cudaMemcpy(dt.par.blocks, pb.data(), pb.size() * sizeof(int), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(dt.par.ftypes, pf.data(), pf.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    }
   }
   levels_.resize(tt.max_level + 1);
   nonleaf_.resize(tt.max_level + 1);
@@ -305,6 +327,8 @@ MacGpu::~MacGpu() {
   for (auto &t : towers_) {
     fr(t.all.blocks);
     fr(t.all.ftypes);
+    fr(t.par.blocks);
+    fr(t.par.ftypes);
   }
   for (auto &l : levels_) fr(l.blocks);
   for (auto &l : nonleaf_) fr(l.blocks);
@@ -337,6 +361,7 @@ MacGpu::~MacGpu() {
   fr(d_part_);
   fr(d_opP_);
   for (auto &q : d_sfac_) fr(q);
+  for (auto &q : d_pfac_) fr(q);
   for (auto &q : d_face_) fr(q);
   learned_free();
   fr(d_opS_);
@@ -365,6 +390,18 @@ BlockList MacGpu::sublevel_list(int L, int l) const {
     const long w = (long)t.all.n * ncell_;
     r.sa = d_sfac_[L] + (long)b * ncell_;
     r.ia = d_sfac_[L] + w + (long)b * ncell_;
+  }
+  return r;
+}
+BlockList MacGpu::parity_list(int L, int g, bool skip_top) const {
+  const DevTower &t = towers_[L];
+  const int b = g == 0 ? (skip_top ? t.par_top : 0) : t.par_split;
+  const int e = g == 0 ? t.par_split : t.par.n;
+  BlockList r{t.par.blocks + b, t.par.ftypes + b, e - b};
+  if (L < (int)d_pfac_.size() && d_pfac_[L]) {
+    const long w = (long)t.par.n * ncell_;
+    r.sa = d_pfac_[L] + (long)b * ncell_;
+    r.ia = d_pfac_[L] + w + (long)b * ncell_;
   }
   return r;
 }

@@ -37,6 +37,9 @@ struct SolverParams {
   int smooth_variant = -1;    // device smoother launch bounds: -1 autotune at prepare, else variant index
   int learned = 0;            // device path, FP32 V-cycle: apply the trained block correction
   int fuse_prolong = 1;       // device path: prolongation fused with the first red sweep of its level
+  int sublevel_order = 1;     // device V-cycle smoothing order over a tower's sublevels: 0 = finest to
+                              // coarsest, red then black per sublevel (the reference's); 1 = one launch per
+                              // colour and level parity (sublevels two levels apart never touch)
 };
 
 struct SolveInfo {
@@ -148,10 +151,18 @@ class MacGpu {
     DevList all;
     std::vector<int> begin, end;
     std::vector<int> blocks;
+    // the smoothed sublevels regrouped by level parity: [L, L-2, ... | L-1,
+    // L-3, ...]; group 0 is [0, par_split), its first par_top entries are
+    // the blocks of level L
+    DevList par;
+    int par_split = 0, par_top = 0;
   };
 
   BlockList tower_list(int L) const;
   BlockList sublevel_list(int L, int l) const;
+  // parity group g of tower L (sublevel_order 1); skip_top leaves out the
+  // level-L blocks of group 0
+  BlockList parity_list(int L, int g, bool skip_top) const;
   BlockList level_list(int l) const;
   BlockList nonleaf_list(int l) const;
 
@@ -251,6 +262,7 @@ class MacGpu {
   double *d_part_ = nullptr;
   double *d_opP_ = nullptr, *d_opS_ = nullptr;  // factors of the device solve's operator
   std::vector<double *> d_sfac_;                // FP64 smoother factors per tower: sa then ia
+  std::vector<double *> d_pfac_;                // the same for the parity-grouped tower lists
   std::vector<double *> d_face_;                // face fields of the projection step (u, w, flux)
   LearnedState ls_;
   std::vector<double *> *record_ = nullptr;     // iterates recorded by a collection solve
@@ -276,13 +288,14 @@ class MacGpu {
   cudaGraphExec_t graph_exec_ = nullptr;
   int graph_prec_ = -1, graph_npost_ = -1;
   int kernels_per_iter_ = 0;
-  int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1, graph_nn_ = -1;
+  int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1, graph_nn_ = -1, graph_order_ = -1;
+  bool graph_stale() const;
   int rbgs_variant_[2] = {-1, -1};  // tuned smoother variant per precision (0 FP64, 1 FP32)
   float rbgs_us_[2][16] = {};       // measured microseconds per variant (kRbgsVariants <= 16)
   // cooperative V-cycle
   VPhase *d_phases_ = nullptr;
   std::vector<VPhase> h_phases_;
-  int n_phases_ = 0, program_npost_ = -1, coop_grid_ = 0;
+  int n_phases_ = 0, program_npost_ = -1, program_order_ = -1, coop_grid_ = 0;
   unsigned *d_bar_ = nullptr;  // [0] count, [1] generation, [2] error word
   // cluster V-cycle: restriction program, bottom, prolongation/smoothing program
   int n_down_ = 0, cluster_size_ = 0;

@@ -139,12 +139,18 @@ void MacGpu::build_vcycle_program() {
   for (int l = 2; l <= L; l++) {
     if (levels_[l].n == 0) continue;
     push(kPhaseProlong, 0, level_list(l));
-    for (int s = 0; s < prm_.n_post; s++)
+    for (int s = 0; s < prm_.n_post; s++) {
+      if (prm_.sublevel_order == 1) {
+        for (int rb = 0; rb < 2; rb++)
+          for (int g = 0; g < 2; g++) push(kPhaseSmooth, rb, parity_list(l, g, false));
+        continue;
+      }
       for (int ll = l; ll >= 1; ll--) {
         BlockList sl = sublevel_list(l, ll);
         if (sl.n == 0) break;
         for (int rb = 0; rb < 2; rb++) push(kPhaseSmooth, rb, sl);
       }
+    }
   }
   push(kPhaseOut, 0, tower_list(L));
   if (d_phases_) cudaFree(d_phases_);
@@ -158,6 +164,7 @@ void MacGpu::build_vcycle_program() {
     CK(cudaMemset(d_bar_, 0, 4 * sizeof(unsigned)));
   }
   program_npost_ = prm_.n_post;
+  program_order_ = prm_.sublevel_order;
 }
 
 template <typename T>

@@ -65,12 +65,13 @@ def test_device_path_matches_oracle_on_workload():
         assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-8, (precision, info)
 
 
+@pytest.mark.parametrize("order", [0, 1])
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name", ["t2s", "t3s", "c1"])
-def test_fused_vcycles_match_per_phase_launches(name, precision):
+def test_fused_vcycles_match_per_phase_launches(name, precision, order):
     """the one-launch cooperative V-cycle and the thread-block-cluster V-cycle
-    run the same cell functions in the same phase order: identical iterations
-    and bit-identical solutions"""
+    run the same cell functions in the same phase order (either sublevel
+    order): identical iterations and bit-identical solutions"""
     g, t, tb, S = setup_solver(name)
     S.set_rhs_compact(g["sv_rhs"])
     out = []
@@ -79,7 +80,7 @@ def test_fused_vcycles_match_per_phase_launches(name, precision):
     for vk, cc in ((0, 16384), (1, 16384), (2, 600), (2, 1 << 30)):
         S.set_zero_sol()
         S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=precision, bottom=1,
-                     vcycle_kernel=vk, cluster_cells=cc)
+                     vcycle_kernel=vk, cluster_cells=cc, sublevel_order=order)
         info = S.cg_solve()
         assert info["status"] == 0, info
         out.append((info["iterations"], S.get_sol_compact()))
@@ -139,3 +140,24 @@ def test_nan_in_the_rhs_ends_as_breakdown_not_convergence():
     S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=50, precision=1, bottom=1)
     info = S.cg_solve()
     assert info["status"] == 1, info
+
+
+@pytest.mark.parametrize("name", ["config1", "config2"])
+def test_sublevel_orders_both_converge(name):
+    """the parity-grouped smoothing order (default) and the reference's
+    per-sublevel order are both fixed linear preconditioners: both reach the
+    criterion, within a few iterations of each other"""
+    from sayakaamr_gb300 import workloads
+    p = workloads.CONFIGS[name]()
+    S = workloads.make_solver(p)
+    its = []
+    for order in (0, 1):
+        S.set_zero_sol()
+        S.set_params(tol_rel=1e-8, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=1, bottom=1,
+                     sublevel_order=order)
+        info = S.cg_solve()
+        assert info["status"] == 0, (order, info)
+        assert info["rnorm"] < 1e-8 * info["rnorm0"]
+        its.append(info["iterations"])
+    print(name, "iterations per-sublevel order %d, parity order %d" % tuple(its))
+    assert abs(its[0] - its[1]) <= max(3, its[0] // 4), its
