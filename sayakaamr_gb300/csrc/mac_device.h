@@ -40,6 +40,20 @@ struct Coef {
   T alpha, beta;
 };
 
+// Halo descriptor of a tower list entry, kHX ints: the ids every face of
+// the block reads, precomputed so that a cell's gathers wait on one load
+// (the descriptor) instead of a chain through the topology tables:
+//   [f]            f < 2*ndim: same-level neighbour (FINE_FINE), coarse leaf
+//                  (FINE_CRSE) or -1
+//   [kHXInfo]      face types (low 16 bits) | which_child << 16
+//   [kHXBlock]     the block id
+//   [kHXKids+4f+k] CRSE_FINE face f: the fine child covering transverse
+//                  halves k (bit j = half of the j-th transverse dimension)
+constexpr int kHX = 32;
+constexpr int kHXInfo = 6;
+constexpr int kHXBlock = 7;
+constexpr int kHXKids = 8;
+
 // a block list with per-block packed face types (2 bits per face)
 struct BlockList {
   const int *blocks;
@@ -48,6 +62,7 @@ struct BlockList {
   // FP64 smoother factors of a tower sublevel list, [entry][cell]:
   // sa = dv*vf/diag, ia = 1/diag (0 where vf = 0); null when not built
   const double *sa = nullptr, *ia = nullptr;
+  const int *hx = nullptr;  // halo descriptors [entry][kHX] of tower lists, else null
 };
 
 // BiCGSTAB state kept on the device (FP64 scalars and control flags) by the

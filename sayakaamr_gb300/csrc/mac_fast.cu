@@ -454,7 +454,8 @@ __global__ void __launch_bounds__(kTPB) k_smooth_factors(Topo t, Coef<double> c,
 // sum T * phi_nb over the faces of cell ijk that are not physical boundaries
 template <int ND, typename TX>
 __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &c, int b, uint16_t ft,
-                                             const int ijk[3], int ci, const TX *__restrict__ x) {
+                                             const int ijk[3], int ci, const TX *__restrict__ x,
+                                             const int *__restrict__ hx = nullptr) {
   using namespace stencil;
   const int nb = t.nb;
   const long cb = (long)b * t.ncell;
@@ -470,11 +471,13 @@ __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &
     } else {
       const int ty = face_type_of(ft, f);
       if (ty == 0)
-        off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], (double)same_level_ghost<TX, false>(t, b, f, ijk, x), off);
+        off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], (double)same_level_ghost<TX, false>(t, b, f, ijk, x, hx),
+                       off);
       else if (ty == 2)
-        off = __fma_rn(cf_coef(c, t, b, d, fx, 1.5), (double)fine_crse_ghost<TX, ND, false>(t, b, f, ijk, x), off);
+        off = __fma_rn(cf_coef(c, t, b, d, fx, 1.5), (double)fine_crse_ghost<TX, ND, false>(t, b, f, ijk, x, hx),
+                       off);
       else if (ty == 3)
-        off += crse_fine_sum<double, ND, false>(t, c, b, f, ijk, x);
+        off += crse_fine_sum<double, ND, false>(t, c, b, f, ijk, x, hx);
     }
   }
   return off;
@@ -500,9 +503,11 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
     int p, ci, ijk[3];
     split_cell<ND>(it, t, p, ci);
     decode_fast<ND>(ci, t, ijk);
-    const int b = L.blocks[p];
+    const int *e = L.hx ? L.hx + (long)p * kHX : nullptr;
+    const int b = e ? e[kHXBlock] : L.blocks[p];
+    const uint16_t ft = e ? (uint16_t)(e[kHXInfo] & 0xffff) : L.ftypes[p];
     const long q = (long)b * t.ncell + ci;
-    const double off = op_offdiag<ND, TX>(t, c, b, L.ftypes[p], ijk, ci, x);
+    const double off = op_offdiag<ND, TX>(t, c, b, ft, ijk, ci, x, e);
     const double sc = S[q];
     double yv = __fma_rn((double)x[q], P[q], -off * sc);
     if (MODE >= 2) yv = sc != 0.0 ? w[q] - yv : 0.0;

@@ -84,8 +84,14 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs(Topo t, Coef<T> c, Bloc
   color_cell_fast<ND>(h, t, color, ijk);
   for (int p = blockIdx.y; p < L.n; p += gridDim.y) {
     const long fo = (long)p * t.ncell;
-    smooth_cell_fast<T, ND>(t, c, L.blocks[p], L.ftypes[p], ijk, phi, rhs, L.sa ? L.sa + fo : nullptr,
-                            L.ia ? L.ia + fo : nullptr);
+    if (L.hx) {
+      const int *e = L.hx + (long)p * kHX;
+      smooth_cell_fast<T, ND>(t, c, e[kHXBlock], (uint16_t)(e[kHXInfo] & 0xffff), ijk, phi, rhs,
+                              L.sa ? L.sa + fo : nullptr, L.ia ? L.ia + fo : nullptr, e);
+    } else {
+      smooth_cell_fast<T, ND>(t, c, L.blocks[p], L.ftypes[p], ijk, phi, rhs, L.sa ? L.sa + fo : nullptr,
+                              L.ia ? L.ia + fo : nullptr);
+    }
   }
 }
 
@@ -153,8 +159,9 @@ __global__ void k_flux(Topo t, Coef<double> c, BlockList L, int dir, const doubl
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int p = (int)(it / nfb);
     const int fxi = (int)(it - (long)p * nfb);
-    const int b = L.blocks[p];
-    const uint16_t ft = L.ftypes[p];
+    const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
+    const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
+    const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
     // decode the face-centred index: dimension dir has nb+1 entries
     const int e0 = nb + (dir == 0), e1 = nb + (dir == 1);
     int fi[3];
@@ -231,8 +238,9 @@ __global__ void k_fix_bc(Topo t, Coef<double> c, BlockList L, const double *__re
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int p = (int)(it / ncell);
     const int ci = (int)(it - (long)p * ncell);
-    const int b = L.blocks[p];
-    const uint16_t ft = L.ftypes[p];
+    const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
+    const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
+    const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
     int ijk[3];
     decode<ND>(ci, nb, ijk);
     const double dv = c.geom[b * 8 + 6];
@@ -324,8 +332,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
   T *hk = hc + 2 * ND * nface;
   T *hv = hk + 2 * ND * nface;
   for (int p = blockIdx.x; p < L.n; p += gridDim.x) {
-    const int b = L.blocks[p];
-    const uint16_t ft = L.ftypes[p];
+    const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
+    const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
+    const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
     const long cb = (long)b * ncell;
     const long fb = (long)b * t.nfb;
     if ((ncell & 3) == 0 && sizeof(T) == 4) {
@@ -358,16 +367,16 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
       T vc = 0, vk = 0, vv = 0;
       if (ty == 0) {
         vc = vk = c.tff[d][fb + fx];
-        vv = same_level_ghost<T, false>(t, b, f, ijk, phi);
+        vv = same_level_ghost<T, false>(t, b, f, ijk, phi, hxe);
       } else if (ty == 1) {
         if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
       } else if (ty == 2) {
         vc = vk = cf_coef(c, t, b, d, fx, (T)1.5);
-        vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi);
+        vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi, hxe);
       } else {
         vc = cf_coef(c, t, b, d, fx, (T)0.75);
         vk = (T)1;
-        vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi);
+        vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi, hxe);
       }
       hc[e] = vc;
       hk[e] = vk;
@@ -486,8 +495,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_rbgs_bulk(Topo t, Coef<T> c, Bl
   T *hk = hc + 2 * ND * nface;
   T *hv = hk + 2 * ND * nface;
   const int p = blockIdx.x;
-  const int b = L.blocks[p];
-  const uint16_t ft = L.ftypes[p];
+  const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
+  const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
+  const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
   const long cb = (long)b * ncell, fb = (long)b * nfb;
   const unsigned tile_bytes = (unsigned)(ncell * sizeof(T)), face_bytes = (unsigned)(nfb * sizeof(T));
   if (threadIdx.x == 0) mbar_init(mbar, 1);
@@ -518,16 +528,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_rbgs_bulk(Topo t, Coef<T> c, Bl
     T vc = 0, vk = 0, vv = 0;
     if (ty == 0) {
       vc = vk = c.tff[d][fb + fx];
-      vv = same_level_ghost<T, false>(t, b, f, ijk, phi);
+      vv = same_level_ghost<T, false>(t, b, f, ijk, phi, hxe);
     } else if (ty == 1) {
       if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
     } else if (ty == 2) {
       vc = vk = cf_coef(c, t, b, d, fx, (T)1.5);
-      vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi);
+      vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi, hxe);
     } else {
       vc = cf_coef(c, t, b, d, fx, (T)0.75);
       vk = (T)1;
-      vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi);
+      vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi, hxe);
     }
     hc[e] = vc;
     hk[e] = vk;
@@ -638,8 +648,9 @@ __global__ void __launch_bounds__(kStreamThreads, 1) k_rbgs_stream(Topo t, Coef<
   for (int p = blockIdx.x; p < L.n; p += gridDim.x, k++) {
     const int j = k & 1;
     if (threadIdx.x == 0 && p + (int)gridDim.x < L.n) issue(p + gridDim.x, j ^ 1);
-    const int b = L.blocks[p];
-    const uint16_t ft = L.ftypes[p];
+    const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
+    const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
+    const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
     const long cb = (long)b * ncell, fb = (long)b * nfb;
     for (int e = threadIdx.x; e < 2 * ND * nface; e += blockDim.x) {
       const int f = e / nface, m = e - f * nface;
@@ -661,16 +672,16 @@ __global__ void __launch_bounds__(kStreamThreads, 1) k_rbgs_stream(Topo t, Coef<
       T vc = 0, vk = 0, vv = 0;
       if (ty == 0) {
         vc = vk = c.tff[d][fb + fx];
-        vv = same_level_ghost<T, false>(t, b, f, ijk, phi);
+        vv = same_level_ghost<T, false>(t, b, f, ijk, phi, hxe);
       } else if (ty == 1) {
         if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
       } else if (ty == 2) {
         vc = vk = cf_coef(c, t, b, d, fx, (T)1.5);
-        vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi);
+        vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi, hxe);
       } else {
         vc = cf_coef(c, t, b, d, fx, (T)0.75);
         vk = (T)1;
-        vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi);
+        vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi, hxe);
       }
       hc[e] = vc;
       hk[e] = vk;
@@ -823,8 +834,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
   T *hk = hc + 2 * ND * nface;
   T *hv = hk + 2 * ND * nface;
   for (int p = blockIdx.x; p < L.n; p += gridDim.x) {
-    const int b = L.blocks[p];
-    const uint16_t ft = L.ftypes[p];
+    const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
+    const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
+    const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
     const long cb = (long)b * ncell;
     const long fb = (long)b * t.nfb;
     for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
@@ -860,11 +872,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
         if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
       } else if (ty == 2) {
         vc = vk = cf_coef(c, t, b, d, fx, (T)1.5);
-        vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi);
+        vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi, hxe);
       } else {  // not at the finest level of a tower
         vc = cf_coef(c, t, b, d, fx, (T)0.75);
         vk = (T)1;
-        vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi);
+        vv = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi, hxe);
       }
       hc[e] = vc;
       hk[e] = vk;

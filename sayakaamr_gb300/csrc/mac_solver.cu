@@ -200,6 +200,30 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
   tree_from_tables(tt, t);
   std::vector<Tower> tw = build_towers(t);
   towers_.resize(tt.max_level + 1);
+  // halo descriptors of a tower list (see kHX)
+  auto make_hx = [&](const std::vector<int> &blk, const std::vector<uint16_t> &fts) {
+    std::vector<int> hx(blk.size() * kHX, -1);
+    for (size_t p = 0; p < blk.size(); p++) {
+      const int b = blk[p];
+      int *e = &hx[p * kHX];
+      e[kHXInfo] = (int)((unsigned)fts[p] | ((unsigned)tt.which_child[b] << 16));
+      e[kHXBlock] = b;
+      for (int f = 0; f < 2 * nd; f++) {
+        const int ty = (fts[p] >> (2 * f)) & 3, d = f >> 1, s = f & 1;
+        if (ty == 0) e[f] = tt.neighbor[b * 6 + f];
+        if (ty == 2) e[f] = fc_neigh_[b * 6 + f];
+        if (ty != 3) continue;
+        const int N = tt.neighbor[b * 6 + f];
+        for (int k = 0; k < (1 << (nd - 1)); k++) {
+          int cidx = (1 - s) << d, j = 0;
+          for (int q = 0; q < nd; q++)
+            if (q != d) cidx |= ((k >> j++) & 1) << q;
+          e[kHXKids + f * 4 + k] = tt.child[N * 8 + cidx];
+        }
+      }
+    }
+    return hx;
+  };
   for (int L = 1; L <= tt.max_level; L++) {
     const Tower &src = tw[L];
     DevTower &dt = towers_[L];
@@ -216,9 +240,12 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
     dt.all.n = n;
     dt.all.blocks = dalloc<int>(n);
     dt.all.ftypes = dalloc<uint16_t>(n);
+    dt.all.hx = dalloc<int>((size_t)n * kHX);
     if (n) {
       CK(cudaMemcpy(dt.all.blocks, src.blocks.data(), n * sizeof(int), cudaMemcpyHostToDevice));
       CK(cudaMemcpy(dt.all.ftypes, ft.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice));
+      const std::vector<int> hx = make_hx(src.blocks, ft);
+      CK(cudaMemcpy(dt.all.hx, hx.data(), hx.size() * sizeof(int), cudaMemcpyHostToDevice));
     }
     // parity-grouped copy of the sublevels the V-cycle smooths (L down to
     // the first empty sublevel, as the per-sublevel loop does)
@@ -238,9 +265,12 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
     dt.par.n = (int)pb.size();
     dt.par.blocks = dalloc<int>(pb.size());
     dt.par.ftypes = dalloc<uint16_t>(pb.size());
+    dt.par.hx = dalloc<int>(pb.size() * kHX);
     if (!pb.empty()) {
       CK(cudaMemcpy(dt.par.blocks, pb.data(), pb.size() * sizeof(int), cudaMemcpyHostToDevice));
       CK(cudaMemcpy(dt.par.ftypes, pf.data(), pf.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+      const std::vector<int> hx = make_hx(pb, pf);
+      CK(cudaMemcpy(dt.par.hx, hx.data(), hx.size() * sizeof(int), cudaMemcpyHostToDevice));
     }
   }
   levels_.resize(tt.max_level + 1);
@@ -329,6 +359,8 @@ MacGpu::~MacGpu() {
     fr(t.all.ftypes);
     fr(t.par.blocks);
     fr(t.par.ftypes);
+    fr(t.all.hx);
+    fr(t.par.hx);
   }
   for (auto &l : levels_) fr(l.blocks);
   for (auto &l : nonleaf_) fr(l.blocks);
@@ -380,12 +412,15 @@ MacGpu::~MacGpu() {
 // block lists
 BlockList MacGpu::tower_list(int L) const {
   const DevTower &t = towers_[L];
-  return BlockList{t.all.blocks, t.all.ftypes, t.all.n};
+  BlockList r{t.all.blocks, t.all.ftypes, t.all.n};
+  r.hx = t.all.hx;
+  return r;
 }
 BlockList MacGpu::sublevel_list(int L, int l) const {
   const DevTower &t = towers_[L];
   const int b = t.begin[l], e = t.end[l];
   BlockList r{t.all.blocks + b, t.all.ftypes + b, e - b};
+  r.hx = t.all.hx + (long)b * kHX;
   if (L < (int)d_sfac_.size() && d_sfac_[L]) {
     const long w = (long)t.all.n * ncell_;
     r.sa = d_sfac_[L] + (long)b * ncell_;
@@ -398,6 +433,7 @@ BlockList MacGpu::parity_list(int L, int g, bool skip_top) const {
   const int b = g == 0 ? (skip_top ? t.par_top : 0) : t.par_split;
   const int e = g == 0 ? t.par_split : t.par.n;
   BlockList r{t.par.blocks + b, t.par.ftypes + b, e - b};
+  r.hx = t.par.hx + (long)b * kHX;
   if (L < (int)d_pfac_.size() && d_pfac_[L]) {
     const long w = (long)t.par.n * ncell_;
     r.sa = d_pfac_[L] + (long)b * ncell_;

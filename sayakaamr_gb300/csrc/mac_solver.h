@@ -145,6 +145,7 @@ class MacGpu {
   struct DevList {
     int *blocks = nullptr;
     uint16_t *ftypes = nullptr;
+    int *hx = nullptr;  // halo descriptors (tower lists)
     int n = 0;
   };
   struct DevTower {

@@ -84,21 +84,21 @@ __device__ __forceinline__ T cf_coef(const Coef<T> &c, const Topo &t, int b, int
 // reference's RESTRICT_SUM order (lower transverse dimension fastest)
 template <typename T, int ND, bool CG = false, typename TX = T>
 __device__ __forceinline__ T crse_fine_sum(const Topo &t, const Coef<T> &c, int b, int f, const int ijk[3],
-                                           const TX *__restrict__ x) {
+                                           const TX *__restrict__ x, const int *__restrict__ hx = nullptr) {
   const int nb = t.nb, half = nb >> 1;
   const int d = f >> 1, s = f & 1;
-  const int N = t.neighbor[b * 6 + f];
-  int cidx = (1 - s) << d;
+  int cidx = (1 - s) << d, k = 0;
   int base[3] = {0, 0, 0};
   int tq[2] = {0, 0}, nt = 0;
   for (int q = 0; q < ND; q++) {
     if (q == d) continue;
     const int sq = ijk[q] >= half ? 1 : 0;
     cidx |= sq << q;
+    k |= sq << nt;
     base[q] = 2 * (ijk[q] - sq * half);
     tq[nt++] = q;
   }
-  const int F = t.child[N * 8 + cidx];
+  const int F = hx ? hx[kHXKids + f * 4 + k] : t.child[t.neighbor[b * 6 + f] * 8 + cidx];
   int fi[3];
   fi[d] = s == 1 ? 0 : nb - 1;
   const int fside = s == 1 ? 0 : 1;  // the fine block's face toward b
@@ -121,11 +121,12 @@ __device__ __forceinline__ T crse_fine_sum(const Topo &t, const Coef<T> &c, int 
 // value a FINE_CRSE ghost cell holds: the coarse leaf's boundary cell
 // (injection through the parent's ghost layer)
 template <typename T, int ND, bool CG = false>
-__device__ __forceinline__ T fine_crse_ghost(const Topo &t, int b, int f, const int ijk[3], const T *__restrict__ x) {
+__device__ __forceinline__ T fine_crse_ghost(const Topo &t, int b, int f, const int ijk[3], const T *__restrict__ x,
+                                             const int *__restrict__ hx = nullptr) {
   const int nb = t.nb, half = nb >> 1;
   const int d = f >> 1, s = f & 1;
-  const int C = t.fc_neigh[b * 6 + f];
-  const int wc = t.which_child[b];
+  const int C = hx ? hx[f] : t.fc_neigh[b * 6 + f];
+  const int wc = hx ? hx[kHXInfo] >> 16 : t.which_child[b];
   int ci[3] = {0, 0, 0};
   for (int q = 0; q < ND; q++) {
     if (q == d)
@@ -138,9 +139,10 @@ __device__ __forceinline__ T fine_crse_ghost(const Topo &t, int b, int f, const 
 
 // mirrored boundary cell of the same-level neighbour
 template <typename T, bool CG = false>
-__device__ __forceinline__ T same_level_ghost(const Topo &t, int b, int f, const int ijk[3], const T *__restrict__ x) {
+__device__ __forceinline__ T same_level_ghost(const Topo &t, int b, int f, const int ijk[3], const T *__restrict__ x,
+                                              const int *__restrict__ hx = nullptr) {
   const int d = f >> 1, s = f & 1;
-  const int n = t.neighbor[b * 6 + f];
+  const int n = hx ? hx[f] : t.neighbor[b * 6 + f];
   int ni[3] = {ijk[0], ijk[1], ijk[2]};
   ni[d] = s == 1 ? 0 : t.nb - 1;
   return ld<CG>(&x[(long)n * t.ncell + encode(ni, t.nb)]);
@@ -262,7 +264,8 @@ __device__ __forceinline__ double fma_t(double a, double b, double c) { return _
 template <typename T, int ND, bool CG = false>
 __device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c, int b, uint16_t ft,
                                                  const int ijk[3], T *__restrict__ phi, const T *__restrict__ rhs,
-                                                 const double *sa = nullptr, const double *ia = nullptr) {
+                                                 const double *sa = nullptr, const double *ia = nullptr,
+                                                 const int *__restrict__ hx = nullptr) {
   const int nb = t.nb;
   const int ci = t.lnb >= 0 ? ijk[0] + ((ijk[1] + (ijk[2] << t.lnb)) << t.lnb) : encode(ijk, nb);
   const long cb = (long)b * t.ncell;
@@ -292,16 +295,16 @@ __device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c
       if (ty == 0) {
         const T coef = c.tff[d][fb + fx];
         diag += coef;
-        off = fma_t(coef, same_level_ghost<T, CG>(t, b, f, ijk, phi), off);
+        off = fma_t(coef, same_level_ghost<T, CG>(t, b, f, ijk, phi, hx), off);
       } else if (ty == 1) {
         if (t.bc_type[b * 6 + f] != kBCNeumann) diag += c.tff[d][fb + fx] * (T)2.0;
       } else if (ty == 2) {
         const T coef = cf_coef(c, t, b, d, fx, (T)1.5);
         diag += coef;
-        off = fma_t(coef, fine_crse_ghost<T, ND, CG>(t, b, f, ijk, phi), off);
+        off = fma_t(coef, fine_crse_ghost<T, ND, CG>(t, b, f, ijk, phi, hx), off);
       } else {
         diag += cf_coef(c, t, b, d, fx, (T)0.75);
-        off += crse_fine_sum<T, ND, CG>(t, c, b, f, ijk, phi);
+        off += crse_fine_sum<T, ND, CG>(t, c, b, f, ijk, phi, hx);
       }
     }
   }
