@@ -49,10 +49,14 @@ struct Coef {
 //   [kHXBlock]     the block id
 //   [kHXKids+4f+k] CRSE_FINE face f: the fine child covering transverse
 //                  halves k (bit j = half of the j-th transverse dimension)
-constexpr int kHX = 32;
+//   [kHXPar+f]     FINE_FINE face f of a block below level 1: the
+//                  neighbour's parent * 8 + its which_child, else -1
+//   [kHXPar+6]     the block's own parent * 8 + which_child, or -1
+constexpr int kHX = 40;
 constexpr int kHXInfo = 6;
 constexpr int kHXBlock = 7;
 constexpr int kHXKids = 8;
+constexpr int kHXPar = 32;
 
 // a block list with per-block packed face types (2 bits per face)
 struct BlockList {
@@ -63,6 +67,9 @@ struct BlockList {
   // sa = dv*vf/diag, ia = 1/diag (0 where vf = 0); null when not built
   const double *sa = nullptr, *ia = nullptr;
   const int *hx = nullptr;  // halo descriptors [entry][kHX] of tower lists, else null
+  // level lists: [entry] parent * 8 + which_child; non-leaf lists:
+  // [entry][8] children; null elsewhere
+  const int *links = nullptr;
 };
 
 // BiCGSTAB state kept on the device (FP64 scalars and control flags) by the

@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kThreads) k_restrict(Topo t, Coef<T> c, BlockL
   const long total = (long)L.n * ncell;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int p = (int)(it / ncell);
-    restrict_cell<T, ND>(t, c, L.blocks[p], (int)(it - (long)p * ncell), phi);
+    restrict_cell<T, ND>(t, c, L.blocks[p], (int)(it - (long)p * ncell), phi, L.links ? L.links + (long)p * 8 : nullptr);
   }
 }
 
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(kThreads) k_prolong(Topo t, Coef<T> c, BlockLi
   const long total = (long)L.n * ncell;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int p = (int)(it / ncell);
-    prolong_cell<T, ND>(t, c, L.blocks[p], (int)(it - (long)p * ncell), phi);
+    prolong_cell<T, ND>(t, c, L.blocks[p], (int)(it - (long)p * ncell), phi, L.links ? L.links[p] : -1);
   }
 }
 
@@ -812,9 +812,9 @@ int rbgs_bulk_error(bool clear) {
 // the whole tile is written.  Same values as k_prolong + k_rbgs_tile.
 template <typename T, int ND>
 __device__ __forceinline__ T prolonged_value(const Topo &t, const Coef<T> &c, int b, const int ijk[3],
-                                             const T *__restrict__ phi) {
+                                             const T *__restrict__ phi, int pw = -1) {
   const int nb = t.nb, half = nb >> 1;
-  const int P = t.parent[b], wc = t.which_child[b];
+  const int P = pw >= 0 ? pw >> 3 : t.parent[b], wc = pw >= 0 ? pw & 7 : t.which_child[b];
   int pc[3] = {0, 0, 0};
   for (int q = 0; q < ND; q++) pc[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
   const long q = (long)b * t.ncell + encode(ijk, nb);
@@ -842,7 +842,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
     for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
       int ijk[3];
       decode<ND>(i, nb, ijk);
-      tile[i] = prolonged_value<T, ND>(t, c, b, ijk, phi);
+      tile[i] = prolonged_value<T, ND>(t, c, b, ijk, phi, hxe ? hxe[kHXPar + 6] : -1);
     }
     for (int e = threadIdx.x; e < 2 * ND * nface; e += blockDim.x) {
       const int f = e / nface, m = e - f * nface;
@@ -863,11 +863,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
       const int ty = face_type_of(ft, f);
       T vc = 0, vk = 0, vv = 0;
       if (ty == 0) {
-        const int n = t.neighbor[b * 6 + f];
+        const int n = hxe ? hxe[f] : t.neighbor[b * 6 + f];
         int ni[3] = {ijk[0], ijk[1], ijk[2]};
         ni[d] = s ? 0 : nb - 1;
         vc = vk = c.tff[d][fb + fx];
-        vv = prolonged_value<T, ND>(t, c, n, ni, phi);
+        vv = prolonged_value<T, ND>(t, c, n, ni, phi, hxe ? hxe[kHXPar + f] : -1);
       } else if (ty == 1) {
         if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
       } else if (ty == 2) {

@@ -208,9 +208,14 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
       int *e = &hx[p * kHX];
       e[kHXInfo] = (int)((unsigned)fts[p] | ((unsigned)tt.which_child[b] << 16));
       e[kHXBlock] = b;
+      if (tt.parent[b] >= 0) e[kHXPar + 6] = tt.parent[b] * 8 + tt.which_child[b];
       for (int f = 0; f < 2 * nd; f++) {
         const int ty = (fts[p] >> (2 * f)) & 3, d = f >> 1, s = f & 1;
-        if (ty == 0) e[f] = tt.neighbor[b * 6 + f];
+        if (ty == 0) {
+          const int n = tt.neighbor[b * 6 + f];
+          e[f] = n;
+          if (tt.parent[n] >= 0) e[kHXPar + f] = tt.parent[n] * 8 + tt.which_child[n];
+        }
         if (ty == 2) e[f] = fc_neigh_[b * 6 + f];
         if (ty != 3) continue;
         const int N = tt.neighbor[b * 6 + f];
@@ -287,6 +292,15 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
       dl.n = (int)v.size();
       dl.blocks = dalloc<int>(v.size());
       if (!v.empty()) CK(cudaMemcpy(dl.blocks, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice));
+      // level lists: parent * 8 + which_child; non-leaf lists: children
+      std::vector<int> lk;
+      for (int b : v) {
+        if (k == 0) lk.push_back(tt.parent[b] >= 0 ? tt.parent[b] * 8 + tt.which_child[b] : -1);
+        else
+          for (int q = 0; q < 8; q++) lk.push_back(tt.child[b * 8 + q]);
+      }
+      dl.links = dalloc<int>(lk.size());
+      if (!lk.empty()) CK(cudaMemcpy(dl.links, lk.data(), lk.size() * sizeof(int), cudaMemcpyHostToDevice));
     }
   }
 
@@ -362,8 +376,14 @@ MacGpu::~MacGpu() {
     fr(t.all.hx);
     fr(t.par.hx);
   }
-  for (auto &l : levels_) fr(l.blocks);
-  for (auto &l : nonleaf_) fr(l.blocks);
+  for (auto &l : levels_) {
+    fr(l.blocks);
+    fr(l.links);
+  }
+  for (auto &l : nonleaf_) {
+    fr(l.blocks);
+    fr(l.links);
+  }
   fr(d_neighbor_);
   fr(d_child_);
   fr(d_parent_);
@@ -441,8 +461,16 @@ BlockList MacGpu::parity_list(int L, int g, bool skip_top) const {
   }
   return r;
 }
-BlockList MacGpu::level_list(int l) const { return BlockList{levels_[l].blocks, nullptr, levels_[l].n}; }
-BlockList MacGpu::nonleaf_list(int l) const { return BlockList{nonleaf_[l].blocks, nullptr, nonleaf_[l].n}; }
+BlockList MacGpu::level_list(int l) const {
+  BlockList r{levels_[l].blocks, nullptr, levels_[l].n};
+  r.links = levels_[l].links;
+  return r;
+}
+BlockList MacGpu::nonleaf_list(int l) const {
+  BlockList r{nonleaf_[l].blocks, nullptr, nonleaf_[l].n};
+  r.links = nonleaf_[l].links;
+  return r;
+}
 
 // ---------------------------------------------------------------------------
 // coefficients

@@ -145,7 +145,8 @@ class MacGpu {
   struct DevList {
     int *blocks = nullptr;
     uint16_t *ftypes = nullptr;
-    int *hx = nullptr;  // halo descriptors (tower lists)
+    int *hx = nullptr;     // halo descriptors (tower lists)
+    int *links = nullptr;  // parents (level lists) or children (non-leaf lists)
     int n = 0;
   };
   struct DevTower {

@@ -349,7 +349,8 @@ __device__ __forceinline__ void color_cell(int h, int nb, int color, int ijk[3])
 // avg(fine*vf_fine)/vf_coarse (src/SayakaMacIB.cpp:157-232,
 // src/SayakaInterpPatch.cpp:398-444)
 template <typename T, int ND, bool CG = false>
-__device__ __forceinline__ void restrict_cell(const Topo &t, const Coef<T> &c, int b, int ci, T *__restrict__ phi) {
+__device__ __forceinline__ void restrict_cell(const Topo &t, const Coef<T> &c, int b, int ci, T *__restrict__ phi,
+                                              const int *__restrict__ kids = nullptr) {
   const int nb = t.nb, ncell = t.ncell, half = nb >> 1;
   const T wgt = (T)1.0 / (T)(1 << ND);
   int ijk[3];
@@ -360,7 +361,7 @@ __device__ __forceinline__ void restrict_cell(const Topo &t, const Coef<T> &c, i
     cidx |= sq << q;
     fb[q] = 2 * (ijk[q] - sq * half);
   }
-  const int F = t.child[b * 8 + cidx];
+  const int F = kids ? kids[cidx] : t.child[b * 8 + cidx];
   const long fbase = (long)F * ncell;
   T sum = 0;
   for (int kk = 0; kk < (ND == 3 ? 2 : 1); kk++)
@@ -379,11 +380,12 @@ __device__ __forceinline__ void restrict_cell(const Topo &t, const Coef<T> &c, i
 // masked injection of one fine cell of block b from its parent
 // (src/SayakaMacIB.cpp:234-283)
 template <typename T, int ND, bool CG = false>
-__device__ __forceinline__ void prolong_cell(const Topo &t, const Coef<T> &c, int b, int ci, T *__restrict__ phi) {
+__device__ __forceinline__ void prolong_cell(const Topo &t, const Coef<T> &c, int b, int ci, T *__restrict__ phi,
+                                             int pw = -1) {
   const int nb = t.nb, ncell = t.ncell, half = nb >> 1;
   int ijk[3];
   decode<ND>(ci, nb, ijk);
-  const int P = t.parent[b], wc = t.which_child[b];
+  const int P = pw >= 0 ? pw >> 3 : t.parent[b], wc = pw >= 0 ? pw & 7 : t.which_child[b];
   int pc[3] = {0, 0, 0};
   for (int q = 0; q < ND; q++) pc[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
   const T v = ld<CG>(&phi[(long)P * ncell + encode(pc, nb)]);
