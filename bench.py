@@ -72,6 +72,9 @@ def parse():
                     help="vcycle-kernel 2: largest phase (cells) that runs inside the cluster")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--bottom-level", type=int, default=0,
+                    help="level of the dense bottom solve (0: the coarsest uniform level of at most 4096 cells "
+                         "per component)")
     ap.add_argument("--sublevel-order", type=int, default=1,
                     help="V-cycle smoothing order over a tower's sublevels: 0 finest to coarsest per sublevel "
                          "(the reference's), 1 one launch per colour and level parity")
@@ -311,7 +314,7 @@ def main():
                  graph=0 if args.profile else 1, n_post_smooth=max(args.n_post, 1) if args.n_post >= 0 else 2,
                  vcycle_kernel=args.vcycle_kernel,
                  cluster_cells=args.cluster_cells, smooth_variant=args.smooth_variant,
-                 pdl=args.pdl, sublevel_order=args.sublevel_order)
+                 pdl=args.pdl, sublevel_order=args.sublevel_order, bottom_level=args.bottom_level)
     S.prepare()
     ext = torch.cuda.ExternalStream(S.stream())
     if args.kernel >= 0:
@@ -437,6 +440,7 @@ def main():
                    "pdl": bool(args.pdl),
                    "sublevel_order": ("finest to coarsest per sublevel", "one launch per colour and level parity")[
                        args.sublevel_order],
+                   "bottom_level": S.bottom_level(),
                    "smoother_autotune": dict(zip(("variant", "us_per_variant"), S.tuned_smoother(args.precision))),
                    "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "e2e": {"value": ws * prob.leaf_cells / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": h2d,

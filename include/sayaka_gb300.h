@@ -119,6 +119,10 @@ typedef struct sayaka_params {
                              timing every variant on the finest level (default), 0..9 = fixed */
   int32_t learned;        /* device path with the FP32 V-cycle: 1 = add the trained learned block
                              correction after every V-cycle (default 0); see sayaka_mac_learned_* */
+  int32_t bottom_level;   /* device path: level of the dense bottom solve; 0 = auto (the finest level below the
+                             finest whose tower is one uniform level with at most 1024 (2D) / 4096 (3D) cells
+                             per connected component; level 1 otherwise), n >= 1 = level n if its tower is
+                             one uniform level of at most 4096 cells per component */
   int32_t sublevel_order; /* device V-cycle smoothing over a tower's sublevels: 0 = finest to coarsest,
                              red then black per sublevel (the reference's order, mg_smooth_level);
                              1 = one launch per colour and level parity (default) */
@@ -206,6 +210,8 @@ int sayaka_mac_launch_counts(sayaka_mac *h, int32_t *prologue, int32_t *per_iter
  * 8 the block's tile and face coefficients staged by TMA bulk copies,
  * 9 persistent CTAs streaming blocks through double-buffered bulk copies) */
 int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n);
+/* level of the device solve's dense bottom solve once prepared (-1 before) */
+int32_t sayaka_mac_bottom_level(const sayaka_mac *h);
 /* number of blocks in tower L, or at one level of it (sublevel >= 1) */
 int32_t sayaka_mac_tower_size(sayaka_mac *h, int32_t L, int32_t sublevel);
 
@@ -265,6 +271,13 @@ int sayaka_mac_correct_vel(sayaka_mac *h, int32_t dir, double dt, double *u, int
  * blocks that became leaves by coarsening get the average of their old
  * children; a block with a deeper old subtree starts from zero. */
 int sayaka_mac_init_from(sayaka_mac *h, const sayaka_mac *old);
+
+/* ---- self-test of the device solve's integer-pipe conversions (tests) ----
+ * narrow[i] = double -> float of d[i] (round to nearest even) and
+ * widen[i] = float -> double of f[i], widen0[i] = 0.0 + (double)f[i], each
+ * next to the hardware conversion (_hw); no counterpart in the reference */
+int sayaka_fp_selftest(const double *d, const float *f, int n, float *narrow, float *narrow_hw, double *widen,
+                       double *widen_hw, double *widen0, double *widen0_hw);
 
 /* ---- parity hooks on compact all-block arrays (tests and tools) ---- */
 /* the solve's right-hand side (all blocks) */

@@ -40,7 +40,7 @@ class Params(C.Structure):
                 ("bottom", C.c_int32), ("verbose", C.c_int32), ("graph", C.c_int32),
                 ("vcycle_kernel", C.c_int32), ("pdl", C.c_int32),
                 ("cluster_cells", C.c_int32), ("smooth_variant", C.c_int32), ("learned", C.c_int32),
-                ("sublevel_order", C.c_int32)]
+                ("bottom_level", C.c_int32), ("sublevel_order", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -103,6 +103,8 @@ SIGNATURES = {
     "sayaka_mac_correct_vel": (C.c_int, [_V, C.c_int32, C.c_double, _f64p, C.c_int32, C.c_int32, C.c_int32]),
     "sayaka_mac_get_rhs_compact": (C.c_int, [_V, _f64p]),
     "sayaka_mac_init_from": (C.c_int, [_V, _V]),
+    "sayaka_mac_bottom_level": (C.c_int32, [_V]),
+    "sayaka_fp_selftest": (C.c_int, [_f64p, _f32p, C.c_int, _f32p, _f32p, _f64p, _f64p, _f64p, _f64p]),
     "sayaka_mac_learned_nparam": (C.c_int32, []),
     "sayaka_mac_learned_collect": (C.c_int, [_V, C.c_int32, _i32p]),
     "sayaka_mac_learned_train": (C.c_int, [_V, C.c_int32, C.c_float, C.c_int32, C.c_uint32, _f32p]),
@@ -152,6 +154,21 @@ def _f64(a):
 
 class SayakaError(RuntimeError):
     pass
+
+
+def fp_selftest(d, f):
+    """the device solve's integer-pipe conversions next to the hardware ones:
+    (narrow, narrow_hw, widen, widen_hw, widen0, widen0_hw) for doubles d
+    and floats f of the same length"""
+    lib = load_library()
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    n = len(d)
+    assert len(f) == n
+    outs = [np.zeros(n, np.float32), np.zeros(n, np.float32)] + [np.zeros(n, np.float64) for _ in range(4)]
+    ptr = [o.ctypes.data_as(_f32p if o.dtype == np.float32 else _f64p) for o in outs]
+    _check(lib.sayaka_fp_selftest(d.ctypes.data_as(_f64p), f.ctypes.data_as(_f32p), n, *ptr), "fp_selftest")
+    return tuple(outs)
 
 
 def _check(rc, what, handle=None):
@@ -462,6 +479,10 @@ class MacSolver:
         us = (C.c_float * 10)()
         v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 10)
         return int(v), [float(x) for x in us]
+
+    def bottom_level(self):
+        """level of the device solve's dense bottom solve (-1 before prepare)"""
+        return int(self.lib.sayaka_mac_bottom_level(self.h))
 
     def tower_size(self, L, sublevel=0):
         return self.lib.sayaka_mac_tower_size(self.h, int(L), int(sublevel))

@@ -321,6 +321,7 @@ void sayaka_params_default(sayaka_params *p) {
   p->cluster_cells = d.cluster_cells;
   p->smooth_variant = d.smooth_variant;
   p->learned = d.learned;
+  p->bottom_level = d.bottom_level;
   p->sublevel_order = d.sublevel_order;
 }
 
@@ -537,6 +538,7 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.cluster_cells = p->cluster_cells;
     s.smooth_variant = p->smooth_variant;
     s.learned = p->learned;
+    s.bottom_level = p->bottom_level;
     s.sublevel_order = p->sublevel_order;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
@@ -725,6 +727,14 @@ int sayaka_mac_init_from(sayaka_mac *h, const sayaka_mac *old) {
     return st == 0 ? (int)SAYAKA_OK : (int)SAYAKA_CUDA_ERROR;
   });
 }
+int sayaka_fp_selftest(const double *d, const float *f, int n, float *narrow, float *narrow_hw, double *widen,
+                       double *widen_hw, double *widen0, double *widen0_hw) {
+  if (n < 0 || (n > 0 && (!d || !f || !narrow || !narrow_hw || !widen || !widen_hw || !widen0 || !widen0_hw)))
+    return SAYAKA_BAD_INPUT;
+  return sayaka_gb300::fp_selftest(d, f, n, narrow, narrow_hw, widen, widen_hw, widen0, widen0_hw) == 0
+             ? SAYAKA_OK
+             : SAYAKA_CUDA_ERROR;
+}
 int sayaka_mac_get_rhs_compact(sayaka_mac *h, double *out) {
   return guarded(h, [&] {
     if (!out) return (int)SAYAKA_BAD_INPUT;
@@ -747,6 +757,10 @@ int sayaka_mac_residual_compact(sayaka_mac *h, int32_t L, const double *x, const
     h->gpu->residual(L, x, rhs, r);
     return (int)SAYAKA_OK;
   });
+}
+int32_t sayaka_mac_bottom_level(const sayaka_mac *h) {
+  if (!h || !h->gpu) return -1;
+  return h->gpu->bottom_level();
 }
 int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n) {
   if (!h || !h->gpu) return -1;

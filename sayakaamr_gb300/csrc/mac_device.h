@@ -98,11 +98,12 @@ struct FState {
 // rows grouped by component, one CTA tile per 8 rows.
 struct BottomDev {
   const double *binv;          // the components' row-major inverses, back to back
-  const int *blocks;           // level-1 block of every ncell rows, in row order
+  const int *blocks;           // bottom-level block of every ncell rows, in row order
   const int *comp_row0, *comp_n;
   const long long *comp_off;   // start of each component's inverse in binv
   const int *tile_comp, *tile_row0;
   int ntiles, ncell, max_n;
+  const float *binv32 = nullptr;  // FP32 copy of binv for the FP32 V-cycle (bottom level above 1)
 };
 constexpr int kBottomTileRows = 8;
 

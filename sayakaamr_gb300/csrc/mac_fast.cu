@@ -21,6 +21,8 @@
 #include "cuda_check.h"
 #include "mac_stencil.cuh"
 #include "launch.cuh"
+#include "mac_fp.cuh"
+#include "tree.h"
 
 namespace sayaka_gb300 {
 
@@ -107,6 +109,23 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, d
     epi(fin);
     *counter = 0;
   }
+}
+
+// precision conversions of the vector kernels, exact or correctly rounded
+// on the integer pipe (mac_fp.cuh)
+template <typename T>
+__device__ __forceinline__ T narrow_to(double v) {
+  if constexpr (sizeof(T) == 4)
+    return fpint::narrow(v);
+  else
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ double widen_from(T v) {
+  if constexpr (sizeof(T) == 4)
+    return fpint::widen(v);
+  else
+    return v;
 }
 
 __device__ __forceinline__ long cell_of(const BlockList &L, int ncell, int it) {
@@ -287,7 +306,7 @@ __global__ void k_pupdate(BlockList L, int ncell, const FState *st, const double
       pv = __fma_rn(beta, __fma_rn(-om, v[q], p[q]), r[q]);
     }
     p[q] = pv;
-    resid[q] = vf[q] > 0 ? (T)pv : (T)0;
+    resid[q] = fpint::positive(vf[q]) ? narrow_to<T>(pv) : (T)0;
   }
 }
 
@@ -300,16 +319,17 @@ __global__ void __launch_bounds__(kTPB) k_supdate(BlockList L, int ncell, FState
   pdl_enter();
   if (st->done) return;
   const double a = st->alpha;
-  double m[1] = {0.0};
+  unsigned long long mu = 0ull;  // max |s| as bit patterns (NaN-propagating)
   const int total = L.n * ncell;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     const long q = cell_of(L, ncell, it);
     const double sv = __fma_rn(-a, v[q], r[q]);
     s[q] = sv;
-    x[q] = __fma_rn(a, (double)phat[q], x[q]);
-    resid[q] = vf[q] > 0 ? (T)sv : (T)0;
-    m[0] = nmax(m[0], fabs(sv));
+    x[q] = __fma_rn(a, widen_from<TP>(phat[q]), x[q]);
+    resid[q] = fpint::positive(vf[q]) ? narrow_to<T>(sv) : (T)0;
+    mu = fpint::max_abs(mu, sv);
   }
+  double m[1] = {fpint::from_bits(mu)};
   grid_reduce<1>(m, 1u, partials, counter, EpiHalf{st});
 }
 
@@ -321,16 +341,18 @@ __global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, FState
   pdl_enter();
   if (st->done) return;
   const double om = st->omega;
+  unsigned long long mu = 0ull;  // max |r| as bit patterns (NaN-propagating)
   double m[2] = {0.0, 0.0};
   const int total = L.n * ncell;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     const long q = cell_of(L, ncell, it);
-    x[q] = __fma_rn(om, (double)shat[q], x[q]);
+    x[q] = __fma_rn(om, widen_from<T>(shat[q]), x[q]);
     const double rv = __fma_rn(-om, t[q], s[q]);
     r[q] = rv;
-    m[0] = nmax(m[0], fabs(rv));
+    mu = fpint::max_abs(mu, rv);
     m[1] = __fma_rn(rhat[q], rv, m[1]);
   }
+  m[0] = fpint::from_bits(mu);
   grid_reduce<2>(m, 1u, partials, counter, EpiEnd{st});
 }
 
@@ -355,7 +377,10 @@ __global__ void k_vc_out(BlockList L, int ncell, const FState *st, const T *corr
   const int total = L.n * ncell;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     const long q = cell_of(L, ncell, it);
-    out[q] = 0.0 + (double)corr[q];
+    if constexpr (sizeof(T) == 4)
+      out[q] = fpint::widen_plus0(corr[q]);
+    else
+      out[q] = 0.0 + corr[q];
   }
 }
 
@@ -498,6 +523,7 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
   if (MODE == 3 && !st->verify) return;
   if (MODE < 2 && st->done) return;
   double acc[2] = {0.0, 0.0};
+  unsigned long long mu = 0ull;  // MODE >= 2: max |y| as bit patterns
   const int total = L.n * t.ncell;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     int p, ci, ijk[3];
@@ -510,7 +536,7 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
     const double off = op_offdiag<ND, TX>(t, c, b, ft, ijk, ci, x, e);
     const double sc = S[q];
     double yv = __fma_rn((double)x[q], P[q], -off * sc);
-    if (MODE >= 2) yv = sc != 0.0 ? w[q] - yv : 0.0;
+    if (MODE >= 2) yv = fpint::positive(sc) ? w[q] - yv : 0.0;
     y[q] = yv;
     if (MODE == 3) y2[q] = yv;
     if (MODE == 0) acc[0] = __fma_rn(w[q], yv, acc[0]);
@@ -519,10 +545,11 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
       acc[1] = __fma_rn(yv, yv, acc[1]);
     }
     if (MODE >= 2) {
-      acc[0] = nmax(acc[0], fabs(yv));
+      mu = fpint::max_abs(mu, yv);
       acc[1] = __fma_rn(yv, yv, acc[1]);
     }
   }
+  if (MODE >= 2) acc[0] = fpint::from_bits(mu);
   if (MODE == 0) grid_reduce<2>(acc, 0u, partials, counter, EpiAlpha{st});
   if (MODE == 1) grid_reduce<2>(acc, 0u, partials, counter, EpiOmega{st});
   if (MODE == 2) grid_reduce<2>(acc, 1u, partials, counter, EpiInit{st});
@@ -556,34 +583,42 @@ __global__ void __launch_bounds__(kTPB) k_bottom_gemv(BottomDev bd, const T *__r
 // in-place Gauss-Jordan inversion step k of nmat matrices of order m at
 // offsets offs (no pivoting: the pinned, row-scaled level-1 operator has
 // positive pivots)
-__global__ void k_gj_save(int m, int k, int nmat, const long long *offs, const double *a, double *row, double *col) {
+__global__ void k_gj_save(int m, int k, int nmat, const long long *offs, const double *a, double *row, double *col,
+                          double *ipiv) {
   const long total = (long)nmat * m;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int mat = (int)(it / m), i = (int)(it - (long)mat * m);
     const double *am = a + offs[mat];
     row[it] = am[(long)k * m + i];
     col[it] = am[(long)i * m + k];
+    if (i == k) ipiv[mat] = 1.0 / am[(long)k * m + k];
   }
 }
-__global__ void k_gj_step(int m, int k, int nmat, const long long *offs, double *a, const double *row,
-                          const double *col) {
-  const long mm = (long)m * m, total = (long)nmat * mm;
-  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
-    const int mat = (int)(it / mm);
-    const long e = it - (long)mat * mm;
-    const int i = (int)(e / m), j = (int)(e - (long)i * m);
-    const double *rw = row + (long)mat * m, *cl = col + (long)mat * m;
-    const double piv = rw[k];
-    double *am = a + offs[mat];
-    double v;
-    if (i == k)
-      v = j == k ? 1.0 / piv : rw[j] / piv;
-    else
-      v = j == k ? -cl[i] / piv : am[e] - cl[i] * (rw[j] / piv);
-    am[e] = v;
+// one CTA per matrix row: every element uses the step's saved pivot row,
+// pivot column and pivot reciprocal (no division per element)
+__global__ void __launch_bounds__(kTPB) k_gj_step(int m, int k, int nmat, const long long *offs, double *a,
+                                                const double *row, const double *col, const double *ipiv) {
+  const long rows = (long)nmat * m;
+  for (long r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int mat = (int)(r / m), i = (int)(r - (long)mat * m);
+    const double *rw = row + (long)mat * m;
+    const double ip = ipiv[mat], ci = col[r];
+    double *ar = a + offs[mat] + (long)i * m;
+    if (i == k) {
+      for (int j = threadIdx.x; j < m; j += blockDim.x) ar[j] = j == k ? ip : rw[j] * ip;
+    } else {
+      const double f = ci * ip;
+      for (int j = threadIdx.x; j < m; j += blockDim.x) ar[j] = j == k ? -f : __fma_rn(-f, rw[j], ar[j]);
+    }
   }
 }
 // zero column col of the order-m matrix at off (a pinned Neumann cell)
+// FP32 copy of the bottom inverse
+__global__ void k_narrow(long long n, const double *a, float *b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
 __global__ void k_zero_col(long long off, int m, int col, double *a) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) a[off + (long)r * m + col] = 0.0;
 }
@@ -765,9 +800,80 @@ void MacGpu::refresh_fp32() {
 
 // Dense FP64 inverse of the level-1 operator (tower 1 = every level-1 block,
 // faces FINE_FINE or FINE_BC only), rows in tower order, cells in block order.
+// Level of the dense bottom solve.  Level 1 always works (it is uniform and
+// every level-1 face is a same-level or physical face); a finer level B
+// replaces the V-cycle's levels 1..B by one dense solve when tower B is one
+// uniform level (no coarse leaves, no coarse/fine faces) whose connected
+// components have at most kBottomMaxCells cells and whose inverses fit in
+// kBottomMaxBytes.  The auto choice takes the finest such level below the
+// finest level, with components of at most kBottomAutoCells[ndim] cells: the
+// dense product of a 4096-cell component streams a 64 MB FP32 matrix from
+// DRAM per V-cycle (and pushes the V-cycle's working set out of L2), which
+// in 2D costs as much as the cheap coarse levels it replaces (the 2D
+// benchmark workload: 4.48 vs 4.02 ms per solve), while in 3D it replaces
+// dearer levels and saves iterations (the elbow workload: 46.8 vs 53.5 ms,
+// 11 vs 13 iterations).
+constexpr int kBottomMaxCells = 4096;
+constexpr int kBottomAutoCells[4] = {0, 0, 1024, 4096};
+constexpr double kBottomMaxBytes = 1.0e9;
+int MacGpu::choose_bottom_level(std::string *why) const {
+  const int nd = tt_.ndim;
+  auto usable = [&](int B, int max_cells) {
+    const DevTower &tw = towers_[B];
+    const int n = (int)tw.blocks.size();
+    if (n == 0 || tw.end[B] - tw.begin[B] != n) return false;
+    std::vector<int> pos(tt_.num_blocks, -1);
+    for (int p = 0; p < n; p++) pos[tw.blocks[p]] = p;
+    std::vector<int> comp(n, -1);
+    double bytes = 0.0;
+    for (int p0 = 0; p0 < n; p0++) {
+      if (comp[p0] >= 0) continue;
+      std::vector<int> stack{p0};
+      comp[p0] = p0;
+      long cells = 0;
+      while (!stack.empty()) {
+        const int p = stack.back();
+        stack.pop_back();
+        cells += ncell_;
+        for (int f = 0; f < 2 * nd; f++) {
+          const int nbr = tt_.neighbor[tw.blocks[p] * 6 + f];
+          if (nbr <= kPhysBndry) continue;
+          if (nbr < 0 || pos[nbr] < 0) return false;  // coarse/fine face
+          if (comp[pos[nbr]] < 0) {
+            comp[pos[nbr]] = p0;
+            stack.push_back(pos[nbr]);
+          }
+        }
+      }
+      if (B > 1 && cells > max_cells) return false;
+      bytes += 8.0 * (double)cells * (double)cells;
+    }
+    return bytes <= (B > 1 ? kBottomMaxBytes : 4.0e9);
+  };
+  if (prm_.bottom_level >= 1) {
+    const int B = std::min(prm_.bottom_level, std::max(1, finest_ - 1));
+    if (!usable(B, kBottomMaxCells)) {
+      *why = "bottom_level " + std::to_string(B) + ": tower is not one uniform level small enough for the dense solve";
+      return -1;
+    }
+    return B;
+  }
+  int best = 1;
+  for (int B = 2; B < finest_ && usable(B, kBottomAutoCells[nd]); B++) best = B;
+  return best;
+}
+
 void MacGpu::build_bottom() {
   const int nd = tt_.ndim, nb = tt_.nb;
-  const std::vector<int> &B1 = towers_[1].blocks;
+  std::string why;
+  const int LB = choose_bottom_level(&why);
+  if (LB < 1) {
+    fail(why);
+    return;
+  }
+  bot_level_ = LB;
+  bot_param_ = prm_.bottom_level;
+  const std::vector<int> &B1 = towers_[LB].blocks;
   const int nblk1 = (int)B1.size();
   n_bot_ = nblk1 * ncell_;
   if (n_bot_ == 0) return;
@@ -791,7 +897,7 @@ void MacGpu::build_bottom() {
         const int nbr = tt_.neighbor[B1[p] * 6 + f];
         if (nbr < 0) continue;
         if (pos1[nbr] < 0) {
-          fail("level-1 neighbour outside tower 1");
+          fail("bottom-level neighbour outside the bottom tower");
           return;
         }
         if (bcomp[pos1[nbr]] < 0) {
@@ -819,7 +925,7 @@ void MacGpu::build_bottom() {
     }
   }
   if ((double)tot * 8 > 4.0e9 || (double)max_n * 8 > 200.0 * 1024) {
-    fail("level-1 problem too large for the dense bottom solve");
+    fail("bottom-level problem too large for the dense bottom solve");
     return;
   }
   std::vector<double> A((size_t)tot, 0.0);
@@ -947,34 +1053,49 @@ void MacGpu::build_bottom() {
     CK_(cudaMalloc(&d_offs, nmat * sizeof(long long)));
     CK_(cudaMalloc(&row, (size_t)nmat * m * sizeof(double)));
     CK_(cudaMalloc(&col, (size_t)nmat * m * sizeof(double)));
+    double *ipiv = nullptr;
+    CK_(cudaMalloc(&ipiv, nmat * sizeof(double)));
     CK_(cudaMemcpyAsync(d_offs, offs.data(), nmat * sizeof(long long), cudaMemcpyHostToDevice, stream_));
-    const long work = (long)nmat * m * m;
+    const int step_grid = (int)std::min<long>((long)nmat * m, 152 * 16);
     for (int k = 0; k < m; k++) {
-      k_gj_save<<<ew_grid((long)nmat * m), kTPB, 0, stream_>>>(m, k, nmat, d_offs, d_binv_, row, col);
-      k_gj_step<<<ew_grid(work), kTPB, 0, stream_>>>(m, k, nmat, d_offs, d_binv_, row, col);
+      k_gj_save<<<ew_grid((long)nmat * m), kTPB, 0, stream_>>>(m, k, nmat, d_offs, d_binv_, row, col, ipiv);
+      k_gj_step<<<step_grid, kTPB, 0, stream_>>>(m, k, nmat, d_offs, d_binv_, row, col, ipiv);
     }
     CK_(cudaStreamSynchronize(stream_));
     cudaFree(d_offs);
     cudaFree(row);
     cudaFree(col);
+    cudaFree(ipiv);
   }
   for (int r0 : pins) {
     const int c = rcomp[r0];
     k_zero_col<<<(comp_n[c] + kTPB - 1) / kTPB, kTPB, 0, stream_>>>(comp_off[c], comp_n[c], r0 - comp_row0[c], d_binv_);
   }
+  // an FP32 copy for the FP32 V-cycle when the bottom is above level 1: its
+  // product is then large (up to kBottomMaxCells^2 per component) and FP64
+  // multiply-adds run at 1/64 of the FP32 rate here
+  if (LB > 1) {
+    if (cudaMalloc(&d_binv32_, (size_t)tot * sizeof(float)) != cudaSuccess) {
+      d_binv32_ = nullptr;
+      fail("out of device memory (bottom solve)");
+      return;
+    }
+    k_narrow<<<ew_grid(tot), kTPB, 0, stream_>>>(tot, d_binv_, d_binv32_);
+  }
   CK_(cudaStreamSynchronize(stream_));
   bot_ = BottomDev{d_binv_, d_bot_blocks_, d_comp_row0_, d_comp_n_, d_comp_off_, d_tile_comp_, d_tile_row0_,
-                   (int)tile_comp.size(), ncell_, max_n};
+                   (int)tile_comp.size(), ncell_, max_n, d_binv32_};
   n_pins_ = (int)pins.size();
   n_bot_comp_ = nc;
   bottom_ready_ = true;
 }
 
 void MacGpu::bottom_free() {
-  for (void *p : {(void *)d_binv_, (void *)d_bot_blocks_, (void *)d_comp_row0_, (void *)d_comp_n_,
+  for (void *p : {(void *)d_binv32_, (void *)d_binv_, (void *)d_bot_blocks_, (void *)d_comp_row0_, (void *)d_comp_n_,
                   (void *)d_comp_off_, (void *)d_tile_comp_, (void *)d_tile_row0_})
     if (p) cudaFree(p);
   d_binv_ = nullptr;
+  d_binv32_ = nullptr;
   d_bot_blocks_ = d_comp_row0_ = d_comp_n_ = d_tile_comp_ = d_tile_row0_ = nullptr;
   d_comp_off_ = nullptr;
   bot_ = BottomDev{};
@@ -985,12 +1106,13 @@ void MacGpu::bottom_free() {
 template <typename T>
 void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *out) {
   const int *guard = &d_st_->done;
-  for (int l = L; l >= 2; l--) {
+  const int LB = bot_level_;
+  for (int l = L; l >= LB + 1; l--) {
     if (l - 1 >= tt_.max_level || levels_[l - 1].n == 0 || levels_[l].n == 0) continue;
     launch_restrict<T>(topo_, c, nonleaf_list(l - 1), resid, guard, stream_, prm_.pdl != 0);
   }
   bottom_launch<T>(resid, corr);
-  for (int l = 2; l <= L; l++) {
+  for (int l = LB + 1; l <= L; l++) {
     if (levels_[l].n == 0) continue;
     // the level's own sublevel of tower l holds every block of the level, so
     // the prolongation and the red sweep that follows it can be one launch
@@ -1191,10 +1313,13 @@ int MacGpu::cg_solve_enqueue() {
   ensure_fast_buffers();
   // coefficients changed since sayaka_mac_prepare: the fast-path data and the
   // graph must be rebuilt first
-  if (!err_.empty() || !bottom_ready_ || coef_version_ != fast_coef_version_) return -1;
+  if (!err_.empty() || !bottom_ready_ || coef_version_ != fast_coef_version_ || bot_param_ != prm_.bottom_level)
+    return -1;
   if (prm_.graph && graph_stale())
     return -1;
-  if (prm_.vcycle_kernel && (program_npost_ != prm_.n_post || program_order_ != prm_.sublevel_order)) return -1;
+  if (prm_.vcycle_kernel && (program_npost_ != prm_.n_post || program_order_ != prm_.sublevel_order ||
+                             program_bot_ != bot_level_))
+    return -1;
   return enqueue_solve();
 }
 
@@ -1271,11 +1396,17 @@ int MacGpu::prepare_device() {
     build_bottom();
     fast_coef_version_ = coef_version_;
     if (!err_.empty()) return -1;
+  } else if (bot_param_ != prm_.bottom_level) {  // another bottom level asked for
+    CKR_(cudaStreamSynchronize(stream_), -1);
+    drop_graph();
+    build_bottom();
+    if (!err_.empty()) return -1;
   }
   tune_smoother(prm_.precision);
   if (learned_active()) learned_prepare();
   if (!err_.empty()) return -1;
-  if (prm_.vcycle_kernel && (program_npost_ != prm_.n_post || program_order_ != prm_.sublevel_order))
+  if (prm_.vcycle_kernel && (program_npost_ != prm_.n_post || program_order_ != prm_.sublevel_order ||
+                             program_bot_ != bot_level_))
     build_vcycle_program();
   if (prm_.graph && graph_stale())
     capture_loop(prm_.precision);
@@ -1345,6 +1476,44 @@ int MacGpu::enqueue_kernel(int which, int L) {
     return -1;
   }
   return err_.empty() ? 0 : -1;
+}
+
+// self-test of the integer-pipe conversions against the hardware ones
+__global__ void k_fp_selftest(int n, const double *d, const float *f, float *nar, float *nar_hw, double *wid,
+                              double *wid_hw, double *wid0, double *wid0_hw) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    nar[i] = fpint::narrow(d[i]);
+    nar_hw[i] = (float)d[i];
+    wid[i] = fpint::widen(f[i]);
+    wid_hw[i] = (double)f[i];
+    wid0[i] = fpint::widen_plus0(f[i]);
+    wid0_hw[i] = 0.0 + (double)f[i];
+  }
+}
+
+int fp_selftest(const double *d, const float *f, int n, float *nar, float *nar_hw, double *wid, double *wid_hw,
+                double *wid0, double *wid0_hw) {
+  if (n <= 0) return 0;
+  unsigned char *buf = nullptr;
+  const size_t fb = (size_t)n * sizeof(float), db = (size_t)n * sizeof(double);
+  if (cudaMalloc(&buf, 3 * fb + 5 * db) != cudaSuccess) return 2;
+  double *dd = (double *)buf, *w = dd + n, *whw = w + n, *w0 = whw + n, *w0hw = w0 + n;
+  float *ff = (float *)(w0hw + n), *nr = ff + n, *nrhw = nr + n;
+  cudaMemcpy(dd, d, db, cudaMemcpyHostToDevice);
+  cudaMemcpy(ff, f, fb, cudaMemcpyHostToDevice);
+  k_fp_selftest<<<std::min((n + 255) / 256, 1024), 256>>>(n, dd, ff, nr, nrhw, w, whw, w0, w0hw);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) {
+    cudaMemcpy(nar, nr, fb, cudaMemcpyDeviceToHost);
+    cudaMemcpy(nar_hw, nrhw, fb, cudaMemcpyDeviceToHost);
+    cudaMemcpy(wid, w, db, cudaMemcpyDeviceToHost);
+    cudaMemcpy(wid_hw, whw, db, cudaMemcpyDeviceToHost);
+    cudaMemcpy(wid0, w0, db, cudaMemcpyDeviceToHost);
+    cudaMemcpy(wid0_hw, w0hw, db, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(buf);
+  return e == cudaSuccess ? 0 : 2;
 }
 
 }  // namespace sayaka_gb300

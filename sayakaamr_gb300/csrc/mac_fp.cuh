@@ -1,0 +1,73 @@
+// FP64 bookkeeping on the integer pipe.
+//
+// GB300 issues FP64 at 2 operations per SM and clock, and its FP64 pipe
+// also carries FP64 compares, min/max and the FP32 <-> FP64 conversions.
+// The BiCGSTAB vector kernels of the device solve are bound by that pipe, so
+// every operation here that only moves or orders bits is done on 32/64-bit
+// integers instead, with results identical to the FP64 instructions:
+//   * non-negative doubles order like their bit patterns read as integers,
+//     and a NaN (all-ones exponent, non-zero mantissa) orders above +inf, so
+//     the max of |v| over bit patterns is the NaN-propagating max of |v|;
+//   * float -> double is exact: rebias the exponent, widen the mantissa;
+//   * double -> float rounds the 52-bit mantissa to 23 bits, to nearest
+//     with ties to even (IEEE 754 roundTiesToEven), for results in the
+//     normal float range; zeros are exact, everything else (float
+//     denormals, overflow, inf, NaN) goes through the hardware conversion.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace sayaka_gb300 {
+namespace fpint {
+
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+
+// running max of |v| as bit patterns (start from 0 = +0.0)
+__device__ __forceinline__ unsigned long long max_abs(unsigned long long m, double v) {
+  const unsigned long long u = abs_bits(v);
+  return u > m ? u : m;
+}
+
+__device__ __forceinline__ double from_bits(unsigned long long u) { return __longlong_as_double((long long)u); }
+
+// v > 0 for v that is never a NaN (volume fractions, operator factors):
+// positive doubles, and only they, have positive bit patterns as int64
+__device__ __forceinline__ bool positive(double v) { return __double_as_longlong(v) > 0; }
+
+// exact float -> double
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e != 0u && e != 0xffu)
+    return from_bits(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29));
+  if ((u & 0x7fffffffu) == 0u) return from_bits(sign);
+  return (double)f;  // denormal, inf, NaN
+}
+
+// 0.0 + (double)f: as widen, with -0 turned into +0
+__device__ __forceinline__ double widen_plus0(float f) {
+  return (__float_as_uint(f) & 0x7fffffffu) == 0u ? 0.0 : widen(f);
+}
+
+// double -> float, round to nearest, ties to even
+__device__ __forceinline__ float narrow(double d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
+  const int e = (int)((u >> 52) & 0x7ffu);
+  // normal float results: biased float exponent e - 896 in [1, 254]
+  if (e >= 897 && e <= 1150) {
+    const unsigned long long m = u & 0xfffffffffffffull;
+    const unsigned long long rem = m & 0x1fffffffull;  // the 29 bits dropped
+    unsigned r = ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29);
+    if (rem > 0x10000000ull || (rem == 0x10000000ull && (r & 1u))) r += 1u;  // carry may reach the exponent
+    return __uint_as_float(sign | r);  // a carry into exponent 255 is +-inf, as IEEE rounding gives
+  }
+  if ((u & 0x7fffffffffffffffull) == 0ull) return __uint_as_float(sign);
+  return (float)d;
+}
+
+}  // namespace fpint
+}  // namespace sayaka_gb300

@@ -37,6 +37,8 @@ struct SolverParams {
   int smooth_variant = -1;    // device smoother launch bounds: -1 autotune at prepare, else variant index
   int learned = 0;            // device path, FP32 V-cycle: apply the trained block correction
   int fuse_prolong = 1;       // device path: prolongation fused with the first red sweep of its level
+  int bottom_level = 0;       // device path: level of the dense bottom solve; 0 = the coarsest level whose
+                              // tower is one uniform level of at most kBottomMaxCells cells per component
   int sublevel_order = 1;     // device V-cycle smoothing order over a tower's sublevels: 0 = finest to
                               // coarsest, red then black per sublevel (the reference's); 1 = one launch per
                               // colour and level parity (sublevels two levels apart never touch)
@@ -95,6 +97,7 @@ class MacGpu {
   int enqueue_kernel(int which, int L);
   int tower_size(int L, int sublevel) const;
   int tuned_smoother(int precision, float *us, int n) const;
+  int bottom_level() const { return bottom_ready_ ? bot_level_ : -1; }
 
   // building blocks, exposed for parity tests (compact arrays, all blocks)
   void apply(int L, const double *x_all, double *y_all);
@@ -283,6 +286,9 @@ class MacGpu {
       *d_tile_row0_ = nullptr;
   long long *d_comp_off_ = nullptr;
   BottomDev bot_{};
+  float *d_binv32_ = nullptr;
+  int bot_level_ = 1, bot_param_ = -1, program_bot_ = -1;
+  int choose_bottom_level(std::string *why) const;
   int n_bot_ = 0, n_pins_ = 0, n_bot_comp_ = 0;
   void bottom_free();
   void drop_graph();
@@ -308,5 +314,10 @@ class MacGpu {
   int kernels_per_iteration() const { return kernels_per_iter_; }
   static constexpr int kPrologueKernels = 3, kEpilogueKernels = 1;
 };
+
+// integer-pipe precision conversions of the vector kernels against the
+// hardware conversions, on the current device (0 ok, 2 CUDA error)
+int fp_selftest(const double *d, const float *f, int n, float *nar, float *nar_hw, double *wid, double *wid_hw,
+                double *wid0, double *wid0_hw);
 
 }  // namespace sayaka_gb300

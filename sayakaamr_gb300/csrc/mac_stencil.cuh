@@ -396,19 +396,86 @@ __device__ __forceinline__ void prolong_cell(const Topo &t, const Coef<T> &c, in
 // rows [row0, row0 + 8) of one component of the bottom solve:
 // corr = Binv_c * resid_c, one warp per row; rv: shared memory for the
 // component's residual (max_n doubles); every thread of the CTA calls it
+// a component's residual (rows r0 .. r0+m, whole blocks of ncell rows) into
+// shared memory: eight block ids loaded at once, then their cells, so that
+// the loads are in flight together instead of one dependent pair per cell
+template <typename T, bool CG, typename R>
+__device__ __forceinline__ void bottom_gather(const BottomDev &bd, int r0, int m, const T *resid, R *out) {
+  const int nc = bd.ncell, nblk = m / nc;
+  const int *bl = bd.blocks + r0 / nc;
+  for (int p0 = 0; p0 < nblk; p0 += 8) {
+    int bb[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) bb[u] = p0 + u < nblk ? bl[p0 + u] : -1;
+    for (int ci = threadIdx.x; ci < nc; ci += blockDim.x) {
+      T v[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) v[u] = bb[u] >= 0 ? ld<CG>(&resid[(long)bb[u] * nc + ci]) : (T)0;
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+        if (bb[u] >= 0) out[(p0 + u) * nc + ci] = (R)v[u];
+    }
+  }
+}
+
 template <typename T, bool CG = false>
 __device__ __forceinline__ void bottom_tile(const BottomDev &bd, int tile, const T *resid, T *corr, double *rv) {
   const int c = bd.tile_comp[tile], r0 = bd.comp_row0[c], m = bd.comp_n[c], nc = bd.ncell;
-  for (int j = threadIdx.x; j < m; j += blockDim.x) {
-    const int g = r0 + j;
-    rv[j] = (double)ld<CG>(&resid[(long)bd.blocks[g / nc] * nc + g % nc]);
+  if (sizeof(T) == 4 && bd.binv32) {  // FP32 inverse, FP32 accumulation
+    float *rf = reinterpret_cast<float *>(rv);
+    bottom_gather<T, CG>(bd, r0, m, resid, rf);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, row = bd.tile_row0[tile] + (threadIdx.x >> 5);
+    if ((threadIdx.x >> 5) < kBottomTileRows && row < m) {
+      const float4 *a4 = reinterpret_cast<const float4 *>(bd.binv32 + bd.comp_off[c] + (long long)row * m);
+      const float4 *r4 = reinterpret_cast<const float4 *>(rf);
+      float s = 0.f;
+      if ((m & 3) == 0 && ((bd.comp_off[c] + (long long)row * m) & 3) == 0) {
+        // four independent float4 loads in flight per lane
+        const int q4 = m >> 2;
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+        int j = lane;
+        for (; j + 96 < q4; j += 128) {
+          const float4 a0 = a4[j], a1 = a4[j + 32], a2 = a4[j + 64], a3 = a4[j + 96];
+          const float4 x0 = r4[j], x1 = r4[j + 32], x2 = r4[j + 64], x3 = r4[j + 96];
+          s0 = fmaf(a0.w, x0.w, fmaf(a0.z, x0.z, fmaf(a0.y, x0.y, fmaf(a0.x, x0.x, s0))));
+          s1 = fmaf(a1.w, x1.w, fmaf(a1.z, x1.z, fmaf(a1.y, x1.y, fmaf(a1.x, x1.x, s1))));
+          s2 = fmaf(a2.w, x2.w, fmaf(a2.z, x2.z, fmaf(a2.y, x2.y, fmaf(a2.x, x2.x, s2))));
+          s3 = fmaf(a3.w, x3.w, fmaf(a3.z, x3.z, fmaf(a3.y, x3.y, fmaf(a3.x, x3.x, s3))));
+        }
+        for (; j < q4; j += 32) {
+          const float4 a0 = a4[j], x0 = r4[j];
+          s0 = fmaf(a0.w, x0.w, fmaf(a0.z, x0.z, fmaf(a0.y, x0.y, fmaf(a0.x, x0.x, s0))));
+        }
+        s = (s0 + s1) + (s2 + s3);
+      } else {
+        const float *a = bd.binv32 + bd.comp_off[c] + (long long)row * m;
+        for (int j = lane; j < m; j += 32) s = fmaf(a[j], rf[j], s);
+      }
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      const int g = r0 + row;
+      if (lane == 0) corr[(long)bd.blocks[g / nc] * nc + g % nc] = (T)s;
+    }
+    __syncthreads();
+    return;
   }
+  bottom_gather<T, CG>(bd, r0, m, resid, rv);
   __syncthreads();
   const int lane = threadIdx.x & 31, row = bd.tile_row0[tile] + (threadIdx.x >> 5);
   if ((threadIdx.x >> 5) < kBottomTileRows && row < m) {
     const double *a = bd.binv + bd.comp_off[c] + (long long)row * m;
-    double s = 0.0;
-    for (int j = lane; j < m; j += 32) s += a[j] * rv[j];
+    // four independent loads in flight per lane, four partial sums
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int j = lane;
+    for (; j + 96 < m; j += 128) {
+      const double a0 = a[j], a1 = a[j + 32], a2 = a[j + 64], a3 = a[j + 96];
+      s0 += a0 * rv[j];
+      s1 += a1 * rv[j + 32];
+      s2 += a2 * rv[j + 64];
+      s3 += a3 * rv[j + 96];
+    }
+    for (; j < m; j += 32) s0 += a[j] * rv[j];
+    double s = (s0 + s1) + (s2 + s3);
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     const int g = r0 + row;
     if (lane == 0) corr[(long)bd.blocks[g / nc] * nc + g % nc] = (T)s;

@@ -130,13 +130,14 @@ void MacGpu::build_vcycle_program() {
     p.ia = bl.ia;
     v.push_back(p);
   };
-  for (int l = L; l >= 2; l--) {
+  const int LB = bot_level_;
+  for (int l = L; l >= LB + 1; l--) {
     if (l - 1 >= tt_.max_level || levels_[l - 1].n == 0 || levels_[l].n == 0) continue;
     push(kPhaseRestrict, 0, nonleaf_list(l - 1));
   }
   n_down_ = (int)v.size();
   push(kPhaseBottom, 0, BlockList{nullptr, nullptr, 0});
-  for (int l = 2; l <= L; l++) {
+  for (int l = LB + 1; l <= L; l++) {
     if (levels_[l].n == 0) continue;
     push(kPhaseProlong, 0, level_list(l));
     for (int s = 0; s < prm_.n_post; s++) {
@@ -165,6 +166,7 @@ void MacGpu::build_vcycle_program() {
   }
   program_npost_ = prm_.n_post;
   program_order_ = prm_.sublevel_order;
+  program_bot_ = bot_level_;
 }
 
 template <typename T>

@@ -161,3 +161,30 @@ def test_sublevel_orders_both_converge(name):
         its.append(info["iterations"])
     print(name, "iterations per-sublevel order %d, parity order %d" % tuple(its))
     assert abs(its[0] - its[1]) <= max(3, its[0] // 4), its
+
+
+@pytest.mark.parametrize("name", ["config2", "config5"])
+def test_bottom_level_above_one(name):
+    """the dense bottom solve on a finer uniform level (level 2 on both
+    workloads: asked for on config2, chosen automatically on the 3D elbow)
+    replaces the V-cycle's coarsest levels; the solve reaches the
+    criterion, in no more iterations than with the level-1 bottom"""
+    from sayakaamr_gb300 import workloads
+    p = workloads.CONFIGS[name]() if name != "config5" else workloads.config5(max_level=5)
+    S = workloads.make_solver(p)
+    its = {}
+    for lvl in (1, 2 if name == "config2" else 0):
+        S.set_zero_sol()
+        S.set_params(tol_rel=1e-8, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=1, bottom=1,
+                     bottom_level=lvl)
+        info = S.cg_solve()
+        assert info["status"] == 0, (lvl, info)
+        assert info["rnorm"] < 1e-8 * info["rnorm0"]
+        its[lvl] = (info["iterations"], S.bottom_level())
+    k = 2 if name == "config2" else 0
+    print(name, "bottom level 1: %d iterations; level %d: %d" % (its[1][0], its[k][1], its[k][0]))
+    assert its[1][1] == 1 and its[k][1] == 2
+    assert its[k][0] <= its[1][0]
+    S.set_params(bottom_level=0)
+    S.prepare()
+    assert S.bottom_level() == (1 if name == "config2" else 2)
