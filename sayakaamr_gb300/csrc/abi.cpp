@@ -3,8 +3,12 @@
 // compact device layout, validates inputs and turns failures into status codes.
 #include <cuda_runtime.h>
 
+#include <atomic>
+#include <condition_variable>
 #include <cstring>
 #include <exception>
+#include <functional>
+#include <mutex>
 #include <memory>
 #include <algorithm>
 #include <string>
@@ -81,24 +85,83 @@ struct Layout {
   bool ok() const { return ncomp >= 1 && comp >= 0 && comp < ncomp && g >= 0; }
 };
 
+// Persistent host workers for the TreeData <-> compact copies: created on
+// first use and reused by every call (spawning threads per call costs as
+// much as copying a few MB); one job at a time, the caller takes part.
+class HostPool {
+ public:
+  static HostPool &get() {
+    static HostPool *pool = new HostPool();  // never destroyed: workers end with the process
+    return *pool;
+  }
+  int size() const { return (int)workers_.size() + 1; }
+  // task(i) for i in [0, n), on the workers and the calling thread
+  void run(int n, const std::function<void(int)> &task) {
+    std::lock_guard<std::mutex> one_job(job_mu_);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      task_ = &task;
+      n_ = n;
+      next_.store(0);
+      busy_ = (int)workers_.size();
+      gen_++;
+    }
+    cv_.notify_all();
+    drain();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return busy_ == 0; });
+    task_ = nullptr;
+  }
+
+ private:
+  HostPool() {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nw = (int)std::min<unsigned>(16u, hw) - 1;
+    for (int i = 0; i < nw; i++) workers_.emplace_back([this] { loop(); });
+    for (auto &w : workers_) w.detach();
+  }
+  void drain() {
+    for (int i = next_.fetch_add(1); i < n_; i = next_.fetch_add(1)) (*task_)(i);
+  }
+  void loop() {
+    unsigned seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+      }
+      drain();
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--busy_ == 0) done_cv_.notify_one();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex job_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int)> *task_ = nullptr;
+  std::atomic<int> next_{0};
+  int n_ = 0, busy_ = 0;
+  unsigned gen_ = 0;
+};
+
 // valid cells (or faces) of every block: TreeData layout <-> compact
-// fn(b0, b1) over block ranges, on up to 16 host threads for large fields
-// (the row copies of a 16M-cell field take tens of milliseconds on one core)
+// fn(b0, b1) over block ranges; fields from 256 KB up are split over the
+// host pool (the row copies of a 16M-cell field take tens of milliseconds
+// on one core, a 0.4M-cell field a few hundred microseconds)
 template <class F>
 void for_blocks(int nblocks, size_t bytes, F &&fn) {
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const int nt = bytes < (4u << 20) ? 1 : (int)std::min<unsigned>(16u, hw);
-  if (nt <= 1 || nblocks < 2 * nt) {
+  HostPool &pool = HostPool::get();
+  const int nt = bytes < (256u << 10) ? 1 : std::min(pool.size() * 2, std::max(1, nblocks / 16));
+  if (nt <= 1) {
     fn(0, nblocks);
     return;
   }
-  std::vector<std::thread> th;
   const int per = (nblocks + nt - 1) / nt;
-  for (int t = 0; t < nt; t++) {
+  pool.run(nt, [&](int t) {
     const int b0 = t * per, b1 = std::min(nblocks, b0 + per);
-    if (b0 < b1) th.emplace_back([&fn, b0, b1] { fn(b0, b1); });
-  }
-  for (auto &x : th) x.join();
+    if (b0 < b1) fn(b0, b1);
+  });
 }
 
 void pack(const Layout &L, int nblocks, const double *src, double *dst) {
