@@ -31,9 +31,13 @@ namespace {
 constexpr int kTPB = 256;
 constexpr int kMaxRedBlocks = 152 * 4;
 
+// grid of the kernels that end in a grid reduction: every CTA adds one
+// same-address atomic to the reduction's tail, so latency-bound sizes (under
+// 2M cells) take half the CTAs
 inline int red_grid(long work) {
   long g = (work + kTPB - 1) / kTPB;
-  return (int)std::max<long>(1, std::min<long>(g, kMaxRedBlocks));
+  const long cap = work < (1l << 21) ? kMaxRedBlocks / 2 : kMaxRedBlocks;
+  return (int)std::max<long>(1, std::min<long>(g, cap));
 }
 inline int ew_grid(long work) {
   long g = (work + kTPB - 1) / kTPB;
@@ -62,25 +66,39 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, d
   __shared__ double sh[NV][kTPB / 32];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // the kTPB / 32 warp results of sh combined by warp 0 (same tree order
+  // for every CTA and every launch)
+  auto warp0 = [&](double (&r)[NV]) {
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+      double x = lane < kTPB / 32 ? sh[i][lane] : 0.0;
+      for (int o = (kTPB / 64); o > 0; o >>= 1) {
+        const double y = __shfl_xor_sync(0xffffffffu, x, o);
+        x = ((maxmask >> i) & 1) ? nmax(x, y) : x + y;
+      }
+      r[i] = x;
+    }
+  };
 #pragma unroll
   for (int i = 0; i < NV; i++) {
     const double r = ((maxmask >> i) & 1) ? wmax(v[i]) : wsum(v[i]);
     if (lane == 0) sh[i][w] = r;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (w == 0) {
+    double r[NV];
+    warp0(r);
+    if (lane == 0) {
 #pragma unroll
-    for (int i = 0; i < NV; i++) {
-      double r = 0.0;
-      for (int q = 0; q < kTPB / 32; q++) r = ((maxmask >> i) & 1) ? nmax(r, sh[i][q]) : r + sh[i][q];
-      partials[blockIdx.x * NV + i] = r;
+      for (int i = 0; i < NV; i++) partials[blockIdx.x * NV + i] = r[i];
+      // release the partials, acquire everyone else's if this CTA is last
+      unsigned old;
+      asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(old) : "l"(counter) : "memory");
+      last = old == gridDim.x - 1;
     }
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
   if (!last) return;
-  __threadfence();
   double acc[NV];
 #pragma unroll
   for (int i = 0; i < NV; i++) acc[i] = 0.0;
@@ -98,16 +116,13 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, d
     if (lane == 0) sh[i][w] = r;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (w == 0) {
     double fin[NV];
-#pragma unroll
-    for (int i = 0; i < NV; i++) {
-      double r = 0.0;
-      for (int q = 0; q < kTPB / 32; q++) r = ((maxmask >> i) & 1) ? nmax(r, sh[i][q]) : r + sh[i][q];
-      fin[i] = r;
+    warp0(fin);
+    if (lane == 0) {
+      epi(fin);
+      *counter = 0;
     }
-    epi(fin);
-    *counter = 0;
   }
 }
 
