@@ -507,14 +507,14 @@ __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &
     const int fx = face_index(d, ijk, s, nb);
     if (!bnd) {
       const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
-      off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], (double)x[cb + ci + (s ? stride : -stride)], off);
+      off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], widen_from<TX>(x[cb + ci + (s ? stride : -stride)]), off);
     } else {
       const int ty = face_type_of(ft, f);
       if (ty == 0)
-        off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], (double)same_level_ghost<TX, false>(t, b, f, ijk, x, hx),
+        off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], widen_from<TX>(same_level_ghost<TX, false>(t, b, f, ijk, x, hx)),
                        off);
       else if (ty == 2)
-        off = __fma_rn(cf_coef(c, t, b, d, fx, 1.5), (double)fine_crse_ghost<TX, ND, false>(t, b, f, ijk, x, hx),
+        off = __fma_rn(cf_coef(c, t, b, d, fx, 1.5), widen_from<TX>(fine_crse_ghost<TX, ND, false>(t, b, f, ijk, x, hx)),
                        off);
       else if (ty == 3)
         off += crse_fine_sum<double, ND, false>(t, c, b, f, ijk, x, hx);
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
     const long q = (long)b * t.ncell + ci;
     const double off = op_offdiag<ND, TX>(t, c, b, ft, ijk, ci, x, e);
     const double sc = S[q];
-    double yv = __fma_rn((double)x[q], P[q], -off * sc);
+    double yv = __fma_rn(widen_from<TX>(x[q]), P[q], -off * sc);
     if (MODE >= 2) yv = fpint::positive(sc) ? w[q] - yv : 0.0;
     y[q] = yv;
     if (MODE == 3) y2[q] = yv;
@@ -1202,21 +1202,37 @@ void MacGpu::precondition(int L, T *resid, T *corr, const Coef<T> &c, double *ou
   }
 }
 
+// FP32 V-cycle output read by the FP64 kernels in place (its exact widening
+// is integer work there) up to this many tower cells, where the solve is
+// latency-bound and the two widening launches per iteration cost more;
+// larger towers widen it once into FP64 phat / shat
+constexpr long kDirectF32Cells = 1l << 21;
+
 template <typename T>
 void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
+  const long w = (long)tower_list(finest_).n * ncell_;
+  if constexpr (sizeof(T) == 4) {
+    if (!learned_active() && w < kDirectF32Cells) {
+      iteration_body<T, float>(resid, corr, c, corr, corr, nullptr, nullptr);
+      return;
+    }
+    iteration_body<T, double>(resid, corr, c, vec_[kPHAT], vec_[kSHAT], vec_[kPHAT], vec_[kSHAT]);
+  } else {
+    iteration_body<T, double>(resid, corr, c, corr, corr, nullptr, nullptr);
+  }
+}
+
+// One BiCGSTAB iteration.  The V-cycle's output PH (the first
+// preconditioner application) is consumed by the operator and the x update
+// before the second application overwrites it (SH); out_p / out_s, when
+// given, receive the output widened to FP64 (PH / SH point there).
+template <typename T, typename TO>
+void MacGpu::iteration_body(T *resid, T *corr, const Coef<T> &c, const TO *PH, const TO *SH, double *out_p,
+                            double *out_s) {
   const int L = finest_;
   BlockList TL = tower_list(L);
   const long w = (long)TL.n * ncell_;
-  // An FP64 V-cycle's output (corr) serves as phat and later as shat: phat
-  // is consumed before the second V-cycle overwrites corr.  An FP32 V-cycle's
-  // output is widened once into FP64 phat / shat (widening inside the FP64
-  // kernels would cost one FP64-pipe conversion per neighbour read).
   double *R = vec_[kR], *RHAT = vec_[kRHAT], *P = vec_[kP], *S = vec_[kS];
-  constexpr bool widen = sizeof(T) == 4;
-  using TO = typename std::conditional<widen, double, T>::type;
-  double *out_p = widen ? vec_[kPHAT] : nullptr, *out_s = widen ? vec_[kSHAT] : nullptr;
-  const TO *PH = widen ? reinterpret_cast<const TO *>(vec_[kPHAT]) : reinterpret_cast<const TO *>(corr);
-  const TO *SH = widen ? reinterpret_cast<const TO *>(vec_[kSHAT]) : reinterpret_cast<const TO *>(corr);
   double *V = vec_[kV], *Tt = vec_[kT], *X = vec_[kX];
   const bool pdl = prm_.pdl != 0;
   launch_k(pdl, k_pupdate<T>, ew_grid(w), kTPB, 0, stream_, TL, ncell_, (const FState *)d_st_, (const double *)R, P,

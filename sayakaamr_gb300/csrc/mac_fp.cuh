@@ -69,5 +69,17 @@ __device__ __forceinline__ float narrow(double d) {
   return (float)d;
 }
 
+// exact conversion To <- From between float and double on the integer pipe
+// (narrowing rounds to nearest even), identity otherwise
+template <typename To, typename From>
+__device__ __forceinline__ To cvt(From v) {
+  if constexpr (sizeof(To) == 8 && sizeof(From) == 4)
+    return widen(v);
+  else if constexpr (sizeof(To) == 4 && sizeof(From) == 8)
+    return narrow(v);
+  else
+    return (To)v;
+}
+
 }  // namespace fpint
 }  // namespace sayaka_gb300

@@ -211,6 +211,8 @@ class MacGpu {
   void vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *out);
   template <typename T>
   void iteration_device(T *resid, T *corr, const Coef<T> &c);
+  template <typename T, typename TO>
+  void iteration_body(T *resid, T *corr, const Coef<T> &c, const TO *PH, const TO *SH, double *out_p, double *out_s);
   void capture_loop(int precision);
   int enqueue_solve();
   void build_vcycle_program();

@@ -11,6 +11,7 @@
 #include <cstdint>
 
 #include "mac_device.h"
+#include "mac_fp.cuh"
 
 namespace sayaka_gb300 {
 namespace stencil {
@@ -112,7 +113,7 @@ __device__ __forceinline__ T crse_fine_sum(const Topo &t, const Coef<T> &c, int 
       if (ND == 2) fi[2] = 0;
       const int fx = face_index(d, fi, fside, nb);
       const T tf = cf_coef(c, t, F, d, fx, h15);
-      val += tf * (T)ld<CG>(&x[(long)F * t.ncell + encode(fi, nb)]);
+      val += tf * fpint::cvt<T>(ld<CG>(&x[(long)F * t.ncell + encode(fi, nb)]));
     }
   }
   return val;
