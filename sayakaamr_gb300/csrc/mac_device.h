@@ -155,8 +155,11 @@ void launch_prolong(const Topo &t, const Coef<T> &c, const BlockList &fine, T *p
 // (the level's blocks with the tower's face types); same values as
 // launch_prolong + launch_rbgs(color 0)
 template <typename T>
+// X: a list (with halo descriptors) whose red cells are swept in the same
+// launch, blocks that neither read nor are read by L's level
 void launch_prolong_red(const Topo &t, const Coef<T> &c, const BlockList &L, T *phi, const T *rhs,
-                        const int *guard, cudaStream_t s, bool pdl = false);
+                        const int *guard, cudaStream_t s, bool pdl = false,
+                        const BlockList &X = BlockList{nullptr, nullptr, 0});
 
 void launch_flux(const Topo &t, const Coef<double> &c, const BlockList &L, int dir,
                  const double *phi, double *flux, cudaStream_t s);

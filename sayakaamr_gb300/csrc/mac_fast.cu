@@ -1133,8 +1133,11 @@ void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *o
     // the prolongation and the red sweep that follows it can be one launch
     const BlockList top = sublevel_list(l, l);
     const bool fused = prm_.fuse_prolong && prm_.n_post > 0 && top.n == levels_[l].n;
+    // with the parity order, the red sweep of the rest of group 0 (leaf
+    // sublevels l-2, l-4, ...) rides in the same launch
+    const BlockList rest0 = prm_.sublevel_order == 1 ? parity_list(l, 0, true) : BlockList{nullptr, nullptr, 0};
     if (fused)
-      launch_prolong_red<T>(topo_, c, top, corr, resid, guard, stream_, prm_.pdl != 0);
+      launch_prolong_red<T>(topo_, c, top, corr, resid, guard, stream_, prm_.pdl != 0, rest0);
     else
       launch_prolong<T>(topo_, c, level_list(l), corr, guard, stream_, prm_.pdl != 0);
     for (int s = 0; s < prm_.n_post; s++) {
@@ -1144,7 +1147,8 @@ void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *o
         // the other colour, coarse/fine neighbours the other parity)
         for (int rb = 0; rb < 2; rb++)
           for (int g = 0; g < 2; g++) {
-            const BlockList gl = parity_list(l, g, fused && s == 0 && rb == 0 && g == 0);
+            if (fused && s == 0 && rb == 0 && g == 0) continue;  // done by the fused launch
+            const BlockList gl = parity_list(l, g, false);
             if (gl.n > 0) launch_rbgs<T>(topo_, c, gl, rb, corr, resid, guard, stream_, prm_.pdl != 0, rbgs_var<T>());
           }
         continue;

@@ -823,7 +823,8 @@ __device__ __forceinline__ T prolonged_value(const Topo &t, const Coef<T> &c, in
 
 template <typename T, int ND>
 __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, BlockList L, T *__restrict__ phi,
-                                                            const T *__restrict__ rhs, const int *guard) {
+                                                            const T *__restrict__ rhs, const int *guard,
+                                                            BlockList X) {
   extern __shared__ __align__(16) unsigned char pr_smem[];
   pdl_enter();
   if (guard && *guard) return;
@@ -833,7 +834,21 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
   T *hc = tile + ncell;
   T *hk = hc + 2 * ND * nface;
   T *hv = hk + 2 * ND * nface;
-  for (int p = blockIdx.x; p < L.n; p += gridDim.x) {
+  for (int p = blockIdx.x; p < L.n + X.n; p += gridDim.x) {
+    if (p >= L.n) {
+      // the red sweep of a block of X: blocks two or more levels coarser,
+      // which neither read nor are read by the level being prolonged
+      const int px = p - L.n;
+      const long fo = (long)px * ncell;
+      const int *e = X.hx + (long)px * kHX;
+      for (int h = threadIdx.x; h < nhalf; h += blockDim.x) {
+        int ijk[3];
+        color_cell_fast<ND>(h, t, 0, ijk);
+        smooth_cell_fast<T, ND>(t, c, e[kHXBlock], (uint16_t)(e[kHXInfo] & 0xffff), ijk, phi, rhs,
+                                X.sa ? X.sa + fo : nullptr, X.ia ? X.ia + fo : nullptr, e);
+      }
+      continue;
+    }
     const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
     const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
     const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
@@ -932,8 +947,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
 
 template <typename T>
 void launch_prolong_red(const Topo &t, const Coef<T> &c, const BlockList &L, T *phi, const T *rhs,
-                        const int *guard, cudaStream_t s, bool pdl) {
+                        const int *guard, cudaStream_t s, bool pdl, const BlockList &X) {
   if (L.n == 0) return;
+  if (X.n > 0 && !X.hx) return;  // the extra sweep reads its blocks through halo descriptors
   const int nface = t.ndim == 3 ? t.nb * t.nb : t.nb;
   const size_t smem = sizeof(T) * ((size_t)t.ncell + 3 * 2 * t.ndim * (size_t)nface);
   static bool attr[2] = {false, false};
@@ -945,11 +961,11 @@ void launch_prolong_red(const Topo &t, const Coef<T> &c, const BlockList &L, T *
     attr[t.ndim - 2] = true;
   }
   const int threads = std::min(kThreads, ((t.ncell >> 1) + 31) / 32 * 32);
-  const int grid = std::min(L.n, 152 * 64);
+  const int grid = std::min(L.n + X.n, 152 * 64);
   if (t.ndim == 2)
-    launch_k(pdl, k_prolong_red<T, 2>, grid, threads, smem, s, t, c, L, phi, rhs, guard);
+    launch_k(pdl, k_prolong_red<T, 2>, grid, threads, smem, s, t, c, L, phi, rhs, guard, X);
   else
-    launch_k(pdl, k_prolong_red<T, 3>, grid, threads, smem, s, t, c, L, phi, rhs, guard);
+    launch_k(pdl, k_prolong_red<T, 3>, grid, threads, smem, s, t, c, L, phi, rhs, guard, X);
 }
 
 template <typename T, int ND>
@@ -1091,7 +1107,7 @@ void launch_fix_bc(const Topo &t, const Coef<double> &c, const BlockList &L, con
   template void launch_prolong<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,          \
                                   cudaStream_t, bool);                                                          \
   template void launch_prolong_red<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const T *,        \
-                                      const int *, cudaStream_t, bool);
+                                      const int *, cudaStream_t, bool, const BlockList &);
 SAYAKA_INST(double)
 SAYAKA_INST(float)
 #undef SAYAKA_INST
