@@ -75,6 +75,8 @@ def parse():
     ap.add_argument("--bottom-level", type=int, default=0,
                     help="level of the dense bottom solve (0: the coarsest uniform level of at most 4096 cells "
                          "per component)")
+    ap.add_argument("--bottom-half", type=int, default=0,
+                    help="1: FP16 copy of the dense bottom inverse (bottom level above 1)")
     ap.add_argument("--sublevel-order", type=int, default=1,
                     help="V-cycle smoothing order over a tower's sublevels: 0 finest to coarsest per sublevel "
                          "(the reference's), 1 one launch per colour and level parity")
@@ -314,7 +316,8 @@ def main():
                  graph=0 if args.profile else 1, n_post_smooth=max(args.n_post, 1) if args.n_post >= 0 else 2,
                  vcycle_kernel=args.vcycle_kernel,
                  cluster_cells=args.cluster_cells, smooth_variant=args.smooth_variant,
-                 pdl=args.pdl, sublevel_order=args.sublevel_order, bottom_level=args.bottom_level)
+                 pdl=args.pdl, sublevel_order=args.sublevel_order, bottom_level=args.bottom_level,
+                 bottom_half=args.bottom_half)
     S.prepare()
     ext = torch.cuda.ExternalStream(S.stream())
     if args.kernel >= 0:

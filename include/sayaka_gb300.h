@@ -123,6 +123,8 @@ typedef struct sayaka_params {
                              finest whose tower is one uniform level with at most 1024 (2D) / 4096 (3D) cells
                              per connected component; level 1 otherwise), n >= 1 = level n if its tower is
                              one uniform level of at most 4096 cells per component */
+  int32_t bottom_half;    /* device path, FP32 V-cycle, bottom above level 1: 1 = apply an FP16 copy of the
+                             dense inverse with one FP32 scale per row (half the bytes), 0 = FP32 copy */
   int32_t sublevel_order; /* device V-cycle smoothing over a tower's sublevels: 0 = finest to coarsest,
                              red then black per sublevel (the reference's order, mg_smooth_level);
                              1 = one launch per colour and level parity (default) */

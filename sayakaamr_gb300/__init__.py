@@ -40,7 +40,7 @@ class Params(C.Structure):
                 ("bottom", C.c_int32), ("verbose", C.c_int32), ("graph", C.c_int32),
                 ("vcycle_kernel", C.c_int32), ("pdl", C.c_int32),
                 ("cluster_cells", C.c_int32), ("smooth_variant", C.c_int32), ("learned", C.c_int32),
-                ("bottom_level", C.c_int32), ("sublevel_order", C.c_int32)]
+                ("bottom_level", C.c_int32), ("bottom_half", C.c_int32), ("sublevel_order", C.c_int32)]
 
 
 class SolveInfo(C.Structure):

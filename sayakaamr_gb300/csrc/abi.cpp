@@ -385,6 +385,7 @@ void sayaka_params_default(sayaka_params *p) {
   p->smooth_variant = d.smooth_variant;
   p->learned = d.learned;
   p->bottom_level = d.bottom_level;
+  p->bottom_half = d.bottom_half;
   p->sublevel_order = d.sublevel_order;
 }
 
@@ -602,6 +603,7 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.smooth_variant = p->smooth_variant;
     s.learned = p->learned;
     s.bottom_level = p->bottom_level;
+    s.bottom_half = p->bottom_half;
     s.sublevel_order = p->sublevel_order;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;

@@ -104,6 +104,9 @@ struct BottomDev {
   const int *tile_comp, *tile_row0;
   int ntiles, ncell, max_n;
   const float *binv32 = nullptr;  // FP32 copy of binv for the FP32 V-cycle (bottom level above 1)
+  // or, instead, an FP16 copy with one FP32 scale per row (entry = h * scale)
+  const unsigned short *binv16 = nullptr;
+  const float *rscale = nullptr;
 };
 constexpr int kBottomTileRows = 8;
 

@@ -17,6 +17,8 @@
 #include <type_traits>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "mac_solver.h"
 #include "cuda_check.h"
 #include "mac_stencil.cuh"
@@ -628,6 +630,29 @@ __global__ void __launch_bounds__(kTPB) k_gj_step(int m, int k, int nmat, const 
   }
 }
 // zero column col of the order-m matrix at off (a pinned Neumann cell)
+// FP16 copy of the bottom inverse, one CTA per row: scale = max |a| of the
+// row, h = a / scale rounded to nearest
+__global__ void __launch_bounds__(kTPB) k_half_rows(int nrows, const long long *row_off, const int *row_m,
+                                                  const double *a, unsigned short *h, float *scale) {
+  __shared__ double sh[kTPB / 32];
+  for (int g = blockIdx.x; g < nrows; g += gridDim.x) {
+    const double *ar = a + row_off[g];
+    const int m = row_m[g];
+    double mx = 0.0;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) mx = fmax(mx, fabs(ar[j]));
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    mx = 0.0;
+    for (int q = 0; q < kTPB / 32; q++) mx = fmax(mx, sh[q]);
+    const double inv = mx > 0 ? 1.0 / mx : 0.0;
+    for (int j = threadIdx.x; j < m; j += blockDim.x)
+      h[row_off[g] + j] = __half_as_ushort(__double2half(ar[j] * inv));
+    if (threadIdx.x == 0) scale[g] = (float)mx;
+    __syncthreads();
+  }
+}
+
 // FP32 copy of the bottom inverse
 __global__ void k_narrow(long long n, const double *a, float *b) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -1089,9 +1114,40 @@ void MacGpu::build_bottom() {
   // an FP32 copy for the FP32 V-cycle when the bottom is above level 1: its
   // product is then large (up to kBottomMaxCells^2 per component) and FP64
   // multiply-adds run at 1/64 of the FP32 rate here
-  if (LB > 1) {
+  bot_half_ = prm_.bottom_half;
+  // the FP16 product reads rows in 16-byte pieces: every row must start on
+  // a 16-byte boundary (component orders that are multiples of 8)
+  bool rows16 = true;
+  for (int c = 0; c < nc; c++) rows16 = rows16 && comp_n[c] % 8 == 0 && comp_off[c] % 8 == 0;
+  if (LB > 1 && prm_.bottom_half && rows16) {
+    // FP16 rows with one scale each: half the bytes of the FP32 copy
+    std::vector<long long> row_off(n_bot_);
+    std::vector<int> row_m(n_bot_);
+    for (int g = 0; g < n_bot_; g++) {
+      const int c = rcomp[g];
+      row_off[g] = comp_off[c] + (long long)(g - comp_row0[c]) * comp_n[c];
+      row_m[g] = comp_n[c];
+    }
+    long long *d_ro = nullptr;
+    int *d_rm = nullptr;
+    if (cudaMalloc(&d_binv16_, (size_t)tot * sizeof(unsigned short)) != cudaSuccess ||
+        cudaMalloc(&d_rscale_, (size_t)n_bot_ * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&d_ro, (size_t)n_bot_ * sizeof(long long)) != cudaSuccess ||
+        cudaMalloc(&d_rm, (size_t)n_bot_ * sizeof(int)) != cudaSuccess) {
+      fail("out of device memory (bottom solve)");
+      return;
+    }
+    CK_(cudaMemcpyAsync(d_ro, row_off.data(), row_off.size() * sizeof(long long), cudaMemcpyHostToDevice, stream_));
+    CK_(cudaMemcpyAsync(d_rm, row_m.data(), row_m.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    k_half_rows<<<std::min(n_bot_, 152 * 16), kTPB, 0, stream_>>>(n_bot_, d_ro, d_rm, d_binv_, d_binv16_, d_rscale_);
+    CK_(cudaStreamSynchronize(stream_));
+    cudaFree(d_ro);
+    cudaFree(d_rm);
+  } else if (LB > 1) {
     if (cudaMalloc(&d_binv32_, (size_t)tot * sizeof(float)) != cudaSuccess) {
       d_binv32_ = nullptr;
+  d_binv16_ = nullptr;
+  d_rscale_ = nullptr;
       fail("out of device memory (bottom solve)");
       return;
     }
@@ -1099,14 +1155,14 @@ void MacGpu::build_bottom() {
   }
   CK_(cudaStreamSynchronize(stream_));
   bot_ = BottomDev{d_binv_, d_bot_blocks_, d_comp_row0_, d_comp_n_, d_comp_off_, d_tile_comp_, d_tile_row0_,
-                   (int)tile_comp.size(), ncell_, max_n, d_binv32_};
+                   (int)tile_comp.size(), ncell_, max_n, d_binv32_, d_binv16_, d_rscale_};
   n_pins_ = (int)pins.size();
   n_bot_comp_ = nc;
   bottom_ready_ = true;
 }
 
 void MacGpu::bottom_free() {
-  for (void *p : {(void *)d_binv32_, (void *)d_binv_, (void *)d_bot_blocks_, (void *)d_comp_row0_, (void *)d_comp_n_,
+  for (void *p : {(void *)d_binv16_, (void *)d_rscale_, (void *)d_binv32_, (void *)d_binv_, (void *)d_bot_blocks_, (void *)d_comp_row0_, (void *)d_comp_n_,
                   (void *)d_comp_off_, (void *)d_tile_comp_, (void *)d_tile_row0_})
     if (p) cudaFree(p);
   d_binv_ = nullptr;
@@ -1348,7 +1404,8 @@ int MacGpu::cg_solve_enqueue() {
   ensure_fast_buffers();
   // coefficients changed since sayaka_mac_prepare: the fast-path data and the
   // graph must be rebuilt first
-  if (!err_.empty() || !bottom_ready_ || coef_version_ != fast_coef_version_ || bot_param_ != prm_.bottom_level)
+  if (!err_.empty() || !bottom_ready_ || coef_version_ != fast_coef_version_ || bot_param_ != prm_.bottom_level ||
+      bot_half_ != prm_.bottom_half)
     return -1;
   if (prm_.graph && graph_stale())
     return -1;
@@ -1431,7 +1488,7 @@ int MacGpu::prepare_device() {
     build_bottom();
     fast_coef_version_ = coef_version_;
     if (!err_.empty()) return -1;
-  } else if (bot_param_ != prm_.bottom_level) {  // another bottom level asked for
+  } else if (bot_param_ != prm_.bottom_level || bot_half_ != prm_.bottom_half) {  // another bottom asked for
     CKR_(cudaStreamSynchronize(stream_), -1);
     drop_graph();
     build_bottom();

@@ -37,6 +37,7 @@ struct SolverParams {
   int smooth_variant = -1;    // device smoother launch bounds: -1 autotune at prepare, else variant index
   int learned = 0;            // device path, FP32 V-cycle: apply the trained block correction
   int fuse_prolong = 1;       // device path: prolongation fused with the first red sweep of its level
+  int bottom_half = 0;        // device path, FP32 V-cycle, bottom above level 1: 1 = FP16 inverse with row scales
   int bottom_level = 0;       // device path: level of the dense bottom solve; 0 = the coarsest level whose
                               // tower is one uniform level of at most kBottomMaxCells cells per component
   int sublevel_order = 1;     // device V-cycle smoothing order over a tower's sublevels: 0 = finest to
@@ -288,8 +289,9 @@ class MacGpu {
       *d_tile_row0_ = nullptr;
   long long *d_comp_off_ = nullptr;
   BottomDev bot_{};
-  float *d_binv32_ = nullptr;
-  int bot_level_ = 1, bot_param_ = -1, program_bot_ = -1;
+  float *d_binv32_ = nullptr, *d_rscale_ = nullptr;
+  unsigned short *d_binv16_ = nullptr;
+  int bot_level_ = 1, bot_param_ = -1, bot_half_ = -1, program_bot_ = -1;
   int choose_bottom_level(std::string *why) const;
   int n_bot_ = 0, n_pins_ = 0, n_bot_comp_ = 0;
   void bottom_free();

@@ -10,6 +10,8 @@
 
 #include <cstdint>
 
+#include <cuda_fp16.h>
+
 #include "mac_device.h"
 #include "mac_fp.cuh"
 
@@ -422,6 +424,50 @@ __device__ __forceinline__ void bottom_gather(const BottomDev &bd, int r0, int m
 template <typename T, bool CG = false>
 __device__ __forceinline__ void bottom_tile(const BottomDev &bd, int tile, const T *resid, T *corr, double *rv) {
   const int c = bd.tile_comp[tile], r0 = bd.comp_row0[c], m = bd.comp_n[c], nc = bd.ncell;
+  if (sizeof(T) == 4 && bd.binv16) {  // FP16 rows with FP32 scales, FP32 accumulation
+    float *rf = reinterpret_cast<float *>(rv);
+    bottom_gather<T, CG>(bd, r0, m, resid, rf);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, row = bd.tile_row0[tile] + (threadIdx.x >> 5);
+    if ((threadIdx.x >> 5) < kBottomTileRows && row < m) {
+      // rows start on 16-byte boundaries: m and the component offsets are
+      // multiples of the block size (at least 64 cells)
+      const uint4 *a8 = reinterpret_cast<const uint4 *>(bd.binv16 + bd.comp_off[c] + (long long)row * m);
+      const float4 *r4 = reinterpret_cast<const float4 *>(rf);
+      const int q8 = m >> 3;
+      float s0 = 0.f, s1 = 0.f;
+      auto dot8 = [&](const uint4 u, int j, float &acc) {
+        const float2 f0 = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+        const float2 f1 = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
+        const float2 f2 = __half22float2(*reinterpret_cast<const __half2 *>(&u.z));
+        const float2 f3 = __half22float2(*reinterpret_cast<const __half2 *>(&u.w));
+        const float4 x0 = r4[2 * j], x1 = r4[2 * j + 1];
+        acc = fmaf(f0.x, x0.x, acc);
+        acc = fmaf(f0.y, x0.y, acc);
+        acc = fmaf(f1.x, x0.z, acc);
+        acc = fmaf(f1.y, x0.w, acc);
+        acc = fmaf(f2.x, x1.x, acc);
+        acc = fmaf(f2.y, x1.y, acc);
+        acc = fmaf(f3.x, x1.z, acc);
+        acc = fmaf(f3.y, x1.w, acc);
+      };
+      int j = lane;
+      for (; j + 96 < q8; j += 128) {
+        const uint4 u0 = a8[j], u1 = a8[j + 32], u2 = a8[j + 64], u3 = a8[j + 96];
+        dot8(u0, j, s0);
+        dot8(u1, j + 32, s1);
+        dot8(u2, j + 64, s0);
+        dot8(u3, j + 96, s1);
+      }
+      for (; j < q8; j += 32) dot8(a8[j], j, s0);
+      float s = s0 + s1;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      const int g = r0 + row;
+      if (lane == 0) corr[(long)bd.blocks[g / nc] * nc + g % nc] = (T)(s * bd.rscale[g]);
+    }
+    __syncthreads();
+    return;
+  }
   if (sizeof(T) == 4 && bd.binv32) {  // FP32 inverse, FP32 accumulation
     float *rf = reinterpret_cast<float *>(rv);
     bottom_gather<T, CG>(bd, r0, m, resid, rf);

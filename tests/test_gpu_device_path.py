@@ -185,6 +185,13 @@ def test_bottom_level_above_one(name):
     print(name, "bottom level 1: %d iterations; level %d: %d" % (its[1][0], its[k][1], its[k][0]))
     assert its[1][1] == 1 and its[k][1] == 2
     assert its[k][0] <= its[1][0]
-    S.set_params(bottom_level=0)
+    # the FP16 copy of the level-2 inverse (row scales): same criterion, at
+    # most one iteration more
+    S.set_zero_sol()
+    S.set_params(bottom_level=2, bottom_half=1)
+    info = S.cg_solve()
+    assert info["status"] == 0 and info["rnorm"] < 1e-8 * info["rnorm0"], info
+    assert info["iterations"] <= its[k][0] + 1, (info["iterations"], its)
+    S.set_params(bottom_level=0, bottom_half=0)
     S.prepare()
     assert S.bottom_level() == (1 if name == "config2" else 2)
