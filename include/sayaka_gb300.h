@@ -274,6 +274,10 @@ int sayaka_mac_correct_vel(sayaka_mac *h, int32_t dir, double dt, double *u, int
  * children; a block with a deeper old subtree starts from zero. */
 int sayaka_mac_init_from(sayaka_mac *h, const sayaka_mac *old);
 
+/* the library's pending CUDA runtime error on the calling thread (0 =
+ * none), without clearing it: every call of this API leaves none behind */
+int32_t sayaka_cuda_peek_error(void);
+
 /* ---- self-test of the device solve's integer-pipe conversions (tests) ----
  * narrow[i] = double -> float of d[i] (round to nearest even) and
  * widen[i] = float -> double of f[i], widen0[i] = 0.0 + (double)f[i], each

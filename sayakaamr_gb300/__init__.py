@@ -104,6 +104,7 @@ SIGNATURES = {
     "sayaka_mac_get_rhs_compact": (C.c_int, [_V, _f64p]),
     "sayaka_mac_init_from": (C.c_int, [_V, _V]),
     "sayaka_mac_bottom_level": (C.c_int32, [_V]),
+    "sayaka_cuda_peek_error": (C.c_int32, []),
     "sayaka_fp_selftest": (C.c_int, [_f64p, _f32p, C.c_int, _f32p, _f32p, _f64p, _f64p, _f64p, _f64p]),
     "sayaka_mac_learned_nparam": (C.c_int32, []),
     "sayaka_mac_learned_collect": (C.c_int, [_V, C.c_int32, _i32p]),
@@ -154,6 +155,11 @@ def _f64(a):
 
 class SayakaError(RuntimeError):
     pass
+
+
+def cuda_peek_error():
+    """the library's pending CUDA runtime error code on this thread (0: none)"""
+    return int(load_library().sayaka_cuda_peek_error())
 
 
 def fp_selftest(d, f):

@@ -792,6 +792,7 @@ int sayaka_mac_init_from(sayaka_mac *h, const sayaka_mac *old) {
     return st == 0 ? (int)SAYAKA_OK : (int)SAYAKA_CUDA_ERROR;
   });
 }
+int32_t sayaka_cuda_peek_error(void) { return (int32_t)cudaPeekAtLastError(); }
 int sayaka_fp_selftest(const double *d, const float *f, int n, float *narrow, float *narrow_hw, double *widen,
                        double *widen_hw, double *widen0, double *widen0_hw) {
   if (n < 0 || (n > 0 && (!d || !f || !narrow || !narrow_hw || !widen || !widen_hw || !widen0 || !widen0_hw)))

@@ -1134,6 +1134,7 @@ void MacGpu::build_bottom() {
         cudaMalloc(&d_rscale_, (size_t)n_bot_ * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&d_ro, (size_t)n_bot_ * sizeof(long long)) != cudaSuccess ||
         cudaMalloc(&d_rm, (size_t)n_bot_ * sizeof(int)) != cudaSuccess) {
+      if (d_ro) cudaFree(d_ro);
       fail("out of device memory (bottom solve)");
       return;
     }
@@ -1146,8 +1147,6 @@ void MacGpu::build_bottom() {
   } else if (LB > 1) {
     if (cudaMalloc(&d_binv32_, (size_t)tot * sizeof(float)) != cudaSuccess) {
       d_binv32_ = nullptr;
-  d_binv16_ = nullptr;
-  d_rscale_ = nullptr;
       fail("out of device memory (bottom solve)");
       return;
     }
@@ -1167,6 +1166,8 @@ void MacGpu::bottom_free() {
     if (p) cudaFree(p);
   d_binv_ = nullptr;
   d_binv32_ = nullptr;
+  d_binv16_ = nullptr;
+  d_rscale_ = nullptr;
   d_bot_blocks_ = d_comp_row0_ = d_comp_n_ = d_tile_comp_ = d_tile_row0_ = nullptr;
   d_comp_off_ = nullptr;
   bot_ = BottomDev{};

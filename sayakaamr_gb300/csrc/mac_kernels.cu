@@ -384,31 +384,56 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
     }
     __syncthreads();
     const T dv = geom(c, b, 6);
-    for (int h = threadIdx.x; h < nhalf; h += blockDim.x) {
-      int ijk[3];
-      color_cell_fast<ND>(h, t, color, ijk);
-      const int ci = t.lnb >= 0 ? ijk[0] + ((ijk[1] + (ijk[2] << t.lnb)) << t.lnb) : encode(ijk, nb);
+    // a cell's global operands (face coefficients, rhs and vf or the FP64
+    // factors) are gathered before any update: a thread with two cells has
+    // both cells' loads in flight together (the shared-memory tile written
+    // by the updates may alias the operand pointers for the compiler)
+    struct Ops {
+      int ijk[3], ci;
+      T coef[2 * ND], r, v;
+      double sa, ia;
+    };
+    auto gather = [&](int h, Ops &o) {
+      color_cell_fast<ND>(h, t, color, o.ijk);
+      o.ci = t.lnb >= 0 ? o.ijk[0] + ((o.ijk[1] + (o.ijk[2] << t.lnb)) << t.lnb) : encode(o.ijk, nb);
+#pragma unroll
+      for (int f = 0; f < 2 * ND; f++) {
+        const int d = f >> 1, s = f & 1;
+        const bool bnd = s ? o.ijk[d] == nb - 1 : o.ijk[d] == 0;
+        int fx;
+        if (d == 0)
+          fx = o.ijk[0] + s + (nb + 1) * (o.ijk[1] + nb * o.ijk[2]);
+        else if (d == 1)
+          fx = o.ijk[0] + nb * (o.ijk[1] + s + (nb + 1) * o.ijk[2]);
+        else
+          fx = o.ci + s * nb * nb;
+        o.coef[f] = bnd ? (T)0 : c.tff[d][fb + fx];
+      }
+      o.r = rhs[cb + o.ci];
+      if (sizeof(T) == 8 && L.sa) {
+        const long fo = (long)p * ncell + o.ci;
+        o.sa = L.sa[fo];
+        o.ia = L.ia[fo];
+        o.v = 0;
+      } else {
+        o.v = c.vf[cb + o.ci];
+        o.sa = o.ia = 0.0;
+      }
+    };
+    auto update = [&](const Ops &o) {
       T diag = c.alpha * dv;
       T off = 0;
 #pragma unroll
       for (int f = 0; f < 2 * ND; f++) {
         const int d = f >> 1, s = f & 1;
-        const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+        const bool bnd = s ? o.ijk[d] == nb - 1 : o.ijk[d] == 0;
         if (!bnd) {
-          int fx;
-          if (d == 0)
-            fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
-          else if (d == 1)
-            fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
-          else
-            fx = ci + s * nb * nb;
-          const T coef = c.tff[d][fb + fx];
           const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
-          diag += coef;
-          off = fma_t(coef, tile[ci + (s ? stride : -stride)], off);
+          diag += o.coef[f];
+          off = fma_t(o.coef[f], tile[o.ci + (s ? stride : -stride)], off);
         } else {
           const int q0 = d == 0 ? 1 : 0, q1 = d == 2 ? 1 : 2;
-          const int m = ijk[q0] + (ND == 3 ? nb * ijk[q1] : 0);
+          const int m = o.ijk[q0] + (ND == 3 ? nb * o.ijk[q1] : 0);
           const int e = f * nface + m;
           diag += hc[e];
           off = fma_t(hk[e], hv[e], off);
@@ -416,13 +441,19 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
       }
       T unew = 0;
       if (sizeof(T) == 8 && L.sa) {
-        const long fo = (long)p * ncell + ci;
-        unew = fma_t(rhs[cb + ci], (T)L.sa[fo], off * (T)L.ia[fo]);
+        unew = fma_t(o.r, (T)o.sa, off * (T)o.ia);
       } else {
-        const T vfv = c.vf[cb + ci];
-        if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+        if (o.v > 0 && diag > 0) unew = fast_div(fma_t(o.r * dv, o.v, off), diag);
       }
-      tile[ci] = unew;
+      tile[o.ci] = unew;
+    };
+    for (int h = threadIdx.x; h < nhalf; h += 2 * blockDim.x) {
+      const int h2 = h + blockDim.x;
+      Ops o1, o2;
+      gather(h, o1);
+      if (h2 < nhalf) gather(h2, o2);
+      update(o1);
+      if (h2 < nhalf) update(o2);
     }
     __syncthreads();
     if ((ncell & 3) == 0 && sizeof(T) == 4) {

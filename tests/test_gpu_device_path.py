@@ -195,3 +195,13 @@ def test_bottom_level_above_one(name):
     S.set_params(bottom_level=0, bottom_half=0)
     S.prepare()
     assert S.bottom_level() == (1 if name == "config2" else 2)
+    # a solve after the rebuild uses only the new bottom's arrays, and the
+    # handle's teardown frees each array once: no CUDA error is left pending
+    S.set_zero_sol()
+    info = S.cg_solve()
+    assert info["status"] == 0 and info["rnorm"] < 1e-8 * info["rnorm0"], info
+    import gc
+    import sayakaamr_gb300 as sg
+    del S
+    gc.collect()
+    assert sg.cuda_peek_error() == 0
