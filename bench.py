@@ -200,7 +200,10 @@ def cpu_solve(prob, max_iter=2000, budget_s=None, n_iters=None):
     solve's own when it converged within k, else n_iters when given (the
     device solve's count on the same workload), else extrapolated from the
     residual reduction observed over the k iterations (rough: BiCGSTAB's
-    early reduction is not geometric)."""
+    early reduction is not geometric).  The reference's outer iterations get
+    dearer as the solve proceeds (its bottom BiCGSTAB works harder as the
+    outer residual falls), so the sampled rate overstates the CPU's: the
+    bounded baseline favours the CPU."""
     pyoracle, O = cpu_oracle(prob)
 
     def run(n):

@@ -7,6 +7,10 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 namespace sayaka_gb300 {
 
 __device__ __forceinline__ void pdl_enter() {
@@ -14,6 +18,28 @@ __device__ __forceinline__ void pdl_enter() {
   cudaTriggerProgrammaticLaunchCompletion();
   cudaGridDependencySynchronize();
 #endif
+}
+
+// The dynamic shared-memory limit of kernel fn raised to at least `bytes`
+// on the current device, thread-safe and only when it grows: the attribute
+// is per device, so a process with handles on several GPUs sets it on each.
+// A refusal is not left pending as the thread's CUDA error: the launch that
+// needs the memory reports it.
+inline void ensure_max_smem(const void *fn, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, int> set_to;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  int &cur = set_to[{fn, dev}];
+  if (cur >= bytes) return;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
+    cur = bytes;
+  else
+    cudaGetLastError();
 }
 
 template <typename... KArgs, typename... Args>

@@ -1238,7 +1238,7 @@ void MacGpu::bottom_launch(T *resid, T *corr) {
   if (bot_.ntiles == 0) return;
   const size_t smem = (size_t)bot_.max_n * sizeof(double);
   if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_bottom_gemv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    ensure_max_smem((const void *)k_bottom_gemv<T>, (int)smem);
   launch_k(prm_.pdl != 0, k_bottom_gemv<T>, bot_.ntiles, kTPB, smem, stream_, bot_, (const T *)resid, corr,
            (const FState *)d_st_);
 }

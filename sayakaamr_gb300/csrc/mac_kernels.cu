@@ -794,13 +794,12 @@ template <typename T, int ND>
 static void rbgs_stream_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
                            const int *guard, cudaStream_t s, bool pdl) {
   const size_t smem = rbgs_stream_smem<T, ND>(t);
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(k_rbgs_stream<T, ND>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  int dev = 0, nsm = 152;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    nsm = 152;
   }
+  ensure_max_smem((const void *)k_rbgs_stream<T, ND>, 227 * 1024);
   launch_k(pdl, k_rbgs_stream<T, ND>, std::min(L.n, nsm), kStreamThreads, smem, s, t, c, L, color, phi, rhs,
            guard);
 }
@@ -815,11 +814,7 @@ template <typename T, int ND>
 static void rbgs_bulk_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
                          const int *guard, cudaStream_t s, bool pdl) {
   const size_t smem = rbgs_bulk_smem<T, ND>(t);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_rbgs_bulk<T, ND>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  ensure_max_smem((const void *)k_rbgs_bulk<T, ND>, 200 * 1024);
   const int threads = std::min(kThreads, ((t.ncell >> 1) + 31) / 32 * 32);
   launch_k(pdl, k_rbgs_bulk<T, ND>, L.n, threads, smem, s, t, c, L, color, phi, rhs, guard);
 }
@@ -983,14 +978,7 @@ void launch_prolong_red(const Topo &t, const Coef<T> &c, const BlockList &L, T *
   if (X.n > 0 && !X.hx) return;  // the extra sweep reads its blocks through halo descriptors
   const int nface = t.ndim == 3 ? t.nb * t.nb : t.nb;
   const size_t smem = sizeof(T) * ((size_t)t.ncell + 3 * 2 * t.ndim * (size_t)nface);
-  static bool attr[2] = {false, false};
-  if (!attr[t.ndim - 2]) {
-    if (t.ndim == 2)
-      cudaFuncSetAttribute(k_prolong_red<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    else
-      cudaFuncSetAttribute(k_prolong_red<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr[t.ndim - 2] = true;
-  }
+  ensure_max_smem(t.ndim == 2 ? (const void *)k_prolong_red<T, 2> : (const void *)k_prolong_red<T, 3>, 200 * 1024);
   const int threads = std::min(kThreads, ((t.ncell >> 1) + 31) / 32 * 32);
   const int grid = std::min(L.n + X.n, 152 * 64);
   if (t.ndim == 2)
@@ -1009,11 +997,7 @@ template <typename T, int ND, int MINB>
 static void rbgs_tile_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
                          const int *guard, cudaStream_t s, bool pdl) {
   const size_t smem = rbgs_tile_smem<T, ND>(t);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_rbgs_tile<T, ND, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  ensure_max_smem((const void *)k_rbgs_tile<T, ND, MINB>, 200 * 1024);
   const int threads = std::min(kThreads, ((t.ncell >> 1) + 31) / 32 * 32);
   const int grid = std::min(L.n, 152 * 64);
   launch_k(pdl, k_rbgs_tile<T, ND, MINB>, grid, threads, smem, s, t, c, L, color, phi, rhs, guard);

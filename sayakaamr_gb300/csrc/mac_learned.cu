@@ -464,17 +464,14 @@ constexpr size_t infer_smem() {
 }  // namespace
 
 static void set_smem_attrs() {
-  static bool done = false;
-  if (done) return;
-  cudaFuncSetAttribute(k_nn_fwd<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem<16>());
-  cudaFuncSetAttribute(k_nn_bwd<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem<16>());
-  cudaFuncSetAttribute(k_nn_fwd<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem<8>());
-  cudaFuncSetAttribute(k_nn_bwd<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem<8>());
-  cudaFuncSetAttribute(k_nn_infer<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem<16>());
-  cudaFuncSetAttribute(k_nn_infer<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem<8>());
-  cudaFuncSetAttribute(k_nn_forward<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem<16>());
-  cudaFuncSetAttribute(k_nn_forward<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem<8>());
-  done = true;
+  ensure_max_smem((const void *)k_nn_fwd<16>, (int)fwd_smem<16>());
+  ensure_max_smem((const void *)k_nn_bwd<16>, (int)bwd_smem<16>());
+  ensure_max_smem((const void *)k_nn_fwd<8>, (int)fwd_smem<8>());
+  ensure_max_smem((const void *)k_nn_bwd<8>, (int)bwd_smem<8>());
+  ensure_max_smem((const void *)k_nn_infer<16>, (int)infer_smem<16>());
+  ensure_max_smem((const void *)k_nn_infer<8>, (int)infer_smem<8>());
+  ensure_max_smem((const void *)k_nn_forward<16>, (int)infer_smem<16>());
+  ensure_max_smem((const void *)k_nn_forward<8>, (int)infer_smem<8>());
 }
 
 // ---------------------------------------------------------------------------

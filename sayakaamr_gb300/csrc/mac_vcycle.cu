@@ -19,6 +19,7 @@
 
 #include "cuda_check.h"
 #include "mac_solver.h"
+#include "launch.cuh"
 #include "mac_stencil.cuh"
 
 namespace sayaka_gb300 {
@@ -174,7 +175,7 @@ void MacGpu::vcycle_coop(T *resid, T *corr, const Coef<T> &c, double *out) {
   const size_t smem = (size_t)std::max(bot_.max_n, 1) * sizeof(double);
   const void *fn = tt_.ndim == 2 ? (const void *)k_vcycle_coop<T, 2> : (const void *)k_vcycle_coop<T, 3>;
   if (coop_grid_ <= 0) {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 48 * 1024) ensure_max_smem(fn, (int)smem);
     int per_sm = 0, dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
