@@ -211,6 +211,29 @@ double *staging(sayaka_mac *h, size_t n) {
   return h->pinned;
 }
 
+// The calling thread's current device switched to `dev` for a scope and
+// restored afterwards: a handle's calls run on the device its buffers live
+// on, whatever device the caller has current.  Its own failures (no device)
+// are not left pending as the thread's CUDA error.
+struct DeviceScope {
+  int prev = -1;
+  explicit DeviceScope(int dev) {
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    if (cur == dev) return;
+    if (cudaSetDevice(dev) == cudaSuccess)
+      prev = cur;
+    else
+      cudaGetLastError();
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
 template <typename F>
 int guarded(sayaka_mac *h, F &&f) {
   if (!h) return SAYAKA_BAD_INPUT;
@@ -218,6 +241,7 @@ int guarded(sayaka_mac *h, F &&f) {
     h->err = "solver not created";
     return SAYAKA_BAD_INPUT;
   }
+  DeviceScope on_device(h->gpu->device());
   try {
     const int r = f();
     if (r != SAYAKA_OK) return r;
@@ -434,7 +458,14 @@ int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
   return SAYAKA_OK;
 }
 
-void sayaka_mac_destroy(sayaka_mac *h) { delete h; }
+void sayaka_mac_destroy(sayaka_mac *h) {
+  if (h && h->gpu) {
+    DeviceScope on_device(h->gpu->device());
+    delete h;
+    return;
+  }
+  delete h;
+}
 
 const char *sayaka_mac_last_error(const sayaka_mac *h) {
   if (!h) return "null handle";

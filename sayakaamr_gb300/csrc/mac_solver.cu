@@ -152,6 +152,11 @@ void MacGpu::fail(const std::string &m) {
 }
 
 MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
+  // every buffer of the solver lives on the device current at construction
+  if (cudaGetDevice(&device_) != cudaSuccess) {
+    cudaGetLastError();
+    device_ = 0;
+  }
   const int nd = tt.ndim, nb = tt.nb, nbk = tt.num_blocks;
   if (nd < 2 || nd > 3 || nb < 2 || (nb & 1) || nbk <= 0) {
     fail("bad tree tables (ndim 2|3, even nb, blocks > 0)");

@@ -99,6 +99,7 @@ class MacGpu {
   int tower_size(int L, int sublevel) const;
   int tuned_smoother(int precision, float *us, int n) const;
   int bottom_level() const { return bottom_ready_ ? bot_level_ : -1; }
+  int device() const { return device_; }
 
   // building blocks, exposed for parity tests (compact arrays, all blocks)
   void apply(int L, const double *x_all, double *y_all);
@@ -292,6 +293,7 @@ class MacGpu {
   float *d_binv32_ = nullptr, *d_rscale_ = nullptr;
   unsigned short *d_binv16_ = nullptr;
   int bot_level_ = 1, bot_param_ = -1, bot_half_ = -1, program_bot_ = -1;
+  int device_ = 0;
   int choose_bottom_level(std::string *why) const;
   int n_bot_ = 0, n_pins_ = 0, n_bot_comp_ = 0;
   void bottom_free();

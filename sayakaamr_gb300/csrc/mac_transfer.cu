@@ -91,6 +91,10 @@ std::vector<unsigned long long> path_keys(const TreeTables &t) {
 }  // namespace
 
 int MacGpu::init_solution_from(const MacGpu &old, std::string *why) {
+  if (old.device_ != device_) {
+    *why = "init_from: the solvers live on different devices";
+    return 1;
+  }
   if (old.tt_.ndim != tt_.ndim || old.tt_.nb != tt_.nb) {
     *why = "init_from: the trees differ in dimension or block size";
     return 1;
