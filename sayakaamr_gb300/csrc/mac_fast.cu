@@ -838,8 +838,6 @@ void MacGpu::refresh_fp32() {
   c32_.beta = (float)beta_;
 }
 
-// Dense FP64 inverse of the level-1 operator (tower 1 = every level-1 block,
-// faces FINE_FINE or FINE_BC only), rows in tower order, cells in block order.
 // Level of the dense bottom solve.  Level 1 always works (it is uniform and
 // every level-1 face is a same-level or physical face); a finer level B
 // replaces the V-cycle's levels 1..B by one dense solve when tower B is one
@@ -903,6 +901,9 @@ int MacGpu::choose_bottom_level(std::string *why) const {
   return best;
 }
 
+// Dense FP64 inverse of the bottom level's operator (the bottom tower is
+// one uniform level: faces FINE_FINE or FINE_BC only), one per connected
+// component, rows in tower order within a component, cells in block order.
 void MacGpu::build_bottom() {
   const int nd = tt_.ndim, nb = tt_.nb;
   std::string why;
