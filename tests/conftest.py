@@ -23,3 +23,17 @@ def _built():
     build.build_library()
     build.build_oracle()
     yield
+
+
+@pytest.fixture(autouse=True)
+def _no_pending_cuda_error(request):
+    """after every GPU test (its handles collected), the library leaves no
+    CUDA runtime error pending: an error left behind would surface in an
+    unrelated later call"""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    import gc
+    import sayakaamr_gb300 as sg
+    gc.collect()
+    assert sg.cuda_peek_error() == 0, "CUDA error left pending: %d" % sg.cuda_peek_error()
