@@ -109,3 +109,35 @@ def test_checker_finds_faces_left_open(monkeypatch):
     monkeypatch.setattr(W, "_close_solid_faces", lambda tb, vol, area: [a.reshape(-1) for a in area])
     p = W.config2()
     assert open_faces_into_solid(p) > 100
+
+
+def test_forest_keeps_every_link_inside_its_problem():
+    """the batch forest: block ids offset per problem, every neighbour / child
+    / parent link stays inside its problem, physical-boundary codes (<= -20)
+    and -1 kept, fields concatenated in problem order, each right-hand side
+    scaled to |rhs|_inf = 1 over its fluid cells"""
+    rng = np.random.default_rng(11)
+    parts = [W.batch_problem(rng, "p%d" % k) for k in range(4)]
+    f = W.forest(parts, "forest")
+    tb = f.tables
+    n = tb["num_blocks"]
+    assert n == sum(p.num_blocks for p in parts)
+    off = list(f.block_offsets) + [n]
+    owner = np.zeros(n, dtype=int)
+    for k in range(len(parts)):
+        owner[off[k]:off[k + 1]] = k
+    for key, width in (("neighbor", 6), ("child", 8), ("parent", 1)):
+        links = tb[key].reshape(n, width)
+        for k, p in enumerate(parts):
+            mine = links[off[k]:off[k + 1]]
+            orig = p.tables[key].reshape(-1, width)
+            assert np.array_equal(mine[orig < 0], orig[orig < 0])  # -1 and boundary codes kept
+            inside = mine[orig >= 0]
+            assert np.all(owner[inside] == k)
+            assert np.array_equal(inside - off[k], orig[orig >= 0])
+    nc = f.ncell
+    for k, p in enumerate(parts):
+        assert np.array_equal(f.rhs[off[k] * nc:off[k + 1] * nc], p.rhs)
+        assert np.array_equal(f.vol[off[k] * nc:off[k + 1] * nc], p.vol)
+        fluid = p.vol > 0
+        assert abs(np.abs(p.rhs[fluid]).max() - 1.0) < 1e-12
