@@ -41,7 +41,8 @@ TOL = 1e-8
 CPU_BOTTOM_TOL = 1e-10
 WORKLOADS = {
     "config1": "unit square, 4x4 roots, circle r=0.25 refinement, B=1, Neumann walls",
-    "config2": "rho 1:1000 across a smoothed ellipse, fractional IB disk, p=0 top wall",
+    "config2": "rho 1:1000 across a smoothed ellipse, fractional IB disk (faces beside solid cells closed), "
+               "p=0 top wall",
     "config3": "sphere r=0.2 refinement band, IB sphere mask, B ratio 100 across a blob, p=0 top wall",
     "config4": "256 independent problems (64-1024 leaf blocks, 1-4 ellipse IB solids, rho ratio 10-1000) "
                "solved as one forest",
