@@ -292,12 +292,14 @@ int sayaka_mac_get_rhs_compact(sayaka_mac *h, double *out);
 int sayaka_mac_apply_compact(sayaka_mac *h, int32_t L, const double *x, double *y);
 /* mg_residual_level(L) (src/SayakaMacUtil.cpp:9-49) */
 int sayaka_mac_residual_compact(sayaka_mac *h, int32_t L, const double *x, const double *rhs, double *r);
-/* The residual of mg_residual_level(L) (src/SayakaMacUtil.cpp:9-49) with its
- * norms, allocating no device memory: for callers that cannot call cudaMalloc
- * where they need the norm (a fixed memory pool, a host callback).  No
- * counterpart in the reference.  x, rhs, r: DEVICE pointers to compact
+/* The residual r = rhs - A x of tower L with its norms, allocating no device
+ * memory: for callers that cannot call cudaMalloc where they need the norm (a
+ * fixed memory pool, a host callback).  This entry point has no counterpart
+ * in the reference.  x, rhs, r: DEVICE pointers to compact
  * all-block arrays; norms: DEVICE pointer to 2 doubles, set to {|r|_inf, r.r}
- * over tower L; r is written on the tower's cells only.  Enqueued on stream
+ * over tower L (a NaN in r gives a NaN |r|_inf); r is written on the tower's
+ * cells only.  Runs on the handle's device, whatever device is current.
+ * Enqueued on stream
  * (a cudaStream_t; NULL = the solver's stream) without host synchronisation.
  * Scratch is a static 128 KiB device array: towers of more than 2,097,152
  * cells are rejected (SAYAKA_BAD_INPUT, see sayaka_mac_last_error).  All calls
@@ -306,6 +308,13 @@ int sayaka_mac_residual_compact(sayaka_mac *h, int32_t L, const double *x, const
  * scratch address and should come before any stream capture. */
 int sayaka_mac_residual_norm_noalloc(sayaka_mac *h, int32_t L, const double *x, const double *rhs, double *r,
                                      double *norms, void *stream);
+/* the device solve's own FP64 kernels, for comparison with the reference
+ * arithmetic above: which 0 = out = A in on the finest tower with the fast
+ * operator (per-cell factors, FMA; mg_apply_level, src/SayakaMacOperator.cpp:84-137);
+ * which 1 = one smoothing pass of tower L in mg_smooth_level's order with the
+ * fast sweep (launch variant 0..9, -1 the tuned one; in = phi, in2 = rhs) */
+int sayaka_mac_device_kernel_compact(sayaka_mac *h, int32_t which, int32_t L, int32_t variant, const double *in,
+                                     const double *in2, double *out);
 /* one mg_smooth_level(L) (src/SayakaMacOperator.cpp:140-159, 1028-1112) */
 int sayaka_mac_smooth_compact(sayaka_mac *h, int32_t L, const double *phi, const double *rhs, double *out);
 /* mg_restict_wgt for levels finest-1 .. 1 (src/SayakaMacIB.cpp:157-232) */

@@ -77,6 +77,11 @@ struct Case {
 	int rhs_gauss = 0; // 8 gaussians (config-1 style) instead of random
 	int do_ops = 0;    // dump operator-level tests
 	uint64_t seed = 12345;
+	int cap = 20000;   // block capacity (every TreeData allocates for this many blocks)
+	// bottom BiCGSTAB tolerances of the full solve (the reference defaults
+	// 1e-6 / 1e-6 stall the outer solve on 16^d-cell blocks: the absolute
+	// bottom tolerance weakens the preconditioner as the residual falls)
+	double bot_tol_rel = 1e-6, bot_tol_abs = 1e-6;
 };
 
 // the reference's AmrTree::init with a chosen block capacity (the reference
@@ -219,6 +224,7 @@ public:
 	TreeData &areafrac(int d) { return *m_ib_areafrac[d]; }
 	TreeData &bcoef(int d) { return *m_bcoef[d]; }
 	const BlockBCRecord &bcrec(int b) const { return m_bc_rec[b]; }
+	void setBottomTolerance(double rel, double abs) { m_mg_bot_tol_rel = rel; m_mg_bot_tol_abs = abs; }
 
 	// fractional IB injection: leaf values are written directly, then the same
 	// c/f AVG sync + AVG restriction that calcIBFracByLS performs
@@ -657,6 +663,9 @@ static void run_case(const Case &c, const char *outdir, int cap) {
 		S->setRhs(*ud, 0);
 		S->setZeroSol();
 		S->setTolerance(c.tol_rel, c.tol_abs);
+		S->setBottomTolerance(c.bot_tol_rel, c.bot_tol_abs);
+		D.scalar_d("sv_bot_tol_rel", c.bot_tol_rel);
+		D.scalar_d("sv_bot_tol_abs", c.bot_tol_abs);
 		S->setCGUseMGPrecond(1);
 		S->setVerbose(1);
 		int stat = S->cg_solve();
@@ -768,6 +777,20 @@ static Case make_case(const std::string &name) {
 		c.bamp = 0.25;
 		c.do_ops = 1; c.do_solve = 1; c.tol_rel = 1e-11;
 		c.seed = 4242;
+	} else if (name == "n2") {
+		// the benchmark block size (16x16): 4 levels around a circle,
+		// Neumann x walls / Dirichlet y walls, fractional IB disk, variable B
+		c.nroot[0] = c.nroot[1] = 2;
+		c.nb = 16; c.minlevel = 2; c.maxlevel = 5;
+		c.rc[0] = 0.45; c.rc[1] = 0.52; c.rr = 0.3;
+		c.bc_code[2] = c.bc_code[3] = -21;
+		c.bc_math_m21 = Dirichlet;
+		c.ibc[0] = 0.58; c.ibc[1] = 0.41; c.ibr = 0.11;
+		c.bamp = 0.5;
+		c.do_ops = 1; c.do_solve = 1; c.tol_rel = 1e-10;
+		c.seed = 1616;
+		c.cap = 1500;
+		c.bot_tol_rel = 1e-10; c.bot_tol_abs = 0.0;
 	} else {
 		fprintf(stderr, "unknown 2D case %s\n", name.c_str());
 		exit(2);
@@ -789,6 +812,21 @@ static Case make_case(const std::string &name) {
 		c.ibc[0] = 0.35; c.ibc[1] = 0.6; c.ibc[2] = 0.45; c.ibr = 0.12; c.ib_binary = 1;
 		c.do_ops = 1; c.do_solve = 1; c.tol_rel = 1e-10;
 		c.seed = 31337;
+	} else if (name == "n3") {
+		// the benchmark block size (16^3): levels 2-4 refined around a sphere
+		// holding one corner of the level-3 grid (coarse/fine faces on the
+		// finest tower), Neumann
+		// walls with a Dirichlet top, fractional IB sphere, variable B
+		c.nb = 16; c.minlevel = 2; c.maxlevel = 4;
+		c.rc[0] = 0.47; c.rc[1] = 0.52; c.rc[2] = 0.55; c.rr = 0.16;
+		c.bc_code[5] = -21;
+		c.bc_math_m21 = Dirichlet;
+		c.ibc[0] = 0.45; c.ibc[1] = 0.5; c.ibc[2] = 0.52; c.ibr = 0.06;
+		c.bamp = 0.5;
+		c.do_ops = 1; c.do_solve = 1; c.tol_rel = 1e-10;
+		c.seed = 4096;
+		c.cap = 400;
+		c.bot_tol_rel = 1e-10; c.bot_tol_abs = 0.0;
 	} else {
 		fprintf(stderr, "unknown 3D case %s\n", name.c_str());
 		exit(2);
@@ -808,7 +846,7 @@ int main(int argc, char **argv) {
 			continue;
 		}
 		Case c = make_case(argv[a]);
-		run_case(c, argv[1], 20000);
+		run_case(c, argv[1], c.cap);
 	}
 	return 0;
 }

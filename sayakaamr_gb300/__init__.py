@@ -114,6 +114,7 @@ SIGNATURES = {
     "sayaka_mac_learned_loss_grad": (C.c_int, [_V, _f32p, _f32p, C.c_int32, _f32p, _f32p]),
     "sayaka_mac_learned_forward": (C.c_int, [_V, _f32p, C.c_int32, _f32p]),
     "sayaka_mac_smooth_compact": (C.c_int, [_V, C.c_int32, _f64p, _f64p, _f64p]),
+    "sayaka_mac_device_kernel_compact": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p, _f64p]),
     "sayaka_mac_restrict_compact": (C.c_int, [_V, _f64p, _f64p]),
     "sayaka_mac_prolong_compact": (C.c_int, [_V, _f64p, _f64p]),
     "sayaka_mac_vcycle_compact": (C.c_int, [_V, _f64p, _f64p]),
@@ -516,6 +517,23 @@ class MacSolver:
         a, pa = _f64(phi)
         b, pb = _f64(rhs)
         _check(self.lib.sayaka_mac_smooth_compact(self.h, L, pa, pb, out.ctypes.data_as(_f64p)), "smooth", self.h)
+        return out
+
+    def device_apply(self, x):
+        """the device solve's FP64 operator on the finest tower"""
+        y = self._cells()
+        a, pa = _f64(x)
+        _check(self.lib.sayaka_mac_device_kernel_compact(self.h, 0, 0, -1, pa, None, y.ctypes.data_as(_f64p)),
+               "device_apply", self.h)
+        return y
+
+    def device_smooth(self, L, phi, rhs, variant=-1):
+        """one smoothing pass of tower L by the device solve's FP64 sweep"""
+        out = self._cells()
+        a, pa = _f64(phi)
+        b, pb = _f64(rhs)
+        _check(self.lib.sayaka_mac_device_kernel_compact(self.h, 1, int(L), int(variant), pa, pb,
+                                                         out.ctypes.data_as(_f64p)), "device_smooth", self.h)
         return out
 
     def restrict_sweep(self, x):

@@ -89,11 +89,25 @@ def build_oracle(force=False):
     return ORACLE_LIB
 
 
+def reference_src():
+    """the reference's src/ directory: $REF when set (the variable
+    oracle/Makefile takes), else the Makefile's own default"""
+    ref = os.environ.get("REF")
+    if ref:
+        return ref
+    with open(os.path.join(ORACLE_DIR, "Makefile")) as f:
+        for line in f:
+            if line.startswith("REF") and "?=" in line:
+                return line.split("?=", 1)[1].strip()
+    return None
+
+
 def build_reference_oracle():
     """oracle/_ref from the reference sources (only where they are present)."""
-    if not os.path.isdir("/root/reference/src"):
+    ref = reference_src()
+    if not ref or not os.path.isdir(ref):
         return None
-    _run(["make", "-C", ORACLE_DIR, "-j8", "-s"])
+    _run(["make", "-C", ORACLE_DIR, "-j8", "-s", "REF=" + ref])
     return os.path.join(ORACLE_DIR, "_ref")
 
 

@@ -590,6 +590,7 @@ int sayaka_mac_get_sol(sayaka_mac *h, double *data, int32_t ncomp, int32_t ngrow
     double *st = staging(h, (size_t)g.num_blocks() * g.ncell());
     if (!st) return (int)SAYAKA_CUDA_ERROR;
     g.get_sol(st);
+    if (!g.error().empty()) return status_of(h);  // the copy failed: leave the caller's buffer alone
     unpack(L, g.num_blocks(), st, data);
     return (int)SAYAKA_OK;
   });
@@ -874,12 +875,26 @@ int sayaka_mac_residual_norm_noalloc(sayaka_mac *h, int32_t L, const double *x, 
     h->err = "solver not created";
     return SAYAKA_BAD_INPUT;
   }
+  // the handle's device is current for the scratch lookup and the launch,
+  // whatever device the caller has current (restored on return)
+  DeviceScope on_device(h->gpu->device());
   std::string why;
   const cudaStream_t s = stream ? (cudaStream_t)stream : h->gpu->stream();
   const int st = h->gpu->residual_norm_noalloc(L, x, rhs, r, norms, s, &why);
   if (st == 0) return SAYAKA_OK;
   h->err = why;
   return st == 1 ? SAYAKA_BAD_INPUT : SAYAKA_CUDA_ERROR;
+}
+int sayaka_mac_device_kernel_compact(sayaka_mac *h, int32_t which, int32_t L, int32_t variant, const double *in,
+                                     const double *in2, double *out) {
+  return guarded(h, [&] {
+    const int r = h->gpu->device_kernel_compact(which, L, variant, in, in2, out);
+    if (r == 1) {
+      h->err = "device_kernel_compact: which must be 0 or 1, L a tower of the tree, variant < 10, pointers non-null";
+      return (int)SAYAKA_BAD_INPUT;
+    }
+    return (int)SAYAKA_OK;  // CUDA errors are reported by status_of
+  });
 }
 int sayaka_mac_smooth_compact(sayaka_mac *h, int32_t L, const double *phi, const double *rhs, double *out) {
   return guarded(h, [&] {

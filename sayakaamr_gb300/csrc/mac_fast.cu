@@ -1572,6 +1572,55 @@ int MacGpu::enqueue_kernel(int which, int L) {
   return err_.empty() ? 0 : -1;
 }
 
+// Test hook: the device solve's own FP64 kernels on given compact all-block
+// arrays (host pointers), for comparison with the reference arithmetic.
+// which 0: out = A in on the finest tower with the solve's operator (per-cell
+// factors P, S and FMA, k_op_red); which 1: one smoothing pass of tower L
+// (sublevels finest to coarsest, red then black, as mg_smooth_level) with the
+// solve's FP64 sweep, launch variant `variant` (-1: the tuned one); in = phi,
+// in2 = rhs.  Uses (and clobbers) the handle's work vectors.
+int MacGpu::device_kernel_compact(int which, int L, int variant, const double *in, const double *in2, double *out) {
+  if (which < 0 || which > 1 || !in || !out || (which == 1 && !in2)) return 1;
+  if (which == 1 && (L < 1 || L > finest_ || towers_[L].all.n == 0)) return 1;
+  if (variant >= kRbgsVariants) return 1;
+  if (prepare_device() != 0) return 2;
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  if (which == 0) {
+    const BlockList TL = tower_list(finest_);
+    const long w = (long)TL.n * ncell_;
+    CKR_(cudaMemcpyAsync(vec_[kTMP], in, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);
+    CKR_(cudaMemsetAsync(vec_[kV], 0, n * sizeof(double), stream_), 2);
+    CKR_(cudaMemsetAsync(vec_[kRHAT], 0, n * sizeof(double), stream_), 2);
+    CKR_(cudaMemsetAsync(d_st_, 0, sizeof(FState), stream_), 2);
+    if (tt_.ndim == 2)
+      k_op_red<2, 0, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kTMP], vec_[kV], vec_[kRHAT],
+                                                                d_opP_, d_opS_, d_st_, d_part_, d_cnt_);
+    else
+      k_op_red<3, 0, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kTMP], vec_[kV], vec_[kRHAT],
+                                                                d_opP_, d_opS_, d_st_, d_part_, d_cnt_);
+    CKR_(cudaGetLastError(), 2);
+    CKR_(cudaMemcpyAsync(out, vec_[kV], n * sizeof(double), cudaMemcpyDeviceToHost, stream_), 2);
+  } else {
+    const int v = variant >= 0 ? variant : rbgs_var<double>();
+    CKR_(cudaMemcpyAsync(vec_[kCORR], in, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);
+    CKR_(cudaMemcpyAsync(vec_[kRESID], in2, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);
+    for (int ll = L; ll >= 1; ll--) {
+      const BlockList sl = sublevel_list(L, ll);
+      if (sl.n == 0) continue;
+      for (int rb = 0; rb < 2; rb++)
+        launch_rbgs<double>(topo_, c64_, sl, rb, vec_[kCORR], vec_[kRESID], nullptr, stream_, false, v);
+    }
+    CKR_(cudaGetLastError(), 2);
+    CKR_(cudaMemcpyAsync(out, vec_[kCORR], n * sizeof(double), cudaMemcpyDeviceToHost, stream_), 2);
+  }
+  CKR_(cudaStreamSynchronize(stream_), 2);
+  if (rbgs_bulk_error(true) > 0) {
+    fail("bulk-copy smoother: an mbarrier wait timed out");
+    return 2;
+  }
+  return err_.empty() ? 0 : 2;
+}
+
 // self-test of the integer-pipe conversions against the hardware ones
 __global__ void k_fp_selftest(int n, const double *d, const float *f, float *nar, float *nar_hw, double *wid,
                               double *wid_hw, double *wid0, double *wid0_hw) {

@@ -660,6 +660,10 @@ __global__ void __launch_bounds__(kStreamThreads, 1) k_rbgs_stream(Topo t, Coef<
   auto issue = [&](int pp, int j) {  // thread 0: copies of list entry pp into buffer j
     const int bb = L.blocks[pp];
     T *bt = buf0 + j * buf_elems;
+    // buffer j was last read and written through the generic proxy (the
+    // sweep and the copy-out, ordered before this point by __syncthreads);
+    // the bulk copies write it through the async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_expect_tx(&mbar[j], tx);
     bulk_copy(bt, phi + (long)bb * ncell, tile_bytes, &mbar[j]);
     bulk_copy(bt + ncell, rhs + (long)bb * ncell, tile_bytes, &mbar[j]);
@@ -722,6 +726,10 @@ __global__ void __launch_bounds__(kStreamThreads, 1) k_rbgs_stream(Topo t, Coef<
     phase[j] ^= 1u;
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
+        // the error word makes the solve report a CUDA error; should the
+        // bounded drain below also time out, copies may still be landing in
+        // shared memory this CTA released, so nothing the device computes
+        // after the flag is set is trusted (the host reports the failure)
         atomicExch(&g_rbgs_err, 1);
         // let this CTA's copies land before it exits
         mbar_wait(&mbar[j], phase[j] ^ 1u, kWait);

@@ -47,8 +47,11 @@ __device__ __forceinline__ double na_wsum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// max that keeps NaN (fmax drops it): a residual with a NaN in it must
+// report a NaN |r|_inf, as the device solve's norms do
+__device__ __forceinline__ double na_max(double a, double b) { return (a != a || b != b) ? a + b : fmax(a, b); }
 __device__ __forceinline__ double na_wmax(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) v = na_max(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 
@@ -72,7 +75,7 @@ __global__ void __launch_bounds__(kNaThreads) k_resid_norm_na(Topo t, Coef<doubl
     const long q = (long)L.blocks[p] * ncell + ci;
     const double rv = c.vf[q] > 0 ? rhs[q] - ax : 0.0;
     r[q] = rv;
-    m = fmax(m, fabs(rv));
+    m = na_max(m, fabs(rv));
     s += rv * rv;
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -87,7 +90,7 @@ __global__ void __launch_bounds__(kNaThreads) k_resid_norm_na(Topo t, Coef<doubl
   if (threadIdx.x == 0) {
     double bm = 0.0, bs = 0.0;
     for (int i = 0; i < kNaThreads / 32; i++) {
-      bm = fmax(bm, sh[0][i]);
+      bm = na_max(bm, sh[0][i]);
       bs += sh[1][i];
     }
     scratch[2 * blockIdx.x] = bm;
@@ -101,7 +104,7 @@ __global__ void __launch_bounds__(kNaThreads) k_resid_norm_na(Topo t, Coef<doubl
   m = 0.0;
   s = 0.0;
   for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-    m = fmax(m, ((volatile double *)scratch)[2 * b]);
+    m = na_max(m, ((volatile double *)scratch)[2 * b]);
     s += ((volatile double *)scratch)[2 * b + 1];
   }
   __syncthreads();
@@ -115,7 +118,7 @@ __global__ void __launch_bounds__(kNaThreads) k_resid_norm_na(Topo t, Coef<doubl
   if (threadIdx.x == 0) {
     double fm = 0.0, fs = 0.0;
     for (int i = 0; i < kNaThreads / 32; i++) {
-      fm = fmax(fm, sh[0][i]);
+      fm = na_max(fm, sh[0][i]);
       fs += sh[1][i];
     }
     out[0] = fm;

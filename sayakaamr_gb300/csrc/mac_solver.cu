@@ -743,10 +743,12 @@ void MacGpu::set_sol(const double *all, bool dev) {
                      dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream_));
 }
 void MacGpu::zero_sol() { CK(cudaMemsetAsync(vec_[kSOL], 0, (size_t)tt_.num_blocks * ncell_ * sizeof(double), stream_)); }
-void MacGpu::get_sol(double *all, bool dev) const {
-  cudaMemcpyAsync(all, vec_[kSOL], (size_t)tt_.num_blocks * ncell_ * sizeof(double),
-                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream_);
-  cudaStreamSynchronize(stream_);
+void MacGpu::get_sol(double *all, bool dev) {
+  // a failed copy or a failed kernel before it is reported (status
+  // SAYAKA_CUDA_ERROR), never returned as stale data with status OK
+  CK(cudaMemcpyAsync(all, vec_[kSOL], (size_t)tt_.num_blocks * ncell_ * sizeof(double),
+                     dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
 }
 
 // ---------------------------------------------------------------------------

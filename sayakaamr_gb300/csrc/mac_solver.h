@@ -81,7 +81,7 @@ class MacGpu {
   void set_rhs(const double *all, bool on_device = false);
   void set_sol(const double *all, bool on_device = false);
   void zero_sol();
-  void get_sol(double *all, bool on_device = false) const;
+  void get_sol(double *all, bool on_device = false);
   double *rhs_dev() { return vec_[kRHS]; }
   double *sol_dev() { return vec_[kSOL]; }
 
@@ -96,6 +96,9 @@ class MacGpu {
   int prepare_device();
   int solve_state(SolveInfo *info);
   int enqueue_kernel(int which, int L);
+  // the device solve's FP64 operator (which 0) or smoothing pass of tower L
+  // (which 1) on given compact host arrays (0 ok, 1 bad input, 2 CUDA error)
+  int device_kernel_compact(int which, int L, int variant, const double *in, const double *in2, double *out);
   int tower_size(int L, int sublevel) const;
   int tuned_smoother(int precision, float *us, int n) const;
   int bottom_level() const { return bottom_ready_ ? bot_level_ : -1; }

@@ -296,10 +296,11 @@ def config2(seed=2, nb=16, max_level=6, roots=2):
     return _finish("config2", t, tb, vol, area, bface, f, True, dict(tol_rel=1e-8), dirichlet_faces=(3,))
 
 
-def config3(seed=3, nb=16, max_level=5):
+def config3(seed=3, nb=16, max_level=5, band=3.0):
     """3D, 16^3 blocks, 5 levels refined on the sphere r=0.2 (a band of 3
     block widths: 3872 leaf blocks, 15.9M cells), IB solid sphere r=0.08
-    (binary mask), B ratio 100 across a seeded blob, p=0 on the top wall."""
+    (binary mask), B ratio 100 across a seeded blob, p=0 on the top wall.
+    A narrower band (in block widths) gives a smaller tree of the same shape."""
     rng = np.random.default_rng(seed)
     bc_ = rng.uniform(0.35, 0.65, 3)
     br = rng.uniform(0.12, 0.18)
@@ -313,7 +314,7 @@ def config3(seed=3, nb=16, max_level=5):
         return r - br
 
     def need(lo, hi, level):
-        return _straddle(sphere, lo, hi, 3.0)
+        return _straddle(sphere, lo, hi, band)
 
     t = refine_tree(3, nb, (1, 1, 1), (0, 0, 0), (1, 1, 1), 2, max_level, need)
     tb = t.tables()

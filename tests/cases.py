@@ -26,6 +26,16 @@ CASES = {
     "t3n": dict(ndim=3, nroot=(1, 1, 1), nb=4, minlevel=2, maxlevel=4, lo=(0, 0, 0), hi=(1, 1, 1),
                 rc=(0.5, 0.5, 0.5), rr=0.2, bc_code=(-20,) * 6, bc_m20=sg.NEUMANN, bc_m21=sg.NEUMANN,
                 ibc=(0.35, 0.6, 0.45), ibr=0.12, ib_binary=1, bamp=0.0, do_ops=1, tol_rel=1e-10),
+    # the benchmark block size (16^d cells); fixtures hold digests of the
+    # reference's results, and its solve ran with a converged bottom solve
+    "n2": dict(ndim=2, nroot=(2, 2, 1), nb=16, minlevel=2, maxlevel=5, lo=(0, 0, 0), hi=(1, 1, 0),
+               rc=(0.45, 0.52, 0), rr=0.3, bc_code=(-20, -20, -21, -21, -20, -20), bc_m20=sg.NEUMANN,
+               bc_m21=sg.DIRICHLET, ibc=(0.58, 0.41, 0), ibr=0.11, ib_binary=0, bamp=0.5, do_ops=1,
+               tol_rel=1e-10, bot_tol=(1e-10, 0.0)),
+    "n3": dict(ndim=3, nroot=(1, 1, 1), nb=16, minlevel=2, maxlevel=4, lo=(0, 0, 0), hi=(1, 1, 1),
+               rc=(0.47, 0.52, 0.55), rr=0.16, bc_code=(-20, -20, -20, -20, -20, -21), bc_m20=sg.NEUMANN,
+               bc_m21=sg.DIRICHLET, ibc=(0.45, 0.5, 0.52), ibr=0.06, ib_binary=0, bamp=0.5, do_ops=1,
+               tol_rel=1e-10, bot_tol=(1e-10, 0.0)),
 }
 
 

@@ -6,7 +6,7 @@ import pytest
 
 import golden_io
 from cases import CASES, build_tree
-from test_gpu_parity import block_slice, setup_solver, solution_error
+from test_gpu_parity import block_slice, reference_solution, setup_solver, solution_error
 
 pytestmark = pytest.mark.gpu
 
@@ -22,7 +22,7 @@ def test_device_solve_matches_reference(name, precision):
     assert info["status"] == 0, info
     blocks, _ = t.tower(tb["level"].max())
     sol = block_slice(S.get_sol_compact(), blocks, S.ncell)
-    err = solution_error(name, tb, S, blocks, sol, g["sv_sol"])
+    err = solution_error(name, tb, S, blocks, sol, reference_solution(name, g, t, tb, S))
     assert err < 1e-8, (name, precision, err, info)
 
 

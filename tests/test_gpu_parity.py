@@ -52,10 +52,36 @@ def block_slice(arr, blocks, per):
 
 
 def same_bits(a, b):
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
-    # -0.0 == +0.0 is accepted; everything else must match exactly
-    return a.shape == b.shape and bool(np.all((a == b) | (np.isnan(a) & np.isnan(b))))
+    # -0.0 == +0.0 is accepted; everything else must match exactly (b: a
+    # fixture array or, for the 16^d-cell cases, its digest)
+    return golden_io.matches(a, b)
+
+
+def case_oracle(name, tb, S):
+    """the C oracle on the solver's synced coefficients (pinned bit-exact
+    against the reference's by test_coefficients)"""
+    from oracle import pyoracle
+    nd = tb["ndim"]
+    return pyoracle.Oracle(tb, bc_table(name, tb), S.get_coef(2), [S.get_coef(1, d) for d in range(nd)],
+                           [S.get_coef(0, d) for d in range(nd)])
+
+
+def reference_solution(name, g, t, tb, S):
+    """the reference's converged solution on the finest tower's blocks; for a
+    digest fixture, the oracle's solve with the reference's parameters,
+    checked bit for bit against the reference's digest first"""
+    ref = g["sv_sol"]
+    if not isinstance(ref, golden_io.Digest):
+        return ref
+    from oracle import pyoracle
+    c = CASES[name]
+    prm = pyoracle.params(tol_rel=c["tol_rel"], tol_abs=0.0, bot_tol_rel=float(g["sv_bot_tol_rel"][0]),
+                          bot_tol_abs=float(g["sv_bot_tol_abs"][0]))
+    sol, info = case_oracle(name, tb, S).cg_solve(g["sv_rhs"], prm)
+    blocks, _ = t.tower(tb["level"].max())
+    sol = block_slice(sol, blocks, S.ncell)
+    assert ref.matches(sol), "the oracle's solve of %s differs from the reference's" % name
+    return sol
 
 
 def test_coefficients(prob):
@@ -165,20 +191,26 @@ def mean_removed_vc_p(name, g, t, tb, S):
 
 def test_vcycle(prob):
     """The V-cycle's bottom BiCGSTAB stops at a 1e-6 residual, so against the
-    reference it agrees to that tolerance only; against the bit-pinned oracle
-    with a converged bottom solve (1e-13) it agrees to 1e-10."""
+    reference it agrees only to the level that tolerance allows; against the
+    bit-pinned oracle with a converged bottom solve (1e-13) it agrees to 1e-10."""
     from oracle import pyoracle
     name, g, t, tb, S = prob
     p = mean_removed_vc_p(name, g, t, tb, S)
     blocks, _ = t.tower(tb["level"].max())
     S.set_params(n_post_smooth=2, bot_tol_rel=1e-6, bot_tol_abs=1e-6, bot_max_iter=2000, precision=0, bottom=0)
     mine = block_slice(S.vcycle(p), blocks, S.ncell)
+    O = case_oracle(name, tb, S)
     ref = g["vc_phat"]
+    if isinstance(ref, golden_io.Digest):
+        # the oracle's V-cycle with the reference's bottom parameters is the
+        # reference's, bit for bit
+        orc = block_slice(O.vcycle(p, pyoracle.params()), blocks, S.ncell)
+        assert ref.matches(orc), name
+        ref = orc
     err = np.linalg.norm(mine - ref) / np.linalg.norm(ref)
-    assert err < 1e-4, (name, err)
-    nd = tb["ndim"]
-    O = pyoracle.Oracle(tb, bc_table(name, tb), S.get_coef(2), [S.get_coef(1, d) for d in range(nd)],
-                        [S.get_coef(0, d) for d in range(nd)])
+    # the two bottom BiCGSTABs stop at |r| < 1e-6 (absolute) after different
+    # iterates (their dot products sum in different orders): 2.3e-4 on n3
+    assert err < 1e-3, (name, err)
     S.set_params(bot_tol_rel=1e-13, bot_tol_abs=0.0)
     mine = block_slice(S.vcycle(p), blocks, S.ncell)
     orc = block_slice(O.vcycle(p, pyoracle.params(bot_tol_rel=1e-13, bot_tol_abs=0.0)), blocks, S.ncell)
@@ -221,7 +253,7 @@ def test_solve_matches_reference(name):
     assert info["status"] == 0, info
     blocks, _ = t.tower(tb["level"].max())
     sol = block_slice(S.get_sol_compact(), blocks, S.ncell)
-    err = solution_error(name, tb, S, blocks, sol, g["sv_sol"])
+    err = solution_error(name, tb, S, blocks, sol, reference_solution(name, g, t, tb, S))
     assert err < 1e-8, (name, err, info)
 
 

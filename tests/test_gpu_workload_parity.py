@@ -1,0 +1,121 @@
+"""The device solve's fast kernels and the benchmark workloads against the
+reference arithmetic, at the benchmark block size (16^d cells).
+
+* The device solve's FP64 operator (per-cell factors, FMA) and its FP64
+  red-black sweeps (every launch variant the autotuner may pick, the
+  shared-memory tile included) against the reference-arithmetic kernels,
+  which the fixtures pin bit for bit: relative L2 within FAST_RTOL.
+* Full-size and reduced benchmark workloads: the device solve in both
+  V-cycle precisions against the C oracle's converged FP64 solve (the oracle
+  is bit-exact to the reference on every fixture), relative L2 over fluid
+  leaf cells within SOL_RTOL."""
+import numpy as np
+import pytest
+
+import golden_io
+from cases import CASES
+from test_gpu_parity import block_slice, setup_solver
+
+pytestmark = pytest.mark.gpu
+
+FAST_RTOL = 1e-14   # FMA and precomputed factors against the reference's operation order
+SOL_RTOL = 1e-8     # converged solutions (spec tolerance)
+SOLVE_TOL = 1e-11   # relative L-inf residual both solves reach before comparing
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("name", ["n2", "n3", "t2s", "t3s"])
+def test_fast_operator_close_to_reference(name):
+    g, t, tb, S = setup_solver(name)
+    S.set_params(use_mg_precond=1, bottom=1, precision=0)
+    n, nc = tb["num_blocks"], S.ncell
+    x = golden_io.seeded_input(name, "op_x", n * nc)
+    finest = int(tb["level"].max())
+    blocks, _ = t.tower(finest)
+    ref = block_slice(S.apply(finest, x), blocks, nc)
+    assert golden_io.matches(ref, g["op_apply_%d" % finest]), name  # reference arithmetic, bit for bit
+    fast = block_slice(S.device_apply(x), blocks, nc)
+    assert rel(fast, ref) < FAST_RTOL, (name, rel(fast, ref))
+
+
+@pytest.mark.parametrize("variant", [-1, 0, 2, 4, 5, 6, 7, 8, 9])
+@pytest.mark.parametrize("name", ["n2", "n3"])
+def test_fast_sweeps_close_to_reference(name, variant):
+    g, t, tb, S = setup_solver(name)
+    S.set_params(use_mg_precond=1, bottom=1, precision=0)
+    n, nc = tb["num_blocks"], S.ncell
+    corr = golden_io.seeded_input(name, "sm_corr0", n * nc)
+    res = golden_io.seeded_input(name, "sm_resid", n * nc)
+    finest = int(tb["level"].max())
+    for L in (finest, finest - 1):
+        key = "sm_out_%d" % L
+        blocks, _ = t.tower(L)
+        ref = block_slice(S.smooth(L, corr, res), blocks, nc)
+        assert golden_io.matches(ref, g[key]), (name, L)
+        fast = block_slice(S.device_smooth(L, corr, res, variant), blocks, nc)
+        assert rel(fast, ref) < FAST_RTOL, (name, L, variant, rel(fast, ref))
+
+
+def oracle_solution(prob):
+    from oracle import pyoracle
+    vf, af, bc = pyoracle.setup_coefficients(prob.tables, prob.bc, prob.vol, prob.area, prob.bface)
+    O = pyoracle.Oracle(prob.tables, prob.bc, vf, af, bc)
+    sol, info = O.cg_solve(prob.rhs, pyoracle.params(tol_rel=SOLVE_TOL, tol_abs=0.0, bot_tol_rel=1e-10,
+                                                     bot_tol_abs=0.0))
+    assert info["status"] == 0, info
+    return sol, vf
+
+
+def fluid_leaf_error(prob, vf, sol, ref):
+    nc = prob.ncell
+    leaf = prob.leaf
+    m = vf.reshape(-1, nc)[leaf].reshape(-1) > 0
+    a = sol.reshape(-1, nc)[leaf].reshape(-1)[m]
+    b = ref.reshape(-1, nc)[leaf].reshape(-1)[m]
+    return rel(a, b)
+
+
+def device_solutions(prob):
+    from sayakaamr_gb300 import workloads
+    S = workloads.make_solver(prob)
+    out = {}
+    for precision in (0, 1):
+        S.set_zero_sol()
+        S.set_params(tol_rel=SOLVE_TOL, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=precision, bottom=1)
+        info = S.cg_solve()
+        assert info["status"] == 0 and info["rnorm"] < SOLVE_TOL * info["rnorm0"], (precision, info)
+        out[precision] = S.get_sol_compact()
+    return out
+
+
+@pytest.mark.parametrize("which", ["config2", "config3_reduced"])
+def test_workload_solve_matches_oracle(which):
+    """config2 at full size (339,712 cells); config3's geometry on a 4-level
+    tree with a narrower refinement band (1,179,648 cells, levels 3-4)"""
+    from sayakaamr_gb300 import workloads
+    prob = workloads.config2() if which == "config2" else workloads.config3(max_level=4, band=0.5)
+    ref, vf = oracle_solution(prob)
+    for precision, sol in device_solutions(prob).items():
+        err = fluid_leaf_error(prob, vf, sol, ref)
+        assert err < SOL_RTOL, (which, precision, err)
+
+
+def test_batch_problems_match_oracle():
+    """the first four problems of the 256-problem batch workload, solved as
+    one forest on the device, each against the oracle's solve of that
+    problem alone"""
+    from sayakaamr_gb300 import workloads
+    rng = np.random.default_rng(4)  # the batch workload's seed: its first problems
+    parts = [workloads.batch_problem(rng, "config4_%d" % k) for k in range(4)]
+    F = workloads.forest(parts, "config4_head")
+    sols = device_solutions(F)
+    for k, p in enumerate(parts):
+        ref, vf = oracle_solution(p)
+        b0 = F.block_offsets[k]
+        for precision, sol in sols.items():
+            mine = sol.reshape(-1, p.ncell)[b0:b0 + p.num_blocks].reshape(-1)
+            err = fluid_leaf_error(p, vf, mine, ref)
+            assert err < SOL_RTOL, (k, precision, err)

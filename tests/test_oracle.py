@@ -18,9 +18,17 @@ def oracle_for(name):
     tb = t.tables()
     nd, nb, n = tb["ndim"], tb["nb"], tb["num_blocks"]
     nc, nfb = nb ** nd, (nb + 1) * nb ** (nd - 1)
-    vf = g["vf"] if "vf" in g else np.ones(n * nc)
-    af = [g["af%d" % d] if "af%d" % d in g else np.ones(n * nfb) for d in range(nd)]
-    bc = [g["bcoef%d" % d] if "bcoef%d" % d in g else np.ones(n * nfb) for d in range(nd)]
+    if isinstance(g.get("vf"), golden_io.Digest):
+        # digest fixture: the oracle's own coefficient setup, pinned against
+        # the reference's synced fields by test_coefficient_setup
+        from test_gpu_parity_helpers import fractional_ib
+        vol, areas = fractional_ib(name, tb)
+        vf, af, bc = pyoracle.setup_coefficients(tb, bc_table(name, tb), vol, areas,
+                                                 [g["in_b%d" % d] for d in range(nd)])
+    else:
+        vf = g["vf"] if "vf" in g else np.ones(n * nc)
+        af = [g["af%d" % d] if "af%d" % d in g else np.ones(n * nfb) for d in range(nd)]
+        bc = [g["bcoef%d" % d] if "bcoef%d" % d in g else np.ones(n * nfb) for d in range(nd)]
     return g, t, tb, pyoracle.Oracle(tb, bc_table(name, tb), vf, af, bc)
 
 
@@ -34,7 +42,8 @@ def rows(a, blocks, per):
 
 
 def exact(a, b):
-    return a.shape == b.shape and bool(np.all(a == b))
+    """bit-for-bit (fixture arrays or their digests)"""
+    return golden_io.matches(a, b)
 
 
 def test_towers(prob):
@@ -106,23 +115,36 @@ def vc_input(name, g, t, tb, vf):
 def test_vcycle_bit_exact(prob):
     name, g, t, tb, O = prob
     n, nc = tb["num_blocks"], O.ncell
-    vf = g["vf"] if "vf" in g else np.ones(n * nc)
+    vf = g["vf"] if "vf" in g and not isinstance(g["vf"], golden_io.Digest) else oracle_vf(O, n * nc)
     p = vc_input(name, g, t, tb, vf)
     phat = O.vcycle(p, pyoracle.params())
     assert exact(rows(phat, t.tower(tb["level"].max())[0], nc), g["vc_phat"]), name
 
 
-@pytest.mark.parametrize("name", ["t2b", "t3n", "t3s"])
+def oracle_vf(O, n):
+    """the volume fraction the oracle was given"""
+    return np.ctypeslib.as_array(O.P.vf, shape=(n,)).copy()
+
+
+def solve_params(name, g):
+    """the reference solve's parameters as the fixture records them"""
+    c = CASES[name]
+    kw = dict(tol_rel=c["tol_rel"], tol_abs=0.0)
+    if "sv_bot_tol_rel" in g:
+        kw.update(bot_tol_rel=float(g["sv_bot_tol_rel"][0]), bot_tol_abs=float(g["sv_bot_tol_abs"][0]))
+    return pyoracle.params(**kw)
+
+
+@pytest.mark.parametrize("name", ["t2b", "t3n", "t3s", "n2", "n3"])
 def test_solve_bit_exact(name):
     g, t, tb, O = oracle_for(name)
-    c = CASES[name]
-    sol, info = O.cg_solve(g["sv_rhs"], pyoracle.params(tol_rel=c["tol_rel"], tol_abs=0.0))
+    sol, info = O.cg_solve(g["sv_rhs"], solve_params(name, g))
     assert info["status"] == 0
     leaf = t.tower(tb["level"].max())[0]
     assert exact(rows(sol, leaf, O.ncell), g["sv_sol"]), name
 
 
-@pytest.mark.parametrize("name", ["t2s", "t3s"])
+@pytest.mark.parametrize("name", ["t2s", "t3s", "n2", "n3"])
 def test_coefficient_setup(name):
     """setCoefB / IB-fraction sync + restriction against the reference"""
     from test_gpu_parity_helpers import fractional_ib

@@ -98,3 +98,77 @@ def test_noalloc_residual_at_the_size_limit_and_beyond():
     assert "4194304 cells" in msg and "2097152" in msg, msg
     torch.cuda.synchronize()
     assert float(dn.abs().sum()) == 0.0
+
+
+def test_noalloc_residual_keeps_nan():
+    """a NaN in the residual reaches |r|_inf (a dropped NaN would let a
+    diverged iterate pass a convergence test)"""
+    g, t, tb, S = setup_solver("t2s")
+    L = int(tb["level"].max())
+    n = S.num_blocks * S.ncell
+    rng = np.random.default_rng(7)
+    x, rhs = rng.standard_normal(n), rng.standard_normal(n)
+    blocks, _ = t.tower(L)
+    vf = S.get_coef(2)
+    cell = next(int(b) * S.ncell + q for b in blocks for q in range(S.ncell) if vf[int(b) * S.ncell + q] > 0)
+    rhs[cell] = np.nan
+    (r, norms), = _noalloc_twice(S, L, [(x, rhs)])
+    assert np.isnan(r[cell])
+    assert np.isnan(norms[0]) and np.isnan(norms[1]), norms
+
+
+def test_noalloc_residual_allocates_nothing():
+    """free device memory is the same before and after warmed-up calls (the
+    inputs and outputs are made beforehand)"""
+    import torch
+    g, t, tb, S = setup_solver("t3n")
+    L = int(tb["level"].max())
+    n = S.num_blocks * S.ncell
+    rng = np.random.default_rng(11)
+    dx = torch.from_numpy(rng.standard_normal(n)).cuda()
+    drhs = torch.from_numpy(rng.standard_normal(n)).cuda()
+    dr = torch.zeros_like(dx)
+    dn = torch.zeros(2, dtype=torch.float64, device="cuda")
+    fn = _entry(S.lib)
+    stream = torch.cuda.current_stream()
+
+    def call():
+        rc = fn(S.h, L, dx.data_ptr(), drhs.data_ptr(), dr.data_ptr(), dn.data_ptr(), stream.cuda_stream)
+        assert rc == sg.OK, S.lib.sayaka_mac_last_error(S.h)
+
+    call()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    r = S.residual(L, dx.cpu().numpy(), drhs.cpu().numpy())
+    assert np.array_equal(dr.cpu().numpy(), r)
+
+
+def test_noalloc_residual_runs_on_the_handle_device():
+    """with another device current, the call still runs on the device the
+    handle's buffers live on (needs two GPUs)"""
+    import torch
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two visible GPUs")
+    torch.cuda.set_device(0)
+    g, t, tb, S = setup_solver("t2s")
+    L = int(tb["level"].max())
+    n = S.num_blocks * S.ncell
+    rng = np.random.default_rng(3)
+    x, rhs = rng.standard_normal(n), rng.standard_normal(n)
+    dx = torch.from_numpy(x).to("cuda:0")
+    drhs = torch.from_numpy(rhs).to("cuda:0")
+    dr = torch.zeros_like(dx)
+    dn = torch.zeros(2, dtype=torch.float64, device="cuda:0")
+    try:
+        torch.cuda.set_device(1)
+        rc = _entry(S.lib)(S.h, L, dx.data_ptr(), drhs.data_ptr(), dr.data_ptr(), dn.data_ptr(), None)
+        assert rc == sg.OK, S.lib.sayaka_mac_last_error(S.h)
+        assert torch.cuda.current_device() == 1
+    finally:
+        torch.cuda.set_device(0)
+    torch.cuda.synchronize(0)
+    _check_against_existing(S, L, x, rhs, dr.cpu().numpy(), dn.cpu().numpy())
