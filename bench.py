@@ -1,7 +1,10 @@
 #!/usr/bin/env python3
 """Benchmark: MAC-Poisson time to a 1e-8 relative residual and leaf cells/s on
-one GB300, for the config-2 workload (2D, 16x16 blocks, 6 levels, two-phase
-B = 1/rho with rho 1:1000, fractional IB disk, seeded Gaussian RHS).
+one GB300.  Default workload: the largest single-GPU configuration, the batch
+of 256 independent 2D problems (64-1024 leaf blocks of 16x16 cells each, 1-4
+ellipse IB solids, rho ratio 10-1000; 29.4M leaf cells) solved as one forest;
+--config selects the others (config2: 2D 6 levels, config3: 3D 16^3 blocks,
+config5: the elbow pipe).
 
 A step is one complete MG-preconditioned BiCGSTAB solve from a zero initial
 guess to |r|_inf < 1e-8 |r0|_inf (the reference's criterion,
@@ -13,7 +16,13 @@ src/SayakaMacSolver.cpp:891).
   e2e   : the same through the C ABI with host buffers in the reference's
           TreeData layout (setRhs -> cg_solve -> getSol per step)
   cpu_baseline / --impl reference : the C oracle (bit-exact restatement of
-          the reference solver) on the host cores, bounded sample.
+          the reference solver) on the host cores, bounded sample (for the
+          batch workload: whole problems of the batch, one per core).
+  solvers : time to 1e-8 of plain FP64 MG-BiCGSTAB, of the FP32 V-cycle and
+          of the learned correction with the FP32 V-cycle, same workload.
+  error_vs_oracle : relative L2 over fluid leaf cells of the device solution
+          against the C oracle's converged FP64 solve (the batch workload:
+          its first problems), and the final true residual.
 """
 import argparse
 import json
@@ -58,13 +67,20 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="config2")
+    ap.add_argument("--config", default="config4")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the plain-FP64 / FP32 / learned comparison and the oracle error")
     ap.add_argument("--precision", type=int, default=-1,
                     help="V-cycle precision: 1 FP32, 0 FP64, -1 (default) the faster of the two, timed during "
                          "warm-up (the outer BiCGSTAB and its 1e-8 test are FP64 either way)")
     ap.add_argument("--n-post", type=int, default=-1,
                     help="post-smoothing sweeps per level (the reference's setPostSmoothNum, its default 2); "
                          "-1 (default): 1 or 2, whichever solves faster in the warm-up timing")
+    ap.add_argument("--smoother", type=int, default=-1,
+                    help="V-cycle smoother: 0 red-black sweeps (one launch per colour), 1 block-hybrid passes "
+                         "(Gauss-Seidel inside a block, Jacobi between blocks); -1 (default): timed during warm-up")
+    ap.add_argument("--inner-sweeps", type=int, default=-1,
+                    help="smoother 1: red-black sweeps per block and pass (-1: 2 or 3, timed during warm-up)")
     ap.add_argument("--pdl", type=int, default=0, help="programmatic dependent launch between kernels")
     ap.add_argument("--vcycle-kernel", type=int, default=0,
                     help="0: one launch per phase, 1: whole V-cycle as one cooperative launch, "
@@ -241,6 +257,37 @@ def _cpu_worker(args):
     return cpu_solve(prob, max_iter, budget)
 
 
+def cpu_payload(p):
+    """a problem without its tree handle (picklable for the worker processes)"""
+    from sayakaamr_gb300 import workloads
+    q = workloads.Problem(p.name, None, p.tables, p.bc, p.vol, p.area, p.bface, p.rhs, p.params)
+    return q
+
+
+def _cpu_part_worker(q):
+    """one whole problem of the batch solved to 1e-8 by the oracle"""
+    return cpu_solve(q)
+
+
+def cpu_batch_sample(parts, budget_s=CPU_SAMPLE_S):
+    """the batch workload on one host thread: its problems solved whole, one
+    after another, until about budget_s seconds have passed"""
+    cells = secs = 0.0
+    its = []
+    k = 0
+    for p in parts:
+        r = cpu_solve(p)
+        if r["status"] != 0:
+            raise SystemExit("CPU reference solve of %s did not converge" % p.name)
+        cells += p.leaf_cells
+        secs += r["seconds"]
+        its.append(r["iterations"])
+        k += 1
+        if secs >= budget_s:
+            break
+    return dict(value=cells / secs, problems=k, cells=int(cells), seconds=secs, iterations=its)
+
+
 def run_reference(args):
     """--impl reference: the reference solver (the C oracle port: the
     reference library itself does not travel to the GPU host) on every host
@@ -256,6 +303,9 @@ def run_reference(args):
     prob = workloads.CONFIGS[args.config]()
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
+    if getattr(prob, "parts", None):
+        run_reference_batch(args, prob, cores, ctx)
+        return
     t_all = time.perf_counter()
     with ctx.Pool(cores) as pool:
         big = prob.leaf_cells > CPU_FULL_CELLS
@@ -297,6 +347,104 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_reference_batch(args, prob, cores, ctx):
+    """--impl reference on the batch workload: every step solves `cores`
+    whole problems of the batch (consecutive ones, wrapping around) on all
+    host cores at once, one problem per core, each to 1e-8 by the oracle;
+    value = their leaf cells / the step's wall time"""
+    parts = [cpu_payload(p) for p in prob.parts]
+    t_all = time.perf_counter()
+    vals, its = [], []
+    k0 = 0
+    with ctx.Pool(cores) as pool:
+        for s in range(args.warmup + args.steps):
+            chunk = [parts[(k0 + i) % len(parts)] for i in range(cores)]
+            k0 += cores
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_part_worker, chunk)
+            dt = time.perf_counter() - t0
+            if any(r["status"] != 0 for r in res):
+                print(json.dumps({"impl": "reference", "unavailable": "CPU reference solve did not converge"}))
+                return
+            if s >= args.warmup:
+                vals.append(sum(q.leaf_cells for q in chunk) / dt)
+                its.extend(r["iterations"] for r in res)
+    wall = time.perf_counter() - t_all
+    v = statistics.mean(vals)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": prob.leaf_cells / v * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.config, **prob.describe(), "tol_rel": TOL},
+        "cpu_baseline": {"value": v, "unit": "cells/s", "cores": cores, "kind": "port",
+                         "sample": ("C oracle (bit-exact restatement of the reference solver, bottom BiCGSTAB to "
+                                    "1e-10); each step solves %d whole problems of the batch to 1e-8, one per "
+                                    "core (%d problem solves timed, %.1f outer iterations on average); "
+                                    "ms_per_step = the whole batch's leaf cells at that rate"
+                                    % (cores, len(its), statistics.mean(its)))},
+        "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(out))
+
+
+def fluid_leaf_rel_error(p, vf, sol, ref):
+    nc = p.ncell
+    m = vf.reshape(-1, nc)[p.leaf].reshape(-1) > 0
+    a = sol.reshape(-1, nc)[p.leaf].reshape(-1)[m]
+    b = ref.reshape(-1, nc)[p.leaf].reshape(-1)[m]
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+ORACLE_PROBLEMS = 4  # batch workload: problems compared with the oracle
+
+
+def oracle_check(S, prob, timed_sol):
+    """the device solution against the oracle's converged FP64 solve (tol
+    1e-11, bottom 1e-10): at the timed tolerance (1e-8, the solution of the
+    last timed solve) and after a solve to 1e-11; the batch workload on its
+    first ORACLE_PROBLEMS problems.  Also the final true residual of the timed
+    solution under the reference-arithmetic operator, max over fluid leaf
+    cells relative to the right-hand side's."""
+    from oracle import pyoracle
+    parts = getattr(prob, "parts", None)
+    checks = [(p, prob.block_offsets[k]) for k, p in enumerate(parts[:ORACLE_PROBLEMS])] if parts else [(prob, 0)]
+    # true residual of the timed solution (reference-arithmetic kernel)
+    finest = int(prob.tables["level"].max())
+    r = S.residual(finest, timed_sol, prob.rhs)
+    vf_all = S.get_coef(2)
+    leafm = np.zeros(prob.num_blocks, dtype=bool)
+    leafm[prob.leaf] = True
+    fl = (vf_all.reshape(-1, prob.ncell) > 0) & leafm[:, None]
+    true_res = float(np.abs(r.reshape(-1, prob.ncell)[fl]).max() / np.abs(prob.rhs.reshape(-1, prob.ncell)[fl]).max())
+    S.set_params(tol_rel=1e-11)
+    S.prepare()
+    S.set_zero_sol()
+    info = S.cg_solve()
+    tight = S.get_sol_compact()
+    S.set_params(tol_rel=TOL)
+    S.prepare()
+    e8, e11 = [], []
+    t0 = time.perf_counter()
+    for p, b0 in checks:
+        vf, af, bc = pyoracle.setup_coefficients(p.tables, p.bc, p.vol, p.area, p.bface)
+        O = pyoracle.Oracle(p.tables, p.bc, vf, af, bc)
+        ref, oinfo = O.cg_solve(p.rhs, pyoracle.params(tol_rel=1e-11, tol_abs=0.0, bot_tol_rel=1e-10,
+                                                       bot_tol_abs=0.0))
+        if oinfo["status"] != 0:
+            raise SystemExit("oracle solve of %s did not converge" % p.name)
+        sl = slice(b0 * p.ncell, (b0 + p.num_blocks) * p.ncell)
+        e8.append(fluid_leaf_rel_error(p, vf, timed_sol[sl], ref))
+        e11.append(fluid_leaf_rel_error(p, vf, tight[sl], ref))
+    return {"at_1e-8": max(e8), "at_1e-11": max(e11),
+            "true_residual_rel_inf": true_res,
+            "device_rnorm_rel_at_1e-11": info["rnorm"] / info["rnorm0"] if info["rnorm0"] else 0.0,
+            "sample": ("%s; relative L2 over fluid leaf cells against the C oracle's FP64 solve to 1e-11 "
+                       "(bottom BiCGSTAB to 1e-10), max over the problems; oracle time %.1f s"
+                       % ("the batch's first %d problems" % len(checks) if parts else "the whole workload",
+                          time.perf_counter() - t0))}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -321,7 +469,8 @@ def main():
                  vcycle_kernel=args.vcycle_kernel,
                  cluster_cells=args.cluster_cells, smooth_variant=args.smooth_variant,
                  pdl=args.pdl, sublevel_order=args.sublevel_order, bottom_level=args.bottom_level,
-                 bottom_half=args.bottom_half)
+                 bottom_half=args.bottom_half, smoother=max(args.smoother, 0),
+                 inner_sweeps=args.inner_sweeps if args.inner_sweeps > 0 else 2)
     S.prepare()
     ext = torch.cuda.ExternalStream(S.stream())
     if args.kernel >= 0:
@@ -348,38 +497,53 @@ def main():
                 raise SystemExit("warm-up solve failed: %s" % info)
 
     tuning = None
-    if args.precision < 0 or args.n_post < 0:
+    if args.precision < 0 or args.n_post < 0 or args.smoother < 0:
         # the faster solver setting on this workload, from timed warm-up
-        # solves: V-cycle precision (FP32 / FP64) and post-smoothing sweeps
-        tuning = {}
+        # solves: V-cycle precision (FP32 / FP64), smoother (red-black sweeps
+        # or block-hybrid passes of inner_sweeps sweeps) and post-smoothing
+        # sweeps / passes per tower
+        tuning = []
         precs = (1, 0) if args.precision < 0 else (args.precision,)
-        # more sweeps trade V-cycle cost for iterations: 2D latency-bound
-        # solves prefer 2, 3D ones 3-4; the search over a precision stops
-        # after two settings slower than its best
-        posts = (1, 2, 3, 4, 6, 8) if args.n_post < 0 else (args.n_post,)
+        smoothers = (0, 1) if args.smoother < 0 else (args.smoother,)
+        families = []
         for prec in precs:
-            best_prec, worse = None, 0
+            for sm in smoothers:
+                if sm == 0:
+                    families.append((prec, 0, 2, (1, 2, 3, 4, 6, 8)))
+                else:
+                    for inner in ((2, 3) if args.inner_sweeps < 0 else (args.inner_sweeps,)):
+                        families.append((prec, 1, inner, (1, 2, 3, 4)))
+        for prec, sm, inner, posts in families:
+            # more sweeps trade V-cycle cost for iterations: 2D latency-bound
+            # solves prefer 2, 3D ones 3-4; the search over a family stops
+            # after two settings slower than its best
+            if args.n_post >= 0:
+                posts = (args.n_post,)
+            best_f, worse = None, 0
             for npost in posts:
-                S.set_params(precision=prec, n_post_smooth=npost)
+                S.set_params(precision=prec, n_post_smooth=npost, smoother=sm, inner_sweeps=inner)
                 S.prepare()
                 warm()
                 ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
-                for e in ev:
-                    one(e)
+                infos = [one(e) for e in ev]
                 torch.cuda.synchronize()
                 t = statistics.mean(a.elapsed_time(b) for a, b in ev)
-                tuning["precision %d, n_post %d" % (prec, npost)] = (t, prec, npost)
-                if best_prec is None or t < best_prec:
-                    best_prec, worse = t, 0
+                tuning.append(dict(precision=prec, smoother=sm, inner_sweeps=inner, n_post_smooth=npost, ms=t,
+                                   iterations=statistics.mean(i["iterations"] for i in infos)))
+                if best_f is None or t < best_f:
+                    best_f, worse = t, 0
                 else:
                     worse += 1
                     if worse >= 2:
                         break
-        best = min(tuning.values())
-        args.precision, args.n_post = best[1], best[2]
-        tuning = {k: v[0] for k, v in tuning.items()}
-        S.set_params(precision=args.precision, n_post_smooth=args.n_post)
+        best = min(tuning, key=lambda r: r["ms"])
+        args.precision, args.n_post = best["precision"], best["n_post_smooth"]
+        args.smoother, args.inner_sweeps = best["smoother"], best["inner_sweeps"]
+        S.set_params(precision=args.precision, n_post_smooth=args.n_post, smoother=args.smoother,
+                     inner_sweeps=args.inner_sweeps)
         S.prepare()
+    if args.inner_sweeps < 0:
+        args.inner_sweeps = 2
     warm()
     if args.profile:
         torch.cuda.synchronize()
@@ -436,6 +600,15 @@ def main():
     h2d = prob.num_blocks * prob.ncell * 8
     d2h = prob.num_blocks * prob.ncell * 8
 
+    # ---- the metric's comparison: plain FP64 MG vs the FP32 V-cycle vs the
+    # learned correction with the FP32 V-cycle, same workload, same timing ----
+    timed_sol = S.get_sol_compact() if not args.no_compare else None
+    solvers = None if args.no_compare else compare_solvers(S, prob, one, warm, torch, args, tuning)
+    oracle = None if args.no_compare else oracle_check(S, prob, timed_sol)
+    S.set_params(precision=args.precision, n_post_smooth=args.n_post, smoother=args.smoother,
+                 inner_sweeps=args.inner_sweeps, learned=0, tol_rel=TOL)
+    S.prepare()
+
     # ---- roofline of the dominant kernel, timed live on the solver stream ----
     roof = roofline(S, prob, ext, torch, finest, args.precision)
 
@@ -452,6 +625,8 @@ def main():
                    "l2": "flushed (256 MiB write) before every timed solve", "precision": args.precision,
                    "setting_tuning_ms": tuning,
                    "iterations_per_solve": statistics.mean(iters), "n_post_smooth": args.n_post,
+                   "smoother": ("red-black sweeps", "block-hybrid passes (Gauss-Seidel inside a block, Jacobi "
+                                "between blocks), %d sweeps per pass" % args.inner_sweeps)[args.smoother],
                    "vcycle_kernel": ("per-phase launches", "cooperative", "cluster")[args.vcycle_kernel],
                    "cluster_cells": args.cluster_cells if args.vcycle_kernel == 2 else None,
                    "pdl": bool(args.pdl),
@@ -465,8 +640,18 @@ def main():
         "gpu_launches": launches,
         "roofline": roof,
         "clocks": clk.summary(),
+        "solvers": solvers,
+        "error_vs_oracle": oracle,
     }
-    if rank == 0 and not args.no_cpu:
+    parts = getattr(prob, "parts", None)
+    if rank == 0 and not args.no_cpu and parts:
+        cs = cpu_batch_sample([cpu_payload(p) for p in parts])
+        out["cpu_baseline"] = {"value": cs["value"], "unit": "cells/s", "cores": 1, "kind": "port",
+                               "sample": ("the batch's first %d problems (%d leaf cells) each solved whole to 1e-8 "
+                                          "by the C oracle (bit-exact restatement of the reference solver, bottom "
+                                          "BiCGSTAB to 1e-10) on one host thread: %.1f s, %s outer iterations"
+                                          % (cs["problems"], cs["cells"], cs["seconds"], cs["iterations"]))}
+    elif rank == 0 and not args.no_cpu:
         big = prob.leaf_cells > CPU_FULL_CELLS
         cs = cpu_solve(prob, budget_s=CPU_SAMPLE_S if big else None,
                        n_iters=int(math.ceil(statistics.mean(iters))))
@@ -485,6 +670,51 @@ def main():
         print(json.dumps(out))
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def compare_solvers(S, prob, one, warm, torch, args, tuning):
+    """time to 1e-8 (ms, CUDA events, L2 flushed) and iterations of: plain
+    FP64 MG-BiCGSTAB (FP64 V-cycle, the reference's 2 post-smoothing sweeps),
+    the FP32 V-cycle with the tuned sweeps, and the learned block correction
+    with the FP32 V-cycle (trained on this workload's own solver iterates
+    first, 2D only)"""
+    fp32 = dict(precision=1, n_post_smooth=args.n_post, smoother=args.smoother, inner_sweeps=args.inner_sweeps)
+    if tuning:
+        t32 = [r for r in tuning if r["precision"] == 1]
+        if t32:
+            b = min(t32, key=lambda r: r["ms"])
+            fp32 = dict(precision=1, n_post_smooth=b["n_post_smooth"], smoother=b["smoother"],
+                        inner_sweeps=b["inner_sweeps"])
+    # the reference's method on the device: FP64 V-cycle, red-black
+    # Gauss-Seidel with its default 2 post-smoothing sweeps
+    settings = [("plain_fp64_mg", dict(precision=0, n_post_smooth=2, smoother=0, inner_sweeps=2, learned=0)),
+                ("fp32_vcycle", dict(fp32, learned=0))]
+    out = {}
+    learned_note = None
+    if prob.ndim == 2 and prob.nb in (8, 16):
+        S.set_params(**dict(fp32, learned=0))
+        t0 = time.perf_counter()
+        info = S.learned_train_on_workload()
+        learned_note = dict(train_seconds=time.perf_counter() - t0, **info)
+        settings.append(("learned_fp32_vcycle", dict(fp32, learned=1)))
+    for label, prm in settings:
+        S.set_params(**prm)
+        S.prepare()
+        warm()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+        infos = [one(e) for e in ev]
+        torch.cuda.synchronize()
+        if any(i["status"] not in (0, 3) for i in infos):
+            out[label] = {"failed": infos[0]}
+            continue
+        out[label] = {"ms": statistics.mean(a.elapsed_time(b) for a, b in ev),
+                      "iterations": statistics.mean(i["iterations"] for i in infos),
+                      "setting": {k: v for k, v in prm.items() if k != "learned"},
+                      "stall_fallback": any(i["status"] == 3 for i in infos)}
+    if learned_note:
+        out["learned_training"] = learned_note
+    S.set_params(learned=0)
+    return out
 
 
 def kernel_only(S, prob, ext, torch, args):

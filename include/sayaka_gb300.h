@@ -128,6 +128,12 @@ typedef struct sayaka_params {
   int32_t sublevel_order; /* device V-cycle smoothing over a tower's sublevels: 0 = finest to coarsest,
                              red then black per sublevel (the reference's order, mg_smooth_level);
                              1 = one launch per colour and level parity (default) */
+  int32_t smoother;       /* device V-cycle smoother (per-phase V-cycle): 0 = red-black sweeps, one launch per
+                             colour (default); 1 = block-hybrid passes: n_post_smooth passes per tower, each
+                             one launch of inner_sweeps red-black sweeps of every block from shared memory with
+                             the values outside the block frozen (Gauss-Seidel inside a block, Jacobi between
+                             blocks; a fixed linear map, another preconditioner with the same solution) */
+  int32_t inner_sweeps;   /* smoother 1: red-black sweeps per block and pass (default 2) */
 } sayaka_params;
 
 typedef struct sayaka_solve_info {
@@ -236,6 +242,9 @@ int32_t sayaka_mac_learned_nparam(void);
  * (zero initial guess, tolerance 1e-12, at most max_iter iterations): one
  * pair per iterate and finest-tower block; the solution is reset to zero */
 int sayaka_mac_learned_collect(sayaka_mac *h, int32_t max_iter, int32_t *iterates);
+/* the same with at most max_samples pairs (every k-th block of each iterate,
+ * the offset moving between iterates; 0 = no limit), for large forests */
+int sayaka_mac_learned_collect_sampled(sayaka_mac *h, int32_t max_iter, int32_t max_samples, int32_t *iterates);
 /* Adam on the collected pairs, FP32 forward/backward kernels on the GPU;
  * loss = mean over blocks of the weighted squared error (last epoch) */
 int sayaka_mac_learned_train(sayaka_mac *h, int32_t epochs, float lr, int32_t batch, uint32_t seed, float *loss);
@@ -312,7 +321,10 @@ int sayaka_mac_residual_norm_noalloc(sayaka_mac *h, int32_t L, const double *x, 
  * arithmetic above: which 0 = out = A in on the finest tower with the fast
  * operator (per-cell factors, FMA; mg_apply_level, src/SayakaMacOperator.cpp:84-137);
  * which 1 = one smoothing pass of tower L in mg_smooth_level's order with the
- * fast sweep (launch variant 0..9, -1 the tuned one; in = phi, in2 = rhs) */
+ * fast sweep (launch variant 0..9, -1 the tuned one; in = phi, in2 = rhs);
+ * which 2 = one block-hybrid pass (params.smoother 1) over tower L with
+ * `variant` (1..1024) red-black sweeps per block (in = phi, frozen outside
+ * each block; in2 = rhs) */
 int sayaka_mac_device_kernel_compact(sayaka_mac *h, int32_t which, int32_t L, int32_t variant, const double *in,
                                      const double *in2, double *out);
 /* one mg_smooth_level(L) (src/SayakaMacOperator.cpp:140-159, 1028-1112) */

@@ -40,7 +40,8 @@ class Params(C.Structure):
                 ("bottom", C.c_int32), ("verbose", C.c_int32), ("graph", C.c_int32),
                 ("vcycle_kernel", C.c_int32), ("pdl", C.c_int32),
                 ("cluster_cells", C.c_int32), ("smooth_variant", C.c_int32), ("learned", C.c_int32),
-                ("bottom_level", C.c_int32), ("bottom_half", C.c_int32), ("sublevel_order", C.c_int32)]
+                ("bottom_level", C.c_int32), ("bottom_half", C.c_int32), ("sublevel_order", C.c_int32),
+                ("smoother", C.c_int32), ("inner_sweeps", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -108,6 +109,7 @@ SIGNATURES = {
     "sayaka_fp_selftest": (C.c_int, [_f64p, _f32p, C.c_int, _f32p, _f32p, _f64p, _f64p, _f64p, _f64p]),
     "sayaka_mac_learned_nparam": (C.c_int32, []),
     "sayaka_mac_learned_collect": (C.c_int, [_V, C.c_int32, _i32p]),
+    "sayaka_mac_learned_collect_sampled": (C.c_int, [_V, C.c_int32, C.c_int32, _i32p]),
     "sayaka_mac_learned_train": (C.c_int, [_V, C.c_int32, C.c_float, C.c_int32, C.c_uint32, _f32p]),
     "sayaka_mac_learned_get_weights": (C.c_int, [_V, _f32p, C.c_int32]),
     "sayaka_mac_learned_set_weights": (C.c_int, [_V, _f32p, C.c_int32]),
@@ -415,10 +417,21 @@ class MacSolver:
         return a.value, b.value, c.value
 
     # --- learned block correction ---
-    def learned_collect(self, max_iter=200):
+    def learned_collect(self, max_iter=200, max_samples=0):
         n = C.c_int32()
-        _check(self.lib.sayaka_mac_learned_collect(self.h, int(max_iter), C.byref(n)), "learned_collect", self.h)
+        _check(self.lib.sayaka_mac_learned_collect_sampled(self.h, int(max_iter), int(max_samples), C.byref(n)),
+               "learned_collect", self.h)
         return n.value
+
+    def learned_train_on_workload(self, max_samples=40000, epochs=10, lr=1e-3, batch=256, seed=1):
+        """training pairs from this solver's own plain solve of its current
+        right-hand side (at most max_samples blocks), then Adam on the GPU;
+        the right-hand side and a zero solution are left in place"""
+        its = self.learned_collect(200, max_samples)
+        first = self.learned_train(epochs=1, lr=lr, batch=batch, seed=seed)
+        last = self.learned_train(epochs=max(0, epochs - 1), lr=lr, batch=batch, seed=seed + 1)
+        return dict(iterates=its, loss_first_epoch=first, loss_last_epoch=last, epochs=epochs,
+                    max_samples=max_samples)
 
     def learned_train(self, epochs=20, lr=1e-3, batch=256, seed=1):
         loss = C.c_float()
@@ -534,6 +547,16 @@ class MacSolver:
         b, pb = _f64(rhs)
         _check(self.lib.sayaka_mac_device_kernel_compact(self.h, 1, int(L), int(variant), pa, pb,
                                                          out.ctypes.data_as(_f64p)), "device_smooth", self.h)
+        return out
+
+    def device_hybrid_pass(self, L, phi, rhs, sweeps):
+        """one block-hybrid smoothing pass of tower L (FP64), `sweeps`
+        red-black sweeps per block, values outside each block frozen"""
+        out = self._cells()
+        a, pa = _f64(phi)
+        b, pb = _f64(rhs)
+        _check(self.lib.sayaka_mac_device_kernel_compact(self.h, 2, int(L), int(sweeps), pa, pb,
+                                                         out.ctypes.data_as(_f64p)), "device_hybrid_pass", self.h)
         return out
 
     def restrict_sweep(self, x):

@@ -411,6 +411,8 @@ void sayaka_params_default(sayaka_params *p) {
   p->bottom_level = d.bottom_level;
   p->bottom_half = d.bottom_half;
   p->sublevel_order = d.sublevel_order;
+  p->smoother = d.smoother;
+  p->inner_sweeps = d.inner_sweeps;
 }
 
 int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
@@ -637,6 +639,10 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.bottom_level = p->bottom_level;
     s.bottom_half = p->bottom_half;
     s.sublevel_order = p->sublevel_order;
+    if (p->smoother < 0 || p->smoother > 1 || p->inner_sweeps < 1 || p->inner_sweeps > 64)
+      return (int)SAYAKA_BAD_INPUT;
+    s.smoother = p->smoother;
+    s.inner_sweeps = p->inner_sweeps;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
   });
@@ -723,12 +729,16 @@ int sayaka_mac_flux(sayaka_mac *h, int32_t dir, const double *phi, int32_t pn, i
 // ---- learned block correction ----
 int32_t sayaka_mac_learned_nparam(void) { return learned::kNParam; }
 int sayaka_mac_learned_collect(sayaka_mac *h, int32_t max_iter, int32_t *iterates) {
+  return sayaka_mac_learned_collect_sampled(h, max_iter, 0, iterates);
+}
+int sayaka_mac_learned_collect_sampled(sayaka_mac *h, int32_t max_iter, int32_t max_samples, int32_t *iterates) {
   return guarded(h, [&] {
     if (!h->gpu->learned_supported()) {
       h->err = "learned correction: 2D trees with 8x8 or 16x16 blocks only";
       return (int)SAYAKA_BAD_INPUT;
     }
-    const int n = h->gpu->learned_collect(max_iter > 0 ? max_iter : 200);
+    if (max_samples < 0) return (int)SAYAKA_BAD_INPUT;
+    const int n = h->gpu->learned_collect(max_iter > 0 ? max_iter : 200, max_samples);
     if (iterates) *iterates = n < 0 ? 0 : n;
     return n < 0 ? (int)SAYAKA_CUDA_ERROR : (int)SAYAKA_OK;
   });
@@ -890,7 +900,8 @@ int sayaka_mac_device_kernel_compact(sayaka_mac *h, int32_t which, int32_t L, in
   return guarded(h, [&] {
     const int r = h->gpu->device_kernel_compact(which, L, variant, in, in2, out);
     if (r == 1) {
-      h->err = "device_kernel_compact: which must be 0 or 1, L a tower of the tree, variant < 10, pointers non-null";
+      h->err = "device_kernel_compact: which must be 0, 1 or 2, L a tower of the tree, variant < 10 (which 1) or "
+               "1..1024 (which 2), pointers non-null";
       return (int)SAYAKA_BAD_INPUT;
     }
     return (int)SAYAKA_OK;  // CUDA errors are reported by status_of

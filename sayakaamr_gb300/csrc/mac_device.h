@@ -164,6 +164,16 @@ void launch_prolong_red(const Topo &t, const Coef<T> &c, const BlockList &L, T *
                         const int *guard, cudaStream_t s, bool pdl = false,
                         const BlockList &X = BlockList{nullptr, nullptr, 0});
 
+// block-hybrid Gauss-Seidel pass (Gauss-Seidel inside a block, Jacobi
+// between blocks): nsweep red-black sweeps of every block of L from src's
+// values into dst (src unchanged); L may hold several sublevels
+template <typename T>
+void launch_bhgs(const Topo &t, const Coef<T> &c, const BlockList &L, int nsweep, const T *src, T *dst,
+                 const T *rhs, const int *guard, cudaStream_t s, bool pdl = false);
+template <typename T>
+void launch_copy_blocks(const BlockList &L, int ncell, const T *src, T *dst, const int *guard, cudaStream_t s,
+                        bool pdl = false);
+
 void launch_flux(const Topo &t, const Coef<double> &c, const BlockList &L, int dir,
                  const double *phi, double *flux, cudaStream_t s);
 

@@ -690,6 +690,9 @@ void MacGpu::ensure_fast_buffers() {
   d_geom32_ = fa((size_t)nbk * 8);
   d_resid32_ = fa(nc);
   d_corr32_ = fa(nc);
+  d_corr32b_ = fa(nc);
+  if (cudaMalloc(&d_corr64b_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (correction)");
+  else cudaMemset(d_corr64b_, 0, nc * sizeof(double));
   if (cudaMalloc(&d_opP_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
   if (cudaMalloc(&d_opS_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
   if (cudaMalloc(&d_st_, sizeof(FState)) != cudaSuccess) fail("alloc state");
@@ -1187,6 +1190,19 @@ void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *o
   bottom_launch<T>(resid, corr);
   for (int l = LB + 1; l <= L; l++) {
     if (levels_[l].n == 0) continue;
+    if (prm_.smoother == 1) {
+      // block-hybrid passes over every sublevel of tower l at once, reading
+      // one correction vector and writing the other
+      launch_prolong<T>(topo_, c, level_list(l), corr, guard, stream_, prm_.pdl != 0);
+      const BlockList TL = smooth_list(l);
+      T *a = corr, *b = corr_alt<T>();
+      for (int s = 0; s < prm_.n_post; s++) {
+        launch_bhgs<T>(topo_, c, TL, prm_.inner_sweeps, a, b, resid, guard, stream_, prm_.pdl != 0);
+        std::swap(a, b);
+      }
+      if (a != corr) launch_copy_blocks<T>(TL, ncell_, a, corr, guard, stream_, prm_.pdl != 0);
+      continue;
+    }
     // the level's own sublevel of tower l holds every block of the level, so
     // the prolongation and the red sweep that follows it can be one launch
     const BlockList top = sublevel_list(l, l);
@@ -1252,9 +1268,9 @@ template <typename T>
 void MacGpu::precondition(int L, T *resid, T *corr, const Coef<T> &c, double *out) {
   const bool nn = sizeof(T) == 4 && learned_active();
   double *o = nn ? nullptr : out;
-  if (prm_.vcycle_kernel == 2)
+  if (prm_.vcycle_kernel == 2 && prm_.smoother == 0)
     vcycle_cluster<T>(resid, corr, c, o);
-  else if (prm_.vcycle_kernel == 1)
+  else if (prm_.vcycle_kernel == 1 && prm_.smoother == 0)
     vcycle_coop<T>(resid, corr, c, o);
   else
     vcycle_device<T>(L, resid, corr, c, o);
@@ -1381,6 +1397,8 @@ void MacGpu::capture_loop(int precision) {
   graph_var_ = rbgs_variant_[precision == 1];
   graph_nn_ = (int)learned_active();
   graph_order_ = prm_.sublevel_order;
+  graph_smoother_ = prm_.smoother;
+  graph_inner_ = prm_.inner_sweeps;
 }
 
 // the captured graph was recorded with other parameters than the current ones
@@ -1388,7 +1406,8 @@ bool MacGpu::graph_stale() const {
   return !graph_exec_ || graph_prec_ != prm_.precision || graph_npost_ != prm_.n_post ||
          graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl || graph_cc_ != prm_.cluster_cells ||
          graph_var_ != rbgs_variant_[prm_.precision == 1] || graph_nn_ != (int)learned_active() ||
-         graph_order_ != prm_.sublevel_order;
+         graph_order_ != prm_.sublevel_order || graph_smoother_ != prm_.smoother ||
+         graph_inner_ != prm_.inner_sweeps;
 }
 
 int MacGpu::cg_solve_device(SolveInfo *info) {
@@ -1580,9 +1599,10 @@ int MacGpu::enqueue_kernel(int which, int L) {
 // solve's FP64 sweep, launch variant `variant` (-1: the tuned one); in = phi,
 // in2 = rhs.  Uses (and clobbers) the handle's work vectors.
 int MacGpu::device_kernel_compact(int which, int L, int variant, const double *in, const double *in2, double *out) {
-  if (which < 0 || which > 1 || !in || !out || (which == 1 && !in2)) return 1;
-  if (which == 1 && (L < 1 || L > finest_ || towers_[L].all.n == 0)) return 1;
-  if (variant >= kRbgsVariants) return 1;
+  if (which < 0 || which > 2 || !in || !out || (which >= 1 && !in2)) return 1;
+  if (which >= 1 && (L < 1 || L > finest_ || towers_[L].all.n == 0)) return 1;
+  if (which == 1 && variant >= kRbgsVariants) return 1;
+  if (which == 2 && (variant < 1 || variant > 1024)) return 1;
   if (prepare_device() != 0) return 2;
   const size_t n = (size_t)tt_.num_blocks * ncell_;
   if (which == 0) {
@@ -1600,6 +1620,16 @@ int MacGpu::device_kernel_compact(int which, int L, int variant, const double *i
                                                                 d_opP_, d_opS_, d_st_, d_part_, d_cnt_);
     CKR_(cudaGetLastError(), 2);
     CKR_(cudaMemcpyAsync(out, vec_[kV], n * sizeof(double), cudaMemcpyDeviceToHost, stream_), 2);
+  } else if (which == 2) {
+    // one block-hybrid pass over every sublevel of tower L, `variant`
+    // red-black sweeps per block: in (frozen) -> out
+    CKR_(cudaMemcpyAsync(vec_[kTMP], in, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);
+    CKR_(cudaMemcpyAsync(vec_[kRESID], in2, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);
+    CKR_(cudaMemcpyAsync(vec_[kCORR], in, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);
+    launch_bhgs<double>(topo_, c64_, smooth_list(L), variant, vec_[kTMP], vec_[kCORR], vec_[kRESID], nullptr,
+                        stream_, false);
+    CKR_(cudaGetLastError(), 2);
+    CKR_(cudaMemcpyAsync(out, vec_[kCORR], n * sizeof(double), cudaMemcpyDeviceToHost, stream_), 2);
   } else {
     const int v = variant >= 0 ? variant : rbgs_var<double>();
     CKR_(cudaMemcpyAsync(vec_[kCORR], in, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);

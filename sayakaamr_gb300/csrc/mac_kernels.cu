@@ -467,6 +467,144 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
   }
 }
 
+// ---- Block-hybrid Gauss-Seidel: one pass over every block of a list (all
+// sublevels of a tower at once).  Each CTA loads its block's tile from src,
+// takes every value outside the block from src too (frozen for the pass:
+// Jacobi between blocks), runs nsweep red-black sweeps on the tile in shared
+// memory and writes the tile to dst.  src is not written during the pass, so
+// the result does not depend on the order in which CTAs run: the pass is one
+// fixed linear map, like the sweeps it replaces, but it moves a block's data
+// once for nsweep sweeps and needs one launch per pass instead of one per
+// colour, level parity and sweep.  The boundary faces are evaluated as in
+// smooth_cell_fast (same-level, coarse/fine and physical faces).
+template <typename T, int ND, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_bhgs(Topo t, Coef<T> c, BlockList L, int nsweep,
+                                                         const T *__restrict__ src, T *__restrict__ dst,
+                                                         const T *__restrict__ rhs, const int *guard) {
+  extern __shared__ __align__(16) unsigned char bhgs_smem[];
+  pdl_enter();
+  if (guard && *guard) return;
+  const int nb = t.nb, ncell = t.ncell, nhalf = ncell >> 1;
+  const int nface = ND == 3 ? nb * nb : nb;  // cells on one block face
+  T *tile = reinterpret_cast<T *>(bhgs_smem);
+  T *hc = tile + ncell;            // diagonal part of every boundary face of the block
+  T *ho = hc + 2 * ND * nface;     // its off-diagonal part (frozen neighbour values)
+  for (int p = blockIdx.x; p < L.n; p += gridDim.x) {
+    const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
+    const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
+    const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
+    const long cb = (long)b * ncell;
+    const long fb = (long)b * t.nfb;
+    if ((ncell & 3) == 0 && sizeof(T) == 4) {
+      const float4 *s4 = reinterpret_cast<const float4 *>(src + cb);
+      float4 *d4 = reinterpret_cast<float4 *>(tile);
+      for (int i = threadIdx.x; i < (ncell >> 2); i += blockDim.x) d4[i] = s4[i];
+    } else {
+      for (int i = threadIdx.x; i < ncell; i += blockDim.x) tile[i] = src[cb + i];
+    }
+    for (int e = threadIdx.x; e < 2 * ND * nface; e += blockDim.x) {
+      const int f = e / nface, m = e - f * nface;
+      const int d = f >> 1, s = f & 1;
+      int ijk[3] = {0, 0, 0};
+      ijk[d] = s ? nb - 1 : 0;
+      const int q0 = d == 0 ? 1 : 0, q1 = d == 2 ? 1 : 2;
+      ijk[q0] = m % nb;
+      if (ND == 3) ijk[q1] = m / nb;
+      int fx;
+      if (d == 0)
+        fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+      else if (d == 1)
+        fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+      else
+        fx = encode(ijk, nb) + s * nb * nb;
+      const int ty = face_type_of(ft, f);
+      T vc = 0, vo = 0;
+      if (ty == 0) {
+        vc = c.tff[d][fb + fx];
+        vo = vc * same_level_ghost<T, false>(t, b, f, ijk, src, hxe);
+      } else if (ty == 1) {
+        if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
+      } else if (ty == 2) {
+        vc = cf_coef(c, t, b, d, fx, (T)1.5);
+        vo = vc * fine_crse_ghost<T, ND, false>(t, b, f, ijk, src, hxe);
+      } else {
+        vc = cf_coef(c, t, b, d, fx, (T)0.75);
+        vo = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, src, hxe);
+      }
+      hc[e] = vc;
+      ho[e] = vo;
+    }
+    __syncthreads();
+    const T dv = geom(c, b, 6);
+    for (int sw = 0; sw < nsweep; sw++) {
+      for (int color = 0; color < 2; color++) {
+        for (int h = threadIdx.x; h < nhalf; h += blockDim.x) {
+          int ijk[3];
+          color_cell_fast<ND>(h, t, color, ijk);
+          const int ci = t.lnb >= 0 ? ijk[0] + ((ijk[1] + (ijk[2] << t.lnb)) << t.lnb) : encode(ijk, nb);
+          T diag = c.alpha * dv;
+          T off = 0;
+#pragma unroll
+          for (int f = 0; f < 2 * ND; f++) {
+            const int d = f >> 1, s = f & 1;
+            const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+            if (!bnd) {
+              int fx;
+              if (d == 0)
+                fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+              else if (d == 1)
+                fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+              else
+                fx = ci + s * nb * nb;
+              const T coef = c.tff[d][fb + fx];
+              const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+              diag += coef;
+              off = fma_t(coef, tile[ci + (s ? stride : -stride)], off);
+            } else {
+              const int qa = d == 0 ? 1 : 0, qb = d == 2 ? 1 : 2;
+              const int e = f * nface + ijk[qa] + (ND == 3 ? nb * ijk[qb] : 0);
+              diag += hc[e];
+              off += ho[e];
+            }
+          }
+          T unew = 0;
+          if (sizeof(T) == 8 && L.sa) {
+            const long fo = (long)p * ncell + ci;
+            unew = fma_t(rhs[cb + ci], (T)L.sa[fo], off * (T)L.ia[fo]);
+          } else {
+            const T vfv = c.vf[cb + ci];
+            if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+          }
+          tile[ci] = unew;
+        }
+        __syncthreads();
+      }
+    }
+    if ((ncell & 3) == 0 && sizeof(T) == 4) {
+      const float4 *s4 = reinterpret_cast<const float4 *>(tile);
+      float4 *d4 = reinterpret_cast<float4 *>(dst + cb);
+      for (int i = threadIdx.x; i < (ncell >> 2); i += blockDim.x) d4[i] = s4[i];
+    } else {
+      for (int i = threadIdx.x; i < ncell; i += blockDim.x) dst[cb + i] = tile[i];
+    }
+    __syncthreads();
+  }
+}
+
+// dst = src over the blocks of a list
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_copy_blocks(BlockList L, int ncell, const T *__restrict__ src,
+                                                          T *__restrict__ dst, const int *guard) {
+  pdl_enter();
+  if (guard && *guard) return;
+  const long total = (long)L.n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell);
+    const long q = (long)L.blocks[p] * ncell + (it - (long)p * ncell);
+    dst[q] = src[q];
+  }
+}
+
 // ---- the same sweep with the block's phi tile and face coefficients staged
 // by TMA bulk copies (cp.async.bulk, completion on an mbarrier): in the
 // compact layout both are contiguous per block.  The boundary contributions
@@ -1064,6 +1202,32 @@ void launch_rbgs(const Topo &t, const Coef<T> &c, const BlockList &L, int color,
 }
 
 template <typename T>
+void launch_bhgs(const Topo &t, const Coef<T> &c, const BlockList &L, int nsweep, const T *src, T *dst,
+                 const T *rhs, const int *guard, cudaStream_t s, bool pdl) {
+  const int nhalf = t.ncell / 2;
+  if (L.n == 0 || nhalf == 0) return;
+  const int nface = t.ndim == 3 ? t.nb * t.nb : t.nb;
+  const size_t smem = sizeof(T) * ((size_t)t.ncell + 2 * 2 * t.ndim * (size_t)nface);
+  const int threads = std::min(kThreads, (nhalf + 31) / 32 * 32);
+  const int grid = std::min(L.n, 152 * 64);
+  if (t.ndim == 2) {
+    ensure_max_smem((const void *)k_bhgs<T, 2, 2>, 200 * 1024);
+    launch_k(pdl, k_bhgs<T, 2, 2>, grid, threads, smem, s, t, c, L, nsweep, src, dst, rhs, guard);
+  } else {
+    ensure_max_smem((const void *)k_bhgs<T, 3, 2>, 200 * 1024);
+    launch_k(pdl, k_bhgs<T, 3, 2>, grid, threads, smem, s, t, c, L, nsweep, src, dst, rhs, guard);
+  }
+}
+
+template <typename T>
+void launch_copy_blocks(const BlockList &L, int ncell, const T *src, T *dst, const int *guard, cudaStream_t s,
+                        bool pdl) {
+  const long work = (long)L.n * ncell;
+  if (work == 0) return;
+  launch_k(pdl, k_copy_blocks<T>, grid_for(work), kThreads, 0, s, L, ncell, src, dst, guard);
+}
+
+template <typename T>
 void launch_smooth(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
                    const int *guard, cudaStream_t s, bool pdl) {
   const long work = (long)L.n * (t.ncell / 2);
@@ -1130,7 +1294,10 @@ void launch_fix_bc(const Topo &t, const Coef<double> &c, const BlockList &L, con
   template void launch_prolong<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,          \
                                   cudaStream_t, bool);                                                          \
   template void launch_prolong_red<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const T *,        \
-                                      const int *, cudaStream_t, bool, const BlockList &);
+                                      const int *, cudaStream_t, bool, const BlockList &);                      \
+  template void launch_bhgs<T>(const Topo &, const Coef<T> &, const BlockList &, int, const T *, T *,          \
+                               const T *, const int *, cudaStream_t, bool);                                     \
+  template void launch_copy_blocks<T>(const BlockList &, int, const T *, T *, const int *, cudaStream_t, bool);
 SAYAKA_INST(double)
 SAYAKA_INST(float)
 #undef SAYAKA_INST

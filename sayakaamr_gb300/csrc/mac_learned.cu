@@ -87,10 +87,11 @@ __device__ __forceinline__ void cell_features(const Topo &t, const Coef<float> &
 // block-local operator the loss uses: aux = [sa][dv*vf][x-face T][y-face T]
 template <int NB>
 __global__ void k_nn_pairs(Topo t, Coef<float> c, BlockList L, const float *__restrict__ r1,
-                           const double *__restrict__ sa, float *feat, float *aux) {
+                           const double *__restrict__ sa, float *feat, float *aux, int off, int stride) {
   constexpr int NC = NB * NB, NF = (NB + 1) * NB, AUXN = 2 * NC + 2 * NF;
   __shared__ float red[NC / 32];
-  const int p = blockIdx.x, ci = threadIdx.x;
+  // sample blockIdx.x is list entry off + blockIdx.x * stride
+  const int p = off + blockIdx.x * stride, ci = threadIdx.x, o = blockIdx.x;
   const int b = L.blocks[p];
   const long q = (long)b * NC + ci;
   const float rv = r1[q];
@@ -98,8 +99,8 @@ __global__ void k_nn_pairs(Topo t, Coef<float> c, BlockList L, const float *__re
   const float s = m > 0.f ? m : 1.f;
   float f[3];
   cell_features<NB>(t, c, b, ci, rv, s, f);
-  for (int k = 0; k < 3; k++) feat[((long)p * 3 + k) * NC + ci] = f[k];
-  float *ax = aux + (long)p * AUXN;
+  for (int k = 0; k < 3; k++) feat[((long)o * 3 + k) * NC + ci] = f[k];
+  float *ax = aux + (long)o * AUXN;
   ax[ci] = (float)sa[(long)p * NC + ci];
   ax[NC + ci] = c.geom[b * 8 + 6] * c.vf[q];
   for (int k = threadIdx.x; k < NF; k += blockDim.x) {
@@ -603,7 +604,7 @@ inline int lgrid(long w) { return (int)std::max<long>(1, std::min<long>((w + 255
 // tol_rel 1e-12, records every iterate x_k; then, with x* the converged
 // solution, e = x* - x_k, r = A e (FP32), z = V(r), r1 = r - A z, e1 = e - z
 // become one training block per tower block.
-int MacGpu::learned_collect(int max_iters) {
+int MacGpu::learned_collect(int max_iters, int max_samples) {
   if (!learned_supported()) {
     fail("learned correction: 2D blocks of 8 or 16 cells only");
     return -1;
@@ -648,9 +649,21 @@ int MacGpu::learned_collect(int max_iters) {
   }
   cudaMemsetAsync(e, 0, n * sizeof(float), stream_);
   cudaMemsetAsync(r, 0, n * sizeof(float), stream_);
-  learned_reserve((int)rec.size() * TL.n);
+  // at most max_samples pairs: every stride-th block of each iterate, the
+  // offset moving from iterate to iterate
+  const long all = (long)rec.size() * TL.n;
+  const int stride = max_samples > 0 && all > max_samples ? (int)((all + max_samples - 1) / max_samples) : 1;
+  long want = 0;
+  for (size_t k = 0; k < rec.size(); k++) {
+    const int off = (int)((k * 7) % stride);
+    want += off < TL.n ? (TL.n - off + stride - 1) / stride : 0;
+  }
+  learned_reserve((int)want);
   const double *sa = d_sfac_.size() > (size_t)L ? d_sfac_[L] : nullptr;
+  int kit = 0;
   for (double *xk : rec) {
+    const int off = (int)((kit++ * 7) % stride);
+    const int cnt = off < TL.n ? (TL.n - off + stride - 1) / stride : 0;
     if (!err_.empty() || !sa) break;
     k_err32<<<lgrid(w), 256, 0, stream_>>>(TL, ncell_, vec_[kSOL], xk, e);
     launch_apply<float>(topo_, c32_, TL, e, r, nullptr, nullptr, stream_);
@@ -658,12 +671,15 @@ int MacGpu::learned_collect(int max_iters) {
     launch_apply<float>(topo_, c32_, TL, z, r1, r, nullptr, stream_);
     k_sub32<<<lgrid(w), 256, 0, stream_>>>(TL, ncell_, e, z, e);
     const long o = (long)ls_.nsamp * ncell_, oa = (long)ls_.nsamp * aux_len();
-    if (tt_.nb == 16)
-      k_nn_pairs<16><<<TL.n, 256, 0, stream_>>>(topo_, c32_, TL, r1, sa, ls_.feat + 3 * o, ls_.aux + oa);
-    else
-      k_nn_pairs<8><<<TL.n, 64, 0, stream_>>>(topo_, c32_, TL, r1, sa, ls_.feat + 3 * o, ls_.aux + oa);
-    CKR_(cudaGetLastError(), -1);
-    ls_.nsamp += TL.n;
+    if (cnt > 0) {
+      if (tt_.nb == 16)
+        k_nn_pairs<16><<<cnt, 256, 0, stream_>>>(topo_, c32_, TL, r1, sa, ls_.feat + 3 * o, ls_.aux + oa, off,
+                                                 stride);
+      else
+        k_nn_pairs<8><<<cnt, 64, 0, stream_>>>(topo_, c32_, TL, r1, sa, ls_.feat + 3 * o, ls_.aux + oa, off, stride);
+      CKR_(cudaGetLastError(), -1);
+    }
+    ls_.nsamp += cnt;
   }
   CKR_(cudaStreamSynchronize(stream_), -1);
   for (double *p : rec) cudaFree(p);

@@ -414,6 +414,8 @@ MacGpu::~MacGpu() {
   fr(d_geom32_);
   fr(d_resid32_);
   fr(d_corr32_);
+  fr(d_corr32b_);
+  fr(d_corr64b_);
   fr(d_st_);
   fr(d_part_);
   fr(d_opP_);
@@ -450,6 +452,14 @@ BlockList MacGpu::sublevel_list(int L, int l) const {
     const long w = (long)t.all.n * ncell_;
     r.sa = d_sfac_[L] + (long)b * ncell_;
     r.ia = d_sfac_[L] + w + (long)b * ncell_;
+  }
+  return r;
+}
+BlockList MacGpu::smooth_list(int L) const {
+  BlockList r = tower_list(L);
+  if (L < (int)d_sfac_.size() && d_sfac_[L]) {
+    r.sa = d_sfac_[L];
+    r.ia = d_sfac_[L] + (long)r.n * ncell_;
   }
   return r;
 }

@@ -43,6 +43,10 @@ struct SolverParams {
   int sublevel_order = 1;     // device V-cycle smoothing order over a tower's sublevels: 0 = finest to
                               // coarsest, red then black per sublevel (the reference's); 1 = one launch per
                               // colour and level parity (sublevels two levels apart never touch)
+  int smoother = 0;           // device V-cycle smoother: 0 = red-black sweeps (n_post per tower, one launch
+                              // per colour); 1 = block-hybrid passes (n_post per tower, each one launch of
+                              // inner_sweeps red-black sweeps per block, Jacobi between blocks)
+  int inner_sweeps = 2;       // smoother 1: red-black sweeps per block in one pass
 };
 
 struct SolveInfo {
@@ -116,7 +120,7 @@ class MacGpu {
 
   // learned block correction (mac_learned.cu)
   bool learned_supported() const;
-  int learned_collect(int max_iters);
+  int learned_collect(int max_iters, int max_samples = 0);  // max_samples 0: every block of every iterate
   float learned_train(int epochs, float lr, int batch, unsigned seed);
   float learned_loss_grad(const float *feat, const float *aux, int n, float *grad);
   int aux_len() const { return 2 * tt_.nb * tt_.nb + 2 * (tt_.nb + 1) * tt_.nb; }
@@ -269,6 +273,19 @@ class MacGpu {
   long coef_version_ = 1, fast_coef_version_ = 0;
   float *d_tff32_[3] = {}, *d_bcoef32_[3] = {}, *d_afrac32_[3] = {}, *d_vf32_ = nullptr, *d_geom32_ = nullptr;
   float *d_resid32_ = nullptr, *d_corr32_ = nullptr;
+  // second correction vector of the block-hybrid smoother's passes (they
+  // read one and write the other)
+  float *d_corr32b_ = nullptr;
+  double *d_corr64b_ = nullptr;
+  template <typename T>
+  T *corr_alt() {
+    if constexpr (sizeof(T) == 4)
+      return d_corr32b_;
+    else
+      return d_corr64b_;
+  }
+  // tower L with its FP64 smoother factors, every sublevel (block-hybrid passes)
+  BlockList smooth_list(int L) const;
   Coef<float> c32_{};
   FState *d_st_ = nullptr, *h_st_ = nullptr;
   double *d_part_ = nullptr;
@@ -306,6 +323,7 @@ class MacGpu {
   int graph_prec_ = -1, graph_npost_ = -1;
   int kernels_per_iter_ = 0;
   int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1, graph_nn_ = -1, graph_order_ = -1;
+  int graph_smoother_ = -1, graph_inner_ = -1;
   bool graph_stale() const;
   int rbgs_variant_[2] = {-1, -1};  // tuned smoother variant per precision (0 FP64, 1 FP32)
   float rbgs_us_[2][16] = {};       // measured microseconds per variant (kRbgsVariants <= 16)
