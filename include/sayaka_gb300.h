@@ -134,6 +134,10 @@ typedef struct sayaka_params {
                              the values outside the block frozen (Gauss-Seidel inside a block, Jacobi between
                              blocks; a fixed linear map, another preconditioner with the same solution) */
   int32_t inner_sweeps;   /* smoother 1: red-black sweeps per block and pass (default 2) */
+  int32_t per_problem;    /* device path, a tree made of several independent problems (connected components,
+                             e.g. a forest of trees given as one table): 1 = one BiCGSTAB state per problem,
+                             each stopping at its own tolerance, as if solved alone (default); 0 = one shared
+                             state (scalars over all problems) */
 } sayaka_params;
 
 typedef struct sayaka_solve_info {
@@ -220,6 +224,14 @@ int sayaka_mac_launch_counts(sayaka_mac *h, int32_t *prologue, int32_t *per_iter
 int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n);
 /* level of the device solve's dense bottom solve once prepared (-1 before) */
 int32_t sayaka_mac_bottom_level(const sayaka_mac *h);
+/* number of independent problems (connected components) of the handle's
+ * tree; with per_problem = 1 the last device solve's per-problem outcome:
+ * iterations[k] and the final relative residual rel_resid[k] = |r|/|r0| of
+ * problem k (problems numbered by their lowest block id; arrays of n >= the
+ * count, either may be NULL).  Returns the count, or -1 after a solve with
+ * one shared state.  No counterpart in the reference (it solves one tree). */
+int32_t sayaka_mac_problem_count(const sayaka_mac *h);
+int32_t sayaka_mac_problem_states(sayaka_mac *h, int32_t *iterations, double *rel_resid, int32_t n);
 /* number of blocks in tower L, or at one level of it (sublevel >= 1) */
 int32_t sayaka_mac_tower_size(sayaka_mac *h, int32_t L, int32_t sublevel);
 

@@ -41,7 +41,7 @@ class Params(C.Structure):
                 ("vcycle_kernel", C.c_int32), ("pdl", C.c_int32),
                 ("cluster_cells", C.c_int32), ("smooth_variant", C.c_int32), ("learned", C.c_int32),
                 ("bottom_level", C.c_int32), ("bottom_half", C.c_int32), ("sublevel_order", C.c_int32),
-                ("smoother", C.c_int32), ("inner_sweeps", C.c_int32)]
+                ("smoother", C.c_int32), ("inner_sweeps", C.c_int32), ("per_problem", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -105,6 +105,8 @@ SIGNATURES = {
     "sayaka_mac_get_rhs_compact": (C.c_int, [_V, _f64p]),
     "sayaka_mac_init_from": (C.c_int, [_V, _V]),
     "sayaka_mac_bottom_level": (C.c_int32, [_V]),
+    "sayaka_mac_problem_count": (C.c_int32, [_V]),
+    "sayaka_mac_problem_states": (C.c_int32, [_V, _i32p, _f64p, C.c_int32]),
     "sayaka_cuda_peek_error": (C.c_int32, []),
     "sayaka_fp_selftest": (C.c_int, [_f64p, _f32p, C.c_int, _f32p, _f32p, _f64p, _f64p, _f64p, _f64p]),
     "sayaka_mac_learned_nparam": (C.c_int32, []),
@@ -499,6 +501,19 @@ class MacSolver:
         us = (C.c_float * 10)()
         v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 10)
         return int(v), [float(x) for x in us]
+
+    def problem_count(self):
+        """independent problems (connected components) of the tree"""
+        return self.lib.sayaka_mac_problem_count(self.h)
+
+    def problem_states(self):
+        """per-problem (iterations, relative residual) of the last device solve
+        with one state per problem, or None"""
+        n = self.problem_count()
+        it = np.zeros(max(n, 1), dtype=np.int32)
+        rr = np.zeros(max(n, 1))
+        r = self.lib.sayaka_mac_problem_states(self.h, it.ctypes.data_as(_i32p), rr.ctypes.data_as(_f64p), n)
+        return None if r < 0 else (it[:r], rr[:r])
 
     def bottom_level(self):
         """level of the device solve's dense bottom solve (-1 before prepare)"""

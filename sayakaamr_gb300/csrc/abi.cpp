@@ -413,6 +413,7 @@ void sayaka_params_default(sayaka_params *p) {
   p->sublevel_order = d.sublevel_order;
   p->smoother = d.smoother;
   p->inner_sweeps = d.inner_sweeps;
+  p->per_problem = d.per_problem;
 }
 
 int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
@@ -643,6 +644,8 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
       return (int)SAYAKA_BAD_INPUT;
     s.smoother = p->smoother;
     s.inner_sweeps = p->inner_sweeps;
+    if (p->per_problem < 0 || p->per_problem > 1) return (int)SAYAKA_BAD_INPUT;
+    s.per_problem = p->per_problem;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
   });
@@ -865,6 +868,19 @@ int sayaka_mac_residual_compact(sayaka_mac *h, int32_t L, const double *x, const
     h->gpu->residual(L, x, rhs, r);
     return (int)SAYAKA_OK;
   });
+}
+int32_t sayaka_mac_problem_count(const sayaka_mac *h) {
+  if (!h || !h->gpu) return -1;
+  return h->gpu->problems();
+}
+int32_t sayaka_mac_problem_states(sayaka_mac *h, int32_t *iterations, double *rel_resid, int32_t n) {
+  if (!h || !h->gpu || n < 0) return -1;
+  DeviceScope on_device(h->gpu->device());
+  std::vector<int> it(std::max(0, n));
+  const int r = h->gpu->problem_states(it.data(), rel_resid, n);
+  if (r >= 0 && iterations)
+    for (int k = 0; k < n && k < r; k++) iterations[k] = it[k];
+  return r;
 }
 int32_t sayaka_mac_bottom_level(const sayaka_mac *h) {
   if (!h || !h->gpu) return -1;

@@ -58,20 +58,6 @@ constexpr int kHXBlock = 7;
 constexpr int kHXKids = 8;
 constexpr int kHXPar = 32;
 
-// a block list with per-block packed face types (2 bits per face)
-struct BlockList {
-  const int *blocks;
-  const uint16_t *ftypes;  // may be null for lists that need no face types
-  int n;
-  // FP64 smoother factors of a tower sublevel list, [entry][cell]:
-  // sa = dv*vf/diag, ia = 1/diag (0 where vf = 0); null when not built
-  const double *sa = nullptr, *ia = nullptr;
-  const int *hx = nullptr;  // halo descriptors [entry][kHX] of tower lists, else null
-  // level lists: [entry] parent * 8 + which_child; non-leaf lists:
-  // [entry][8] children; null elsewhere
-  const int *links = nullptr;
-};
-
 // BiCGSTAB state kept on the device (FP64 scalars and control flags) by the
 // graph-captured solve of mac_fast.cu
 struct FState {
@@ -93,6 +79,40 @@ struct FState {
   int verify, restart, restarts, pad2_;
 };
 
+// a block list with per-block packed face types (2 bits per face)
+struct BlockList {
+  const int *blocks;
+  const uint16_t *ftypes;  // may be null for lists that need no face types
+  int n;
+  // FP64 smoother factors of a tower sublevel list, [entry][cell]:
+  // sa = dv*vf/diag, ia = 1/diag (0 where vf = 0); null when not built
+  const double *sa = nullptr, *ia = nullptr;
+  const int *hx = nullptr;  // halo descriptors [entry][kHX] of tower lists, else null
+  // level lists: [entry] parent * 8 + which_child; non-leaf lists:
+  // [entry][8] children; null elsewhere
+  const int *links = nullptr;
+  // a forest of independent problems solved with one BiCGSTAB state per
+  // problem (connected component of the tree): comp[block] and the states;
+  // kernels leave the blocks of a finished problem alone.  Null otherwise.
+  const int *comp = nullptr;
+  const FState *stc = nullptr;
+};
+
+// chunks of a block list listed problem by problem (one BiCGSTAB state per
+// problem): the BiCGSTAB kernels run one CTA per chunk of at most kChunkCells
+// cells of one problem
+constexpr int kChunkCells = 2048;
+struct Chunks {
+  const int *comp;       // per chunk: its problem
+  const int *beg, *end;  // per chunk: first and past-last cell of the list
+  const int *c0, *cn;    // per problem: first chunk and number of chunks
+};
+
+// the block belongs to a problem whose solve has finished
+__host__ __device__ __forceinline__ bool block_off(const BlockList &L, int b) {
+  return L.stc && L.stc[L.comp[b]].done;
+}
+
 // The dense FP64 bottom solve: one inverse per connected component of the
 // level-1 blocks (a forest of independent problems has one per problem),
 // rows grouped by component, one CTA tile per 8 rows.
@@ -103,6 +123,8 @@ struct BottomDev {
   const long long *comp_off;   // start of each component's inverse in binv
   const int *tile_comp, *tile_row0;
   int ntiles, ncell, max_n;
+  const int *comp = nullptr;      // per-problem states (see BlockList): rows of finished problems are skipped
+  const FState *stc = nullptr;
   const float *binv32 = nullptr;  // FP32 copy of binv for the FP32 V-cycle (bottom level above 1)
   // or, instead, an FP16 copy with one FP32 scale per row (entry = h * scale)
   const unsigned short *binv16 = nullptr;

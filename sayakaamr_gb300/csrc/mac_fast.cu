@@ -59,12 +59,13 @@ __device__ __forceinline__ double wmax(double v) {
   return v;
 }
 
-// Grid-wide reduction of NV values (bit i of maxmask: max, else sum).  Each
-// CTA writes its partials; the last CTA to arrive combines them in CTA order
-// (deterministic for a fixed grid) and runs `epi` on thread 0.
+// Reduction of NV values (bit i of maxmask: max, else sum) over the `count`
+// CTAs whose partial slots are first .. first+count-1 (this CTA's is `slot`):
+// each CTA writes its partials; the last of them to arrive combines them in
+// slot order (deterministic for a fixed grid) and runs `epi` on thread 0.
 template <int NV, class Epi>
-__device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, double *partials, unsigned *counter,
-                                            Epi epi) {
+__device__ __forceinline__ void seg_reduce(double (&v)[NV], unsigned maxmask, double *partials, unsigned *counter,
+                                           int first, int count, int slot, Epi epi) {
   __shared__ double sh[NV][kTPB / 32];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -92,11 +93,11 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, d
     warp0(r);
     if (lane == 0) {
 #pragma unroll
-      for (int i = 0; i < NV; i++) partials[blockIdx.x * NV + i] = r[i];
+      for (int i = 0; i < NV; i++) partials[slot * NV + i] = r[i];
       // release the partials, acquire everyone else's if this CTA is last
       unsigned old;
       asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(old) : "l"(counter) : "memory");
-      last = old == gridDim.x - 1;
+      last = old == (unsigned)count - 1;
     }
   }
   __syncthreads();
@@ -104,7 +105,7 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, d
   double acc[NV];
 #pragma unroll
   for (int i = 0; i < NV; i++) acc[i] = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+  for (int b = first + threadIdx.x; b < first + count; b += blockDim.x) {
 #pragma unroll
     for (int i = 0; i < NV; i++) {
       const double pv = ((volatile double *)partials)[b * NV + i];
@@ -126,6 +127,52 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, d
       *counter = 0;
     }
   }
+}
+
+// the whole grid as one segment
+template <int NV, class Epi>
+__device__ __forceinline__ void grid_reduce(double (&v)[NV], unsigned maxmask, double *partials, unsigned *counter,
+                                            Epi epi) {
+  seg_reduce<NV>(v, maxmask, partials, counter, 0, (int)gridDim.x, (int)blockIdx.x, epi);
+}
+
+// A forest of independent problems (the connected components of the tree)
+// solved with one BiCGSTAB state per problem: the finest tower's blocks are
+// listed problem by problem, and the BiCGSTAB kernels run one CTA per chunk
+// of at most kChunkCells consecutive cells of one problem, so that every
+// reduction is a segment of whole CTAs (seg_reduce) and every CTA reads one
+// state.
+// the cells a CTA walks, the state it reads and its reduction segment
+struct Work {
+  int it0, it1, step;
+  FState *st;
+  int first, count, slot;
+  unsigned *counter;
+};
+template <bool MULTI>
+__device__ __forceinline__ Work work_of(const Chunks &ch, FState *st, int total, unsigned *counters) {
+  Work w;
+  if constexpr (MULTI) {
+    const int k = blockIdx.x, c = ch.comp[k];
+    w.it0 = ch.beg[k] + threadIdx.x;
+    w.it1 = ch.end[k];
+    w.step = blockDim.x;
+    w.st = st + c;
+    w.first = ch.c0[c];
+    w.count = ch.cn[c];
+    w.slot = k;
+    w.counter = counters ? counters + c : nullptr;
+  } else {
+    w.it0 = blockIdx.x * blockDim.x + threadIdx.x;
+    w.it1 = total;
+    w.step = gridDim.x * blockDim.x;
+    w.st = st;
+    w.first = 0;
+    w.count = gridDim.x;
+    w.slot = blockIdx.x;
+    w.counter = counters;
+  }
+  return w;
 }
 
 // precision conversions of the vector kernels, exact or correctly rounded
@@ -306,15 +353,16 @@ __global__ void k_pro_copy(BlockList L, int ncell, const double *sol, double *x0
 
 // p = r (first iteration) or p = r + beta*(p - omega*v) in the reference's two
 // saxby steps; the V-cycle's residual (rhs - A*0) = masked p in precision T
-template <typename T>
-__global__ void k_pupdate(BlockList L, int ncell, const FState *st, const double *r, double *p, const double *v,
+template <typename T, bool MULTI>
+__global__ void k_pupdate(BlockList L, int ncell, Chunks ch, FState *stb, const double *r, double *p, const double *v,
                           const double *vf, T *resid) {
   pdl_enter();
+  const Work wk = work_of<MULTI>(ch, stb, L.n * ncell, nullptr);
+  const FState *st = wk.st;
   if (st->done) return;
   const bool first = st->iter == 1 || st->restart;
   const double beta = st->beta, om = st->omega;
-  const int total = L.n * ncell;
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+  for (int it = wk.it0; it < wk.it1; it += wk.step) {
     const long q = cell_of(L, ncell, it);
     double pv;
     if (first) {
@@ -329,16 +377,17 @@ __global__ void k_pupdate(BlockList L, int ncell, const FState *st, const double
 
 // s = r - alpha v ; x = x + alpha phat ; V-cycle residual = masked s ; |s|
 // (phat: the FP64 V-cycle's output itself, or the FP32 one widened to FP64)
-template <typename T, typename TP>
-__global__ void __launch_bounds__(kTPB) k_supdate(BlockList L, int ncell, FState *st, const double *r, const double *v,
-                                                double *s, double *x, const TP *phat, const double *vf, T *resid,
-                                                double *partials, unsigned *counter) {
+template <typename T, typename TP, bool MULTI>
+__global__ void __launch_bounds__(kTPB) k_supdate(BlockList L, int ncell, Chunks ch, FState *stb, const double *r,
+                                                const double *v, double *s, double *x, const TP *phat,
+                                                const double *vf, T *resid, double *partials, unsigned *counter) {
   pdl_enter();
+  const Work wk = work_of<MULTI>(ch, stb, L.n * ncell, counter);
+  FState *st = wk.st;
   if (st->done) return;
   const double a = st->alpha;
   unsigned long long mu = 0ull;  // max |s| as bit patterns (NaN-propagating)
-  const int total = L.n * ncell;
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+  for (int it = wk.it0; it < wk.it1; it += wk.step) {
     const long q = cell_of(L, ncell, it);
     const double sv = __fma_rn(-a, v[q], r[q]);
     s[q] = sv;
@@ -347,21 +396,22 @@ __global__ void __launch_bounds__(kTPB) k_supdate(BlockList L, int ncell, FState
     mu = fpint::max_abs(mu, sv);
   }
   double m[1] = {fpint::from_bits(mu)};
-  grid_reduce<1>(m, 1u, partials, counter, EpiHalf{st});
+  seg_reduce<1>(m, 1u, partials, wk.counter, wk.first, wk.count, wk.slot, EpiHalf{st});
 }
 
 // x = x + omega shat ; r = s - omega t ; |r| ; rhat.r
-template <typename T>
-__global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, FState *st, double *x, const T *shat,
-                                                double *r, const double *s, const double *t, const double *rhat,
-                                                double *partials, unsigned *counter) {
+template <typename T, bool MULTI>
+__global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, Chunks ch, FState *stb, double *x,
+                                                const T *shat, double *r, const double *s, const double *t,
+                                                const double *rhat, double *partials, unsigned *counter) {
   pdl_enter();
+  const Work wk = work_of<MULTI>(ch, stb, L.n * ncell, counter);
+  FState *st = wk.st;
   if (st->done) return;
   const double om = st->omega;
   unsigned long long mu = 0ull;  // max |r| as bit patterns (NaN-propagating)
   double m[2] = {0.0, 0.0};
-  const int total = L.n * ncell;
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+  for (int it = wk.it0; it < wk.it1; it += wk.step) {
     const long q = cell_of(L, ncell, it);
     x[q] = __fma_rn(om, widen_from<T>(shat[q]), x[q]);
     const double rv = __fma_rn(-om, t[q], s[q]);
@@ -370,15 +420,17 @@ __global__ void __launch_bounds__(kTPB) k_rupdate(BlockList L, int ncell, FState
     m[1] = __fma_rn(rhat[q], rv, m[1]);
   }
   m[0] = fpint::from_bits(mu);
-  grid_reduce<2>(m, 1u, partials, counter, EpiEnd{st});
+  seg_reduce<2>(m, 1u, partials, wk.counter, wk.first, wk.count, wk.slot, EpiEnd{st});
 }
 
 // after the loop: x0 += x ; sol = x0 when converged
-__global__ void k_finish(BlockList L, int ncell, const FState *st, double *x0, const double *x, double *sol) {
+template <bool MULTI>
+__global__ void k_finish(BlockList L, int ncell, Chunks ch, const FState *stb, double *x0, const double *x,
+                         double *sol) {
   pdl_enter();
-  if (!st->conv) return;
-  const int total = L.n * ncell;
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+  const Work wk = work_of<MULTI>(ch, const_cast<FState *>(stb), L.n * ncell, nullptr);
+  if (!wk.st->conv) return;
+  for (int it = wk.it0; it < wk.it1; it += wk.step) {
     const long q = cell_of(L, ncell, it);
     const double v = x0[q] + x[q];
     x0[q] = v;
@@ -393,11 +445,30 @@ __global__ void k_vc_out(BlockList L, int ncell, const FState *st, const T *corr
   if (st->done) return;
   const int total = L.n * ncell;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
-    const long q = cell_of(L, ncell, it);
+    const int p = it / ncell;
+    if (block_off(L, L.blocks[p])) continue;
+    const long q = (long)L.blocks[p] * ncell + (it - p * ncell);
     if constexpr (sizeof(T) == 4)
       out[q] = fpint::widen_plus0(corr[q]);
     else
       out[q] = 0.0 + corr[q];
+  }
+}
+
+// every problem's state read: the loop goes on while one is not done; the
+// shared state's done flag (the guard of the V-cycle kernels) is set once all are
+__global__ void k_set_cond_multi(cudaGraphConditionalHandle h, const FState *stc, int ncomp, FState *st) {
+  pdl_enter();
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  int a = 0;
+  for (int c = threadIdx.x; c < ncomp; c += blockDim.x) a |= !stc[c].done;
+  if (a) atomicOr(&any, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    st->done = any ? 0 : 1;
+    if (h) cudaGraphSetConditional(h, any ? 1u : 0u);
   }
 }
 
@@ -529,20 +600,21 @@ __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &
 // MODE 0: y = A x, rhat.y (EpiAlpha) ; MODE 1: y = A x, y.w, y.y (EpiOmega) ;
 // MODE 2: y = w - A x (0 where vf = 0), |y|, y.y (EpiInit) ;
 // MODE 3: only while verifying: y = y2 = w - A x, |y|, y.y (EpiVerify)
-template <int ND, int MODE, typename TX>
-__global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockList L, const TX *__restrict__ x,
-                                               double *__restrict__ y, const double *__restrict__ w,
-                                               const double *__restrict__ P, const double *__restrict__ S,
-                                               FState *st, double *partials, unsigned *counter,
-                                               double *__restrict__ y2 = nullptr) {
+template <int ND, int MODE, typename TX, bool MULTI>
+__global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockList L, Chunks ch,
+                                               const TX *__restrict__ x, double *__restrict__ y,
+                                               const double *__restrict__ w, const double *__restrict__ P,
+                                               const double *__restrict__ S, FState *stb, double *partials,
+                                               unsigned *counter, double *__restrict__ y2 = nullptr) {
   using namespace stencil;
   pdl_enter();
+  const Work wk = work_of<MULTI>(ch, stb, L.n * t.ncell, counter);
+  FState *st = wk.st;
   if (MODE == 3 && !st->verify) return;
   if (MODE < 2 && st->done) return;
   double acc[2] = {0.0, 0.0};
   unsigned long long mu = 0ull;  // MODE >= 2: max |y| as bit patterns
-  const int total = L.n * t.ncell;
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+  for (int it = wk.it0; it < wk.it1; it += wk.step) {
     int p, ci, ijk[3];
     split_cell<ND>(it, t, p, ci);
     decode_fast<ND>(ci, t, ijk);
@@ -567,19 +639,20 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
     }
   }
   if (MODE >= 2) acc[0] = fpint::from_bits(mu);
-  if (MODE == 0) grid_reduce<2>(acc, 0u, partials, counter, EpiAlpha{st});
-  if (MODE == 1) grid_reduce<2>(acc, 0u, partials, counter, EpiOmega{st});
-  if (MODE == 2) grid_reduce<2>(acc, 1u, partials, counter, EpiInit{st});
-  if (MODE == 3) grid_reduce<2>(acc, 1u, partials, counter, EpiVerify{st});
+  if (MODE == 0) seg_reduce<2>(acc, 0u, partials, wk.counter, wk.first, wk.count, wk.slot, EpiAlpha{st});
+  if (MODE == 1) seg_reduce<2>(acc, 0u, partials, wk.counter, wk.first, wk.count, wk.slot, EpiOmega{st});
+  if (MODE == 2) seg_reduce<2>(acc, 1u, partials, wk.counter, wk.first, wk.count, wk.slot, EpiInit{st});
+  if (MODE == 3) seg_reduce<2>(acc, 1u, partials, wk.counter, wk.first, wk.count, wk.slot, EpiVerify{st});
 }
 
 // while verifying: x0 += x, x = 0 (the pass's solution folded into x0)
-__global__ void __launch_bounds__(kTPB) k_verify_fold(BlockList L, int ncell, const FState *st, double *x0,
-                                                    double *x) {
+template <bool MULTI>
+__global__ void __launch_bounds__(kTPB) k_verify_fold(BlockList L, int ncell, Chunks ch, const FState *stb,
+                                                    double *x0, double *x) {
   pdl_enter();
-  if (!st->verify) return;
-  const int total = L.n * ncell;
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+  const Work wk = work_of<MULTI>(ch, const_cast<FState *>(stb), L.n * ncell, nullptr);
+  if (!wk.st->verify) return;
+  for (int it = wk.it0; it < wk.it1; it += wk.step) {
     const long q = cell_of(L, ncell, it);
     x0[q] = x0[q] + x[q];
     x[q] = 0.0;
@@ -1158,7 +1231,10 @@ void MacGpu::build_bottom() {
   }
   CK_(cudaStreamSynchronize(stream_));
   bot_ = BottomDev{d_binv_, d_bot_blocks_, d_comp_row0_, d_comp_n_, d_comp_off_, d_tile_comp_, d_tile_row0_,
-                   (int)tile_comp.size(), ncell_, max_n, d_binv32_, d_binv16_, d_rscale_};
+                   (int)tile_comp.size(), ncell_, max_n};
+  bot_.binv32 = d_binv32_;
+  bot_.binv16 = d_binv16_;
+  bot_.rscale = d_rscale_;
   n_pins_ = (int)pins.size();
   n_bot_comp_ = nc;
   bottom_ready_ = true;
@@ -1256,7 +1332,12 @@ void MacGpu::bottom_launch(T *resid, T *corr) {
   const size_t smem = (size_t)bot_.max_n * sizeof(double);
   if (smem > 48 * 1024)
     ensure_max_smem((const void *)k_bottom_gemv<T>, (int)smem);
-  launch_k(prm_.pdl != 0, k_bottom_gemv<T>, bot_.ntiles, kTPB, smem, stream_, bot_, (const T *)resid, corr,
+  BottomDev bd = bot_;
+  if (solve_lists_ && multi()) {
+    bd.comp = d_comp_;
+    bd.stc = d_stc_;
+  }
+  launch_k(prm_.pdl != 0, k_bottom_gemv<T>, bot_.ntiles, kTPB, smem, stream_, bd, (const T *)resid, corr,
            (const FState *)d_st_);
 }
 template void MacGpu::bottom_launch<float>(float *, float *);
@@ -1268,9 +1349,10 @@ template <typename T>
 void MacGpu::precondition(int L, T *resid, T *corr, const Coef<T> &c, double *out) {
   const bool nn = sizeof(T) == 4 && learned_active();
   double *o = nn ? nullptr : out;
-  if (prm_.vcycle_kernel == 2 && prm_.smoother == 0)
+  const bool fused = prm_.smoother == 0 && !(solve_lists_ && multi());
+  if (prm_.vcycle_kernel == 2 && fused)
     vcycle_cluster<T>(resid, corr, c, o);
-  else if (prm_.vcycle_kernel == 1 && prm_.smoother == 0)
+  else if (prm_.vcycle_kernel == 1 && fused)
     vcycle_coop<T>(resid, corr, c, o);
   else
     vcycle_device<T>(L, resid, corr, c, o);
@@ -1308,42 +1390,80 @@ template <typename T, typename TO>
 void MacGpu::iteration_body(T *resid, T *corr, const Coef<T> &c, const TO *PH, const TO *SH, double *out_p,
                             double *out_s) {
   const int L = finest_;
-  BlockList TL = tower_list(L);
+  const bool mp = multi();
+  // the BiCGSTAB kernels: the finest tower (problem by problem and one CTA
+  // per chunk with one state per problem, else grid-stride with one state)
+  const BlockList TL = mp ? BlockList{tlc_.blocks, tlc_.ftypes, tlc_.n, nullptr, nullptr, tlc_.hx} : tower_list(L);
   const long w = (long)TL.n * ncell_;
+  const Chunks ch = chunks();
+  FState *ST = mp ? d_stc_ : d_st_;
+  double *PART = mp ? d_cpart_ : d_part_;
+  unsigned *CNT = mp ? d_ccnt_ : d_cnt_;
+  const int gr = mp ? nchunks_ : red_grid(w), ge = mp ? nchunks_ : ew_grid(w);
   double *R = vec_[kR], *RHAT = vec_[kRHAT], *P = vec_[kP], *S = vec_[kS];
   double *V = vec_[kV], *Tt = vec_[kT], *X = vec_[kX];
   const bool pdl = prm_.pdl != 0;
-  launch_k(pdl, k_pupdate<T>, ew_grid(w), kTPB, 0, stream_, TL, ncell_, (const FState *)d_st_, (const double *)R, P,
-           (const double *)V, (const double *)d_vf_, resid);
+  const double *OP = d_opP_, *OS = d_opS_;
+  auto op = [&](auto mode, const auto *x, double *y, const double *wv, double *y2) {
+    constexpr int M = decltype(mode)::value;
+    using TX = std::remove_const_t<std::remove_pointer_t<decltype(x)>>;
+    if (tt_.ndim == 2) {
+      if (mp)
+        launch_k(pdl, k_op_red<2, M, TX, true>, gr, kTPB, 0, stream_, topo_, c64_, TL, ch, x, y, wv, OP, OS, ST, PART,
+                 CNT, y2);
+      else
+        launch_k(pdl, k_op_red<2, M, TX, false>, gr, kTPB, 0, stream_, topo_, c64_, TL, ch, x, y, wv, OP, OS, ST,
+                 PART, CNT, y2);
+    } else {
+      if (mp)
+        launch_k(pdl, k_op_red<3, M, TX, true>, gr, kTPB, 0, stream_, topo_, c64_, TL, ch, x, y, wv, OP, OS, ST, PART,
+                 CNT, y2);
+      else
+        launch_k(pdl, k_op_red<3, M, TX, false>, gr, kTPB, 0, stream_, topo_, c64_, TL, ch, x, y, wv, OP, OS, ST,
+                 PART, CNT, y2);
+    }
+  };
+  if (mp)
+    launch_k(pdl, k_pupdate<T, true>, ge, kTPB, 0, stream_, TL, ncell_, ch, ST, (const double *)R, P,
+             (const double *)V, (const double *)d_vf_, resid);
+  else
+    launch_k(pdl, k_pupdate<T, false>, ge, kTPB, 0, stream_, TL, ncell_, ch, ST, (const double *)R, P,
+             (const double *)V, (const double *)d_vf_, resid);
   precondition<T>(L, resid, corr, c, out_p);
-  if (tt_.ndim == 2)
-    launch_k(pdl, k_op_red<2, 0, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, PH, V,
-             (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_, (double *)nullptr);
+  op(std::integral_constant<int, 0>{}, PH, V, (const double *)RHAT, (double *)nullptr);
+  if (mp)
+    launch_k(pdl, k_supdate<T, TO, true>, gr, kTPB, 0, stream_, TL, ncell_, ch, ST, (const double *)R,
+             (const double *)V, S, X, PH, (const double *)d_vf_, resid, PART, CNT);
   else
-    launch_k(pdl, k_op_red<3, 0, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, PH, V,
-             (const double *)RHAT, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_, (double *)nullptr);
-  launch_k(pdl, k_supdate<T, TO>, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, (const double *)R, (const double *)V,
-           S, X, PH, (const double *)d_vf_, resid, d_part_, d_cnt_);
+    launch_k(pdl, k_supdate<T, TO, false>, gr, kTPB, 0, stream_, TL, ncell_, ch, ST, (const double *)R,
+             (const double *)V, S, X, PH, (const double *)d_vf_, resid, PART, CNT);
   precondition<T>(L, resid, corr, c, out_s);
-  if (tt_.ndim == 2)
-    launch_k(pdl, k_op_red<2, 1, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, SH, Tt,
-             (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_, (double *)nullptr);
+  op(std::integral_constant<int, 1>{}, SH, Tt, (const double *)S, (double *)nullptr);
+  if (mp)
+    launch_k(pdl, k_rupdate<TO, true>, gr, kTPB, 0, stream_, TL, ncell_, ch, ST, X, SH, R, (const double *)S,
+             (const double *)Tt, (const double *)RHAT, PART, CNT);
   else
-    launch_k(pdl, k_op_red<3, 1, TO>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, SH, Tt,
-             (const double *)S, (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_, (double *)nullptr);
-  launch_k(pdl, k_rupdate<TO>, red_grid(w), kTPB, 0, stream_, TL, ncell_, d_st_, X, SH, R,
-           (const double *)S, (const double *)Tt, (const double *)RHAT, d_part_, d_cnt_);
+    launch_k(pdl, k_rupdate<TO, false>, gr, kTPB, 0, stream_, TL, ncell_, ch, ST, X, SH, R, (const double *)S,
+             (const double *)Tt, (const double *)RHAT, PART, CNT);
   // verified convergence (both kernels return at once unless a pass converged)
   double *X0 = vec_[kX0];
-  launch_k(pdl, k_verify_fold, ew_grid(w), kTPB, 0, stream_, TL, ncell_, (const FState *)d_st_, X0, X);
-  if (tt_.ndim == 2)
-    launch_k(pdl, k_op_red<2, 3, double>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)X0, R,
-             (const double *)vec_[kRHS], (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_,
-             RHAT);
+  if (mp)
+    launch_k(pdl, k_verify_fold<true>, ge, kTPB, 0, stream_, TL, ncell_, ch, (const FState *)ST, X0, X);
   else
-    launch_k(pdl, k_op_red<3, 3, double>, red_grid(w), kTPB, 0, stream_, topo_, c64_, TL, (const double *)X0, R,
-             (const double *)vec_[kRHS], (const double *)d_opP_, (const double *)d_opS_, d_st_, d_part_, d_cnt_,
-             RHAT);
+    launch_k(pdl, k_verify_fold<false>, ge, kTPB, 0, stream_, TL, ncell_, ch, (const FState *)ST, X0, X);
+  op(std::integral_constant<int, 3>{}, (const double *)X0, R, (const double *)vec_[kRHS], RHAT);
+}
+
+// the chunk table of the per-problem states (empty with one shared state)
+Chunks MacGpu::chunks() const {
+  Chunks ch{};
+  if (!multi()) return ch;
+  ch.comp = d_chunk_;
+  ch.beg = d_chunk_ + nchunks_;
+  ch.end = d_chunk_ + 2 * nchunks_;
+  ch.c0 = d_chunk_ + 3 * nchunks_;
+  ch.cn = d_chunk_ + 3 * nchunks_ + ncomp_;
+  return ch;
 }
 
 void MacGpu::drop_graph() {
@@ -1371,11 +1491,16 @@ void MacGpu::capture_loop(int precision) {
   CK_(cudaGraphAddNode(&node, graph_, nullptr, nullptr, 0, &np));
   cudaGraph_t body = np.conditional.phGraph_out[0];
   CK_(cudaStreamBeginCaptureToGraph(stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  solve_lists_ = true;
   if (precision == 1)
     iteration_device<float>(d_resid32_, d_corr32_, c32_);
   else
     iteration_device<double>(vec_[kRESID], vec_[kCORR], c64_);
-  launch_k(prm_.pdl != 0, k_set_cond, 1, 1, 0, stream_, h, (const FState *)d_st_);
+  solve_lists_ = false;
+  if (multi())
+    launch_k(prm_.pdl != 0, k_set_cond_multi, 1, 256, 0, stream_, h, (const FState *)d_stc_, ncomp_, d_st_);
+  else
+    launch_k(prm_.pdl != 0, k_set_cond, 1, 1, 0, stream_, h, (const FState *)d_st_);
   cudaGraph_t out = nullptr;
   CK_(cudaStreamEndCapture(stream_, &out));
   // count the kernel nodes of one iteration (reported as launches per step)
@@ -1399,6 +1524,7 @@ void MacGpu::capture_loop(int precision) {
   graph_order_ = prm_.sublevel_order;
   graph_smoother_ = prm_.smoother;
   graph_inner_ = prm_.inner_sweeps;
+  graph_multi_ = (int)multi();
 }
 
 // the captured graph was recorded with other parameters than the current ones
@@ -1407,7 +1533,7 @@ bool MacGpu::graph_stale() const {
          graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl || graph_cc_ != prm_.cluster_cells ||
          graph_var_ != rbgs_variant_[prm_.precision == 1] || graph_nn_ != (int)learned_active() ||
          graph_order_ != prm_.sublevel_order || graph_smoother_ != prm_.smoother ||
-         graph_inner_ != prm_.inner_sweeps;
+         graph_inner_ != prm_.inner_sweeps || graph_multi_ != (int)multi();
 }
 
 int MacGpu::cg_solve_device(SolveInfo *info) {
@@ -1438,8 +1564,12 @@ int MacGpu::cg_solve_enqueue() {
 
 int MacGpu::enqueue_solve() {
   const int L = finest_;
-  BlockList TL = tower_list(L);
+  const bool mp = multi();
+  const BlockList TL = mp ? BlockList{tlc_.blocks, tlc_.ftypes, tlc_.n, nullptr, nullptr, tlc_.hx} : tower_list(L);
   const long w = (long)TL.n * ncell_;
+  const Chunks ch = chunks();
+  FState *ST = mp ? d_stc_ : d_st_;
+  const int gr = mp ? nchunks_ : red_grid(w), ge = mp ? nchunks_ : ew_grid(w);
   FState init{};
   init.tol_rel = prm_.tol_rel;
   init.tol_abs = prm_.tol_abs;
@@ -1448,15 +1578,31 @@ int MacGpu::enqueue_solve() {
   init.nn_best = 1e300;
   *h_st_ = init;
   CKR_(cudaMemcpyAsync(d_st_, h_st_, sizeof(FState), cudaMemcpyHostToDevice, stream_), -1);
+  if (mp) {
+    for (int c = 0; c < ncomp_; c++) h_stc_[c] = init;
+    CKR_(cudaMemcpyAsync(d_stc_, h_stc_, ncomp_ * sizeof(FState), cudaMemcpyHostToDevice, stream_), -1);
+  }
   // prologue: x0 = sol, x = 0, r = rhs - A x0, rhat = r, |r0|, rho
   k_pro_copy<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, vec_[kSOL], vec_[kX0], vec_[kX]);
-  if (tt_.ndim == 2)
-    k_op_red<2, 2, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_opP_,
-                                                      d_opS_, d_st_, d_part_, d_cnt_);
-  else
-    k_op_red<3, 2, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kX0], vec_[kR], vec_[kRHS], d_opP_,
-                                                      d_opS_, d_st_, d_part_, d_cnt_);
+  double *PART = mp ? d_cpart_ : d_part_;
+  unsigned *CNT = mp ? d_ccnt_ : d_cnt_;
+  if (tt_.ndim == 2) {
+    if (mp)
+      k_op_red<2, 2, double, true><<<gr, kTPB, 0, stream_>>>(topo_, c64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
+                                                             d_opP_, d_opS_, ST, PART, CNT);
+    else
+      k_op_red<2, 2, double, false><<<gr, kTPB, 0, stream_>>>(topo_, c64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
+                                                              d_opP_, d_opS_, ST, PART, CNT);
+  } else {
+    if (mp)
+      k_op_red<3, 2, double, true><<<gr, kTPB, 0, stream_>>>(topo_, c64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
+                                                             d_opP_, d_opS_, ST, PART, CNT);
+    else
+      k_op_red<3, 2, double, false><<<gr, kTPB, 0, stream_>>>(topo_, c64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
+                                                              d_opP_, d_opS_, ST, PART, CNT);
+  }
   vcopy(TL, vec_[kRHAT], vec_[kR]);
+  if (mp) k_set_cond_multi<<<1, 256, 0, stream_>>>(0, d_stc_, ncomp_, d_st_);
   if (prm_.max_iter > 0) {
     if (prm_.graph) {
       CKR_(cudaGraphLaunch(graph_exec_, stream_), -1);
@@ -1464,10 +1610,13 @@ int MacGpu::enqueue_solve() {
       // the captured iteration's kernels, launched directly; the host reads
       // the convergence flag after every iteration
       for (int it = 0; it < prm_.max_iter; it++) {
+        solve_lists_ = true;
         if (prm_.precision == 1)
           iteration_device<float>(d_resid32_, d_corr32_, c32_);
         else
           iteration_device<double>(vec_[kRESID], vec_[kCORR], c64_);
+        solve_lists_ = false;
+        if (mp) k_set_cond_multi<<<1, 256, 0, stream_>>>(0, d_stc_, ncomp_, d_st_);
         if (record_) {  // a collection solve keeps every iterate
           double *cp = nullptr;
           const size_t n = (size_t)tt_.num_blocks * ncell_;
@@ -1484,7 +1633,11 @@ int MacGpu::enqueue_solve() {
       }
     }
   }
-  k_finish<<<ew_grid(w), kTPB, 0, stream_>>>(TL, ncell_, d_st_, vec_[kX0], vec_[kX], vec_[kSOL]);
+  if (mp)
+    k_finish<true><<<ge, kTPB, 0, stream_>>>(TL, ncell_, ch, ST, vec_[kX0], vec_[kX], vec_[kSOL]);
+  else
+    k_finish<false><<<ge, kTPB, 0, stream_>>>(TL, ncell_, ch, ST, vec_[kX0], vec_[kX], vec_[kSOL]);
+  last_multi_ = mp;
   return err_.empty() ? 0 : -1;
 }
 
@@ -1546,6 +1699,30 @@ int MacGpu::solve_state(SolveInfo *info) {
     fail("bulk-copy smoother: an mbarrier wait timed out");
     return -1;
   }
+  if (last_multi_) {
+    // one state per problem: the largest iteration count and initial
+    // residual, rnorm / rnorm0 = the largest relative residual; breakdown if
+    // any problem broke down, not converged if any did not converge
+    CKR_(cudaMemcpy(h_stc_, d_stc_, ncomp_ * sizeof(FState), cudaMemcpyDeviceToHost), -1);
+    int its = 0, stat = 0, unconv = 0, nnoff = 0;
+    double r0 = 0.0, rel = 0.0;
+    for (int c = 0; c < ncomp_; c++) {
+      const FState &q = h_stc_[c];
+      its = std::max(its, q.trivial ? 0 : q.iter);
+      stat |= q.stat;
+      unconv |= !(q.conv || q.trivial);
+      nnoff |= q.nn_off;
+      r0 = std::max(r0, q.rnorm0);
+      if (q.rnorm0 > 0) rel = std::max(rel, q.rnorm / q.rnorm0);
+      if (q.rnorm != q.rnorm) rel = q.rnorm;
+    }
+    info->iterations = its;
+    info->rnorm0 = r0;
+    info->rnorm = rel * r0;
+    info->status = stat ? 1 : (unconv ? 2 : (nnoff ? 3 : 0));
+    info->seconds = 0;
+    return 0;
+  }
   const FState &st = *h_st_;
   info->iterations = st.trivial ? 0 : st.iter;
   info->rnorm0 = st.rnorm0;
@@ -1553,6 +1730,17 @@ int MacGpu::solve_state(SolveInfo *info) {
   info->status = st.stat ? 1 : ((st.conv || st.trivial) ? (st.nn_off ? 3 : 0) : 2);
   info->seconds = 0;
   return 0;
+}
+
+int MacGpu::problem_states(int *iterations, double *rel_resid, int n) {
+  if (!last_multi_) return -1;
+  CKR_(cudaMemcpy(h_stc_, d_stc_, ncomp_ * sizeof(FState), cudaMemcpyDeviceToHost), -1);
+  for (int c = 0; c < ncomp_ && c < n; c++) {
+    const FState &q = h_stc_[c];
+    if (iterations) iterations[c] = q.trivial ? 0 : q.iter;
+    if (rel_resid) rel_resid[c] = q.rnorm0 > 0 ? q.rnorm / q.rnorm0 : 0.0;
+  }
+  return ncomp_;
 }
 
 int MacGpu::tower_size(int L, int sublevel) const {
@@ -1580,11 +1768,13 @@ int MacGpu::enqueue_kernel(int which, int L) {
     const long w = (long)TL.n * ncell_;
     CKR_(cudaMemsetAsync(d_st_, 0, sizeof(FState), stream_), -1);
     if (tt_.ndim == 2)
-      k_op_red<2, 0, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kSOL], vec_[kV], vec_[kRHAT], d_opP_,
-                                                        d_opS_, d_st_, d_part_, d_cnt_);
+      k_op_red<2, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, Chunks{}, vec_[kSOL], vec_[kV],
+                                                                      vec_[kRHAT], d_opP_, d_opS_, d_st_, d_part_,
+                                                                      d_cnt_);
     else
-      k_op_red<3, 0, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kSOL], vec_[kV], vec_[kRHAT], d_opP_,
-                                                        d_opS_, d_st_, d_part_, d_cnt_);
+      k_op_red<3, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, Chunks{}, vec_[kSOL], vec_[kV],
+                                                                      vec_[kRHAT], d_opP_, d_opS_, d_st_, d_part_,
+                                                                      d_cnt_);
   } else {
     return -1;
   }
@@ -1613,11 +1803,13 @@ int MacGpu::device_kernel_compact(int which, int L, int variant, const double *i
     CKR_(cudaMemsetAsync(vec_[kRHAT], 0, n * sizeof(double), stream_), 2);
     CKR_(cudaMemsetAsync(d_st_, 0, sizeof(FState), stream_), 2);
     if (tt_.ndim == 2)
-      k_op_red<2, 0, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kTMP], vec_[kV], vec_[kRHAT],
-                                                                d_opP_, d_opS_, d_st_, d_part_, d_cnt_);
+      k_op_red<2, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, Chunks{}, vec_[kTMP],
+                                                                      vec_[kV], vec_[kRHAT], d_opP_, d_opS_, d_st_,
+                                                                      d_part_, d_cnt_);
     else
-      k_op_red<3, 0, double><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, vec_[kTMP], vec_[kV], vec_[kRHAT],
-                                                                d_opP_, d_opS_, d_st_, d_part_, d_cnt_);
+      k_op_red<3, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, Chunks{}, vec_[kTMP],
+                                                                      vec_[kV], vec_[kRHAT], d_opP_, d_opS_, d_st_,
+                                                                      d_part_, d_cnt_);
     CKR_(cudaGetLastError(), 2);
     CKR_(cudaMemcpyAsync(out, vec_[kV], n * sizeof(double), cudaMemcpyDeviceToHost, stream_), 2);
   } else if (which == 2) {

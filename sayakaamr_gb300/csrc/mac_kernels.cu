@@ -43,6 +43,7 @@ __global__ void __launch_bounds__(kThreads) k_apply(Topo t, Coef<T> c, BlockList
     const int p = (int)(it / ncell);
     const int ci = (int)(it - (long)p * ncell);
     const int b = L.blocks[p];
+    if (block_off(L, b)) continue;
     const long q = (long)b * ncell + ci;
     T out = apply_cell<T, ND>(t, c, b, L.ftypes[p], ci, x);
     if (rhs) out = c.vf[q] > 0 ? rhs[q] - out : (T)0;
@@ -84,6 +85,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs(Topo t, Coef<T> c, Bloc
   color_cell_fast<ND>(h, t, color, ijk);
   for (int p = blockIdx.y; p < L.n; p += gridDim.y) {
     const long fo = (long)p * t.ncell;
+    if (L.stc && block_off(L, L.hx ? L.hx[(long)p * kHX + kHXBlock] : L.blocks[p])) continue;
     if (L.hx) {
       const int *e = L.hx + (long)p * kHX;
       smooth_cell_fast<T, ND>(t, c, e[kHXBlock], (uint16_t)(e[kHXInfo] & 0xffff), ijk, phi, rhs,
@@ -108,6 +110,7 @@ __global__ void __launch_bounds__(kThreads) k_restrict(Topo t, Coef<T> c, BlockL
   const long total = (long)L.n * ncell;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int p = (int)(it / ncell);
+    if (block_off(L, L.blocks[p])) continue;
     restrict_cell<T, ND>(t, c, L.blocks[p], (int)(it - (long)p * ncell), phi, L.links ? L.links + (long)p * 8 : nullptr);
   }
 }
@@ -122,6 +125,7 @@ __global__ void __launch_bounds__(kThreads) k_prolong(Topo t, Coef<T> c, BlockLi
   const long total = (long)L.n * ncell;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int p = (int)(it / ncell);
+    if (block_off(L, L.blocks[p])) continue;
     prolong_cell<T, ND>(t, c, L.blocks[p], (int)(it - (long)p * ncell), phi, L.links ? L.links[p] : -1);
   }
 }
@@ -334,6 +338,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
   for (int p = blockIdx.x; p < L.n; p += gridDim.x) {
     const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
     const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
+    if (block_off(L, b)) continue;  // uniform over the CTA
     const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
     const long cb = (long)b * ncell;
     const long fb = (long)b * t.nfb;
@@ -492,6 +497,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_bhgs(Topo t, Coef<T> c, Bloc
   for (int p = blockIdx.x; p < L.n; p += gridDim.x) {
     const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
     const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
+    if (block_off(L, b)) continue;  // uniform over the CTA
     const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
     const long cb = (long)b * ncell;
     const long fb = (long)b * t.nfb;
@@ -600,6 +606,7 @@ __global__ void __launch_bounds__(kThreads) k_copy_blocks(BlockList L, int ncell
   const long total = (long)L.n * ncell;
   for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
     const int p = (int)(it / ncell);
+    if (block_off(L, L.blocks[p])) continue;
     const long q = (long)L.blocks[p] * ncell + (it - (long)p * ncell);
     dst[q] = src[q];
   }
@@ -1013,6 +1020,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
       const int px = p - L.n;
       const long fo = (long)px * ncell;
       const int *e = X.hx + (long)px * kHX;
+      if (block_off(X, e[kHXBlock])) continue;
       for (int h = threadIdx.x; h < nhalf; h += blockDim.x) {
         int ijk[3];
         color_cell_fast<ND>(h, t, 0, ijk);
@@ -1023,6 +1031,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
     }
     const int *hxe = L.hx ? L.hx + (long)p * kHX : nullptr;
     const int b = hxe ? hxe[kHXBlock] : L.blocks[p];
+    if (block_off(L, b)) continue;  // uniform over the CTA
     const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
     const long cb = (long)b * ncell;
     const long fb = (long)b * t.nfb;
@@ -1185,6 +1194,7 @@ void launch_rbgs(const Topo &t, const Coef<T> &c, const BlockList &L, int color,
   const size_t tile = t.ndim == 2 ? rbgs_tile_smem<T, 2>(t) : rbgs_tile_smem<T, 3>(t);
   if (variant >= 5 && tile > 200 * 1024) variant = 3;
   const bool aligned = (t.ncell * sizeof(T)) % 16 == 0 && (t.nfb * sizeof(T)) % 16 == 0;
+  if (L.stc && variant >= 8) variant = 7;  // the bulk-copy variants know no per-problem states
   if (variant == 8) {
     const size_t bulk = t.ndim == 2 ? rbgs_bulk_smem<T, 2>(t) : rbgs_bulk_smem<T, 3>(t);
     if (bulk > 200 * 1024 || !aligned) variant = 7;

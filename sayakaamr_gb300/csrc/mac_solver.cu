@@ -4,6 +4,7 @@
 #include "mac_solver.h"
 
 #include <algorithm>
+#include <functional>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -283,6 +284,90 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
       CK(cudaMemcpy(dt.par.hx, hx.data(), hx.size() * sizeof(int), cudaMemcpyHostToDevice));
     }
   }
+  // Independent problems in one tree (a forest: no neighbour, parent or child
+  // link between them) each get their own BiCGSTAB state.  Components are
+  // numbered in the order of their lowest block id.
+  {
+    std::vector<int> up(nbk);
+    for (int b = 0; b < nbk; b++) up[b] = b;
+    std::function<int(int)> root = [&](int b) {
+      while (up[b] != b) b = up[b] = up[up[b]];
+      return b;
+    };
+    auto join = [&](int a, int b) {
+      if (b < 0 || b >= nbk) return;
+      a = root(a);
+      b = root(b);
+      if (a != b) up[std::max(a, b)] = std::min(a, b);
+    };
+    for (int b = 0; b < nbk; b++) {
+      for (int f = 0; f < 2 * nd; f++) join(b, tt.neighbor[b * 6 + f]);
+      join(b, tt.parent[b]);
+    }
+    comp_of_block_.assign(nbk, 0);
+    std::vector<int> id(nbk, -1);
+    ncomp_ = 0;
+    for (int b = 0; b < nbk; b++) {
+      const int r = root(b);
+      if (id[r] < 0) id[r] = ncomp_++;
+      comp_of_block_[b] = id[r];
+    }
+  }
+  if (ncomp_ > 1 && towers_[finest_].all.n > 0) {
+    // the finest tower problem by problem, and its chunks (see Chunks)
+    const DevTower &ft = towers_[finest_];
+    const int n = ft.all.n;
+    std::vector<int> perm(n);
+    for (int p = 0; p < n; p++) perm[p] = p;
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) {
+      return comp_of_block_[ft.blocks[a]] < comp_of_block_[ft.blocks[b]];
+    });
+    std::vector<uint16_t> ftypes(n);
+    CK(cudaMemcpy(ftypes.data(), ft.all.ftypes, n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+    std::vector<int> pb(n);
+    std::vector<uint16_t> pf(n);
+    for (int p = 0; p < n; p++) {
+      pb[p] = ft.blocks[perm[p]];
+      pf[p] = ftypes[perm[p]];
+    }
+    tlc_.n = n;
+    tlc_.blocks = dalloc<int>(n);
+    tlc_.ftypes = dalloc<uint16_t>(n);
+    tlc_.hx = dalloc<int>((size_t)n * kHX);
+    CK(cudaMemcpy(tlc_.blocks, pb.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(tlc_.ftypes, pf.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    const std::vector<int> hx = make_hx(pb, pf);
+    CK(cudaMemcpy(tlc_.hx, hx.data(), hx.size() * sizeof(int), cudaMemcpyHostToDevice));
+    std::vector<int> ccomp, cbeg, cend, c0(ncomp_, 0), cn(ncomp_, 0);
+    const long nc = ncell_;
+    for (int p = 0; p < n;) {
+      const int c = comp_of_block_[pb[p]];
+      int q = p;
+      while (q < n && comp_of_block_[pb[q]] == c) q++;
+      c0[c] = (int)ccomp.size();
+      for (long a = (long)p * nc; a < (long)q * nc; a += kChunkCells) {
+        ccomp.push_back(c);
+        cbeg.push_back((int)a);
+        cend.push_back((int)std::min<long>(a + kChunkCells, (long)q * nc));
+      }
+      cn[c] = (int)ccomp.size() - c0[c];
+      p = q;
+    }
+    nchunks_ = (int)ccomp.size();
+    std::vector<int> all;
+    for (auto *v : {&ccomp, &cbeg, &cend}) all.insert(all.end(), v->begin(), v->end());
+    all.insert(all.end(), c0.begin(), c0.end());
+    all.insert(all.end(), cn.begin(), cn.end());
+    d_chunk_ = dalloc<int>(all.size());
+    CK(cudaMemcpy(d_chunk_, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
+    d_comp_ = dalloc<int>(nbk);
+    CK(cudaMemcpy(d_comp_, comp_of_block_.data(), nbk * sizeof(int), cudaMemcpyHostToDevice));
+    d_stc_ = dalloc<FState>(ncomp_);
+    d_cpart_ = dalloc<double>((size_t)nchunks_ * 2);
+    d_ccnt_ = dalloc<unsigned>(ncomp_);
+    CK(cudaMemset(d_ccnt_, 0, ncomp_ * sizeof(unsigned)));
+    CK(cudaMallocHost(&h_stc_, ncomp_ * sizeof(FState)));
+  }
   levels_.resize(tt.max_level + 1);
   nonleaf_.resize(tt.max_level + 1);
   level_blocks_.resize(tt.max_level + 1);
@@ -416,6 +501,15 @@ MacGpu::~MacGpu() {
   fr(d_corr32_);
   fr(d_corr32b_);
   fr(d_corr64b_);
+  fr(tlc_.blocks);
+  fr(tlc_.ftypes);
+  fr(tlc_.hx);
+  fr(d_chunk_);
+  fr(d_comp_);
+  fr(d_stc_);
+  fr(d_cpart_);
+  fr(d_ccnt_);
+  if (h_stc_) cudaFreeHost(h_stc_);
   fr(d_st_);
   fr(d_part_);
   fr(d_opP_);
@@ -441,6 +535,14 @@ BlockList MacGpu::tower_list(int L) const {
   const DevTower &t = towers_[L];
   BlockList r{t.all.blocks, t.all.ftypes, t.all.n};
   r.hx = t.all.hx;
+  return attach(r);
+}
+// lists built while a solve is recorded carry the per-problem states
+BlockList MacGpu::attach(BlockList r) const {
+  if (solve_lists_ && multi()) {
+    r.comp = d_comp_;
+    r.stc = d_stc_;
+  }
   return r;
 }
 BlockList MacGpu::sublevel_list(int L, int l) const {
@@ -453,7 +555,7 @@ BlockList MacGpu::sublevel_list(int L, int l) const {
     r.sa = d_sfac_[L] + (long)b * ncell_;
     r.ia = d_sfac_[L] + w + (long)b * ncell_;
   }
-  return r;
+  return attach(r);
 }
 BlockList MacGpu::smooth_list(int L) const {
   BlockList r = tower_list(L);
@@ -474,17 +576,17 @@ BlockList MacGpu::parity_list(int L, int g, bool skip_top) const {
     r.sa = d_pfac_[L] + (long)b * ncell_;
     r.ia = d_pfac_[L] + w + (long)b * ncell_;
   }
-  return r;
+  return attach(r);
 }
 BlockList MacGpu::level_list(int l) const {
   BlockList r{levels_[l].blocks, nullptr, levels_[l].n};
   r.links = levels_[l].links;
-  return r;
+  return attach(r);
 }
 BlockList MacGpu::nonleaf_list(int l) const {
   BlockList r{nonleaf_[l].blocks, nullptr, nonleaf_[l].n};
   r.links = nonleaf_[l].links;
-  return r;
+  return attach(r);
 }
 
 // ---------------------------------------------------------------------------

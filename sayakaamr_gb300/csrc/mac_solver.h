@@ -47,6 +47,9 @@ struct SolverParams {
                               // per colour); 1 = block-hybrid passes (n_post per tower, each one launch of
                               // inner_sweeps red-black sweeps per block, Jacobi between blocks)
   int inner_sweeps = 2;       // smoother 1: red-black sweeps per block in one pass
+  int per_problem = 1;        // device path, a tree of several independent problems (connected components):
+                              // 1 = one BiCGSTAB state per problem, each stopping at its own tolerance;
+                              // 0 = one state shared by all
 };
 
 struct SolveInfo {
@@ -106,6 +109,12 @@ class MacGpu {
   int tower_size(int L, int sublevel) const;
   int tuned_smoother(int precision, float *us, int n) const;
   int bottom_level() const { return bottom_ready_ ? bot_level_ : -1; }
+  // number of independent problems (connected components) of the tree
+  int problems() const { return ncomp_; }
+  // per-problem outcome of the last device solve (one state per problem):
+  // iterations and final relative residual |r|/|r0|; returns the problem
+  // count, or -1 when the last solve shared one state
+  int problem_states(int *iterations, double *rel_resid, int n);
   int device() const { return device_; }
 
   // building blocks, exposed for parity tests (compact arrays, all blocks)
@@ -286,6 +295,21 @@ class MacGpu {
   }
   // tower L with its FP64 smoother factors, every sublevel (block-hybrid passes)
   BlockList smooth_list(int L) const;
+  // independent problems of a forest (connected components of the tree)
+  // with one BiCGSTAB state each (prm_.per_problem): the finest tower listed
+  // problem by problem, its chunks, the states and the reduction scratch
+  int ncomp_ = 1;
+  std::vector<int> comp_of_block_;
+  int *d_comp_ = nullptr;
+  DevList tlc_;
+  int *d_chunk_ = nullptr;  // [comp | beg | end] per chunk, then [first chunk | chunks] per problem
+  int nchunks_ = 0;
+  FState *d_stc_ = nullptr, *h_stc_ = nullptr;
+  double *d_cpart_ = nullptr;
+  unsigned *d_ccnt_ = nullptr;
+  bool solve_lists_ = false;  // block lists carry the states (set while a solve is recorded)
+  bool multi() const { return ncomp_ > 1 && prm_.per_problem != 0 && d_stc_ != nullptr; }
+  BlockList attach(BlockList r) const;
   Coef<float> c32_{};
   FState *d_st_ = nullptr, *h_st_ = nullptr;
   double *d_part_ = nullptr;
@@ -323,7 +347,9 @@ class MacGpu {
   int graph_prec_ = -1, graph_npost_ = -1;
   int kernels_per_iter_ = 0;
   int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1, graph_nn_ = -1, graph_order_ = -1;
-  int graph_smoother_ = -1, graph_inner_ = -1;
+  int graph_smoother_ = -1, graph_inner_ = -1, graph_multi_ = -1;
+  bool last_multi_ = false;  // the last device solve kept one state per problem
+  Chunks chunks() const;
   bool graph_stale() const;
   int rbgs_variant_[2] = {-1, -1};  // tuned smoother variant per precision (0 FP64, 1 FP32)
   float rbgs_us_[2][16] = {};       // measured microseconds per variant (kRbgsVariants <= 16)

@@ -424,6 +424,8 @@ __device__ __forceinline__ void bottom_gather(const BottomDev &bd, int r0, int m
 template <typename T, bool CG = false>
 __device__ __forceinline__ void bottom_tile(const BottomDev &bd, int tile, const T *resid, T *corr, double *rv) {
   const int c = bd.tile_comp[tile], r0 = bd.comp_row0[c], m = bd.comp_n[c], nc = bd.ncell;
+  // a finished problem of a forest (per-problem states): nothing to solve
+  if (bd.stc && bd.stc[bd.comp[bd.blocks[r0 / nc]]].done) return;
   if (sizeof(T) == 4 && bd.binv16) {  // FP16 rows with FP32 scales, FP32 accumulation
     float *rf = reinterpret_cast<float *>(rv);
     bottom_gather<T, CG>(bd, r0, m, resid, rf);

@@ -34,7 +34,8 @@ def test_hybrid_pass_solves_each_block_with_frozen_neighbours(name):
         w = phi.copy()
         w[sl] = out[sl]
         r = S.residual(L, w, rhs)[sl]
-        assert np.abs(r).max() < BLOCK_RTOL * np.abs(r_in[sl]).max(), (b, np.abs(r).max(), np.abs(r_in[sl]).max())
+        # (<=: an all-solid block has no equations, its residual is 0 before and after)
+        assert np.abs(r).max() <= BLOCK_RTOL * np.abs(r_in[sl]).max(), (b, np.abs(r).max(), np.abs(r_in[sl]).max())
     # cells outside the tower keep their input values
     mask = np.ones(n, dtype=bool)
     mask[blocks] = False
