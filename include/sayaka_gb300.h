@@ -194,6 +194,17 @@ int sayaka_mac_get_sol_compact(sayaka_mac *h, double *cells, int32_t on_device);
 int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p);
 /* cg_solve (src/SayakaMacSolver.cpp:455-680): BiCGSTAB on the finest tower */
 int sayaka_mac_cg_solve(sayaka_mac *h, sayaka_solve_info *info);
+/* mg_solve (src/SayakaMacSolver.cpp:43-162): stand-alone V-cycles on the
+ * finest tower (reference arithmetic, bottom BiCGSTAB with bot_tol_*), SOL
+ * updated in place from its current value, until |r|_inf < |r0|_inf tol_rel +
+ * tol_abs or max_iter; SAYAKA_NOT_CONVERGED when the tolerance is not met,
+ * SAYAKA_BREAKDOWN when the bottom solve breaks down (the reference exits).
+ * The reference runs its preconditioner's fixed V-cycle count instead of
+ * max_iter after a preconditioned cg_solve; this one always follows max_iter. */
+int sayaka_mac_mg_solve(sayaka_mac *h, sayaka_solve_info *info);
+/* relax_solve (src/SayakaMacSolver.cpp:377-452): red-black Gauss-Seidel
+ * sweeps of the finest tower (mg_smooth_level) on SOL, same stopping test */
+int sayaka_mac_relax_solve(sayaka_mac *h, sayaka_solve_info *info);
 
 /* Device-resident solve path (params.bottom = 1, use_mg_precond = 1):
  * build the FP32 coefficient copies, the dense level-1 inverse and the CUDA

@@ -937,6 +937,86 @@ int orc_cg_solve(const orc_problem *P, const orc_params *prm, const double *rhs,
   return st;
 }
 
+/* mg_solve (src/SayakaMacSolver.cpp:43-162): stand-alone V-cycles on the
+ * finest tower.  RESID = RHS - L(SOL); every iteration clears CORR, restricts
+ * RESID down to level 1, solves the bottom, prolongs and post-smooths up,
+ * adds CORR to SOL and recomputes RESID and its L-inf norm; stops when
+ * |r| < |r0| tol_rel + tol_abs or after max_iter iterations.  sol holds the
+ * initial guess.  Returns 1 when the bottom solve breaks down (the reference
+ * exits), else 0; info->status 2 when it did not converge. */
+int orc_mg_solve(const orc_problem *P, const orc_params *prm, const double *rhs, double *sol, orc_info *info) {
+  solver_t s;
+  solver_init(&s, P, prm);
+  ctx_t *c = &s.c;
+  const int L = c->finest;
+  to_grown(c, rhs, s.v[B_RHS]);
+  to_grown(c, sol, s.v[B_SOL]);
+  g_residual(c, L, s.v[B_RESID], s.v[B_SOL], s.v[B_RHS], &s.R);
+  const double r0 = t_norm(c, L, s.v[B_RESID]);
+  double rn = r0;
+  int it = 0, conv = 0, st = 0;
+  for (it = 1; it <= prm->max_iter; it++) {
+    memset(s.v[B_CORR], 0, sizeof(double) * (size_t)c->nblk * c->gcell);
+    for (int l = L; l >= 2; l--) g_restrict(c, l - 1, s.v[B_RESID], s.v[B_TMP]);
+    if (bottom_solve(&s) != 0) {
+      st = 1;
+      break;
+    }
+    for (int l = 2; l <= L; l++) {
+      g_prolong(c, l, s.v[B_CORR]);
+      for (int k = 0; k < prm->n_post; k++) g_smooth(c, l, s.v[B_CORR], s.v[B_RESID], &s.R);
+    }
+    t_axpby(c, L, s.v[B_SOL], 1.0, s.v[B_SOL], 1.0, s.v[B_CORR]);
+    g_residual(c, L, s.v[B_RESID], s.v[B_SOL], s.v[B_RHS], &s.R);
+    rn = t_norm(c, L, s.v[B_RESID]);
+    if (rn < r0 * prm->tol_rel + prm->tol_abs) {
+      conv = 1;
+      break;
+    }
+  }
+  if (it > prm->max_iter) it = prm->max_iter;
+  from_grown(c, s.v[B_SOL], sol);
+  info->status = st ? 1 : (conv ? 0 : 2);
+  info->iterations = it;
+  info->rnorm0 = r0;
+  info->rnorm = rn;
+  solver_free(&s);
+  return st;
+}
+
+/* relax_solve (src/SayakaMacSolver.cpp:377-452): red-black Gauss-Seidel
+ * sweeps of the finest tower on SOL with RHS (mg_smooth_level), the residual's
+ * L-inf norm after each, until |r| < |r0| tol_rel + tol_abs or max_iter */
+int orc_relax_solve(const orc_problem *P, const orc_params *prm, const double *rhs, double *sol, orc_info *info) {
+  solver_t s;
+  solver_init(&s, P, prm);
+  ctx_t *c = &s.c;
+  const int L = c->finest;
+  to_grown(c, rhs, s.v[B_RHS]);
+  to_grown(c, sol, s.v[B_SOL]);
+  g_residual(c, L, s.v[B_RESID], s.v[B_SOL], s.v[B_RHS], &s.R);
+  const double r0 = t_norm(c, L, s.v[B_RESID]);
+  double rn = r0;
+  int it = 0, conv = 0;
+  for (it = 1; it <= prm->max_iter; it++) {
+    g_smooth(c, L, s.v[B_SOL], s.v[B_RHS], &s.R);
+    g_residual(c, L, s.v[B_RESID], s.v[B_SOL], s.v[B_RHS], &s.R);
+    rn = t_norm(c, L, s.v[B_RESID]);
+    if (rn < r0 * prm->tol_rel + prm->tol_abs) {
+      conv = 1;
+      break;
+    }
+  }
+  if (it > prm->max_iter) it = prm->max_iter;
+  from_grown(c, s.v[B_SOL], sol);
+  info->status = conv ? 0 : 2;
+  info->iterations = it;
+  info->rnorm0 = r0;
+  info->rnorm = rn;
+  solver_free(&s);
+  return 0;
+}
+
 /* tower block list, begin/end and face types (for table checks) */
 int orc_tower(const orc_problem *P, int L, int32_t *blocks, int32_t *n, int32_t *begin_end, int32_t *ftypes) {
   ctx_t c;

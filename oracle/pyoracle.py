@@ -171,6 +171,21 @@ class Oracle:
                               C.byref(info))
         return sol, dict(status=info.status, iterations=info.iterations, rnorm0=info.rnorm0, rnorm=info.rnorm)
 
+    def mg_solve(self, rhs, prm=None, sol0=None):
+        """mg_solve: stand-alone V-cycle iterations (src/SayakaMacSolver.cpp:43-162)"""
+        return self._solve(self.lib.orc_mg_solve, rhs, prm, sol0)
+
+    def relax_solve(self, rhs, prm=None, sol0=None):
+        """relax_solve: Gauss-Seidel sweeps of the finest tower (src/SayakaMacSolver.cpp:377-452)"""
+        return self._solve(self.lib.orc_relax_solve, rhs, prm, sol0)
+
+    def _solve(self, fn, rhs, prm, sol0):
+        prm = prm or params()
+        sol = np.zeros(self.n * self.ncell) if sol0 is None else np.array(sol0, dtype=np.float64)
+        info = _Info()
+        fn(C.byref(self.P), C.byref(prm), self._in(rhs), sol.ctypes.data_as(_f64p), C.byref(info))
+        return sol, dict(status=info.status, iterations=info.iterations, rnorm0=info.rnorm0, rnorm=info.rnorm)
+
     def tower(self, L):
         blocks = np.zeros(self.n, dtype=np.int32)
         n = C.c_int32()

@@ -391,6 +391,9 @@ static bool dump_tower(int L, int finest) {
 	return NDIM == 2 || L == 1 || L >= finest - 1;
 }
 
+// iterations of the mg_solve / relax_solve dumps (tests/golden_io.py: MG_ITERS, RELAX_ITERS)
+static const int kMgIters = 6, kRelaxIters = 25;
+
 // ---------------------------------------------------------------------------
 static void run_case(const Case &c, const char *outdir, int cap) {
 	std::string path = std::string(outdir) + "/" + c.name + ".bin";
@@ -683,6 +686,28 @@ static void run_case(const Case &c, const char *outdir, int cap) {
 		D.scalar_d("sv_true_resid_inf", rn);
 		D.scalar_d("sv_rhs_inf", bn);
 		fprintf(stderr, "[%s] solve stat=%d |r|inf=%.3e |b|inf=%.3e\n", c.name.c_str(), stat, rn, bn);
+		// the other two solvers of the public API on the same problem, a fixed
+		// number of iterations each (the relative tolerance is out of reach)
+		if (c.do_ops && !all_neumann) {
+			std::unique_ptr<TreeData> rd(TreeData::CreateCellData(tree, 1, 1));
+			set_cell(*rd, 0, ALL, f);
+			S->setRhs(*rd, 0);
+			S->setZeroSol();
+			S->setTolerance(1e-30, 0.0);
+			S->setMaxIteration(kMgIters);
+			S->setVerbose(0);
+			// the preconditioned cg_solve above left the fixed V-cycle count
+			// of the preconditioner (1) set, which mg_solve would obey
+			S->setMGFixedIter(0);
+			S->mg_solve();
+			S->getSol(*ud, 0);
+			D.f64("mg_sol", get_cell(*ud, 0, LEAF));
+			S->setZeroSol();
+			S->setMaxIteration(kRelaxIters);
+			S->relax_solve();
+			S->getSol(*ud, 0);
+			D.f64("rx_sol", get_cell(*ud, 0, LEAF));
+		}
 	}
 }
 

@@ -86,6 +86,8 @@ SIGNATURES = {
     "sayaka_mac_get_sol_compact": (C.c_int, [_V, _V, C.c_int32]),
     "sayaka_mac_set_params": (C.c_int, [_V, C.POINTER(Params)]),
     "sayaka_mac_cg_solve": (C.c_int, [_V, C.POINTER(SolveInfo)]),
+    "sayaka_mac_mg_solve": (C.c_int, [_V, C.POINTER(SolveInfo)]),
+    "sayaka_mac_relax_solve": (C.c_int, [_V, C.POINTER(SolveInfo)]),
     "sayaka_mac_prepare": (C.c_int, [_V]),
     "sayaka_mac_cg_solve_async": (C.c_int, [_V]),
     "sayaka_mac_solve_info": (C.c_int, [_V, C.POINTER(SolveInfo)]),
@@ -385,6 +387,22 @@ class MacSolver:
         out = np.zeros(self.num_blocks * self.ncell)
         _check(self.lib.sayaka_mac_get_sol_compact(self.h, C.c_void_p(out.ctypes.data), 0), "get_sol", self.h)
         return out
+
+    def mg_solve(self):
+        """stand-alone V-cycles (MacSolver::mg_solve)"""
+        return self._solve(self.lib.sayaka_mac_mg_solve, "mg_solve")
+
+    def relax_solve(self):
+        """Gauss-Seidel sweeps of the finest tower (MacSolver::relax_solve)"""
+        return self._solve(self.lib.sayaka_mac_relax_solve, "relax_solve")
+
+    def _solve(self, fn, what):
+        info = SolveInfo()
+        rc = fn(self.h, C.byref(info))
+        if rc not in (OK, BREAKDOWN, NOT_CONVERGED):
+            _check(rc, what, self.h)
+        return dict(status=info.status, iterations=info.iterations, rnorm0=info.rnorm0, rnorm=info.rnorm,
+                    seconds=info.seconds, rc=rc)
 
     def cg_solve(self):
         info = SolveInfo()

@@ -651,6 +651,25 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
   });
 }
 
+static int solve_with(sayaka_mac *h, sayaka_solve_info *info, int (MacGpu::*fn)(SolveInfo *)) {
+  return guarded(h, [&] {
+    SolveInfo si;
+    const int st = (h->gpu.get()->*fn)(&si);
+    if (info) {
+      info->status = si.status;
+      info->iterations = si.iterations;
+      info->rnorm0 = si.rnorm0;
+      info->rnorm = si.rnorm;
+      info->seconds = si.seconds;
+    }
+    if (st < 0) return (int)SAYAKA_CUDA_ERROR;
+    return si.status == 0 ? (int)SAYAKA_OK : (si.status == 1 ? (int)SAYAKA_BREAKDOWN : (int)SAYAKA_NOT_CONVERGED);
+  });
+}
+int sayaka_mac_mg_solve(sayaka_mac *h, sayaka_solve_info *info) { return solve_with(h, info, &MacGpu::mg_solve); }
+int sayaka_mac_relax_solve(sayaka_mac *h, sayaka_solve_info *info) {
+  return solve_with(h, info, &MacGpu::relax_solve);
+}
 int sayaka_mac_cg_solve(sayaka_mac *h, sayaka_solve_info *info) {
   return guarded(h, [&] {
     SolveInfo si;

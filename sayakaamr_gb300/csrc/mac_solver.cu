@@ -1054,6 +1054,85 @@ int MacGpu::cg_solve(SolveInfo *info) {
   return stat;
 }
 
+// mg_solve (src/SayakaMacSolver.cpp:43-162): stand-alone V-cycles on the
+// finest tower with the reference's arithmetic (host-driven, the bottom by
+// BiCGSTAB with the bottom tolerances): RESID = RHS - L(SOL), then per
+// iteration CORR = 0, restriction of RESID to level 1, bottom solve,
+// prolongation and post-smoothing up, SOL += CORR, RESID and its L-inf norm,
+// until |r| < |r0| tol_rel + tol_abs or max_iter.  The reference exits on a
+// bottom breakdown (status BREAKDOWN here) and runs its preconditioner's
+// fixed V-cycle count instead of max_iter once a preconditioned cg_solve set
+// it; this entry point always follows max_iter and the tolerance.
+int MacGpu::mg_solve(SolveInfo *info) {
+  auto t0 = std::chrono::steady_clock::now();
+  const int L = finest_;
+  const BlockList TL = tower_list(L);
+  const size_t n = (size_t)tt_.num_blocks * ncell_;
+  double *SOL = vec_[kSOL], *RHS = vec_[kRHS], *RES = vec_[kRESID], *COR = vec_[kCORR];
+  mg_apply(L, RES, SOL, RHS);
+  const double r0 = vnorm(TL, RES);
+  double rn = r0;
+  int it = 0, conv = 0, stat = 0;
+  for (it = 1; it <= prm_.max_iter && err_.empty(); it++) {
+    CKR(cudaMemsetAsync(COR, 0, n * sizeof(double), stream_), -1);
+    for (int l = L; l >= 2; l--) mg_restrict(l - 1, RES);
+    if (bottom_solve() != 0) {
+      stat = 1;
+      break;
+    }
+    for (int l = 2; l <= L; l++) {
+      mg_prolong(l, COR);
+      for (int s = 0; s < prm_.n_post; s++) mg_smooth(l, COR, RES);
+    }
+    vaxpby(TL, SOL, 1.0, SOL, 1.0, COR);
+    mg_apply(L, RES, SOL, RHS);
+    rn = vnorm(TL, RES);
+    if (rn < r0 * prm_.tol_rel + prm_.tol_abs) {
+      conv = 1;
+      break;
+    }
+  }
+  CKR(cudaStreamSynchronize(stream_), -1);
+  info->iterations = std::min(it, prm_.max_iter);
+  info->rnorm0 = r0;
+  info->rnorm = rn;
+  info->status = stat ? 1 : (conv ? 0 : 2);
+  info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return err_.empty() ? 0 : -1;
+}
+
+// relax_solve (src/SayakaMacSolver.cpp:377-452): red-black Gauss-Seidel
+// sweeps of the finest tower (mg_smooth_level) on SOL with RHS, the
+// residual's L-inf norm after each, until |r| < |r0| tol_rel + tol_abs or
+// max_iter (the reference returns 0 either way; status 2 here when the
+// tolerance was not met)
+int MacGpu::relax_solve(SolveInfo *info) {
+  auto t0 = std::chrono::steady_clock::now();
+  const int L = finest_;
+  const BlockList TL = tower_list(L);
+  double *SOL = vec_[kSOL], *RHS = vec_[kRHS], *RES = vec_[kRESID];
+  mg_apply(L, RES, SOL, RHS);
+  const double r0 = vnorm(TL, RES);
+  double rn = r0;
+  int it = 0, conv = 0;
+  for (it = 1; it <= prm_.max_iter && err_.empty(); it++) {
+    mg_smooth(L, SOL, RHS);
+    mg_apply(L, RES, SOL, RHS);
+    rn = vnorm(TL, RES);
+    if (rn < r0 * prm_.tol_rel + prm_.tol_abs) {
+      conv = 1;
+      break;
+    }
+  }
+  CKR(cudaStreamSynchronize(stream_), -1);
+  info->iterations = std::min(it, prm_.max_iter);
+  info->rnorm0 = r0;
+  info->rnorm = rn;
+  info->status = conv ? 0 : 2;
+  info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return err_.empty() ? 0 : -1;
+}
+
 // ---------------------------------------------------------------------------
 // parity hooks (compact all-block arrays on the host)
 void MacGpu::apply(int L, const double *x, double *y) {

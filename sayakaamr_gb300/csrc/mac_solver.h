@@ -96,6 +96,10 @@ class MacGpu {
   const SolverParams &params() const { return prm_; }
 
   int cg_solve(SolveInfo *info);
+  // mg_solve / relax_solve: stand-alone V-cycles / Gauss-Seidel sweeps on the
+  // finest tower, reference arithmetic (0 ok, -1 CUDA error; info->status)
+  int mg_solve(SolveInfo *info);
+  int relax_solve(SolveInfo *info);
   // graph-captured device-resident solve (dense bottom); enqueue variant for
   // timing: no host synchronisation, the result stays on the device
   int cg_solve_device(SolveInfo *info);

@@ -24,6 +24,10 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 TAG = dict(op_x=1, op_rhs=2, sm_corr0=3, sm_resid=4, rs_in=5, pr_in=6, fx_phi=7,
            vc_p=8, bc_phi=9, bc_rhs0=10, sv_rand=11)
 
+# iterations of the mg_solve / relax_solve dumps (kMgIters, kRelaxIters of
+# oracle/ref_dump.cpp), run with a relative tolerance of 1e-30
+MG_ITERS, RELAX_ITERS = 6, 25
+
 # per-fixture seeds (must match make_case() in oracle/ref_dump.cpp)
 SEEDS = dict(c1=20251, t2s=777, t2b=4242, t3s=99, t3n=31337, n2=1616, n3=4096)
 

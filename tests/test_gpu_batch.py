@@ -50,9 +50,11 @@ def test_forest_matches_individual_problems(precision, per_problem):
         # this problem's residual on its own leaf cells
         assert np.abs(r[blocks][leaf][fluid]).max() < 1e-8, k
         _, ik, xk = solve(p, precision)
-        if per_problem:
+        if per_problem and int(p.tables["level"].max()) == finest:
             # its own stopping point: the same iterations as alone, up to the
-            # rounding of differently ordered dot products
+            # rounding of differently ordered dot products.  (A problem
+            # shallower than the forest is smoothed once more per extra tower
+            # of the forest's V-cycle, so it may take fewer.)
             assert abs(int(its[k]) - ik["iterations"]) <= 1, (k, its[k], ik["iterations"])
         a = xs[blocks][leaf][fluid]
         b = xk.reshape(-1, nc)[leaf][fluid]

@@ -158,3 +158,20 @@ def test_coefficient_setup(name):
     for d in range(nd):
         assert exact(af[d], g["af%d" % d]), d
         assert exact(bc[d], g["bcoef%d" % d]), d
+
+
+@pytest.mark.parametrize("name", ["t2s", "t3s", "n2", "n3"])
+def test_mg_and_relax_solves_bit_exact(name):
+    """mg_solve (stand-alone V-cycles, bottom BiCGSTAB with the solve's bottom
+    tolerances) and relax_solve (Gauss-Seidel sweeps), a fixed number of
+    iterations each, against the reference's"""
+    g, t, tb, O = oracle_for(name)
+    leaf = t.tower(tb["level"].max())[0]
+    kw = dict(tol_rel=1e-30, tol_abs=0.0, bot_tol_rel=float(g["sv_bot_tol_rel"][0]),
+              bot_tol_abs=float(g["sv_bot_tol_abs"][0]))
+    sol, info = O.mg_solve(g["sv_rhs"], pyoracle.params(max_iter=golden_io.MG_ITERS, **kw))
+    assert info["iterations"] == golden_io.MG_ITERS and info["status"] == 2, info
+    assert exact(rows(sol, leaf, O.ncell), g["mg_sol"]), name
+    sol, info = O.relax_solve(g["sv_rhs"], pyoracle.params(max_iter=golden_io.RELAX_ITERS, **kw))
+    assert info["iterations"] == golden_io.RELAX_ITERS, info
+    assert exact(rows(sol, leaf, O.ncell), g["rx_sol"]), name
