@@ -494,11 +494,17 @@ def main():
             timed_events[1].record(ext)
         return S.solve_info()
 
-    def warm():
+    def warm(setting=None):
         for _ in range(args.warmup):
             info = one()
             if info["status"] != 0:
-                raise SystemExit("warm-up solve failed: %s" % info)
+                st = S.problem_states()
+                where = ""
+                if st is not None:
+                    its, rel = st
+                    bad = [(int(i), int(its[i]), float(rel[i])) for i in range(len(rel)) if not rel[i] < TOL]
+                    where = "; problems not converged (index, iterations, relative residual): %s" % bad[:8]
+                raise SystemExit("warm-up solve failed: %s, setting %s%s" % (info, setting, where))
 
     tuning = None
     if args.precision < 0 or args.n_post < 0 or args.smoother < 0:
@@ -527,7 +533,7 @@ def main():
             for npost in posts:
                 S.set_params(precision=prec, n_post_smooth=npost, smoother=sm, inner_sweeps=inner)
                 S.prepare()
-                warm()
+                warm(dict(precision=prec, smoother=sm, inner_sweeps=inner, n_post_smooth=npost))
                 ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
                 infos = [one(e) for e in ev]
                 torch.cuda.synchronize()
@@ -704,7 +710,7 @@ def compare_solvers(S, prob, one, warm, torch, args, tuning):
     for label, prm in settings:
         S.set_params(**prm)
         S.prepare()
-        warm()
+        warm(dict(label=label, **prm))
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
         infos = [one(e) for e in ev]
         torch.cuda.synchronize()

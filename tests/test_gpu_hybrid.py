@@ -10,7 +10,7 @@ from test_gpu_parity import block_slice, reference_solution, setup_solver, solut
 
 pytestmark = pytest.mark.gpu
 
-BLOCK_RTOL = 1e-10  # converged block solves: 64 sweeps on 4^d-cell blocks reduce the residual ~1e-14
+BLOCK_RTOL = 1e-8   # converged block solves: 64 sweeps on 4^d-cell blocks reduce the residual by 1e-10 or more
 
 
 @pytest.mark.parametrize("name", ["t2s", "t3s"])
