@@ -103,6 +103,16 @@ def parse():
                     help="time one kernel alone and exit (for ncu): 0 FP64 operator on the finest tower, "
                          "1 FP32 / 2 FP64 red-black sweep (one colour) of the finest level, "
                          "3 the device solve's FP64 operator + dot product")
+    ap.add_argument("--sequence", type=int, default=0,
+                    help="config5 only: time a sequence of this many pressure solves of the elbow with the sphere "
+                         "moving along the pipe, a regrid every --regrid-every steps, setup inside the timed region")
+    ap.add_argument("--regrid-every", type=int, default=5)
+    ap.add_argument("--problems", type=int, default=256,
+                    help="config4: number of problems of the batch (256; fewer for a small profiling case)")
+    ap.add_argument("--max-level", type=int, default=7, help="--sequence: finest level of the elbow tree")
+    ap.add_argument("--bottom-refresh", type=int, default=1,
+                    help="--sequence: 1 rebuild the dense bottom inverse after every coefficient change, 0 keep "
+                         "the inverse of the last tree between regrids")
     ap.add_argument("--profile", action="store_true",
                     help="run one solve between cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     return ap.parse_args()
@@ -300,7 +310,8 @@ def run_reference(args):
         return
     import multiprocessing as mp
     from sayakaamr_gb300 import workloads
-    prob = workloads.CONFIGS[args.config]()
+    prob = (workloads.config4(n_problems=args.problems) if args.config == "config4"
+            else workloads.CONFIGS[args.config]())
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     if getattr(prob, "parts", None):
@@ -465,7 +476,11 @@ def main():
     import sayakaamr_gb300 as sg
     from sayakaamr_gb300 import workloads
 
-    prob = workloads.CONFIGS[args.config]()
+    if args.sequence > 0:
+        run_sequence(args, torch, ws, rank, local)
+        return
+    prob = (workloads.config4(n_problems=args.problems) if args.config == "config4"
+            else workloads.CONFIGS[args.config]())
     S = workloads.make_solver(prob)
     S.set_params(tol_rel=TOL, tol_abs=0.0, use_mg_precond=1, max_iter=2000, precision=max(args.precision, 0),
                  bottom=1,
@@ -494,10 +509,10 @@ def main():
             timed_events[1].record(ext)
         return S.solve_info()
 
-    def warm(setting=None):
+    def warm(setting=None, ok=(0,)):
         for _ in range(args.warmup):
             info = one()
-            if info["status"] != 0:
+            if info["status"] not in ok:
                 st = S.problem_states()
                 where = ""
                 if st is not None:
@@ -643,6 +658,7 @@ def main():
                    "sublevel_order": ("finest to coarsest per sublevel", "one launch per colour and level parity")[
                        args.sublevel_order],
                    "bottom_level": S.bottom_level(),
+                   "constant_coef_blocks": S.uniform_blocks(),
                    "smoother_autotune": dict(zip(("variant", "us_per_variant"), S.tuned_smoother(args.precision))),
                    "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "e2e": {"value": ws * prob.leaf_cells / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": h2d,
@@ -682,6 +698,160 @@ def main():
         torch.distributed.destroy_process_group()
 
 
+# ---- config5 as a sequence: the elbow pipe with a moving sphere ----------
+def _elbow_geometry(torch, tb, sc, seed):
+    """the step's level set on every block's grown box (1 ghost layer, the
+    reference's TreeData layout) and its right-hand side on every block's
+    cells, computed with torch on the GPU and copied to host memory: fluid
+    = inside the tube and outside the sphere; rhs = -(8 seeded Gaussians,
+    sigma 0.08) on the leaf blocks"""
+    from sayakaamr_gb300 import workloads as W
+    dev = "cuda"
+    n, nb = tb["num_blocks"], tb["nb"]
+    lo = torch.as_tensor(tb["block_lo"].reshape(n, 3), device=dev)
+    dx = torch.as_tensor(tb["block_len"].reshape(n, 3) / nb, device=dev)
+
+    def centres(G, shift):
+        r = torch.arange(G, device=dev, dtype=torch.float64) + shift
+        k, j, i = torch.meshgrid(r, r, r, indexing="ij")
+        idx = torch.stack([i.reshape(-1), j.reshape(-1), k.reshape(-1)], 1)
+        return lo[:, None, :] + idx[None] * dx[:, None, :]
+
+    c = torch.as_tensor(W.ELBOW_C, device=dev)
+    R = W.ELBOW_R
+
+    def seg(p, a, b):
+        a = torch.as_tensor(a, device=dev)
+        b = torch.as_tensor(b, device=dev)
+        ab = b - a
+        t = torch.clamp(((p - a) * ab).sum(-1) / (ab * ab).sum(), 0.0, 1.0)
+        return torch.linalg.norm(p - (a + t[..., None] * ab), dim=-1)
+
+    def level_set(p):
+        x, y, z = p[..., 0] - c[0], p[..., 1] - c[1], p[..., 2] - c[2]
+        ang = torch.atan2(y, x)
+        arc = torch.sqrt((torch.hypot(x, y) - R) ** 2 + z * z)
+        d = torch.where((ang >= 0) & (ang <= 0.5 * math.pi), arc, torch.full_like(arc, float("inf")))
+        d = torch.minimum(d, seg(p, [W.ELBOW_C[0] + R, 0.0, W.ELBOW_C[2]], [W.ELBOW_C[0] + R, W.ELBOW_C[1],
+                                                                            W.ELBOW_C[2]]))
+        d = torch.minimum(d, seg(p, [W.ELBOW_C[0], W.ELBOW_C[1] + R, W.ELBOW_C[2]], [0.0, W.ELBOW_C[1] + R,
+                                                                                    W.ELBOW_C[2]]))
+        sp = torch.linalg.norm(p - torch.as_tensor(sc, device=dev), dim=-1) - W.SPHERE_R
+        return torch.minimum(W.ELBOW_TUBE - d, sp)
+
+    ls = level_set(centres(nb + 2, -0.5)).reshape(-1)
+    pc = centres(nb, 0.5)
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    amp = torch.randn(8, generator=g, dtype=torch.float64).to(dev)
+    cen = (0.1 + 0.8 * torch.rand(8, 3, generator=g, dtype=torch.float64)).to(dev)
+    f = torch.zeros(pc.shape[:2], dtype=torch.float64, device=dev)
+    for q in range(8):
+        f += amp[q] * torch.exp(-((pc - cen[q]) ** 2).sum(-1) / (2 * 0.08 ** 2))
+    leaf = torch.as_tensor(tb["node_type"] == 1, device=dev)
+    rhs = (-f * leaf[:, None]).reshape(-1)
+    return ls.cpu().numpy(), rhs.cpu().numpy()
+
+
+def run_sequence(args, torch, ws, rank, local):
+    """--sequence K (config5): K pressure solves of the elbow while the
+    sphere moves from 10% to 90% of the centreline; every --regrid-every
+    steps the tree is regridded toward the sphere's new position (host tree
+    mirror) and a new solver is built on it, warm-started from the old
+    solution by the device regrid transfer; between regrids the solver takes
+    the step's fractions (setIBFracByLS from the level set, on the device)
+    and right-hand side and solves from the previous solution.  Timed per
+    step (wall clock, host synchronised): the solver's setup (tree upload,
+    coefficients, prepare) and the solve; the geometry (level set and
+    right-hand side, computed with torch) and the host tree regrid are
+    reported beside it, outside the solver time."""
+    import sayakaamr_gb300 as sg
+    from sayakaamr_gb300 import workloads as W
+    if args.config != "config5":
+        raise SystemExit("--sequence runs the config5 elbow sequence")
+    K, every = args.sequence, max(1, args.regrid_every)
+    prm = dict(tol_rel=TOL, tol_abs=0.0, use_mg_precond=1, max_iter=2000, bottom=1, graph=1,
+               precision=1 if args.precision < 0 else args.precision,
+               n_post_smooth=4 if args.n_post < 0 else args.n_post, bottom_level=args.bottom_level,
+               bottom_refresh=args.bottom_refresh, smoother=max(args.smoother, 0))
+    t0 = time.perf_counter()
+    sc = W.elbow_point(0.1)
+    tree = W.elbow_tree(sc, max_level=args.max_level)
+    tree_build_s = time.perf_counter() - t0
+    S = None
+    steps = []
+    geo_s = regrid_tree_s = 0.0
+    cells = 0
+    for k in range(K):
+        sc = W.elbow_point(0.1 + 0.8 * k / max(1, K - 1))
+        new_tree = k == 0 or k % every == 0
+        if k > 0 and new_tree:
+            t0 = time.perf_counter()
+            W.elbow_regrid(tree, sc, args.max_level)
+            regrid_tree_s += time.perf_counter() - t0
+        if new_tree:
+            tb = tree.tables()
+            n = tb["num_blocks"]
+            bc = np.full((n, 6), -1, dtype=np.int32)
+            nbr = tb["neighbor"].reshape(n, 6)
+            for fc in range(6):
+                bc[nbr[:, fc] <= -20, fc] = sg.DIRICHLET if fc == 0 else sg.NEUMANN
+            leaf_cells = int((tb["node_type"] == 1).sum()) * tb["nb"] ** 3
+        t0 = time.perf_counter()
+        ls, rhs = _elbow_geometry(torch, tb, sc, 5000 + k)
+        geo_s += time.perf_counter() - t0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if new_tree:
+            S2 = sg.MacSolver(tb)
+            S2.set_bc(bc.reshape(-1))
+            S2.set_ib_frac_by_ls(ls, ncomp=1, ngrow=1, comp=0)
+            S2.set_params(**prm)
+            if S is None:
+                S2.set_zero_sol()
+            else:
+                S2.init_from(S)
+            S = S2
+        else:
+            S.set_ib_frac_by_ls(ls, ncomp=1, ngrow=1, comp=0)
+        S.set_rhs_compact(rhs)
+        S.prepare()
+        t1 = time.perf_counter()
+        S.cg_solve_async()
+        info = S.solve_info()
+        t2 = time.perf_counter()
+        if info["status"] != 0 or not info["rnorm"] < TOL * info["rnorm0"]:
+            raise SystemExit("sequence step %d did not converge: %s" % (k, info))
+        steps.append(dict(setup_s=t1 - t0, solve_s=t2 - t1, iterations=info["iterations"], new_tree=new_tree,
+                          blocks=int(tb["num_blocks"]), leaf_cells=leaf_cells))
+        cells += leaf_cells
+    total = sum(r["setup_s"] + r["solve_s"] for r in steps)
+    setup = sum(r["setup_s"] for r in steps)
+    its = [r["iterations"] for r in steps]
+    out = {
+        "metric": METRIC, "value": cells / total, "unit": "cells/s", "n_gpus": ws, "steps": K, "warmup": 0,
+        "ms_per_step": total / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 outer BiCGSTAB + %s V-cycle, f64 bottom" % ("f32" if prm["precision"] == 1 else "f64"),
+        "data": "synthetic",
+        "config": {"workload": "config5 sequence: elbow pipe (tube 0.1, bend 0.3), sphere r=0.04 moving from 10%% "
+                               "to 90%% of the centreline over %d solves, regrid every %d, %d^3-cell blocks, up to "
+                               "%d levels, binary IB from the level set (setIBFracByLS), p=0 outlet"
+                               % (K, every, 8, args.max_level),
+                   "tol_rel": TOL, "params": prm},
+        "sequence": {"total_s": total, "setup_s": setup, "setup_share": setup / total,
+                     "solve_s": total - setup, "regrids": sum(1 for r in steps if r["new_tree"]) - 1,
+                     "iterations_mean": statistics.mean(its), "iterations_max": max(its),
+                     "setup_s_regrid_steps": sum(r["setup_s"] for r in steps if r["new_tree"]),
+                     "setup_s_other_steps": sum(r["setup_s"] for r in steps if not r["new_tree"]),
+                     "geometry_s_outside": geo_s, "host_tree_regrid_s_outside": regrid_tree_s,
+                     "initial_tree_s_outside": tree_build_s,
+                     "per_step": [[round(r["setup_s"] * 1e3, 2), round(r["solve_s"] * 1e3, 2), r["iterations"]]
+                                  for r in steps],
+                     "per_step_columns": ["setup ms", "solve ms", "iterations"]},
+    }
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def compare_solvers(S, prob, one, warm, torch, args, tuning):
     """time to 1e-8 (ms, CUDA events, L2 flushed) and iterations of: plain
     FP64 MG-BiCGSTAB (FP64 V-cycle, the reference's 2 post-smoothing sweeps),
@@ -710,7 +880,12 @@ def compare_solvers(S, prob, one, warm, torch, args, tuning):
     for label, prm in settings:
         S.set_params(**prm)
         S.prepare()
-        warm(dict(label=label, **prm))
+        try:
+            # status 3: converged after the learned correction was switched off
+            warm(dict(label=label, **prm), ok=(0, 3))
+        except SystemExit as e:
+            out[label] = {"failed": str(e)}
+            continue
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
         infos = [one(e) for e in ev]
         torch.cuda.synchronize()

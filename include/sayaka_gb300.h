@@ -138,6 +138,20 @@ typedef struct sayaka_params {
                              e.g. a forest of trees given as one table): 1 = one BiCGSTAB state per problem,
                              each stopping at its own tolerance, as if solved alone (default); 0 = one shared
                              state (scalars over all problems) */
+  int32_t uniform;        /* device path: 1 = blocks whose face coefficients are constant per direction and
+                             whose cells are all fluid (vf = 1) read the coefficients from a per-block record
+                             instead of the face arrays and vf (same arithmetic, same results; default);
+                             0 = every block reads the arrays */
+  int32_t bottom_refresh; /* device path: 1 = the dense bottom inverse is rebuilt after every coefficient change
+                             (default); 0 = the inverse of the last build is kept while only coefficients change
+                             (a fixed coarsest-level solve of the preconditioner, slightly stale; the outer
+                             BiCGSTAB still converges to the new operator's solution) */
+  int32_t learned_tc05;   /* learned correction of 16x16-cell blocks: 1 = its 32 -> 32 layer as an implicit GEMM
+                             on tcgen05 with the accumulator in tensor memory (default); 0 = on mma.sync warp
+                             MMAs (the same network, products summed in another order) */
+  int32_t learned_loss;   /* training loss of the learned correction u: 0 = the residual u leaves under the
+                             block-local operator; 1 = the distance of u to the block-local part of the error the
+                             V-cycle left, known from the solver's own converged solution (default) */
 } sayaka_params;
 
 typedef struct sayaka_solve_info {
@@ -243,6 +257,11 @@ int32_t sayaka_mac_bottom_level(const sayaka_mac *h);
  * one shared state.  No counterpart in the reference (it solves one tree). */
 int32_t sayaka_mac_problem_count(const sayaka_mac *h);
 int32_t sayaka_mac_problem_states(sayaka_mac *h, int32_t *iterations, double *rel_resid, int32_t n);
+/* number of constant-coefficient blocks of the tree (face coefficients
+ * constant per direction, every cell fluid), whose records the device solve
+ * reads with params.uniform = 1; prepares the device solve first.  -1 on
+ * error.  No counterpart in the reference (a property of this layout). */
+int32_t sayaka_mac_uniform_blocks(sayaka_mac *h);
 /* number of blocks in tower L, or at one level of it (sublevel >= 1) */
 int32_t sayaka_mac_tower_size(sayaka_mac *h, int32_t L, int32_t sublevel);
 

@@ -7,10 +7,11 @@ Network (sayakaamr_gb300/csrc/mac_learned.h): per block of nb x nb cells,
 channels, ReLU after the first two.  Parameter vector (FP32):
 w1[32][3][9], b1[32], w2[32][32][9], b2[32], w3[32][9], b3.
 The output is projected onto the block-local part (its least-squares fit by
-{1, x, y} over the block removed).  Loss of n blocks: the residual the
-correction u = sa * P(y) leaves under the block-local operator
+{1, x, y} over the block removed).  Loss of n blocks, for the correction
+u = sa * P(y): mode 0, the residual u leaves under the block-local operator
 A u = (K u) / (dv vf), (K u)_c = sum_f T_f (u_c - u_nb), u = 0 outside:
-(1/n) * sum (feat0 - A u)^2, with aux = [sa][dv vf][x-face T][y-face T].
+(1/n) * sum (feat0 - A u)^2; mode 1, the distance to the stored error
+target e: (1/n) * sum (u - e)^2.  aux = [sa][dv vf][x-face T][y-face T][e].
 No counterpart in the
 reference library; pinned by finite differences in tests/test_nn_oracle.py.
 """
@@ -97,26 +98,32 @@ def split_aux(aux, nb):
     sa = aux[:, :nc].reshape(n, nb, nb)
     dvvf = aux[:, nc:2 * nc].reshape(n, nb, nb)
     tx = aux[:, 2 * nc:2 * nc + nf].reshape(n, nb, nb + 1)
-    ty = aux[:, 2 * nc + nf:].reshape(n, nb + 1, nb)
-    return sa, dvvf, tx, ty
+    ty = aux[:, 2 * nc + nf:2 * nc + 2 * nf].reshape(n, nb + 1, nb)
+    e = aux[:, 2 * nc + 2 * nf:].reshape(n, nb, nb)
+    return sa, dvvf, tx, ty, e
 
 
-def loss_grad(w, feat, aux, nb):
+def loss_grad(w, feat, aux, nb, mode=1):
     w1, b1, w2, b2, w3, b3 = unpack(w)
     n = feat.shape[0]
     x = np.asarray(feat, dtype=np.float64).reshape(n, CIN, nb, nb)
-    sa, dvvf, tx, ty = split_aux(aux, nb)
+    sa, dvvf, tx, ty, e = split_aux(aux, nb)
     a1 = conv(x, w1, b1)
     h1 = np.maximum(a1, 0.0)
     a2 = conv(h1, w2, b2)
     h2 = np.maximum(a2, 0.0)
     y = local_part(conv(h2, w3, b3)[:, 0].reshape(n, nb * nb), nb).reshape(n, nb, nb)
     u = sa * y
-    inv = np.where(dvvf > 0, 1.0 / np.where(dvvf > 0, dvvf, 1.0), 0.0)
-    res = x[:, 0] - _K(u, tx, ty) * inv
-    loss = float(np.sum(res * res) / n)
-    g = -2.0 * res / n
-    dldu = _K(g * inv, tx, ty)
+    if mode == 1:
+        res = u - e
+        loss = float(np.sum(res * res) / n)
+        dldu = 2.0 * res / n
+    else:
+        inv = np.where(dvvf > 0, 1.0 / np.where(dvvf > 0, dvvf, 1.0), 0.0)
+        res = x[:, 0] - _K(u, tx, ty) * inv
+        loss = float(np.sum(res * res) / n)
+        g = -2.0 * res / n
+        dldu = _K(g * inv, tx, ty)
     gy = local_part((sa * dldu).reshape(n, nb * nb), nb).reshape(n, nb, nb)[:, None]
     g3, gb3, gh2 = conv_grad(h2, w3, gy)
     ga2 = gh2 * (a2 > 0)
@@ -135,7 +142,8 @@ def random_aux(rng, n, nb):
     dvvf = np.where(rng.uniform(0, 1, (n, nc)) < 0.1, 0.0, 1.0)
     sa = sa * dvvf
     t = rng.uniform(0.5, 2.0, (n, 2 * nf))
-    return np.concatenate([sa, dvvf, t], axis=1).astype(np.float32)
+    e = rng.normal(0.0, 0.1, (n, nc)) * dvvf
+    return np.concatenate([sa, dvvf, t, e], axis=1).astype(np.float32)
 
 
 def to_bf16(a):

@@ -41,7 +41,9 @@ class Params(C.Structure):
                 ("vcycle_kernel", C.c_int32), ("pdl", C.c_int32),
                 ("cluster_cells", C.c_int32), ("smooth_variant", C.c_int32), ("learned", C.c_int32),
                 ("bottom_level", C.c_int32), ("bottom_half", C.c_int32), ("sublevel_order", C.c_int32),
-                ("smoother", C.c_int32), ("inner_sweeps", C.c_int32), ("per_problem", C.c_int32)]
+                ("smoother", C.c_int32), ("inner_sweeps", C.c_int32), ("per_problem", C.c_int32),
+                ("uniform", C.c_int32), ("bottom_refresh", C.c_int32),
+                ("learned_tc05", C.c_int32), ("learned_loss", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -108,6 +110,7 @@ SIGNATURES = {
     "sayaka_mac_init_from": (C.c_int, [_V, _V]),
     "sayaka_mac_bottom_level": (C.c_int32, [_V]),
     "sayaka_mac_problem_count": (C.c_int32, [_V]),
+    "sayaka_mac_uniform_blocks": (C.c_int32, [_V]),
     "sayaka_mac_problem_states": (C.c_int32, [_V, _i32p, _f64p, C.c_int32]),
     "sayaka_cuda_peek_error": (C.c_int32, []),
     "sayaka_fp_selftest": (C.c_int, [_f64p, _f32p, C.c_int, _f32p, _f32p, _f64p, _f64p, _f64p, _f64p]),
@@ -532,6 +535,13 @@ class MacSolver:
         rr = np.zeros(max(n, 1))
         r = self.lib.sayaka_mac_problem_states(self.h, it.ctypes.data_as(_i32p), rr.ctypes.data_as(_f64p), n)
         return None if r < 0 else (it[:r], rr[:r])
+
+    def uniform_blocks(self):
+        """constant-coefficient blocks of the tree (prepares the device solve)"""
+        n = self.lib.sayaka_mac_uniform_blocks(self.h)
+        if n < 0:
+            _check(CUDA_ERROR, "uniform_blocks", self.h)
+        return n
 
     def bottom_level(self):
         """level of the device solve's dense bottom solve (-1 before prepare)"""

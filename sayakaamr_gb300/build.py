@@ -27,7 +27,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]
 SOURCES = ["tree.cpp", "tower.cpp", "abi.cpp", "mac_solver.cu", "mac_kernels.cu", "mac_fast.cu", "mac_vcycle.cu",
-           "mac_noalloc.cu", "mac_projection.cu",
+           "mac_noalloc.cu", "mac_projection.cu", "mac_coef.cu",
            "mac_learned.cu", "mac_transfer.cu"]
 
 

@@ -414,6 +414,10 @@ void sayaka_params_default(sayaka_params *p) {
   p->smoother = d.smoother;
   p->inner_sweeps = d.inner_sweeps;
   p->per_problem = d.per_problem;
+  p->uniform = d.uniform;
+  p->bottom_refresh = d.bottom_refresh;
+  p->learned_tc05 = d.learned_tc05;
+  p->learned_loss = d.learned_loss;
 }
 
 int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
@@ -646,6 +650,14 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.inner_sweeps = p->inner_sweeps;
     if (p->per_problem < 0 || p->per_problem > 1) return (int)SAYAKA_BAD_INPUT;
     s.per_problem = p->per_problem;
+    if (p->uniform < 0 || p->uniform > 1) return (int)SAYAKA_BAD_INPUT;
+    s.uniform = p->uniform;
+    if (p->bottom_refresh < 0 || p->bottom_refresh > 1) return (int)SAYAKA_BAD_INPUT;
+    s.bottom_refresh = p->bottom_refresh;
+    if (p->learned_tc05 < 0 || p->learned_tc05 > 1) return (int)SAYAKA_BAD_INPUT;
+    s.learned_tc05 = p->learned_tc05;
+    if (p->learned_loss < 0 || p->learned_loss > 1) return (int)SAYAKA_BAD_INPUT;
+    s.learned_loss = p->learned_loss;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
   });
@@ -900,6 +912,15 @@ int32_t sayaka_mac_problem_states(sayaka_mac *h, int32_t *iterations, double *re
   if (r >= 0 && iterations)
     for (int k = 0; k < n && k < r; k++) iterations[k] = it[k];
   return r;
+}
+int32_t sayaka_mac_uniform_blocks(sayaka_mac *h) {
+  if (!h || !h->gpu) return -1;
+  int n = -1;
+  const int rc = guarded(h, [&] {
+    n = h->gpu->uniform_blocks();
+    return n < 0 ? (int)SAYAKA_CUDA_ERROR : (int)SAYAKA_OK;
+  });
+  return rc == (int)SAYAKA_OK ? n : -1;
 }
 int32_t sayaka_mac_bottom_level(const sayaka_mac *h) {
   if (!h || !h->gpu) return -1;

@@ -38,7 +38,17 @@ struct Coef {
   const T *afrac[3];  // IB area fraction
   const T *vf;        // IB volume fraction
   T alpha, beta;
+  // Constant-coefficient blocks (device solve only; null elsewhere):
+  // kUni values per block, [0..2] the same-level face coefficient of every
+  // face of direction 0..2 of the block, [3] nonzero when the block is one
+  // (every face of direction d has coefficient [d] and every cell vf = 1);
+  // FP64 records also hold the factors of the block's interior cells (no
+  // face on the block boundary): [4] P and [5] S of the outer operator,
+  // [6] sa and [7] ia of the FP64 smoother.  Kernels read these instead of
+  // the face arrays and vf, with the same arithmetic in the same order.
+  const T *ut = nullptr;
 };
+constexpr int kUni = 8;
 
 // Halo descriptor of a tower list entry, kHX ints: the ids every face of
 // the block reads, precomputed so that a cell's gathers wait on one load

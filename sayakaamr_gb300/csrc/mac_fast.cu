@@ -309,7 +309,10 @@ struct EpiEnd {  // |r|, rhat.r of the next iteration
         st->nn_best = v[0];
         st->nn_since = 0;
       } else if (++st->nn_since >= 4) {
+        // the preconditioner changes from here on: the next iteration
+        // restarts the search direction from the residual (p = r)
         st->nn_off = 1;
+        st->restart = 1;
       }
     }
     if (st->omega == 0) {
@@ -564,11 +567,63 @@ __global__ void __launch_bounds__(kTPB) k_smooth_factors(Topo t, Coef<double> c,
   }
 }
 
+// Constant-coefficient block records (Coef::ut), one CTA per block: a block
+// qualifies when every face of direction d carries the same coefficient T_d
+// (boundary faces included) and every cell has vf = 1.  Its interior cells'
+// factors are those k_op_prep and k_smooth_factors compute, in the same
+// order: diag = alpha*dv + T_0 + T_0 + T_1 + T_1 (+ T_2 + T_2).  The FP32
+// record holds the FP32 coefficients, equal throughout the block too.
+template <int ND>
+__global__ void __launch_bounds__(kTPB) k_uniform(Topo t, Coef<double> c, Coef<float> c32, double *u64,
+                                                float *u32) {
+  __shared__ int ok;
+  for (int b = blockIdx.x; b < t.nblocks; b += gridDim.x) {
+    if (threadIdx.x == 0) ok = 1;
+    __syncthreads();
+    const long fb = (long)b * t.nfb, cb = (long)b * t.ncell;
+    bool good = true;
+    for (int d = 0; d < ND; d++) {
+      const double t0 = c.tff[d][fb];
+      for (int i = threadIdx.x; i < t.nfb; i += blockDim.x) good = good && c.tff[d][fb + i] == t0;
+    }
+    for (int i = threadIdx.x; i < t.ncell; i += blockDim.x) good = good && c.vf[cb + i] == 1.0;
+    if (!good) ok = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double T[3] = {0.0, 0.0, 0.0};
+      float T32[3] = {0.f, 0.f, 0.f};
+      for (int d = 0; d < ND; d++) {
+        T[d] = c.tff[d][fb];
+        T32[d] = c32.tff[d][fb];
+      }
+      const double dv = c.geom[b * 8 + 6];
+      double diag = c.alpha * dv;
+      for (int f = 0; f < 2 * ND; f++) diag += T[f >> 1];
+      const bool on = ok && diag > 0;
+      const double sc = 1.0 / (dv * 1.0);
+      double *u = u64 + (long)b * kUni;
+      float *v = u32 + (long)b * kUni;
+      for (int d = 0; d < 3; d++) {
+        u[d] = T[d];
+        v[d] = T32[d];
+      }
+      u[3] = on ? 1.0 : 0.0;
+      v[3] = on ? 1.f : 0.f;
+      u[4] = on ? diag * sc : 0.0;
+      u[5] = on ? sc : 0.0;
+      u[6] = on ? dv * 1.0 / diag : 0.0;
+      u[7] = on ? 1.0 / diag : 0.0;
+      for (int k = 4; k < kUni; k++) v[k] = 0.f;
+    }
+    __syncthreads();
+  }
+}
+
 // sum T * phi_nb over the faces of cell ijk that are not physical boundaries
 template <int ND, typename TX>
 __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &c, int b, uint16_t ft,
                                              const int ijk[3], int ci, const TX *__restrict__ x,
-                                             const int *__restrict__ hx = nullptr) {
+                                             const int *__restrict__ hx = nullptr, const double *u = nullptr) {
   using namespace stencil;
   const int nb = t.nb;
   const long cb = (long)b * t.ncell;
@@ -580,12 +635,13 @@ __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &
     const int fx = face_index(d, ijk, s, nb);
     if (!bnd) {
       const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
-      off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], widen_from<TX>(x[cb + ci + (s ? stride : -stride)]), off);
+      off = __fma_rn(u ? u[d] : c.tff[d][(long)b * t.nfb + fx], widen_from<TX>(x[cb + ci + (s ? stride : -stride)]),
+                     off);
     } else {
       const int ty = face_type_of(ft, f);
       if (ty == 0)
-        off = __fma_rn(c.tff[d][(long)b * t.nfb + fx], widen_from<TX>(same_level_ghost<TX, false>(t, b, f, ijk, x, hx)),
-                       off);
+        off = __fma_rn(u ? u[d] : c.tff[d][(long)b * t.nfb + fx],
+                       widen_from<TX>(same_level_ghost<TX, false>(t, b, f, ijk, x, hx)), off);
       else if (ty == 2)
         off = __fma_rn(cf_coef(c, t, b, d, fx, 1.5), widen_from<TX>(fine_crse_ghost<TX, ND, false>(t, b, f, ijk, x, hx)),
                        off);
@@ -622,9 +678,15 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
     const int b = e ? e[kHXBlock] : L.blocks[p];
     const uint16_t ft = e ? (uint16_t)(e[kHXInfo] & 0xffff) : L.ftypes[p];
     const long q = (long)b * t.ncell + ci;
-    const double off = op_offdiag<ND, TX>(t, c, b, ft, ijk, ci, x, e);
-    const double sc = S[q];
-    double yv = __fma_rn(widen_from<TX>(x[q]), P[q], -off * sc);
+    // constant-coefficient block: face coefficients and S from its record,
+    // P too for an interior cell (the boundary cells' P depends on the face types)
+    const double *u = uniform_of(c, b);
+    const double off = op_offdiag<ND, TX>(t, c, b, ft, ijk, ci, x, e, u);
+    bool inner = true;
+#pragma unroll
+    for (int d = 0; d < ND; d++) inner = inner && ijk[d] > 0 && ijk[d] < t.nb - 1;
+    const double sc = u ? u[5] : S[q];
+    double yv = __fma_rn(widen_from<TX>(x[q]), (u && inner) ? u[4] : P[q], -off * sc);
     if (MODE >= 2) yv = fpint::positive(sc) ? w[q] - yv : 0.0;
     y[q] = yv;
     if (MODE == 3) y2[q] = yv;
@@ -768,6 +830,13 @@ void MacGpu::ensure_fast_buffers() {
   else cudaMemset(d_corr64b_, 0, nc * sizeof(double));
   if (cudaMalloc(&d_opP_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
   if (cudaMalloc(&d_opS_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
+  if (cudaMalloc(&d_uni64_, (size_t)std::max(nbk, 1) * kUni * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_uni32_, (size_t)std::max(nbk, 1) * kUni * sizeof(float)) != cudaSuccess)
+    fail("out of device memory (block records)");
+  else {
+    cudaMemset(d_uni64_, 0, (size_t)std::max(nbk, 1) * kUni * sizeof(double));
+    cudaMemset(d_uni32_, 0, (size_t)std::max(nbk, 1) * kUni * sizeof(float));
+  }
   if (cudaMalloc(&d_st_, sizeof(FState)) != cudaSuccess) fail("alloc state");
   if (cudaMallocHost(&h_st_, sizeof(FState)) != cudaSuccess) fail("alloc pinned state");
   if (cudaMalloc(&d_part_, sizeof(double) * kMaxRedBlocks * 4) != cudaSuccess) fail("alloc partials");
@@ -851,7 +920,7 @@ void MacGpu::tune_smoother(int precision) {
       if (pi)
         launch_rbgs<float>(topo_, c32_, sl, color, d_corr32_, d_resid32_, nullptr, stream_, false, v);
       else
-        launch_rbgs<double>(topo_, c64_, sl, color, vec_[kCORR], vec_[kRESID], nullptr, stream_, false, v);
+        launch_rbgs<double>(topo_, cd64_, sl, color, vec_[kCORR], vec_[kRESID], nullptr, stream_, false, v);
     };
     go(0);
     go(1);
@@ -897,6 +966,27 @@ void MacGpu::build_op_factors() {
   else
     k_op_prep<3><<<ew_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, d_opP_, d_opS_);
   CK(cudaGetLastError());
+}
+
+// constant-coefficient block records from the current coefficients (after
+// refresh_fp32: the FP32 record takes the FP32 face coefficients)
+void MacGpu::build_uniform() {
+  const int nbk = tt_.num_blocks;
+  if (nbk == 0) return;
+  const int grid = std::min(nbk, 152 * 8);
+  if (tt_.ndim == 2)
+    k_uniform<2><<<grid, kTPB, 0, stream_>>>(topo_, c64_, c32_, d_uni64_, d_uni32_);
+  else
+    k_uniform<3><<<grid, kTPB, 0, stream_>>>(topo_, c64_, c32_, d_uni64_, d_uni32_);
+  CK(cudaGetLastError());
+}
+
+// the coefficients the device solve's kernels read: with params.uniform the
+// records of the constant-coefficient blocks, else the face arrays only
+void MacGpu::bind_uniform() {
+  cd64_ = c64_;
+  cd64_.ut = prm_.uniform ? d_uni64_ : nullptr;
+  c32_.ut = prm_.uniform ? d_uni32_ : nullptr;
 }
 
 // FP32 copies of the coefficients for the FP32 V-cycle
@@ -991,6 +1081,7 @@ void MacGpu::build_bottom() {
   bot_level_ = LB;
   bot_param_ = prm_.bottom_level;
   const std::vector<int> &B1 = towers_[LB].blocks;
+  pull_coefs(&B1);  // the bottom blocks' coefficients, assembled on the host
   const int nblk1 = (int)B1.size();
   n_bot_ = nblk1 * ncell_;
   if (n_bot_ == 0) return;
@@ -1133,13 +1224,18 @@ void MacGpu::build_bottom() {
       pins.push_back(r0);
     }
   }
-  bottom_free();
   std::vector<int> tile_comp, tile_row0;
   for (int c = 0; c < nc; c++)
     for (int r = 0; r < comp_n[c]; r += kBottomTileRows) {
       tile_comp.push_back(c);
       tile_row0.push_back(r);
     }
+  // The structure (level, components, row order) depends on the tree
+  // alone: after a coefficient change the device arrays are rewritten in
+  // place, so that a captured solve graph, which holds their addresses,
+  // stays valid.
+  const bool reuse = d_binv_ && bot_built_level_ == LB && bot_built_tot_ == tot && bot_built_half_ == prm_.bottom_half;
+  if (!reuse) bottom_free();
   auto up = [&](auto *&dptr, const auto &v) {
     using E = typename std::remove_reference<decltype(v[0])>::type;
     if (cudaMalloc(&dptr, std::max<size_t>(v.size(), 1) * sizeof(E)) != cudaSuccess) {
@@ -1148,14 +1244,21 @@ void MacGpu::build_bottom() {
     }
     if (!v.empty()) CK_(cudaMemcpyAsync(dptr, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, stream_));
   };
-  up(d_binv_, A);
-  up(d_bot_blocks_, order);
-  up(d_comp_row0_, comp_row0);
-  up(d_comp_n_, comp_n);
-  up(d_comp_off_, comp_off);
-  up(d_tile_comp_, tile_comp);
-  up(d_tile_row0_, tile_row0);
+  if (reuse) {
+    CK_(cudaMemcpyAsync(d_binv_, A.data(), A.size() * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  } else {
+    up(d_binv_, A);
+    up(d_bot_blocks_, order);
+    up(d_comp_row0_, comp_row0);
+    up(d_comp_n_, comp_n);
+    up(d_comp_off_, comp_off);
+    up(d_tile_comp_, tile_comp);
+    up(d_tile_row0_, tile_row0);
+  }
   if (!err_.empty()) return;
+  bot_built_level_ = LB;
+  bot_built_tot_ = tot;
+  bot_built_half_ = prm_.bottom_half;
   // Gauss-Jordan, batched over the components of equal order
   std::vector<int> sizes(comp_n);
   std::sort(sizes.begin(), sizes.end());
@@ -1207,8 +1310,8 @@ void MacGpu::build_bottom() {
     }
     long long *d_ro = nullptr;
     int *d_rm = nullptr;
-    if (cudaMalloc(&d_binv16_, (size_t)tot * sizeof(unsigned short)) != cudaSuccess ||
-        cudaMalloc(&d_rscale_, (size_t)n_bot_ * sizeof(float)) != cudaSuccess ||
+    if ((!d_binv16_ && cudaMalloc(&d_binv16_, (size_t)tot * sizeof(unsigned short)) != cudaSuccess) ||
+        (!d_rscale_ && cudaMalloc(&d_rscale_, (size_t)n_bot_ * sizeof(float)) != cudaSuccess) ||
         cudaMalloc(&d_ro, (size_t)n_bot_ * sizeof(long long)) != cudaSuccess ||
         cudaMalloc(&d_rm, (size_t)n_bot_ * sizeof(int)) != cudaSuccess) {
       if (d_ro) cudaFree(d_ro);
@@ -1222,7 +1325,7 @@ void MacGpu::build_bottom() {
     cudaFree(d_ro);
     cudaFree(d_rm);
   } else if (LB > 1) {
-    if (cudaMalloc(&d_binv32_, (size_t)tot * sizeof(float)) != cudaSuccess) {
+    if (!d_binv32_ && cudaMalloc(&d_binv32_, (size_t)tot * sizeof(float)) != cudaSuccess) {
       d_binv32_ = nullptr;
       fail("out of device memory (bottom solve)");
       return;
@@ -1251,6 +1354,8 @@ void MacGpu::bottom_free() {
   d_bot_blocks_ = d_comp_row0_ = d_comp_n_ = d_tile_comp_ = d_tile_row0_ = nullptr;
   d_comp_off_ = nullptr;
   bot_ = BottomDev{};
+  bot_built_level_ = -1;
+  bot_built_tot_ = -1;
 }
 
 // one V-cycle with zero initial guess in precision T; the input residual
@@ -1409,17 +1514,17 @@ void MacGpu::iteration_body(T *resid, T *corr, const Coef<T> &c, const TO *PH, c
     using TX = std::remove_const_t<std::remove_pointer_t<decltype(x)>>;
     if (tt_.ndim == 2) {
       if (mp)
-        launch_k(pdl, k_op_red<2, M, TX, true>, gr, kTPB, 0, stream_, topo_, c64_, TL, ch, x, y, wv, OP, OS, ST, PART,
+        launch_k(pdl, k_op_red<2, M, TX, true>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS, ST, PART,
                  CNT, y2);
       else
-        launch_k(pdl, k_op_red<2, M, TX, false>, gr, kTPB, 0, stream_, topo_, c64_, TL, ch, x, y, wv, OP, OS, ST,
+        launch_k(pdl, k_op_red<2, M, TX, false>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS, ST,
                  PART, CNT, y2);
     } else {
       if (mp)
-        launch_k(pdl, k_op_red<3, M, TX, true>, gr, kTPB, 0, stream_, topo_, c64_, TL, ch, x, y, wv, OP, OS, ST, PART,
+        launch_k(pdl, k_op_red<3, M, TX, true>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS, ST, PART,
                  CNT, y2);
       else
-        launch_k(pdl, k_op_red<3, M, TX, false>, gr, kTPB, 0, stream_, topo_, c64_, TL, ch, x, y, wv, OP, OS, ST,
+        launch_k(pdl, k_op_red<3, M, TX, false>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS, ST,
                  PART, CNT, y2);
     }
   };
@@ -1495,7 +1600,7 @@ void MacGpu::capture_loop(int precision) {
   if (precision == 1)
     iteration_device<float>(d_resid32_, d_corr32_, c32_);
   else
-    iteration_device<double>(vec_[kRESID], vec_[kCORR], c64_);
+    iteration_device<double>(vec_[kRESID], vec_[kCORR], cd64_);
   solve_lists_ = false;
   if (multi())
     launch_k(prm_.pdl != 0, k_set_cond_multi, 1, 256, 0, stream_, h, (const FState *)d_stc_, ncomp_, d_st_);
@@ -1525,6 +1630,7 @@ void MacGpu::capture_loop(int precision) {
   graph_smoother_ = prm_.smoother;
   graph_inner_ = prm_.inner_sweeps;
   graph_multi_ = (int)multi();
+  graph_uniform_ = prm_.uniform;
 }
 
 // the captured graph was recorded with other parameters than the current ones
@@ -1533,7 +1639,7 @@ bool MacGpu::graph_stale() const {
          graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl || graph_cc_ != prm_.cluster_cells ||
          graph_var_ != rbgs_variant_[prm_.precision == 1] || graph_nn_ != (int)learned_active() ||
          graph_order_ != prm_.sublevel_order || graph_smoother_ != prm_.smoother ||
-         graph_inner_ != prm_.inner_sweeps || graph_multi_ != (int)multi();
+         graph_inner_ != prm_.inner_sweeps || graph_multi_ != (int)multi() || graph_uniform_ != prm_.uniform;
 }
 
 int MacGpu::cg_solve_device(SolveInfo *info) {
@@ -1588,17 +1694,17 @@ int MacGpu::enqueue_solve() {
   unsigned *CNT = mp ? d_ccnt_ : d_cnt_;
   if (tt_.ndim == 2) {
     if (mp)
-      k_op_red<2, 2, double, true><<<gr, kTPB, 0, stream_>>>(topo_, c64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
+      k_op_red<2, 2, double, true><<<gr, kTPB, 0, stream_>>>(topo_, cd64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
                                                              d_opP_, d_opS_, ST, PART, CNT);
     else
-      k_op_red<2, 2, double, false><<<gr, kTPB, 0, stream_>>>(topo_, c64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
+      k_op_red<2, 2, double, false><<<gr, kTPB, 0, stream_>>>(topo_, cd64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
                                                               d_opP_, d_opS_, ST, PART, CNT);
   } else {
     if (mp)
-      k_op_red<3, 2, double, true><<<gr, kTPB, 0, stream_>>>(topo_, c64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
+      k_op_red<3, 2, double, true><<<gr, kTPB, 0, stream_>>>(topo_, cd64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
                                                              d_opP_, d_opS_, ST, PART, CNT);
     else
-      k_op_red<3, 2, double, false><<<gr, kTPB, 0, stream_>>>(topo_, c64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
+      k_op_red<3, 2, double, false><<<gr, kTPB, 0, stream_>>>(topo_, cd64_, TL, ch, vec_[kX0], vec_[kR], vec_[kRHS],
                                                               d_opP_, d_opS_, ST, PART, CNT);
   }
   vcopy(TL, vec_[kRHAT], vec_[kR]);
@@ -1614,7 +1720,7 @@ int MacGpu::enqueue_solve() {
         if (prm_.precision == 1)
           iteration_device<float>(d_resid32_, d_corr32_, c32_);
         else
-          iteration_device<double>(vec_[kRESID], vec_[kCORR], c64_);
+          iteration_device<double>(vec_[kRESID], vec_[kCORR], cd64_);
         solve_lists_ = false;
         if (mp) k_set_cond_multi<<<1, 256, 0, stream_>>>(0, d_stc_, ncomp_, d_st_);
         if (record_) {  // a collection solve keeps every iterate
@@ -1650,24 +1756,30 @@ int MacGpu::prepare_device() {
   ensure_fast_buffers();
   if (!err_.empty()) return -1;
   if (coef_version_ != fast_coef_version_) {
-    // The captured graph holds kernel arguments by value, among them the
-    // bottom solve's device arrays, which build_bottom frees and allocates
-    // again: drop the graph (after the stream's work is done) so that the
-    // next solve captures it afresh with the new arguments.
-    CKR_(cudaStreamSynchronize(stream_), -1);
-    drop_graph();
+    // Every array of the coefficient set is rewritten in place (stream
+    // order keeps it behind any solve in flight), so a captured graph,
+    // which holds kernel arguments by value, stays valid -- unless the
+    // bottom solve's arrays had to be allocated afresh.
+    const BottomDev before = bot_;
     refresh_fp32();
+    build_uniform();
     build_op_factors();
     build_smooth_factors();
-    build_bottom();
+    if (prm_.bottom_refresh || !bottom_ready_ || bot_param_ != prm_.bottom_level || bot_half_ != prm_.bottom_half)
+      build_bottom();
     fast_coef_version_ = coef_version_;
     if (!err_.empty()) return -1;
+    if (std::memcmp(&before, &bot_, sizeof(BottomDev)) != 0) {
+      CKR_(cudaStreamSynchronize(stream_), -1);
+      drop_graph();
+    }
   } else if (bot_param_ != prm_.bottom_level || bot_half_ != prm_.bottom_half) {  // another bottom asked for
     CKR_(cudaStreamSynchronize(stream_), -1);
     drop_graph();
     build_bottom();
     if (!err_.empty()) return -1;
   }
+  bind_uniform();
   tune_smoother(prm_.precision);
   if (learned_active()) learned_prepare();
   if (!err_.empty()) return -1;
@@ -1697,6 +1809,10 @@ int MacGpu::solve_state(SolveInfo *info) {
   }
   if (rbgs_bulk_error(true) > 0) {
     fail("bulk-copy smoother: an mbarrier wait timed out");
+    return -1;
+  }
+  if (learned_active() && nn_tc_error(true) > 0) {
+    fail("learned correction: a tensor-core wait timed out");
     return -1;
   }
   if (last_multi_) {
@@ -1743,6 +1859,17 @@ int MacGpu::problem_states(int *iterations, double *rel_resid, int n) {
   return ncomp_;
 }
 
+int MacGpu::uniform_blocks() {
+  if (prepare_device() != 0) return -1;
+  std::vector<double> u((size_t)tt_.num_blocks * kUni);
+  if (u.empty()) return 0;
+  CKR_(cudaMemcpyAsync(u.data(), d_uni64_, u.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_), -1);
+  CKR_(cudaStreamSynchronize(stream_), -1);
+  int n = 0;
+  for (int b = 0; b < tt_.num_blocks; b++) n += u[(size_t)b * kUni + 3] != 0.0;
+  return n;
+}
+
 int MacGpu::tower_size(int L, int sublevel) const {
   if (L < 1 || L > tt_.max_level) return -1;
   const DevTower &t = towers_[L];
@@ -1754,13 +1881,14 @@ int MacGpu::tower_size(int L, int sublevel) const {
 int MacGpu::enqueue_kernel(int which, int L) {
   if (L < 1 || L > tt_.max_level || towers_[L].all.n == 0) return -1;
   ensure_fast_buffers();
+  bind_uniform();
   if (which == 0) {
     launch_apply<double>(topo_, c64_, tower_list(L), vec_[kSOL], vec_[kV], nullptr, nullptr, stream_);
   } else if (which == 1) {
     launch_rbgs<float>(topo_, c32_, sublevel_list(L, L), 0, d_corr32_, d_resid32_, nullptr, stream_, false,
                        rbgs_var<float>());
   } else if (which == 2) {
-    launch_rbgs<double>(topo_, c64_, sublevel_list(L, L), 0, vec_[kCORR], vec_[kRESID], nullptr, stream_, false,
+    launch_rbgs<double>(topo_, cd64_, sublevel_list(L, L), 0, vec_[kCORR], vec_[kRESID], nullptr, stream_, false,
                         rbgs_var<double>());
   } else if (which == 3) {
     if (L != finest_) return -1;
@@ -1768,11 +1896,11 @@ int MacGpu::enqueue_kernel(int which, int L) {
     const long w = (long)TL.n * ncell_;
     CKR_(cudaMemsetAsync(d_st_, 0, sizeof(FState), stream_), -1);
     if (tt_.ndim == 2)
-      k_op_red<2, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, Chunks{}, vec_[kSOL], vec_[kV],
+      k_op_red<2, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, cd64_, TL, Chunks{}, vec_[kSOL], vec_[kV],
                                                                       vec_[kRHAT], d_opP_, d_opS_, d_st_, d_part_,
                                                                       d_cnt_);
     else
-      k_op_red<3, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, Chunks{}, vec_[kSOL], vec_[kV],
+      k_op_red<3, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, cd64_, TL, Chunks{}, vec_[kSOL], vec_[kV],
                                                                       vec_[kRHAT], d_opP_, d_opS_, d_st_, d_part_,
                                                                       d_cnt_);
   } else {
@@ -1803,11 +1931,11 @@ int MacGpu::device_kernel_compact(int which, int L, int variant, const double *i
     CKR_(cudaMemsetAsync(vec_[kRHAT], 0, n * sizeof(double), stream_), 2);
     CKR_(cudaMemsetAsync(d_st_, 0, sizeof(FState), stream_), 2);
     if (tt_.ndim == 2)
-      k_op_red<2, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, Chunks{}, vec_[kTMP],
+      k_op_red<2, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, cd64_, TL, Chunks{}, vec_[kTMP],
                                                                       vec_[kV], vec_[kRHAT], d_opP_, d_opS_, d_st_,
                                                                       d_part_, d_cnt_);
     else
-      k_op_red<3, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, Chunks{}, vec_[kTMP],
+      k_op_red<3, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, cd64_, TL, Chunks{}, vec_[kTMP],
                                                                       vec_[kV], vec_[kRHAT], d_opP_, d_opS_, d_st_,
                                                                       d_part_, d_cnt_);
     CKR_(cudaGetLastError(), 2);
@@ -1818,7 +1946,7 @@ int MacGpu::device_kernel_compact(int which, int L, int variant, const double *i
     CKR_(cudaMemcpyAsync(vec_[kTMP], in, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);
     CKR_(cudaMemcpyAsync(vec_[kRESID], in2, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);
     CKR_(cudaMemcpyAsync(vec_[kCORR], in, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);
-    launch_bhgs<double>(topo_, c64_, smooth_list(L), variant, vec_[kTMP], vec_[kCORR], vec_[kRESID], nullptr,
+    launch_bhgs<double>(topo_, cd64_, smooth_list(L), variant, vec_[kTMP], vec_[kCORR], vec_[kRESID], nullptr,
                         stream_, false);
     CKR_(cudaGetLastError(), 2);
     CKR_(cudaMemcpyAsync(out, vec_[kCORR], n * sizeof(double), cudaMemcpyDeviceToHost, stream_), 2);
@@ -1830,7 +1958,7 @@ int MacGpu::device_kernel_compact(int which, int L, int variant, const double *i
       const BlockList sl = sublevel_list(L, ll);
       if (sl.n == 0) continue;
       for (int rb = 0; rb < 2; rb++)
-        launch_rbgs<double>(topo_, c64_, sl, rb, vec_[kCORR], vec_[kRESID], nullptr, stream_, false, v);
+        launch_rbgs<double>(topo_, cd64_, sl, rb, vec_[kCORR], vec_[kRESID], nullptr, stream_, false, v);
     }
     CKR_(cudaGetLastError(), 2);
     CKR_(cudaMemcpyAsync(out, vec_[kCORR], n * sizeof(double), cudaMemcpyDeviceToHost, stream_), 2);

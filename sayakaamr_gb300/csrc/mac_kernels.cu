@@ -369,12 +369,13 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
       else
         fx = encode(ijk, nb) + s * nb * nb;
       const int ty = face_type_of(ft, f);
+      const T *u = uniform_of(c, b);
       T vc = 0, vk = 0, vv = 0;
       if (ty == 0) {
-        vc = vk = c.tff[d][fb + fx];
+        vc = vk = u ? u[d] : c.tff[d][fb + fx];
         vv = same_level_ghost<T, false>(t, b, f, ijk, phi, hxe);
       } else if (ty == 1) {
-        if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
+        if (t.bc_type[b * 6 + f] != kBCNeumann) vc = (u ? u[d] : c.tff[d][fb + fx]) * (T)2.0;
       } else if (ty == 2) {
         vc = vk = cf_coef(c, t, b, d, fx, (T)1.5);
         vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi, hxe);
@@ -389,6 +390,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
     }
     __syncthreads();
     const T dv = geom(c, b, 6);
+    const T *u = uniform_of(c, b);  // constant coefficients: no face or vf loads
     // a cell's global operands (face coefficients, rhs and vf or the FP64
     // factors) are gathered before any update: a thread with two cells has
     // both cells' loads in flight together (the shared-memory tile written
@@ -412,16 +414,24 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
           fx = o.ijk[0] + nb * (o.ijk[1] + s + (nb + 1) * o.ijk[2]);
         else
           fx = o.ci + s * nb * nb;
-        o.coef[f] = bnd ? (T)0 : c.tff[d][fb + fx];
+        o.coef[f] = bnd ? (T)0 : (u ? u[d] : c.tff[d][fb + fx]);
       }
       o.r = rhs[cb + o.ci];
       if (sizeof(T) == 8 && L.sa) {
-        const long fo = (long)p * ncell + o.ci;
-        o.sa = L.sa[fo];
-        o.ia = L.ia[fo];
+        bool inner = true;
+#pragma unroll
+        for (int q = 0; q < ND; q++) inner = inner && o.ijk[q] > 0 && o.ijk[q] < nb - 1;
+        if (u && inner) {
+          o.sa = u[6];
+          o.ia = u[7];
+        } else {
+          const long fo = (long)p * ncell + o.ci;
+          o.sa = L.sa[fo];
+          o.ia = L.ia[fo];
+        }
         o.v = 0;
       } else {
-        o.v = c.vf[cb + o.ci];
+        o.v = u ? (T)1 : c.vf[cb + o.ci];
         o.sa = o.ia = 0.0;
       }
     };
@@ -524,12 +534,13 @@ __global__ void __launch_bounds__(kThreads, MINB) k_bhgs(Topo t, Coef<T> c, Bloc
       else
         fx = encode(ijk, nb) + s * nb * nb;
       const int ty = face_type_of(ft, f);
+      const T *u = uniform_of(c, b);
       T vc = 0, vo = 0;
       if (ty == 0) {
-        vc = c.tff[d][fb + fx];
+        vc = u ? u[d] : c.tff[d][fb + fx];
         vo = vc * same_level_ghost<T, false>(t, b, f, ijk, src, hxe);
       } else if (ty == 1) {
-        if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
+        if (t.bc_type[b * 6 + f] != kBCNeumann) vc = (u ? u[d] : c.tff[d][fb + fx]) * (T)2.0;
       } else if (ty == 2) {
         vc = cf_coef(c, t, b, d, fx, (T)1.5);
         vo = vc * fine_crse_ghost<T, ND, false>(t, b, f, ijk, src, hxe);
@@ -542,6 +553,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_bhgs(Topo t, Coef<T> c, Bloc
     }
     __syncthreads();
     const T dv = geom(c, b, 6);
+    const T *u = uniform_of(c, b);  // constant coefficients: no face or vf loads
     for (int sw = 0; sw < nsweep; sw++) {
       for (int color = 0; color < 2; color++) {
         for (int h = threadIdx.x; h < nhalf; h += blockDim.x) {
@@ -562,7 +574,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_bhgs(Topo t, Coef<T> c, Bloc
                 fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
               else
                 fx = ci + s * nb * nb;
-              const T coef = c.tff[d][fb + fx];
+              const T coef = u ? u[d] : c.tff[d][fb + fx];
               const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
               diag += coef;
               off = fma_t(coef, tile[ci + (s ? stride : -stride)], off);
@@ -575,10 +587,14 @@ __global__ void __launch_bounds__(kThreads, MINB) k_bhgs(Topo t, Coef<T> c, Bloc
           }
           T unew = 0;
           if (sizeof(T) == 8 && L.sa) {
+            bool inner = true;
+#pragma unroll
+            for (int q = 0; q < ND; q++) inner = inner && ijk[q] > 0 && ijk[q] < nb - 1;
             const long fo = (long)p * ncell + ci;
-            unew = fma_t(rhs[cb + ci], (T)L.sa[fo], off * (T)L.ia[fo]);
+            const bool ui = u && inner;
+            unew = fma_t(rhs[cb + ci], ui ? u[6] : (T)L.sa[fo], off * (ui ? u[7] : (T)L.ia[fo]));
           } else {
-            const T vfv = c.vf[cb + ci];
+            const T vfv = u ? (T)1 : c.vf[cb + ci];
             if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
           }
           tile[ci] = unew;
@@ -989,15 +1005,16 @@ int rbgs_bulk_error(bool clear) {
 // fly from their own parents, coarse neighbours (FINE_CRSE) are read as they
 // are; the red cells are then updated with the tiled sweep's arithmetic and
 // the whole tile is written.  Same values as k_prolong + k_rbgs_tile.
+// (fluid: block b is known to have vf = 1 everywhere)
 template <typename T, int ND>
 __device__ __forceinline__ T prolonged_value(const Topo &t, const Coef<T> &c, int b, const int ijk[3],
-                                             const T *__restrict__ phi, int pw = -1) {
+                                             const T *__restrict__ phi, int pw = -1, bool fluid = false) {
   const int nb = t.nb, half = nb >> 1;
   const int P = pw >= 0 ? pw >> 3 : t.parent[b], wc = pw >= 0 ? pw & 7 : t.which_child[b];
   int pc[3] = {0, 0, 0};
   for (int q = 0; q < ND; q++) pc[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
   const long q = (long)b * t.ncell + encode(ijk, nb);
-  return c.vf[q] > 0 ? phi[(long)P * t.ncell + encode(pc, nb)] : (T)0;
+  return (fluid || c.vf[q] > 0) ? phi[(long)P * t.ncell + encode(pc, nb)] : (T)0;
 }
 
 template <typename T, int ND>
@@ -1035,10 +1052,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
     const uint16_t ft = hxe ? (uint16_t)(hxe[kHXInfo] & 0xffff) : L.ftypes[p];
     const long cb = (long)b * ncell;
     const long fb = (long)b * t.nfb;
+    const T *u = uniform_of(c, b);  // constant coefficients: no face or vf loads
     for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
       int ijk[3];
       decode<ND>(i, nb, ijk);
-      tile[i] = prolonged_value<T, ND>(t, c, b, ijk, phi, hxe ? hxe[kHXPar + 6] : -1);
+      tile[i] = prolonged_value<T, ND>(t, c, b, ijk, phi, hxe ? hxe[kHXPar + 6] : -1, u != nullptr);
     }
     for (int e = threadIdx.x; e < 2 * ND * nface; e += blockDim.x) {
       const int f = e / nface, m = e - f * nface;
@@ -1062,10 +1080,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
         const int n = hxe ? hxe[f] : t.neighbor[b * 6 + f];
         int ni[3] = {ijk[0], ijk[1], ijk[2]};
         ni[d] = s ? 0 : nb - 1;
-        vc = vk = c.tff[d][fb + fx];
+        vc = vk = u ? u[d] : c.tff[d][fb + fx];
         vv = prolonged_value<T, ND>(t, c, n, ni, phi, hxe ? hxe[kHXPar + f] : -1);
       } else if (ty == 1) {
-        if (t.bc_type[b * 6 + f] != kBCNeumann) vc = c.tff[d][fb + fx] * (T)2.0;
+        if (t.bc_type[b * 6 + f] != kBCNeumann) vc = (u ? u[d] : c.tff[d][fb + fx]) * (T)2.0;
       } else if (ty == 2) {
         vc = vk = cf_coef(c, t, b, d, fx, (T)1.5);
         vv = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi, hxe);
@@ -1098,7 +1116,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
             fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
           else
             fx = ci + s * nb * nb;
-          const T coef = c.tff[d][fb + fx];
+          const T coef = u ? u[d] : c.tff[d][fb + fx];
           const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
           diag += coef;
           off = fma_t(coef, tile[ci + (s ? stride : -stride)], off);
@@ -1112,10 +1130,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
       }
       T unew = 0;
       if (sizeof(T) == 8 && L.sa) {
+        bool inner = true;
+#pragma unroll
+        for (int q = 0; q < ND; q++) inner = inner && ijk[q] > 0 && ijk[q] < nb - 1;
         const long fo = (long)p * ncell + ci;
-        unew = fma_t(rhs[cb + ci], (T)L.sa[fo], off * (T)L.ia[fo]);
+        const bool ui = u && inner;
+        unew = fma_t(rhs[cb + ci], ui ? u[6] : (T)L.sa[fo], off * (ui ? u[7] : (T)L.ia[fo]));
       } else {
-        const T vfv = c.vf[cb + ci];
+        const T vfv = u ? (T)1 : c.vf[cb + ci];
         if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
       }
       tile[ci] = unew;

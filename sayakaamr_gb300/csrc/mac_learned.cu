@@ -87,8 +87,9 @@ __device__ __forceinline__ void cell_features(const Topo &t, const Coef<float> &
 // block-local operator the loss uses: aux = [sa][dv*vf][x-face T][y-face T]
 template <int NB>
 __global__ void k_nn_pairs(Topo t, Coef<float> c, BlockList L, const float *__restrict__ r1,
-                           const double *__restrict__ sa, float *feat, float *aux, int off, int stride) {
-  constexpr int NC = NB * NB, NF = (NB + 1) * NB, AUXN = 2 * NC + 2 * NF;
+                           const float *__restrict__ err, const double *__restrict__ sa, float *feat, float *aux,
+                           int off, int stride) {
+  constexpr int NC = NB * NB, NF = (NB + 1) * NB, AUXN = 3 * NC + 2 * NF;
   __shared__ float red[NC / 32];
   // sample blockIdx.x is list entry off + blockIdx.x * stride
   const int p = off + blockIdx.x * stride, ci = threadIdx.x, o = blockIdx.x;
@@ -107,6 +108,8 @@ __global__ void k_nn_pairs(Topo t, Coef<float> c, BlockList L, const float *__re
     ax[2 * NC + k] = c.tff[0][(long)b * t.nfb + k];
     ax[2 * NC + NF + k] = c.tff[1][(long)b * t.nfb + k];
   }
+  // the error the V-cycle left (x* - x - z), block-local part, in units of s
+  ax[2 * NC + 2 * NF + ci] = local_part<NB>(c.vf[q] > 0.f ? err[q] / s : 0.f, red);
 }
 
 // (K u)_c = sum over the cell's faces of T_f (u_c - u_nb), u = 0 outside the
@@ -120,17 +123,21 @@ __device__ __forceinline__ float local_K(const float *u, const float *tx, const 
          ty[i + NB * j] * (uc - u[pc - P]) + ty[i + NB * (j + 1)] * (uc - u[pc + P]);
 }
 
-// ---- FP32 forward for training: activations and the loss gradient
-// The loss of one block is the residual the correction leaves behind under
-// the block-local operator A = D^-1 K (K symmetric: face coefficients T,
-// zero outside the block; D = dv*vf):
-//   L = inv_norm * sum (r1/s - A u)^2,  u = sa * P(y)
+// ---- FP32 forward for training: activations and the loss gradient, for
+// the correction u = sa * P(y) of one block.  Loss 0 (residual): the
+// residual the correction leaves under the block-local operator A = D^-1 K
+// (K symmetric: face coefficients T, zero outside the block; D = dv*vf):
+//   L = inv_norm * sum (r1/s - A u)^2,
 // dL/du = K (D^-1 g) with g = -2 inv_norm (r1/s - A u), dL/dy = P(sa dL/du).
+// Loss 1 (error): the distance to the block-local part of the error the
+// V-cycle left, e = P(x* - x - z) / s (stored with the pair):
+//   L = inv_norm * sum (u - e)^2,  dL/dy = P(sa * 2 inv_norm (u - e)).
 template <int NB>
 __global__ void __launch_bounds__(NB *NB) k_nn_fwd(const float *__restrict__ W, const float *__restrict__ feat,
                                                    const float *__restrict__ aux, const int *__restrict__ idx,
-                                                   float *h1g, float *h2g, float *dyg, float *loss, float inv_norm) {
-  constexpr int NC = NB * NB, P = NB + 2, PP = P * P, NF = (NB + 1) * NB, AUXN = 2 * NC + 2 * NF;
+                                                   float *h1g, float *h2g, float *dyg, float *loss, float inv_norm,
+                                                   int mode) {
+  constexpr int NC = NB * NB, P = NB + 2, PP = P * P, NF = (NB + 1) * NB, AUXN = 3 * NC + 2 * NF;
   extern __shared__ float sm[];
   float *x0 = sm;             // [3][P][P]
   float *h1 = x0 + 3 * PP;    // [32][P][P]
@@ -169,17 +176,23 @@ __global__ void __launch_bounds__(NB *NB) k_nn_fwd(const float *__restrict__ W, 
     h1g[((long)blockIdx.x * kC + co) * NC + ci] = h1[co * PP + pc];
     h2g[((long)blockIdx.x * kC + co) * NC + ci] = h2[co * PP + pc];
   }
-  const float *sav = ax, *dvvf = ax + NC, *tx = ax + 2 * NC, *ty = ax + 2 * NC + NF;
+  const float *sav = ax, *dvvf = ax + NC, *tx = ax + 2 * NC, *ty = ax + 2 * NC + NF, *tg = ax + 2 * NC + 2 * NF;
   y = local_part<NB>(y, red);
-  ut[pc] = sav[ci] * y;
-  __syncthreads();
-  const float au = dvvf[ci] > 0.f ? local_K<NB>(ut, tx, ty, i, j) / dvvf[ci] : 0.f;
-  const float res = x0[pc] - au;
-  const float gv = -2.f * inv_norm * res;
-  __syncthreads();
-  ut[pc] = dvvf[ci] > 0.f ? gv / dvvf[ci] : 0.f;
-  __syncthreads();
-  const float dldu = local_K<NB>(ut, tx, ty, i, j);
+  float res, dldu;
+  if (mode == 1) {
+    res = sav[ci] * y - tg[ci];
+    dldu = 2.f * inv_norm * res;
+  } else {
+    ut[pc] = sav[ci] * y;
+    __syncthreads();
+    const float au = dvvf[ci] > 0.f ? local_K<NB>(ut, tx, ty, i, j) / dvvf[ci] : 0.f;
+    res = x0[pc] - au;
+    const float gv = -2.f * inv_norm * res;
+    __syncthreads();
+    ut[pc] = dvvf[ci] > 0.f ? gv / dvvf[ci] : 0.f;
+    __syncthreads();
+    dldu = local_K<NB>(ut, tx, ty, i, j);
+  }
   // the projection is symmetric: the gradient goes back through it unchanged
   dyg[(long)blockIdx.x * NC + ci] = local_part<NB>(sav[ci] * dldu, red);
   float l = wsumf(res * res * inv_norm);
@@ -304,6 +317,15 @@ __global__ void k_w2_bf16(const float *W, __nv_bfloat16 *o) {
   }
 }
 
+// A forest solved with one BiCGSTAB state per problem switches the
+// correction off problem by problem: a block is left alone once its
+// problem's solve has finished or its correction has stalled.
+__device__ __forceinline__ bool nn_block_off(const BlockList &L, int b) {
+  if (!L.stc) return false;
+  const FState &q = L.stc[L.comp[b]];
+  return q.done || q.nn_off;
+}
+
 // ---- inference: r1 = resid - A corr on the tower (skipped once stalled)
 template <int ND>
 __global__ void __launch_bounds__(256) k_nn_resid(Topo t, Coef<float> c, BlockList L, const float *__restrict__ corr,
@@ -314,6 +336,7 @@ __global__ void __launch_bounds__(256) k_nn_resid(Topo t, Coef<float> c, BlockLi
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
     const int p = it / t.ncell, ci = it - p * t.ncell;
     const int b = L.blocks[p];
+    if (nn_block_off(L, b)) continue;
     const long q = (long)b * t.ncell + ci;
     const float a = stencil::apply_cell<float, ND>(t, c, b, L.ftypes[p], ci, corr);
     r1[q] = c.vf[q] > 0 ? resid[q] - a : 0.f;
@@ -406,9 +429,172 @@ __device__ __forceinline__ float nn_tail_bf16(const float *__restrict__ W, const
   return y;
 }
 
+// ---- the 32 -> 32 layer of 16x16 blocks on the 5th-generation tensor
+// cores (tcgen05.mma, accumulator in tensor memory).  The layer is an
+// implicit GEMM over the block's padded 18x18 pixel grid,
+//   D[pixel][out] = sum over taps t, channels k of h1[pixel + off_t][k] * W_t[out][k],
+// with the rows taken on the padded grid itself (halo columns included), so
+// that every tap's A operand is one shared-memory matrix shifted by off_t
+// pixels and no im2col copy is made.  Three M = 128 tiles cover the
+// interior pixels 19 .. 304; rows that fall on halo pixels are discarded.
+// h1 and the weights are stored in the canonical no-swizzle K-major layout:
+// [channel chunk of 8][row][8 channels] BF16, so that one core matrix (8
+// rows x 16 bytes) is contiguous, 8-row groups are SBO = 128 bytes apart and
+// channel chunks LBO = rows * 16 bytes apart.  One thread issues the 54 MMAs
+// (3 tiles x 9 taps x 2 K-steps of 16); their completion arrives on an
+// mbarrier; each warp then reads its lane quarter of the accumulators with
+// tcgen05.ld.  Every wait is bounded: on a timeout the kernel raises
+// g_nn_err, waits (bounded) once more and frees its tensor memory.
+namespace tc05 {
+constexpr int P = 18, PP = P * P;
+constexpr int kRow0 = P + 1;      // first interior pixel
+constexpr int kTiles = 3;         // M = 128 tiles from kRow0
+constexpr int kPixA = 424;        // rows of the A matrix: >= kRow0 + 3*128 + P + 1, a multiple of 8
+constexpr int kCols = 128;        // tensor-memory columns: 3 tiles x 32 (power of two)
+constexpr uint32_t kLboA = kPixA * 16, kLboB = kC * 16, kSbo = 128;
+// instruction descriptor of kind::f16: FP32 accumulator (bit 4), BF16 A and
+// B (bits 7, 10), both K-major, N = 32 (bits 17-22: N >> 3), M = 128
+// (bits 24-28: M >> 4)
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kC >> 3) << 17) | ((128u >> 4) << 24);
+constexpr long kWaitLimit = 1l << 22;
+
+// shared-memory matrix descriptor, no swizzle (bits 0-13 address >> 4,
+// 16-29 LBO >> 4, 32-45 SBO >> 4, bit 46 the descriptor version)
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (long i = 0; i < kWaitLimit; i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+}  // namespace tc05
+
+__device__ int g_nn_err;  // a tensor-core wait timed out (read and cleared by the host)
+
+template <int NB>
+constexpr size_t tc_smem() {
+  return sizeof(float) * (3 * tc05::PP + 1232 + kC * tc05::PP) + 128 + (size_t)4 * tc05::kPixA * 16 +
+         (size_t)9 * 4 * kC * 16 + 64;
+}
+
+// the tcgen05 form of nn_tail_bf16 for 16x16 blocks (same inputs, same
+// output; the hidden layer's products are summed in another order)
+__device__ __forceinline__ float nn_tail_tc05(const float *__restrict__ W, const __nv_bfloat16 *__restrict__ w2bf,
+                                              float *x0, unsigned char *rest) {
+  using namespace tc05;
+  constexpr int NB = 16;
+  float *ws = reinterpret_cast<float *>(rest);  // w1, b1 | b2 | w3, b3 (1217 floats, 1232 reserved)
+  float *w1 = ws, *b1 = ws + kC * kCin * 9, *b2 = b1 + kC, *w3 = b2 + kC, *b3 = w3 + kC * 9;
+  float *h2 = ws + 1232;  // [32][PP] FP32
+  unsigned char *base = reinterpret_cast<unsigned char *>(h2 + kC * PP);
+  base += (128 - (smem_u32(base) & 127)) & 127;  // 128-byte aligned operand area
+  __nv_bfloat16 *ha = reinterpret_cast<__nv_bfloat16 *>(base);                    // [4][kPixA][8]
+  __nv_bfloat16 *wb = reinterpret_cast<__nv_bfloat16 *>(base + 4 * kPixA * 16);  // [9][4][32][8]
+  uint64_t *bar = reinterpret_cast<uint64_t *>(base + 4 * kPixA * 16 + 9 * 4 * kC * 16);
+  uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
+  const int ci = threadIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int pc = (ci / NB + 1) * P + (ci % NB + 1);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  for (int k = threadIdx.x; k < kC * kCin * 9 + kC; k += blockDim.x) ws[k] = W[kOW1 + k];
+  for (int k = threadIdx.x; k < kC; k += blockDim.x) b2[k] = W[kOB2 + k];
+  for (int k = threadIdx.x; k < kC * 9 + 1; k += blockDim.x) w3[k] = W[kOW3 + k];
+  // w2bf is [tap][out][in]; wb is [tap][in / 8][out][in % 8]
+  for (int k = threadIdx.x; k < 9 * kC * kC; k += blockDim.x) {
+    const int tp = k / (kC * kC), o = (k / kC) % kC, i = k % kC;
+    wb[((tp * 4 + (i >> 3)) * kC + o) * 8 + (i & 7)] = w2bf[k];
+  }
+  for (int k = threadIdx.x; k < 4 * kPixA * 8 / 2; k += blockDim.x) reinterpret_cast<uint32_t *>(ha)[k] = 0u;
+  for (int k = threadIdx.x; k < kC * PP; k += blockDim.x) h2[k] = 0.f;
+  __syncthreads();
+  // input layer (FP32) -> BF16 A matrix
+  for (int co = 0; co < kC; co++) {
+    float a = b1[co];
+    for (int cin = 0; cin < kCin; cin++)
+      for (int tp = 0; tp < 9; tp++) a += w1[(co * kCin + cin) * 9 + tp] * x0[cin * PP + pc + (tp / 3 - 1) * P + (tp % 3 - 1)];
+    ha[((co >> 3) * kPixA + pc) * 8 + (co & 7)] = __float2bfloat16_rn(fmaxf(a, 0.f));
+  }
+  // generic-proxy writes of the operands made visible to the tensor core
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *slot;
+  if (threadIdx.x == 0) {
+    const uint32_t a0 = smem_u32(ha), b0 = smem_u32(wb);
+    for (int t = 0; t < kTiles; t++)
+      for (int tp = 0; tp < 9; tp++) {
+        const int off = (tp / 3 - 1) * P + (tp % 3 - 1);
+        for (int kh = 0; kh < 2; kh++) {
+          const uint64_t ad = sdesc(a0 + (uint32_t)(kRow0 + 128 * t + off) * 16 + kh * 2 * kLboA, kLboA, kSbo);
+          const uint64_t bd = sdesc(b0 + (uint32_t)tp * 4 * kC * 16 + kh * 2 * kLboB, kLboB, kSbo);
+          const uint32_t acc = (tp | kh) ? 1u : 0u;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem + 32 * t),
+              "l"(ad), "l"(bd), "r"(kIdesc), "r"(acc));
+        }
+      }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+  }
+  bool ok = mbar_wait(smem_u32(bar), 0);
+  if (!ok) {
+    if (threadIdx.x == 0) atomicExch(&g_nn_err, 1);
+    ok = mbar_wait(smem_u32(bar), 0) && false;  // drain (bounded), the results are not used
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    const int q = warp & 3;
+    for (int t = warp < 4 ? 0 : 1; t < kTiles; t += 2) {
+      uint32_t r[32];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+          "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(tmem + ((uint32_t)(32 * q) << 16) + 32 * t));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      const int pix = kRow0 + 128 * t + 32 * q + lane;
+      const int py = pix / P, px = pix - py * P;
+      if (py >= 1 && py <= NB && px >= 1 && px <= NB)
+        for (int n = 0; n < kC; n++) h2[n * PP + pix] = fmaxf(__uint_as_float(r[n]) + b2[n], 0.f);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
+  }
+  float y = b3[0];
+  for (int cin = 0; cin < kC; cin++)
+    for (int tp = 0; tp < 9; tp++) y += w3[cin * 9 + tp] * h2[cin * PP + pc + (tp / 3 - 1) * P + (tp % 3 - 1)];
+  return y;
+}
+
 // inference inside the solve: corr += s * sa * net(features of r1), one CTA
 // per block of the finest tower, one thread per cell
-template <int NB>
+template <int NB, bool TC = false>
 __global__ void __launch_bounds__(NB *NB) k_nn_infer(Topo t, Coef<float> c, BlockList L, const float *__restrict__ W,
                                                      const __nv_bfloat16 *__restrict__ w2bf,
                                                      const float *__restrict__ r1, const double *__restrict__ sa,
@@ -420,6 +606,7 @@ __global__ void __launch_bounds__(NB *NB) k_nn_infer(Topo t, Coef<float> c, Bloc
   if (st->done || st->nn_off) return;
   const int p = blockIdx.x, ci = threadIdx.x, pc = (ci / NB + 1) * P + (ci % NB + 1);
   const int b = L.blocks[p];
+  if (nn_block_off(L, b)) return;  // uniform over the CTA
   const long q = (long)b * NC + ci;
   for (int k = threadIdx.x; k < 3 * PP; k += blockDim.x) x0[k] = 0.f;
   const float rv = r1[q];
@@ -428,12 +615,17 @@ __global__ void __launch_bounds__(NB *NB) k_nn_infer(Topo t, Coef<float> c, Bloc
   float f[3];
   cell_features<NB>(t, c, b, ci, rv, s, f);
   for (int k = 0; k < 3; k++) x0[k * PP + pc] = f[k];
-  const float y = local_part<NB>(nn_tail_bf16<NB>(W, w2bf, x0, smraw + 3 * PP * sizeof(float)), red);
+  float y0;
+  if constexpr (TC)
+    y0 = nn_tail_tc05(W, w2bf, x0, smraw + 3 * PP * sizeof(float));
+  else
+    y0 = nn_tail_bf16<NB>(W, w2bf, x0, smraw + 3 * PP * sizeof(float));
+  const float y = local_part<NB>(y0, red);
   corr[q] += s * (float)sa[(long)p * NC + ci] * y;
 }
 
 // the tensor-core forward on explicit feature blocks (test hook)
-template <int NB>
+template <int NB, bool TC = false>
 __global__ void __launch_bounds__(NB *NB) k_nn_forward(const float *__restrict__ W,
                                                        const __nv_bfloat16 *__restrict__ w2bf,
                                                        const float *__restrict__ feat, float *__restrict__ y) {
@@ -444,12 +636,15 @@ __global__ void __launch_bounds__(NB *NB) k_nn_forward(const float *__restrict__
   for (int k = threadIdx.x; k < 3 * PP; k += blockDim.x) x0[k] = 0.f;
   __syncthreads();
   for (int k = 0; k < 3; k++) x0[k * PP + pc] = feat[((long)blockIdx.x * 3 + k) * NC + ci];
-  y[(long)blockIdx.x * NC + ci] = nn_tail_bf16<NB>(W, w2bf, x0, smraw + 3 * PP * sizeof(float));
+  if constexpr (TC)
+    y[(long)blockIdx.x * NC + ci] = nn_tail_tc05(W, w2bf, x0, smraw + 3 * PP * sizeof(float));
+  else
+    y[(long)blockIdx.x * NC + ci] = nn_tail_bf16<NB>(W, w2bf, x0, smraw + 3 * PP * sizeof(float));
 }
 
 template <int NB>
 constexpr size_t fwd_smem() {
-  return sizeof(float) * ((3 + 2 * kC) * (NB + 2) * (NB + 2) + kNParam + 2 * NB * NB + 2 * (NB + 1) * NB +
+  return sizeof(float) * ((3 + 2 * kC) * (NB + 2) * (NB + 2) + kNParam + 3 * NB * NB + 2 * (NB + 1) * NB +
                           (NB + 2) * (NB + 2));
 }
 template <int NB>
@@ -464,6 +659,17 @@ constexpr size_t infer_smem() {
 
 }  // namespace
 
+// the tensor-core wait error word (g_nn_err): its value, cleared when asked
+int nn_tc_error(bool clear) {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_nn_err, sizeof(int)) != cudaSuccess) return -1;
+  if (clear && v) {
+    const int z = 0;
+    if (cudaMemcpyToSymbol(g_nn_err, &z, sizeof(int)) != cudaSuccess) return -1;
+  }
+  return v;
+}
+
 static void set_smem_attrs() {
   ensure_max_smem((const void *)k_nn_fwd<16>, (int)fwd_smem<16>());
   ensure_max_smem((const void *)k_nn_bwd<16>, (int)bwd_smem<16>());
@@ -473,6 +679,8 @@ static void set_smem_attrs() {
   ensure_max_smem((const void *)k_nn_infer<8>, (int)infer_smem<8>());
   ensure_max_smem((const void *)k_nn_forward<16>, (int)infer_smem<16>());
   ensure_max_smem((const void *)k_nn_forward<8>, (int)infer_smem<8>());
+  ensure_max_smem((const void *)k_nn_infer<16, true>, (int)tc_smem<16>());
+  ensure_max_smem((const void *)k_nn_forward<16, true>, (int)tc_smem<16>());
 }
 
 // ---------------------------------------------------------------------------
@@ -673,10 +881,11 @@ int MacGpu::learned_collect(int max_iters, int max_samples) {
     const long o = (long)ls_.nsamp * ncell_, oa = (long)ls_.nsamp * aux_len();
     if (cnt > 0) {
       if (tt_.nb == 16)
-        k_nn_pairs<16><<<cnt, 256, 0, stream_>>>(topo_, c32_, TL, r1, sa, ls_.feat + 3 * o, ls_.aux + oa, off,
+        k_nn_pairs<16><<<cnt, 256, 0, stream_>>>(topo_, c32_, TL, r1, e, sa, ls_.feat + 3 * o, ls_.aux + oa, off,
                                                  stride);
       else
-        k_nn_pairs<8><<<cnt, 64, 0, stream_>>>(topo_, c32_, TL, r1, sa, ls_.feat + 3 * o, ls_.aux + oa, off, stride);
+        k_nn_pairs<8><<<cnt, 64, 0, stream_>>>(topo_, c32_, TL, r1, e, sa, ls_.feat + 3 * o, ls_.aux + oa, off,
+                                               stride);
       CKR_(cudaGetLastError(), -1);
     }
     ls_.nsamp += cnt;
@@ -698,11 +907,11 @@ float MacGpu::learned_grad(const int *d_idx, int nblk, float inv_norm, float *h1
   CKR_(cudaMemsetAsync(ls_.loss, 0, sizeof(float), stream_), 0.f);
   if (ls_.nb == 16) {
     k_nn_fwd<16><<<nblk, 256, fwd_smem<16>(), stream_>>>(ls_.w, ls_.feat, ls_.aux, d_idx, h1, h2, dy,
-                                                         ls_.loss, inv_norm);
+                                                         ls_.loss, inv_norm, prm_.learned_loss);
     k_nn_bwd<16><<<nblk, 256, bwd_smem<16>(), stream_>>>(ls_.w, ls_.feat, d_idx, h1, h2, dy, ls_.g);
   } else {
     k_nn_fwd<8><<<nblk, 64, fwd_smem<8>(), stream_>>>(ls_.w, ls_.feat, ls_.aux, d_idx, h1, h2, dy,
-                                                      ls_.loss, inv_norm);
+                                                      ls_.loss, inv_norm, prm_.learned_loss);
     k_nn_bwd<8><<<nblk, 64, bwd_smem<8>(), stream_>>>(ls_.w, ls_.feat, d_idx, h1, h2, dy, ls_.g);
   }
   CKR_(cudaGetLastError(), 0.f);
@@ -808,15 +1017,23 @@ int MacGpu::learned_forward(const float *feat, int n, float *y) {
     return -1;
   }
   CKR_(cudaMemcpyAsync(df, feat, (size_t)n * 3 * nc * sizeof(float), cudaMemcpyHostToDevice, stream_), -1);
-  if (ls_.nb == 16)
-    k_nn_forward<16><<<n, 256, infer_smem<16>(), stream_>>>(ls_.w, (const __nv_bfloat16 *)ls_.w2bf, df, dy);
-  else
+  if (ls_.nb == 16) {
+    if (prm_.learned_tc05)
+      k_nn_forward<16, true><<<n, 256, tc_smem<16>(), stream_>>>(ls_.w, (const __nv_bfloat16 *)ls_.w2bf, df, dy);
+    else
+      k_nn_forward<16><<<n, 256, infer_smem<16>(), stream_>>>(ls_.w, (const __nv_bfloat16 *)ls_.w2bf, df, dy);
+  } else {
     k_nn_forward<8><<<n, 64, infer_smem<8>(), stream_>>>(ls_.w, (const __nv_bfloat16 *)ls_.w2bf, df, dy);
+  }
   CKR_(cudaGetLastError(), -1);
   CKR_(cudaMemcpyAsync(y, dy, (size_t)n * nc * sizeof(float), cudaMemcpyDeviceToHost, stream_), -1);
   CKR_(cudaStreamSynchronize(stream_), -1);
   cudaFree(df);
   cudaFree(dy);
+  if (nn_tc_error(true) > 0) {
+    fail("learned correction: a tensor-core wait timed out");
+    return -1;
+  }
   return 0;
 }
 
@@ -848,8 +1065,12 @@ void MacGpu::learned_apply(float *resid, float *corr) {
   launch_k(false, k_nn_resid<2>, lgrid(w), 256, 0, stream_, topo_, c32_, TL, (const float *)corr,
            (const float *)resid, ls_.r1, (const FState *)d_st_);
   if (ls_.nb == 16)
-    launch_k(false, k_nn_infer<16>, TL.n, 256, infer_smem<16>(), stream_, topo_, c32_, TL, (const float *)ls_.w,
-             (const __nv_bfloat16 *)ls_.w2bf, (const float *)ls_.r1, sa, corr, (const FState *)d_st_);
+    if (prm_.learned_tc05)
+      launch_k(false, k_nn_infer<16, true>, TL.n, 256, tc_smem<16>(), stream_, topo_, c32_, TL, (const float *)ls_.w,
+               (const __nv_bfloat16 *)ls_.w2bf, (const float *)ls_.r1, sa, corr, (const FState *)d_st_);
+    else
+      launch_k(false, k_nn_infer<16>, TL.n, 256, infer_smem<16>(), stream_, topo_, c32_, TL, (const float *)ls_.w,
+               (const __nv_bfloat16 *)ls_.w2bf, (const float *)ls_.r1, sa, corr, (const FState *)d_st_);
   else
     launch_k(false, k_nn_infer<8>, TL.n, 64, infer_smem<8>(), stream_, topo_, c32_, TL, (const float *)ls_.w,
              (const __nv_bfloat16 *)ls_.w2bf, (const float *)ls_.r1, sa, corr, (const FState *)d_st_);

@@ -56,4 +56,8 @@ struct LearnedState {
   bool trained = false;
 };
 
+// error word of the tcgen05 inference (a tensor-core wait timed out):
+// 1 if raised since the last clear, -1 on a CUDA error
+int nn_tc_error(bool clear);
+
 }  // namespace sayaka_gb300

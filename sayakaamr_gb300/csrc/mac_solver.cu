@@ -518,6 +518,9 @@ MacGpu::~MacGpu() {
   for (auto &q : d_face_) fr(q);
   learned_free();
   fr(d_opS_);
+  free_coef_lists();
+  fr(d_uni64_);
+  fr(d_uni32_);
   fr(d_cnt_);
   bottom_free();
   fr(d_phases_);
@@ -596,7 +599,13 @@ void MacGpu::set_scalars(double alpha, double beta) {
   beta_ = beta;
   c64_.alpha = alpha;
   c64_.beta = beta;
-  upload_coefs();
+  if (!coef_uploaded_) {  // the initial coefficients (B = 1, fractions 1)
+    upload_coefs();
+    coef_uploaded_ = true;
+    return;
+  }
+  recompute_face_coef();
+  coef_version_++;
 }
 
 void MacGpu::upload_coefs() {
@@ -625,206 +634,6 @@ void MacGpu::recompute_face_coef() {
   launch_face_coef<double>(topo_, d_geom_, b, a, beta_, o, stream_);
 }
 
-// index helpers for host-side face/cell restriction
-static inline int cell_index(int i, int j, int k, int nb) { return i + nb * (j + nb * k); }
-static inline int face_idx(int d, int i, int j, int k, int nb) {
-  const int e0 = nb + (d == 0), e1 = nb + (d == 1);
-  return i + e0 * (j + e1 * k);
-}
-
-// FLUX_SYNC_AVG of face data at coarse/fine faces of the finest tower
-// (src/SayakaTower.cpp:298-415): fine face values are averaged into the
-// parent's face, then copied to the coarse neighbour's matching face.
-void MacGpu::sync_face_avg_host(int dir, std::vector<double> &F) const {
-  const int nd = tt_.ndim, nb = tt_.nb, half = nb / 2;
-  const DevTower &tw = towers_[finest_];
-  const double scale = nd == 3 ? 0.25 : 0.5;
-  const int kz = nd == 3 ? 1 : 0;
-  for (int l = finest_; l >= 2; l--) {
-    // fine level: restrict FINE_CRSE faces into the parent
-    for (int p = tw.begin[l]; p < tw.end[l]; p++) {
-      const int b = tw.blocks[p];
-      for (int side = 0; side <= 1; side++) {
-        const int f = 2 * dir + side;
-        const int nbr = tt_.neighbor[b * 6 + f];
-        if (!(nbr < 0 && nbr > kPhysBndry)) continue;  // not FINE_CRSE
-        const int P = tt_.parent[b], wc = tt_.which_child[b];
-        int off[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-        for (int q = 0; q < nd; q++) {
-          off[q] = ((wc >> q) & 1) * half;
-          lo[q] = off[q];
-          hi[q] = off[q] + half - 1;
-        }
-        // boundary face of the child's sub-box on `side`
-        lo[dir] = hi[dir] = side == 0 ? off[dir] : off[dir] + half;
-        for (int k = lo[2]; k <= hi[2]; k++)
-          for (int j = lo[1]; j <= hi[1]; j++)
-            for (int i = lo[0]; i <= hi[0]; i++) {
-              const int cc[3] = {i, j, k};
-              double val = 0;
-              const int t0 = dir == 0 ? 1 : 0;
-              const int t1 = dir == 2 ? 1 : 2;
-              for (int a1 = 0; a1 <= (nd == 3 ? 1 : 0); a1++)
-                for (int a0 = 0; a0 <= 1; a0++) {
-                  int fi[3];
-                  fi[dir] = 2 * (cc[dir] - off[dir]);
-                  fi[t0] = 2 * (cc[t0] - off[t0]) + a0;
-                  if (nd == 3) fi[t1] = 2 * (cc[t1] - off[t1]) + a1;
-                  else fi[2] = 0;
-                  if (nd == 2 && t0 == 2) continue;
-                  val += F[(size_t)b * nfb_ + face_idx(dir, fi[0], fi[1], fi[2], nb)];
-                }
-              F[(size_t)P * nfb_ + face_idx(dir, i, j, k, nb)] = val * scale;
-            }
-        (void)kz;
-      }
-    }
-    // coarse level: copy into CRSE_FINE faces
-    for (int p = tw.begin[l - 1]; p < tw.end[l - 1]; p++) {
-      const int b = tw.blocks[p];
-      for (int side = 0; side <= 1; side++) {
-        const int f = 2 * dir + side;
-        const int nbr = tt_.neighbor[b * 6 + f];
-        if (!(nbr >= 0 && tt_.node_type[nbr] != kNodeLeaf)) continue;
-        // CRSE_FINE only when the coarse block sits below the tower level
-        if (l - 1 >= finest_) continue;
-        int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-        for (int q = 0; q < nd; q++) hi[q] = nb - 1;
-        for (int k = lo[2]; k <= hi[2]; k++)
-          for (int j = lo[1]; j <= hi[1]; j++)
-            for (int i = lo[0]; i <= hi[0]; i++) {
-              int di[3] = {i, j, k}, si[3] = {i, j, k};
-              if (((dir == 0) && i != 0) || ((dir == 1) && j != 0) || ((dir == 2) && k != 0)) continue;
-              di[dir] = side == 0 ? 0 : nb;
-              si[dir] = side == 0 ? nb : 0;
-              F[(size_t)b * nfb_ + face_idx(dir, di[0], di[1], di[2], nb)] =
-                  F[(size_t)nbr * nfb_ + face_idx(dir, si[0], si[1], si[2], nb)];
-            }
-      }
-    }
-  }
-}
-
-// AVG restriction of face data onto non-leaf blocks, finest-1 .. 1
-// (src/SayakaFillPatch.cpp:401-447 with src/SayakaInterpPatch.cpp:627-691)
-void MacGpu::restrict_face_avg_host(int dir, std::vector<double> &F) const {
-  const int nd = tt_.ndim, nb = tt_.nb, half = nb / 2;
-  const double scale = nd == 3 ? 0.25 : 0.5;
-  for (int l = finest_ - 1; l >= 1; l--) {
-    for (int b : nonleaf_blocks_[l]) {
-      for (int c = 0; c < (1 << nd); c++) {
-        const int C = tt_.child[b * 8 + c];
-        int off[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-        for (int q = 0; q < nd; q++) {
-          off[q] = ((c >> q) & 1) * half;
-          lo[q] = off[q];
-          hi[q] = off[q] + half - 1;
-        }
-        hi[dir] += 1;  // staggered in dir
-        for (int k = lo[2]; k <= hi[2]; k++)
-          for (int j = lo[1]; j <= hi[1]; j++)
-            for (int i = lo[0]; i <= hi[0]; i++) {
-              const int cc[3] = {i, j, k};
-              double val = 0;
-              const int t0 = dir == 0 ? 1 : 0;
-              const int t1 = dir == 2 ? 1 : 2;
-              for (int a1 = 0; a1 <= (nd == 3 ? 1 : 0); a1++)
-                for (int a0 = 0; a0 <= 1; a0++) {
-                  int fi[3];
-                  fi[dir] = 2 * (cc[dir] - off[dir]);
-                  fi[t0] = 2 * (cc[t0] - off[t0]) + a0;
-                  if (nd == 3) fi[t1] = 2 * (cc[t1] - off[t1]) + a1;
-                  else fi[2] = 0;
-                  val += F[(size_t)C * nfb_ + face_idx(dir, fi[0], fi[1], fi[2], nb)];
-                }
-              F[(size_t)b * nfb_ + face_idx(dir, i, j, k, nb)] = val * scale;
-            }
-      }
-    }
-  }
-}
-
-// AVG restriction of cell data onto non-leaf blocks, finest-1 .. 1
-void MacGpu::restrict_cell_avg_host(std::vector<double> &V) const {
-  const int nd = tt_.ndim, nb = tt_.nb, half = nb / 2;
-  const double wgt = 1.0 / (1 << nd);
-  for (int l = finest_ - 1; l >= 1; l--) {
-    for (int b : nonleaf_blocks_[l]) {
-      for (int k = 0; k < (nd == 3 ? nb : 1); k++)
-        for (int j = 0; j < nb; j++)
-          for (int i = 0; i < nb; i++) {
-            const int ijk[3] = {i, j, k};
-            int c = 0, fb[3] = {0, 0, 0};
-            for (int q = 0; q < nd; q++) {
-              const int s = ijk[q] >= half;
-              c |= s << q;
-              fb[q] = 2 * (ijk[q] - s * half);
-            }
-            const int C = tt_.child[b * 8 + c];
-            double sum = 0;
-            for (int kk = 0; kk < (nd == 3 ? 2 : 1); kk++)
-              for (int jj = 0; jj < 2; jj++)
-                for (int ii = 0; ii < 2; ii++)
-                  sum += V[(size_t)C * ncell_ + cell_index(fb[0] + ii, fb[1] + jj, fb[2] + kk, nb)];
-            V[(size_t)b * ncell_ + cell_index(i, j, k, nb)] = sum * wgt;
-          }
-    }
-  }
-}
-
-void MacGpu::set_coef_b_leaf(int dir, const double *face_all) {
-  std::vector<double> &B = bcoef_[dir];
-  const DevTower &tw = towers_[finest_];
-  for (int b : tw.blocks) std::memcpy(&B[(size_t)b * nfb_], &face_all[(size_t)b * nfb_], nfb_ * sizeof(double));
-  sync_face_avg_host(dir, B);
-  restrict_face_avg_host(dir, B);
-  upload_coefs();
-}
-
-void MacGpu::set_ib_frac_leaf(const double *vol_all, const double *const area_all[3]) {
-  const DevTower &tw = towers_[finest_];
-  for (int b : tw.blocks) {
-    std::memcpy(&vf_[(size_t)b * ncell_], &vol_all[(size_t)b * ncell_], ncell_ * sizeof(double));
-    for (int d = 0; d < tt_.ndim; d++)
-      std::memcpy(&afrac_[d][(size_t)b * nfb_], &area_all[d][(size_t)b * nfb_], nfb_ * sizeof(double));
-  }
-  for (int d = 0; d < tt_.ndim; d++) sync_face_avg_host(d, afrac_[d]);
-  restrict_cell_avg_host(vf_);
-  for (int d = 0; d < tt_.ndim; d++) restrict_face_avg_host(d, afrac_[d]);
-  upload_coefs();
-}
-
-// binary fractions from a level set with >= 1 ghost layer, ls <= 0 solid
-// (src/SayakaMacIB.cpp:99-154)
-void MacGpu::set_ib_frac_by_ls(const double *ls, int ng) {
-  const int nd = tt_.ndim, nb = tt_.nb;
-  const int G = nb + 2 * ng;
-  const size_t gsz = nd == 3 ? (size_t)G * G * G : (size_t)G * G;
-  auto L = [&](int b, int i, int j, int k) {
-    return ls[(size_t)b * gsz + (i + ng) + (size_t)G * ((j + ng) + (size_t)G * (nd == 3 ? k + ng : 0))];
-  };
-  std::vector<double> vol(vf_);
-  std::vector<double> area[3];
-  for (int d = 0; d < nd; d++) area[d] = afrac_[d];
-  const DevTower &tw = towers_[finest_];
-  for (int b : tw.blocks) {
-    for (int k = 0; k < (nd == 3 ? nb : 1); k++)
-      for (int j = 0; j < nb; j++)
-        for (int i = 0; i < nb; i++) vol[(size_t)b * ncell_ + cell_index(i, j, k, nb)] = L(b, i, j, k) <= 0 ? 0.0 : 1.0;
-    for (int d = 0; d < nd; d++) {
-      const int ii = d == 0, jj = d == 1, kk = d == 2;
-      for (int k = 0; k < (nd == 3 ? nb + kk : 1); k++)
-        for (int j = 0; j < nb + jj; j++)
-          for (int i = 0; i < nb + ii; i++) {
-            const bool solid = L(b, i - ii, j - jj, k - kk) <= 0 || L(b, i, j, k) <= 0;
-            area[d][(size_t)b * nfb_ + face_idx(d, i, j, k, nb)] = solid ? 0.0 : 1.0;
-          }
-    }
-  }
-  const double *ap[3] = {area[0].data(), nd >= 2 ? area[1].data() : nullptr, nd == 3 ? area[2].data() : nullptr};
-  set_ib_frac_leaf(vol.data(), ap);
-}
-
 void MacGpu::set_bc_types(const int *bc6) {
   for (int b = 0; b < tt_.num_blocks; b++)
     for (int f = 0; f < 6; f++) {
@@ -835,7 +644,8 @@ void MacGpu::set_bc_types(const int *bc6) {
   coef_version_++;
 }
 
-void MacGpu::get_coef(int which, int dir, double *out) const {
+void MacGpu::get_coef(int which, int dir, double *out) {
+  pull_coefs();
   if (which == 0)
     std::memcpy(out, bcoef_[dir].data(), bcoef_[dir].size() * sizeof(double));
   else if (which == 1)

@@ -47,6 +47,15 @@ struct SolverParams {
                               // per colour); 1 = block-hybrid passes (n_post per tower, each one launch of
                               // inner_sweeps red-black sweeps per block, Jacobi between blocks)
   int inner_sweeps = 2;       // smoother 1: red-black sweeps per block in one pass
+  int learned_loss = 1;       // training loss of the learned correction: 0 = the block-local residual it
+                              // leaves, 1 = its distance to the error the V-cycle left (block-local part)
+  int learned_tc05 = 1;       // learned correction of 16x16 blocks: 1 = hidden layer on tcgen05 (tensor memory
+                              // accumulator), 0 = on mma.sync (the same network; products summed in another order)
+  int bottom_refresh = 1;     // device path: 1 = the dense bottom inverse is rebuilt after every coefficient
+                              // change; 0 = kept from the last build until the tree or the bottom level changes
+                              // (a fixed, slightly stale coarsest-level solve inside the preconditioner)
+  int uniform = 1;            // device path: constant-coefficient blocks read their face coefficients from a
+                              // per-block record (same results; 0 = every block reads the face arrays)
   int per_problem = 1;        // device path, a tree of several independent problems (connected components):
                               // 1 = one BiCGSTAB state per problem, each stopping at its own tolerance;
                               // 0 = one state shared by all
@@ -82,7 +91,7 @@ class MacGpu {
   void set_ib_frac_leaf(const double *vol_all, const double *const area_all[3]);  // src/SayakaMacIB.cpp:34-97
   void set_ib_frac_by_ls(const double *ls_grown, int ngrow);   // binary fractions from a level set
   void set_bc_types(const int *bc6);                            // math BC per block face (-1 interior)
-  void get_coef(int which, int dir, double *out_all) const;     // 0 B, 1 area frac, 2 vol frac
+  void get_coef(int which, int dir, double *out_all);           // 0 B, 1 area frac, 2 vol frac
 
   // user vectors (compact, all blocks)
   void set_rhs(const double *all, bool on_device = false);
@@ -119,6 +128,7 @@ class MacGpu {
   // iterations and final relative residual |r|/|r0|; returns the problem
   // count, or -1 when the last solve shared one state
   int problem_states(int *iterations, double *rel_resid, int n);
+  int uniform_blocks();  // constant-coefficient blocks (after preparing the device solve)
   int device() const { return device_; }
 
   // building blocks, exposed for parity tests (compact arrays, all blocks)
@@ -136,7 +146,7 @@ class MacGpu {
   int learned_collect(int max_iters, int max_samples = 0);  // max_samples 0: every block of every iterate
   float learned_train(int epochs, float lr, int batch, unsigned seed);
   float learned_loss_grad(const float *feat, const float *aux, int n, float *grad);
-  int aux_len() const { return 2 * tt_.nb * tt_.nb + 2 * (tt_.nb + 1) * tt_.nb; }
+  int aux_len() const { return 3 * tt_.nb * tt_.nb + 2 * (tt_.nb + 1) * tt_.nb; }
   int learned_forward(const float *feat, int n, float *y);
   int learned_set_weights(const float *w, int n);
   int learned_get_weights(float *w, int n);
@@ -195,9 +205,22 @@ class MacGpu {
 
   void upload_coefs();
   void recompute_face_coef();
-  void sync_face_avg_host(int dir, std::vector<double> &face) const;
-  void restrict_face_avg_host(int dir, std::vector<double> &face) const;
-  void restrict_cell_avg_host(std::vector<double> &cell) const;
+  // coefficient averaging on the device (mac_coef.cu)
+  void build_coef_lists();
+  void free_coef_lists();
+  void coef_average(int dmask, double *const F[3], double *V);
+  void coef_changed();
+  void pull_coefs(const std::vector<int> *blocks = nullptr);
+  std::vector<int *> d_sync_up_, d_sync_copy_;
+  std::vector<int> n_sync_up_, n_sync_copy_;
+  bool coef_lists_ = false;
+  bool coef_uploaded_ = false;    // the initial coefficients are on the device
+  // the bottom solve's arrays were allocated for this level, size and form
+  int bot_built_level_ = -1, bot_built_half_ = -1;
+  long long bot_built_tot_ = -1;
+  bool host_coef_stale_ = false;  // bcoef_/afrac_/vf_ behind the device arrays
+  double *d_ls_ = nullptr;        // level set staged for set_ib_frac_by_ls
+  size_t ls_cap_ = 0;
 
   // vector ops over a block list (FP64)
   void vcopy(const BlockList &L, double *dst, const double *src);
@@ -318,6 +341,13 @@ class MacGpu {
   FState *d_st_ = nullptr, *h_st_ = nullptr;
   double *d_part_ = nullptr;
   double *d_opP_ = nullptr, *d_opS_ = nullptr;  // factors of the device solve's operator
+  // constant-coefficient block records (Coef::ut) and the FP64 coefficients
+  // the device solve's kernels read (c64_ with the records when enabled)
+  double *d_uni64_ = nullptr;
+  float *d_uni32_ = nullptr;
+  Coef<double> cd64_{};
+  void build_uniform();
+  void bind_uniform();
   std::vector<double *> d_sfac_;                // FP64 smoother factors per tower: sa then ia
   std::vector<double *> d_pfac_;                // the same for the parity-grouped tower lists
   std::vector<double *> d_face_;                // face fields of the projection step (u, w, flux)
@@ -351,7 +381,7 @@ class MacGpu {
   int graph_prec_ = -1, graph_npost_ = -1;
   int kernels_per_iter_ = 0;
   int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1, graph_nn_ = -1, graph_order_ = -1;
-  int graph_smoother_ = -1, graph_inner_ = -1, graph_multi_ = -1;
+  int graph_smoother_ = -1, graph_inner_ = -1, graph_multi_ = -1, graph_uniform_ = -1;
   bool last_multi_ = false;  // the last device solve kept one state per problem
   Chunks chunks() const;
   bool graph_stale() const;

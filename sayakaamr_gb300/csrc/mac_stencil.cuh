@@ -72,6 +72,15 @@ __device__ __forceinline__ int face_index(int d, const int ijk[3], int s, int nb
 template <typename T>
 __device__ __forceinline__ T geom(const Coef<T> &c, int b, int q) { return c.geom[b * 8 + q]; }
 
+// the record of block b when it is a constant-coefficient block (Coef::ut),
+// else null
+template <typename T>
+__device__ __forceinline__ const T *uniform_of(const Coef<T> &c, int b) {
+  if (!c.ut) return nullptr;
+  const T *u = c.ut + (long)b * kUni;
+  return u[3] != (T)0 ? u : nullptr;
+}
+
 // coefficient of a coarse/fine face: ((beta*ds)/(dx*h))*B*a
 // (src/SayakaMacOperator.cpp:1155-1161 and :1258-1266)
 template <typename T>
@@ -274,12 +283,15 @@ __device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c
   const long cb = (long)b * t.ncell;
   const long fb = (long)b * t.nfb;
   const T dv = geom(c, b, 6);
+  const T *u = uniform_of(c, b);  // constant coefficients: no face or vf loads
   T diag = c.alpha * dv;
   T off = 0;
+  bool inner = true;
 #pragma unroll
   for (int f = 0; f < 2 * ND; f++) {
     const int d = f >> 1, s = f & 1;
     const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+    inner = inner && !bnd;
     // face index (first dimension fastest, nb+1 faces along d)
     int fx;
     if (d == 0)
@@ -289,18 +301,18 @@ __device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c
     else
       fx = ci + s * nb * nb;
     if (!bnd) {
-      const T coef = c.tff[d][fb + fx];
+      const T coef = u ? u[d] : c.tff[d][fb + fx];
       const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
       diag += coef;
       off = fma_t(coef, ld<CG>(&phi[cb + ci + (s ? stride : -stride)]), off);
     } else {
       const int ty = face_type_of(ft, f);
       if (ty == 0) {
-        const T coef = c.tff[d][fb + fx];
+        const T coef = u ? u[d] : c.tff[d][fb + fx];
         diag += coef;
         off = fma_t(coef, same_level_ghost<T, CG>(t, b, f, ijk, phi, hx), off);
       } else if (ty == 1) {
-        if (t.bc_type[b * 6 + f] != kBCNeumann) diag += c.tff[d][fb + fx] * (T)2.0;
+        if (t.bc_type[b * 6 + f] != kBCNeumann) diag += (u ? u[d] : c.tff[d][fb + fx]) * (T)2.0;
       } else if (ty == 2) {
         const T coef = cf_coef(c, t, b, d, fx, (T)1.5);
         diag += coef;
@@ -312,10 +324,11 @@ __device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c
     }
   }
   if (sizeof(T) == 8 && sa) {
-    phi[cb + ci] = fma_t(ld<CG>(&rhs[cb + ci]), (T)sa[ci], off * (T)ia[ci]);
+    const bool ui = u && inner;  // interior cell of a constant-coefficient block
+    phi[cb + ci] = fma_t(ld<CG>(&rhs[cb + ci]), ui ? u[6] : (T)sa[ci], off * (ui ? u[7] : (T)ia[ci]));
     return;
   }
-  const T vfv = c.vf[cb + ci];
+  const T vfv = u ? (T)1 : c.vf[cb + ci];
   T unew = 0;
   if (vfv > 0 && diag > 0) unew = fast_div(fma_t(ld<CG>(&rhs[cb + ci]) * dv, vfv, off), diag);
   phi[cb + ci] = unew;

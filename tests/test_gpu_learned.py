@@ -23,9 +23,11 @@ def small_solver(nb):
     return sg.MacSolver(t.tables())
 
 
+@pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("nb", [8, 16])
-def test_training_gradient_matches_oracle(nb):
+def test_training_gradient_matches_oracle(nb, mode):
     S = small_solver(nb)
+    S.set_params(learned_loss=mode)
     rng = np.random.default_rng(nb)
     w = nn.init(nb)
     S.set_learned_weights(w)
@@ -33,7 +35,7 @@ def test_training_gradient_matches_oracle(nb):
     feat = rng.standard_normal((n, 3, nb * nb)).astype(np.float32)
     aux = nn.random_aux(rng, n, nb)
     loss, g = S.learned_loss_grad(feat, aux)
-    lref, gref = nn.loss_grad(w, feat, aux, nb)
+    lref, gref = nn.loss_grad(w, feat, aux, nb, mode)
     assert abs(loss - lref) <= GRAD_RTOL * abs(lref)
     scale = np.abs(gref).max()
     assert np.max(np.abs(g - gref)) <= GRAD_RTOL * scale, np.max(np.abs(g - gref)) / scale
@@ -50,6 +52,23 @@ def test_tensor_core_forward_matches_oracle(nb):
     ref = nn.forward(w, feat, nb, bf16=True, project=False)
     scale = np.abs(ref).max()
     assert np.max(np.abs(y - ref)) <= BF16_RTOL * scale
+
+
+def test_tcgen05_forward_matches_warp_mma():
+    """16x16 blocks: the hidden layer as a tcgen05 implicit GEMM (tensor
+    memory accumulator) and as mma.sync warp MMAs give the same network
+    output up to the order of the FP32 sums"""
+    S = small_solver(16)
+    rng = np.random.default_rng(7)
+    S.set_learned_weights(nn.init(31))
+    feat = rng.standard_normal((6, 3, 256)).astype(np.float32)
+    out = {}
+    for tc in (1, 0):
+        S.set_params(learned_tc05=tc)
+        out[tc] = S.learned_forward(feat)
+    scale = np.abs(out[0]).max()
+    assert scale > 0
+    assert np.max(np.abs(out[1] - out[0])) <= 1e-4 * scale, np.max(np.abs(out[1] - out[0])) / scale
 
 
 @pytest.fixture(scope="module")

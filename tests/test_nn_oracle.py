@@ -2,17 +2,19 @@
 against central finite differences of its own loss, so that the GPU
 gradient test compares against a pinned oracle."""
 import numpy as np
+import pytest
 
 from oracle import nn_oracle as nn
 
 
-def test_oracle_gradient_matches_finite_differences():
+@pytest.mark.parametrize("mode", [0, 1])
+def test_oracle_gradient_matches_finite_differences(mode):
     nb = 8
     rng = np.random.default_rng(5)
     w = nn.init(3).astype(np.float64)
     feat = rng.standard_normal((2, 3, nb * nb))
     aux = nn.random_aux(rng, 2, nb).astype(np.float64)
-    _, g = nn.loss_grad(w, feat, aux, nb)
+    _, g = nn.loss_grad(w, feat, aux, nb, mode)
     idx = np.concatenate([rng.choice(np.arange(lo, hi), 6, replace=False) for lo, hi in
                           ((nn.OW1, nn.OB1), (nn.OB1, nn.OW2), (nn.OW2, nn.OB2), (nn.OB2, nn.OW3),
                            (nn.OW3, nn.OB3))] + [np.array([nn.OB3])])
@@ -21,7 +23,7 @@ def test_oracle_gradient_matches_finite_differences():
         wp, wm = w.copy(), w.copy()
         wp[k] += h
         wm[k] -= h
-        fd = (nn.loss_grad(wp, feat, aux, nb)[0] - nn.loss_grad(wm, feat, aux, nb)[0]) / (2 * h)
+        fd = (nn.loss_grad(wp, feat, aux, nb, mode)[0] - nn.loss_grad(wm, feat, aux, nb, mode)[0]) / (2 * h)
         assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(g[k])), (k, fd, g[k])
 
 
