@@ -110,9 +110,9 @@ def parse():
     ap.add_argument("--problems", type=int, default=256,
                     help="config4: number of problems of the batch (256; fewer for a small profiling case)")
     ap.add_argument("--max-level", type=int, default=7, help="--sequence: finest level of the elbow tree")
-    ap.add_argument("--bottom-refresh", type=int, default=1,
-                    help="--sequence: 1 rebuild the dense bottom inverse after every coefficient change, 0 keep "
-                         "the inverse of the last tree between regrids")
+    ap.add_argument("--bottom-refresh", type=int, default=0,
+                    help="--sequence: 1 rebuild the dense bottom inverse after every coefficient change, 0 (default) "
+                         "keep the inverse of the last tree between regrids")
     ap.add_argument("--profile", action="store_true",
                     help="run one solve between cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     return ap.parse_args()
@@ -740,6 +740,9 @@ def _elbow_geometry(torch, tb, sc, seed):
         return torch.minimum(W.ELBOW_TUBE - d, sp)
 
     ls = level_set(centres(nb + 2, -0.5)).reshape(-1)
+    # host copies in pinned memory (the solver's uploads run at full speed)
+    ls_h = torch.empty(ls.shape, dtype=torch.float64, pin_memory=True)
+    ls_h.copy_(ls)
     pc = centres(nb, 0.5)
     g = torch.Generator(device="cpu").manual_seed(seed)
     amp = torch.randn(8, generator=g, dtype=torch.float64).to(dev)
@@ -749,7 +752,9 @@ def _elbow_geometry(torch, tb, sc, seed):
         f += amp[q] * torch.exp(-((pc - cen[q]) ** 2).sum(-1) / (2 * 0.08 ** 2))
     leaf = torch.as_tensor(tb["node_type"] == 1, device=dev)
     rhs = (-f * leaf[:, None]).reshape(-1)
-    return ls.cpu().numpy(), rhs.cpu().numpy()
+    rhs_h = torch.empty(rhs.shape, dtype=torch.float64, pin_memory=True)
+    rhs_h.copy_(rhs)
+    return ls_h.numpy(), rhs_h.numpy()
 
 
 def run_sequence(args, torch, ws, rank, local):
@@ -769,9 +774,13 @@ def run_sequence(args, torch, ws, rank, local):
     if args.config != "config5":
         raise SystemExit("--sequence runs the config5 elbow sequence")
     K, every = args.sequence, max(1, args.regrid_every)
+    # the dense bottom solve on level 1 (512 cells per component here): its
+    # inverse is rebuilt in milliseconds after a regrid, where level 2's
+    # (4096 cells) takes about 0.26 s
     prm = dict(tol_rel=TOL, tol_abs=0.0, use_mg_precond=1, max_iter=2000, bottom=1, graph=1,
                precision=1 if args.precision < 0 else args.precision,
-               n_post_smooth=4 if args.n_post < 0 else args.n_post, bottom_level=args.bottom_level,
+               n_post_smooth=4 if args.n_post < 0 else args.n_post,
+               bottom_level=args.bottom_level if args.bottom_level > 0 else 1,
                bottom_refresh=args.bottom_refresh, smoother=max(args.smoother, 0))
     t0 = time.perf_counter()
     sc = W.elbow_point(0.1)
@@ -801,28 +810,44 @@ def run_sequence(args, torch, ws, rank, local):
         geo_s += time.perf_counter() - t0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        ph = {}
+
+        def mark(name, t_prev, solver):
+            torch.cuda.ExternalStream(solver.stream()).synchronize()
+            now = time.perf_counter()
+            ph[name] = (now - t_prev) * 1e3
+            return now
         if new_tree:
             S2 = sg.MacSolver(tb)
             S2.set_bc(bc.reshape(-1))
+            ta = mark("create", t0, S2)
             S2.set_ib_frac_by_ls(ls, ncomp=1, ngrow=1, comp=0)
+            ta = mark("fractions", ta, S2)
             S2.set_params(**prm)
             if S is None:
                 S2.set_zero_sol()
             else:
                 S2.init_from(S)
+            ta = mark("transfer", ta, S2)
             S = S2
         else:
             S.set_ib_frac_by_ls(ls, ncomp=1, ngrow=1, comp=0)
+            ta = mark("fractions", t0, S)
         S.set_rhs_compact(rhs)
+        ta = mark("rhs", ta, S)
         S.prepare()
+        mark("prepare", ta, S)
         t1 = time.perf_counter()
+        if k == 0 and prm.get("smooth_variant", -1) < 0:
+            # later trees of the sequence use the variant the first one tuned
+            prm["smooth_variant"] = S.tuned_smoother(prm["precision"])[0]
         S.cg_solve_async()
         info = S.solve_info()
         t2 = time.perf_counter()
         if info["status"] != 0 or not info["rnorm"] < TOL * info["rnorm0"]:
             raise SystemExit("sequence step %d did not converge: %s" % (k, info))
         steps.append(dict(setup_s=t1 - t0, solve_s=t2 - t1, iterations=info["iterations"], new_tree=new_tree,
-                          blocks=int(tb["num_blocks"]), leaf_cells=leaf_cells))
+                          blocks=int(tb["num_blocks"]), leaf_cells=leaf_cells, phases=ph))
         cells += leaf_cells
     total = sum(r["setup_s"] + r["solve_s"] for r in steps)
     setup = sum(r["setup_s"] for r in steps)
@@ -846,7 +871,9 @@ def run_sequence(args, torch, ws, rank, local):
                      "initial_tree_s_outside": tree_build_s,
                      "per_step": [[round(r["setup_s"] * 1e3, 2), round(r["solve_s"] * 1e3, 2), r["iterations"]]
                                   for r in steps],
-                     "per_step_columns": ["setup ms", "solve ms", "iterations"]},
+                     "per_step_columns": ["setup ms", "solve ms", "iterations"],
+                     "setup_phases_ms_regrid_step": steps[every if K > every else 0]["phases"],
+                     "setup_phases_ms_other_step": steps[1 if K > 1 else 0]["phases"]},
     }
     if rank == 0:
         print(json.dumps(out))

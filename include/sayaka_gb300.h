@@ -150,8 +150,8 @@ typedef struct sayaka_params {
                              on tcgen05 with the accumulator in tensor memory (default); 0 = on mma.sync warp
                              MMAs (the same network, products summed in another order) */
   int32_t learned_loss;   /* training loss of the learned correction u: 0 = the residual u leaves under the
-                             block-local operator; 1 = the distance of u to the block-local part of the error the
-                             V-cycle left, known from the solver's own converged solution (default) */
+                             block-local operator (default); 1 = the distance of u to the block-local part of the
+                             error the V-cycle left, known from the solver's own converged solution */
 } sayaka_params;
 
 typedef struct sayaka_solve_info {
@@ -242,10 +242,12 @@ int sayaka_mac_launch_counts(sayaka_mac *h, int32_t *prologue, int32_t *per_iter
 /* the launch-bounds variant of the device smoother that the autotuner chose
  * for precision (0 FP64, 1 FP32 V-cycle) at sayaka_mac_prepare, -1 if not
  * tuned yet; us (may be NULL) receives the measured microseconds per variant
- * (n entries, 10 variants: 0-4 one thread per cell with register caps
+ * (n entries, 12 variants: 0-4 one thread per cell with register caps
  * 128/80/64/40/32, 5-7 the block staged in shared memory, caps 128/64/40,
  * 8 the block's tile and face coefficients staged by TMA bulk copies,
- * 9 persistent CTAs streaming blocks through double-buffered bulk copies) */
+ * 9 persistent CTAs streaming blocks through double-buffered bulk copies,
+ * 10-11 two cells per thread (the same cell of two blocks, operands of both
+ * gathered before either is updated), caps 64/80) */
 int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n);
 /* level of the device solve's dense bottom solve once prepared (-1 before) */
 int32_t sayaka_mac_bottom_level(const sayaka_mac *h);
@@ -290,11 +292,16 @@ int sayaka_mac_learned_collect_sampled(sayaka_mac *h, int32_t max_iter, int32_t 
 /* Adam on the collected pairs, FP32 forward/backward kernels on the GPU;
  * loss = mean over blocks of the weighted squared error (last epoch) */
 int sayaka_mac_learned_train(sayaka_mac *h, int32_t epochs, float lr, int32_t batch, uint32_t seed, float *loss);
+/* the same loss, mean over blocks, of the collected pairs under the current
+ * weights, without training (held-out evaluation: collect the pairs of
+ * another right-hand side first) */
+int sayaka_mac_learned_eval(sayaka_mac *h, float *loss);
 int sayaka_mac_learned_get_weights(sayaka_mac *h, float *w, int32_t n);
 int sayaka_mac_learned_set_weights(sayaka_mac *h, const float *w, int32_t n);
 /* test hooks: loss and weight gradient of explicit blocks (feat [n][3][nb*nb];
- * aux [n][2*nb*nb + 2*(nb+1)*nb] = Jacobi factor, dv*vf, x-face and y-face
- * coefficients of the block-local operator), and the tensor-core (BF16)
+ * aux [n][3*nb*nb + 2*(nb+1)*nb] = Jacobi factor, dv*vf, x-face and y-face
+ * coefficients of the block-local operator, error target), and the
+ * tensor-core (BF16)
  * forward of explicit feature blocks (y [n][nb*nb]) */
 int sayaka_mac_learned_loss_grad(sayaka_mac *h, const float *feat, const float *aux, int32_t n, float *grad,
                                  float *loss);

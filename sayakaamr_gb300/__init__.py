@@ -118,6 +118,7 @@ SIGNATURES = {
     "sayaka_mac_learned_collect": (C.c_int, [_V, C.c_int32, _i32p]),
     "sayaka_mac_learned_collect_sampled": (C.c_int, [_V, C.c_int32, C.c_int32, _i32p]),
     "sayaka_mac_learned_train": (C.c_int, [_V, C.c_int32, C.c_float, C.c_int32, C.c_uint32, _f32p]),
+    "sayaka_mac_learned_eval": (C.c_int, [_V, _f32p]),
     "sayaka_mac_learned_get_weights": (C.c_int, [_V, _f32p, C.c_int32]),
     "sayaka_mac_learned_set_weights": (C.c_int, [_V, _f32p, C.c_int32]),
     "sayaka_mac_learned_loss_grad": (C.c_int, [_V, _f32p, _f32p, C.c_int32, _f32p, _f32p]),
@@ -462,6 +463,12 @@ class MacSolver:
                                                  C.byref(loss)), "learned_train", self.h)
         return loss.value
 
+    def learned_eval(self):
+        """mean loss of the collected pairs under the current weights (no training)"""
+        loss = C.c_float()
+        _check(self.lib.sayaka_mac_learned_eval(self.h, C.byref(loss)), "learned_eval", self.h)
+        return loss.value
+
     def learned_weights(self):
         n = self.lib.sayaka_mac_learned_nparam()
         w = np.zeros(n, dtype=np.float32)
@@ -519,8 +526,8 @@ class MacSolver:
 
     def tuned_smoother(self, precision):
         """(chosen variant, microseconds per variant) of the smoother autotuner"""
-        us = (C.c_float * 10)()
-        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 10)
+        us = (C.c_float * 12)()
+        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 12)
         return int(v), [float(x) for x in us]
 
     def problem_count(self):

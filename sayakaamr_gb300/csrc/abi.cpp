@@ -508,6 +508,10 @@ int sayaka_mac_set_ib_frac_by_ls(sayaka_mac *h, const double *ls, int32_t ncomp,
     if (!ls || ngrow < 1) return (int)SAYAKA_BAD_INPUT;
     Layout L(g.ndim(), g.nb(), ncomp, ngrow, comp, -1);
     if (!L.ok()) return (int)SAYAKA_BAD_INPUT;
+    if (ncomp == 1) {  // the buffer is the grown boxes already
+      g.set_ib_frac_by_ls(ls, ngrow);
+      return (int)SAYAKA_OK;
+    }
     // extract the grown box of component `comp` for every block
     std::vector<double> grown((size_t)g.num_blocks() * L.cap);
     for (int b = 0; b < g.num_blocks(); b++)
@@ -785,6 +789,17 @@ int sayaka_mac_learned_train(sayaka_mac *h, int32_t epochs, float lr, int32_t ba
       return (int)SAYAKA_BAD_INPUT;
     }
     const float l = h->gpu->learned_train(epochs, lr, batch, seed);
+    if (loss) *loss = l;
+    return l < 0 ? (int)SAYAKA_CUDA_ERROR : (int)SAYAKA_OK;
+  });
+}
+int sayaka_mac_learned_eval(sayaka_mac *h, float *loss) {
+  return guarded(h, [&] {
+    if (h->gpu->learned_samples() == 0) {
+      h->err = "learned correction: no pairs to evaluate (call sayaka_mac_learned_collect first)";
+      return (int)SAYAKA_BAD_INPUT;
+    }
+    const float l = h->gpu->learned_eval();
     if (loss) *loss = l;
     return l < 0 ? (int)SAYAKA_CUDA_ERROR : (int)SAYAKA_OK;
   });

@@ -97,6 +97,44 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs(Topo t, Coef<T> c, Bloc
   }
 }
 
+// the same sweep with CPT cells per thread, the same cell of CPT blocks
+// (entries p, p + G, ..., G = gridDim.y): every cell's operands are gathered
+// before any is updated, so that a thread keeps CPT cells' loads in flight
+// (smooth_gather / smooth_update: the values of smooth_cell_fast)
+template <typename T, int ND, int MINB, int CPT>
+__global__ void __launch_bounds__(kThreads, MINB) k_rbgs_ilp(Topo t, Coef<T> c, BlockList L, int color,
+                                                             T *__restrict__ phi, const T *__restrict__ rhs,
+                                                             const int *guard) {
+  pdl_enter();
+  if (guard && *guard) return;
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= (t.ncell >> 1)) return;
+  int ijk[3];
+  color_cell_fast<ND>(h, t, color, ijk);
+  const int G = gridDim.y;
+  for (int p0 = blockIdx.y; p0 < L.n; p0 += CPT * G) {
+    SmoothOps<T, ND> o[CPT];
+    bool on[CPT];
+#pragma unroll
+    for (int k = 0; k < CPT; k++) {
+      const int p = p0 + k * G;
+      on[k] = false;
+      if (p >= L.n) continue;
+      const long fo = (long)p * t.ncell;
+      const int *e = L.hx ? L.hx + (long)p * kHX : nullptr;
+      const int b = e ? e[kHXBlock] : L.blocks[p];
+      if (L.stc && block_off(L, b)) continue;
+      const uint16_t ft = e ? (uint16_t)(e[kHXInfo] & 0xffff) : L.ftypes[p];
+      smooth_gather<T, ND>(t, c, b, ft, ijk, phi, rhs, L.sa ? L.sa + fo : nullptr, L.ia ? L.ia + fo : nullptr, e,
+                           o[k]);
+      on[k] = true;
+    }
+#pragma unroll
+    for (int k = 0; k < CPT; k++)
+      if (on[k]) smooth_update<T, ND>(c, o[k], phi);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // volume-weighted restriction onto the non-leaf blocks of a level:
 // coarse = avg(fine*vf_fine)/vf_coarse (src/SayakaMacIB.cpp:157-232 with
@@ -1188,9 +1226,22 @@ static void rbgs_go(const Topo &t, const Coef<T> &c, const BlockList &L, int col
   launch_k(pdl, k_rbgs<T, ND, MINB>, grid, threads, 0, s, t, c, L, color, phi, rhs, guard);
 }
 
+// variants 10, 11: CPT = 2 cells per thread (k_rbgs_ilp), caps 64 and 80
+template <typename T, int ND, int MINB, int CPT>
+static void rbgs_ilp_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
+                        const int *guard, cudaStream_t s, bool pdl, dim3 grid, int threads) {
+  grid.y = std::min((L.n + CPT - 1) / CPT, 65535);
+  launch_k(pdl, k_rbgs_ilp<T, ND, MINB, CPT>, grid, threads, 0, s, t, c, L, color, phi, rhs, guard);
+}
+
 template <typename T, int ND>
 static void rbgs_nd(int variant, const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi,
                     const T *rhs, const int *guard, cudaStream_t s, bool pdl, dim3 grid, int threads) {
+  switch (variant) {
+    case 10: rbgs_ilp_go<T, ND, 4, 2>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); return;
+    case 11: rbgs_ilp_go<T, ND, 3, 2>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); return;
+    default: break;
+  }
   switch (variant) {
     case 0: rbgs_go<T, ND, 2>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
     case 1: rbgs_go<T, ND, 3>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); break;
@@ -1214,9 +1265,9 @@ void launch_rbgs(const Topo &t, const Coef<T> &c, const BlockList &L, int color,
   // the bulk-copy variant also needs 16-byte multiples for the tile and the
   // face rows of a block (and L.n CTAs in one grid dimension)
   const size_t tile = t.ndim == 2 ? rbgs_tile_smem<T, 2>(t) : rbgs_tile_smem<T, 3>(t);
-  if (variant >= 5 && tile > 200 * 1024) variant = 3;
+  if (variant >= 5 && variant <= 9 && tile > 200 * 1024) variant = 3;
   const bool aligned = (t.ncell * sizeof(T)) % 16 == 0 && (t.nfb * sizeof(T)) % 16 == 0;
-  if (L.stc && variant >= 8) variant = 7;  // the bulk-copy variants know no per-problem states
+  if (L.stc && (variant == 8 || variant == 9)) variant = 7;  // the bulk-copy variants know no per-problem states
   if (variant == 8) {
     const size_t bulk = t.ndim == 2 ? rbgs_bulk_smem<T, 2>(t) : rbgs_bulk_smem<T, 3>(t);
     if (bulk > 200 * 1024 || !aligned) variant = 7;

@@ -967,6 +967,41 @@ float MacGpu::learned_train(int epochs, float lr, int batch, unsigned seed) {
   return err_.empty() ? last : -1.f;
 }
 
+// mean loss (per block) of the collected pairs under the current weights:
+// the training forward over the whole set, no update (the gradient it
+// accumulates is discarded)
+float MacGpu::learned_eval() {
+  if (!ls_.w || ls_.nsamp == 0) return -1.f;
+  set_smem_attrs();
+  const int batch = std::min(256, ls_.nsamp);
+  const size_t nc = (size_t)ncell_;
+  float *h1 = nullptr, *h2 = nullptr, *dy = nullptr;
+  int *d_idx = nullptr;
+  cudaMalloc(&h1, (size_t)batch * kC * nc * sizeof(float));
+  cudaMalloc(&h2, (size_t)batch * kC * nc * sizeof(float));
+  cudaMalloc(&dy, (size_t)batch * nc * sizeof(float));
+  cudaMalloc(&d_idx, (size_t)ls_.nsamp * sizeof(int));
+  if (!h1 || !h2 || !dy || !d_idx) {
+    fail("out of device memory (evaluation)");
+    return -1.f;
+  }
+  std::vector<int> idx(ls_.nsamp);
+  for (int k = 0; k < ls_.nsamp; k++) idx[k] = k;
+  CKR_(cudaMemcpyAsync(d_idx, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), -1.f);
+  double tot = 0.0;
+  for (int s0 = 0; s0 < ls_.nsamp; s0 += batch) {
+    const int nblk = std::min(batch, ls_.nsamp - s0);
+    tot += learned_grad(d_idx + s0, nblk, 1.f / (float)nblk, h1, h2, dy) * nblk;
+  }
+  CKR_(cudaMemsetAsync(ls_.g, 0, kNParam * sizeof(float), stream_), -1.f);
+  CKR_(cudaStreamSynchronize(stream_), -1.f);
+  cudaFree(h1);
+  cudaFree(h2);
+  cudaFree(dy);
+  cudaFree(d_idx);
+  return err_.empty() ? (float)(tot / ls_.nsamp) : -1.f;
+}
+
 // loss and gradient of explicit training blocks (a test hook): feat
 // [n][3][ncell] and aux [n][aux_len()] on the host; grad [kNParam]
 float MacGpu::learned_loss_grad(const float *feat, const float *aux, int n, float *grad) {

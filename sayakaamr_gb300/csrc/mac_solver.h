@@ -47,7 +47,7 @@ struct SolverParams {
                               // per colour); 1 = block-hybrid passes (n_post per tower, each one launch of
                               // inner_sweeps red-black sweeps per block, Jacobi between blocks)
   int inner_sweeps = 2;       // smoother 1: red-black sweeps per block in one pass
-  int learned_loss = 1;       // training loss of the learned correction: 0 = the block-local residual it
+  int learned_loss = 0;       // training loss of the learned correction: 0 = the block-local residual it
                               // leaves, 1 = its distance to the error the V-cycle left (block-local part)
   int learned_tc05 = 1;       // learned correction of 16x16 blocks: 1 = hidden layer on tcgen05 (tensor memory
                               // accumulator), 0 = on mma.sync (the same network; products summed in another order)
@@ -145,6 +145,7 @@ class MacGpu {
   bool learned_supported() const;
   int learned_collect(int max_iters, int max_samples = 0);  // max_samples 0: every block of every iterate
   float learned_train(int epochs, float lr, int batch, unsigned seed);
+  float learned_eval();  // mean loss of the collected pairs under the current weights
   float learned_loss_grad(const float *feat, const float *aux, int n, float *grad);
   int aux_len() const { return 3 * tt_.nb * tt_.nb + 2 * (tt_.nb + 1) * tt_.nb; }
   int learned_forward(const float *feat, int n, float *y);

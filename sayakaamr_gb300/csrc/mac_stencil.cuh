@@ -334,6 +334,101 @@ __device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c
   phi[cb + ci] = unew;
 }
 
+// smooth_cell_fast in two halves, for threads that update several cells:
+// smooth_gather loads one cell's operands into registers, per face its part
+// of the diagonal (dp), the off-diagonal factor (kc) and value (v) -- the
+// tiled sweep's form; smooth_update then combines them in the same order
+// with the same operations (kc = 1 for a CRSE_FINE face, 0 for a physical
+// one: fma(1, v, off) = off + v, fma(0, 0, off) = off), so the result is the
+// same as smooth_cell_fast's.  A thread gathers all its cells before
+// updating any, so that their global loads are in flight together (none of
+// them reads a cell that the launch writes).
+template <typename T, int ND>
+struct SmoothOps {
+  long q;
+  T dv, r, vf;
+  T dp[2 * ND], kc[2 * ND], v[2 * ND];
+  double sa, ia;
+  bool fac;
+};
+template <typename T, int ND>
+__device__ __forceinline__ void smooth_gather(const Topo &t, const Coef<T> &c, int b, uint16_t ft, const int ijk[3],
+                                              const T *__restrict__ phi, const T *__restrict__ rhs,
+                                              const double *sa, const double *ia, const int *__restrict__ hx,
+                                              SmoothOps<T, ND> &o) {
+  const int nb = t.nb;
+  const int ci = t.lnb >= 0 ? ijk[0] + ((ijk[1] + (ijk[2] << t.lnb)) << t.lnb) : encode(ijk, nb);
+  const long cb = (long)b * t.ncell;
+  const long fb = (long)b * t.nfb;
+  const T *u = uniform_of(c, b);
+  o.q = cb + ci;
+  o.dv = geom(c, b, 6);
+  bool inner = true;
+#pragma unroll
+  for (int f = 0; f < 2 * ND; f++) {
+    const int d = f >> 1, s = f & 1;
+    const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+    inner = inner && !bnd;
+    int fx;
+    if (d == 0)
+      fx = ijk[0] + s + (nb + 1) * (ijk[1] + nb * ijk[2]);
+    else if (d == 1)
+      fx = ijk[0] + nb * (ijk[1] + s + (nb + 1) * ijk[2]);
+    else
+      fx = ci + s * nb * nb;
+    if (!bnd) {
+      const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+      o.dp[f] = o.kc[f] = u ? u[d] : c.tff[d][fb + fx];
+      o.v[f] = phi[cb + ci + (s ? stride : -stride)];
+      continue;
+    }
+    const int ty = face_type_of(ft, f);
+    if (ty == 0) {
+      o.dp[f] = o.kc[f] = u ? u[d] : c.tff[d][fb + fx];
+      o.v[f] = same_level_ghost<T, false>(t, b, f, ijk, phi, hx);
+    } else if (ty == 1) {
+      o.dp[f] = t.bc_type[b * 6 + f] != kBCNeumann ? (u ? u[d] : c.tff[d][fb + fx]) * (T)2.0 : (T)0;
+      o.kc[f] = (T)0;
+      o.v[f] = (T)0;
+    } else if (ty == 2) {
+      o.dp[f] = o.kc[f] = cf_coef(c, t, b, d, fx, (T)1.5);
+      o.v[f] = fine_crse_ghost<T, ND, false>(t, b, f, ijk, phi, hx);
+    } else {
+      o.dp[f] = cf_coef(c, t, b, d, fx, (T)0.75);
+      o.kc[f] = (T)1;
+      o.v[f] = crse_fine_sum<T, ND, false>(t, c, b, f, ijk, phi, hx);
+    }
+  }
+  o.r = rhs[cb + ci];
+  o.fac = sizeof(T) == 8 && sa;
+  if (o.fac) {
+    const bool ui = u && inner;
+    o.sa = ui ? (double)u[6] : sa[ci];
+    o.ia = ui ? (double)u[7] : ia[ci];
+    o.vf = (T)0;
+  } else {
+    o.vf = u ? (T)1 : c.vf[cb + ci];
+    o.sa = o.ia = 0.0;
+  }
+}
+template <typename T, int ND>
+__device__ __forceinline__ void smooth_update(const Coef<T> &c, const SmoothOps<T, ND> &o, T *__restrict__ phi) {
+  T diag = c.alpha * o.dv;
+  T off = 0;
+#pragma unroll
+  for (int f = 0; f < 2 * ND; f++) {
+    diag += o.dp[f];
+    off = fma_t(o.kc[f], o.v[f], off);
+  }
+  if (o.fac) {
+    phi[o.q] = fma_t(o.r, (T)o.sa, off * (T)o.ia);
+    return;
+  }
+  T unew = 0;
+  if (o.vf > 0 && diag > 0) unew = fast_div(fma_t(o.r * o.dv, o.vf, off), diag);
+  phi[o.q] = unew;
+}
+
 // colour cell with shifts when nb is a power of two
 template <int ND>
 __device__ __forceinline__ void color_cell_fast(int h, const Topo &t, int color, int ijk[3]) {
