@@ -356,33 +356,65 @@ void MacGpu::set_ib_frac_by_ls(const double *ls, int ng) {
   coef_changed();
 }
 
-// the host copies of B, the area and the volume fractions brought up to
-// date with the device arrays (all blocks, or only `blocks`; a partial
-// update leaves the copies marked stale)
-void MacGpu::pull_coefs(const std::vector<int> *blocks) {
-  if (!host_coef_stale_) return;
+// the host copies of B, the area and the volume fractions (allocated on
+// first use) brought up to date with the device arrays
+void MacGpu::pull_coefs() {
   const int nd = tt_.ndim;
-  if (!blocks) {
-    for (int d = 0; d < nd; d++) {
-      CK(cudaMemcpyAsync(bcoef_[d].data(), d_bcoef_[d], bcoef_[d].size() * sizeof(double), cudaMemcpyDeviceToHost,
-                         stream_));
-      CK(cudaMemcpyAsync(afrac_[d].data(), d_afrac_[d], afrac_[d].size() * sizeof(double), cudaMemcpyDeviceToHost,
-                         stream_));
+  const size_t nf = (size_t)tt_.num_blocks * nfb_, nc = (size_t)tt_.num_blocks * ncell_;
+  if (vf_.size() != nc) {
+    for (int d = 0; d < 3; d++) {
+      bcoef_[d].assign(d < nd ? nf : 1, 0.0);
+      afrac_[d].assign(d < nd ? nf : 1, 0.0);
     }
-    CK(cudaMemcpyAsync(vf_.data(), d_vf_, vf_.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    CK(cudaStreamSynchronize(stream_));
-    host_coef_stale_ = false;
-    return;
+    vf_.assign(nc, 0.0);
+    host_coef_stale_ = true;
   }
-  for (int b : *blocks) {
-    const size_t fo = (size_t)b * nfb_, co = (size_t)b * ncell_;
+  if (!host_coef_stale_) return;
+  for (int d = 0; d < nd; d++) {
+    CK(cudaMemcpyAsync(bcoef_[d].data(), d_bcoef_[d], nf * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaMemcpyAsync(afrac_[d].data(), d_afrac_[d], nf * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  }
+  CK(cudaMemcpyAsync(vf_.data(), d_vf_, nc * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  host_coef_stale_ = false;
+}
+
+void MacGpu::pull_block_coefs(const std::vector<int> &blocks, std::vector<double> &vf,
+                              std::vector<double> (&bc)[3], std::vector<double> (&af)[3]) {
+  const int nd = tt_.ndim, n = (int)blocks.size();
+  vf.assign((size_t)n * ncell_, 0.0);
+  for (int d = 0; d < 3; d++) {
+    bc[d].assign(d < nd ? (size_t)n * nfb_ : 0, 0.0);
+    af[d].assign(d < nd ? (size_t)n * nfb_ : 0, 0.0);
+  }
+  for (int p = 0; p < n; p++) {
+    const size_t fo = (size_t)blocks[p] * nfb_, co = (size_t)blocks[p] * ncell_;
     for (int d = 0; d < nd; d++) {
-      CK(cudaMemcpyAsync(&bcoef_[d][fo], d_bcoef_[d] + fo, nfb_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
-      CK(cudaMemcpyAsync(&afrac_[d][fo], d_afrac_[d] + fo, nfb_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+      CK(cudaMemcpyAsync(&bc[d][(size_t)p * nfb_], d_bcoef_[d] + fo, nfb_ * sizeof(double), cudaMemcpyDeviceToHost,
+                         stream_));
+      CK(cudaMemcpyAsync(&af[d][(size_t)p * nfb_], d_afrac_[d] + fo, nfb_ * sizeof(double), cudaMemcpyDeviceToHost,
+                         stream_));
     }
-    CK(cudaMemcpyAsync(&vf_[co], d_vf_ + co, ncell_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaMemcpyAsync(&vf[(size_t)p * ncell_], d_vf_ + co, ncell_ * sizeof(double), cudaMemcpyDeviceToHost,
+                       stream_));
   }
   CK(cudaStreamSynchronize(stream_));
+}
+
+__global__ void k_fill(long n, double v, double *a) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) a[i] = v;
+}
+
+// B = 1 and every fraction 1, set on the device (no host upload)
+void MacGpu::init_coefs() {
+  const long nf = (long)tt_.num_blocks * nfb_, nc = (long)tt_.num_blocks * ncell_;
+  for (int d = 0; d < tt_.ndim; d++) {
+    k_fill<<<cgrid(nf), kCT, 0, stream_>>>(nf, 1.0, d_bcoef_[d]);
+    k_fill<<<cgrid(nf), kCT, 0, stream_>>>(nf, 1.0, d_afrac_[d]);
+  }
+  k_fill<<<cgrid(nc), kCT, 0, stream_>>>(nc, 1.0, d_vf_);
+  CK(cudaGetLastError());
+  coef_changed();
 }
 
 }  // namespace sayaka_gb300

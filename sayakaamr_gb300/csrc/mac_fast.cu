@@ -1082,7 +1082,9 @@ void MacGpu::build_bottom() {
   bot_level_ = LB;
   bot_param_ = prm_.bottom_level;
   const std::vector<int> &B1 = towers_[LB].blocks;
-  pull_coefs(&B1);  // the bottom blocks' coefficients, assembled on the host
+  // the bottom blocks' coefficients (compact, in B1 order), assembled on the host
+  std::vector<double> vfB, bB[3], aB[3];
+  pull_block_coefs(B1, vfB, bB, aB);
   const int nblk1 = (int)B1.size();
   n_bot_ = nblk1 * ncell_;
   if (n_bot_ == 0) return;
@@ -1156,7 +1158,7 @@ void MacGpu::build_bottom() {
         const int g = rowpos[b] * ncell_ + cc, row = g - r0;
         rcomp[g] = c;
         int ijk[3] = {cc % nb, nd >= 2 ? (cc / nb) % nb : 0, nd == 3 ? cc / (nb * nb) : 0};
-        const double vf = vf_[(size_t)b * ncell_ + cc];
+        const double vf = vfB[(size_t)pos1[b] * ncell_ + cc];
         if (!(vf > 0)) {
           Ac[(size_t)row * m + row] = 1.0;
           continue;
@@ -1167,8 +1169,8 @@ void MacGpu::build_bottom() {
           const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
           const int fx = fidx(d, ijk, s);
           double T = beta_ * geom_[b * 8 + 3 + d] / geom_[b * 8 + d];
-          T = T * bcoef_[d][(size_t)b * nfb_ + fx];
-          T = T * afrac_[d][(size_t)b * nfb_ + fx];
+          T = T * bB[d][(size_t)pos1[b] * nfb_ + fx];
+          T = T * aB[d][(size_t)pos1[b] * nfb_ + fx];
           int ncol = -1;
           if (!bnd) {
             int q[3] = {ijk[0], ijk[1], ijk[2]};
@@ -1203,7 +1205,7 @@ void MacGpu::build_bottom() {
   std::vector<int> seen(n_bot_, -1), pins;
   for (int r0 = 0; r0 < n_bot_; r0++) {
     const int b = order[r0 / ncell_];
-    if (seen[r0] >= 0 || !(vf_[(size_t)b * ncell_ + r0 % ncell_] > 0)) continue;
+    if (seen[r0] >= 0 || !(vfB[(size_t)pos1[b] * ncell_ + r0 % ncell_] > 0)) continue;
     std::vector<int> stack{r0};
     seen[r0] = r0;
     bool dirichlet = false;

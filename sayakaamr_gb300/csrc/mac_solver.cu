@@ -195,11 +195,8 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
       if (nbr < 0 && nbr > kPhysBndry && tt.parent[b] >= 0) fc_neigh_[b * 6 + f] = tt.neighbor[tt.parent[b] * 6 + f];
     }
   bc_type_.assign((size_t)nbk * 6, -1);
-  for (int d = 0; d < 3; d++) {
-    bcoef_[d].assign(d < nd ? (size_t)nbk * nfb_ : 1, 1.0);
-    afrac_[d].assign(d < nd ? (size_t)nbk * nfb_ : 1, 1.0);
-  }
-  vf_.assign((size_t)nbk * ncell_, 1.0);
+  // the host copies of B and the fractions are filled on demand (pull_coefs)
+  host_coef_stale_ = true;
 
   // towers and level lists
   AmrTree t;
@@ -600,26 +597,12 @@ void MacGpu::set_scalars(double alpha, double beta) {
   c64_.alpha = alpha;
   c64_.beta = beta;
   if (!coef_uploaded_) {  // the initial coefficients (B = 1, fractions 1)
-    upload_coefs();
+    init_coefs();
     coef_uploaded_ = true;
     return;
   }
   recompute_face_coef();
   coef_version_++;
-}
-
-void MacGpu::upload_coefs() {
-  const int nd = tt_.ndim, nbk = tt_.num_blocks;
-  for (int d = 0; d < nd; d++) {
-    CK(cudaMemcpyAsync(d_bcoef_[d], bcoef_[d].data(), (size_t)nbk * nfb_ * sizeof(double), cudaMemcpyHostToDevice,
-                       stream_));
-    CK(cudaMemcpyAsync(d_afrac_[d], afrac_[d].data(), (size_t)nbk * nfb_ * sizeof(double), cudaMemcpyHostToDevice,
-                       stream_));
-  }
-  CK(cudaMemcpyAsync(d_vf_, vf_.data(), (size_t)nbk * ncell_ * sizeof(double), cudaMemcpyHostToDevice, stream_));
-  recompute_face_coef();
-  coef_version_++;
-  CK(cudaStreamSynchronize(stream_));
 }
 
 void MacGpu::recompute_face_coef() {

@@ -204,14 +204,17 @@ class MacGpu {
   BlockList level_list(int l) const;
   BlockList nonleaf_list(int l) const;
 
-  void upload_coefs();
+  void init_coefs();  // B = 1 and fractions 1 on every block, on the device
   void recompute_face_coef();
   // coefficient averaging on the device (mac_coef.cu)
   void build_coef_lists();
   void free_coef_lists();
   void coef_average(int dmask, double *const F[3], double *V);
   void coef_changed();
-  void pull_coefs(const std::vector<int> *blocks = nullptr);
+  void pull_coefs();
+  // B, area and volume fractions of the listed blocks, compact in list order
+  void pull_block_coefs(const std::vector<int> &blocks, std::vector<double> &vf, std::vector<double> (&bc)[3],
+                        std::vector<double> (&af)[3]);
   std::vector<int *> d_sync_up_, d_sync_copy_;
   std::vector<int> n_sync_up_, n_sync_copy_;
   bool coef_lists_ = false;
