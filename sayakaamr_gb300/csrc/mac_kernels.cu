@@ -135,6 +135,133 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_ilp(Topo t, Coef<T> c, 
   }
 }
 
+// The 2D sweep of 16x16 blocks with one warp per block: lane l holds row
+// l/2, columns 8(l%2) .. 8(l%2)+7 of phi and rhs in registers (two 16-byte
+// loads each), neighbours inside the block come from the lane's own
+// registers and from lanes l-1, l+1 (columns) and l-2, l+2 (rows) by
+// shuffles, and the block is written back whole (the cells of the other
+// colour with their unchanged values) with two 16-byte stores per lane.  The
+// fast path takes constant-coefficient blocks (a block record) whose faces
+// are all same-level or physical; their halo cells are loaded from the
+// neighbour block (one value per lane for the side faces, two 16-byte loads
+// for the bottom and top rows).  Any other block is swept cell by cell with
+// smooth_cell_fast.  Per cell the arithmetic is smooth_cell_fast's, face by
+// face in the same order, so every path gives the same bits.
+template <int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_rbgs_warp16(Topo t, Coef<float> c, BlockList L, int color,
+                                                                float *__restrict__ phi, const float *__restrict__ rhs,
+                                                                const int *guard) {
+  pdl_enter();
+  if (guard && *guard) return;
+  constexpr int NB = 16, NC = 256;
+  const int lane = threadIdx.x & 31;
+  const int warps = blockDim.x >> 5;
+  const int j = lane >> 1, hh = lane & 1, c0 = 8 * hh;
+  for (int p = blockIdx.x * warps + (threadIdx.x >> 5); p < L.n; p += gridDim.x * warps) {
+    const int *e = L.hx ? L.hx + (long)p * kHX : nullptr;
+    const int b = e ? e[kHXBlock] : L.blocks[p];
+    if (L.stc && block_off(L, b)) continue;  // uniform over the warp
+    const uint16_t ft = e ? (uint16_t)(e[kHXInfo] & 0xffff) : L.ftypes[p];
+    const float *u = uniform_of(c, b);
+    bool fast = u != nullptr;
+#pragma unroll
+    for (int f = 0; f < 4; f++) fast = fast && face_type_of(ft, f) <= 1;
+    if (!fast) {
+      // four cells of the colour per lane, as k_rbgs does them
+      for (int k = 0; k < 4; k++) {
+        const int h = lane * 4 + k;  // half-cell index 0..127
+        int ijk[3];
+        color_cell_fast<2>(h, t, color, ijk);
+        smooth_cell_fast<float, 2>(t, c, b, ft, ijk, phi, rhs, nullptr, nullptr, e);
+      }
+      continue;
+    }
+    const long cb = (long)b * NC;
+    const float4 *src = reinterpret_cast<const float4 *>(phi + cb + j * NB + c0);
+    const float4 *rsrc = reinterpret_cast<const float4 *>(rhs + cb + j * NB + c0);
+    const float4 p0 = src[0], p1 = src[1], r0 = rsrc[0], r1 = rsrc[1];
+    float v[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+    const float r[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+    const int ty[4] = {face_type_of(ft, 0), face_type_of(ft, 1), face_type_of(ft, 2), face_type_of(ft, 3)};
+    // halo values (same-level faces only; physical faces have no off-diagonal term)
+    float hl = 0.f, hr = 0.f;
+    if (hh == 0 && ty[0] == 0) {
+      const int n = e ? e[0] : t.neighbor[b * 6 + 0];
+      hl = phi[(long)n * NC + j * NB + (NB - 1)];
+    }
+    if (hh == 1 && ty[1] == 0) {
+      const int n = e ? e[1] : t.neighbor[b * 6 + 1];
+      hr = phi[(long)n * NC + j * NB];
+    }
+    float hv[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if ((j == 0 && ty[2] == 0) || (j == NB - 1 && ty[3] == 0)) {
+      const int f = j == 0 ? 2 : 3;
+      const int n = e ? e[f] : t.neighbor[b * 6 + f];
+      const int row = j == 0 ? NB - 1 : 0;
+      const float4 *hs = reinterpret_cast<const float4 *>(phi + (long)n * NC + row * NB + c0);
+      const float4 a0 = hs[0], a1 = hs[1];
+      hv[0] = a0.x, hv[1] = a0.y, hv[2] = a0.z, hv[3] = a0.w, hv[4] = a1.x, hv[5] = a1.y, hv[6] = a1.z, hv[7] = a1.w;
+    }
+    const float dv = geom(c, b, 6);
+    const float T0 = u[0], T1 = u[1];
+    const bool dir[4] = {t.bc_type[b * 6 + 0] != kBCNeumann, t.bc_type[b * 6 + 1] != kBCNeumann,
+                         t.bc_type[b * 6 + 2] != kBCNeumann, t.bc_type[b * 6 + 3] != kBCNeumann};
+    // neighbours across lanes: v[7] of the left half, v[0] of the right half
+    const float from_left = __shfl_up_sync(0xffffffffu, v[7], 1);
+    const float from_right = __shfl_down_sync(0xffffffffu, v[0], 1);
+    const int par = (color + j) & 1;  // column parity of this row's cells of the colour
+    float dn[8], up[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      dn[k] = __shfl_up_sync(0xffffffffu, v[k], 2);
+      up[k] = __shfl_down_sync(0xffffffffu, v[k], 2);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      if ((k & 1) != par) continue;
+      const int i = c0 + k;
+      float diag = c.alpha * dv;
+      float off = 0.f;
+      // f = 0: left
+      if (i > 0 || ty[0] == 0) {
+        const float nbv = k > 0 ? v[k - 1] : (hh == 1 ? from_left : hl);
+        diag += T0;
+        off = fma_t(T0, nbv, off);
+      } else if (dir[0]) {
+        diag += T0 * 2.0f;
+      }
+      // f = 1: right
+      if (i < NB - 1 || ty[1] == 0) {
+        const float nbv = k < 7 ? v[k + 1] : (hh == 0 ? from_right : hr);
+        diag += T0;
+        off = fma_t(T0, nbv, off);
+      } else if (dir[1]) {
+        diag += T0 * 2.0f;
+      }
+      // f = 2: down
+      if (j > 0 || ty[2] == 0) {
+        const float nbv = j > 0 ? dn[k] : hv[k];
+        diag += T1;
+        off = fma_t(T1, nbv, off);
+      } else if (dir[2]) {
+        diag += T1 * 2.0f;
+      }
+      // f = 3: up
+      if (j < NB - 1 || ty[3] == 0) {
+        const float nbv = j < NB - 1 ? up[k] : hv[k];
+        diag += T1;
+        off = fma_t(T1, nbv, off);
+      } else if (dir[3]) {
+        diag += T1 * 2.0f;
+      }
+      v[k] = diag > 0.f ? fast_div(fma_t(r[k] * dv, 1.0f, off), diag) : 0.f;
+    }
+    float4 *dst = reinterpret_cast<float4 *>(phi + cb + j * NB + c0);
+    dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+    dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // volume-weighted restriction onto the non-leaf blocks of a level:
 // coarse = avg(fine*vf_fine)/vf_coarse (src/SayakaMacIB.cpp:157-232 with
@@ -777,6 +904,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_rbgs_bulk(Topo t, Coef<T> c, Bl
   const bool ok = mbar_wait(mbar, 0, kWait);
   if (__syncthreads_or(!ok)) {
     if (threadIdx.x == 0) {
+      // the error word makes the solve report a CUDA error; should this
+      // bounded drain time out too, copies may still land in shared memory
+      // the CTA released, so nothing the device computes after the flag is
+      // set is trusted (the host reports the failure after the solve)
       atomicExch(&g_rbgs_err, 1);
       mbar_wait(mbar, 0, kWait);  // let the copies into this CTA's shared memory land before it exits
     }
@@ -1226,7 +1357,8 @@ static void rbgs_go(const Topo &t, const Coef<T> &c, const BlockList &L, int col
   launch_k(pdl, k_rbgs<T, ND, MINB>, grid, threads, 0, s, t, c, L, color, phi, rhs, guard);
 }
 
-// variants 10, 11: CPT = 2 cells per thread (k_rbgs_ilp), caps 64 and 80
+// variant 10: CPT = 2 cells per thread (k_rbgs_ilp), cap 64; variant 11: one
+// warp per 16x16 block in 2D FP32 (k_rbgs_warp16), elsewhere variant 3
 template <typename T, int ND, int MINB, int CPT>
 static void rbgs_ilp_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
                         const int *guard, cudaStream_t s, bool pdl, dim3 grid, int threads) {
@@ -1239,7 +1371,16 @@ static void rbgs_nd(int variant, const Topo &t, const Coef<T> &c, const BlockLis
                     const T *rhs, const int *guard, cudaStream_t s, bool pdl, dim3 grid, int threads) {
   switch (variant) {
     case 10: rbgs_ilp_go<T, ND, 4, 2>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); return;
-    case 11: rbgs_ilp_go<T, ND, 3, 2>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); return;
+    case 11:
+      if constexpr (ND == 2 && sizeof(T) == 4) {
+        if (t.nb == 16) {
+          const int g = std::min((L.n + 7) / 8, 152 * 64);
+          launch_k(pdl, k_rbgs_warp16<4>, g, kThreads, 0, s, t, c, L, color, phi, rhs, guard);
+          return;
+        }
+      }
+      rbgs_go<T, ND, 6>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads);
+      return;
     default: break;
   }
   switch (variant) {

@@ -82,3 +82,27 @@ def test_device_solve_bit_identical_with_records(name, precision, smoother):
     assert np.array_equal(res[0][1], res[1][1])
     if name == "config2":
         assert S.uniform_blocks() > 0
+
+
+@pytest.mark.parametrize("name", ["config2", "config4"])
+def test_warp_per_block_sweep_is_bit_identical(name):
+    """the FP32 sweep of 16x16 blocks with one warp per block (registers,
+    shuffles, 16-byte loads; autotuner variant 11) against the one-thread-
+    per-cell sweep (variant 3): identical iterations and solutions, on a
+    workload with constant-coefficient blocks (its fast path) and cut or
+    coarse/fine blocks (its cell-by-cell path), and on a small forest solved
+    with one state per problem"""
+    from sayakaamr_gb300 import workloads
+    p = workloads.config4(n_problems=6) if name == "config4" else workloads.config2()
+    S = workloads.make_solver(p)
+    res = []
+    for var in (3, 11):
+        S.set_zero_sol()
+        S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=1, bottom=1,
+                     smooth_variant=var)
+        info = S.cg_solve()
+        assert info["status"] == 0, info
+        res.append((info["iterations"], S.get_sol_compact()))
+    assert res[0][0] == res[1][0]
+    assert np.array_equal(res[0][1], res[1][1])
+    assert S.uniform_blocks() > 0
