@@ -242,14 +242,14 @@ int sayaka_mac_launch_counts(sayaka_mac *h, int32_t *prologue, int32_t *per_iter
 /* the launch-bounds variant of the device smoother that the autotuner chose
  * for precision (0 FP64, 1 FP32 V-cycle) at sayaka_mac_prepare, -1 if not
  * tuned yet; us (may be NULL) receives the measured microseconds per variant
- * (n entries, 12 variants: 0-4 one thread per cell with register caps
+ * (n entries, 13 variants: 0-4 one thread per cell with register caps
  * 128/80/64/40/32, 5-7 the block staged in shared memory, caps 128/64/40,
  * 8 the block's tile and face coefficients staged by TMA bulk copies,
  * 9 persistent CTAs streaming blocks through double-buffered bulk copies,
  * 10 two cells per thread (the same cell of two blocks, operands of both
- * gathered before either is updated), cap 64, 11 one warp per 16x16 block
- * of a 2D FP32 sweep with the block in registers: 16-byte loads and stores,
- * neighbours by shuffles (elsewhere the same as 3)) */
+ * gathered before either is updated), cap 64, 11-12 one warp per 16x16
+ * block of a 2D FP32 sweep with the block in registers: 16-byte loads and
+ * stores, neighbours by shuffles, caps 64/48 (elsewhere the same as 3)) */
 int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n);
 /* level of the device solve's dense bottom solve once prepared (-1 before) */
 int32_t sayaka_mac_bottom_level(const sayaka_mac *h);

@@ -526,8 +526,8 @@ class MacSolver:
 
     def tuned_smoother(self, precision):
         """(chosen variant, microseconds per variant) of the smoother autotuner"""
-        us = (C.c_float * 12)()
-        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 12)
+        us = (C.c_float * 13)()
+        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 13)
         return int(v), [float(x) for x in us]
 
     def problem_count(self):

@@ -170,7 +170,7 @@ void launch_smooth(const Topo &t, const Coef<T> &c, const BlockList &L, int colo
                    const T *rhs, const int *guard, cudaStream_t s, bool pdl = false);
 // the device solve's smoother (smooth_cell_fast); `variant` picks the
 // launch bounds (0..kRbgsVariants-1), chosen per workload by the autotuner
-constexpr int kRbgsVariants = 12;
+constexpr int kRbgsVariants = 13;
 // error word of the bulk-copy smoother variant (an mbarrier wait timed out);
 // read (and cleared) by the host after a solve
 int rbgs_bulk_error(bool clear);

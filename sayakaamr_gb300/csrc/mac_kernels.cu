@@ -210,14 +210,13 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_warp16(Topo t, Coef<flo
     const float from_left = __shfl_up_sync(0xffffffffu, v[7], 1);
     const float from_right = __shfl_down_sync(0xffffffffu, v[0], 1);
     const int par = (color + j) & 1;  // column parity of this row's cells of the colour
-    float dn[8], up[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      dn[k] = __shfl_up_sync(0xffffffffu, v[k], 2);
-      up[k] = __shfl_down_sync(0xffffffffu, v[k], 2);
-    }
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
+      // rows j-1 and j+1 from lanes l-2 and l+2; their column-k cell has the
+      // other colour (their row parity differs), so it is still the old value
+      // even after those lanes updated their own cells in place
+      const float dnk = __shfl_up_sync(0xffffffffu, v[k], 2);
+      const float upk = __shfl_down_sync(0xffffffffu, v[k], 2);
       if ((k & 1) != par) continue;
       const int i = c0 + k;
       float diag = c.alpha * dv;
@@ -240,7 +239,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_warp16(Topo t, Coef<flo
       }
       // f = 2: down
       if (j > 0 || ty[2] == 0) {
-        const float nbv = j > 0 ? dn[k] : hv[k];
+        const float nbv = j > 0 ? dnk : hv[k];
         diag += T1;
         off = fma_t(T1, nbv, off);
       } else if (dir[2]) {
@@ -248,7 +247,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_warp16(Topo t, Coef<flo
       }
       // f = 3: up
       if (j < NB - 1 || ty[3] == 0) {
-        const float nbv = j < NB - 1 ? up[k] : hv[k];
+        const float nbv = j < NB - 1 ? upk : hv[k];
         diag += T1;
         off = fma_t(T1, nbv, off);
       } else if (dir[3]) {
@@ -1357,8 +1356,9 @@ static void rbgs_go(const Topo &t, const Coef<T> &c, const BlockList &L, int col
   launch_k(pdl, k_rbgs<T, ND, MINB>, grid, threads, 0, s, t, c, L, color, phi, rhs, guard);
 }
 
-// variant 10: CPT = 2 cells per thread (k_rbgs_ilp), cap 64; variant 11: one
-// warp per 16x16 block in 2D FP32 (k_rbgs_warp16), elsewhere variant 3
+// variant 10: CPT = 2 cells per thread (k_rbgs_ilp), cap 64; variants 11, 12:
+// one warp per 16x16 block in 2D FP32 (k_rbgs_warp16, caps 64 and 48),
+// elsewhere variant 3
 template <typename T, int ND, int MINB, int CPT>
 static void rbgs_ilp_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
                         const int *guard, cudaStream_t s, bool pdl, dim3 grid, int threads) {
@@ -1372,10 +1372,14 @@ static void rbgs_nd(int variant, const Topo &t, const Coef<T> &c, const BlockLis
   switch (variant) {
     case 10: rbgs_ilp_go<T, ND, 4, 2>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); return;
     case 11:
+    case 12:
       if constexpr (ND == 2 && sizeof(T) == 4) {
         if (t.nb == 16) {
           const int g = std::min((L.n + 7) / 8, 152 * 64);
-          launch_k(pdl, k_rbgs_warp16<4>, g, kThreads, 0, s, t, c, L, color, phi, rhs, guard);
+          if (variant == 11)
+            launch_k(pdl, k_rbgs_warp16<4>, g, kThreads, 0, s, t, c, L, color, phi, rhs, guard);
+          else
+            launch_k(pdl, k_rbgs_warp16<5>, g, kThreads, 0, s, t, c, L, color, phi, rhs, guard);
           return;
         }
       }

@@ -113,7 +113,7 @@ def test_smoother_variants_are_bit_identical(name, precision):
     g, t, tb, S = setup_solver(name)
     S.set_rhs_compact(g["sv_rhs"])
     out = []
-    for var in (-1, 0, 4, 5, 7, 8, 9, 10, 11):
+    for var in (-1, 0, 4, 5, 7, 8, 9, 10, 11, 12):
         S.set_zero_sol()
         S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=precision, bottom=1,
                      smooth_variant=var)
@@ -122,7 +122,7 @@ def test_smoother_variants_are_bit_identical(name, precision):
         out.append((info["iterations"], S.get_sol_compact()))
         if var == -1:
             v, us = S.tuned_smoother(precision)
-            assert 0 <= v < 12 and all(u > 0 for u in us), (v, us)
+            assert 0 <= v < 13 and all(u > 0 for u in us), (v, us)
     for k in range(1, len(out)):
         assert out[0][0] == out[k][0], k
         assert np.array_equal(out[0][1], out[k][1]), k
