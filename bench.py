@@ -702,9 +702,9 @@ def main():
 def _elbow_geometry(torch, tb, sc, seed):
     """the step's level set on every block's grown box (1 ghost layer, the
     reference's TreeData layout) and its right-hand side on every block's
-    cells, computed with torch on the GPU and copied to host memory: fluid
-    = inside the tube and outside the sphere; rhs = -(8 seeded Gaussians,
-    sigma 0.08) on the leaf blocks"""
+    cells, computed with torch on the GPU and left there (the solver reads
+    them in place): fluid = inside the tube and outside the sphere; rhs =
+    -(8 seeded Gaussians, sigma 0.08) on the leaf blocks"""
     from sayakaamr_gb300 import workloads as W
     dev = "cuda"
     n, nb = tb["num_blocks"], tb["nb"]
@@ -739,10 +739,7 @@ def _elbow_geometry(torch, tb, sc, seed):
         sp = torch.linalg.norm(p - torch.as_tensor(sc, device=dev), dim=-1) - W.SPHERE_R
         return torch.minimum(W.ELBOW_TUBE - d, sp)
 
-    ls = level_set(centres(nb + 2, -0.5)).reshape(-1)
-    # host copies in pinned memory (the solver's uploads run at full speed)
-    ls_h = torch.empty(ls.shape, dtype=torch.float64, pin_memory=True)
-    ls_h.copy_(ls)
+    ls = level_set(centres(nb + 2, -0.5)).reshape(-1).contiguous()
     pc = centres(nb, 0.5)
     g = torch.Generator(device="cpu").manual_seed(seed)
     amp = torch.randn(8, generator=g, dtype=torch.float64).to(dev)
@@ -751,10 +748,8 @@ def _elbow_geometry(torch, tb, sc, seed):
     for q in range(8):
         f += amp[q] * torch.exp(-((pc - cen[q]) ** 2).sum(-1) / (2 * 0.08 ** 2))
     leaf = torch.as_tensor(tb["node_type"] == 1, device=dev)
-    rhs = (-f * leaf[:, None]).reshape(-1)
-    rhs_h = torch.empty(rhs.shape, dtype=torch.float64, pin_memory=True)
-    rhs_h.copy_(rhs)
-    return ls_h.numpy(), rhs_h.numpy()
+    rhs = (-f * leaf[:, None]).reshape(-1).contiguous()
+    return ls, rhs
 
 
 def run_sequence(args, torch, ws, rank, local):
@@ -821,7 +816,7 @@ def run_sequence(args, torch, ws, rank, local):
             S2 = sg.MacSolver(tb)
             S2.set_bc(bc.reshape(-1))
             ta = mark("create", t0, S2)
-            S2.set_ib_frac_by_ls(ls, ncomp=1, ngrow=1, comp=0)
+            S2.set_ib_frac_by_ls_device(ls.data_ptr(), ngrow=1)
             ta = mark("fractions", ta, S2)
             S2.set_params(**prm)
             if S is None:
@@ -831,9 +826,9 @@ def run_sequence(args, torch, ws, rank, local):
             ta = mark("transfer", ta, S2)
             S = S2
         else:
-            S.set_ib_frac_by_ls(ls, ncomp=1, ngrow=1, comp=0)
+            S.set_ib_frac_by_ls_device(ls.data_ptr(), ngrow=1)
             ta = mark("fractions", t0, S)
-        S.set_rhs_compact(rhs)
+        S.set_rhs_device(rhs.data_ptr())
         ta = mark("rhs", ta, S)
         S.prepare()
         mark("prepare", ta, S)

@@ -149,6 +149,13 @@ typedef struct sayaka_params {
   int32_t learned_tc05;   /* learned correction of 16x16-cell blocks: 1 = its 32 -> 32 layer as an implicit GEMM
                              on tcgen05 with the accumulator in tensor memory (default); 0 = on mma.sync warp
                              MMAs (the same network, products summed in another order) */
+  int32_t vcycle_out;     /* how the FP64 kernels read the FP32 V-cycle's output: 0 = by tower size (in place,
+                             with an exact widening on the integer pipe, up to 2,097,152 tower cells; widened
+                             once into FP64 vectors above; default), 1 = always in place, 2 = always widened */
+  int32_t prolong_form;   /* device V-cycle, the prolongation fused with the first red sweep of its level:
+                             1 = one warp per block with the block in registers (2D FP32 16x16 blocks,
+                             default; elsewhere form 0), 0 = one CTA per block with a shared-memory tile; the
+                             same values */
   int32_t learned_loss;   /* training loss of the learned correction u: 0 = the residual u leaves under the
                              block-local operator (default); 1 = the distance of u to the block-local part of the
                              error the V-cycle left, known from the solver's own converged solution */
@@ -181,6 +188,11 @@ int sayaka_mac_set_coef_b(sayaka_mac *h, int32_t dir, const double *face, int32_
 /* setIBFracByLS (src/SayakaMacIB.cpp:34-154): binary fractions, ls <= 0
  * solid; ls cell data with ngrow >= 1 */
 int sayaka_mac_set_ib_frac_by_ls(sayaka_mac *h, const double *ls, int32_t ncomp, int32_t ngrow, int32_t comp);
+/* the same from one component given as the grown boxes of every block back
+ * to back ((nb + 2 ngrow)^ndim values per block, i fastest); `on_device` != 0:
+ * the pointer is device memory (a level set computed on the GPU is used
+ * where it lies, no host round trip) */
+int sayaka_mac_set_ib_frac_by_ls_compact(sayaka_mac *h, const double *ls, int32_t ngrow, int32_t on_device);
 /* fractional IB fractions on leaf blocks (the protected m_ib_volfrac /
  * m_ib_areafrac of src/SayakaMacSolver.h:383-384), then the same c/f AVG sync
  * and AVG restriction; compact arrays, area[d] for d < ndim */

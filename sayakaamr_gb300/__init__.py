@@ -43,7 +43,8 @@ class Params(C.Structure):
                 ("bottom_level", C.c_int32), ("bottom_half", C.c_int32), ("sublevel_order", C.c_int32),
                 ("smoother", C.c_int32), ("inner_sweeps", C.c_int32), ("per_problem", C.c_int32),
                 ("uniform", C.c_int32), ("bottom_refresh", C.c_int32),
-                ("learned_tc05", C.c_int32), ("learned_loss", C.c_int32)]
+                ("learned_tc05", C.c_int32), ("vcycle_out", C.c_int32), ("prolong_form", C.c_int32),
+                ("learned_loss", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -77,6 +78,7 @@ SIGNATURES = {
     "sayaka_mac_set_coef_b": (C.c_int, [_V, C.c_int32, _f64p, C.c_int32, C.c_int32, C.c_int32]),
     "sayaka_mac_set_ib_frac_by_ls": (C.c_int, [_V, _f64p, C.c_int32, C.c_int32, C.c_int32]),
     "sayaka_mac_set_ib_frac_compact": (C.c_int, [_V, _f64p, _f64p, _f64p, _f64p]),
+    "sayaka_mac_set_ib_frac_by_ls_compact": (C.c_int, [_V, _V, C.c_int32, C.c_int32]),
     "sayaka_mac_set_bc": (C.c_int, [_V, _i32p]),
     "sayaka_mac_fix_bc": (C.c_int, [_V, _f64p, C.c_int32, C.c_int32, C.c_int32, _f64p, C.c_int32, C.c_int32,
                                     C.c_int32]),
@@ -344,6 +346,16 @@ class MacSolver:
     def set_ib_frac_by_ls(self, ls, ncomp=1, ngrow=1, comp=0):
         a, p = _f64(ls)
         _check(self.lib.sayaka_mac_set_ib_frac_by_ls(self.h, p, ncomp, ngrow, comp), "set_ib_frac_by_ls", self.h)
+
+    def set_ib_frac_by_ls_device(self, ptr, ngrow=1):
+        """binary fractions from a level set already on the device: ptr is the
+        device address of every block's grown box (one component)"""
+        _check(self.lib.sayaka_mac_set_ib_frac_by_ls_compact(self.h, C.c_void_p(int(ptr)), int(ngrow), 1),
+               "set_ib_frac_by_ls", self.h)
+
+    def set_rhs_device(self, ptr):
+        """the right-hand side from device memory (compact, all blocks)"""
+        _check(self.lib.sayaka_mac_set_rhs_compact(self.h, C.c_void_p(int(ptr)), 1), "set_rhs", self.h)
 
     def set_ib_frac_compact(self, vol, areas):
         v, pv = _f64(vol)

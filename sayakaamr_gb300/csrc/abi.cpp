@@ -418,6 +418,8 @@ void sayaka_params_default(sayaka_params *p) {
   p->bottom_refresh = d.bottom_refresh;
   p->learned_tc05 = d.learned_tc05;
   p->learned_loss = d.learned_loss;
+  p->prolong_form = d.prolong_form;
+  p->vcycle_out = d.vcycle_out;
 }
 
 int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
@@ -518,6 +520,14 @@ int sayaka_mac_set_ib_frac_by_ls(sayaka_mac *h, const double *ls, int32_t ncomp,
       std::memcpy(&grown[(size_t)b * L.cap], ls + (size_t)b * L.cap * ncomp + (size_t)comp * L.cap,
                   L.cap * sizeof(double));
     g.set_ib_frac_by_ls(grown.data(), ngrow);
+    return (int)SAYAKA_OK;
+  });
+}
+
+int sayaka_mac_set_ib_frac_by_ls_compact(sayaka_mac *h, const double *ls, int32_t ngrow, int32_t on_device) {
+  return guarded(h, [&] {
+    if (!ls || ngrow < 1 || ngrow > 8) return (int)SAYAKA_BAD_INPUT;
+    h->gpu->set_ib_frac_by_ls(ls, ngrow, on_device != 0);
     return (int)SAYAKA_OK;
   });
 }
@@ -662,6 +672,10 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.learned_tc05 = p->learned_tc05;
     if (p->learned_loss < 0 || p->learned_loss > 1) return (int)SAYAKA_BAD_INPUT;
     s.learned_loss = p->learned_loss;
+    if (p->prolong_form < 0 || p->prolong_form > 1) return (int)SAYAKA_BAD_INPUT;
+    s.prolong_form = p->prolong_form;
+    if (p->vcycle_out < 0 || p->vcycle_out > 2) return (int)SAYAKA_BAD_INPUT;
+    s.vcycle_out = p->vcycle_out;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
   });

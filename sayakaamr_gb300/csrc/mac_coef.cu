@@ -329,28 +329,33 @@ void MacGpu::set_ib_frac_leaf(const double *vol_all, const double *const area_al
 }
 
 // binary fractions from a level set (every block's grown box, ng >= 1
-// ghost layers, ls <= 0 solid), computed on the finest tower's blocks
-void MacGpu::set_ib_frac_by_ls(const double *ls, int ng) {
+// ghost layers, ls <= 0 solid; host or, with dev, device memory), computed
+// on the finest tower's blocks
+void MacGpu::set_ib_frac_by_ls(const double *ls, int ng, bool dev) {
   const int nd = tt_.ndim, G = tt_.nb + 2 * ng;
   const size_t gsz = nd == 3 ? (size_t)G * G * G : (size_t)G * G;
   const size_t bytes = (size_t)tt_.num_blocks * gsz * sizeof(double);
-  if (bytes > ls_cap_) {
-    CK(cudaStreamSynchronize(stream_));
-    if (d_ls_) cudaFree(d_ls_);
-    d_ls_ = nullptr;
-    ls_cap_ = 0;
-    if (cudaMalloc(&d_ls_, bytes) != cudaSuccess) {
-      fail("out of device memory (level set)");
-      return;
+  const double *src = ls;
+  if (!dev) {  // staged in a device buffer kept for the next call
+    if (bytes > ls_cap_) {
+      CK(cudaStreamSynchronize(stream_));
+      if (d_ls_) cudaFree(d_ls_);
+      d_ls_ = nullptr;
+      ls_cap_ = 0;
+      if (cudaMalloc(&d_ls_, bytes) != cudaSuccess) {
+        fail("out of device memory (level set)");
+        return;
+      }
+      ls_cap_ = bytes;
     }
-    ls_cap_ = bytes;
+    CK(cudaMemcpyAsync(d_ls_, ls, bytes, cudaMemcpyHostToDevice, stream_));
+    src = d_ls_;
   }
-  CK(cudaMemcpyAsync(d_ls_, ls, bytes, cudaMemcpyHostToDevice, stream_));
   const DevTower &tw = towers_[finest_];
   Faces fa{{d_afrac_[0], d_afrac_[1], d_afrac_[2]}};
   const long work = (long)tw.all.n * (ncell_ + nd * nfb_);
   if (work)
-    k_ls_frac<<<cgrid(work), kCT, 0, stream_>>>(nd, tt_.nb, ncell_, nfb_, tw.all.blocks, tw.all.n, d_ls_, ng, d_vf_,
+    k_ls_frac<<<cgrid(work), kCT, 0, stream_>>>(nd, tt_.nb, ncell_, nfb_, tw.all.blocks, tw.all.n, src, ng, d_vf_,
                                                 fa);
   coef_average((1 << nd) - 1, d_afrac_, d_vf_);
   coef_changed();

@@ -192,9 +192,10 @@ void launch_prolong(const Topo &t, const Coef<T> &c, const BlockList &fine, T *p
 template <typename T>
 // X: a list (with halo descriptors) whose red cells are swept in the same
 // launch, blocks that neither read nor are read by L's level
+// form 1: one warp per block (2D FP32 16x16 blocks; elsewhere the CTA form 0)
 void launch_prolong_red(const Topo &t, const Coef<T> &c, const BlockList &L, T *phi, const T *rhs,
                         const int *guard, cudaStream_t s, bool pdl = false,
-                        const BlockList &X = BlockList{nullptr, nullptr, 0});
+                        const BlockList &X = BlockList{nullptr, nullptr, 0}, int form = 0);
 
 // block-hybrid Gauss-Seidel pass (Gauss-Seidel inside a block, Jacobi
 // between blocks): nsweep red-black sweeps of every block of L from src's

@@ -854,6 +854,13 @@ void MacGpu::ensure_fast_buffers() {
   fast_ready_ = true;
 }
 
+// the FP64 smoother factors of the current coefficients, built on first need
+void MacGpu::ensure_smooth_factors() {
+  if (sfac_version_ == coef_version_) return;
+  build_smooth_factors();
+  sfac_version_ = coef_version_;
+}
+
 // FP64 smoother factors for the towers the V-cycle smooths (2 .. finest)
 void MacGpu::build_smooth_factors() {
   if ((int)d_sfac_.size() < finest_ + 1) d_sfac_.resize(finest_ + 1, nullptr);
@@ -1395,7 +1402,7 @@ void MacGpu::vcycle_device(int L, T *resid, T *corr, const Coef<T> &c, double *o
     // sublevels l-2, l-4, ...) rides in the same launch
     const BlockList rest0 = prm_.sublevel_order == 1 ? parity_list(l, 0, true) : BlockList{nullptr, nullptr, 0};
     if (fused)
-      launch_prolong_red<T>(topo_, c, top, corr, resid, guard, stream_, prm_.pdl != 0, rest0);
+      launch_prolong_red<T>(topo_, c, top, corr, resid, guard, stream_, prm_.pdl != 0, rest0, prm_.prolong_form);
     else
       launch_prolong<T>(topo_, c, level_list(l), corr, guard, stream_, prm_.pdl != 0);
     for (int s = 0; s < prm_.n_post; s++) {
@@ -1480,7 +1487,8 @@ template <typename T>
 void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
   const long w = (long)tower_list(finest_).n * ncell_;
   if constexpr (sizeof(T) == 4) {
-    if (!learned_active() && w < kDirectF32Cells) {
+    const bool direct = prm_.vcycle_out == 1 || (prm_.vcycle_out == 0 && w < kDirectF32Cells);
+    if (!learned_active() && direct) {
       iteration_body<T, float>(resid, corr, c, corr, corr, nullptr, nullptr);
       return;
     }
@@ -1634,6 +1642,8 @@ void MacGpu::capture_loop(int precision) {
   graph_inner_ = prm_.inner_sweeps;
   graph_multi_ = (int)multi();
   graph_uniform_ = prm_.uniform;
+  graph_pform_ = prm_.prolong_form;
+  graph_vout_ = prm_.vcycle_out;
 }
 
 // the captured graph was recorded with other parameters than the current ones
@@ -1642,7 +1652,8 @@ bool MacGpu::graph_stale() const {
          graph_coop_ != prm_.vcycle_kernel || graph_pdl_ != prm_.pdl || graph_cc_ != prm_.cluster_cells ||
          graph_var_ != rbgs_variant_[prm_.precision == 1] || graph_nn_ != (int)learned_active() ||
          graph_order_ != prm_.sublevel_order || graph_smoother_ != prm_.smoother ||
-         graph_inner_ != prm_.inner_sweeps || graph_multi_ != (int)multi() || graph_uniform_ != prm_.uniform;
+         graph_inner_ != prm_.inner_sweeps || graph_multi_ != (int)multi() || graph_uniform_ != prm_.uniform ||
+         graph_pform_ != prm_.prolong_form || graph_vout_ != prm_.vcycle_out;
 }
 
 int MacGpu::cg_solve_device(SolveInfo *info) {
@@ -1767,7 +1778,6 @@ int MacGpu::prepare_device() {
     refresh_fp32();
     build_uniform();
     build_op_factors();
-    build_smooth_factors();
     if (prm_.bottom_refresh || !bottom_ready_ || bot_param_ != prm_.bottom_level || bot_half_ != prm_.bottom_half)
       build_bottom();
     fast_coef_version_ = coef_version_;
@@ -1783,6 +1793,9 @@ int MacGpu::prepare_device() {
     if (!err_.empty()) return -1;
   }
   bind_uniform();
+  // the FP64 smoother factors serve the FP64 V-cycle and the learned
+  // correction only: an FP32 solve does not build them
+  if (prm_.precision == 0 || learned_active()) ensure_smooth_factors();
   tune_smoother(prm_.precision);
   if (learned_active()) learned_prepare();
   if (!err_.empty()) return -1;
@@ -1885,6 +1898,7 @@ int MacGpu::enqueue_kernel(int which, int L) {
   if (L < 1 || L > tt_.max_level || towers_[L].all.n == 0) return -1;
   ensure_fast_buffers();
   bind_uniform();
+  if (which == 2) ensure_smooth_factors();
   if (which == 0) {
     launch_apply<double>(topo_, c64_, tower_list(L), vec_[kSOL], vec_[kV], nullptr, nullptr, stream_);
   } else if (which == 1) {
@@ -1925,6 +1939,7 @@ int MacGpu::device_kernel_compact(int which, int L, int variant, const double *i
   if (which == 1 && variant >= kRbgsVariants) return 1;
   if (which == 2 && (variant < 1 || variant > 1024)) return 1;
   if (prepare_device() != 0) return 2;
+  ensure_smooth_factors();
   const size_t n = (size_t)tt_.num_blocks * ncell_;
   if (which == 0) {
     const BlockList TL = tower_list(finest_);

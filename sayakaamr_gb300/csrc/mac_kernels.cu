@@ -135,6 +135,150 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_ilp(Topo t, Coef<T> c, 
   }
 }
 
+// (fluid: block b is known to have vf = 1 everywhere)
+template <typename T, int ND>
+__device__ __forceinline__ T prolonged_value(const Topo &t, const Coef<T> &c, int b, const int ijk[3],
+                                             const T *__restrict__ phi, int pw = -1, bool fluid = false) {
+  const int nb = t.nb, half = nb >> 1;
+  const int P = pw >= 0 ? pw >> 3 : t.parent[b], wc = pw >= 0 ? pw & 7 : t.which_child[b];
+  int pc[3] = {0, 0, 0};
+  for (int q = 0; q < ND; q++) pc[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
+  const long q = (long)b * t.ncell + encode(ijk, nb);
+  return (fluid || c.vf[q] > 0) ? phi[(long)P * t.ncell + encode(pc, nb)] : (T)0;
+}
+
+// One warp updates the cells of colour `color` of one 16x16 block of a 2D
+// FP32 sweep, any block: lane l holds row l/2, columns 8(l%2) .. +7 in
+// registers, v[] (PROLONG: the block's values prolonged from its parent,
+// masked by vf, as k_prolong_red's tile; else phi), neighbours inside the
+// block from registers and shuffles, every boundary face by its type as
+// smooth_cell_fast and k_prolong_red take it (same-level: the neighbour's
+// value, prolonged from its own parent when PROLONG; coarse/fine: the
+// coarse ghost or the fine-side sum; physical: the diagonal term), face
+// coefficients from the block record or the face arrays; the whole block is
+// written back.  Per cell the operations are those of smooth_cell_fast /
+// k_prolong_red in the same order: the same bits.
+template <bool PROLONG>
+__device__ __forceinline__ void warp_block16(const Topo &t, const Coef<float> &c, int b, uint16_t ft, const int *e,
+                                             int color, float *__restrict__ phi, const float *__restrict__ rhs,
+                                             int lane) {
+  constexpr int NB = 16, NC = 256;
+  const int j = lane >> 1, hh = lane & 1, c0 = 8 * hh;
+  const long cb = (long)b * NC, fb = (long)b * t.nfb;
+  const float *u = uniform_of(c, b);
+  float v[8];
+  if constexpr (PROLONG) {
+    const int pw = e ? e[kHXPar + 6] : t.parent[b] * 8 + t.which_child[b];
+    const int P = pw >> 3, wc = pw & 7;
+    const float4 q4 = *reinterpret_cast<const float4 *>(phi + (long)P * NC + (8 * ((wc >> 1) & 1) + (j >> 1)) * NB +
+                                                         8 * (wc & 1) + 4 * hh);
+    const float pv[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = (u || c.vf[cb + j * NB + c0 + k] > 0) ? pv[k >> 1] : 0.f;
+  } else {
+    const float4 *src = reinterpret_cast<const float4 *>(phi + cb + j * NB + c0);
+    const float4 p0 = src[0], p1 = src[1];
+    v[0] = p0.x, v[1] = p0.y, v[2] = p0.z, v[3] = p0.w, v[4] = p1.x, v[5] = p1.y, v[6] = p1.z, v[7] = p1.w;
+  }
+  const float4 *rsrc = reinterpret_cast<const float4 *>(rhs + cb + j * NB + c0);
+  const float4 r0 = rsrc[0], r1 = rsrc[1];
+  const float r[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+  const float dv = geom(c, b, 6);
+  const float from_left = __shfl_up_sync(0xffffffffu, v[7], 1);
+  const float from_right = __shfl_down_sync(0xffffffffu, v[0], 1);
+  const int par = (color + j) & 1;
+  // value across boundary face f of cell ijk (same-level, coarse/fine)
+  auto across = [&](int f, const int ijk[3], int ty) -> float {
+    if (ty == 0) {
+      const int n = e ? e[f] : t.neighbor[b * 6 + f];
+      int ni[3] = {ijk[0], ijk[1], 0};
+      ni[f >> 1] = (f & 1) ? 0 : NB - 1;
+      if constexpr (PROLONG)
+        return prolonged_value<float, 2>(t, c, n, ni, phi, e ? e[kHXPar + f] : -1);
+      else
+        return phi[(long)n * NC + ni[0] + NB * ni[1]];
+    }
+    return fine_crse_ghost<float, 2, false>(t, b, f, ijk, phi, e);
+  };
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const float dnk = __shfl_up_sync(0xffffffffu, v[k], 2);
+    const float upk = __shfl_down_sync(0xffffffffu, v[k], 2);
+    if ((k & 1) != par) continue;
+    const int i = c0 + k;
+    const int ijk[3] = {i, j, 0};
+    float diag = c.alpha * dv;
+    float off = 0.f;
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+      const int d = f >> 1, sd = f & 1;
+      const bool bnd = d == 0 ? (sd ? i == NB - 1 : i == 0) : (sd ? j == NB - 1 : j == 0);
+      const int fx = d == 0 ? i + sd + (NB + 1) * j : i + NB * (j + sd);
+      if (!bnd) {
+        const float coef = u ? u[d] : c.tff[d][fb + fx];
+        float nbv;
+        if (f == 0)
+          nbv = k > 0 ? v[k - 1] : from_left;
+        else if (f == 1)
+          nbv = k < 7 ? v[k + 1] : from_right;
+        else if (f == 2)
+          nbv = dnk;
+        else
+          nbv = upk;
+        diag += coef;
+        off = fma_t(coef, nbv, off);
+        continue;
+      }
+      const int ty = face_type_of(ft, f);
+      if (ty == 0) {
+        const float coef = u ? u[d] : c.tff[d][fb + fx];
+        diag += coef;
+        off = fma_t(coef, across(f, ijk, 0), off);
+      } else if (ty == 1) {
+        if (t.bc_type[b * 6 + f] != kBCNeumann) diag += (u ? u[d] : c.tff[d][fb + fx]) * 2.0f;
+      } else if (ty == 2) {
+        const float coef = cf_coef(c, t, b, d, fx, 1.5f);
+        diag += coef;
+        off = fma_t(coef, across(f, ijk, 2), off);
+      } else {
+        diag += cf_coef(c, t, b, d, fx, 0.75f);
+        off = fma_t(1.0f, crse_fine_sum<float, 2, false>(t, c, b, f, ijk, phi, e), off);
+      }
+    }
+    const float vfv = u ? 1.0f : c.vf[cb + j * NB + i];
+    v[k] = (vfv > 0.f && diag > 0.f) ? fast_div(fma_t(r[k] * dv, vfv, off), diag) : 0.f;
+  }
+  float4 *dst = reinterpret_cast<float4 *>(phi + cb + j * NB + c0);
+  dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+  dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+
+// prolongation of a level fused with its first red sweep (k_prolong_red's
+// values), 2D FP32 16x16 blocks, one warp per block of L, then one warp per
+// block of X for the red sweep of the coarser same-parity sublevels
+template <int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_prolong_red_warp16(Topo t, Coef<float> c, BlockList L,
+                                                                       float *__restrict__ phi,
+                                                                       const float *__restrict__ rhs,
+                                                                       const int *guard, BlockList X) {
+  pdl_enter();
+  if (guard && *guard) return;
+  const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+  for (int p = blockIdx.x * warps + (threadIdx.x >> 5); p < L.n + X.n; p += gridDim.x * warps) {
+    const bool top = p < L.n;
+    const BlockList &Q = top ? L : X;
+    const int q = top ? p : p - L.n;
+    const int *e = Q.hx ? Q.hx + (long)q * kHX : nullptr;
+    const int b = e ? e[kHXBlock] : Q.blocks[q];
+    if (Q.stc && block_off(Q, b)) continue;  // uniform over the warp
+    const uint16_t ft = e ? (uint16_t)(e[kHXInfo] & 0xffff) : Q.ftypes[q];
+    if (top)
+      warp_block16<true>(t, c, b, ft, e, 0, phi, rhs, lane);
+    else
+      warp_block16<false>(t, c, b, ft, e, 0, phi, rhs, lane);
+  }
+}
+
 // The 2D sweep of 16x16 blocks with one warp per block: lane l holds row
 // l/2, columns 8(l%2) .. 8(l%2)+7 of phi and rhs in registers (two 16-byte
 // loads each), neighbours inside the block come from the lane's own
@@ -167,7 +311,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_warp16(Topo t, Coef<flo
 #pragma unroll
     for (int f = 0; f < 4; f++) fast = fast && face_type_of(ft, f) <= 1;
     if (!fast) {
-      // four cells of the colour per lane, as k_rbgs does them
+      // four cells of the colour per lane, as k_rbgs does them (measured
+      // faster for these blocks than warp_block16's register form)
       for (int k = 0; k < 4; k++) {
         const int h = lane * 4 + k;  // half-cell index 0..127
         int ijk[3];
@@ -1173,17 +1318,6 @@ int rbgs_bulk_error(bool clear) {
 // fly from their own parents, coarse neighbours (FINE_CRSE) are read as they
 // are; the red cells are then updated with the tiled sweep's arithmetic and
 // the whole tile is written.  Same values as k_prolong + k_rbgs_tile.
-// (fluid: block b is known to have vf = 1 everywhere)
-template <typename T, int ND>
-__device__ __forceinline__ T prolonged_value(const Topo &t, const Coef<T> &c, int b, const int ijk[3],
-                                             const T *__restrict__ phi, int pw = -1, bool fluid = false) {
-  const int nb = t.nb, half = nb >> 1;
-  const int P = pw >= 0 ? pw >> 3 : t.parent[b], wc = pw >= 0 ? pw & 7 : t.which_child[b];
-  int pc[3] = {0, 0, 0};
-  for (int q = 0; q < ND; q++) pc[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
-  const long q = (long)b * t.ncell + encode(ijk, nb);
-  return (fluid || c.vf[q] > 0) ? phi[(long)P * t.ncell + encode(pc, nb)] : (T)0;
-}
 
 template <typename T, int ND>
 __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, BlockList L, T *__restrict__ phi,
@@ -1318,9 +1452,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
 
 template <typename T>
 void launch_prolong_red(const Topo &t, const Coef<T> &c, const BlockList &L, T *phi, const T *rhs,
-                        const int *guard, cudaStream_t s, bool pdl, const BlockList &X) {
+                        const int *guard, cudaStream_t s, bool pdl, const BlockList &X, int form) {
   if (L.n == 0) return;
   if (X.n > 0 && !X.hx) return;  // the extra sweep reads its blocks through halo descriptors
+  if constexpr (sizeof(T) == 4) {
+    if (form == 1 && t.ndim == 2 && t.nb == 16) {
+      const int g = std::min((L.n + X.n + 7) / 8, 152 * 64);
+      launch_k(pdl, k_prolong_red_warp16<5>, g, kThreads, 0, s, t, c, L, phi, rhs, guard, X);
+      return;
+    }
+  }
   const int nface = t.ndim == 3 ? t.nb * t.nb : t.nb;
   const size_t smem = sizeof(T) * ((size_t)t.ncell + 3 * 2 * t.ndim * (size_t)nface);
   ensure_max_smem(t.ndim == 2 ? (const void *)k_prolong_red<T, 2> : (const void *)k_prolong_red<T, 3>, 200 * 1024);
@@ -1522,7 +1663,7 @@ void launch_fix_bc(const Topo &t, const Coef<double> &c, const BlockList &L, con
   template void launch_prolong<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const int *,          \
                                   cudaStream_t, bool);                                                          \
   template void launch_prolong_red<T>(const Topo &, const Coef<T> &, const BlockList &, T *, const T *,        \
-                                      const int *, cudaStream_t, bool, const BlockList &);                      \
+                                      const int *, cudaStream_t, bool, const BlockList &, int);                 \
   template void launch_bhgs<T>(const Topo &, const Coef<T> &, const BlockList &, int, const T *, T *,          \
                                const T *, const int *, cudaStream_t, bool);                                     \
   template void launch_copy_blocks<T>(const BlockList &, int, const T *, T *, const int *, cudaStream_t, bool);

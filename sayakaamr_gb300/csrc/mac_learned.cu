@@ -831,6 +831,7 @@ int MacGpu::learned_collect(int max_iters, int max_samples) {
     prm_ = save;
     return -1;
   }
+  ensure_smooth_factors();  // sa scales the pairs
   const size_t n = (size_t)tt_.num_blocks * ncell_;
   std::vector<double *> rec;
   record_ = &rec;

@@ -37,6 +37,10 @@ struct SolverParams {
   int smooth_variant = -1;    // device smoother launch bounds: -1 autotune at prepare, else variant index
   int learned = 0;            // device path, FP32 V-cycle: apply the trained block correction
   int fuse_prolong = 1;       // device path: prolongation fused with the first red sweep of its level
+  int vcycle_out = 0;         // FP32 V-cycle output to the FP64 kernels: 0 = in place up to 2M tower cells, else
+                              // widened once into FP64 vectors; 1 = always in place; 2 = always widened
+  int prolong_form = 1;       // that fused launch: 1 = one warp per block (2D FP32 16x16 blocks), 0 = one CTA
+                              // per block with a shared-memory tile (same values)
   int bottom_half = 0;        // device path, FP32 V-cycle, bottom above level 1: 1 = FP16 inverse with row scales
   int bottom_level = 0;       // device path: level of the dense bottom solve; 0 = the coarsest level whose
                               // tower is one uniform level of at most kBottomMaxCells cells per component
@@ -89,7 +93,7 @@ class MacGpu {
   void set_scalars(double alpha, double beta);
   void set_coef_b_leaf(int dir, const double *face_all);       // src/SayakaMacCoef.cpp:36-76
   void set_ib_frac_leaf(const double *vol_all, const double *const area_all[3]);  // src/SayakaMacIB.cpp:34-97
-  void set_ib_frac_by_ls(const double *ls_grown, int ngrow);   // binary fractions from a level set
+  void set_ib_frac_by_ls(const double *ls_grown, int ngrow, bool dev = false);  // binary fractions from a level set
   void set_bc_types(const int *bc6);                            // math BC per block face (-1 interior)
   void get_coef(int which, int dir, double *out_all);           // 0 B, 1 area frac, 2 vol frac
 
@@ -249,6 +253,8 @@ class MacGpu {
   void refresh_fp32();
   void build_op_factors();
   void build_smooth_factors();
+  void ensure_smooth_factors();
+  long sfac_version_ = -1;  // coefficient version of the FP64 smoother factors
   void tune_smoother(int precision);
   template <typename T>
   int rbgs_var() const {
@@ -385,7 +391,8 @@ class MacGpu {
   int graph_prec_ = -1, graph_npost_ = -1;
   int kernels_per_iter_ = 0;
   int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1, graph_nn_ = -1, graph_order_ = -1;
-  int graph_smoother_ = -1, graph_inner_ = -1, graph_multi_ = -1, graph_uniform_ = -1;
+  int graph_smoother_ = -1, graph_inner_ = -1, graph_multi_ = -1, graph_uniform_ = -1, graph_pform_ = -1,
+      graph_vout_ = -1;
   bool last_multi_ = false;  // the last device solve kept one state per problem
   Chunks chunks() const;
   bool graph_stale() const;

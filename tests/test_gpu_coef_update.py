@@ -71,3 +71,29 @@ def test_kept_bottom_inverse_still_converges():
         out.append(_solve(S))
     a, b = out[0][1], out[1][1]
     assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(a)
+
+
+def test_level_set_fractions_from_device_memory():
+    """setIBFracByLS from a level set in device memory (the compact entry
+    point) gives the same fractions as the host TreeData entry point"""
+    import torch
+    p = workloads.config2(max_level=4)
+    tb = p.tables
+    n, nb = tb["num_blocks"], tb["nb"]
+    G = nb + 2
+    lo = tb["block_lo"].reshape(n, 3)[:, :2]
+    dx = tb["block_len"].reshape(n, 3)[:, :2] / nb
+    r = np.arange(G) - 0.5
+    jj, ii = np.meshgrid(r, r, indexing="ij")
+    x = lo[:, None, None, 0] + ii[None] * dx[:, None, None, 0]
+    y = lo[:, None, None, 1] + jj[None] * dx[:, None, None, 1]
+    ls = (np.hypot(x - 0.52, y - 0.47) - 0.17).reshape(-1)
+    A = workloads.make_solver(p, **PARAMS)
+    A.set_ib_frac_by_ls(ls, ncomp=1, ngrow=1, comp=0)
+    B = workloads.make_solver(p, **PARAMS)
+    d = torch.from_numpy(ls).cuda()
+    torch.cuda.synchronize()
+    B.set_ib_frac_by_ls_device(d.data_ptr(), ngrow=1)
+    for which, dd in ((2, 0), (1, 0), (1, 1)):
+        assert np.array_equal(A.get_coef(which, dd), B.get_coef(which, dd)), (which, dd)
+    assert (A.get_coef(2) == 0).any() and (A.get_coef(2) == 1).any()

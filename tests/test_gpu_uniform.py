@@ -107,3 +107,28 @@ def test_warp_per_block_sweep_is_bit_identical(name):
         assert res[0][0] == res[k][0], k
         assert np.array_equal(res[0][1], res[k][1]), k
     assert S.uniform_blocks() > 0
+
+
+@pytest.mark.parametrize("name", ["config2", "config4", "c1"])
+def test_warp_prolongation_is_bit_identical(name):
+    """the prolongation fused with the first red sweep, one warp per block
+    (prolong_form 1, 2D FP32 16x16 blocks) against one CTA per block with a
+    shared-memory tile (prolong_form 0): identical iterations and solutions
+    (c1 has 8x8 blocks, where form 1 falls back to form 0)"""
+    from sayakaamr_gb300 import workloads
+    if name == "c1":
+        g, t, tb, S = setup_solver(name)
+        S.set_rhs_compact(g["sv_rhs"])
+    else:
+        p = workloads.config4(n_problems=6) if name == "config4" else workloads.config2()
+        S = workloads.make_solver(p)
+    res = []
+    for form in (0, 1):
+        S.set_zero_sol()
+        S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=1, bottom=1,
+                     prolong_form=form, smooth_variant=12)
+        info = S.cg_solve()
+        assert info["status"] == 0, info
+        res.append((info["iterations"], S.get_sol_compact()))
+    assert res[0][0] == res[1][0]
+    assert np.array_equal(res[0][1], res[1][1])
