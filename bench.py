@@ -936,13 +936,14 @@ def kernel_only(S, prob, ext, torch, args):
         S.enqueue_kernel(args.kernel, finest)
     b.record(ext)
     torch.cuda.synchronize()
+    cells = S.tower_size(finest, finest) * prob.ncell
     print(json.dumps({"kernel": args.kernel, "config": args.config, "launches": args.steps,
-                      "us_per_launch": a.elapsed_time(b) * 1e3 / args.steps}))
+                      "us_per_launch": a.elapsed_time(b) * 1e3 / args.steps, "cells_of_the_level": cells}))
 
 
 # ncu summaries of the dominant sweep per (workload, V-cycle precision)
 PROFILES = {("config2", 0): "k_rbgs_config2.md", ("config2", 1): "k_rbgs_f32_config2.md",
-            ("config3", 1): "k_rbgs_tile_config3.md"}
+            ("config3", 1): "k_rbgs_tile_config3.md", ("config4", 1): "k_rbgs_warp16_config4.md"}
 
 
 def profiled_traffic(workload, precision):
@@ -993,7 +994,13 @@ def roofline(S, prob, ext, torch, finest, precision):
     achieved = bytes_per_launch / (us * 1e-6) / 1e9
     variant, _ = S.tuned_smoother(precision)
     traffic, traffic_src = profiled_traffic(prob.name, precision)
-    kind = "k_rbgs_tile (block staged in shared memory)" if variant >= 5 else "k_rbgs (one thread per cell)"
+    warp = variant in (11, 12) and prob.ndim == 2 and prob.nb == 16 and p == 4
+    kind = ("k_rbgs (one thread per cell)" if variant <= 4 or (variant >= 11 and not warp) else
+            "k_rbgs_tile (block staged in shared memory)" if variant <= 7 else
+            "k_rbgs_bulk (tile and faces staged by TMA bulk copies)" if variant == 8 else
+            "k_rbgs_stream (persistent, double-buffered bulk copies)" if variant == 9 else
+            "k_rbgs_ilp (two cells per thread)" if variant == 10 else
+            "k_rbgs_warp16 (one warp per block, registers and shuffles)")
     l2 = bytes_per_launch < 100e6
     return {"kernel": "%s<%s,%dD>, autotuned variant %d, finest level, one colour"
                       % (kind, "float" if p == 4 else "double", prob.ndim, variant),

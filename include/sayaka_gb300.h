@@ -149,9 +149,9 @@ typedef struct sayaka_params {
   int32_t learned_tc05;   /* learned correction of 16x16-cell blocks: 1 = its 32 -> 32 layer as an implicit GEMM
                              on tcgen05 with the accumulator in tensor memory (default); 0 = on mma.sync warp
                              MMAs (the same network, products summed in another order) */
-  int32_t vcycle_out;     /* how the FP64 kernels read the FP32 V-cycle's output: 0 = by tower size (in place,
-                             with an exact widening on the integer pipe, up to 2,097,152 tower cells; widened
-                             once into FP64 vectors above; default), 1 = always in place, 2 = always widened */
+  int32_t vcycle_out;     /* how the FP64 kernels read the FP32 V-cycle's output: 0 = in place (an exact widening
+                             on the integer pipe) in 2D and up to 2,097,152 tower cells in 3D, widened once into
+                             FP64 vectors on larger 3D towers (default); 1 = always in place; 2 = always widened */
   int32_t prolong_form;   /* device V-cycle, the prolongation fused with the first red sweep of its level:
                              1 = one warp per block with the block in registers (2D FP32 16x16 blocks,
                              default; elsewhere form 0), 0 = one CTA per block with a shared-memory tile; the

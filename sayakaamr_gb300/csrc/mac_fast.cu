@@ -1478,16 +1478,19 @@ void MacGpu::precondition(int L, T *resid, T *corr, const Coef<T> &c, double *ou
 }
 
 // FP32 V-cycle output read by the FP64 kernels in place (its exact widening
-// is integer work there) up to this many tower cells, where the solve is
-// latency-bound and the two widening launches per iteration cost more;
-// larger towers widen it once into FP64 phat / shat
+// is integer work there) in 2D and up to this many tower cells in 3D, where
+// the two widening launches per iteration cost more than the in-place
+// widenings (batch workload, 2D, 29M cells: 62.9 vs 64.6 ms); larger 3D
+// towers, whose operator reads six neighbours per cell, widen it once into
+// FP64 phat / shat (config3: 29.1 vs 33.7 ms in place)
 constexpr long kDirectF32Cells = 1l << 21;
 
 template <typename T>
 void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
   const long w = (long)tower_list(finest_).n * ncell_;
   if constexpr (sizeof(T) == 4) {
-    const bool direct = prm_.vcycle_out == 1 || (prm_.vcycle_out == 0 && w < kDirectF32Cells);
+    const bool direct =
+        prm_.vcycle_out == 1 || (prm_.vcycle_out == 0 && (tt_.ndim == 2 || w < kDirectF32Cells));
     if (!learned_active() && direct) {
       iteration_body<T, float>(resid, corr, c, corr, corr, nullptr, nullptr);
       return;

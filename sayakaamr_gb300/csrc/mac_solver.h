@@ -37,8 +37,9 @@ struct SolverParams {
   int smooth_variant = -1;    // device smoother launch bounds: -1 autotune at prepare, else variant index
   int learned = 0;            // device path, FP32 V-cycle: apply the trained block correction
   int fuse_prolong = 1;       // device path: prolongation fused with the first red sweep of its level
-  int vcycle_out = 0;         // FP32 V-cycle output to the FP64 kernels: 0 = in place up to 2M tower cells, else
-                              // widened once into FP64 vectors; 1 = always in place; 2 = always widened
+  int vcycle_out = 0;         // FP32 V-cycle output to the FP64 kernels: 0 = in place in 2D and up to 2M tower
+                              // cells in 3D, else widened once into FP64 vectors; 1 = always in place; 2 = always
+                              // widened
   int prolong_form = 1;       // that fused launch: 1 = one warp per block (2D FP32 16x16 blocks), 0 = one CTA
                               // per block with a shared-memory tile (same values)
   int bottom_half = 0;        // device path, FP32 V-cycle, bottom above level 1: 1 = FP16 inverse with row scales
