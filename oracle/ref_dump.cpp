@@ -82,6 +82,7 @@ struct Case {
 	// 1e-6 / 1e-6 stall the outer solve on 16^d-cell blocks: the absolute
 	// bottom tolerance weakens the preconditioner as the residual falls)
 	double bot_tol_rel = 1e-6, bot_tol_abs = 1e-6;
+	int ngrow = 1;     // tree ghost layers (centered-linear prolongation needs 2)
 };
 
 // the reference's AmrTree::init with a chosen block capacity (the reference
@@ -135,8 +136,8 @@ static void build_tree(const Case &c, AmrTree &tree, int cap) {
 	IndexBox vbox(Vector3i::VecMake(0, 0, 0),
 		Vector3i::VecMake(c.nb - 1, c.nb - 1, NDIM == 3 ? c.nb - 1 : 0));
 	tree.blockValidIndex = vbox;
-	tree.blockGrownIndex = IndexBox::Extend(vbox, 1);
-	tree.blockNumGrow = 1;
+	tree.blockGrownIndex = IndexBox::Extend(vbox, c.ngrow);
+	tree.blockNumGrow = c.ngrow;
 	tree_alloc(tree, cap);
 
 	RealBox pbox(c.lo, c.hi);
@@ -768,6 +769,119 @@ static void run_regrid_case(const char *outdir, const std::string &name) {
   fprintf(stderr, "[%s] blocks=%d\n", name.c_str(), tree.numBlocks);
 }
 
+static void dump_tables(Dump &D, const std::string &p, const AmrTree &t) {
+  const int n = t.numBlocks;
+  std::vector<int> level(n), nbr(n * 6), ch(n * 8), par(n), wc(n), nt(n);
+  for (int i = 0; i < n; i++) {
+    level[i] = t[i].refineLevel;
+    par[i] = t[i].parent;
+    wc[i] = t[i].whichChild;
+    nt[i] = t[i].nodeType;
+    for (int f = 0; f < 6; f++) nbr[i * 6 + f] = t[i].neighbor[f];
+    for (int q = 0; q < 8; q++) ch[i * 8 + q] = t[i].child[q];
+  }
+  D.scalar_i(p + "num_blocks", n);
+  D.i32(p + "level", level);
+  D.i32(p + "neighbor", nbr);
+  D.i32(p + "child", ch);
+  D.i32(p + "parent", par);
+  D.i32(p + "which_child", wc);
+  D.i32(p + "node_type", nt);
+}
+
+// A cell field carried across one regrid by the reference itself: the field
+// (two ghost layers) is registered as the tree's state with centered-linear
+// prolongation and average restriction (the pressure settings of
+// src/Test6.h:618-631) and a BC register that uses every math BC kind with
+// non-zero values; random leaf values are averaged down (restrictAll), one
+// regrid refines near a moved circle and coarsens away from it, and
+// AmrTree::initNewBlockDataAfterRegrid fills the new blocks.  The old and new
+// tables and the field before and after are dumped.
+static void run_transfer_case(const char *outdir, const std::string &name) {
+  std::string path = std::string(outdir) + "/" + name + ".bin";
+  Dump D(path.c_str());
+  Case c;
+  c.name = name;
+  for (int d = 0; d < NDIM; d++) c.hi[d] = 1.0;
+  c.nb = NDIM == 3 ? 4 : 8;
+  c.minlevel = 2;
+  c.maxlevel = NDIM == 3 ? 4 : 5;
+  // refinement around a small interior circle (sphere); the regrid then
+  // follows a larger one that crosses the x, y-hi (and z) sides, so that
+  // new blocks appear beside the physical boundaries
+  c.rc[0] = 0.41;
+  c.rc[1] = 0.33;
+  c.rc[2] = 0.45;
+  c.rr = 0.26;
+  c.ngrow = 2;
+  c.seed = NDIM == 3 ? 8803 : 8802;
+  g_seed = c.seed;
+  AmrTree tree;
+  build_tree(c, tree, 20000);
+  std::unique_ptr<TreeData> u(TreeData::CreateCellData(tree, 1, 2));
+  BCPatch bcp;
+  bcp.defineByData(*u);
+  // x-lo Dirichlet 0.75, x-hi SimpleFill -0.5, y-lo and y-hi Neumann, z-lo
+  // Neumann, z-hi Dirichlet 1.5; edges and corners Neumann
+  const int math[6] = {Dirichlet, SimpleFill, Neumann, Neumann, Neumann, Dirichlet};
+  const double val[6] = {0.75, -0.5, 0.0, 0.0, 0.0, 1.5};
+  BCRegister &reg = bcp.boundaryRegister(0);
+  for (int s = 0; s < SurroundingIndex::NumSurr; s++) reg.setBCMap(SurroundingIndex(s), -20, Neumann);
+  std::vector<int> bc_math;
+  std::vector<double> bc_val;
+  for (int f = 0; f < FaceIndex::NumFace; f++) {
+    const SurroundingIndex si = SurroundingIndex::FaceSurrounding(FaceIndex(f));
+    reg.setBCMap(si, -20, math[f]);
+    reg.setBCVal(si, -20, val[f]);
+    bc_math.push_back(math[f]);
+    bc_val.push_back(val[f]);
+  }
+  D.scalar_i("ndim", NDIM);
+  D.scalar_i("nb", c.nb);
+  D.i32("bc_math", bc_math);
+  D.f64("bc_val", bc_val);
+  FillPatch fill(tree, *u);
+  fill.setProlongation(0, InterpPatch::PROLONG_CENTERED_LINEAR);
+  fill.setRestriction(0, InterpPatch::RESTRICT_AVERAGE);
+  fill.setBC(bcp);
+  TreeStateData st;
+  st.new_data = u.get();
+  st.fill_new_patch = &fill;
+  st.bc_patch = &bcp;
+  tree.treeStateData.push_back(st);
+
+  dump_tables(D, "old_", tree);
+  const int ncell = cells_per_block(tree);
+  set_cell(*u, 0, all_blocks(tree), rand_vec(1, (size_t)tree.numBlocks * ncell));
+  fill.restrictAll(0, 1);
+  D.f64("old_x", get_cell(*u, 0, all_blocks(tree)));
+
+  // the circle moves and grows; one regrid pass refines and coarsens
+  c.rc[0] = 0.47;
+  c.rc[1] = 0.71;
+  c.rc[2] = 0.5;
+  c.rr = 0.56;
+  int nref = 0, ncrs = 0;
+  for (int i = 0; i < tree.numBlocks; i++) {
+    tree.refineFlag[i] = 0;
+    tree.coarsenFlag[i] = 0;
+    if (!tree[i].isLeaf()) continue;
+    const bool near = block_straddles(c, tree[i]);
+    if (near && tree[i].getLevel() < c.maxlevel) tree.refineFlag[i] = 1, nref++;
+    if (!near && tree[i].getLevel() > c.minlevel) tree.coarsenFlag[i] = 1, ncrs++;
+  }
+  tree.regrid();
+  tree.initNewBlockDataAfterRegrid();
+  std::vector<int> nc(tree.numBlocks);
+  int nnew = 0;
+  for (int i = 0; i < tree.numBlocks; i++) nc[i] = tree.newChildFlag[i], nnew += nc[i];
+  dump_tables(D, "new_", tree);
+  D.i32("new_child_flag", nc);
+  D.f64("new_x", get_cell(*u, 0, all_blocks(tree)));
+  fprintf(stderr, "[%s] blocks=%d refine flags=%d coarsen flags=%d new blocks=%d\n", name.c_str(), tree.numBlocks,
+          nref, ncrs, nnew);
+}
+
 // ---------------------------------------------------------------------------
 static Case make_case(const std::string &name) {
 	Case c;
@@ -868,6 +982,10 @@ int main(int argc, char **argv) {
 	for (int a = 2; a < argc; a++) {
 		if (std::string(argv[a]).rfind("rg", 0) == 0) {
 			run_regrid_case(argv[1], argv[a]);
+			continue;
+		}
+		if (std::string(argv[a]).rfind("tf", 0) == 0) {
+			run_transfer_case(argv[1], argv[a]);
 			continue;
 		}
 		Case c = make_case(argv[a]);
