@@ -41,6 +41,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "MAC Poisson time to 1e-8 rel residual & cells/s: learned+FP32 vs plain MG, GB300"
 TOL = 1e-8
+# iteration limit of a solver setting tried by the setting search
+TUNE_MAX_ITER = 200
 # CPU reference solve: the reference algorithm with its bottom BiCGSTAB run
 # to convergence (relative 1e-10) -- the preconditioner the GPU path applies
 # exactly.  With the reference's default bottom tolerances (1e-6 relative and
@@ -99,6 +101,9 @@ def parse():
                          "(the reference's), 1 one launch per colour and level parity")
     ap.add_argument("--smooth-variant", type=int, default=-1,
                     help="device smoother launch-bounds variant (-1: autotuned at prepare)")
+    ap.add_argument("--vcycle-out", type=int, default=0,
+                    help="FP32 V-cycle output: 0 read in place, 1 read in place with the operator in double-float, "
+                         "2 widened into FP64 vectors")
     ap.add_argument("--kernel", type=int, default=-1,
                     help="time one kernel alone and exit (for ncu): 0 FP64 operator on the finest tower, "
                          "1 FP32 / 2 FP64 red-black sweep (one colour) of the finest level, "
@@ -113,6 +118,9 @@ def parse():
     ap.add_argument("--bottom-refresh", type=int, default=0,
                     help="--sequence: 1 rebuild the dense bottom inverse after every coefficient change, 0 (default) "
                          "keep the inverse of the last tree between regrids")
+    ap.add_argument("--transfer", default="centered_linear", choices=["centered_linear", "injection"],
+                    help="--sequence: the solution carried across a regrid by the reference's transfer "
+                         "(average-down, centered-linear new blocks; default) or by injection")
     ap.add_argument("--profile", action="store_true",
                     help="run one solve between cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     return ap.parse_args()
@@ -486,7 +494,7 @@ def main():
                  bottom=1,
                  graph=0 if args.profile else 1, n_post_smooth=max(args.n_post, 1) if args.n_post >= 0 else 2,
                  vcycle_kernel=args.vcycle_kernel,
-                 cluster_cells=args.cluster_cells, smooth_variant=args.smooth_variant,
+                 cluster_cells=args.cluster_cells, smooth_variant=args.smooth_variant, vcycle_out=args.vcycle_out,
                  pdl=args.pdl, sublevel_order=args.sublevel_order, bottom_level=args.bottom_level,
                  bottom_half=args.bottom_half, smoother=max(args.smoother, 0),
                  inner_sweeps=args.inner_sweeps if args.inner_sweeps > 0 else 2)
@@ -509,7 +517,9 @@ def main():
             timed_events[1].record(ext)
         return S.solve_info()
 
-    def warm(setting=None, ok=(0,)):
+    def warm(setting=None, ok=(0,), tolerate=False):
+        """W warm-up solves; a failed one ends the run, or (tolerate) is
+        returned as a description"""
         for _ in range(args.warmup):
             info = one()
             if info["status"] not in ok:
@@ -519,7 +529,11 @@ def main():
                     its, rel = st
                     bad = [(int(i), int(its[i]), float(rel[i])) for i in range(len(rel)) if not rel[i] < TOL]
                     where = "; problems not converged (index, iterations, relative residual): %s" % bad[:8]
-                raise SystemExit("warm-up solve failed: %s, setting %s%s" % (info, setting, where))
+                msg = "warm-up solve failed: %s, setting %s%s" % (info, setting, where)
+                if tolerate:
+                    return msg
+                raise SystemExit(msg)
+        return None
 
     tuning = None
     if args.precision < 0 or args.n_post < 0 or args.smoother < 0:
@@ -546,9 +560,20 @@ def main():
                 posts = (args.n_post,)
             best_f, worse = None, 0
             for npost in posts:
-                S.set_params(precision=prec, n_post_smooth=npost, smoother=sm, inner_sweeps=inner)
+                # a setting that needs more than TUNE_MAX_ITER iterations is
+                # not a candidate: it is recorded as not converged and skipped
+                S.set_params(precision=prec, n_post_smooth=npost, smoother=sm, inner_sweeps=inner,
+                             max_iter=TUNE_MAX_ITER)
                 S.prepare()
-                warm(dict(precision=prec, smoother=sm, inner_sweeps=inner, n_post_smooth=npost))
+                failed = warm(dict(precision=prec, smoother=sm, inner_sweeps=inner, n_post_smooth=npost),
+                              tolerate=True)
+                if failed:
+                    tuning.append(dict(precision=prec, smoother=sm, inner_sweeps=inner, n_post_smooth=npost,
+                                       ms=None, not_converged=failed[:300]))
+                    worse += 1
+                    if worse >= 2:
+                        break
+                    continue
                 ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
                 infos = [one(e) for e in ev]
                 torch.cuda.synchronize()
@@ -561,11 +586,11 @@ def main():
                     worse += 1
                     if worse >= 2:
                         break
-        best = min(tuning, key=lambda r: r["ms"])
+        best = min((r for r in tuning if r["ms"] is not None), key=lambda r: r["ms"])
         args.precision, args.n_post = best["precision"], best["n_post_smooth"]
         args.smoother, args.inner_sweeps = best["smoother"], best["inner_sweeps"]
         S.set_params(precision=args.precision, n_post_smooth=args.n_post, smoother=args.smoother,
-                     inner_sweeps=args.inner_sweeps)
+                     inner_sweeps=args.inner_sweeps, max_iter=2000)
         S.prepare()
     if args.inner_sweeps < 0:
         args.inner_sweeps = 2
@@ -822,7 +847,7 @@ def run_sequence(args, torch, ws, rank, local):
             if S is None:
                 S2.set_zero_sol()
             else:
-                S2.init_from(S)
+                S2.init_from(S, prolong=args.transfer)
             ta = mark("transfer", ta, S2)
             S = S2
         else:
@@ -856,7 +881,7 @@ def run_sequence(args, torch, ws, rank, local):
                                "to 90%% of the centreline over %d solves, regrid every %d, %d^3-cell blocks, up to "
                                "%d levels, binary IB from the level set (setIBFracByLS), p=0 outlet"
                                % (K, every, 8, args.max_level),
-                   "tol_rel": TOL, "params": prm},
+                   "tol_rel": TOL, "params": prm, "transfer": args.transfer},
         "sequence": {"total_s": total, "setup_s": setup, "setup_share": setup / total,
                      "solve_s": total - setup, "regrids": sum(1 for r in steps if r["new_tree"]) - 1,
                      "iterations_mean": statistics.mean(its), "iterations_max": max(its),
@@ -882,7 +907,7 @@ def compare_solvers(S, prob, one, warm, torch, args, tuning):
     first, 2D only)"""
     fp32 = dict(precision=1, n_post_smooth=args.n_post, smoother=args.smoother, inner_sweeps=args.inner_sweeps)
     if tuning:
-        t32 = [r for r in tuning if r["precision"] == 1]
+        t32 = [r for r in tuning if r["precision"] == 1 and r["ms"] is not None]
         if t32:
             b = min(t32, key=lambda r: r["ms"])
             fp32 = dict(precision=1, n_post_smooth=b["n_post_smooth"], smoother=b["smoother"],

@@ -149,9 +149,10 @@ typedef struct sayaka_params {
   int32_t learned_tc05;   /* learned correction of 16x16-cell blocks: 1 = its 32 -> 32 layer as an implicit GEMM
                              on tcgen05 with the accumulator in tensor memory (default); 0 = on mma.sync warp
                              MMAs (the same network, products summed in another order) */
-  int32_t vcycle_out;     /* how the FP64 kernels read the FP32 V-cycle's output: 0 = in place (an exact widening
-                             on the integer pipe) in 2D and up to 2,097,152 tower cells in 3D, widened once into
-                             FP64 vectors on larger 3D towers (default); 1 = always in place; 2 = always widened */
+  int32_t vcycle_out;     /* how the BiCGSTAB kernels read the FP32 V-cycle's output: 0 = in place, widened
+                             exactly on the integer pipe where they read it (default); 1 = in place, the
+                             operator evaluated in double-float on the FP32 pipe; 2 = widened once into FP64
+                             vectors */
   int32_t prolong_form;   /* device V-cycle, the prolongation fused with the first red sweep of its level:
                              1 = one warp per block with the block in registers (2D FP32 16x16 blocks,
                              default; elsewhere form 0), 0 = one CTA per block with a shared-memory tile; the
@@ -345,6 +346,16 @@ int sayaka_mac_correct_vel(sayaka_mac *h, int32_t dir, double dt, double *u, int
  * blocks that became leaves by coarsening get the average of their old
  * children; a block with a deeper old subtree starts from zero. */
 int sayaka_mac_init_from(sayaka_mac *h, const sayaka_mac *old);
+/* The reference's own transfer for a cell state with PROLONG_CENTERED_LINEAR
+ * and RESTRICT_AVERAGE, bit for bit: the solution of `old` is averaged down
+ * (FillPatch::restrictAll, src/SayakaFillPatch.cpp:378-437), blocks present in
+ * both trees keep it, and the new blocks are filled level by level by
+ * AmrTree::initNewBlockDataAfterRegrid (src/SayakaRegrid.cpp:987-1105):
+ * centered-linear interpolation from the parent
+ * (src/SayakaInterpPatch.cpp:228-306), the parent's face ghosts from its
+ * same-level neighbours or its physical BC (the types of sayaka_mac_set_bc,
+ * values bc_val[face position] as the BCRegister's; NULL = all 0). */
+int sayaka_mac_init_new_block_data(sayaka_mac *h, const sayaka_mac *old, const double *bc_val);
 
 /* the library's pending CUDA runtime error on the calling thread (0 =
  * none), without clearing it: every call of this API leaves none behind */
@@ -387,7 +398,9 @@ int sayaka_mac_residual_norm_noalloc(sayaka_mac *h, int32_t L, const double *x, 
  * fast sweep (launch variant 0..9, -1 the tuned one; in = phi, in2 = rhs);
  * which 2 = one block-hybrid pass (params.smoother 1) over tower L with
  * `variant` (1..1024) red-black sweeps per block (in = phi, frozen outside
- * each block; in2 = rhs) */
+ * each block; in2 = rhs); which 3 = out = A x on the finest tower for x = in
+ * rounded to FP32, with the double-float operator the BiCGSTAB iteration
+ * applies to the FP32 V-cycle's output (in2 unused) */
 int sayaka_mac_device_kernel_compact(sayaka_mac *h, int32_t which, int32_t L, int32_t variant, const double *in,
                                      const double *in2, double *out);
 /* one mg_smooth_level(L) (src/SayakaMacOperator.cpp:140-159, 1028-1112) */

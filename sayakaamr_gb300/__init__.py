@@ -110,6 +110,7 @@ SIGNATURES = {
     "sayaka_mac_correct_vel": (C.c_int, [_V, C.c_int32, C.c_double, _f64p, C.c_int32, C.c_int32, C.c_int32]),
     "sayaka_mac_get_rhs_compact": (C.c_int, [_V, _f64p]),
     "sayaka_mac_init_from": (C.c_int, [_V, _V]),
+    "sayaka_mac_init_new_block_data": (C.c_int, [_V, _V, _f64p]),
     "sayaka_mac_bottom_level": (C.c_int32, [_V]),
     "sayaka_mac_problem_count": (C.c_int32, [_V]),
     "sayaka_mac_uniform_blocks": (C.c_int32, [_V]),
@@ -526,10 +527,24 @@ class MacSolver:
         _check(self.lib.sayaka_mac_correct_vel(self.h, int(d), float(dt), u.ctypes.data_as(_f64p), ncomp, ngrow,
                                                comp), "correct_vel", self.h)
 
-    def init_from(self, old):
+    def init_from(self, old, prolong="injection", bc_val=None):
         """the solution of `old` (the solver of the tree before a regrid) as
-        this solver's initial solution"""
-        _check(self.lib.sayaka_mac_init_from(self.h, old.h), "init_from", self.h)
+        this solver's initial solution: prolong "injection" (copy, injection
+        from the nearest old leaf ancestor, average of old children) or
+        "centered_linear" (the reference's initNewBlockDataAfterRegrid after an
+        average-down, with the BC values bc_val[face position], default 0)"""
+        if prolong == "injection":
+            _check(self.lib.sayaka_mac_init_from(self.h, old.h), "init_from", self.h)
+        elif prolong == "centered_linear":
+            v = None
+            if bc_val is not None:
+                v = np.zeros(6)
+                b = np.asarray(bc_val, dtype=np.float64).reshape(-1)
+                v[:b.size] = b  # one value per face position (2 * ndim), the rest unused
+            _check(self.lib.sayaka_mac_init_new_block_data(self.h, old.h, None if v is None else v.ctypes.data_as(_f64p)),
+                   "init_new_block_data", self.h)
+        else:
+            raise ValueError("prolong must be 'injection' or 'centered_linear'")
 
     def get_rhs_compact(self):
         r = self._cells()
@@ -600,6 +615,15 @@ class MacSolver:
         a, pa = _f64(x)
         _check(self.lib.sayaka_mac_device_kernel_compact(self.h, 0, 0, -1, pa, None, y.ctypes.data_as(_f64p)),
                "device_apply", self.h)
+        return y
+
+    def device_apply_f32(self, x):
+        """the BiCGSTAB iteration's operator on x rounded to FP32 (the
+        double-float path that reads the FP32 V-cycle's output)"""
+        y = self._cells()
+        a, pa = _f64(x)
+        _check(self.lib.sayaka_mac_device_kernel_compact(self.h, 3, 0, -1, pa, None, y.ctypes.data_as(_f64p)),
+               "device_apply_f32", self.h)
         return y
 
     def device_smooth(self, L, phi, rhs, variant=-1):

@@ -897,6 +897,19 @@ int sayaka_mac_init_from(sayaka_mac *h, const sayaka_mac *old) {
     return st == 0 ? (int)SAYAKA_OK : (int)SAYAKA_CUDA_ERROR;
   });
 }
+int sayaka_mac_init_new_block_data(sayaka_mac *h, const sayaka_mac *old, const double *bc_val) {
+  return guarded(h, [&] {
+    if (!old || !old->gpu) return (int)SAYAKA_BAD_INPUT;
+    std::string why;
+    const int st = h->gpu->init_new_block_data(*old->gpu, bc_val, &why);
+    if (st == 1) {
+      h->err = why;
+      return (int)SAYAKA_BAD_INPUT;
+    }
+    if (st != 0 && !why.empty()) h->err = why;
+    return st == 0 ? (int)SAYAKA_OK : (int)SAYAKA_CUDA_ERROR;
+  });
+}
 int32_t sayaka_cuda_peek_error(void) { return (int32_t)cudaPeekAtLastError(); }
 int sayaka_fp_selftest(const double *d, const float *f, int n, float *narrow, float *narrow_hw, double *widen,
                        double *widen_hw, double *widen0, double *widen0_hw) {
@@ -985,8 +998,8 @@ int sayaka_mac_device_kernel_compact(sayaka_mac *h, int32_t which, int32_t L, in
   return guarded(h, [&] {
     const int r = h->gpu->device_kernel_compact(which, L, variant, in, in2, out);
     if (r == 1) {
-      h->err = "device_kernel_compact: which must be 0, 1 or 2, L a tower of the tree, variant < 10 (which 1) or "
-               "1..1024 (which 2), pointers non-null";
+      h->err = "device_kernel_compact: which must be 0..3, L a tower of the tree (which 1, 2), a smoother variant "
+               "(which 1) or 1..1024 (which 2), pointers non-null";
       return (int)SAYAKA_BAD_INPUT;
     }
     return (int)SAYAKA_OK;  // CUDA errors are reported by status_of

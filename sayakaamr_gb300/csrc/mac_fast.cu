@@ -22,6 +22,7 @@
 #include "mac_solver.h"
 #include "cuda_check.h"
 #include "mac_stencil.cuh"
+#include "mac_df.cuh"
 #include "launch.cuh"
 #include "mac_fp.cuh"
 #include "tree.h"
@@ -657,14 +658,58 @@ __device__ __forceinline__ double op_offdiag(const Topo &t, const Coef<double> &
 // MODE 0: y = A x, rhat.y (EpiAlpha) ; MODE 1: y = A x, y.w, y.y (EpiOmega) ;
 // MODE 2: y = w - A x (0 where vf = 0), |y|, y.y (EpiInit) ;
 // MODE 3: only while verifying: y = y2 = w - A x, |y|, y.y (EpiVerify)
-template <int ND, int MODE, typename TX, bool MULTI>
+// The operator in double-float (mac_df.cuh) for an FP32 input x: the sum of
+// T * x over the faces, then P * x - S * sum, with T, P and S as double-float
+// pairs (the records' and the per-cell factors' nearest double-float values,
+// T of a block without a record split on the fly); the coarse/fine faces'
+// terms are formed in FP64 as in op_offdiag and added in double-float.  The
+// result, about 48 significand bits, is rounded to FP64 once.
+template <int ND>
+__device__ __forceinline__ dfl::df op_offdiag_df(const Topo &t, const Coef<double> &c, int b, uint16_t ft,
+                                                 const int ijk[3], int ci, const float *__restrict__ x,
+                                                 const int *__restrict__ hx, const float2 *u2) {
+  using namespace stencil;
+  const int nb = t.nb;
+  const long cb = (long)b * t.ncell;
+  dfl::df off = {0.f, 0.f};
+#pragma unroll
+  for (int f = 0; f < 2 * ND; f++) {
+    const int d = f >> 1, s = f & 1;
+    const bool bnd = s ? ijk[d] == nb - 1 : ijk[d] == 0;
+    const int fx = face_index(d, ijk, s, nb);
+    if (!bnd) {
+      const int stride = d == 0 ? 1 : (d == 1 ? nb : nb * nb);
+      const dfl::df T = u2 ? dfl::load(u2 + d) : dfl::from_double(c.tff[d][(long)b * t.nfb + fx]);
+      off = dfl::add(off, dfl::mul_f(T, x[cb + ci + (s ? stride : -stride)]));
+    } else {
+      const int ty = face_type_of(ft, f);
+      if (ty == 0) {
+        const dfl::df T = u2 ? dfl::load(u2 + d) : dfl::from_double(c.tff[d][(long)b * t.nfb + fx]);
+        off = dfl::add(off, dfl::mul_f(T, same_level_ghost<float, false>(t, b, f, ijk, x, hx)));
+      } else if (ty == 2) {
+        off = dfl::add(off, dfl::mul_f(dfl::from_double(cf_coef(c, t, b, d, fx, 1.5)),
+                                       fine_crse_ghost<float, ND, false>(t, b, f, ijk, x, hx)));
+      } else if (ty == 3) {
+        off = dfl::add(off, dfl::from_double(crse_fine_sum<double, ND, false>(t, c, b, f, ijk, x, hx)));
+      }
+    }
+  }
+  return off;
+}
+
+template <int ND, int MODE, typename TX, bool MULTI, bool DFOP = false>
 __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockList L, Chunks ch,
                                                const TX *__restrict__ x, double *__restrict__ y,
                                                const double *__restrict__ w, const double *__restrict__ P,
                                                const double *__restrict__ S, FState *stb, double *partials,
-                                               unsigned *counter, double *__restrict__ y2 = nullptr) {
+                                               unsigned *counter, double *__restrict__ y2 = nullptr,
+                                               const float2 *__restrict__ P2 = nullptr,
+                                               const float2 *__restrict__ S2 = nullptr,
+                                               const float2 *__restrict__ U2 = nullptr) {
   using namespace stencil;
   pdl_enter();
+  // DFOP: modes 0 and 1 of an FP32 input in double-float
+  constexpr bool DF = DFOP && sizeof(TX) == 4 && MODE < 2;
   const Work wk = work_of<MULTI>(ch, stb, L.n * t.ncell, counter);
   FState *st = wk.st;
   if (MODE == 3 && !st->verify) return;
@@ -682,13 +727,22 @@ __global__ void __launch_bounds__(kTPB) k_op_red(Topo t, Coef<double> c, BlockLi
     // constant-coefficient block: face coefficients and S from its record,
     // P too for an interior cell (the boundary cells' P depends on the face types)
     const double *u = uniform_of(c, b);
-    const double off = op_offdiag<ND, TX>(t, c, b, ft, ijk, ci, x, e, u);
     bool inner = true;
 #pragma unroll
     for (int d = 0; d < ND; d++) inner = inner && ijk[d] > 0 && ijk[d] < t.nb - 1;
-    const double sc = u ? u[5] : S[q];
-    double yv = __fma_rn(widen_from<TX>(x[q]), (u && inner) ? u[4] : P[q], -off * sc);
-    if (MODE >= 2) yv = fpint::positive(sc) ? w[q] - yv : 0.0;
+    double yv;
+    if constexpr (DF) {
+      const float2 *u2 = u ? U2 + (long)b * kUni : nullptr;
+      const dfl::df off = op_offdiag_df<ND>(t, c, b, ft, ijk, ci, x, e, u2);
+      const dfl::df pf = (u2 && inner) ? dfl::load(u2 + 4) : dfl::load(P2 + q);
+      const dfl::df sf = u2 ? dfl::load(u2 + 5) : dfl::load(S2 + q);
+      yv = dfl::to_double(dfl::add(dfl::mul_f(pf, x[q]), dfl::neg(dfl::mul(off, sf))));
+    } else {
+      const double off = op_offdiag<ND, TX>(t, c, b, ft, ijk, ci, x, e, u);
+      const double sc = u ? u[5] : S[q];
+      yv = __fma_rn(widen_from<TX>(x[q]), (u && inner) ? u[4] : P[q], -off * sc);
+    }
+    if constexpr (MODE >= 2) yv = fpint::positive(u ? u[5] : S[q]) ? w[q] - yv : 0.0;
     y[q] = yv;
     if (MODE == 3) y2[q] = yv;
     if (MODE == 0) acc[0] = __fma_rn(w[q], yv, acc[0]);
@@ -799,6 +853,14 @@ __global__ void k_zero_col(long long off, int m, int col, double *a) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) a[off + (long)r * m + col] = 0.0;
 }
 
+// nearest double-float pairs of FP64 values
+__global__ void k_split_df(long n, const double *src, float2 *dst) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const dfl::df v = dfl::from_double(src[i]);
+    dst[i] = make_float2(v.hi, v.lo);
+  }
+}
+
 __global__ void k_to_f32(long n, const double *src, float *dst) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     dst[i] = (float)src[i];
@@ -831,6 +893,12 @@ void MacGpu::ensure_fast_buffers() {
   else cudaMemset(d_corr64b_, 0, nc * sizeof(double));
   if (cudaMalloc(&d_opP_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
   if (cudaMalloc(&d_opS_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
+  if (cudaMalloc(&d_opP2_, nc * sizeof(float2)) != cudaSuccess ||
+      cudaMalloc(&d_opS2_, nc * sizeof(float2)) != cudaSuccess ||
+      cudaMalloc(&d_uni2_, (size_t)std::max(nbk, 1) * kUni * sizeof(float2)) != cudaSuccess)
+    fail("out of device memory (operator factors)");
+  else
+    cudaMemset(d_uni2_, 0, (size_t)std::max(nbk, 1) * kUni * sizeof(float2));
   if (cudaMalloc(&d_uni64_, (size_t)std::max(nbk, 1) * kUni * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&d_uni32_, (size_t)std::max(nbk, 1) * kUni * sizeof(float)) != cudaSuccess)
     fail("out of device memory (block records)");
@@ -973,6 +1041,9 @@ void MacGpu::build_op_factors() {
     k_op_prep<2><<<ew_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, d_opP_, d_opS_);
   else
     k_op_prep<3><<<ew_grid(w), kTPB, 0, stream_>>>(topo_, c64_, TL, d_opP_, d_opS_);
+  const long nc = (long)tt_.num_blocks * ncell_;
+  k_split_df<<<ew_grid(nc), kTPB, 0, stream_>>>(nc, d_opP_, d_opP2_);
+  k_split_df<<<ew_grid(nc), kTPB, 0, stream_>>>(nc, d_opS_, d_opS2_);
   CK(cudaGetLastError());
 }
 
@@ -986,6 +1057,8 @@ void MacGpu::build_uniform() {
     k_uniform<2><<<grid, kTPB, 0, stream_>>>(topo_, c64_, c32_, d_uni64_, d_uni32_);
   else
     k_uniform<3><<<grid, kTPB, 0, stream_>>>(topo_, c64_, c32_, d_uni64_, d_uni32_);
+  const long nu = (long)nbk * kUni;
+  k_split_df<<<ew_grid(nu), kTPB, 0, stream_>>>(nu, d_uni64_, d_uni2_);
   CK(cudaGetLastError());
 }
 
@@ -1477,20 +1550,16 @@ void MacGpu::precondition(int L, T *resid, T *corr, const Coef<T> &c, double *ou
   }
 }
 
-// FP32 V-cycle output read by the FP64 kernels in place (its exact widening
-// is integer work there) in 2D and up to this many tower cells in 3D, where
-// the two widening launches per iteration cost more than the in-place
-// widenings (batch workload, 2D, 29M cells: 62.9 vs 64.6 ms); larger 3D
-// towers, whose operator reads six neighbours per cell, widen it once into
-// FP64 phat / shat (config3: 29.1 vs 33.7 ms in place)
-constexpr long kDirectF32Cells = 1l << 21;
-
+// FP32 V-cycle output read in place by the BiCGSTAB kernels, widened exactly
+// on the integer pipe where they read it (params.vcycle_out 0, or 1 with the
+// operator in double-float); params.vcycle_out 2 widens it once into FP64
+// phat / shat instead.  On the batch workload (2D, 29M cells) the three run
+// within 1%: 63.2 (in place), 63.9 (double-float operator) and 64.6 ms
+// (widened); on config3 (3D, 15.9M cells) 27.5, 27.8 and 27.5 ms.
 template <typename T>
 void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
-  const long w = (long)tower_list(finest_).n * ncell_;
   if constexpr (sizeof(T) == 4) {
-    const bool direct =
-        prm_.vcycle_out == 1 || (prm_.vcycle_out == 0 && (tt_.ndim == 2 || w < kDirectF32Cells));
+    const bool direct = prm_.vcycle_out != 2;
     if (!learned_active() && direct) {
       iteration_body<T, float>(resid, corr, c, corr, corr, nullptr, nullptr);
       return;
@@ -1523,24 +1592,37 @@ void MacGpu::iteration_body(T *resid, T *corr, const Coef<T> &c, const TO *PH, c
   double *V = vec_[kV], *Tt = vec_[kT], *X = vec_[kX];
   const bool pdl = prm_.pdl != 0;
   const double *OP = d_opP_, *OS = d_opS_;
+  const float2 *OP2 = d_opP2_, *OS2 = d_opS2_, *U2 = d_uni2_;
+  // params.vcycle_out 1: the operator of the FP32 V-cycle's output in double-float
+  const bool dfop = prm_.vcycle_out == 1;
   auto op = [&](auto mode, const auto *x, double *y, const double *wv, double *y2) {
     constexpr int M = decltype(mode)::value;
     using TX = std::remove_const_t<std::remove_pointer_t<decltype(x)>>;
-    if (tt_.ndim == 2) {
-      if (mp)
-        launch_k(pdl, k_op_red<2, M, TX, true>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS, ST, PART,
-                 CNT, y2);
-      else
-        launch_k(pdl, k_op_red<2, M, TX, false>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS, ST,
-                 PART, CNT, y2);
-    } else {
-      if (mp)
-        launch_k(pdl, k_op_red<3, M, TX, true>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS, ST, PART,
-                 CNT, y2);
-      else
-        launch_k(pdl, k_op_red<3, M, TX, false>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS, ST,
-                 PART, CNT, y2);
+    auto go = [&](auto df) {
+      constexpr bool D = decltype(df)::value;
+      if (tt_.ndim == 2) {
+        if (mp)
+          launch_k(pdl, k_op_red<2, M, TX, true, D>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS, ST,
+                   PART, CNT, y2, OP2, OS2, U2);
+        else
+          launch_k(pdl, k_op_red<2, M, TX, false, D>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS,
+                   ST, PART, CNT, y2, OP2, OS2, U2);
+      } else {
+        if (mp)
+          launch_k(pdl, k_op_red<3, M, TX, true, D>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS, ST,
+                   PART, CNT, y2, OP2, OS2, U2);
+        else
+          launch_k(pdl, k_op_red<3, M, TX, false, D>, gr, kTPB, 0, stream_, topo_, cd64_, TL, ch, x, y, wv, OP, OS,
+                   ST, PART, CNT, y2, OP2, OS2, U2);
+      }
+    };
+    if constexpr (sizeof(TX) == 4 && M < 2) {
+      if (dfop) {
+        go(std::true_type{});
+        return;
+      }
     }
+    go(std::false_type{});
   };
   if (mp)
     launch_k(pdl, k_pupdate<T, true>, ge, kTPB, 0, stream_, TL, ncell_, ch, ST, (const double *)R, P,
@@ -1937,8 +2019,8 @@ int MacGpu::enqueue_kernel(int which, int L) {
 // solve's FP64 sweep, launch variant `variant` (-1: the tuned one); in = phi,
 // in2 = rhs.  Uses (and clobbers) the handle's work vectors.
 int MacGpu::device_kernel_compact(int which, int L, int variant, const double *in, const double *in2, double *out) {
-  if (which < 0 || which > 2 || !in || !out || (which >= 1 && !in2)) return 1;
-  if (which >= 1 && (L < 1 || L > finest_ || towers_[L].all.n == 0)) return 1;
+  if (which < 0 || which > 3 || !in || !out || ((which == 1 || which == 2) && !in2)) return 1;
+  if ((which == 1 || which == 2) && (L < 1 || L > finest_ || towers_[L].all.n == 0)) return 1;
   if (which == 1 && variant >= kRbgsVariants) return 1;
   if (which == 2 && (variant < 1 || variant > 1024)) return 1;
   if (prepare_device() != 0) return 2;
@@ -1959,6 +2041,26 @@ int MacGpu::device_kernel_compact(int which, int L, int variant, const double *i
       k_op_red<3, 0, double, false><<<red_grid(w), kTPB, 0, stream_>>>(topo_, cd64_, TL, Chunks{}, vec_[kTMP],
                                                                       vec_[kV], vec_[kRHAT], d_opP_, d_opS_, d_st_,
                                                                       d_part_, d_cnt_);
+    CKR_(cudaGetLastError(), 2);
+    CKR_(cudaMemcpyAsync(out, vec_[kV], n * sizeof(double), cudaMemcpyDeviceToHost, stream_), 2);
+  } else if (which == 3) {
+    // the operator of the BiCGSTAB iteration on an FP32 input (double-float
+    // path): in rounded to FP32, then y = A x on the finest tower
+    const BlockList TL = tower_list(finest_);
+    const long w = (long)TL.n * ncell_;
+    CKR_(cudaMemcpyAsync(vec_[kTMP], in, n * sizeof(double), cudaMemcpyHostToDevice, stream_), 2);
+    k_narrow<<<ew_grid((long)n), kTPB, 0, stream_>>>((long long)n, vec_[kTMP], d_corr32_);
+    CKR_(cudaMemsetAsync(vec_[kV], 0, n * sizeof(double), stream_), 2);
+    CKR_(cudaMemsetAsync(vec_[kRHAT], 0, n * sizeof(double), stream_), 2);
+    CKR_(cudaMemsetAsync(d_st_, 0, sizeof(FState), stream_), 2);
+    if (tt_.ndim == 2)
+      k_op_red<2, 0, float, false, true><<<red_grid(w), kTPB, 0, stream_>>>(
+          topo_, cd64_, TL, Chunks{}, d_corr32_, vec_[kV], vec_[kRHAT], d_opP_, d_opS_, d_st_, d_part_, d_cnt_,
+          nullptr, d_opP2_, d_opS2_, d_uni2_);
+    else
+      k_op_red<3, 0, float, false, true><<<red_grid(w), kTPB, 0, stream_>>>(
+          topo_, cd64_, TL, Chunks{}, d_corr32_, vec_[kV], vec_[kRHAT], d_opP_, d_opS_, d_st_, d_part_, d_cnt_,
+          nullptr, d_opP2_, d_opS2_, d_uni2_);
     CKR_(cudaGetLastError(), 2);
     CKR_(cudaMemcpyAsync(out, vec_[kV], n * sizeof(double), cudaMemcpyDeviceToHost, stream_), 2);
   } else if (which == 2) {

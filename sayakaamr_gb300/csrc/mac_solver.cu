@@ -515,6 +515,9 @@ MacGpu::~MacGpu() {
   for (auto &q : d_face_) fr(q);
   learned_free();
   fr(d_opS_);
+  fr(d_opP2_);
+  fr(d_opS2_);
+  fr(d_uni2_);
   free_coef_lists();
   fr(d_uni64_);
   fr(d_uni32_);

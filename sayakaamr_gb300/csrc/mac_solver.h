@@ -37,9 +37,9 @@ struct SolverParams {
   int smooth_variant = -1;    // device smoother launch bounds: -1 autotune at prepare, else variant index
   int learned = 0;            // device path, FP32 V-cycle: apply the trained block correction
   int fuse_prolong = 1;       // device path: prolongation fused with the first red sweep of its level
-  int vcycle_out = 0;         // FP32 V-cycle output to the FP64 kernels: 0 = in place in 2D and up to 2M tower
-                              // cells in 3D, else widened once into FP64 vectors; 1 = always in place; 2 = always
-                              // widened
+  int vcycle_out = 0;         // FP32 V-cycle output to the BiCGSTAB kernels: 0 = read in place (FP64 operator),
+                              // 1 = read in place with the operator in double-float, 2 = widened once into FP64
+                              // vectors (FP64 operator)
   int prolong_form = 1;       // that fused launch: 1 = one warp per block (2D FP32 16x16 blocks), 0 = one CTA
                               // per block with a shared-memory tile (same values)
   int bottom_half = 0;        // device path, FP32 V-cycle, bottom above level 1: 1 = FP16 inverse with row scales
@@ -166,6 +166,10 @@ class MacGpu {
   // the solution of a solver on the tree before a regrid, carried onto this
   // tree (0 ok, 1 bad input: why says which, 2 CUDA error)
   int init_solution_from(const MacGpu &old, std::string *why);
+  // the same as AmrTree::initNewBlockDataAfterRegrid with centered-linear
+  // prolongation after an average-down of the old solution; bc_val: the BC
+  // value of each face position (null = 0)
+  int init_new_block_data(const MacGpu &old, const double *bc_val, std::string *why);
 
   // r = rhs - A x on tower L and out = {|r|_inf, r.r}; device pointers to
   // compact all-block arrays, enqueued on s, no device allocation (scratch in
@@ -352,6 +356,8 @@ class MacGpu {
   FState *d_st_ = nullptr, *h_st_ = nullptr;
   double *d_part_ = nullptr;
   double *d_opP_ = nullptr, *d_opS_ = nullptr;  // factors of the device solve's operator
+  // their nearest double-float pairs, and those of the block records
+  float2 *d_opP2_ = nullptr, *d_opS2_ = nullptr, *d_uni2_ = nullptr;
   // constant-coefficient block records (Coef::ut) and the FP64 coefficients
   // the device solve's kernels read (c64_ with the records when enabled)
   double *d_uni64_ = nullptr;

@@ -1,14 +1,26 @@
 // The solution of a solver on an old tree carried onto the tree after a
-// regrid (the cell data part of AmrTree::initNewBlockDataAfterRegrid,
+// regrid (the cell-data part of AmrTree::initNewBlockDataAfterRegrid,
 // src/SayakaRegrid.cpp:987-1105, for the pressure the next solve starts
 // from).  Blocks are matched by their root and the child path from it, which
-// survives the id repacking of a regrid.  Every leaf of the new tree gets
+// survives the id repacking of a regrid.  Two transfers:
+//
+// init_solution_from (injection): every leaf of the new tree gets
 //   * a copy of the same block of the old tree, or
 //   * injection from its nearest old leaf ancestor when the block was refined
-//     (the reference's prolongBlock of a new child, repeated when a regrid
-//     refined more than one level), or
+//     (repeated when a regrid refined more than one level), or
 //   * the average of its old children when it became a leaf by coarsening,
 //   * zero where the old tree had a deeper subtree (a valid initial guess).
+//
+// init_new_block_data (the reference's own sequence for a cell state with
+// PROLONG_CENTERED_LINEAR / RESTRICT_AVERAGE): the old field is averaged
+// down (FillPatch::restrictAll, src/SayakaFillPatch.cpp:378-437), every block
+// present in both trees keeps its data, and the new blocks are filled level
+// by level from their parent by centered-linear interpolation
+// (prolongCellBlockData_CenteredLinear, src/SayakaInterpPatch.cpp:228-306)
+// with the parent's face ghosts from its same-level neighbours or its
+// physical BC (fillBlockBndryAtSameLevel, BCPatch::fillBasicCellBlockBC,
+// src/SayakaBoundaryPatch.cpp:139-234).  Same operations in the same order as
+// the reference: bit-identical results.
 #include <unordered_map>
 #include <vector>
 
@@ -86,6 +98,107 @@ std::vector<unsigned long long> path_keys(const TreeTables &t) {
     key[b] = ((unsigned long long)x << 44) | ((unsigned long long)depth << 39) | path;
   }
   return key;
+}
+
+// FillPatch::restrictAll, one level: every listed (non-leaf) block's cells =
+// (sum of its 2^d fine cells, k, j, i order, from 0) * (1 / 2^d)
+__global__ void __launch_bounds__(kXT) k_avg_down(int ndim, int nb, int ncell, int n, const int *__restrict__ blocks,
+                                                const int *__restrict__ child, double *__restrict__ x) {
+  const long total = (long)n * ncell;
+  const int half = nb >> 1;
+  const double wgt = 1.0 / (double)(1 << ndim);
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell), ci = (int)(it - (long)p * ncell);
+    const int b = blocks[p];
+    int ijk[3];
+    ijk[0] = ci % nb;
+    ijk[1] = ndim >= 2 ? (ci / nb) % nb : 0;
+    ijk[2] = ndim == 3 ? ci / (nb * nb) : 0;
+    int cidx = 0, fb[3] = {0, 0, 0};
+    for (int q = 0; q < ndim; q++) {
+      const int sq = ijk[q] >= half ? 1 : 0;
+      cidx |= sq << q;
+      fb[q] = 2 * (ijk[q] - sq * half);
+    }
+    const double *F = x + (long)child[b * 8 + cidx] * ncell;
+    double sum = 0.0;
+    for (int kk = 0; kk < (ndim == 3 ? 2 : 1); kk++)
+      for (int jj = 0; jj < 2; jj++)
+        for (int ii = 0; ii < 2; ii++) {
+          const int fi[3] = {fb[0] + ii, fb[1] + jj, ndim == 3 ? fb[2] + kk : 0};
+          sum = __dadd_rn(sum, F[stencil::encode(fi, nb)]);
+        }
+    x[(long)b * ncell + ci] = __dmul_rn(sum, wgt);
+  }
+}
+
+// x_new[dst[i]] = x_old[src[i]], whole blocks
+__global__ void __launch_bounds__(kXT) k_copy_blocks(int ncell, int n, const int *__restrict__ dst,
+                                                   const int *__restrict__ src, const double *__restrict__ xo,
+                                                   double *__restrict__ x) {
+  const long total = (long)n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell), ci = (int)(it - (long)p * ncell);
+    x[(long)dst[p] * ncell + ci] = xo[(long)src[p] * ncell + ci];
+  }
+}
+
+struct BcValues {
+  double v[6];
+};
+
+// the parent's cell at coarse index c, moved by dir = +-1 along q; outside the
+// parent, its face ghost: the same-level neighbour's mirrored cell, else the
+// physical BC of that face (Neumann: the boundary cell; Dirichlet:
+// 2 * value - boundary cell; SimpleFill: the value)
+__device__ __forceinline__ double parent_cell(const Topo &t, const int *level, const BcValues &bv, int P,
+                                              const int c[3], int q, int dir, const double *x) {
+  int a[3] = {c[0], c[1], c[2]};
+  a[q] += dir;
+  const int nb = t.nb;
+  if (a[q] >= 0 && a[q] < nb) return x[(long)P * t.ncell + stencil::encode(a, nb)];
+  const int f = 2 * q + (dir > 0 ? 1 : 0);
+  const int n = t.neighbor[P * 6 + f];
+  if (n >= 0 && level[n] == level[P]) {
+    a[q] = dir > 0 ? 0 : nb - 1;
+    return x[(long)n * t.ncell + stencil::encode(a, nb)];
+  }
+  const double vref = x[(long)P * t.ncell + stencil::encode(c, nb)];
+  if (n <= kPhysBndry) {
+    const int bt = t.bc_type[P * 6 + f];
+    if (bt == 1) return __dsub_rn(__dmul_rn(2.0, bv.v[f]), vref);
+    if (bt == 2) return bv.v[f];
+  }
+  return vref;  // Neumann (no same-level neighbour inside the domain cannot occur in a 2:1-balanced tree)
+}
+
+// prolongCellBlockData_CenteredLinear of every listed block from its parent
+template <int ND>
+__global__ void __launch_bounds__(kXT) k_prolong_centered(Topo t, int n, const int *__restrict__ blocks,
+                                                        const int *__restrict__ level, BcValues bv, double *x) {
+  const int nb = t.nb, ncell = t.ncell, half = nb >> 1;
+  const long total = (long)n * ncell;
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int p = (int)(it / ncell), ci = (int)(it - (long)p * ncell);
+    const int b = blocks[p], P = t.parent[b], wc = t.which_child[b];
+    int ijk[3], c[3] = {0, 0, 0};
+    ijk[0] = ci % nb;
+    ijk[1] = (ci / nb) % nb;
+    ijk[2] = ND == 3 ? ci / (nb * nb) : 0;
+    for (int q = 0; q < ND; q++) c[q] = ((wc >> q) & 1) * half + (ijk[q] >> 1);
+    const double c0 = x[(long)P * ncell + stencil::encode(c, nb)];
+    double g[3] = {0.0, 0.0, 0.0}, rel[3] = {0.0, 0.0, 0.0};
+    for (int q = 0; q < ND; q++) {
+      const double cp = parent_cell(t, level, bv, P, c, q, 1, x);
+      const double cm = parent_cell(t, level, bv, P, c, q, -1, x);
+      g[q] = __dmul_rn(0.5, __dsub_rn(cp, cm));
+      rel[q] = (ijk[q] & 1) ? 0.25 : -0.25;
+    }
+    double v = __dadd_rn(c0, __dmul_rn(rel[0], g[0]));
+    v = __dadd_rn(v, __dmul_rn(rel[1], g[1]));
+    v = __dadd_rn(v, __dmul_rn(rel[2], g[2]));  // 2D: + 0 * 0, as the reference's third term
+    x[(long)b * ncell + ci] = v;
+  }
 }
 
 }  // namespace
@@ -168,6 +281,98 @@ int MacGpu::init_solution_from(const MacGpu &old, std::string *why) {
         vec_[kSOL]);
   CKR_(cudaGetLastError(), 2);
   CKR_(cudaStreamSynchronize(stream_), 2);
+  cudaFree(d);
+  return 0;
+}
+
+int MacGpu::init_new_block_data(const MacGpu &old, const double *bc_val, std::string *why) {
+  if (old.device_ != device_) {
+    *why = "init_new_block_data: the solvers live on different devices";
+    return 1;
+  }
+  if (old.tt_.ndim != tt_.ndim || old.tt_.nb != tt_.nb || tt_.ndim < 2) {
+    *why = "init_new_block_data: the trees differ in dimension or block size";
+    return 1;
+  }
+  if (tt_.max_level > 13 || old.tt_.max_level > 13) {
+    *why = "init_new_block_data: more than 13 levels";
+    return 1;
+  }
+  BcValues bv{};
+  for (int f = 0; f < 6; f++) bv.v[f] = bc_val ? bc_val[f] : 0.0;
+  const std::vector<unsigned long long> ko = path_keys(old.tt_), kn = path_keys(tt_);
+  std::unordered_map<unsigned long long, int> where;
+  where.reserve(ko.size() * 2);
+  for (int b = 0; b < old.tt_.num_blocks; b++) where[ko[b]] = b;
+  // host lists: the old tree's non-leaf blocks by level (restriction, finest-1
+  // .. 1), the kept blocks (new id, old id), the new blocks by level
+  std::vector<int> pack;
+  std::vector<std::pair<int, int>> avg_lv;  // (offset, count) per level, in launch order
+  int old_finest = 1;
+  for (int b = 0; b < old.tt_.num_blocks; b++)
+    if (old.tt_.node_type[b] == kNodeLeaf) old_finest = std::max(old_finest, old.tt_.level[b]);
+  for (int l = old_finest - 1; l >= 1; l--) {
+    const int off = (int)pack.size();
+    for (int b = 0; b < old.tt_.num_blocks; b++)
+      if (old.tt_.level[b] == l && old.tt_.node_type[b] != kNodeLeaf) pack.push_back(b);
+    avg_lv.push_back({off, (int)pack.size() - off});
+  }
+  const int keep_off = (int)pack.size();
+  std::vector<int> keep_src, fresh;
+  for (int b = 0; b < tt_.num_blocks; b++) {
+    auto it = where.find(kn[b]);
+    if (it != where.end()) {
+      pack.push_back(b);
+      keep_src.push_back(it->second);
+    } else {
+      fresh.push_back(b);
+    }
+  }
+  const int nkeep = (int)keep_src.size();
+  const int src_off = (int)pack.size();
+  pack.insert(pack.end(), keep_src.begin(), keep_src.end());
+  std::vector<std::pair<int, int>> new_lv;
+  for (int l = 2; l <= tt_.max_level; l++) {
+    const int off = (int)pack.size();
+    for (int b : fresh)
+      if (tt_.level[b] == l) pack.push_back(b);
+    if ((int)pack.size() > off) new_lv.push_back({off, (int)pack.size() - off});
+  }
+  const int level_off = (int)pack.size();
+  pack.insert(pack.end(), tt_.level.begin(), tt_.level.end());
+  const size_t nold = (size_t)old.tt_.num_blocks * ncell_, n = (size_t)tt_.num_blocks * ncell_;
+  int *d = nullptr;
+  double *tmp = nullptr;
+  CKR_(cudaMalloc(&d, std::max<size_t>(pack.size(), 1) * sizeof(int)), 2);
+  if (cudaMalloc(&tmp, std::max<size_t>(nold, 1) * sizeof(double)) != cudaSuccess) {
+    cudaFree(d);
+    *why = "init_new_block_data: out of device memory";
+    return 2;
+  }
+  CKR_(cudaMemcpyAsync(d, pack.data(), pack.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), 2);
+  // the old solver's solution is complete once its stream is idle
+  CKR_(cudaStreamSynchronize(old.stream_), 2);
+  CKR_(cudaMemcpyAsync(tmp, old.vec_[kSOL], nold * sizeof(double), cudaMemcpyDeviceToDevice, stream_), 2);
+  auto grid = [](long w) { return (int)std::max<long>(1, std::min<long>((w + kXT - 1) / kXT, 152 * 32)); };
+  for (const auto &lv : avg_lv)
+    if (lv.second > 0)
+      k_avg_down<<<grid((long)lv.second * ncell_), kXT, 0, stream_>>>(tt_.ndim, tt_.nb, ncell_, lv.second,
+                                                                     d + lv.first, old.topo_.child, tmp);
+  CKR_(cudaMemsetAsync(vec_[kSOL], 0, n * sizeof(double), stream_), 2);
+  if (nkeep > 0)
+    k_copy_blocks<<<grid((long)nkeep * ncell_), kXT, 0, stream_>>>(ncell_, nkeep, d + keep_off, d + src_off, tmp,
+                                                                   vec_[kSOL]);
+  for (const auto &lv : new_lv) {
+    if (tt_.ndim == 2)
+      k_prolong_centered<2><<<grid((long)lv.second * ncell_), kXT, 0, stream_>>>(topo_, lv.second, d + lv.first,
+                                                                                 d + level_off, bv, vec_[kSOL]);
+    else
+      k_prolong_centered<3><<<grid((long)lv.second * ncell_), kXT, 0, stream_>>>(topo_, lv.second, d + lv.first,
+                                                                                 d + level_off, bv, vec_[kSOL]);
+  }
+  CKR_(cudaGetLastError(), 2);
+  CKR_(cudaStreamSynchronize(stream_), 2);
+  cudaFree(tmp);
   cudaFree(d);
   return 0;
 }

@@ -1,85 +1,24 @@
-"""The solution carried across a regrid (sayaka_mac_init_from), on the GPU
-through the C ABI, against a numpy restatement bit for bit: blocks matched by
-root and child path are copied, refined blocks take injection from their
-nearest old leaf ancestor (the reference's prolongBlock of a new child,
-level by level: src/SayakaRegrid.cpp:987-1105), blocks that became leaves by
-coarsening take the average of their old children, blocks over a deeper old
-subtree start from zero.  The elbow sequence then warm-starts every solve
-after a regrid from the previous tree's solution."""
+"""The solution carried across a regrid, on the GPU through the C ABI.
+sayaka_mac_init_new_block_data (the reference's initNewBlockDataAfterRegrid
+with centered-linear prolongation, src/SayakaRegrid.cpp:987-1105) against the
+reference's own outputs (tests/golden/tf2, tf3) and the pinned numpy
+restatement (oracle/transfer_oracle.py) bit for bit; sayaka_mac_init_from
+(injection) against its restatement: blocks matched by root and child path
+are copied, refined blocks take injection from their nearest old leaf
+ancestor, blocks that became leaves by coarsening take the average of their
+old children, blocks over a deeper old subtree start from zero.  The elbow
+sequence then warm-starts every solve after a regrid from the previous
+tree's solution."""
 import numpy as np
 import pytest
 
 import sayakaamr_gb300 as sg
+from golden_io import load, seeded
+from oracle import transfer_oracle as to
 from sayakaamr_gb300 import workloads
+from test_transfer_oracle import TF, bc_types, build_trees
 
 pytestmark = pytest.mark.gpu
-
-
-def path_key(tb, b):
-    path = []
-    while tb["parent"][b] >= 0:
-        path.append(int(tb["which_child"][b]))
-        b = int(tb["parent"][b])
-    return (b, tuple(reversed(path)))
-
-
-def cell_ijk(nb, nd):
-    c = np.arange(nb ** nd)
-    return [c % nb, (c // nb) % nb if nd >= 2 else 0 * c, c // (nb * nb) if nd == 3 else 0 * c]
-
-
-def encode(ijk, nb, nd):
-    out = ijk[0] + nb * ijk[1]
-    return out + nb * nb * ijk[2] if nd == 3 else out
-
-
-def expected_transfer(tb_old, x_old, tb_new):
-    nd, nb = int(tb_new["ndim"]), int(tb_new["nb"])
-    ncell, half = nb ** nd, nb // 2
-    x_old = x_old.reshape(-1, ncell)
-    where = {path_key(tb_old, b): b for b in range(tb_old["num_blocks"])}
-    old_leaf = tb_old["node_type"] == 1
-    out = np.zeros((tb_new["num_blocks"], ncell))
-    ijk = cell_ijk(nb, nd)
-    kinds = [0, 0, 0, 0]
-    for b in np.nonzero(tb_new["node_type"] == 1)[0]:
-        root, path = path_key(tb_new, b)
-        ob = where.get((root, path))
-        if ob is not None and old_leaf[ob]:
-            out[b] = x_old[ob]
-            kinds[0] += 1
-            continue
-        if ob is None:
-            # nearest old ancestor, then injection one level at a time
-            for up in range(1, len(path) + 1):
-                oa = where.get((root, path[:len(path) - up]))
-                if oa is not None:
-                    break
-            if oa is not None and old_leaf[oa]:
-                pc = [a.copy() for a in ijk]
-                for digit in reversed(path[len(path) - up:]):
-                    for q in range(nd):
-                        pc[q] = ((digit >> q) & 1) * half + (pc[q] >> 1)
-                out[b] = x_old[oa][encode(pc, nb, nd)]
-                kinds[1] += 1
-                continue
-        if ob is not None:
-            kids = tb_old["child"].reshape(-1, 8)[ob][:1 << nd]
-            if np.all(kids >= 0) and np.all(old_leaf[kids]):
-                sq = [(a >= half).astype(int) for a in ijk]
-                cidx = sum(sq[q] << q for q in range(nd))
-                fb = [2 * (ijk[q] - sq[q] * half) for q in range(nd)] + [0] * (3 - nd)
-                acc = np.zeros(ncell)
-                for kk in range(2 if nd == 3 else 1):
-                    for jj in range(2):
-                        for ii in range(2):
-                            fi = [fb[0] + ii, fb[1] + jj, fb[2] + kk]
-                            acc = acc + x_old[kids[cidx], encode(fi, nb, nd)]
-                out[b] = acc / float(1 << nd)
-                kinds[2] += 1
-                continue
-        kinds[3] += 1
-    return out.reshape(-1), kinds
 
 
 def test_transfer_across_multilevel_refine_and_coarsen():
@@ -115,7 +54,7 @@ def test_transfer_across_multilevel_refine_and_coarsen():
     t.set_refine_flags(f)
     t.regrid()
     tb_new = t.tables()
-    want, kinds = expected_transfer(tb_old, x_old, tb_new)
+    want, kinds = to.transfer_injection(tb_old, x_old, tb_new)
     assert kinds[0] > 0 and kinds[1] > 0 and kinds[2] > 0, kinds
     S_new = sg.MacSolver(tb_new)
     S_new.init_from(S_old)
@@ -136,7 +75,7 @@ def test_elbow_warm_start_after_regrid():
             if S is not None:
                 x_prev = S.get_sol_compact()
                 S_new.init_from(S)
-                want, kinds = expected_transfer(tb_prev, x_prev, prob.tables)
+                want, kinds = to.transfer_injection(tb_prev, x_prev, prob.tables)
                 assert np.array_equal(S_new.get_sol_compact(), want), kinds
                 assert kinds[0] > 0, kinds
             S, tb_prev = S_new, prob.tables
@@ -148,3 +87,65 @@ def test_elbow_warm_start_after_regrid():
         assert info["rnorm"] < 1e-8 * info["rnorm0"]
         its.append((k, regridded, info["iterations"]))
     print("step, regridded, iterations:", its)
+
+
+@pytest.mark.parametrize("name", ["tf2", "tf3"])
+def test_centered_linear_transfer_matches_reference(name):
+    """the reference's regrid transfer (average-down, kept blocks, centered-
+    linear new blocks with same-level and Dirichlet / Neumann / SimpleFill
+    ghosts) through the C ABI, against the reference's dump"""
+    g = load(name)
+    tb_old, tb_new = build_trees(name)
+    nc = tb_old["nb"] ** tb_old["ndim"]
+    S_old = sg.MacSolver(tb_old)
+    S_old.set_init_sol(seeded(TF[name]["seed"], 1, tb_old["num_blocks"] * nc), ncomp=1, ngrow=0, comp=0)
+    S_new = sg.MacSolver(tb_new)
+    S_new.set_bc(bc_types(tb_new, g["bc_math"]))
+    S_new.init_from(S_old, prolong="centered_linear", bc_val=g["bc_val"])
+    assert np.array_equal(S_new.get_sol_compact(), g["new_x"])
+
+
+def test_centered_linear_transfer_across_several_regrids():
+    """old and new trees several regrids apart (new blocks whose parents are
+    new too): the CUDA transfer against the restatement"""
+    nb, nd = 8, 2
+    t = sg.AmrTree(nd, nb, 2, 5, 4000)
+    t.init_uniform_root((1, 1, 1), (0, 0, 0), (1, 1, 0), (-20,) * 6, (0,) * 6)
+    t.init_refine_to_min_level()
+    tb = t.tables()
+    lv2 = np.nonzero((tb["level"] == 2) & (tb["node_type"] == 1))[0]
+    f = np.zeros(tb["num_blocks"], np.int32)
+    f[lv2[:2]] = 1
+    t.set_refine_flags(f)
+    t.regrid()
+    tb_old = t.tables()
+    rng = np.random.default_rng(23)
+    x_old = rng.standard_normal(tb_old["num_blocks"] * nb ** nd)
+    S_old = sg.MacSolver(tb_old)
+    S_old.set_init_sol(x_old, ncomp=1, ngrow=0, comp=0)
+    kids1 = tb_old["child"].reshape(-1, 8)[lv2[0]][:4]
+    c = np.zeros(tb_old["num_blocks"], np.int32)
+    c[kids1] = 1
+    f = np.zeros(tb_old["num_blocks"], np.int32)
+    f[lv2[3]] = 1
+    t.set_refine_flags(f)
+    t.set_coarsen_flags(c)
+    t.regrid()
+    tb1 = t.tables()
+    f = np.zeros(tb1["num_blocks"], np.int32)
+    f[np.nonzero((tb1["level"] == 3) & (tb1["node_type"] == 1))[0][-1]] = 1
+    t.set_refine_flags(f)
+    t.regrid()
+    tb_new = t.tables()
+    bct = np.where(np.asarray(tb_new["neighbor"]).reshape(-1, 6) <= to.PHYS_BNDRY,
+                   np.array([1, 2, 0, 1, 0, 0]), -1).astype(np.int32).reshape(-1)
+    bc_val = np.array([0.5, -1.25, 0.0, 2.0, 0.0, 0.0])
+    want, new = to.transfer_reference(tb_old, x_old, tb_new, bct, bc_val)
+    assert new.sum() > 0
+    # a new block whose parent is new as well
+    par = np.asarray(tb_new["parent"])
+    assert any(new[par[b]] for b in np.nonzero(new)[0])
+    S_new = sg.MacSolver(tb_new)
+    S_new.set_bc(bct)
+    S_new.init_from(S_old, prolong="centered_linear", bc_val=bc_val)
+    assert np.array_equal(S_new.get_sol_compact(), want)
