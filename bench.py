@@ -660,7 +660,7 @@ def main():
     S.prepare()
 
     # ---- roofline of the dominant kernel, timed live on the solver stream ----
-    roof = roofline(S, prob, ext, torch, finest, args.precision)
+    roof = roofline(S, prob, ext, torch, finest, args.precision, args.smoother)
 
     out = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
@@ -987,7 +987,7 @@ def profiled_traffic(workload, precision):
     return float(m.group(1)) * 1e6, "profiles/" + name
 
 
-def roofline(S, prob, ext, torch, finest, precision):
+def roofline(S, prob, ext, torch, finest, precision, smoother=0):
     """dominant kernel: the red-black sweep (one colour) over the finest level
     of the finest tower, in the V-cycle's precision, with the variant the
     autotuner chose.  Algorithmic bytes per launch = cells of that level x
@@ -1034,6 +1034,8 @@ def roofline(S, prob, ext, torch, finest, precision):
             "bytes_per_launch": bytes_per_launch, "us_per_launch": us,
             "peak_source": src + " (burst copy)",
             "note": ("working set fits in L2 at this size: latency-bound; " if l2 else "") +
+                    ("the setting chosen smooths with block-hybrid passes (k_bhgs), which read the same "
+                     "arrays once per pass; " if smoother == 1 else "") +
                     "DRAM traffic per launch from the ncu summaries"}
 
 

@@ -111,7 +111,7 @@ struct BlockList {
 // chunks of a block list listed problem by problem (one BiCGSTAB state per
 // problem): the BiCGSTAB kernels run one CTA per chunk of at most kChunkCells
 // cells of one problem
-constexpr int kChunkCells = 2048;
+constexpr int kChunkCells = 8192;  // 32 cells per thread: the per-thread reduction epilogue is FP64 work
 struct Chunks {
   const int *comp;       // per chunk: its problem
   const int *beg, *end;  // per chunk: first and past-last cell of the list

@@ -51,19 +51,25 @@ __device__ __forceinline__ double wsum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-// max that keeps NaN (fmax drops it): a NaN anywhere in a vector must reach
-// the convergence test and end the solve as a breakdown, not as convergence
-__device__ __forceinline__ double nmax(double a, double b) { return (a != a || b != b) ? a + b : fmax(a, b); }
-
-__device__ __forceinline__ double wmax(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = nmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
 
 // Reduction of NV values (bit i of maxmask: max, else sum) over the `count`
 // CTAs whose partial slots are first .. first+count-1 (this CTA's is `slot`):
 // each CTA writes its partials; the last of them to arrive combines them in
 // slot order (deterministic for a fixed grid) and runs `epi` on thread 0.
+// Max values are non-negative (norms): they combine as their bit patterns
+// read as unsigned integers, on the integer pipe.  A NaN (all-ones exponent,
+// non-zero mantissa) orders above +inf, so a NaN anywhere in a vector reaches
+// the convergence test and ends the solve as a breakdown, not as convergence.
+__device__ __forceinline__ double bmax(double a, double b) {
+  const unsigned long long x = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long y = (unsigned long long)__double_as_longlong(b);
+  return __longlong_as_double((long long)(x > y ? x : y));
+}
+__device__ __forceinline__ double wbmax(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = bmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
 template <int NV, class Epi>
 __device__ __forceinline__ void seg_reduce(double (&v)[NV], unsigned maxmask, double *partials, unsigned *counter,
                                            int first, int count, int slot, Epi epi) {
@@ -78,14 +84,14 @@ __device__ __forceinline__ void seg_reduce(double (&v)[NV], unsigned maxmask, do
       double x = lane < kTPB / 32 ? sh[i][lane] : 0.0;
       for (int o = (kTPB / 64); o > 0; o >>= 1) {
         const double y = __shfl_xor_sync(0xffffffffu, x, o);
-        x = ((maxmask >> i) & 1) ? nmax(x, y) : x + y;
+        x = ((maxmask >> i) & 1) ? bmax(x, y) : x + y;
       }
       r[i] = x;
     }
   };
 #pragma unroll
   for (int i = 0; i < NV; i++) {
-    const double r = ((maxmask >> i) & 1) ? wmax(v[i]) : wsum(v[i]);
+    const double r = ((maxmask >> i) & 1) ? wbmax(v[i]) : wsum(v[i]);
     if (lane == 0) sh[i][w] = r;
   }
   __syncthreads();
@@ -110,13 +116,13 @@ __device__ __forceinline__ void seg_reduce(double (&v)[NV], unsigned maxmask, do
 #pragma unroll
     for (int i = 0; i < NV; i++) {
       const double pv = ((volatile double *)partials)[b * NV + i];
-      acc[i] = ((maxmask >> i) & 1) ? nmax(acc[i], pv) : acc[i] + pv;
+      acc[i] = ((maxmask >> i) & 1) ? bmax(acc[i], pv) : acc[i] + pv;
     }
   }
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < NV; i++) {
-    const double r = ((maxmask >> i) & 1) ? wmax(acc[i]) : wsum(acc[i]);
+    const double r = ((maxmask >> i) & 1) ? wbmax(acc[i]) : wsum(acc[i]);
     if (lane == 0) sh[i][w] = r;
   }
   __syncthreads();

@@ -74,11 +74,15 @@ __device__ __forceinline__ T geom(const Coef<T> &c, int b, int q) { return c.geo
 
 // the record of block b when it is a constant-coefficient block (Coef::ut),
 // else null
+// (the flag is 0 or 1: tested as bits, so that no FP64 compare is issued)
 template <typename T>
 __device__ __forceinline__ const T *uniform_of(const Coef<T> &c, int b) {
   if (!c.ut) return nullptr;
   const T *u = c.ut + (long)b * kUni;
-  return u[3] != (T)0 ? u : nullptr;
+  if constexpr (sizeof(T) == 8)
+    return __double_as_longlong(u[3]) != 0 ? u : nullptr;
+  else
+    return __float_as_uint(u[3]) != 0u ? u : nullptr;
 }
 
 // coefficient of a coarse/fine face: ((beta*ds)/(dx*h))*B*a
