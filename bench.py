@@ -268,9 +268,19 @@ def cpu_solve(prob, max_iter=2000, budget_s=None, n_iters=None):
                 sampled=True, per_iteration=per_it, sample_iterations=info["iterations"])
 
 
+def oracle_workloads():
+    """the workload generators with their trees built by the oracle's
+    restatement of the reference's tree (oracle/tree_oracle.py, the same
+    tables bit for bit), so that the reference arm runs no product code"""
+    from sayakaamr_gb300 import workloads
+    from oracle.tree_oracle import TreeOracle
+    workloads.use_tree_builder(TreeOracle)
+    return workloads
+
+
 def _cpu_worker(args):
     name, max_iter, budget = args
-    from sayakaamr_gb300 import workloads
+    workloads = oracle_workloads()
     prob = workloads.CONFIGS[name]()
     return cpu_solve(prob, max_iter, budget)
 
@@ -317,7 +327,7 @@ def run_reference(args):
     if rank != 0:
         return
     import multiprocessing as mp
-    from sayakaamr_gb300 import workloads
+    workloads = oracle_workloads()
     prob = (workloads.config4(n_problems=args.problems) if args.config == "config4"
             else workloads.CONFIGS[args.config]())
     cores = os.cpu_count() or 1
@@ -351,7 +361,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.config, **prob.describe(), "tol_rel": TOL},
+        "config": {"workload": args.config, **prob.describe(), "tol_rel": TOL,
+                   "trees": "built by the oracle's restatement of the reference's tree (oracle/tree_oracle.py)"},
         "cpu_baseline": {"value": v, "unit": "cells/s", "cores": cores, "kind": "port",
                          "sample": ("C oracle (bit-exact restatement of the reference solver, bottom BiCGSTAB to "
                                     "1e-10), one copy of the workload per core; " +
@@ -394,7 +405,8 @@ def run_reference_batch(args, prob, cores, ctx):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": prob.leaf_cells / v * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.config, **prob.describe(), "tol_rel": TOL},
+        "config": {"workload": args.config, **prob.describe(), "tol_rel": TOL,
+                   "trees": "built by the oracle's restatement of the reference's tree (oracle/tree_oracle.py)"},
         "cpu_baseline": {"value": v, "unit": "cells/s", "cores": cores, "kind": "port",
                          "sample": ("C oracle (bit-exact restatement of the reference solver, bottom BiCGSTAB to "
                                     "1e-10); each step solves %d whole problems of the batch to 1e-8, one per "

@@ -63,10 +63,22 @@ def face_centres(tb, fd):
     return lo[:, None, :] + idx[None, :, :] * dx[:, None, :]
 
 
+# the class that builds the trees: this package's AmrTree, or any class with
+# its interface (init_uniform_root, init_refine_to_min_level,
+# set_refine_flags, regrid, tables) and the same tables
+_tree_class = AmrTree
+
+
+def use_tree_builder(cls=None):
+    """build the workloads' trees with `cls` (None: this package's AmrTree)"""
+    global _tree_class
+    _tree_class = cls or AmrTree
+
+
 def refine_tree(ndim, nb, nroot, lo, hi, min_level, max_level, need_refine, bc_code=(-20,) * 6, capacity=200000):
     """Root grid + static refinement to min_level + level-by-level refinement
     of the leaf blocks for which need_refine(block_lo, block_hi, level) is true."""
-    t = AmrTree(ndim, nb, min_level, max_level, capacity)
+    t = _tree_class(ndim, nb, min_level, max_level, capacity)
     t.init_uniform_root(nroot, lo, hi, bc_code, (0,) * 6)
     t.init_refine_to_min_level()
     for level in range(1, max_level):
