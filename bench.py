@@ -102,8 +102,8 @@ def parse():
     ap.add_argument("--smooth-variant", type=int, default=-1,
                     help="device smoother launch-bounds variant (-1: autotuned at prepare)")
     ap.add_argument("--vcycle-out", type=int, default=0,
-                    help="FP32 V-cycle output: 0 read in place, 1 read in place with the operator in double-float, "
-                         "2 widened into FP64 vectors")
+                    help="FP32 V-cycle output: 0 auto (in place in 2D and on small 3D towers), 1 in place with the "
+                         "operator in double-float, 2 widened into FP64 vectors, 3 in place")
     ap.add_argument("--kernel", type=int, default=-1,
                     help="time one kernel alone and exit (for ncu): 0 FP64 operator on the finest tower, "
                          "1 FP32 / 2 FP64 red-black sweep (one colour) of the finest level, "

@@ -101,6 +101,14 @@ class MacSolverGpu {
   }
   void setZeroSol() { check(sayaka_mac_set_zero_sol(m_h)); }
   void getSol(TreeData &d, int c) { check(sayaka_mac_get_sol(m_h, base(d), d.numComp(), d.numGrow(), c)); }
+  /* after AmrTree::regrid: the solution of the solver of the old tree as the
+   * initial solution, carried as AmrTree::initNewBlockDataAfterRegrid carries
+   * a cell state with centered-linear prolongation after an average-down
+   * (src/SayakaRegrid.cpp:987-1105); bc_val[face position] are the BC values
+   * of the pressure's register (null: 0).  Call setBC first. */
+  void setInitSolFromRegrid(const MacSolverGpu &old, const double *bc_val = nullptr) {
+    check(sayaka_mac_init_new_block_data(m_h, old.m_h, bc_val));
+  }
 
   /* solver parameters (src/SayakaMacSolver.h:346-358) */
   void setTolerance(double rel, double abs) {

@@ -123,8 +123,8 @@ typedef struct sayaka_params {
                              finest whose tower is one uniform level with at most 1024 (2D) / 4096 (3D) cells
                              per connected component; level 1 otherwise), n >= 1 = level n if its tower is
                              one uniform level of at most 4096 cells per component */
-  int32_t bottom_half;    /* device path, FP32 V-cycle, bottom above level 1: 1 = apply an FP16 copy of the
-                             dense inverse with one FP32 scale per row (half the bytes), 0 = FP32 copy */
+  int32_t bottom_half;    /* device path, FP32 V-cycle: 1 = apply an FP16 copy of the dense bottom inverse
+                             with one FP32 scale per row (half the bytes), 0 = an FP32 copy */
   int32_t sublevel_order; /* device V-cycle smoothing over a tower's sublevels: 0 = finest to coarsest,
                              red then black per sublevel (the reference's order, mg_smooth_level);
                              1 = one launch per colour and level parity (default) */
@@ -149,10 +149,11 @@ typedef struct sayaka_params {
   int32_t learned_tc05;   /* learned correction of 16x16-cell blocks: 1 = its 32 -> 32 layer as an implicit GEMM
                              on tcgen05 with the accumulator in tensor memory (default); 0 = on mma.sync warp
                              MMAs (the same network, products summed in another order) */
-  int32_t vcycle_out;     /* how the BiCGSTAB kernels read the FP32 V-cycle's output: 0 = in place, widened
-                             exactly on the integer pipe where they read it (default); 1 = in place, the
-                             operator evaluated in double-float on the FP32 pipe; 2 = widened once into FP64
-                             vectors */
+  int32_t vcycle_out;     /* how the BiCGSTAB kernels read the FP32 V-cycle's output: 0 = in place (widened
+                             exactly on the integer pipe where they read it) in 2D and on 3D towers of at most
+                             2,097,152 cells, widened once into FP64 vectors on larger 3D towers (default); 1 =
+                             in place, the operator evaluated in double-float on the FP32 pipe; 2 = always
+                             widened; 3 = always in place */
   int32_t prolong_form;   /* device V-cycle, the prolongation fused with the first red sweep of its level:
                              1 = one warp per block with the block in registers (2D FP32 16x16 blocks,
                              default; elsewhere form 0), 0 = one CTA per block with a shared-memory tile; the
@@ -262,8 +263,12 @@ int sayaka_mac_launch_counts(sayaka_mac *h, int32_t *prologue, int32_t *per_iter
  * 10 two cells per thread (the same cell of two blocks, operands of both
  * gathered before either is updated), cap 64, 11-12 one warp per 16x16
  * block of a 2D FP32 sweep with the block in registers: 16-byte loads and
- * stores, neighbours by shuffles, caps 64/48 (elsewhere the same as 3)) */
+ * stores, neighbours by shuffles, caps 64/48, 13 the same with every load of
+ * a block issued before its first branch, cap 64 (elsewhere 11-13 are the
+ * same as 3)) */
 int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n);
+/* number of smoother launch variants the autotuner times */
+int32_t sayaka_smoother_variants(void);
 /* level of the device solve's dense bottom solve once prepared (-1 before) */
 int32_t sayaka_mac_bottom_level(const sayaka_mac *h);
 /* number of independent problems (connected components) of the handle's

@@ -99,6 +99,7 @@ SIGNATURES = {
     "sayaka_mac_enqueue_kernel": (C.c_int, [_V, C.c_int32, C.c_int32]),
     "sayaka_mac_tower_size": (C.c_int32, [_V, C.c_int32, C.c_int32]),
     "sayaka_mac_tuned_smoother": (C.c_int32, [_V, C.c_int32, C.POINTER(C.c_float), C.c_int32]),
+    "sayaka_smoother_variants": (C.c_int32, []),
     "sayaka_mac_launch_counts": (C.c_int, [_V, _i32p, _i32p, _i32p]),
     "sayaka_mac_flux": (C.c_int, [_V, C.c_int32, _f64p, C.c_int32, C.c_int32, C.c_int32, _f64p, C.c_int32,
                                   C.c_int32, C.c_int32]),
@@ -553,9 +554,10 @@ class MacSolver:
 
     def tuned_smoother(self, precision):
         """(chosen variant, microseconds per variant) of the smoother autotuner"""
-        us = (C.c_float * 13)()
-        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 13)
-        return int(v), [float(x) for x in us]
+        us = (C.c_float * 16)()
+        v = self.lib.sayaka_mac_tuned_smoother(self.h, int(precision), us, 16)
+        n = int(self.lib.sayaka_smoother_variants())
+        return int(v), [float(x) for x in us][:n]
 
     def problem_count(self):
         """independent problems (connected components) of the tree"""

@@ -674,7 +674,7 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.learned_loss = p->learned_loss;
     if (p->prolong_form < 0 || p->prolong_form > 1) return (int)SAYAKA_BAD_INPUT;
     s.prolong_form = p->prolong_form;
-    if (p->vcycle_out < 0 || p->vcycle_out > 2) return (int)SAYAKA_BAD_INPUT;
+    if (p->vcycle_out < 0 || p->vcycle_out > 3) return (int)SAYAKA_BAD_INPUT;
     s.vcycle_out = p->vcycle_out;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
@@ -968,6 +968,7 @@ int32_t sayaka_mac_bottom_level(const sayaka_mac *h) {
   if (!h || !h->gpu) return -1;
   return h->gpu->bottom_level();
 }
+int32_t sayaka_smoother_variants(void) { return kRbgsVariants; }
 int32_t sayaka_mac_tuned_smoother(sayaka_mac *h, int32_t precision, float *us, int32_t n) {
   if (!h || !h->gpu) return -1;
   float tmp[16] = {};

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "dev_alloc.h"
 #include "cuda_check.h"
 #include "mac_device.h"
 #include "mac_solver.h"
@@ -242,7 +243,7 @@ void MacGpu::build_coef_lists() {
       }
     auto up_dev = [&](const std::vector<int> &v, int *&d) {
       if (v.empty()) return;
-      if (cudaMalloc(&d, v.size() * sizeof(int)) != cudaSuccess) {
+      if (dev_malloc(&d, v.size() * sizeof(int)) != cudaSuccess) {
         fail("out of device memory (coefficient lists)");
         return;
       }
@@ -258,12 +259,12 @@ void MacGpu::build_coef_lists() {
 
 void MacGpu::free_coef_lists() {
   for (auto *p : d_sync_up_)
-    if (p) cudaFree(p);
+    if (p) dev_free(p);
   for (auto *p : d_sync_copy_)
-    if (p) cudaFree(p);
+    if (p) dev_free(p);
   d_sync_up_.clear();
   d_sync_copy_.clear();
-  if (d_ls_) cudaFree(d_ls_);
+  if (d_ls_) dev_free(d_ls_);
   d_ls_ = nullptr;
   coef_lists_ = false;
 }
@@ -339,10 +340,10 @@ void MacGpu::set_ib_frac_by_ls(const double *ls, int ng, bool dev) {
   if (!dev) {  // staged in a device buffer kept for the next call
     if (bytes > ls_cap_) {
       CK(cudaStreamSynchronize(stream_));
-      if (d_ls_) cudaFree(d_ls_);
+      if (d_ls_) dev_free(d_ls_);
       d_ls_ = nullptr;
       ls_cap_ = 0;
-      if (cudaMalloc(&d_ls_, bytes) != cudaSuccess) {
+      if (dev_malloc(&d_ls_, bytes) != cudaSuccess) {
         fail("out of device memory (level set)");
         return;
       }

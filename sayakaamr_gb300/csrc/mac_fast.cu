@@ -19,6 +19,7 @@
 
 #include <cuda_fp16.h>
 
+#include "dev_alloc.h"
 #include "mac_solver.h"
 #include "cuda_check.h"
 #include "mac_stencil.cuh"
@@ -881,8 +882,8 @@ void MacGpu::ensure_fast_buffers() {
   const size_t nc = (size_t)nbk * ncell_, nf = (size_t)nbk * nfb_;
   auto fa = [&](size_t n) {
     float *p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(float)) != cudaSuccess) fail("out of device memory (fp32)");
-    else cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(float));
+    if (dev_malloc(&p, std::max<size_t>(n, 1) * sizeof(float)) != cudaSuccess) fail("out of device memory (fp32)");
+    else cudaMemsetAsync(p, 0, std::max<size_t>(n, 1) * sizeof(float), stream_);
     return p;
   };
   for (int d = 0; d < nd; d++) {
@@ -895,28 +896,28 @@ void MacGpu::ensure_fast_buffers() {
   d_resid32_ = fa(nc);
   d_corr32_ = fa(nc);
   d_corr32b_ = fa(nc);
-  if (cudaMalloc(&d_corr64b_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (correction)");
-  else cudaMemset(d_corr64b_, 0, nc * sizeof(double));
-  if (cudaMalloc(&d_opP_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
-  if (cudaMalloc(&d_opS_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
-  if (cudaMalloc(&d_opP2_, nc * sizeof(float2)) != cudaSuccess ||
-      cudaMalloc(&d_opS2_, nc * sizeof(float2)) != cudaSuccess ||
-      cudaMalloc(&d_uni2_, (size_t)std::max(nbk, 1) * kUni * sizeof(float2)) != cudaSuccess)
+  if (dev_malloc(&d_corr64b_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (correction)");
+  else cudaMemsetAsync(d_corr64b_, 0, nc * sizeof(double), stream_);
+  if (dev_malloc(&d_opP_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
+  if (dev_malloc(&d_opS_, nc * sizeof(double)) != cudaSuccess) fail("out of device memory (operator factors)");
+  if (dev_malloc(&d_opP2_, nc * sizeof(float2)) != cudaSuccess ||
+      dev_malloc(&d_opS2_, nc * sizeof(float2)) != cudaSuccess ||
+      dev_malloc(&d_uni2_, (size_t)std::max(nbk, 1) * kUni * sizeof(float2)) != cudaSuccess)
     fail("out of device memory (operator factors)");
   else
-    cudaMemset(d_uni2_, 0, (size_t)std::max(nbk, 1) * kUni * sizeof(float2));
-  if (cudaMalloc(&d_uni64_, (size_t)std::max(nbk, 1) * kUni * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&d_uni32_, (size_t)std::max(nbk, 1) * kUni * sizeof(float)) != cudaSuccess)
+    cudaMemsetAsync(d_uni2_, 0, (size_t)std::max(nbk, 1) * kUni * sizeof(float2), stream_);
+  if (dev_malloc(&d_uni64_, (size_t)std::max(nbk, 1) * kUni * sizeof(double)) != cudaSuccess ||
+      dev_malloc(&d_uni32_, (size_t)std::max(nbk, 1) * kUni * sizeof(float)) != cudaSuccess)
     fail("out of device memory (block records)");
   else {
-    cudaMemset(d_uni64_, 0, (size_t)std::max(nbk, 1) * kUni * sizeof(double));
-    cudaMemset(d_uni32_, 0, (size_t)std::max(nbk, 1) * kUni * sizeof(float));
+    cudaMemsetAsync(d_uni64_, 0, (size_t)std::max(nbk, 1) * kUni * sizeof(double), stream_);
+    cudaMemsetAsync(d_uni32_, 0, (size_t)std::max(nbk, 1) * kUni * sizeof(float), stream_);
   }
-  if (cudaMalloc(&d_st_, sizeof(FState)) != cudaSuccess) fail("alloc state");
+  if (dev_malloc(&d_st_, sizeof(FState)) != cudaSuccess) fail("alloc state");
   if (cudaMallocHost(&h_st_, sizeof(FState)) != cudaSuccess) fail("alloc pinned state");
-  if (cudaMalloc(&d_part_, sizeof(double) * kMaxRedBlocks * 4) != cudaSuccess) fail("alloc partials");
-  if (cudaMalloc(&d_cnt_, sizeof(unsigned) * 4) != cudaSuccess) fail("alloc counter");
-  cudaMemset(d_cnt_, 0, sizeof(unsigned) * 4);
+  if (dev_malloc(&d_part_, sizeof(double) * kMaxRedBlocks * 4) != cudaSuccess) fail("alloc partials");
+  if (dev_malloc(&d_cnt_, sizeof(unsigned) * 4) != cudaSuccess) fail("alloc counter");
+  cudaMemsetAsync(d_cnt_, 0, sizeof(unsigned) * 4, stream_);
   c32_.geom = d_geom32_;
   for (int d = 0; d < 3; d++) {
     const int dd = d < nd ? d : 0;
@@ -942,7 +943,7 @@ void MacGpu::build_smooth_factors() {
     const BlockList TL = tower_list(l);
     const long w = (long)TL.n * ncell_;
     if (w == 0) continue;
-    if (!d_sfac_[l] && cudaMalloc(&d_sfac_[l], 2 * w * sizeof(double)) != cudaSuccess) {
+    if (!d_sfac_[l] && dev_malloc(&d_sfac_[l], 2 * w * sizeof(double)) != cudaSuccess) {
       d_sfac_[l] = nullptr;
       fail("out of device memory (smoother factors)");
       return;
@@ -960,7 +961,7 @@ void MacGpu::build_smooth_factors() {
     const BlockList PL{tw.par.blocks, tw.par.ftypes, tw.par.n};
     const long w = (long)PL.n * ncell_;
     if (w == 0) continue;
-    if (!d_pfac_[l] && cudaMalloc(&d_pfac_[l], 2 * w * sizeof(double)) != cudaSuccess) {
+    if (!d_pfac_[l] && dev_malloc(&d_pfac_[l], 2 * w * sizeof(double)) != cudaSuccess) {
       d_pfac_[l] = nullptr;
       fail("out of device memory (smoother factors)");
       return;
@@ -1327,7 +1328,7 @@ void MacGpu::build_bottom() {
   if (!reuse) bottom_free();
   auto up = [&](auto *&dptr, const auto &v) {
     using E = typename std::remove_reference<decltype(v[0])>::type;
-    if (cudaMalloc(&dptr, std::max<size_t>(v.size(), 1) * sizeof(E)) != cudaSuccess) {
+    if (dev_malloc(&dptr, std::max<size_t>(v.size(), 1) * sizeof(E)) != cudaSuccess) {
       fail("out of device memory (bottom solve)");
       return;
     }
@@ -1359,11 +1360,11 @@ void MacGpu::build_bottom() {
     const int nmat = (int)offs.size();
     long long *d_offs = nullptr;
     double *row = nullptr, *col = nullptr;
-    CK_(cudaMalloc(&d_offs, nmat * sizeof(long long)));
-    CK_(cudaMalloc(&row, (size_t)nmat * m * sizeof(double)));
-    CK_(cudaMalloc(&col, (size_t)nmat * m * sizeof(double)));
+    CK_(dev_malloc(&d_offs, nmat * sizeof(long long)));
+    CK_(dev_malloc(&row, (size_t)nmat * m * sizeof(double)));
+    CK_(dev_malloc(&col, (size_t)nmat * m * sizeof(double)));
     double *ipiv = nullptr;
-    CK_(cudaMalloc(&ipiv, nmat * sizeof(double)));
+    CK_(dev_malloc(&ipiv, nmat * sizeof(double)));
     CK_(cudaMemcpyAsync(d_offs, offs.data(), nmat * sizeof(long long), cudaMemcpyHostToDevice, stream_));
     const int step_grid = (int)std::min<long>((long)nmat * m, 152 * 16);
     for (int k = 0; k < m; k++) {
@@ -1371,24 +1372,26 @@ void MacGpu::build_bottom() {
       k_gj_step<<<step_grid, kTPB, 0, stream_>>>(m, k, nmat, d_offs, d_binv_, row, col, ipiv);
     }
     CK_(cudaStreamSynchronize(stream_));
-    cudaFree(d_offs);
-    cudaFree(row);
-    cudaFree(col);
-    cudaFree(ipiv);
+    dev_free(d_offs);
+    dev_free(row);
+    dev_free(col);
+    dev_free(ipiv);
   }
   for (int r0 : pins) {
     const int c = rcomp[r0];
     k_zero_col<<<(comp_n[c] + kTPB - 1) / kTPB, kTPB, 0, stream_>>>(comp_off[c], comp_n[c], r0 - comp_row0[c], d_binv_);
   }
-  // an FP32 copy for the FP32 V-cycle when the bottom is above level 1: its
-  // product is then large (up to kBottomMaxCells^2 per component) and FP64
-  // multiply-adds run at 1/64 of the FP32 rate here
+  // an FP32 (or FP16) copy for the FP32 V-cycle: the product is large when
+  // the bottom is above level 1 (up to kBottomMaxCells^2 per component) or
+  // when a forest has one component per problem (the batch workload: 584 MB
+  // of FP64 inverse per product), and FP64 multiply-adds run at 1/64 of the
+  // FP32 rate here
   bot_half_ = prm_.bottom_half;
   // the FP16 product reads rows in 16-byte pieces: every row must start on
   // a 16-byte boundary (component orders that are multiples of 8)
   bool rows16 = true;
   for (int c = 0; c < nc; c++) rows16 = rows16 && comp_n[c] % 8 == 0 && comp_off[c] % 8 == 0;
-  if (LB > 1 && prm_.bottom_half && rows16) {
+  if (prm_.bottom_half && rows16) {
     // FP16 rows with one scale each: half the bytes of the FP32 copy
     std::vector<long long> row_off(n_bot_);
     std::vector<int> row_m(n_bot_);
@@ -1399,11 +1402,11 @@ void MacGpu::build_bottom() {
     }
     long long *d_ro = nullptr;
     int *d_rm = nullptr;
-    if ((!d_binv16_ && cudaMalloc(&d_binv16_, (size_t)tot * sizeof(unsigned short)) != cudaSuccess) ||
-        (!d_rscale_ && cudaMalloc(&d_rscale_, (size_t)n_bot_ * sizeof(float)) != cudaSuccess) ||
-        cudaMalloc(&d_ro, (size_t)n_bot_ * sizeof(long long)) != cudaSuccess ||
-        cudaMalloc(&d_rm, (size_t)n_bot_ * sizeof(int)) != cudaSuccess) {
-      if (d_ro) cudaFree(d_ro);
+    if ((!d_binv16_ && dev_malloc(&d_binv16_, (size_t)tot * sizeof(unsigned short)) != cudaSuccess) ||
+        (!d_rscale_ && dev_malloc(&d_rscale_, (size_t)n_bot_ * sizeof(float)) != cudaSuccess) ||
+        dev_malloc(&d_ro, (size_t)n_bot_ * sizeof(long long)) != cudaSuccess ||
+        dev_malloc(&d_rm, (size_t)n_bot_ * sizeof(int)) != cudaSuccess) {
+      if (d_ro) dev_free(d_ro);
       fail("out of device memory (bottom solve)");
       return;
     }
@@ -1411,10 +1414,10 @@ void MacGpu::build_bottom() {
     CK_(cudaMemcpyAsync(d_rm, row_m.data(), row_m.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
     k_half_rows<<<std::min(n_bot_, 152 * 16), kTPB, 0, stream_>>>(n_bot_, d_ro, d_rm, d_binv_, d_binv16_, d_rscale_);
     CK_(cudaStreamSynchronize(stream_));
-    cudaFree(d_ro);
-    cudaFree(d_rm);
-  } else if (LB > 1) {
-    if (!d_binv32_ && cudaMalloc(&d_binv32_, (size_t)tot * sizeof(float)) != cudaSuccess) {
+    dev_free(d_ro);
+    dev_free(d_rm);
+  } else {
+    if (!d_binv32_ && dev_malloc(&d_binv32_, (size_t)tot * sizeof(float)) != cudaSuccess) {
       d_binv32_ = nullptr;
       fail("out of device memory (bottom solve)");
       return;
@@ -1435,7 +1438,7 @@ void MacGpu::build_bottom() {
 void MacGpu::bottom_free() {
   for (void *p : {(void *)d_binv16_, (void *)d_rscale_, (void *)d_binv32_, (void *)d_binv_, (void *)d_bot_blocks_, (void *)d_comp_row0_, (void *)d_comp_n_,
                   (void *)d_comp_off_, (void *)d_tile_comp_, (void *)d_tile_row0_})
-    if (p) cudaFree(p);
+    if (p) dev_free(p);
   d_binv_ = nullptr;
   d_binv32_ = nullptr;
   d_binv16_ = nullptr;
@@ -1557,15 +1560,21 @@ void MacGpu::precondition(int L, T *resid, T *corr, const Coef<T> &c, double *ou
 }
 
 // FP32 V-cycle output read in place by the BiCGSTAB kernels, widened exactly
-// on the integer pipe where they read it (params.vcycle_out 0, or 1 with the
-// operator in double-float); params.vcycle_out 2 widens it once into FP64
-// phat / shat instead.  On the batch workload (2D, 29M cells) the three run
-// within 1%: 63.2 (in place), 63.9 (double-float operator) and 64.6 ms
-// (widened); on config3 (3D, 15.9M cells) 27.5, 27.8 and 27.5 ms.
+// on the integer pipe where they read it, or widened once into FP64 phat /
+// shat.  params.vcycle_out 0 (auto): in place in 2D and on 3D towers of at
+// most 2M cells, where it saves two launches per iteration (batch workload,
+// 2D, 29M cells: 58.8 in place vs 60.4 ms widened); larger 3D towers widen,
+// since the 3D operator reads seven cells and their integer widenings cost
+// more than the launches (config3, 15.9M cells: 31.6 in place vs 27.3 ms).
+// 1 = in place with the operator in double-float, 2 = always widened, 3 =
+// always in place.
+constexpr long kDirectF32Cells = 1l << 21;
 template <typename T>
 void MacGpu::iteration_device(T *resid, T *corr, const Coef<T> &c) {
   if constexpr (sizeof(T) == 4) {
-    const bool direct = prm_.vcycle_out != 2;
+    const long w = (long)tower_list(finest_).n * ncell_;
+    const bool direct = prm_.vcycle_out == 1 || prm_.vcycle_out == 3 ||
+                        (prm_.vcycle_out == 0 && (tt_.ndim == 2 || w <= kDirectF32Cells));
     if (!learned_active() && direct) {
       iteration_body<T, float>(resid, corr, c, corr, corr, nullptr, nullptr);
       return;
@@ -1831,7 +1840,7 @@ int MacGpu::enqueue_solve() {
         if (record_) {  // a collection solve keeps every iterate
           double *cp = nullptr;
           const size_t n = (size_t)tt_.num_blocks * ncell_;
-          if (cudaMalloc(&cp, n * sizeof(double)) != cudaSuccess) {
+          if (dev_malloc(&cp, n * sizeof(double)) != cudaSuccess) {
             fail("out of device memory (recorded iterates)");
             return -1;
           }
@@ -1909,7 +1918,7 @@ int MacGpu::solve_state(SolveInfo *info) {
     unsigned w[4];
     CKR_(cudaMemcpy(w, d_bar_, sizeof(w), cudaMemcpyDeviceToHost), -1);
     if (w[2] != 0) {
-      cudaMemset(d_bar_, 0, 4 * sizeof(unsigned));
+      cudaMemsetAsync(d_bar_, 0, 4 * sizeof(unsigned), stream_);
       fail("cooperative V-cycle: grid barrier timed out");
       return -1;
     }
@@ -2118,7 +2127,7 @@ int fp_selftest(const double *d, const float *f, int n, float *nar, float *nar_h
   if (n <= 0) return 0;
   unsigned char *buf = nullptr;
   const size_t fb = (size_t)n * sizeof(float), db = (size_t)n * sizeof(double);
-  if (cudaMalloc(&buf, 3 * fb + 5 * db) != cudaSuccess) return 2;
+  if (dev_malloc(&buf, 3 * fb + 5 * db) != cudaSuccess) return 2;
   double *dd = (double *)buf, *w = dd + n, *whw = w + n, *w0 = whw + n, *w0hw = w0 + n;
   float *ff = (float *)(w0hw + n), *nr = ff + n, *nrhw = nr + n;
   cudaMemcpy(dd, d, db, cudaMemcpyHostToDevice);
@@ -2134,7 +2143,7 @@ int fp_selftest(const double *d, const float *f, int n, float *nar, float *nar_h
     cudaMemcpy(wid0, w0, db, cudaMemcpyDeviceToHost);
     cudaMemcpy(wid0_hw, w0hw, db, cudaMemcpyDeviceToHost);
   }
-  cudaFree(buf);
+  dev_free(buf);
   return e == cudaSuccess ? 0 : 2;
 }
 

@@ -406,6 +406,125 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_warp16(Topo t, Coef<flo
   }
 }
 
+// the cell-by-cell sweep of one block (four cells of the colour per lane)
+__device__ __forceinline__ void warp16_slow_block(const Topo &t, const Coef<float> &c, int b, uint16_t ft, int color,
+                                               float *__restrict__ phi, const float *__restrict__ rhs, const int *e,
+                                               int lane) {
+  for (int k = 0; k < 4; k++) {
+    const int h = lane * 4 + k;
+    int ijk[3];
+    color_cell_fast<2>(h, t, color, ijk);
+    smooth_cell_fast<float, 2>(t, c, b, ft, ijk, phi, rhs, nullptr, nullptr, e);
+  }
+}
+
+// k_rbgs_warp16 with every load of a block issued before its first branch:
+// the descriptor (two vector loads), then at once the block record, dv, the
+// face BC types, phi and rhs and the halo values (their ids and face types
+// come with the descriptor), and only then the problem's done flag, the
+// fast-path test and the sweep.  The latency of a block is then about three
+// dependent loads (descriptor, data, done flag) instead of six.  Same
+// arithmetic, same bits.  Needs the list's halo descriptors.
+template <int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_rbgs_warp16_flat(Topo t, Coef<float> c, BlockList L, int color,
+                                                                     float *__restrict__ phi,
+                                                                     const float *__restrict__ rhs,
+                                                                     const int *guard) {
+  pdl_enter();
+  if (guard && *guard) return;
+  constexpr int NB = 16, NC = 256;
+  const int lane = threadIdx.x & 31;
+  const int warps = blockDim.x >> 5;
+  const int j = lane >> 1, hh = lane & 1, c0 = 8 * hh;
+  for (int p = blockIdx.x * warps + (threadIdx.x >> 5); p < L.n; p += gridDim.x * warps) {
+    const int *e = L.hx + (long)p * kHX;
+    const int4 nb4 = *reinterpret_cast<const int4 *>(e);           // face neighbours 0..3
+    const int2 ib = *reinterpret_cast<const int2 *>(e + kHXInfo);  // info, block
+    const int b = ib.y;
+    const uint16_t ft = (uint16_t)(ib.x & 0xffff);
+    const int ty[4] = {face_type_of(ft, 0), face_type_of(ft, 1), face_type_of(ft, 2), face_type_of(ft, 3)};
+    const long cb = (long)b * NC;
+    // ---- every load of the block
+    const int comp = L.stc ? L.comp[b] : 0;
+    const float4 rec = c.ut ? *reinterpret_cast<const float4 *>(c.ut + (long)b * kUni) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float dv = geom(c, b, 6);
+    const int2 bc01 = *reinterpret_cast<const int2 *>(t.bc_type + b * 6);
+    const int2 bc23 = *reinterpret_cast<const int2 *>(t.bc_type + b * 6 + 2);
+    const int par = (color + j) & 1;  // column parity of this row's cells of the colour
+    const float4 *src = reinterpret_cast<const float4 *>(phi + cb + j * NB + c0);
+    const float4 *rsrc = reinterpret_cast<const float4 *>(rhs + cb + j * NB + c0);
+    const float4 p0 = src[0], p1 = src[1], r0 = rsrc[0], r1 = rsrc[1];
+    float hl = 0.f, hr = 0.f;
+    if (hh == 0 && ty[0] == 0) hl = phi[(long)nb4.x * NC + j * NB + (NB - 1)];
+    if (hh == 1 && ty[1] == 0) hr = phi[(long)nb4.y * NC + j * NB];
+    float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
+    if ((j == 0 && ty[2] == 0) || (j == NB - 1 && ty[3] == 0)) {
+      const int n = j == 0 ? nb4.z : nb4.w;
+      const float4 *hs = reinterpret_cast<const float4 *>(phi + (long)n * NC + (j == 0 ? NB - 1 : 0) * NB + c0);
+      a0 = hs[0];
+      a1 = hs[1];
+    }
+    // ---- then the decisions
+    if (L.stc && L.stc[comp].done) continue;  // uniform over the warp
+    bool fast = c.ut != nullptr && __float_as_uint(rec.w) != 0u;
+#pragma unroll
+    for (int f = 0; f < 4; f++) fast = fast && ty[f] <= 1;
+    if (!fast) {
+      warp16_slow_block(t, c, b, ft, color, phi, rhs, e, lane);
+      continue;
+    }
+    float v[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+    // rhs and the halo row of the colour's four cells only (cell k = 2q + par)
+    const float rs[4] = {par ? r0.y : r0.x, par ? r0.w : r0.z, par ? r1.y : r1.x, par ? r1.w : r1.z};
+    const float hs4[4] = {par ? a0.y : a0.x, par ? a0.w : a0.z, par ? a1.y : a1.x, par ? a1.w : a1.z};
+    const float T0 = rec.x, T1 = rec.y;
+    const bool dir[4] = {bc01.x != kBCNeumann, bc01.y != kBCNeumann, bc23.x != kBCNeumann, bc23.y != kBCNeumann};
+    const float from_left = __shfl_up_sync(0xffffffffu, v[7], 1);
+    const float from_right = __shfl_down_sync(0xffffffffu, v[0], 1);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const float dnk = __shfl_up_sync(0xffffffffu, v[k], 2);
+      const float upk = __shfl_down_sync(0xffffffffu, v[k], 2);
+      if ((k & 1) != par) continue;
+      const int i = c0 + k;
+      float diag = c.alpha * dv;
+      float off = 0.f;
+      if (i > 0 || ty[0] == 0) {
+        const float nbv = k > 0 ? v[k - 1] : (hh == 1 ? from_left : hl);
+        diag += T0;
+        off = fma_t(T0, nbv, off);
+      } else if (dir[0]) {
+        diag += T0 * 2.0f;
+      }
+      if (i < NB - 1 || ty[1] == 0) {
+        const float nbv = k < 7 ? v[k + 1] : (hh == 0 ? from_right : hr);
+        diag += T0;
+        off = fma_t(T0, nbv, off);
+      } else if (dir[1]) {
+        diag += T0 * 2.0f;
+      }
+      if (j > 0 || ty[2] == 0) {
+        const float nbv = j > 0 ? dnk : hs4[k >> 1];
+        diag += T1;
+        off = fma_t(T1, nbv, off);
+      } else if (dir[2]) {
+        diag += T1 * 2.0f;
+      }
+      if (j < NB - 1 || ty[3] == 0) {
+        const float nbv = j < NB - 1 ? upk : hs4[k >> 1];
+        diag += T1;
+        off = fma_t(T1, nbv, off);
+      } else if (dir[3]) {
+        diag += T1 * 2.0f;
+      }
+      v[k] = diag > 0.f ? fast_div(fma_t(rs[k >> 1] * dv, 1.0f, off), diag) : 0.f;
+    }
+    float4 *dst = reinterpret_cast<float4 *>(phi + cb + j * NB + c0);
+    dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+    dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // volume-weighted restriction onto the non-leaf blocks of a level:
 // coarse = avg(fine*vf_fine)/vf_coarse (src/SayakaMacIB.cpp:157-232 with
@@ -1498,8 +1617,11 @@ static void rbgs_go(const Topo &t, const Coef<T> &c, const BlockList &L, int col
 }
 
 // variant 10: CPT = 2 cells per thread (k_rbgs_ilp), cap 64; variants 11, 12:
-// one warp per 16x16 block in 2D FP32 (k_rbgs_warp16, caps 64 and 48),
-// elsewhere variant 3
+// one warp per 16x16 block in 2D FP32 (k_rbgs_warp16, caps 64 and 48);
+// variant 13: the same with every load issued before the first branch
+// (k_rbgs_warp16_flat, cap 64: at 48 registers it spills and loses,
+// 20.8 vs 16.9 us on the batch workload's first 64 problems); elsewhere
+// variant 3
 template <typename T, int ND, int MINB, int CPT>
 static void rbgs_ilp_go(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi, const T *rhs,
                         const int *guard, cudaStream_t s, bool pdl, dim3 grid, int threads) {
@@ -1514,13 +1636,16 @@ static void rbgs_nd(int variant, const Topo &t, const Coef<T> &c, const BlockLis
     case 10: rbgs_ilp_go<T, ND, 4, 2>(t, c, L, color, phi, rhs, guard, s, pdl, grid, threads); return;
     case 11:
     case 12:
+    case 13:
       if constexpr (ND == 2 && sizeof(T) == 4) {
         if (t.nb == 16) {
           const int g = std::min((L.n + 7) / 8, 152 * 64);
           if (variant == 11)
             launch_k(pdl, k_rbgs_warp16<4>, g, kThreads, 0, s, t, c, L, color, phi, rhs, guard);
-          else
+          else if (variant == 12 || !L.hx)
             launch_k(pdl, k_rbgs_warp16<5>, g, kThreads, 0, s, t, c, L, color, phi, rhs, guard);
+          else
+            launch_k(pdl, k_rbgs_warp16_flat<4>, g, kThreads, 0, s, t, c, L, color, phi, rhs, guard);
           return;
         }
       }

@@ -10,6 +10,7 @@
 #include <random>
 #include <vector>
 
+#include "dev_alloc.h"
 #include "cuda_check.h"
 #include "mac_learned.h"
 #include "mac_solver.h"
@@ -692,7 +693,7 @@ void MacGpu::learned_init(unsigned seed) {
   LearnedState &L = ls_;
   L.nb = tt_.nb;
   auto fa = [&](float *&p, size_t n) {
-    if (!p && cudaMalloc(&p, n * sizeof(float)) != cudaSuccess) {
+    if (!p && dev_malloc(&p, n * sizeof(float)) != cudaSuccess) {
       p = nullptr;
       fail("out of device memory (learned)");
     }
@@ -702,7 +703,7 @@ void MacGpu::learned_init(unsigned seed) {
   fa(L.m, kNParam);
   fa(L.v, kNParam);
   fa(L.loss, 1);
-  if (!L.w2bf && cudaMalloc(&L.w2bf, 9 * kC * kC * sizeof(uint16_t)) != cudaSuccess) fail("out of device memory");
+  if (!L.w2bf && dev_malloc(&L.w2bf, 9 * kC * kC * sizeof(uint16_t)) != cudaSuccess) fail("out of device memory");
   if (!err_.empty()) return;
   // He initialisation; the output layer starts at zero, so the untrained
   // correction is zero and the preconditioner is the plain V-cycle
@@ -750,9 +751,9 @@ void MacGpu::learned_reserve(int more) {
   const size_t nc = (size_t)ncell_;
   const size_t na = aux_len();
   float *f = nullptr, *a = nullptr;
-  if (cudaMalloc(&f, (size_t)cap * 3 * nc * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&a, (size_t)cap * na * sizeof(float)) != cudaSuccess) {
-    if (f) cudaFree(f);
+  if (dev_malloc(&f, (size_t)cap * 3 * nc * sizeof(float)) != cudaSuccess ||
+      dev_malloc(&a, (size_t)cap * na * sizeof(float)) != cudaSuccess) {
+    if (f) dev_free(f);
     fail("out of device memory (training set)");
     return;
   }
@@ -760,8 +761,8 @@ void MacGpu::learned_reserve(int more) {
     CK(cudaMemcpyAsync(f, L.feat, (size_t)L.nsamp * 3 * nc * sizeof(float), cudaMemcpyDeviceToDevice, stream_));
     CK(cudaMemcpyAsync(a, L.aux, (size_t)L.nsamp * na * sizeof(float), cudaMemcpyDeviceToDevice, stream_));
   }
-  if (L.feat) cudaFree(L.feat);
-  if (L.aux) cudaFree(L.aux);
+  if (L.feat) dev_free(L.feat);
+  if (L.aux) dev_free(L.aux);
   L.feat = f;
   L.aux = a;
   L.cap = cap;
@@ -770,8 +771,8 @@ void MacGpu::learned_reserve(int more) {
 void MacGpu::learned_free() {
   LearnedState &L = ls_;
   for (float *p : {L.w, L.g, L.m, L.v, L.loss, L.feat, L.aux, L.r1, L.scale})
-    if (p) cudaFree(p);
-  if (L.w2bf) cudaFree(L.w2bf);
+    if (p) dev_free(p);
+  if (L.w2bf) dev_free(L.w2bf);
   L = LearnedState{};
 }
 
@@ -840,7 +841,7 @@ int MacGpu::learned_collect(int max_iters, int max_samples) {
   record_ = nullptr;
   prm_ = save;
   if (rc != 0) {
-    for (double *p : rec) cudaFree(p);
+    for (double *p : rec) dev_free(p);
     return -1;
   }
   CKR_(cudaStreamSynchronize(stream_), -1);
@@ -848,10 +849,10 @@ int MacGpu::learned_collect(int max_iters, int max_samples) {
   const BlockList TL = tower_list(L);
   const long w = (long)TL.n * ncell_;
   float *e = nullptr, *r = nullptr, *z = nullptr, *r1 = nullptr;
-  cudaMalloc(&e, n * sizeof(float));
-  cudaMalloc(&r, n * sizeof(float));
-  cudaMalloc(&z, n * sizeof(float));
-  cudaMalloc(&r1, n * sizeof(float));
+  dev_malloc(&e, n * sizeof(float));
+  dev_malloc(&r, n * sizeof(float));
+  dev_malloc(&z, n * sizeof(float));
+  dev_malloc(&r1, n * sizeof(float));
   if (!e || !r || !z || !r1) {
     fail("out of device memory (collection)");
     return -1;
@@ -892,11 +893,11 @@ int MacGpu::learned_collect(int max_iters, int max_samples) {
     ls_.nsamp += cnt;
   }
   CKR_(cudaStreamSynchronize(stream_), -1);
-  for (double *p : rec) cudaFree(p);
-  cudaFree(e);
-  cudaFree(r);
-  cudaFree(z);
-  cudaFree(r1);
+  for (double *p : rec) dev_free(p);
+  dev_free(e);
+  dev_free(r);
+  dev_free(z);
+  dev_free(r1);
   // the collection solve overwrote the solution: leave a zero guess
   zero_sol();
   return err_.empty() ? (int)rec.size() : -1;
@@ -931,10 +932,10 @@ float MacGpu::learned_train(int epochs, float lr, int batch, unsigned seed) {
   const size_t nc = (size_t)ncell_;
   float *h1 = nullptr, *h2 = nullptr, *dy = nullptr;
   int *d_idx = nullptr;
-  cudaMalloc(&h1, (size_t)batch * kC * nc * sizeof(float));
-  cudaMalloc(&h2, (size_t)batch * kC * nc * sizeof(float));
-  cudaMalloc(&dy, (size_t)batch * nc * sizeof(float));
-  cudaMalloc(&d_idx, (size_t)ls_.nsamp * sizeof(int));
+  dev_malloc(&h1, (size_t)batch * kC * nc * sizeof(float));
+  dev_malloc(&h2, (size_t)batch * kC * nc * sizeof(float));
+  dev_malloc(&dy, (size_t)batch * nc * sizeof(float));
+  dev_malloc(&d_idx, (size_t)ls_.nsamp * sizeof(int));
   if (!h1 || !h2 || !dy || !d_idx) {
     fail("out of device memory (training)");
     return -1.f;
@@ -959,10 +960,10 @@ float MacGpu::learned_train(int epochs, float lr, int batch, unsigned seed) {
     last = (float)(tot / ls_.nsamp);
   }
   CKR_(cudaStreamSynchronize(stream_), -1.f);
-  cudaFree(h1);
-  cudaFree(h2);
-  cudaFree(dy);
-  cudaFree(d_idx);
+  dev_free(h1);
+  dev_free(h2);
+  dev_free(dy);
+  dev_free(d_idx);
   learned_sync_bf16();
   ls_.trained = true;
   return err_.empty() ? last : -1.f;
@@ -978,10 +979,10 @@ float MacGpu::learned_eval() {
   const size_t nc = (size_t)ncell_;
   float *h1 = nullptr, *h2 = nullptr, *dy = nullptr;
   int *d_idx = nullptr;
-  cudaMalloc(&h1, (size_t)batch * kC * nc * sizeof(float));
-  cudaMalloc(&h2, (size_t)batch * kC * nc * sizeof(float));
-  cudaMalloc(&dy, (size_t)batch * nc * sizeof(float));
-  cudaMalloc(&d_idx, (size_t)ls_.nsamp * sizeof(int));
+  dev_malloc(&h1, (size_t)batch * kC * nc * sizeof(float));
+  dev_malloc(&h2, (size_t)batch * kC * nc * sizeof(float));
+  dev_malloc(&dy, (size_t)batch * nc * sizeof(float));
+  dev_malloc(&d_idx, (size_t)ls_.nsamp * sizeof(int));
   if (!h1 || !h2 || !dy || !d_idx) {
     fail("out of device memory (evaluation)");
     return -1.f;
@@ -996,10 +997,10 @@ float MacGpu::learned_eval() {
   }
   CKR_(cudaMemsetAsync(ls_.g, 0, kNParam * sizeof(float), stream_), -1.f);
   CKR_(cudaStreamSynchronize(stream_), -1.f);
-  cudaFree(h1);
-  cudaFree(h2);
-  cudaFree(dy);
-  cudaFree(d_idx);
+  dev_free(h1);
+  dev_free(h2);
+  dev_free(dy);
+  dev_free(d_idx);
   return err_.empty() ? (float)(tot / ls_.nsamp) : -1.f;
 }
 
@@ -1018,10 +1019,10 @@ float MacGpu::learned_loss_grad(const float *feat, const float *aux, int n, floa
   ls_.nsamp = n;
   float *h1 = nullptr, *h2 = nullptr, *dy = nullptr;
   int *d_idx = nullptr;
-  cudaMalloc(&h1, (size_t)n * kC * nc * sizeof(float));
-  cudaMalloc(&h2, (size_t)n * kC * nc * sizeof(float));
-  cudaMalloc(&dy, (size_t)n * nc * sizeof(float));
-  cudaMalloc(&d_idx, (size_t)n * sizeof(int));
+  dev_malloc(&h1, (size_t)n * kC * nc * sizeof(float));
+  dev_malloc(&h2, (size_t)n * kC * nc * sizeof(float));
+  dev_malloc(&dy, (size_t)n * nc * sizeof(float));
+  dev_malloc(&d_idx, (size_t)n * sizeof(int));
   std::vector<int> idx(n);
   for (int k = 0; k < n; k++) idx[k] = k;
   cudaMemcpyAsync(d_idx, idx.data(), n * sizeof(int), cudaMemcpyHostToDevice, stream_);
@@ -1030,10 +1031,10 @@ float MacGpu::learned_loss_grad(const float *feat, const float *aux, int n, floa
   CKR_(cudaMemcpyAsync(grad, ls_.g, kNParam * sizeof(float), cudaMemcpyDeviceToHost, stream_), -1.f);
   CKR_(cudaStreamSynchronize(stream_), -1.f);
   CKR_(cudaMemsetAsync(ls_.g, 0, kNParam * sizeof(float), stream_), -1.f);
-  cudaFree(h1);
-  cudaFree(h2);
-  cudaFree(dy);
-  cudaFree(d_idx);
+  dev_free(h1);
+  dev_free(h2);
+  dev_free(dy);
+  dev_free(d_idx);
   // the explicit blocks replaced the training set
   (void)keep;
   ls_.nsamp = 0;
@@ -1046,9 +1047,9 @@ int MacGpu::learned_forward(const float *feat, int n, float *y) {
   set_smem_attrs();
   const size_t nc = (size_t)ncell_;
   float *df = nullptr, *dy = nullptr;
-  if (cudaMalloc(&df, (size_t)n * 3 * nc * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&dy, (size_t)n * nc * sizeof(float)) != cudaSuccess) {
-    if (df) cudaFree(df);
+  if (dev_malloc(&df, (size_t)n * 3 * nc * sizeof(float)) != cudaSuccess ||
+      dev_malloc(&dy, (size_t)n * nc * sizeof(float)) != cudaSuccess) {
+    if (df) dev_free(df);
     fail("out of device memory");
     return -1;
   }
@@ -1064,8 +1065,8 @@ int MacGpu::learned_forward(const float *feat, int n, float *y) {
   CKR_(cudaGetLastError(), -1);
   CKR_(cudaMemcpyAsync(y, dy, (size_t)n * nc * sizeof(float), cudaMemcpyDeviceToHost, stream_), -1);
   CKR_(cudaStreamSynchronize(stream_), -1);
-  cudaFree(df);
-  cudaFree(dy);
+  dev_free(df);
+  dev_free(dy);
   if (nn_tc_error(true) > 0) {
     fail("learned correction: a tensor-core wait timed out");
     return -1;
@@ -1079,7 +1080,7 @@ void MacGpu::learned_prepare() {
   set_smem_attrs();
   if (ls_.r1) return;
   const size_t n = (size_t)tt_.num_blocks * ncell_;
-  if (cudaMalloc(&ls_.r1, n * sizeof(float)) != cudaSuccess) {
+  if (dev_malloc(&ls_.r1, n * sizeof(float)) != cudaSuccess) {
     ls_.r1 = nullptr;
     fail("out of device memory (learned)");
     return;

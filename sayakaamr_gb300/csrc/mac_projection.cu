@@ -10,6 +10,7 @@
 //      u_dir += dt * mg_flux_level(finest, dir, p)
 //    on the finest tower's blocks (TreeData::AddEqual over the valid faces),
 //    with p the solver's solution, which stays on the device.
+#include "dev_alloc.h"
 #include "cuda_check.h"
 #include "mac_solver.h"
 #include "mac_stencil.cuh"
@@ -69,7 +70,7 @@ double *MacGpu::face_scratch(int k) {
   if ((int)d_face_.size() < 7) d_face_.resize(7, nullptr);
   if (!d_face_[k]) {
     const size_t nf = (size_t)tt_.num_blocks * nfb_;
-    if (cudaMalloc(&d_face_[k], nf * sizeof(double)) != cudaSuccess) {
+    if (dev_malloc(&d_face_[k], nf * sizeof(double)) != cudaSuccess) {
       d_face_[k] = nullptr;
       fail("out of device memory (face fields)");
     }

@@ -1,6 +1,9 @@
 // Host orchestration of the GPU MAC solver: device pools, block lists,
 // coefficient setup, vector kernels / reductions, the V-cycle preconditioner
 // and the BiCGSTAB driver.
+#include <mutex>
+
+#include "dev_alloc.h"
 #include "mac_solver.h"
 
 #include <algorithm>
@@ -14,6 +17,38 @@
 #include "tree.h"
 
 namespace sayaka_gb300 {
+
+// the pool of each device keeps what is freed (release threshold raised once
+// per device and process)
+static void pool_keep_freed() {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    unsigned long long keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done[dev] = true;
+}
+
+cudaError_t dev_malloc_bytes(void **p, size_t bytes) {
+  pool_keep_freed();
+  const cudaError_t e = cudaMallocAsync(p, bytes, 0);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(0);
+}
+
+cudaError_t dev_free(void *p) {
+  if (!p) return cudaSuccess;
+  const cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return e;
+  return cudaFreeAsync(p, 0);
+}
+
 
 #include "cuda_check.h"
 
@@ -124,9 +159,45 @@ __global__ void __launch_bounds__(kThreads) k_reduce(BlockList L, int ncell, con
 template <typename T>
 T *dalloc(size_t n) {
   T *p = nullptr;
-  if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
+  if (dev_malloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
   cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T));
+  cudaStreamSynchronize(0);  // zeroed before any stream of the solver touches it
   return p;
+}
+
+// halo descriptors of a tower list (see kHX), one thread per entry
+__global__ void k_make_hx(int n, int nd, const int *__restrict__ blocks, const uint16_t *__restrict__ fts,
+                          const int *__restrict__ neighbor, const int *__restrict__ parent,
+                          const int *__restrict__ which_child, const int *__restrict__ child,
+                          const int *__restrict__ fc_neigh, int *__restrict__ hx) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const int b = blocks[p];
+    const unsigned ft = fts[p];
+    int e[kHX];
+    for (int k = 0; k < kHX; k++) e[k] = -1;
+    e[kHXInfo] = (int)(ft | ((unsigned)which_child[b] << 16));
+    e[kHXBlock] = b;
+    if (parent[b] >= 0) e[kHXPar + 6] = parent[b] * 8 + which_child[b];
+    for (int f = 0; f < 2 * nd; f++) {
+      const int ty = (ft >> (2 * f)) & 3, d = f >> 1, s = f & 1;
+      if (ty == 0) {
+        const int nbr = neighbor[b * 6 + f];
+        e[f] = nbr;
+        if (parent[nbr] >= 0) e[kHXPar + f] = parent[nbr] * 8 + which_child[nbr];
+      }
+      if (ty == 2) e[f] = fc_neigh[b * 6 + f];
+      if (ty != 3) continue;
+      const int N = neighbor[b * 6 + f];
+      for (int k = 0; k < (1 << (nd - 1)); k++) {
+        int cidx = (1 - s) << d, j = 0;
+        for (int q = 0; q < nd; q++)
+          if (q != d) cidx |= ((k >> j++) & 1) << q;
+        e[kHXKids + f * 4 + k] = child[N * 8 + cidx];
+      }
+    }
+    int *out = hx + (long)p * kHX;
+    for (int k = 0; k < kHX; k++) out[k] = e[k];
+  }
 }
 
 void tree_from_tables(const TreeTables &tt, AmrTree &t) {
@@ -203,34 +274,25 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
   tree_from_tables(tt, t);
   std::vector<Tower> tw = build_towers(t);
   towers_.resize(tt.max_level + 1);
-  // halo descriptors of a tower list (see kHX)
-  auto make_hx = [&](const std::vector<int> &blk, const std::vector<uint16_t> &fts) {
-    std::vector<int> hx(blk.size() * kHX, -1);
-    for (size_t p = 0; p < blk.size(); p++) {
-      const int b = blk[p];
-      int *e = &hx[p * kHX];
-      e[kHXInfo] = (int)((unsigned)fts[p] | ((unsigned)tt.which_child[b] << 16));
-      e[kHXBlock] = b;
-      if (tt.parent[b] >= 0) e[kHXPar + 6] = tt.parent[b] * 8 + tt.which_child[b];
-      for (int f = 0; f < 2 * nd; f++) {
-        const int ty = (fts[p] >> (2 * f)) & 3, d = f >> 1, s = f & 1;
-        if (ty == 0) {
-          const int n = tt.neighbor[b * 6 + f];
-          e[f] = n;
-          if (tt.parent[n] >= 0) e[kHXPar + f] = tt.parent[n] * 8 + tt.which_child[n];
-        }
-        if (ty == 2) e[f] = fc_neigh_[b * 6 + f];
-        if (ty != 3) continue;
-        const int N = tt.neighbor[b * 6 + f];
-        for (int k = 0; k < (1 << (nd - 1)); k++) {
-          int cidx = (1 - s) << d, j = 0;
-          for (int q = 0; q < nd; q++)
-            if (q != d) cidx |= ((k >> j++) & 1) << q;
-          e[kHXKids + f * 4 + k] = tt.child[N * 8 + cidx];
-        }
-      }
-    }
-    return hx;
+  // device tables (the halo descriptors below are built from them)
+  d_neighbor_ = dalloc<int>((size_t)nbk * 6);
+  d_child_ = dalloc<int>((size_t)nbk * 8);
+  d_parent_ = dalloc<int>(nbk);
+  d_wc_ = dalloc<int>(nbk);
+  d_fc_neigh_ = dalloc<int>((size_t)nbk * 6);
+  d_bc_type_ = dalloc<int>((size_t)nbk * 6);
+  d_geom_ = dalloc<double>((size_t)nbk * 8);
+  CK(cudaMemcpy(d_neighbor_, tt.neighbor.data(), (size_t)nbk * 6 * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_child_, tt.child.data(), (size_t)nbk * 8 * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_parent_, tt.parent.data(), (size_t)nbk * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_wc_, tt.which_child.data(), (size_t)nbk * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_fc_neigh_, fc_neigh_.data(), (size_t)nbk * 6 * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_geom_, geom_.data(), (size_t)nbk * 8 * sizeof(double), cudaMemcpyHostToDevice));
+  // halo descriptors of a tower list (see kHX), built on the device
+  auto make_hx = [&](const int *blk, const uint16_t *fts, int n, int *hx) {
+    if (n <= 0) return;
+    k_make_hx<<<std::min((n + 255) / 256, 152 * 8), 256, 0, stream_>>>(n, nd, blk, fts, d_neighbor_, d_parent_, d_wc_,
+                                                                      d_child_, d_fc_neigh_, hx);
   };
   for (int L = 1; L <= tt.max_level; L++) {
     const Tower &src = tw[L];
@@ -252,8 +314,7 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
     if (n) {
       CK(cudaMemcpy(dt.all.blocks, src.blocks.data(), n * sizeof(int), cudaMemcpyHostToDevice));
       CK(cudaMemcpy(dt.all.ftypes, ft.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice));
-      const std::vector<int> hx = make_hx(src.blocks, ft);
-      CK(cudaMemcpy(dt.all.hx, hx.data(), hx.size() * sizeof(int), cudaMemcpyHostToDevice));
+      make_hx(dt.all.blocks, dt.all.ftypes, n, dt.all.hx);
     }
     // parity-grouped copy of the sublevels the V-cycle smooths (L down to
     // the first empty sublevel, as the per-sublevel loop does)
@@ -277,8 +338,7 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
     if (!pb.empty()) {
       CK(cudaMemcpy(dt.par.blocks, pb.data(), pb.size() * sizeof(int), cudaMemcpyHostToDevice));
       CK(cudaMemcpy(dt.par.ftypes, pf.data(), pf.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
-      const std::vector<int> hx = make_hx(pb, pf);
-      CK(cudaMemcpy(dt.par.hx, hx.data(), hx.size() * sizeof(int), cudaMemcpyHostToDevice));
+      make_hx(dt.par.blocks, dt.par.ftypes, (int)pb.size(), dt.par.hx);
     }
   }
   // Independent problems in one tree (a forest: no neighbour, parent or child
@@ -333,8 +393,7 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
     tlc_.hx = dalloc<int>((size_t)n * kHX);
     CK(cudaMemcpy(tlc_.blocks, pb.data(), n * sizeof(int), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(tlc_.ftypes, pf.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice));
-    const std::vector<int> hx = make_hx(pb, pf);
-    CK(cudaMemcpy(tlc_.hx, hx.data(), hx.size() * sizeof(int), cudaMemcpyHostToDevice));
+    make_hx(tlc_.blocks, tlc_.ftypes, n, tlc_.hx);
     std::vector<int> ccomp, cbeg, cend, c0(ncomp_, 0), cn(ncomp_, 0);
     const long nc = ncell_;
     for (int p = 0; p < n;) {
@@ -362,7 +421,7 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
     d_stc_ = dalloc<FState>(ncomp_);
     d_cpart_ = dalloc<double>((size_t)nchunks_ * 2);
     d_ccnt_ = dalloc<unsigned>(ncomp_);
-    CK(cudaMemset(d_ccnt_, 0, ncomp_ * sizeof(unsigned)));
+    CK(cudaMemsetAsync(d_ccnt_, 0, ncomp_ * sizeof(unsigned), stream_));
     CK(cudaMallocHost(&h_stc_, ncomp_ * sizeof(FState)));
   }
   levels_.resize(tt.max_level + 1);
@@ -391,20 +450,6 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
     }
   }
 
-  // device tables
-  d_neighbor_ = dalloc<int>((size_t)nbk * 6);
-  d_child_ = dalloc<int>((size_t)nbk * 8);
-  d_parent_ = dalloc<int>(nbk);
-  d_wc_ = dalloc<int>(nbk);
-  d_fc_neigh_ = dalloc<int>((size_t)nbk * 6);
-  d_bc_type_ = dalloc<int>((size_t)nbk * 6);
-  d_geom_ = dalloc<double>((size_t)nbk * 8);
-  CK(cudaMemcpy(d_neighbor_, tt.neighbor.data(), (size_t)nbk * 6 * sizeof(int), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d_child_, tt.child.data(), (size_t)nbk * 8 * sizeof(int), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d_parent_, tt.parent.data(), (size_t)nbk * sizeof(int), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d_wc_, tt.which_child.data(), (size_t)nbk * sizeof(int), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d_fc_neigh_, fc_neigh_.data(), (size_t)nbk * 6 * sizeof(int), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d_geom_, geom_.data(), (size_t)nbk * 8 * sizeof(double), cudaMemcpyHostToDevice));
   for (int d = 0; d < nd; d++) {
     d_bcoef_[d] = dalloc<double>((size_t)nbk * nfb_);
     d_afrac_[d] = dalloc<double>((size_t)nbk * nfb_);
@@ -453,7 +498,7 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
 
 MacGpu::~MacGpu() {
   auto fr = [](void *p) {
-    if (p) cudaFree(p);
+    if (p) dev_free(p);
   };
   for (auto &t : towers_) {
     fr(t.all.blocks);
@@ -983,25 +1028,25 @@ void MacGpu::flux(int dir, const double *phi, double *out) {
   const size_t nf = (size_t)tt_.num_blocks * nfb_;
   CK(cudaMemcpyAsync(vec_[kP], phi, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
   double *fl = nullptr;
-  CK(cudaMalloc(&fl, nf * sizeof(double)));
+  CK(dev_malloc(&fl, nf * sizeof(double)));
   CK(cudaMemsetAsync(fl, 0, nf * sizeof(double), stream_));
   launch_flux(topo_, c64_, tower_list(finest_), dir, vec_[kP], fl, stream_);
   CK(cudaMemcpyAsync(out, fl, nf * sizeof(double), cudaMemcpyDeviceToHost, stream_));
   CK(cudaStreamSynchronize(stream_));
-  cudaFree(fl);
+  dev_free(fl);
 }
 void MacGpu::fix_bc(const double *phig, int ng, double *rhs) {
   const int nd = tt_.ndim, G = tt_.nb + 2 * ng;
   const size_t gsz = (size_t)tt_.num_blocks * (nd == 3 ? (size_t)G * G * G : (size_t)G * G);
   const size_t n = (size_t)tt_.num_blocks * ncell_;
   double *dg = nullptr;
-  CK(cudaMalloc(&dg, gsz * sizeof(double)));
+  CK(dev_malloc(&dg, gsz * sizeof(double)));
   CK(cudaMemcpyAsync(dg, phig, gsz * sizeof(double), cudaMemcpyHostToDevice, stream_));
   CK(cudaMemcpyAsync(vec_[kTMP], rhs, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
   launch_fix_bc(topo_, c64_, tower_list(finest_), dg, ng, vec_[kTMP], stream_);
   CK(cudaMemcpyAsync(rhs, vec_[kTMP], n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
   CK(cudaStreamSynchronize(stream_));
-  cudaFree(dg);
+  dev_free(dg);
 }
 
 }  // namespace sayaka_gb300

@@ -37,12 +37,13 @@ struct SolverParams {
   int smooth_variant = -1;    // device smoother launch bounds: -1 autotune at prepare, else variant index
   int learned = 0;            // device path, FP32 V-cycle: apply the trained block correction
   int fuse_prolong = 1;       // device path: prolongation fused with the first red sweep of its level
-  int vcycle_out = 0;         // FP32 V-cycle output to the BiCGSTAB kernels: 0 = read in place (FP64 operator),
-                              // 1 = read in place with the operator in double-float, 2 = widened once into FP64
-                              // vectors (FP64 operator)
+  int vcycle_out = 0;         // FP32 V-cycle output to the BiCGSTAB kernels: 0 = read in place in 2D and on 3D
+                              // towers up to 2M cells, else widened once into FP64 vectors; 1 = in place with the
+                              // operator in double-float; 2 = always widened; 3 = always in place
   int prolong_form = 1;       // that fused launch: 1 = one warp per block (2D FP32 16x16 blocks), 0 = one CTA
                               // per block with a shared-memory tile (same values)
-  int bottom_half = 0;        // device path, FP32 V-cycle, bottom above level 1: 1 = FP16 inverse with row scales
+  int bottom_half = 0;        // device path, FP32 V-cycle: 1 = FP16 copy of the bottom inverse with row scales,
+                              // 0 = FP32 copy
   int bottom_level = 0;       // device path: level of the dense bottom solve; 0 = the coarsest level whose
                               // tower is one uniform level of at most kBottomMaxCells cells per component
   int sublevel_order = 1;     // device V-cycle smoothing order over a tower's sublevels: 0 = finest to

@@ -24,6 +24,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "dev_alloc.h"
 #include "cuda_check.h"
 #include "mac_solver.h"
 #include "mac_stencil.cuh"
@@ -266,7 +267,7 @@ int MacGpu::init_solution_from(const MacGpu &old, std::string *why) {
   const size_t n = (size_t)tt_.num_blocks * ncell_;
   int *d = nullptr;
   const size_t ints = (size_t)nmap * 4 + kids.size();
-  CKR_(cudaMalloc(&d, std::max<size_t>(ints, 1) * sizeof(int)), 2);
+  CKR_(dev_malloc(&d, std::max<size_t>(ints, 1) * sizeof(int)), 2);
   std::vector<int> pack;
   pack.reserve(ints);
   for (auto *v : {&blk, &kind, &src, &wc, &kids}) pack.insert(pack.end(), v->begin(), v->end());
@@ -281,7 +282,7 @@ int MacGpu::init_solution_from(const MacGpu &old, std::string *why) {
         vec_[kSOL]);
   CKR_(cudaGetLastError(), 2);
   CKR_(cudaStreamSynchronize(stream_), 2);
-  cudaFree(d);
+  dev_free(d);
   return 0;
 }
 
@@ -343,9 +344,9 @@ int MacGpu::init_new_block_data(const MacGpu &old, const double *bc_val, std::st
   const size_t nold = (size_t)old.tt_.num_blocks * ncell_, n = (size_t)tt_.num_blocks * ncell_;
   int *d = nullptr;
   double *tmp = nullptr;
-  CKR_(cudaMalloc(&d, std::max<size_t>(pack.size(), 1) * sizeof(int)), 2);
-  if (cudaMalloc(&tmp, std::max<size_t>(nold, 1) * sizeof(double)) != cudaSuccess) {
-    cudaFree(d);
+  CKR_(dev_malloc(&d, std::max<size_t>(pack.size(), 1) * sizeof(int)), 2);
+  if (dev_malloc(&tmp, std::max<size_t>(nold, 1) * sizeof(double)) != cudaSuccess) {
+    dev_free(d);
     *why = "init_new_block_data: out of device memory";
     return 2;
   }
@@ -372,8 +373,8 @@ int MacGpu::init_new_block_data(const MacGpu &old, const double *bc_val, std::st
   }
   CKR_(cudaGetLastError(), 2);
   CKR_(cudaStreamSynchronize(stream_), 2);
-  cudaFree(tmp);
-  cudaFree(d);
+  dev_free(tmp);
+  dev_free(d);
   return 0;
 }
 

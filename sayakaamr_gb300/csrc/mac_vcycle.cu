@@ -17,6 +17,7 @@
 // guarantees that all CTAs are resident, so the bound is only a safety net.
 #include <vector>
 
+#include "dev_alloc.h"
 #include "cuda_check.h"
 #include "mac_solver.h"
 #include "launch.cuh"
@@ -155,15 +156,15 @@ void MacGpu::build_vcycle_program() {
     }
   }
   push(kPhaseOut, 0, tower_list(L));
-  if (d_phases_) cudaFree(d_phases_);
+  if (d_phases_) dev_free(d_phases_);
   d_phases_ = nullptr;
   n_phases_ = (int)v.size();
   h_phases_ = v;
-  CK(cudaMalloc(&d_phases_, v.size() * sizeof(VPhase)));
+  CK(dev_malloc(&d_phases_, v.size() * sizeof(VPhase)));
   CK(cudaMemcpy(d_phases_, v.data(), v.size() * sizeof(VPhase), cudaMemcpyHostToDevice));
   if (!d_bar_) {
-    CK(cudaMalloc(&d_bar_, 4 * sizeof(unsigned)));
-    CK(cudaMemset(d_bar_, 0, 4 * sizeof(unsigned)));
+    CK(dev_malloc(&d_bar_, 4 * sizeof(unsigned)));
+    CK(cudaMemsetAsync(d_bar_, 0, 4 * sizeof(unsigned), stream_));
   }
   program_npost_ = prm_.n_post;
   program_order_ = prm_.sublevel_order;

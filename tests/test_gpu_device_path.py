@@ -122,7 +122,7 @@ def test_smoother_variants_are_bit_identical(name, precision):
         out.append((info["iterations"], S.get_sol_compact()))
         if var == -1:
             v, us = S.tuned_smoother(precision)
-            assert 0 <= v < 13 and all(u > 0 for u in us), (v, us)
+            assert 0 <= v < 14 and all(u > 0 for u in us), (v, us)
     for k in range(1, len(out)):
         assert out[0][0] == out[k][0], k
         assert np.array_equal(out[0][1], out[k][1]), k

@@ -87,8 +87,9 @@ def test_device_solve_bit_identical_with_records(name, precision, smoother):
 @pytest.mark.parametrize("name", ["config2", "config4"])
 def test_warp_per_block_sweep_is_bit_identical(name):
     """the FP32 sweep of 16x16 blocks with one warp per block (registers,
-    shuffles, 16-byte loads; autotuner variant 11) against the one-thread-
-    per-cell sweep (variant 3): identical iterations and solutions, on a
+    shuffles, 16-byte loads; autotuner variants 11, 12, and 13 with every
+    load issued before the first branch) against the one-thread-per-cell
+    sweep (variant 3): identical iterations and solutions, on a
     workload with constant-coefficient blocks (its fast path) and cut or
     coarse/fine blocks (its cell-by-cell path), and on a small forest solved
     with one state per problem"""
@@ -96,14 +97,14 @@ def test_warp_per_block_sweep_is_bit_identical(name):
     p = workloads.config4(n_problems=6) if name == "config4" else workloads.config2()
     S = workloads.make_solver(p)
     res = []
-    for var in (3, 11, 12):
+    for var in (3, 11, 12, 13):
         S.set_zero_sol()
         S.set_params(tol_rel=1e-10, tol_abs=0.0, use_mg_precond=1, max_iter=500, precision=1, bottom=1,
                      smooth_variant=var)
         info = S.cg_solve()
         assert info["status"] == 0, info
         res.append((info["iterations"], S.get_sol_compact()))
-    for k in (1, 2):
+    for k in (1, 2, 3):
         assert res[0][0] == res[k][0], k
         assert np.array_equal(res[0][1], res[k][1]), k
     assert S.uniform_blocks() > 0
