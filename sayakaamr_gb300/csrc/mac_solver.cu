@@ -201,7 +201,7 @@ __global__ void k_make_hx(int n, int nd, const int *__restrict__ blocks, const u
 }
 
 void tree_from_tables(const TreeTables &tt, AmrTree &t) {
-  t.init(tt.ndim, tt.nb, tt.min_level, tt.max_level, std::max(tt.num_blocks, 1));
+  t.init(tt.ndim, tt.nb, tt.min_level, tt.max_level, std::max(tt.num_blocks, 1), false);
   t.num_blocks = tt.num_blocks;
   for (int b = 0; b < tt.num_blocks; b++) {
     TreeNode &n = t.nodes[b];

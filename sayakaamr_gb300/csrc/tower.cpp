@@ -1,5 +1,7 @@
 #include "tower.h"
 
+#include <thread>
+
 namespace sayaka_gb300 {
 
 static Tower build_one(const AmrTree &t, int L) {
@@ -9,6 +11,10 @@ static Tower build_one(const AmrTree &t, int L) {
   tw.end.assign(L + 1, 0);
   if (L >= (int)t.levels.size() || t.levels[L].empty()) return tw;
   const int nf = t.num_face(), nc = t.num_child(), half = t.nb / 2;
+  size_t cap = 0;
+  for (int l = L; l >= 1; l--) cap += t.levels[l].size();
+  tw.blocks.reserve(cap);
+  tw.regs.reserve(cap * kMaxFace);
   for (int l = L; l >= 1; l--) {
     tw.begin[l] = (int)tw.blocks.size();
     for (int b : t.levels[l]) {
@@ -51,9 +57,12 @@ static Tower build_one(const AmrTree &t, int L) {
   return tw;
 }
 
+// the towers are independent: one host thread per level
 std::vector<Tower> build_towers(const AmrTree &t) {
   std::vector<Tower> v(t.max_level + 1);
-  for (int L = 1; L <= t.max_level; L++) v[L] = build_one(t, L);
+  std::vector<std::thread> th;
+  for (int L = 1; L <= t.max_level; L++) th.emplace_back([&v, &t, L] { v[L] = build_one(t, L); });
+  for (auto &x : th) x.join();
   return v;
 }
 

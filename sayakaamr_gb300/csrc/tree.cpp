@@ -50,7 +50,7 @@ int AmrTree::surr_index(int ii, int jj, int kk) const {
   return s;
 }
 
-void AmrTree::init(int ndim_, int nb_, int min_level_, int max_level_, int capacity_) {
+void AmrTree::init(int ndim_, int nb_, int min_level_, int max_level_, int capacity_, bool surroundings) {
   ndim = ndim_;
   nb = nb_;
   min_level = min_level_;
@@ -62,7 +62,7 @@ void AmrTree::init(int ndim_, int nb_, int min_level_, int max_level_, int capac
   refine_flag.assign(capacity, 0);
   coarsen_flag.assign(capacity, 0);
   new_child_flag.assign(capacity, 0);
-  surr.assign(capacity, SurrBlocks());
+  surr.assign(surroundings ? capacity : 0, SurrBlocks());
   for (auto &s : surr) s.reset();
   levels.assign(max_level + 1, std::vector<int>());
 }

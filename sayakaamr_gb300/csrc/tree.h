@@ -79,7 +79,9 @@ class AmrTree {
   int num_child() const { return 1 << ndim; }
 
   // allocate `capacity` block slots (src/SayakaTree.cpp:34-91)
-  void init(int ndim, int nb, int min_level, int max_level, int capacity);
+  // (surroundings = false: without the 3x3x3 tables, for a tree that only
+  // serves as the source of towers)
+  void init(int ndim, int nb, int min_level, int max_level, int capacity, bool surroundings = true);
   // root blocks on a uniform grid (src/SayakaTree.cpp:93-201)
   void init_uniform_root(const int ndiv[3], const double lo[3], const double hi[3],
                          const int bc_type[6], const bool periodic[6]);
