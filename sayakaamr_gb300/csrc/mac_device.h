@@ -28,6 +28,7 @@ struct Topo {
   const int *which_child;// [nblocks]
   const int *fc_neigh;   // [nblocks*6] coarse leaf behind a -1 neighbour
   const int *bc_type;    // [nblocks*6] BCMath of physical faces, -1 otherwise
+  int *err = nullptr;    // the solver's error word (a bounded wait that ran out sets it)
 };
 
 template <typename T>
@@ -175,7 +176,8 @@ void launch_smooth(const Topo &t, const Coef<T> &c, const BlockList &L, int colo
 constexpr int kRbgsVariants = 14;
 // error word of the bulk-copy smoother variant (an mbarrier wait timed out);
 // read (and cleared) by the host after a solve
-int rbgs_bulk_error(bool clear);
+// the solver's error word (Topo::err) after its stream is idle; clear: reset it
+int rbgs_bulk_error(int *err, cudaStream_t s, bool clear);
 template <typename T>
 void launch_rbgs(const Topo &t, const Coef<T> &c, const BlockList &L, int color, T *phi,
                    const T *rhs, const int *guard, cudaStream_t s, bool pdl = false,

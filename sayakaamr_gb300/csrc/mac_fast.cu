@@ -1014,6 +1014,8 @@ void MacGpu::tune_smoother(int precision) {
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
     rbgs_us_[pi][v] = ms * 1e3f / reps;
+    // a variant whose bounded waits ran out is not a candidate
+    if (rbgs_bulk_error(topo_.err, stream_, true) != 0) rbgs_us_[pi][v] = 1e30f;
     if (rbgs_us_[pi][v] < best) {
       best = rbgs_us_[pi][v];
       bi = v;
@@ -1923,7 +1925,7 @@ int MacGpu::solve_state(SolveInfo *info) {
       return -1;
     }
   }
-  if (rbgs_bulk_error(true) > 0) {
+  if (rbgs_bulk_error(topo_.err, stream_, true) > 0) {
     fail("bulk-copy smoother: an mbarrier wait timed out");
     return -1;
   }
@@ -2102,7 +2104,7 @@ int MacGpu::device_kernel_compact(int which, int L, int variant, const double *i
     CKR_(cudaMemcpyAsync(out, vec_[kCORR], n * sizeof(double), cudaMemcpyDeviceToHost, stream_), 2);
   }
   CKR_(cudaStreamSynchronize(stream_), 2);
-  if (rbgs_bulk_error(true) > 0) {
+  if (rbgs_bulk_error(topo_.err, stream_, true) > 0) {
     fail("bulk-copy smoother: an mbarrier wait timed out");
     return 2;
   }

@@ -1061,9 +1061,8 @@ __global__ void __launch_bounds__(kThreads) k_copy_blocks(BlockList L, int ncell
 // compact layout both are contiguous per block.  The boundary contributions
 // are gathered while the copies are in flight; the update then reads tile
 // and coefficients from shared memory.  The wait is bounded: a CTA that
-// times out raises g_rbgs_err, waits (bounded) for its own copies and leaves
-// the block unchanged.
-__device__ int g_rbgs_err;
+// times out raises the solver's error word (Topo::err), waits (bounded) for
+// its own copies and leaves the block unchanged.
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -1171,7 +1170,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_rbgs_bulk(Topo t, Coef<T> c, Bl
       // bounded drain time out too, copies may still land in shared memory
       // the CTA released, so nothing the device computes after the flag is
       // set is trusted (the host reports the failure after the solve)
-      atomicExch(&g_rbgs_err, 1);
+      if (t.err) atomicExch(t.err, 1);
       mbar_wait(mbar, 0, kWait);  // let the copies into this CTA's shared memory land before it exits
     }
     return;
@@ -1323,7 +1322,7 @@ __global__ void __launch_bounds__(kStreamThreads, 1) k_rbgs_stream(Topo t, Coef<
         // bounded drain below also time out, copies may still be landing in
         // shared memory this CTA released, so nothing the device computes
         // after the flag is set is trusted (the host reports the failure)
-        atomicExch(&g_rbgs_err, 1);
+        if (t.err) atomicExch(t.err, 1);
         // let this CTA's copies land before it exits
         mbar_wait(&mbar[j], phase[j] ^ 1u, kWait);
         if (p + (int)gridDim.x < L.n) mbar_wait(&mbar[j ^ 1], phase[j ^ 1], kWait);
@@ -1420,12 +1419,14 @@ static void rbgs_bulk_go(const Topo &t, const Coef<T> &c, const BlockList &L, in
   launch_k(pdl, k_rbgs_bulk<T, ND>, L.n, threads, smem, s, t, c, L, color, phi, rhs, guard);
 }
 
-int rbgs_bulk_error(bool clear) {
+int rbgs_bulk_error(int *err, cudaStream_t s, bool clear) {
+  if (!err) return 0;
   int v = 0;
-  if (cudaMemcpyFromSymbol(&v, g_rbgs_err, sizeof(int)) != cudaSuccess) return -1;
+  if (cudaMemcpyAsync(&v, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return -1;
   if (clear && v) {
-    const int z = 0;
-    cudaMemcpyToSymbol(g_rbgs_err, &z, sizeof(int));
+    if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) return -1;
   }
   return v;
 }

@@ -281,6 +281,7 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
   d_wc_ = dalloc<int>(nbk);
   d_fc_neigh_ = dalloc<int>((size_t)nbk * 6);
   d_bc_type_ = dalloc<int>((size_t)nbk * 6);
+  d_err_ = dalloc<int>(1);
   d_geom_ = dalloc<double>((size_t)nbk * 8);
   CK(cudaMemcpy(d_neighbor_, tt.neighbor.data(), (size_t)nbk * 6 * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(d_child_, tt.child.data(), (size_t)nbk * 8 * sizeof(int), cudaMemcpyHostToDevice));
@@ -479,6 +480,7 @@ MacGpu::MacGpu(const TreeTables &tt) : tt_(tt) {
   topo_.which_child = d_wc_;
   topo_.fc_neigh = d_fc_neigh_;
   topo_.bc_type = d_bc_type_;
+  topo_.err = d_err_;
 
   c64_.geom = d_geom_;
   for (int d = 0; d < 3; d++) {
@@ -522,6 +524,7 @@ MacGpu::~MacGpu() {
   fr(d_wc_);
   fr(d_fc_neigh_);
   fr(d_bc_type_);
+  fr(d_err_);
   fr(d_geom_);
   for (int d = 0; d < 3; d++) {
     fr(d_bcoef_[d]);

@@ -305,6 +305,7 @@ class MacGpu {
   // device tables
   int *d_neighbor_ = nullptr, *d_child_ = nullptr, *d_parent_ = nullptr, *d_wc_ = nullptr;
   int *d_fc_neigh_ = nullptr, *d_bc_type_ = nullptr;
+  int *d_err_ = nullptr;  // error word of the bounded waits (Topo::err)
   double *d_geom_ = nullptr;
   double *d_bcoef_[3] = {nullptr, nullptr, nullptr}, *d_afrac_[3] = {nullptr, nullptr, nullptr};
   double *d_tff_[3] = {nullptr, nullptr, nullptr}, *d_vf_ = nullptr;
