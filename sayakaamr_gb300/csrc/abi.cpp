@@ -572,12 +572,29 @@ int sayaka_mac_fix_bc(sayaka_mac *h, const double *phi, int32_t pn, int32_t pg, 
   });
 }
 
+// the device address of `p` when it is pinned (page-locked) host memory the
+// GPU can read and write directly, else null (pageable memory is never
+// touched by a kernel: it goes through the staging copy)
+static const void *pinned_device_ptr(const void *p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 static int set_field(sayaka_mac *h, const double *data, int32_t ncomp, int32_t ngrow, int32_t comp, bool rhs) {
   return guarded(h, [&] {
     MacGpu &g = *h->gpu;
     if (!data) return (int)SAYAKA_BAD_INPUT;
     Layout L(g.ndim(), g.nb(), ncomp, ngrow, comp, -1);
     if (!L.ok()) return (int)SAYAKA_BAD_INPUT;
+    // pinned TreeData: gathered by the GPU straight from host memory
+    if (const void *dp = pinned_device_ptr(data)) {
+      if (g.set_field_td(static_cast<const double *>(dp), ncomp, ngrow, comp, rhs) != 0) return status_of(h);
+      return (int)SAYAKA_OK;
+    }
     double *st = staging(h, (size_t)g.num_blocks() * g.ncell());
     if (!st) return (int)SAYAKA_CUDA_ERROR;
     pack(L, g.num_blocks(), data, st);
@@ -608,6 +625,11 @@ int sayaka_mac_get_sol(sayaka_mac *h, double *data, int32_t ncomp, int32_t ngrow
     if (!data) return (int)SAYAKA_BAD_INPUT;
     Layout L(g.ndim(), g.nb(), ncomp, ngrow, comp, -1);
     if (!L.ok()) return (int)SAYAKA_BAD_INPUT;
+    // pinned TreeData: scattered by the GPU straight into host memory
+    if (const void *dp = pinned_device_ptr(data)) {
+      if (g.get_sol_td(static_cast<double *>(const_cast<void *>(dp)), ncomp, ngrow, comp) != 0) return status_of(h);
+      return (int)SAYAKA_OK;
+    }
     double *st = staging(h, (size_t)g.num_blocks() * g.ncell());
     if (!st) return (int)SAYAKA_CUDA_ERROR;
     g.get_sol(st);

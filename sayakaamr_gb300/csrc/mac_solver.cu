@@ -200,6 +200,32 @@ __global__ void k_make_hx(int n, int nd, const int *__restrict__ blocks, const u
   }
 }
 
+// A TreeData-layout field (per block `ncomp` components of G0 x G1 x G2
+// values, G = nb + 2 ngrow in each dimension) and the compact vector of the
+// valid cells, one thread per cell, x fastest on both sides
+struct TdLayout {
+  int nd, nb, ncomp, g, comp;
+  long G0, G1, cap;
+};
+__device__ __forceinline__ long td_at(const TdLayout &L, int b, int i, int j, int k) {
+  const long gz = L.nd == 3 ? L.g : 0;
+  return (long)b * L.cap * L.ncomp + (long)L.comp * L.cap + (i + L.g) + L.G0 * ((j + L.g) + L.G1 * (k + gz));
+}
+__global__ void k_td_gather(TdLayout L, long total, int ncell, const double *__restrict__ td, double *__restrict__ out) {
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int b = (int)(it / ncell), ci = (int)(it - (long)b * ncell);
+    const int i = ci % L.nb, j = (ci / L.nb) % L.nb, k = L.nd == 3 ? ci / (L.nb * L.nb) : 0;
+    out[it] = td[td_at(L, b, i, j, k)];
+  }
+}
+__global__ void k_td_scatter(TdLayout L, long total, int ncell, const double *__restrict__ in, double *__restrict__ td) {
+  for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < total; it += (long)gridDim.x * blockDim.x) {
+    const int b = (int)(it / ncell), ci = (int)(it - (long)b * ncell);
+    const int i = ci % L.nb, j = (ci / L.nb) % L.nb, k = L.nd == 3 ? ci / (L.nb * L.nb) : 0;
+    td[td_at(L, b, i, j, k)] = in[it];
+  }
+}
+
 void tree_from_tables(const TreeTables &tt, AmrTree &t) {
   t.init(tt.ndim, tt.nb, tt.min_level, tt.max_level, std::max(tt.num_blocks, 1), false);
   t.num_blocks = tt.num_blocks;
@@ -693,6 +719,27 @@ void MacGpu::get_coef(int which, int dir, double *out) {
 void MacGpu::set_rhs(const double *all, bool dev) {
   CK(cudaMemcpyAsync(vec_[kRHS], all, (size_t)tt_.num_blocks * ncell_ * sizeof(double),
                      dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream_));
+}
+static TdLayout td_layout(int nd, int nb, int ncomp, int ngrow, int comp) {
+  TdLayout L{nd, nb, ncomp, ngrow, comp, nb + 2l * ngrow, nd >= 2 ? nb + 2l * ngrow : 1, 0};
+  L.cap = L.G0 * L.G1 * (nd == 3 ? nb + 2l * ngrow : 1);
+  return L;
+}
+int MacGpu::set_field_td(const double *td, int ncomp, int ngrow, int comp, bool rhs) {
+  const long total = (long)tt_.num_blocks * ncell_;
+  k_td_gather<<<grid_for(total), kThreads, 0, stream_>>>(td_layout(tt_.ndim, tt_.nb, ncomp, ngrow, comp), total, ncell_,
+                                                         td, vec_[rhs ? kRHS : kSOL]);
+  CKR(cudaGetLastError(), 2);
+  CKR(cudaStreamSynchronize(stream_), 2);
+  return 0;
+}
+int MacGpu::get_sol_td(double *td, int ncomp, int ngrow, int comp) {
+  const long total = (long)tt_.num_blocks * ncell_;
+  k_td_scatter<<<grid_for(total), kThreads, 0, stream_>>>(td_layout(tt_.ndim, tt_.nb, ncomp, ngrow, comp), total,
+                                                          ncell_, vec_[kSOL], td);
+  CKR(cudaGetLastError(), 2);
+  CKR(cudaStreamSynchronize(stream_), 2);
+  return 0;
 }
 void MacGpu::set_sol(const double *all, bool dev) {
   CK(cudaMemcpyAsync(vec_[kSOL], all, (size_t)tt_.num_blocks * ncell_ * sizeof(double),

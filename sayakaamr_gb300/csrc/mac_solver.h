@@ -104,6 +104,12 @@ class MacGpu {
   void set_sol(const double *all, bool on_device = false);
   void zero_sol();
   void get_sol(double *all, bool on_device = false);
+  // the same between the device and a TreeData-layout field (ncomp
+  // components of ngrow ghost layers per block) that the GPU can address:
+  // pinned host memory read and written by the kernel over the CPU-GPU link,
+  // no staging copy (0 ok, else a CUDA error was recorded)
+  int set_field_td(const double *td, int ncomp, int ngrow, int comp, bool rhs);
+  int get_sol_td(double *td, int ncomp, int ngrow, int comp);
   double *rhs_dev() { return vec_[kRHS]; }
   double *sol_dev() { return vec_[kSOL]; }
 
