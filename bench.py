@@ -101,6 +101,9 @@ def parse():
                          "(the reference's), 1 one launch per colour and level parity")
     ap.add_argument("--smooth-variant", type=int, default=-1,
                     help="device smoother launch-bounds variant (-1: autotuned at prepare)")
+    ap.add_argument("--omega", type=float, default=-1.0,
+                    help="relaxation weight of the V-cycle's red-black updates (params.relax_omega; -1: 1.0, 1.1 or "
+                         "1.2, timed during warm-up with the chosen setting)")
     ap.add_argument("--vcycle-out", type=int, default=0,
                     help="FP32 V-cycle output: 0 auto (in place in 2D and on small 3D towers), 1 in place with the "
                          "operator in double-float, 2 widened into FP64 vectors, 3 in place")
@@ -606,6 +609,27 @@ def main():
         S.prepare()
     if args.inner_sweeps < 0:
         args.inner_sweeps = 2
+    omega_tuning = None
+    if args.omega < 0:
+        # the smoother's relaxation weight with the chosen setting, timed the
+        # same way: over-relaxed red-black sweeps are another fixed linear
+        # preconditioner (the same solution), often with fewer iterations
+        omega_tuning = []
+        for om in (1.0, 1.1, 1.2):
+            S.set_params(relax_omega=om, max_iter=TUNE_MAX_ITER)
+            S.prepare()
+            failed = warm(dict(relax_omega=om), tolerate=True)
+            if failed:
+                omega_tuning.append(dict(omega=om, ms=None, not_converged=failed[:300]))
+                continue
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+            infos = [one(e) for e in ev]
+            torch.cuda.synchronize()
+            omega_tuning.append(dict(omega=om, ms=statistics.mean(a.elapsed_time(b) for a, b in ev),
+                                     iterations=statistics.mean(i["iterations"] for i in infos)))
+        args.omega = min((r for r in omega_tuning if r["ms"] is not None), key=lambda r: r["ms"])["omega"]
+    S.set_params(relax_omega=args.omega, max_iter=2000)
+    S.prepare()
     warm()
     if args.profile:
         torch.cuda.synchronize()
@@ -668,7 +692,7 @@ def main():
     solvers = None if args.no_compare else compare_solvers(S, prob, one, warm, torch, args, tuning)
     oracle = None if args.no_compare else oracle_check(S, prob, timed_sol)
     S.set_params(precision=args.precision, n_post_smooth=args.n_post, smoother=args.smoother,
-                 inner_sweeps=args.inner_sweeps, learned=0, tol_rel=TOL)
+                 inner_sweeps=args.inner_sweeps, learned=0, tol_rel=TOL, relax_omega=args.omega)
     S.prepare()
 
     # ---- roofline of the dominant kernel, timed live on the solver stream ----
@@ -686,6 +710,7 @@ def main():
                    "leaf_cells": prob.leaf_cells, "blocks": prob.num_blocks, "tol_rel": TOL,
                    "l2": "flushed (256 MiB write) before every timed solve", "precision": args.precision,
                    "setting_tuning_ms": tuning,
+                   "relax_omega": args.omega, "omega_tuning_ms": omega_tuning,
                    "iterations_per_solve": statistics.mean(iters), "n_post_smooth": args.n_post,
                    "smoother": ("red-black sweeps", "block-hybrid passes (Gauss-Seidel inside a block, Jacobi "
                                 "between blocks), %d sweeps per pass" % args.inner_sweeps)[args.smoother],
@@ -813,7 +838,8 @@ def run_sequence(args, torch, ws, rank, local):
                precision=1 if args.precision < 0 else args.precision,
                n_post_smooth=4 if args.n_post < 0 else args.n_post,
                bottom_level=args.bottom_level if args.bottom_level > 0 else 1,
-               bottom_refresh=args.bottom_refresh, smoother=max(args.smoother, 0))
+               bottom_refresh=args.bottom_refresh, smoother=max(args.smoother, 0),
+               relax_omega=args.omega if args.omega > 0 else 1.0)
     t0 = time.perf_counter()
     sc = W.elbow_point(0.1)
     tree = W.elbow_tree(sc, max_level=args.max_level)
@@ -917,16 +943,18 @@ def compare_solvers(S, prob, one, warm, torch, args, tuning):
     the FP32 V-cycle with the tuned sweeps, and the learned block correction
     with the FP32 V-cycle (trained on this workload's own solver iterates
     first, 2D only)"""
-    fp32 = dict(precision=1, n_post_smooth=args.n_post, smoother=args.smoother, inner_sweeps=args.inner_sweeps)
+    fp32 = dict(precision=1, n_post_smooth=args.n_post, smoother=args.smoother, inner_sweeps=args.inner_sweeps,
+                relax_omega=args.omega)
     if tuning:
         t32 = [r for r in tuning if r["precision"] == 1 and r["ms"] is not None]
         if t32:
             b = min(t32, key=lambda r: r["ms"])
             fp32 = dict(precision=1, n_post_smooth=b["n_post_smooth"], smoother=b["smoother"],
-                        inner_sweeps=b["inner_sweeps"])
+                        inner_sweeps=b["inner_sweeps"], relax_omega=args.omega)
     # the reference's method on the device: FP64 V-cycle, red-black
     # Gauss-Seidel with its default 2 post-smoothing sweeps
-    settings = [("plain_fp64_mg", dict(precision=0, n_post_smooth=2, smoother=0, inner_sweeps=2, learned=0)),
+    settings = [("plain_fp64_mg", dict(precision=0, n_post_smooth=2, smoother=0, inner_sweeps=2, learned=0,
+                                       relax_omega=1.0)),
                 ("fp32_vcycle", dict(fp32, learned=0))]
     out = {}
     learned_note = None

@@ -161,6 +161,11 @@ typedef struct sayaka_params {
   int32_t learned_loss;   /* training loss of the learned correction u: 0 = the residual u leaves under the
                              block-local operator (default); 1 = the distance of u to the block-local part of the
                              error the V-cycle left, known from the solver's own converged solution */
+  double relax_omega;     /* device V-cycle: relaxation weight of every red-black update of a fluid cell,
+                             u = u_old + omega * (u_gs - u_old), in (0, 2); 1 = Gauss-Seidel, the reference's
+                             smoother (default).  Over-relaxation (about 1.1) is another fixed linear
+                             preconditioner with the same solution; the reference-order host path
+                             (bottom 0) ignores it */
 } sayaka_params;
 
 typedef struct sayaka_solve_info {

@@ -53,6 +53,10 @@ typedef struct orc_params {
   int use_precond;
   double bot_tol_rel, bot_tol_abs;
   int bot_max_iter;
+  /* relaxation weight of the V-cycle's red-black updates of fluid cells,
+   * u_old + omega (u_gs - u_old): 1 is the reference's Gauss-Seidel; other
+   * values restate the product's over-relaxed smoother (params.relax_omega) */
+  double omega;
 } orc_params;
 
 typedef struct orc_info {
@@ -75,6 +79,7 @@ typedef struct {
   int **lev;   /* tree level lists */
   int *nlev;
   double *dx, *ds, *dv; /* per block metrics */
+  double omega;         /* smoother relaxation weight (orc_params.omega) */
 } ctx_t;
 
 static int ipow(int a, int e) {
@@ -94,6 +99,7 @@ static int fidx(const ctx_t *c, int d, int i, int j, int k) {
 
 static void ctx_init(ctx_t *c, const orc_problem *P) {
   c->P = P;
+  c->omega = 1.0;
   c->nd = P->ndim;
   c->nb = P->nb;
   c->G = P->nb + 2;
@@ -441,6 +447,7 @@ static void smooth_block(const ctx_t *c, int b, const int *ft, double *phi, cons
         const double r = G_(c, rhs, b, i, j, k), vf = V_(c, P->vf, b, i, j, k);
         double unew = 0;
         if (vf > 0) unew = (r * c->dv[b] * vf + offdiag) / diag;
+        if (vf > 0 && c->omega != 1.0) unew = c->omega * unew + (1.0 - c->omega) * G_(c, phi, b, i, j, k);
         G_(c, phi, b, i, j, k) = unew;
         for (int f = 0; f < 2 * nd; f++) {
           if (!fcf[f]) continue;
@@ -643,7 +650,10 @@ static void solver_init(solver_t *s, const orc_problem *P, const orc_params *prm
   ctx_init(&s->c, P);
   regs_new(&s->c, &s->R);
   for (int i = 0; i < NVEC; i++) s->v[i] = gnew(&s->c);
-  if (prm) s->prm = *prm;
+  if (prm) {
+    s->prm = *prm;
+    if (prm->omega > 0.0) s->c.omega = prm->omega;
+  }
 }
 static void solver_free(solver_t *s) {
   for (int i = 0; i < NVEC; i++) free(s->v[i]);
@@ -798,6 +808,20 @@ int orc_residual(const orc_problem *P, int L, const double *x, const double *rhs
 int orc_smooth(const orc_problem *P, int L, const double *phi, const double *rhs, double *out) {
   solver_t s;
   solver_init(&s, P, NULL);
+  to_grown(&s.c, phi, s.v[B_CORR]);
+  to_grown(&s.c, rhs, s.v[B_RESID]);
+  g_smooth(&s.c, L, s.v[B_CORR], s.v[B_RESID], &s.R);
+  from_grown(&s.c, s.v[B_CORR], out);
+  solver_free(&s);
+  return 0;
+}
+
+/* orc_smooth with relaxed updates of the fluid cells (orc_params.omega) */
+int orc_smooth_relaxed(const orc_problem *P, int L, const double *phi, const double *rhs, double omega,
+                       double *out) {
+  solver_t s;
+  solver_init(&s, P, NULL);
+  s.c.omega = omega;
   to_grown(&s.c, phi, s.v[B_CORR]);
   to_grown(&s.c, rhs, s.v[B_RESID]);
   g_smooth(&s.c, L, s.v[B_CORR], s.v[B_RESID], &s.R);

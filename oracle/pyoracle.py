@@ -26,7 +26,7 @@ class _Problem(C.Structure):
 class _Params(C.Structure):
     _fields_ = [("max_iter", C.c_int), ("tol_rel", C.c_double), ("tol_abs", C.c_double), ("n_post", C.c_int),
                 ("use_precond", C.c_int), ("bot_tol_rel", C.c_double), ("bot_tol_abs", C.c_double),
-                ("bot_max_iter", C.c_int)]
+                ("bot_max_iter", C.c_int), ("omega", C.c_double)]
 
 
 class _Info(C.Structure):
@@ -47,8 +47,8 @@ def load():
 
 
 def params(max_iter=2000, tol_rel=1e-6, tol_abs=0.0, n_post=2, use_precond=1, bot_tol_rel=1e-6, bot_tol_abs=1e-6,
-           bot_max_iter=2000):
-    return _Params(max_iter, tol_rel, tol_abs, n_post, use_precond, bot_tol_rel, bot_tol_abs, bot_max_iter)
+           bot_max_iter=2000, omega=1.0):
+    return _Params(max_iter, tol_rel, tol_abs, n_post, use_precond, bot_tol_rel, bot_tol_abs, bot_max_iter, omega)
 
 
 def setup_coefficients(tables, bc, vf=None, af=None, bcoef=None):
@@ -132,9 +132,13 @@ class Oracle:
         self.lib.orc_residual(C.byref(self.P), int(L), self._in(x), self._in(rhs), r.ctypes.data_as(_f64p))
         return r
 
-    def smooth(self, L, phi, rhs):
+    def smooth(self, L, phi, rhs, omega=1.0):
         out = self._cells()
-        self.lib.orc_smooth(C.byref(self.P), int(L), self._in(phi), self._in(rhs), out.ctypes.data_as(_f64p))
+        if omega == 1.0:
+            self.lib.orc_smooth(C.byref(self.P), int(L), self._in(phi), self._in(rhs), out.ctypes.data_as(_f64p))
+        else:
+            self.lib.orc_smooth_relaxed(C.byref(self.P), int(L), self._in(phi), self._in(rhs), C.c_double(omega),
+                                        out.ctypes.data_as(_f64p))
         return out
 
     def restrict_sweep(self, x):

@@ -44,7 +44,7 @@ class Params(C.Structure):
                 ("smoother", C.c_int32), ("inner_sweeps", C.c_int32), ("per_problem", C.c_int32),
                 ("uniform", C.c_int32), ("bottom_refresh", C.c_int32),
                 ("learned_tc05", C.c_int32), ("vcycle_out", C.c_int32), ("prolong_form", C.c_int32),
-                ("learned_loss", C.c_int32)]
+                ("learned_loss", C.c_int32), ("relax_omega", C.c_double)]
 
 
 class SolveInfo(C.Structure):

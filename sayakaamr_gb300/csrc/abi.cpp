@@ -420,6 +420,7 @@ void sayaka_params_default(sayaka_params *p) {
   p->learned_loss = d.learned_loss;
   p->prolong_form = d.prolong_form;
   p->vcycle_out = d.vcycle_out;
+  p->relax_omega = d.relax_omega;
 }
 
 int sayaka_mac_create(const sayaka_tree_tables *tb, sayaka_mac **out) {
@@ -698,6 +699,8 @@ int sayaka_mac_set_params(sayaka_mac *h, const sayaka_params *p) {
     s.prolong_form = p->prolong_form;
     if (p->vcycle_out < 0 || p->vcycle_out > 3) return (int)SAYAKA_BAD_INPUT;
     s.vcycle_out = p->vcycle_out;
+    if (!(p->relax_omega > 0.0 && p->relax_omega < 2.0)) return (int)SAYAKA_BAD_INPUT;
+    s.relax_omega = p->relax_omega;
     h->gpu->set_params(s);
     return (int)SAYAKA_OK;
   });

@@ -39,6 +39,9 @@ struct Coef {
   const T *afrac[3];  // IB area fraction
   const T *vf;        // IB volume fraction
   T alpha, beta;
+  // relaxation weight of the device V-cycle's red-black updates of fluid
+  // cells (1: Gauss-Seidel; the reference-arithmetic kernels ignore it)
+  T omega = 1;
   // Constant-coefficient blocks (device solve only; null elsewhere):
   // kUni values per block, [0..2] the same-level face coefficient of every
   // face of direction 0..2 of the block, [3] nonzero when the block is one

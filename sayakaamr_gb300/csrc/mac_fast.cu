@@ -1077,6 +1077,9 @@ void MacGpu::bind_uniform() {
   cd64_ = c64_;
   cd64_.ut = prm_.uniform ? d_uni64_ : nullptr;
   c32_.ut = prm_.uniform ? d_uni32_ : nullptr;
+  // the smoothers' relaxation weight (1: plain Gauss-Seidel, the reference's)
+  cd64_.omega = prm_.relax_omega;
+  c32_.omega = (float)prm_.relax_omega;
 }
 
 // FP32 copies of the coefficients for the FP32 V-cycle
@@ -1746,6 +1749,7 @@ void MacGpu::capture_loop(int precision) {
   graph_uniform_ = prm_.uniform;
   graph_pform_ = prm_.prolong_form;
   graph_vout_ = prm_.vcycle_out;
+  graph_omega_ = prm_.relax_omega;
 }
 
 // the captured graph was recorded with other parameters than the current ones
@@ -1755,7 +1759,8 @@ bool MacGpu::graph_stale() const {
          graph_var_ != rbgs_variant_[prm_.precision == 1] || graph_nn_ != (int)learned_active() ||
          graph_order_ != prm_.sublevel_order || graph_smoother_ != prm_.smoother ||
          graph_inner_ != prm_.inner_sweeps || graph_multi_ != (int)multi() || graph_uniform_ != prm_.uniform ||
-         graph_pform_ != prm_.prolong_form || graph_vout_ != prm_.vcycle_out;
+         graph_pform_ != prm_.prolong_form || graph_vout_ != prm_.vcycle_out ||
+         graph_omega_ != prm_.relax_omega;
 }
 
 int MacGpu::cg_solve_device(SolveInfo *info) {

@@ -246,7 +246,7 @@ __device__ __forceinline__ void warp_block16(const Topo &t, const Coef<float> &c
       }
     }
     const float vfv = u ? 1.0f : c.vf[cb + j * NB + i];
-    v[k] = (vfv > 0.f && diag > 0.f) ? fast_div(fma_t(r[k] * dv, vfv, off), diag) : 0.f;
+    v[k] = (vfv > 0.f && diag > 0.f) ? relax(c.omega, fast_div(fma_t(r[k] * dv, vfv, off), diag), v[k]) : 0.f;
   }
   float4 *dst = reinterpret_cast<float4 *>(phi + cb + j * NB + c0);
   dst[0] = make_float4(v[0], v[1], v[2], v[3]);
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_warp16(Topo t, Coef<flo
       } else if (dir[3]) {
         diag += T1 * 2.0f;
       }
-      v[k] = diag > 0.f ? fast_div(fma_t(r[k] * dv, 1.0f, off), diag) : 0.f;
+      v[k] = diag > 0.f ? relax(c.omega, fast_div(fma_t(r[k] * dv, 1.0f, off), diag), v[k]) : 0.f;
     }
     float4 *dst = reinterpret_cast<float4 *>(phi + cb + j * NB + c0);
     dst[0] = make_float4(v[0], v[1], v[2], v[3]);
@@ -517,7 +517,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_warp16_flat(Topo t, Coe
       } else if (dir[3]) {
         diag += T1 * 2.0f;
       }
-      v[k] = diag > 0.f ? fast_div(fma_t(rs[k >> 1] * dv, 1.0f, off), diag) : 0.f;
+      v[k] = diag > 0.f ? relax(c.omega, fast_div(fma_t(rs[k >> 1] * dv, 1.0f, off), diag), v[k]) : 0.f;
     }
     float4 *dst = reinterpret_cast<float4 *>(phi + cb + j * NB + c0);
     dst[0] = make_float4(v[0], v[1], v[2], v[3]);
@@ -885,8 +885,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_rbgs_tile(Topo t, Coef<T> c,
       T unew = 0;
       if (sizeof(T) == 8 && L.sa) {
         unew = fma_t(o.r, (T)o.sa, off * (T)o.ia);
+        if (o.ia != 0) unew = relax(c.omega, unew, tile[o.ci]);
       } else {
-        if (o.v > 0 && diag > 0) unew = fast_div(fma_t(o.r * dv, o.v, off), diag);
+        if (o.v > 0 && diag > 0) unew = relax(c.omega, fast_div(fma_t(o.r * dv, o.v, off), diag), tile[o.ci]);
       }
       tile[o.ci] = unew;
     };
@@ -1020,10 +1021,12 @@ __global__ void __launch_bounds__(kThreads, MINB) k_bhgs(Topo t, Coef<T> c, Bloc
             for (int q = 0; q < ND; q++) inner = inner && ijk[q] > 0 && ijk[q] < nb - 1;
             const long fo = (long)p * ncell + ci;
             const bool ui = u && inner;
-            unew = fma_t(rhs[cb + ci], ui ? u[6] : (T)L.sa[fo], off * (ui ? u[7] : (T)L.ia[fo]));
+            const T iav = ui ? u[7] : (T)L.ia[fo];  // 0 in a solid cell
+            unew = fma_t(rhs[cb + ci], ui ? u[6] : (T)L.sa[fo], off * iav);
+            if (iav != (T)0) unew = relax(c.omega, unew, tile[ci]);
           } else {
             const T vfv = u ? (T)1 : c.vf[cb + ci];
-            if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+            if (vfv > 0 && diag > 0) unew = relax(c.omega, fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag), tile[ci]);
           }
           tile[ci] = unew;
         }
@@ -1210,9 +1213,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_rbgs_bulk(Topo t, Coef<T> c, Bl
     if (sizeof(T) == 8 && L.sa) {
       const long fo = (long)p * ncell + ci;
       unew = fma_t(rhs[cb + ci], (T)L.sa[fo], off * (T)L.ia[fo]);
+      if (L.ia[fo] != 0.0) unew = relax(c.omega, unew, tile[ci]);
     } else {
       const T vfv = c.vf[cb + ci];
-      if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+      if (vfv > 0 && diag > 0) unew = relax(c.omega, fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag), tile[ci]);
     }
     tile[ci] = unew;
   }
@@ -1366,9 +1370,10 @@ __global__ void __launch_bounds__(kStreamThreads, 1) k_rbgs_stream(Topo t, Coef<
       if (sizeof(T) == 8 && L.sa) {
         const long fo = (long)p * ncell + ci;
         unew = fma_t(rh[ci], (T)L.sa[fo], off * (T)L.ia[fo]);
+        if (L.ia[fo] != 0.0) unew = relax(c.omega, unew, tile[ci]);
       } else {
         const T vfv = vfs[ci];
-        if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rh[ci] * dv, vfv, off), diag);
+        if (vfv > 0 && diag > 0) unew = relax(c.omega, fast_div(fma_t(rh[ci] * dv, vfv, off), diag), tile[ci]);
       }
       tile[ci] = unew;
     }
@@ -1557,10 +1562,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_prolong_red(Topo t, Coef<T> c, 
         for (int q = 0; q < ND; q++) inner = inner && ijk[q] > 0 && ijk[q] < nb - 1;
         const long fo = (long)p * ncell + ci;
         const bool ui = u && inner;
-        unew = fma_t(rhs[cb + ci], ui ? u[6] : (T)L.sa[fo], off * (ui ? u[7] : (T)L.ia[fo]));
+        const T iav = ui ? u[7] : (T)L.ia[fo];  // 0 in a solid cell
+        unew = fma_t(rhs[cb + ci], ui ? u[6] : (T)L.sa[fo], off * iav);
+        if (iav != (T)0) unew = relax(c.omega, unew, tile[ci]);
       } else {
         const T vfv = u ? (T)1 : c.vf[cb + ci];
-        if (vfv > 0 && diag > 0) unew = fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag);
+        if (vfv > 0 && diag > 0) unew = relax(c.omega, fast_div(fma_t(rhs[cb + ci] * dv, vfv, off), diag), tile[ci]);
       }
       tile[ci] = unew;
     }

@@ -65,6 +65,8 @@ struct SolverParams {
   int per_problem = 1;        // device path, a tree of several independent problems (connected components):
                               // 1 = one BiCGSTAB state per problem, each stopping at its own tolerance;
                               // 0 = one state shared by all
+  double relax_omega = 1.0;   // device V-cycle smoothers: relaxation weight of every red-black update of a fluid
+                              // cell, u = u_old + omega * (u_gs - u_old); 1 = plain Gauss-Seidel (default)
 };
 
 struct SolveInfo {
@@ -408,6 +410,7 @@ class MacGpu {
   int graph_coop_ = -1, graph_pdl_ = -1, graph_cc_ = -1, graph_var_ = -1, graph_nn_ = -1, graph_order_ = -1;
   int graph_smoother_ = -1, graph_inner_ = -1, graph_multi_ = -1, graph_uniform_ = -1, graph_pform_ = -1,
       graph_vout_ = -1;
+  double graph_omega_ = -1.0;
   bool last_multi_ = false;  // the last device solve kept one state per problem
   Chunks chunks() const;
   bool graph_stale() const;

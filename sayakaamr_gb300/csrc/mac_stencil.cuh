@@ -271,6 +271,15 @@ __device__ __forceinline__ double fast_div(double a, double b) { return a / b; }
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
 
+// the relaxed red-black update of a fluid cell, u_old + omega (u_gs - u_old)
+// (successive over-relaxation for omega > 1); omega 1 returns u_gs itself,
+// the plain Gauss-Seidel update with the same bits.  omega is a launch
+// argument, so the test is uniform over the grid.
+template <typename T>
+__device__ __forceinline__ T relax(T omega, T unew, T old) {
+  return omega == (T)1 ? unew : fma_t(omega, unew - old, old);
+}
+
 // red-black update of the device solve's V-cycle: the smoother of
 // smooth_cell with 32-bit shift indexing, FMA accumulation and a fast
 // division.  Same face coefficients and gathers, different rounding; every
@@ -329,12 +338,18 @@ __device__ __forceinline__ void smooth_cell_fast(const Topo &t, const Coef<T> &c
   }
   if (sizeof(T) == 8 && sa) {
     const bool ui = u && inner;  // interior cell of a constant-coefficient block
-    phi[cb + ci] = fma_t(ld<CG>(&rhs[cb + ci]), ui ? u[6] : (T)sa[ci], off * (ui ? u[7] : (T)ia[ci]));
+    const T iav = ui ? u[7] : (T)ia[ci];  // 0 in a solid cell
+    T unew = fma_t(ld<CG>(&rhs[cb + ci]), ui ? u[6] : (T)sa[ci], off * iav);
+    if (c.omega != (T)1 && iav != (T)0) unew = relax(c.omega, unew, ld<CG>(&phi[cb + ci]));
+    phi[cb + ci] = unew;
     return;
   }
   const T vfv = u ? (T)1 : c.vf[cb + ci];
   T unew = 0;
-  if (vfv > 0 && diag > 0) unew = fast_div(fma_t(ld<CG>(&rhs[cb + ci]) * dv, vfv, off), diag);
+  if (vfv > 0 && diag > 0) {
+    unew = fast_div(fma_t(ld<CG>(&rhs[cb + ci]) * dv, vfv, off), diag);
+    if (c.omega != (T)1) unew = relax(c.omega, unew, ld<CG>(&phi[cb + ci]));
+  }
   phi[cb + ci] = unew;
 }
 
@@ -425,11 +440,16 @@ __device__ __forceinline__ void smooth_update(const Coef<T> &c, const SmoothOps<
     off = fma_t(o.kc[f], o.v[f], off);
   }
   if (o.fac) {
-    phi[o.q] = fma_t(o.r, (T)o.sa, off * (T)o.ia);
+    T unew = fma_t(o.r, (T)o.sa, off * (T)o.ia);
+    if (c.omega != (T)1 && o.ia != 0.0) unew = relax(c.omega, unew, phi[o.q]);
+    phi[o.q] = unew;
     return;
   }
   T unew = 0;
-  if (o.vf > 0 && diag > 0) unew = fast_div(fma_t(o.r * o.dv, o.vf, off), diag);
+  if (o.vf > 0 && diag > 0) {
+    unew = fast_div(fma_t(o.r * o.dv, o.vf, off), diag);
+    if (c.omega != (T)1) unew = relax(c.omega, unew, phi[o.q]);
+  }
   phi[o.q] = unew;
 }
 

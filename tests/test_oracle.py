@@ -175,3 +175,50 @@ def test_mg_and_relax_solves_bit_exact(name):
     sol, info = O.relax_solve(g["sv_rhs"], pyoracle.params(max_iter=golden_io.RELAX_ITERS, **kw))
     assert info["iterations"] == golden_io.RELAX_ITERS, info
     assert exact(rows(sol, leaf, O.ncell), g["rx_sol"]), name
+
+
+@pytest.mark.parametrize("name", ["t2s", "t3s"])
+def test_relaxed_smoother(name):
+    """the over-relaxed smoother (orc_params.omega, the product's
+    params.relax_omega): omega 1 is the reference's sweep bit for bit, a
+    sweep's red cells (updated from old black values only) are
+    u_old + omega (u_gs - u_old) of the plain sweep's red cells, and the
+    relaxed V-cycle is another preconditioner with the same solution"""
+    g, t, tb, O = oracle_for(name)
+    n, nc, nb, nd = tb["num_blocks"], O.ncell, tb["nb"], tb["ndim"]
+    L = int(tb["level"].max())
+    rng = np.random.default_rng(5)
+    phi, rhs = rng.standard_normal(n * nc), rng.standard_normal(n * nc)
+    plain = O.smooth(L, phi, rhs)
+    w1 = np.empty_like(plain)
+    O.lib.orc_smooth_relaxed(pyoracle.C.byref(O.P), L, O._in(phi), O._in(rhs), pyoracle.C.c_double(1.0),
+                             w1.ctypes.data_as(pyoracle._f64p))
+    assert exact(w1, plain)
+    # red cells (i+j+k even) of the finest level's blocks, swept first: both
+    # sweeps read the same old values when they update them
+    om = 1.3
+    relaxed = O.smooth(L, phi, rhs, omega=om)
+    idx = np.indices((nb,) * nd).reshape(nd, -1)[::-1]  # cell index ci = i + nb j (+ nb^2 k)
+    red = (idx.sum(axis=0) % 2) == 0
+    vf = oracle_vf(O, n * nc).reshape(n, nc)
+    blocks = [b for b in t.tower(L)[0] if tb["level"][b] == L]
+    checked = 0
+    for b in blocks:
+        m = red & (vf[b] > 0)
+        if not m.any():
+            continue
+        checked += 1
+        a = relaxed.reshape(n, nc)[b][m]
+        want = om * plain.reshape(n, nc)[b][m] + (1 - om) * phi.reshape(n, nc)[b][m]
+        assert np.allclose(a, want, rtol=1e-13, atol=1e-13 * np.abs(want).max()), b
+    assert checked > 0
+    sols = []
+    for omega in (1.0, 1.1):
+        sol, info = O.cg_solve(g["sv_rhs"], pyoracle.params(tol_rel=1e-11, tol_abs=0.0, bot_tol_rel=1e-10,
+                                                            bot_tol_abs=0.0, omega=omega))
+        assert info["status"] == 0, (omega, info)
+        sols.append(rows(sol, t.tower(L)[0], nc))
+    d = sols[1] - sols[0]
+    if tb["neighbor"].min() > -30:  # all-Neumann trees: compare up to a constant
+        d = d - d.mean()
+    assert np.linalg.norm(d) <= 1e-8 * np.linalg.norm(sols[0])
