@@ -512,7 +512,8 @@ def main():
                  cluster_cells=args.cluster_cells, smooth_variant=args.smooth_variant, vcycle_out=args.vcycle_out,
                  pdl=args.pdl, sublevel_order=args.sublevel_order, bottom_level=args.bottom_level,
                  bottom_half=args.bottom_half, smoother=max(args.smoother, 0),
-                 inner_sweeps=args.inner_sweeps if args.inner_sweeps > 0 else 2)
+                 inner_sweeps=args.inner_sweeps if args.inner_sweeps > 0 else 2,
+                 relax_omega=args.omega if args.omega > 0 else 1.0)
     S.prepare()
     ext = torch.cuda.ExternalStream(S.stream())
     if args.kernel >= 0:
